@@ -1,0 +1,321 @@
+#!/usr/bin/env python
+"""Benchmark: simulated reads/s (and placed mutations/s) of the GB300 path.
+
+Workload: the full-scale configuration — synthetic 3.1 Gbp genome in 24
+chromosomes (GC 41%), 3 samples x 1e4 leaves, 3 exposure epochs, 100x paired
+150 bp reads, purity 0.7, error rate 1e-3, plus the normal sample.  One step =
+place the mutations on the forest (new seed) and sequence all four samples.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs one independent replica per GPU (the path does not exchange data
+between instances), launched by torch.distributed.run.  ``--impl reference``
+times the CPU restatement of the reference path (the oracle's std::mt19937_64
+port) on the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "reads/s + mutations placed/s on 1 GB300 vs host CPU; batched calib grad-evals/s"
+WORKLOAD = ("config2 full scale: 3.1 Gbp/24 chr GC 41%, 3 samples x 1e4 leaves, 3 epochs "
+            "SNV {1.5e-8,3e-8,5e-8} indel 0.1x, 3 SBS + 2 ID signatures, 100x paired 150 bp, "
+            "insert binomial(350, 10), purity 0.7, error 1e-3, + normal sample")
+# algorithmic bytes of one simulated read and of one read-locus visit (alt+depth
+# read-modify-write), the per-unit contract of the read kernel
+BYTES_PER_READ = 38
+BYTES_PER_SITE_HIT = 8
+CPU_SAMPLE_SCALE = 0.01   # genome fraction of the CPU sample (31 Mbp over the 24 chromosomes)
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample_workload():
+    from process_gb300 import synth
+    return synth.config2(seed=2, genome_scale=CPU_SAMPLE_SCALE)
+
+
+def run_cpu(steps: int, warmup: int, threads: int, sample_desc: str):
+    """Times the oracle's reference-engine port (std::mt19937_64) on the host."""
+    import oracle
+    from process_gb300.engine import seq_cfg
+    oracle.build()
+    w = cpu_sample_workload()
+    e = oracle.OracleEngine.like(w)
+    sp = np.array([e.species[(m, ep)] for m, ep in zip(w.forest.mutant, w.forest.epistate)], dtype=np.uint32)
+    chr_index = {n: i for i, n in enumerate(w.genome.chr_names)}
+    c, _ = seq_cfg(chr_index=lambda x: chr_index[x], **w.seq)
+    reads = muts = 0
+    t_place = t_seq = 0.0
+    for s in range(warmup + steps):
+        t0 = time.perf_counter()
+        p = e.place(w.forest, sp, w.n_pre_snv, 0, w.n_pre_indel, 0, seed=100 + s, flavour=1)
+        t1 = time.perf_counter()
+        _, _, r = p.sequence(c, 200 + s, flavour=1, threads=threads)
+        t2 = time.perf_counter()
+        if s >= warmup:
+            n = len(p.table()["locus"])
+            reads += r
+            muts += n
+            t_place += t1 - t0
+            t_seq += t2 - t1
+    return {"reads_per_s": reads / (t_place + t_seq), "seq_reads_per_s": reads / t_seq,
+            "mutations_placed_per_s": muts / t_place, "reads": reads, "mutations": muts,
+            "seconds": t_place + t_seq, "threads": threads, "sample": sample_desc}
+
+
+def reference_arm(args):
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    desc = (f"oracle std::mt19937_64 port (oracle/oracle.cpp flavour 1) on {CPU_SAMPLE_SCALE:.0%} of the genome "
+            "(31 Mbp over the same 24 chromosomes), full forest, 100x paired, purity 0.7, + normal; "
+            "placement single-threaded, reads over all host threads")
+    r = run_cpu(args.steps, args.warmup, threads, desc)
+    line = {"metric": METRIC, "value": r["reads_per_s"], "unit": "reads/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * r["seconds"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": desc},
+            "secondary": {"mutations_placed_per_s": r["mutations_placed_per_s"],
+                          "sequencing_reads_per_s": r["seq_reads_per_s"]},
+            "cpu_baseline": {"value": r["reads_per_s"], "unit": "reads/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": r["reads_per_s"], "unit": "reads/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    world = env_int("WORLD_SIZE", 1)
+    rank = env_int("RANK", 0)
+    local = env_int("LOCAL_RANK", 0)
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build() if rank == 0 or world == 1 else None
+    if world > 1:
+        dist.barrier()
+    from process_gb300 import _lib, synth
+    from process_gb300.engine import sequence_counts
+    import ctypes as C
+
+    w = synth.config2(seed=2)
+    eng = synth.build_engine(w)
+    stream = torch.cuda.current_stream()
+    _lib.check(_lib.lib().pg_engine_set_stream(eng._h, C.c_void_p(stream.cuda_stream)))
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def launches():
+        n = C.c_uint64()
+        _lib.check(_lib.lib().pg_launch_count(C.byref(n)))
+        return n.value
+
+    seed0 = 1000 * rank
+    for s in range(args.warmup):
+        pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=seed0 + s)
+        sequence_counts(pf, seed0 + 500 + s, **w.seq)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    place_ms = seq_ms = read_kernel_ms = 0.0
+    reads = muts = 0
+    last = None
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        n0 = launches()
+        wall0 = time.perf_counter()
+        for s in range(args.steps):
+            flush.fill_(s & 0xFF)                 # evict L2 between steps
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=seed0 + 10_000 + s)
+            e1.record(stream)
+            res = sequence_counts(pf, seed0 + 20_000 + s, **w.seq)
+            e2.record(stream)
+            e2.synchronize()
+            place_ms += e0.elapsed_time(e1)
+            seq_ms += e1.elapsed_time(e2)
+            read_kernel_ms += res.kernel_ms()
+            reads += res.dims()[2]
+            muts += pf.num_of_mutations
+            last = (pf, res)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        n_launch = launches() - n0
+    step_ms = (place_ms + seq_ms) / args.steps
+    t = torch.tensor([place_ms + seq_ms, place_ms, seq_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t[0])
+    value = world * reads / (total_ms / 1000.0)
+    # read-locus visits of the last step, for the roofline's algorithmic bytes
+    pf, res = last
+    alt, dep = res.counts()
+    site_hits = int(dep.astype(np.int64).sum())
+    reads_last = res.dims()[2]
+    kms = res.kernel_ms()
+    alg_bytes = BYTES_PER_READ * reads_last + BYTES_PER_SITE_HIT * site_hits
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (kms / 1000.0) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "k_reads_traffic.json"
+    if tf.exists():
+        d = json.loads(tf.read_text())
+        # traffic per read scaled to this launch (traffic grows with reads)
+        traffic = d.get("dram_bytes_per_read", 0.0) * reads_last if d.get("dram_bytes_per_read") else None
+
+    # end to end through the public API from host buffers: forest upload,
+    # placement, sequencing and the alt/depth tables back to host memory
+    e2e_steps = min(args.steps, 3)
+    forest_bytes = w.forest.num_of_nodes * (4 + 8 + 4 + 4 + 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_reads = 0
+    d2h = 0
+    for s in range(e2e_steps):
+        pf2 = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=seed0 + 30_000 + s)
+        r2 = sequence_counts(pf2, seed0 + 40_000 + s, **w.seq)
+        a2, d2 = r2.counts()
+        e2e_reads += r2.dims()[2]
+        d2h += a2.nbytes + d2.nbytes
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * e2e_reads / e2e_s
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            desc = (f"oracle std::mt19937_64 port on {CPU_SAMPLE_SCALE:.0%} of the genome (31 Mbp over the same "
+                    "24 chromosomes), full forest, 100x paired, purity 0.7, + normal, 1 step")
+            r = run_cpu(1, 0, threads, desc)
+            r1 = run_cpu(1, 0, 1, desc)
+            cpu = {"value": r["reads_per_s"], "unit": "reads/s", "cores": threads, "kind": "port", "sample": desc,
+                   "single_core_value": r1["reads_per_s"],
+                   "mutations_placed_per_s": r["mutations_placed_per_s"]}
+        clocks = clk.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "reads_per_step_per_gpu": reads // args.steps,
+                       "mutations_per_step_per_gpu": muts // args.steps,
+                       "l2": "flushed between steps (256 MiB write); record and count tables exceed L2",
+                       "parallelism": f"replicas x{world}"},
+            "secondary": {"mutations_placed_per_s": world * muts / (float(t[1]) / 1000.0),
+                          "sequencing_reads_per_s": world * reads / (float(t[2]) / 1000.0),
+                          "place_ms_per_step": float(t[1]) / args.steps, "seq_ms_per_step": float(t[2]) / args.steps,
+                          "bracket_wall_s": wall},
+            "roofline": {"kernel": "k_reads", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "algorithmic_bytes": alg_bytes, "kernel_ms": kms,
+                         "per_unit": f"{BYTES_PER_READ} B/read + {BYTES_PER_SITE_HIT} B/site hit"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": forest_bytes,
+                    "d2h_bytes_per_step": d2h // max(1, e2e_steps)},
+            "gpu_launches": n_launch,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,183 @@
+/*
+ * process_gb300 — C-ABI of the GB300 mutation-placement and bulk-sequencing
+ * path of ProCESS.
+ *
+ * The two RACES call sites this library replaces are
+ *   m_engine.place_mutations(...)      src/mutation_engine.cpp:1097-1101
+ *   simulator(sequencer, ...)          src/seq_simulation.cpp:371,413,423
+ * Everything above them (the Rcpp modules src/mutations.cpp:392-756,
+ * src/sequencing.cpp:193-282 and the data-frame flatteners
+ * src/seq_simulation.cpp:52-181) keeps its signatures; the Rcpp shim maps
+ * each argument onto the calls below.
+ *
+ * Conventions
+ *   - Every function returns a pg_status; 0 is success.  On failure
+ *     pg_last_error() holds a message for the calling thread; the Rcpp shim
+ *     rethrows it as std::runtime_error / std::domain_error, as the reference
+ *     does (src/sequencers.cpp:78-105, src/seq_simulation.cpp:431-451).
+ *   - Handles are opaque and owned by the library until their _destroy call.
+ *     Inputs are copied during the call: the caller may free them afterwards.
+ *   - Calls are synchronous on the engine's CUDA stream; device results stay
+ *     in HBM until a _copy function moves them to caller-owned host memory.
+ *   - Chromosome positions in/out are 1-based (chr_pos); absolute positions
+ *     are 0-based offsets into the concatenated genome.
+ */
+#ifndef PROCESS_GB300_H
+#define PROCESS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int pg_status;
+enum {
+  PG_OK = 0,
+  PG_ERR_DOMAIN = 1,      /* invalid argument (reference: std::domain_error) */
+  PG_ERR_RUNTIME = 2,     /* runtime failure (reference: std::runtime_error) */
+  PG_ERR_CUDA = 3,        /* CUDA error or no device */
+  PG_ERR_NOMEM = 4,       /* device allocation failed */
+  PG_ERR_UNSUPPORTED = 5  /* feature not built in this library */
+};
+
+typedef struct pg_engine pg_engine;
+typedef struct pg_forest pg_forest;
+typedef struct pg_placed pg_placed;
+typedef struct pg_seq_result pg_seq_result;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* pg_last_error(void);
+/* Library version string. */
+const char* pg_version(void);
+/* Number of visible CUDA devices (0 when none). */
+pg_status pg_device_count(int* n);
+
+/* ------------------------------------------------------------------ engine
+ * Replaces MutationEngine construction: build_MutationEngine /
+ * init_mutation_engine (src/mutation_engine.cpp:489-496, 653-699), i.e. the
+ * reference genome load plus build_contex_index (:211-275, call
+ * ContextIndex::build_index :260) and build_rs_index (:289-359, call
+ * RSIndex::build_index :344).  Both indices are built on the GPU. */
+typedef struct {
+  uint32_t n_chr;
+  const uint32_t* chr_lengths;      /* bases per chromosome */
+  const uint8_t* bases;             /* concatenated codes A=0 C=1 G=2 T=3, or NULL: synthetic genome */
+  uint64_t synthetic_seed;          /* seeded i.i.d. bases when bases == NULL */
+  double synthetic_gc;              /* GC fraction of the synthetic genome */
+  uint32_t context_sampling;        /* keep 1 in N occurrences per context (reference default 100) */
+  uint32_t max_repetition_storage;  /* positions kept per ID class (reference default 500000) */
+} pg_genome_desc;
+
+pg_status pg_engine_create(const pg_genome_desc* genome, pg_engine** out);
+pg_status pg_engine_destroy(pg_engine* eng);
+/* Runs every later call of the engine on the caller's cudaStream_t (NULL =
+ * the engine's own stream).  No reference counterpart: the reference has no
+ * device; this lets a host framework order the calls with its own work. */
+pg_status pg_engine_set_stream(pg_engine* eng, void* cuda_stream);
+/* Number of kernels this library has launched in the process so far. */
+pg_status pg_launch_count(uint64_t* n);
+
+/* Genome size and per-class position counts of the indices (ctx: 32 entries,
+ * id: 83 entries; either may be NULL).  get_genome_info, src/mutation_engine.cpp. */
+pg_status pg_engine_genome_info(const pg_engine* eng, uint64_t* total_len, uint64_t* ctx_total,
+                                uint64_t* id_total, uint32_t* ctx_stored, uint32_t* id_stored);
+/* Copies n bases (codes 0..3) of the concatenated genome from `start`. */
+pg_status pg_engine_read_genome(const pg_engine* eng, uint64_t start, uint64_t n, uint8_t* out);
+/* Bases (codes 0..3; 4 outside the genome) at n absolute positions. */
+pg_status pg_engine_gather_bases(const pg_engine* eng, uint64_t n, const uint32_t* positions, uint8_t* out);
+/* Copies the stored positions of index class `cls` (which: 0 = SBS context, 1 = ID class). */
+pg_status pg_engine_read_index(const pg_engine* eng, int which, uint32_t cls, uint32_t* out, uint32_t capacity,
+                               uint32_t* n_out);
+
+/* Signatures (Signature<SBSType|IDType>::read_from_stream,
+ * src/mutation_engine.cpp:389-397): n_sigs rows of 96 (type 0, SBS) or 83
+ * (type 1, ID) class probabilities in COSMIC order. */
+pg_status pg_engine_set_signatures(pg_engine* eng, int type, uint32_t n_sigs, const double* probs);
+/* MutationEngine::add_exposure(time, exposure) (src/mutation_engine.cpp:734-739):
+ * coefficients over the n_sigs signatures of `type`, active from `time`. */
+pg_status pg_engine_add_exposure(pg_engine* eng, int type, double time, const double* coeffs);
+/* Passenger rates per base per division of a species (mutant + epistate),
+ * MutationEngine::add_mutant / get_passenger_rates (src/mutation_engine.cpp:864-1083). */
+pg_status pg_engine_set_species_rates(pg_engine* eng, uint32_t species, double snv, double indel, double cna);
+/* Per-epoch passenger rates (epoch = interval between consecutive exposure
+ * change times); overrides the constant rates of the species. */
+pg_status pg_engine_set_species_epoch_rates(pg_engine* eng, uint32_t species, uint32_t n_epochs,
+                                            const double* snv, const double* indel);
+/* Mutant of a species: drivers are applied on the first edge whose mutant
+ * differs from its parent's (driver lists, src/mutation_engine.cpp:789-862). */
+pg_status pg_engine_set_species_mutant(pg_engine* eng, uint32_t species, uint32_t mutant);
+/* Driver SNV/indel of a mutant, in application order (SIDMut, src/sid.cpp:18-146).
+ * ref/alt are base strings (indels: VCF style, sharing the first base);
+ * allele < 0 = random allele. */
+pg_status pg_engine_add_driver_sid(pg_engine* eng, uint32_t mutant, uint32_t chr_index, uint32_t chr_pos,
+                                   const char* ref, const char* alt, int32_t allele);
+/* Driver CNA (src/cna.cpp:21-138) and whole-genome doubling (src/wg_doubling.hpp). */
+pg_status pg_engine_add_driver_cna(pg_engine* eng, uint32_t mutant, int type_amplification, uint32_t chr_index,
+                                   uint32_t begin, uint32_t length, int32_t allele, int32_t src_allele);
+pg_status pg_engine_add_driver_wgd(pg_engine* eng, uint32_t mutant);
+/* infinite_sites_model property (src/mutation_engine.hpp:148-156). */
+pg_status pg_engine_set_infinite_sites(pg_engine* eng, int on);
+pg_status pg_engine_get_infinite_sites(const pg_engine* eng, int* on);
+
+/* ------------------------------------------------------------------ forest
+ * SamplesForest (src/samples_forest.hpp:31, node fields src/forest.hpp:29-68):
+ * nodes in topological order (parent index < node index, -1 for roots),
+ * birth time, species id, sample index of leaves (-1 for internal nodes) and
+ * the number of cell divisions on the edge into the node (NULL = 1 each). */
+pg_status pg_forest_create(uint32_t n_nodes, const int32_t* parent, const double* birth, const uint32_t* species,
+                           const int32_t* sample, const uint32_t* divisions, uint32_t n_samples, pg_forest** out);
+pg_status pg_forest_destroy(pg_forest* forest);
+
+/* ------------------------------------------------------------------ placement
+ * MutationEngine::place_mutations(forest, #preneoplastic SNVs, SBS signature,
+ * #preneoplastic indels, ID signature, seed) (src/mutation_engine.cpp:1085-1113;
+ * R defaults "SBS1"/"ID1", src/mutation_engine.hpp:160-206): sig indices
+ * select rows of the signature tables. */
+pg_status pg_place_mutations(pg_engine* eng, const pg_forest* forest, uint32_t n_pre_snv, uint32_t pre_sbs_sig,
+                             uint32_t n_pre_indel, uint32_t pre_id_sig, uint64_t seed, pg_placed** out);
+pg_status pg_placed_destroy(pg_placed* placed);
+pg_status pg_placed_count(const pg_placed* placed, uint64_t* n_mutations);
+/* Placed mutations sorted by (absolute locus, slot); any pointer may be NULL.
+ * aux: SNV alt base code; indel bit0 = insertion, bits1-3 = length, bits 8.. inserted bases. */
+pg_status pg_placed_copy(const pg_placed* placed, uint32_t* locus, uint32_t* edge, uint32_t* aux, uint8_t* cls,
+                         uint8_t* sig, uint8_t* allele, uint8_t* kind, uint8_t* nature);
+/* Device time of the placement kernels of the last place call (ms). */
+pg_status pg_placed_kernel_ms(const pg_placed* placed, float* ms);
+
+/* ------------------------------------------------------------------ sequencing
+ * simulate_seq / simulate_normal_seq (src/seq_simulation.cpp:517-679; R
+ * defaults src/sequencing.cpp:193-209,268-282) down to the read simulator. */
+enum { PG_INSERT_BINOMIAL = 0, PG_INSERT_NORMAL = 1 };
+typedef struct {
+  double coverage;              /* default 10 */
+  uint32_t read_size;           /* default 150 */
+  uint32_t insert_size_mean;    /* 0 = single-end reads */
+  uint32_t insert_size_stddev;  /* default 10 */
+  int insert_model;             /* PG_INSERT_BINOMIAL (reference get_bin_dist) or PG_INSERT_NORMAL */
+  double error_rate;            /* BasicIlluminaSequencer error rate; 0 = ErrorlessIlluminaSequencer */
+  double purity;                /* default 1 */
+  int with_normal_sample;       /* default 1 */
+  int preneoplastic_in_normal;  /* default 0 */
+  int normal_only;              /* simulate_normal_seq: sequence only the normal sample */
+  uint32_t n_chr_sel;           /* 0 = every chromosome */
+  const uint32_t* chr_sel;      /* chromosome indices */
+  uint32_t tile_size;           /* 0 = automatic */
+} pg_seq_cfg;
+
+pg_status pg_simulate_seq(const pg_placed* placed, const pg_seq_cfg* cfg, uint64_t seed, pg_seq_result** out);
+pg_status pg_seq_result_destroy(pg_seq_result* res);
+/* Sequenced samples = forest samples (+ the normal sample, last). */
+pg_status pg_seq_result_dims(const pg_seq_result* res, uint32_t* n_samples, uint64_t* n_mutations,
+                             uint64_t* n_reads);
+/* alt ("occurrences") and depth ("coverage") as [n_samples][n_mutations]
+ * int32, in the order of pg_placed_copy. */
+pg_status pg_seq_result_copy(const pg_seq_result* res, int32_t* alt, int32_t* depth);
+/* Device time of the read kernel of the call (ms). */
+pg_status pg_seq_result_kernel_ms(const pg_seq_result* res, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PROCESS_GB300_H */

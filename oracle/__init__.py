@@ -1,0 +1,232 @@
+"""ORACLE — test infrastructure only (the product never imports this package).
+
+ctypes wrapper of ``oracle/_build/liboracle.so``, the sequential CPU
+restatement of the placement and sequencing path (oracle.cpp).  PARITY
+UNPINNED: RACES, which holds the reference arithmetic, is absent; the
+restatement follows ProCESS's call sites and data contracts (see oracle.cpp).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+_L = None
+
+
+def build() -> Path:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _L
+    if _L is None:
+        if not LIB_PATH.exists():
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        P = C.c_void_p
+        u8p, u32p, i32p, u64p, f64p = (C.POINTER(t) for t in (C.c_uint8, C.c_uint32, C.c_int32, C.c_uint64,
+                                                                C.c_double))
+        sig = {
+            "orc_last_error": (C.c_char_p, []),
+            "orc_philox": (None, [C.c_uint32] * 6 + [u32p]),
+            "orc_log": (C.c_double, [C.c_double]),
+            "orc_exp": (C.c_double, [C.c_double]),
+            "orc_log_factorial": (C.c_double, [C.c_double]),
+            "orc_poisson": (C.c_uint64, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_double]),
+            "orc_binomial": (C.c_uint64, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint64,
+                                          C.c_double]),
+            "orc_genome_synth": (None, [C.c_uint64, C.c_uint64, C.c_double, u8p]),
+            "orc_engine_create": (P, [C.c_uint32, u32p, u8p, C.c_uint64, C.c_double, C.c_uint32, C.c_uint32]),
+            "orc_engine_destroy": (None, [P]),
+            "orc_engine_index_info": (None, [P, u64p, u64p, u32p, u32p]),
+            "orc_engine_read_index": (None, [P, C.c_int, C.c_uint32, u32p]),
+            "orc_engine_read_genome": (None, [P, u8p]),
+            "orc_engine_set_signatures": (None, [P, C.c_int, C.c_uint32, f64p]),
+            "orc_engine_add_exposure": (None, [P, C.c_int, C.c_double, f64p]),
+            "orc_engine_set_species_rates": (None, [P, C.c_uint32, C.c_double, C.c_double]),
+            "orc_engine_set_species_epoch_rates": (None, [P, C.c_uint32, C.c_uint32, f64p, f64p]),
+            "orc_engine_set_species_mutant": (None, [P, C.c_uint32, C.c_uint32]),
+            "orc_engine_add_driver_sid": (None, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_char_p, C.c_char_p,
+                                                 C.c_int32]),
+            "orc_engine_set_infinite_sites": (None, [P, C.c_int]),
+            "orc_place": (P, [P, C.c_uint32, i32p, f64p, u32p, i32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32,
+                              C.c_uint32, C.c_uint32, C.c_uint64, C.c_int]),
+            "orc_placed_destroy": (None, [P]),
+            "orc_placed_count": (C.c_uint64, [P]),
+            "orc_placed_copy": (None, [P, u32p, u32p, u32p, u8p, u8p, u8p, u8p, u8p]),
+            "orc_placed_set": (None, [P, C.c_uint64, u32p, u32p, u8p, u8p]),
+            "orc_seq": (P, [P, C.c_void_p, C.c_uint64, C.c_int, C.c_double, C.c_int]),
+            "orc_seq_destroy": (None, [P]),
+            "orc_seq_samples": (C.c_uint32, [P]),
+            "orc_seq_reads": (C.c_uint64, [P]),
+            "orc_seq_copy": (None, [P, i32p, i32p]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _L = L
+    return _L
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(C.POINTER(t))
+
+
+def _err():
+    return lib().orc_last_error().decode()
+
+
+class OracleEngine:
+    """Mirror of process_gb300.MutationEngine over the CPU restatement."""
+
+    def __init__(self, chr_lengths, bases=None, seed=0, gc=0.5, context_sampling=100, max_rep=500000):
+        self.chr_lengths = np.ascontiguousarray(chr_lengths, dtype=np.uint32)
+        b = None if bases is None else np.ascontiguousarray(bases, dtype=np.uint8)
+        self._h = lib().orc_engine_create(len(self.chr_lengths), _p(self.chr_lengths, C.c_uint32),
+                                          _p(b, C.c_uint8), int(seed), float(gc), int(context_sampling),
+                                          int(max_rep))
+        if not self._h:
+            raise RuntimeError(_err())
+        self.sig_names = [[], []]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_engine_destroy(self._h)
+            self._h = None
+
+    @classmethod
+    def like(cls, w, **kw):
+        """An oracle engine configured like process_gb300.synth.build_engine(w)."""
+        g = w.genome
+        e = cls(g.chr_lengths, g.bases, g.seed, g.gc, context_sampling=w.context_sampling, **kw)
+        e.set_signatures(0, w.sbs)
+        e.set_signatures(1, w.ids)
+        species = {}
+        for mut_id, (name, rates, drivers) in enumerate(w.mutants):
+            keys = set(rates.keys())
+            per_epi = {"": rates} if keys <= {"SNV", "indel", "CNA"} else dict(rates)
+            for epi, r in per_epi.items():
+                sid = species.setdefault((name, epi), len(species))
+                snv, indel = r.get("SNV", 0.0), r.get("indel", 0.0)
+                if np.ndim(snv) or np.ndim(indel):
+                    n = max(np.size(snv), np.size(indel))
+                    e.set_epoch_rates(sid, np.broadcast_to(np.asarray(snv, float), (n,)),
+                                      np.broadcast_to(np.asarray(indel, float), (n,)))
+                else:
+                    e.set_rates(sid, snv, indel)
+                lib().orc_engine_set_species_mutant(e._h, sid, mut_id)
+        e.species = species
+        for t, coeffs in w.exposures:
+            e.add_exposure(t, coeffs)
+        return e
+
+    def set_signatures(self, ty, sigs: dict):
+        names = list(sigs)
+        mat = np.ascontiguousarray(np.array([sigs[k] for k in names], dtype=np.float64))
+        lib().orc_engine_set_signatures(self._h, ty, len(names), _p(mat, C.c_double))
+        self.sig_names[ty] = names
+
+    def add_exposure(self, time, coeffs: dict):
+        for ty in (0, 1):
+            v = np.zeros(len(self.sig_names[ty]))
+            used = False
+            for k, c in coeffs.items():
+                if k in self.sig_names[ty]:
+                    v[self.sig_names[ty].index(k)] = c
+                    used = True
+            if used:
+                lib().orc_engine_add_exposure(self._h, ty, float(time), _p(np.ascontiguousarray(v), C.c_double))
+
+    def set_rates(self, sid, snv, indel):
+        lib().orc_engine_set_species_rates(self._h, sid, float(snv), float(indel))
+
+    def set_epoch_rates(self, sid, snv, indel):
+        s = np.ascontiguousarray(snv, dtype=np.float64)
+        i = np.ascontiguousarray(indel, dtype=np.float64)
+        lib().orc_engine_set_species_epoch_rates(self._h, sid, len(s), _p(s, C.c_double), _p(i, C.c_double))
+
+    def add_driver_sid(self, mutant, chr_idx, pos, ref, alt, allele=-1):
+        lib().orc_engine_add_driver_sid(self._h, mutant, chr_idx, pos, ref.encode(), alt.encode(), allele)
+
+    def set_infinite_sites(self, on):
+        lib().orc_engine_set_infinite_sites(self._h, 1 if on else 0)
+
+    def index_info(self):
+        ct, it = np.zeros(32, np.uint64), np.zeros(83, np.uint64)
+        cl, il = np.zeros(32, np.uint32), np.zeros(83, np.uint32)
+        lib().orc_engine_index_info(self._h, _p(ct, C.c_uint64), _p(it, C.c_uint64), _p(cl, C.c_uint32),
+                                    _p(il, C.c_uint32))
+        return {"ctx_total": ct, "id_total": it, "ctx_stored": cl, "id_stored": il}
+
+    def read_index(self, which, cls):
+        n = self.index_info()["ctx_stored" if which == 0 else "id_stored"][cls]
+        out = np.empty(n, dtype=np.uint32)
+        lib().orc_engine_read_index(self._h, which, cls, _p(out, C.c_uint32))
+        return out
+
+    def read_genome(self):
+        out = np.empty(int(self.chr_lengths.astype(np.uint64).sum()), dtype=np.uint8)
+        lib().orc_engine_read_genome(self._h, _p(out, C.c_uint8))
+        return out
+
+    def place(self, forest, species, n_pre_snv=0, pre_sbs=0, n_pre_id=0, pre_id=0, seed=0, flavour=0):
+        parent = np.ascontiguousarray(forest.parent, dtype=np.int32)
+        birth = np.ascontiguousarray(forest.birth_time, dtype=np.float64)
+        sp = np.ascontiguousarray(species, dtype=np.uint32)
+        sample = np.ascontiguousarray(np.where(forest.is_leaf, forest.sample, -1), dtype=np.int32)
+        div = np.ascontiguousarray(forest.divisions, dtype=np.uint32)
+        h = lib().orc_place(self._h, forest.num_of_nodes, _p(parent, C.c_int32), _p(birth, C.c_double),
+                            _p(sp, C.c_uint32), _p(sample, C.c_int32), _p(div, C.c_uint32),
+                            len(forest.sample_names), n_pre_snv, pre_sbs, n_pre_id, pre_id, int(seed), flavour)
+        if not h:
+            raise RuntimeError(_err())
+        return OraclePlaced(h)
+
+
+class OraclePlaced:
+    def __init__(self, h):
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_placed_destroy(self._h)
+            self._h = None
+
+    def table(self) -> dict:
+        n = lib().orc_placed_count(self._h)
+        t = {k: np.empty(n, dtype=np.uint32) for k in ("locus", "edge", "aux")}
+        t.update({k: np.empty(n, dtype=np.uint8) for k in ("cls", "sig", "allele", "kind", "nature")})
+        lib().orc_placed_copy(self._h, *(_p(t[k], C.c_uint32) for k in ("locus", "edge", "aux")),
+                              *(_p(t[k], C.c_uint8) for k in ("cls", "sig", "allele", "kind", "nature")))
+        return t
+
+    def set_table(self, t: dict):
+        arrs = [np.ascontiguousarray(t[k], dtype=d) for k, d in
+                (("locus", np.uint32), ("edge", np.uint32), ("allele", np.uint8), ("kind", np.uint8))]
+        lib().orc_placed_set(self._h, len(arrs[0]), _p(arrs[0], C.c_uint32), _p(arrs[1], C.c_uint32),
+                             _p(arrs[2], C.c_uint8), _p(arrs[3], C.c_uint8))
+
+    def sequence(self, cfg, seed, flavour=0, fraction=1.0, threads=1):
+        """cfg: a process_gb300._lib.SeqCfg (same layout as the oracle's)."""
+        h = lib().orc_seq(self._h, C.addressof(cfg), int(seed), flavour, float(fraction), int(threads))
+        if not h:
+            raise RuntimeError(_err())
+        try:
+            s = lib().orc_seq_samples(h)
+            n = lib().orc_placed_count(self._h)
+            alt = np.empty((s, n), dtype=np.int32)
+            dep = np.empty((s, n), dtype=np.int32)
+            lib().orc_seq_copy(h, _p(alt, C.c_int32), _p(dep, C.c_int32))
+            reads = lib().orc_seq_reads(h)
+        finally:
+            lib().orc_seq_destroy(h)
+        return alt, dep, reads

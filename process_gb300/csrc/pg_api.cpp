@@ -1,0 +1,1074 @@
+// C-ABI of the library (declared in include/process_gb300.h): handles,
+// validation, host-side table preparation and orchestration of the kernels.
+#include "../../include/process_gb300.h"
+#include "pg_common.cuh"
+#include "pg_kernels.h"
+#include "pg_scan.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void pg::note_launch(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct DomainError : std::runtime_error { using std::runtime_error::runtime_error; };
+struct Unsupported : std::runtime_error { using std::runtime_error::runtime_error; };
+struct CudaError : std::runtime_error { using std::runtime_error::runtime_error; };
+struct NoMem : std::runtime_error { using std::runtime_error::runtime_error; };
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) { cudaGetLastError(); throw NoMem(std::string(what) + ": out of device memory"); }
+    throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+template <class F>
+pg_status guarded(F&& f) {
+  try {
+    f();
+    g_last_error.clear();
+    return PG_OK;
+  } catch (const DomainError& e) { g_last_error = e.what(); return PG_ERR_DOMAIN; }
+  catch (const Unsupported& e) { g_last_error = e.what(); return PG_ERR_UNSUPPORTED; }
+  catch (const CudaError& e) { g_last_error = e.what(); return PG_ERR_CUDA; }
+  catch (const NoMem& e) { g_last_error = e.what(); return PG_ERR_NOMEM; }
+  catch (const std::exception& e) { g_last_error = e.what(); return PG_ERR_RUNTIME; }
+  catch (...) { g_last_error = "unknown error"; return PG_ERR_RUNTIME; }
+}
+
+void require(bool c, const std::string& msg) { if (!c) throw DomainError(msg); }
+
+// ---------------------------------------------------------------- device memory
+// A small caching pool: freed blocks are kept per engine and reused by size,
+// so repeated place/sequence calls do not pay cudaMalloc/cudaFree.
+class Pool {
+ public:
+  ~Pool() { release_all(); }
+  void* get(size_t bytes) {
+    if (bytes == 0) bytes = 256;
+    bytes = (bytes + 255) & ~size_t(255);
+    auto it = free_.lower_bound(bytes);
+    if (it != free_.end() && it->first <= 2 * bytes) {
+      void* p = it->second;
+      sizes_[p] = it->first;
+      free_.erase(it);
+      return p;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      release_free();
+      ck(cudaMalloc(&p, bytes), "cudaMalloc");
+    }
+    sizes_[p] = bytes;
+    return p;
+  }
+  void put(void* p) {
+    if (!p) return;
+    auto it = sizes_.find(p);
+    if (it == sizes_.end()) return;
+    free_.emplace(it->second, p);
+    sizes_.erase(it);
+  }
+  void release_free() {
+    for (auto& kv : free_) cudaFree(kv.second);
+    free_.clear();
+  }
+  void release_all() {
+    release_free();
+    for (auto& kv : sizes_) cudaFree(kv.first);
+    sizes_.clear();
+  }
+
+ private:
+  std::multimap<size_t, void*> free_;
+  std::map<void*, size_t> sizes_;
+};
+
+template <class T>
+struct DBuf {  // device buffer drawn from a pool
+  Pool* pool = nullptr;
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(Pool* pl, size_t count) : pool(pl), p(static_cast<T*>(pl->get(sizeof(T) * std::max<size_t>(count, 1)))), n(count) {}
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { reset(); pool = o.pool; p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { reset(); }
+  void reset() { if (p && pool) pool->put(p); p = nullptr; n = 0; }
+};
+
+template <class T>
+DBuf<T> upload(Pool* pool, const std::vector<T>& v, cudaStream_t st) {
+  DBuf<T> b(pool, v.size());
+  if (!v.empty()) ck(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st), "upload");
+  return b;
+}
+
+// ---------------------------------------------------------------- CDF tables
+// thresholds floor(CDF * 2^31); the last class with positive mass gets 2^31
+std::vector<uint32_t> cdf_thresholds(const std::vector<double>& w) {
+  std::vector<uint32_t> thr(w.size(), 0);
+  double tot = 0;
+  for (double x : w) tot += x;
+  if (!(tot > 0)) return thr;
+  size_t last = 0;
+  for (size_t i = 0; i < w.size(); ++i) if (w[i] > 0) last = i;
+  double c = 0;
+  for (size_t i = 0; i < w.size(); ++i) {
+    c += w[i];
+    double t = std::floor(c / tot * 2147483648.0);
+    if (t > 2147483648.0) t = 2147483648.0;
+    thr[i] = (i >= last) ? 2147483648u : uint32_t(t);
+  }
+  return thr;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- handles
+struct Species {
+  double snv = 0, indel = 0, cna = 0;
+  std::vector<double> snv_epoch, indel_epoch;  // optional per-epoch overrides
+  uint32_t mutant = 0;
+  bool has_rates = false;
+};
+
+struct DriverSpec {
+  uint32_t chr, pos;  // 0-based chr index, 1-based position
+  std::string ref, alt;
+  int32_t allele;
+};
+
+struct pg_engine {
+  int device = 0;
+  cudaStream_t st = nullptr;         // the stream every call of the engine runs on
+  cudaStream_t own_st = nullptr;     // the engine's own stream (destroyed with it)
+  Pool pool;
+  uint32_t n_chr = 0;
+  std::vector<uint32_t> chr_len, chr_off;  // chr_off: n_chr + 1 entries
+  uint64_t G = 0;
+  DBuf<uint32_t> genome, chr_off_d;
+  uint32_t context_sampling = 100, max_rep = 500000;
+  // index
+  std::vector<uint64_t> ctx_total, id_total;
+  std::vector<uint32_t> ctx_len, id_len;
+  std::vector<uint64_t> ctx_off, id_off;
+  DBuf<uint32_t> ctx_lists, id_lists, ctx_len_d, id_len_d;
+  DBuf<uint64_t> ctx_off_d, id_off_d;
+  // signatures and exposures
+  uint32_t n_sig[2] = {0, 0};
+  std::vector<double> sigs[2];
+  std::map<double, std::vector<double>> expo[2];
+  std::map<uint32_t, Species> species;
+  std::map<uint32_t, std::vector<DriverSpec>> drivers;
+  bool infinite_sites = true;
+
+  ~pg_engine() {
+    genome.reset(); chr_off_d.reset(); ctx_lists.reset(); id_lists.reset();
+    ctx_len_d.reset(); id_len_d.reset(); ctx_off_d.reset(); id_off_d.reset();
+    pool.release_all();
+    if (own_st) cudaStreamDestroy(own_st);
+  }
+};
+
+struct pg_forest {
+  uint32_t n = 0, n_samples = 0;
+  std::vector<int32_t> parent, sample;
+  std::vector<double> birth;
+  std::vector<uint32_t> species, divisions;
+  std::vector<uint32_t> tin, tout;             // Euler intervals (preorder)
+  std::vector<std::vector<uint32_t>> leaves;   // per sample: tin of its leaves
+};
+
+struct pg_placed {
+  pg_engine* eng = nullptr;
+  uint32_t n_nodes = 0, n_samples = 0;
+  std::vector<uint32_t> tin, tout;
+  std::vector<std::vector<uint32_t>> leaves;
+  uint64_t M = 0;
+  DBuf<uint32_t> locus, edge, aux, attempt;
+  DBuf<uint8_t> cls, sig, allele, kind, nature;
+  float kernel_ms = 0;
+  pg::PlaceOut view() const {
+    return {locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, kind.p, nature.p, attempt.p};
+  }
+};
+
+struct pg_seq_result {
+  pg_engine* eng = nullptr;
+  uint32_t n_samples = 0;
+  uint64_t M = 0, n_reads = 0;
+  DBuf<uint32_t> alt, depth;
+  float kernel_ms = 0;
+};
+
+namespace {
+
+struct Timer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t st;
+  explicit Timer(cudaStream_t s) : st(s) {
+    ck(cudaEventCreate(&a), "event"); ck(cudaEventCreate(&b), "event");
+    ck(cudaEventRecord(a, st), "event");
+  }
+  float stop() {
+    ck(cudaEventRecord(b, st), "event");
+    ck(cudaEventSynchronize(b), "event");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~Timer() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); }
+};
+
+void select_device(const pg_engine* e) { ck(cudaSetDevice(e->device), "cudaSetDevice"); }
+
+void build_indices(pg_engine* e) {
+  const uint32_t ntiles = pg::index_num_tiles(e->G);
+  for (int which = 0; which < 2; ++which) {
+    const int NC = pg::index_num_classes(which);
+    DBuf<uint32_t> cnt(&e->pool, uint64_t(NC) * ntiles);
+    DBuf<uint32_t> part(&e->pool, pg::scan_part_elems(ntiles, NC));
+    DBuf<uint32_t> tot(&e->pool, NC);
+    pg::index_count(which, e->genome.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, part.p, tot.p, e->st);
+    std::vector<uint32_t> tot_h(NC);
+    ck(cudaMemcpyAsync(tot_h.data(), tot.p, sizeof(uint32_t) * NC, cudaMemcpyDeviceToHost, e->st), "index totals");
+    ck(cudaStreamSynchronize(e->st), "index count");
+    std::vector<uint32_t> stride(NC), len(NC);
+    std::vector<uint64_t> off(NC + 1, 0);
+    std::vector<uint64_t>& total = which == 0 ? e->ctx_total : e->id_total;
+    total.assign(NC, 0);
+    for (int k = 0; k < NC; ++k) {
+      total[k] = tot_h[k];
+      uint64_t sd;
+      if (which == 0) sd = e->context_sampling;
+      else sd = std::max<uint64_t>(1, (uint64_t(tot_h[k]) + e->max_rep - 1) / e->max_rep);
+      stride[k] = uint32_t(sd);
+      len[k] = uint32_t((uint64_t(tot_h[k]) + sd - 1) / sd);
+      off[k + 1] = off[k] + len[k];
+    }
+    auto stride_d = upload(&e->pool, stride, e->st);
+    auto len_d = upload(&e->pool, len, e->st);
+    std::vector<uint64_t> off_k(off.begin(), off.begin() + NC);
+    auto off_d = upload(&e->pool, off_k, e->st);
+    DBuf<uint32_t> lists(&e->pool, off[NC]);
+    pg::index_emit(which, e->genome.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p, off_d.p, len_d.p,
+                   lists.p, e->st);
+    ck(cudaStreamSynchronize(e->st), "index emit");
+    ck(cudaGetLastError(), "index kernels");
+    if (which == 0) {
+      e->ctx_len = len; e->ctx_off = off_k;
+      e->ctx_lists = std::move(lists); e->ctx_len_d = std::move(len_d); e->ctx_off_d = std::move(off_d);
+    } else {
+      e->id_len = len; e->id_off = off_k;
+      e->id_lists = std::move(lists); e->id_len_d = std::move(len_d); e->id_off_d = std::move(off_d);
+    }
+  }
+}
+
+uint32_t code_of(char c) {
+  switch (c) {
+    case 'A': case 'a': return 0;
+    case 'C': case 'c': return 1;
+    case 'G': case 'g': return 2;
+    case 'T': case 't': return 3;
+  }
+  throw DomainError(std::string("invalid base '") + c + "'");
+}
+
+// Euler intervals of the forest (preorder index, subtree end)
+void euler(pg_forest& f) {
+  std::vector<std::vector<uint32_t>> kids(f.n);
+  std::vector<uint32_t> roots;
+  for (uint32_t v = 0; v < f.n; ++v) {
+    if (f.parent[v] < 0) roots.push_back(v); else kids[f.parent[v]].push_back(v);
+  }
+  f.tin.assign(f.n, 0); f.tout.assign(f.n, 0);
+  uint32_t clock = 0;
+  std::vector<std::pair<uint32_t, uint32_t>> stack;  // node, next child
+  for (uint32_t r : roots) {
+    stack.push_back({r, 0});
+    f.tin[r] = clock++;
+    while (!stack.empty()) {
+      auto& top = stack.back();
+      if (top.second < kids[top.first].size()) {
+        const uint32_t c = kids[top.first][top.second++];
+        f.tin[c] = clock++;
+        stack.push_back({c, 0});
+      } else {
+        f.tout[top.first] = clock;
+        stack.pop_back();
+      }
+    }
+  }
+  f.leaves.assign(f.n_samples, {});
+  for (uint32_t v = 0; v < f.n; ++v) {
+    if (kids[v].empty() && f.sample[v] >= 0) f.leaves[f.sample[v]].push_back(f.tin[v]);
+  }
+}
+
+}  // namespace
+
+// ====================================================================== C-ABI
+extern "C" {
+
+const char* pg_last_error(void) { return g_last_error.c_str(); }
+const char* pg_version(void) { return "process_gb300 0.1 (sm_103a)"; }
+
+pg_status pg_device_count(int* n) {
+  return guarded([&] {
+    require(n != nullptr, "n is NULL");
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (e != cudaSuccess) { cudaGetLastError(); c = 0; }
+    *n = c;
+  });
+}
+
+pg_status pg_engine_create(const pg_genome_desc* gd, pg_engine** out) {
+  return guarded([&] {
+    require(gd && out, "NULL argument");
+    require(gd->n_chr > 0 && gd->chr_lengths, "the genome needs at least one chromosome");
+    require(gd->context_sampling >= 1, "context_sampling must be positive");
+    require(gd->max_repetition_storage >= 1, "max_repetition_storage must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      throw CudaError("no CUDA device: the GB300 kernels of process_gb300 need a GPU");
+    }
+    auto e = std::make_unique<pg_engine>();
+    ck(cudaGetDevice(&e->device), "cudaGetDevice");
+    ck(cudaStreamCreateWithFlags(&e->own_st, cudaStreamNonBlocking), "stream");
+    e->st = e->own_st;
+    e->n_chr = gd->n_chr;
+    e->chr_len.assign(gd->chr_lengths, gd->chr_lengths + gd->n_chr);
+    e->chr_off.assign(gd->n_chr + 1, 0);
+    uint64_t G = 0;
+    for (uint32_t c = 0; c < gd->n_chr; ++c) {
+      require(e->chr_len[c] > 0, "chromosome lengths must be positive");
+      e->chr_off[c] = uint32_t(G);
+      G += e->chr_len[c];
+      require(G < (uint64_t(1) << 32) - 1024, "genome longer than the u32 position space");
+    }
+    e->chr_off[gd->n_chr] = uint32_t(G);
+    e->G = G;
+    e->context_sampling = gd->context_sampling;
+    e->max_rep = gd->max_repetition_storage;
+    e->chr_off_d = upload(&e->pool, e->chr_off, e->st);
+    const uint64_t nwords = (G + 15) / 16;
+    e->genome = DBuf<uint32_t>(&e->pool, nwords + 4);
+    ck(cudaMemsetAsync(e->genome.p, 0, sizeof(uint32_t) * (nwords + 4), e->st), "memset");
+    if (gd->bases) {
+      DBuf<uint8_t> codes(&e->pool, G);
+      ck(cudaMemcpyAsync(codes.p, gd->bases, G, cudaMemcpyHostToDevice, e->st), "genome upload");
+      pg::genome_pack(e->genome.p, codes.p, G, e->st);
+      ck(cudaStreamSynchronize(e->st), "genome pack");
+    } else {
+      require(gd->synthetic_gc >= 0 && gd->synthetic_gc <= 1, "synthetic_gc must be in [0,1]");
+      pg::genome_synth(e->genome.p, G, gd->synthetic_seed, gd->synthetic_gc, e->st);
+    }
+    ck(cudaGetLastError(), "genome kernels");
+    build_indices(e.get());
+    *out = e.release();
+  });
+}
+
+pg_status pg_engine_set_stream(pg_engine* e, void* stream) {
+  return guarded([&] {
+    require(e != nullptr, "NULL engine");
+    select_device(e);
+    ck(cudaStreamSynchronize(e->st), "stream switch");
+    e->st = stream ? static_cast<cudaStream_t>(stream) : e->own_st;
+  });
+}
+
+pg_status pg_launch_count(uint64_t* n) {
+  return guarded([&] { require(n != nullptr, "NULL argument"); *n = g_launches.load(); });
+}
+
+pg_status pg_engine_destroy(pg_engine* eng) {
+  return guarded([&] { if (eng) { cudaSetDevice(eng->device); delete eng; } });
+}
+
+pg_status pg_engine_genome_info(const pg_engine* e, uint64_t* total_len, uint64_t* ctx_total, uint64_t* id_total,
+                                uint32_t* ctx_stored, uint32_t* id_stored) {
+  return guarded([&] {
+    require(e != nullptr, "NULL engine");
+    if (total_len) *total_len = e->G;
+    if (ctx_total) std::copy(e->ctx_total.begin(), e->ctx_total.end(), ctx_total);
+    if (id_total) std::copy(e->id_total.begin(), e->id_total.end(), id_total);
+    if (ctx_stored) std::copy(e->ctx_len.begin(), e->ctx_len.end(), ctx_stored);
+    if (id_stored) std::copy(e->id_len.begin(), e->id_len.end(), id_stored);
+  });
+}
+
+pg_status pg_engine_read_genome(const pg_engine* e, uint64_t start, uint64_t n, uint8_t* out) {
+  return guarded([&] {
+    require(e && out, "NULL argument");
+    require(start + n <= e->G, "range outside the genome");
+    select_device(e);
+    const uint64_t w0 = start / 16, w1 = (start + n + 15) / 16;
+    std::vector<uint32_t> words(w1 - w0);
+    if (!words.empty())
+      ck(cudaMemcpy(words.data(), e->genome.p + w0, sizeof(uint32_t) * words.size(), cudaMemcpyDeviceToHost), "read");
+    for (uint64_t i = 0; i < n; ++i) {
+      const uint64_t p = start + i;
+      out[i] = uint8_t((words[p / 16 - w0] >> (2 * (p % 16))) & 3u);
+    }
+  });
+}
+
+pg_status pg_engine_gather_bases(const pg_engine* e, uint64_t n, const uint32_t* pos, uint8_t* out) {
+  return guarded([&] {
+    require(e && (n == 0 || (pos && out)), "NULL argument");
+    if (n == 0) return;
+    select_device(e);
+    Pool* P = const_cast<Pool*>(&e->pool);
+    DBuf<uint32_t> pd(P, n);
+    DBuf<uint8_t> od(P, n);
+    ck(cudaMemcpyAsync(pd.p, pos, 4 * n, cudaMemcpyHostToDevice, e->st), "upload");
+    pg::genome_gather(e->genome.p, e->G, pd.p, n, od.p, e->st);
+    ck(cudaMemcpyAsync(out, od.p, n, cudaMemcpyDeviceToHost, e->st), "download");
+    ck(cudaStreamSynchronize(e->st), "gather");
+  });
+}
+
+pg_status pg_engine_read_index(const pg_engine* e, int which, uint32_t cls, uint32_t* out, uint32_t capacity,
+                               uint32_t* n_out) {
+  return guarded([&] {
+    require(e && n_out, "NULL argument");
+    require(which == 0 || which == 1, "which must be 0 (SBS) or 1 (ID)");
+    const auto& len = which == 0 ? e->ctx_len : e->id_len;
+    const auto& off = which == 0 ? e->ctx_off : e->id_off;
+    require(cls < len.size(), "class out of range");
+    *n_out = len[cls];
+    if (out && len[cls]) {
+      require(capacity >= len[cls], "output capacity too small");
+      select_device(e);
+      const uint32_t* base = (which == 0 ? e->ctx_lists.p : e->id_lists.p) + off[cls];
+      ck(cudaMemcpy(out, base, sizeof(uint32_t) * len[cls], cudaMemcpyDeviceToHost), "read index");
+    }
+  });
+}
+
+pg_status pg_engine_set_signatures(pg_engine* e, int type, uint32_t n_sigs, const double* probs) {
+  return guarded([&] {
+    require(e && probs, "NULL argument");
+    require(type == 0 || type == 1, "type must be 0 (SBS) or 1 (ID)");
+    require(n_sigs > 0 && n_sigs < 255, "between 1 and 254 signatures");
+    const uint32_t NC = type == 0 ? 96 : 83;
+    for (uint64_t i = 0; i < uint64_t(n_sigs) * NC; ++i)
+      require(probs[i] >= 0 && std::isfinite(probs[i]), "signature probabilities must be non-negative");
+    e->n_sig[type] = n_sigs;
+    e->sigs[type].assign(probs, probs + uint64_t(n_sigs) * NC);
+    e->expo[type].clear();
+  });
+}
+
+pg_status pg_engine_add_exposure(pg_engine* e, int type, double time, const double* coeffs) {
+  return guarded([&] {
+    require(e && coeffs, "NULL argument");
+    require(type == 0 || type == 1, "type must be 0 (SBS) or 1 (ID)");
+    require(e->n_sig[type] > 0, "set the signatures before adding exposures");
+    require(std::isfinite(time), "exposure time must be finite");
+    double tot = 0;
+    for (uint32_t i = 0; i < e->n_sig[type]; ++i) {
+      require(coeffs[i] >= 0, "exposure coefficients must be non-negative");
+      tot += coeffs[i];
+    }
+    require(tot > 0, "exposure coefficients must not all be zero");
+    e->expo[type][time] = std::vector<double>(coeffs, coeffs + e->n_sig[type]);
+  });
+}
+
+pg_status pg_engine_set_species_rates(pg_engine* e, uint32_t sp, double snv, double indel, double cna) {
+  return guarded([&] {
+    require(e != nullptr, "NULL engine");
+    require(snv >= 0, std::to_string(snv) + ": SNV rates must be non-negative");
+    require(indel >= 0, std::to_string(indel) + ": indel rates must be non-negative");
+    require(cna >= 0, std::to_string(cna) + ": CNA rates must be non-negative");
+    auto& s = e->species[sp];
+    s.snv = snv; s.indel = indel; s.cna = cna; s.has_rates = true;
+  });
+}
+
+pg_status pg_engine_set_species_epoch_rates(pg_engine* e, uint32_t sp, uint32_t n_epochs, const double* snv,
+                                            const double* indel) {
+  return guarded([&] {
+    require(e && snv && indel, "NULL argument");
+    require(n_epochs >= 1 && n_epochs <= pg::MAX_EPOCHS, "between 1 and 16 epochs");
+    for (uint32_t i = 0; i < n_epochs; ++i) require(snv[i] >= 0 && indel[i] >= 0, "rates must be non-negative");
+    auto& s = e->species[sp];
+    s.snv_epoch.assign(snv, snv + n_epochs);
+    s.indel_epoch.assign(indel, indel + n_epochs);
+    s.has_rates = true;
+  });
+}
+
+pg_status pg_engine_set_species_mutant(pg_engine* e, uint32_t sp, uint32_t mutant) {
+  return guarded([&] { require(e != nullptr, "NULL engine"); e->species[sp].mutant = mutant; });
+}
+
+pg_status pg_engine_add_driver_sid(pg_engine* e, uint32_t mutant, uint32_t chr, uint32_t pos, const char* ref,
+                                   const char* alt, int32_t allele) {
+  return guarded([&] {
+    require(e && ref && alt, "NULL argument");
+    require(chr < e->n_chr, "unknown chromosome");
+    std::string r(ref), a(alt);
+    require(!r.empty() && !a.empty(), "empty ref/alt");
+    require(pos >= 1 && pos + r.size() - 1 <= e->chr_len[chr], "mutation outside the chromosome");
+    require(r.size() == 1 || a.size() == 1, "indels share exactly their first base");
+    if (r.size() != 1 || a.size() != 1) require(r[0] == a[0], "indel ref and alt must share their first base");
+    require(r.size() <= 6 && a.size() <= 6, "driver indels up to 5 bases");
+    for (char c : r) code_of(c);
+    for (char c : a) code_of(c);
+    require(allele >= -1 && allele <= 1, "allele must be 0, 1 or random (-1)");
+    e->drivers[mutant].push_back({chr, pos, r, a, allele});
+  });
+}
+
+pg_status pg_engine_add_driver_cna(pg_engine* e, uint32_t, int, uint32_t, uint32_t, uint32_t, int32_t, int32_t) {
+  return guarded([&] {
+    require(e != nullptr, "NULL engine");
+    throw Unsupported("driver CNAs are not built in this version of process_gb300");
+  });
+}
+
+pg_status pg_engine_add_driver_wgd(pg_engine* e, uint32_t) {
+  return guarded([&] {
+    require(e != nullptr, "NULL engine");
+    throw Unsupported("whole-genome doubling is not built in this version of process_gb300");
+  });
+}
+
+pg_status pg_engine_set_infinite_sites(pg_engine* e, int on) {
+  return guarded([&] { require(e != nullptr, "NULL engine"); e->infinite_sites = on != 0; });
+}
+pg_status pg_engine_get_infinite_sites(const pg_engine* e, int* on) {
+  return guarded([&] { require(e && on, "NULL argument"); *on = e->infinite_sites ? 1 : 0; });
+}
+
+pg_status pg_forest_create(uint32_t n, const int32_t* parent, const double* birth, const uint32_t* species,
+                           const int32_t* sample, const uint32_t* divisions, uint32_t n_samples, pg_forest** out) {
+  return guarded([&] {
+    require(out && parent && birth && species && sample, "NULL argument");
+    require(n > 0, "empty forest");
+    require(n < (1u << 30), "forest too large");
+    auto f = std::make_unique<pg_forest>();
+    f->n = n; f->n_samples = n_samples;
+    f->parent.assign(parent, parent + n);
+    f->birth.assign(birth, birth + n);
+    f->species.assign(species, species + n);
+    f->sample.assign(sample, sample + n);
+    f->divisions.assign(n, 1);
+    if (divisions) f->divisions.assign(divisions, divisions + n);
+    for (uint32_t v = 0; v < n; ++v) {
+      require(f->parent[v] < int32_t(v) && f->parent[v] >= -1, "nodes must be in topological order (parent < node)");
+      require(std::isfinite(f->birth[v]), "birth times must be finite");
+      require(f->divisions[v] >= 1 && f->divisions[v] <= 1000000, "divisions per edge in [1, 1e6]");
+      require(f->sample[v] >= -1 && f->sample[v] < int32_t(n_samples), "sample index out of range");
+      if (f->parent[v] >= 0) require(f->birth[v] >= f->birth[f->parent[v]], "a cell is born after its parent");
+    }
+    euler(*f);
+    *out = f.release();
+  });
+}
+
+pg_status pg_forest_destroy(pg_forest* f) {
+  return guarded([&] { delete f; });
+}
+
+pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_snv, uint32_t pre_sbs_sig,
+                             uint32_t n_pre_id, uint32_t pre_id_sig, uint64_t seed, pg_placed** out) {
+  return guarded([&] {
+    require(e && f && out, "NULL argument");
+    select_device(e);
+    cudaStream_t st = e->st;
+    // ---- epochs: union of exposure change times
+    std::vector<double> times;
+    for (int ty = 0; ty < 2; ++ty) for (auto& kv : e->expo[ty]) times.push_back(kv.first);
+    std::sort(times.begin(), times.end());
+    times.erase(std::unique(times.begin(), times.end()), times.end());
+    if (times.empty()) times.push_back(0.0);
+    require(times.size() <= pg::MAX_EPOCHS, "at most 16 exposure epochs");
+    const uint32_t E = uint32_t(times.size());
+    // ---- species
+    uint32_t S = 0;
+    for (uint32_t v = 0; v < f->n; ++v) S = std::max(S, f->species[v] + 1);
+    std::vector<double> snv_rate(uint64_t(S) * E, 0.0), id_rate(uint64_t(S) * E, 0.0);
+    bool need_sbs = n_pre_snv > 0, need_id = n_pre_id > 0;
+    std::vector<uint8_t> used(S, 0);
+    for (uint32_t v = 0; v < f->n; ++v) used[f->species[v]] = 1;
+    for (uint32_t s = 0; s < S; ++s) {
+      if (!used[s]) continue;
+      auto it = e->species.find(s);
+      require(it != e->species.end() && it->second.has_rates,
+              "species " + std::to_string(s) + " has no passenger rates: add its mutant first");
+      const Species& sp = it->second;
+      for (uint32_t ep = 0; ep < E; ++ep) {
+        double rs = sp.snv, ri = sp.indel;
+        if (!sp.snv_epoch.empty()) {
+          require(sp.snv_epoch.size() == E, "per-epoch rates must cover every exposure epoch");
+          rs = sp.snv_epoch[ep]; ri = sp.indel_epoch[ep];
+        }
+        snv_rate[uint64_t(s) * E + ep] = rs;
+        id_rate[uint64_t(s) * E + ep] = ri;
+        need_sbs = need_sbs || rs > 0;
+        need_id = need_id || ri > 0;
+      }
+    }
+    // ---- CDF tables
+    std::vector<uint32_t> sig_cdf[2], expo_cdf[2];
+    for (int ty = 0; ty < 2; ++ty) {
+      const uint32_t NC = ty == 0 ? 96 : 83;
+      const bool need = ty == 0 ? need_sbs : need_id;
+      const uint32_t ns = std::max<uint32_t>(e->n_sig[ty], 1);
+      if (need) {
+        require(e->n_sig[ty] > 0, ty == 0 ? "no SBS signatures set" : "no ID signatures set");
+      }
+      std::vector<uint8_t> usable(ns, 0);
+      sig_cdf[ty].assign(uint64_t(ns) * NC, 0);
+      for (uint32_t s = 0; s < e->n_sig[ty]; ++s) {
+        std::vector<double> w(NC);
+        for (uint32_t k = 0; k < NC; ++k) {
+          const uint32_t list = ty == 0 ? uint32_t(pg::sbs_class_context(int(k))) : k;
+          const uint32_t len = ty == 0 ? e->ctx_len[list] : e->id_len[list];
+          w[k] = len > 0 ? e->sigs[ty][uint64_t(s) * NC + k] : 0.0;
+          if (w[k] > 0) usable[s] = 1;
+        }
+        auto thr = cdf_thresholds(w);
+        std::copy(thr.begin(), thr.end(), sig_cdf[ty].begin() + uint64_t(s) * NC);
+      }
+      expo_cdf[ty].assign(uint64_t(E + 1) * ns, 0);
+      for (uint32_t ep = 0; ep < E; ++ep) {
+        std::vector<double> w(ns, 0.0);
+        if (!e->expo[ty].empty()) {
+          auto it = e->expo[ty].upper_bound(times[ep]);
+          if (it == e->expo[ty].begin()) w = it->second; else w = std::prev(it)->second;
+        } else if (need && e->n_sig[ty] > 0) {
+          bool used_type = false;
+          for (uint32_t s = 0; s < S; ++s) if (used[s]) used_type = used_type || (ty == 0 ? snv_rate[uint64_t(s) * E + ep] > 0 : id_rate[uint64_t(s) * E + ep] > 0);
+          require(!used_type, ty == 0 ? "no SBS exposure: add an exposure before placing mutations"
+                                      : "no ID exposure: add an exposure before placing mutations");
+        }
+        for (uint32_t s = 0; s < ns && s < w.size(); ++s) {
+          if (w[s] > 0 && !usable[s]) throw DomainError("signature " + std::to_string(s) +
+                                                       " has no class with indexed positions");
+        }
+        auto thr = cdf_thresholds(w);
+        std::copy(thr.begin(), thr.end(), expo_cdf[ty].begin() + uint64_t(ep) * ns);
+      }
+      const uint32_t pre_sig = ty == 0 ? pre_sbs_sig : pre_id_sig;
+      const uint32_t n_pre = ty == 0 ? n_pre_snv : n_pre_id;
+      if (n_pre > 0) {
+        require(pre_sig < e->n_sig[ty], "unknown preneoplastic signature");
+        require(usable[pre_sig], "the preneoplastic signature has no class with indexed positions");
+        std::vector<double> w(ns, 0.0);
+        w[pre_sig] = 1.0;
+        auto thr = cdf_thresholds(w);
+        std::copy(thr.begin(), thr.end(), expo_cdf[ty].begin() + uint64_t(E) * ns);
+      }
+    }
+    // ---- device tables
+    Pool* P = &e->pool;
+    auto parent_d = upload(P, f->parent, st);
+    auto birth_d = upload(P, f->birth, st);
+    auto species_d = upload(P, f->species, st);
+    auto div_d = upload(P, f->divisions, st);
+    auto times_d = upload(P, times, st);
+    auto snv_d = upload(P, snv_rate, st);
+    auto id_d = upload(P, id_rate, st);
+    auto sbs_sig_d = upload(P, sig_cdf[0], st);
+    auto id_sig_d = upload(P, sig_cdf[1], st);
+    auto sbs_expo_d = upload(P, expo_cdf[0], st);
+    auto id_expo_d = upload(P, expo_cdf[1], st);
+    pg::PlaceTables t{};
+    t.n_nodes = f->n; t.parent = parent_d.p; t.birth = birth_d.p; t.species = species_d.p; t.divisions = div_d.p;
+    t.n_epochs = E; t.epoch_start = times_d.p; t.snv_rate = snv_d.p; t.indel_rate = id_d.p;
+    t.allelic_size = 2.0 * double(e->G);
+    t.n_sbs_sigs = std::max<uint32_t>(e->n_sig[0], 1); t.n_id_sigs = std::max<uint32_t>(e->n_sig[1], 1);
+    t.sbs_expo_cdf = sbs_expo_d.p; t.sbs_sig_cdf = sbs_sig_d.p; t.id_expo_cdf = id_expo_d.p; t.id_sig_cdf = id_sig_d.p;
+    t.genome = e->genome.p;
+    t.ctx_off = e->ctx_off_d.p; t.ctx_len = e->ctx_len_d.p; t.ctx_lists = e->ctx_lists.p;
+    t.id_off = e->id_off_d.p; t.id_len = e->id_len_d.p; t.id_lists = e->id_lists.p;
+
+    // ---- drivers: first edge of each mutant
+    std::vector<pg::DriverRec> drv;
+    for (uint32_t v = 0; v < f->n; ++v) {
+      auto mut_of = [&](uint32_t node) {
+        auto it = e->species.find(f->species[node]);
+        return it == e->species.end() ? 0u : it->second.mutant;
+      };
+      const uint32_t m = mut_of(v);
+      if (f->parent[v] >= 0 && mut_of(uint32_t(f->parent[v])) == m) continue;
+      auto it = e->drivers.find(m);
+      if (it == e->drivers.end()) continue;
+      for (const auto& d : it->second) {
+        pg::DriverRec r{};
+        const uint32_t abs = e->chr_off[d.chr] + d.pos - 1;
+        r.edge = v;
+        r.allele = d.allele < 0 ? 0xffu : uint32_t(d.allele);
+        if (d.ref.size() == 1 && d.alt.size() == 1) {
+          r.kind = pg::KIND_SNV; r.locus = abs; r.aux = code_of(d.alt[0]);
+        } else {
+          r.kind = pg::KIND_INDEL; r.locus = abs;  // the shared first base is the anchor
+          if (d.alt.size() > 1) {
+            uint32_t bases = 0;
+            for (size_t k = 1; k < d.alt.size(); ++k) bases |= code_of(d.alt[k]) << (2 * (k - 1));
+            r.aux = 1u | (uint32_t(d.alt.size() - 1) << 1) | (bases << 8);
+          } else {
+            r.aux = 0u | (uint32_t(d.ref.size() - 1) << 1);
+          }
+        }
+        drv.push_back(r);
+      }
+    }
+
+    Timer timer(st);
+    // ---- per-edge counts and offsets
+    const uint64_t ncell = uint64_t(f->n + 1) * E;
+    DBuf<uint32_t> cnt_snv(P, ncell), cnt_id(P, ncell), off_snv(P, ncell), off_id(P, ncell);
+    DBuf<uint32_t> part(P, pg::scan_part_elems(ncell, 1)), tot(P, 2);
+    pg::place_edge_counts(t, cnt_snv.p, cnt_id.p, seed, n_pre_snv, n_pre_id, st);
+    pg::scan_rows<uint32_t>(cnt_snv.p, off_snv.p, ncell, 1, part.p, tot.p, st);
+    pg::scan_rows<uint32_t>(cnt_id.p, off_id.p, ncell, 1, part.p, tot.p + 1, st);
+    uint32_t tot_h[2];
+    ck(cudaMemcpyAsync(tot_h, tot.p, sizeof(tot_h), cudaMemcpyDeviceToHost, st), "counts");
+    ck(cudaStreamSynchronize(st), "edge counts");
+    const uint64_t n_snv = tot_h[0], n_id = tot_h[1];
+    const uint64_t n_all = n_snv + n_id + drv.size();
+    require(n_all < (1ull << 31), "too many mutations for one placement call");
+    // ---- outputs
+    auto pl = std::make_unique<pg_placed>();
+    pl->eng = e; pl->n_nodes = f->n; pl->n_samples = f->n_samples;
+    pl->tin = f->tin; pl->tout = f->tout; pl->leaves = f->leaves;
+    pl->M = n_all;
+    DBuf<uint32_t> locus(P, n_all), edge(P, n_all), aux(P, n_all), attempt(P, n_all);
+    DBuf<uint8_t> cls(P, n_all), sig(P, n_all), allele(P, n_all), kind(P, n_all), nature(P, n_all);
+    pg::PlaceOut o{locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, kind.p, nature.p, attempt.p};
+    DBuf<uint32_t> err(P, 1);
+    ck(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st), "memset");
+    pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), nullptr,
+                               uint32_t(n_snv + n_id), 0, err.p, st);
+    auto drv_d = upload(P, drv, st);
+    pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), uint32_t(n_snv + n_id), seed, st);
+    // ---- infinite sites
+    if (e->infinite_sites && n_snv + n_id > 0) {
+      uint32_t cap = 1024;
+      while (cap < 2 * n_all) cap <<= 1;
+      DBuf<uint32_t> hkeys(P, cap), ckeys(P, cap), cvals(P, cap), pend_a(P, n_snv + n_id), pend_b(P, n_snv + n_id);
+      DBuf<uint8_t> lost(P, n_snv + n_id);
+      DBuf<uint32_t> n_next(P, 1);
+      ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+      // drivers occupy their loci first
+      pg::sites_insert_accepted(hkeys.p, cap - 1, locus.p + n_snv + n_id, uint32_t(drv.size()), st);
+      const uint32_t* pending = nullptr;
+      uint32_t n_pend = uint32_t(n_snv + n_id);
+      uint32_t* next = pend_a.p;
+      int round = 0;
+      while (n_pend > 0) {
+        require(round < 256, "infinite sites model: no free locus left for some mutations");
+        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
+        pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
+                        n_next.p, err.p, st);
+        uint32_t nn = 0;
+        ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+        ck(cudaStreamSynchronize(st), "infinite sites round");
+        if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, nn,
+                                           1, err.p, st);
+        pending = next;
+        next = (next == pend_a.p) ? pend_b.p : pend_a.p;
+        n_pend = nn;
+        ++round;
+      }
+    }
+    // ---- sort by locus
+    const uint32_t nb = pg::sort_num_buckets(e->G);
+    DBuf<uint32_t> bcnt(P, nb), bfill(P, nb), bpart(P, pg::scan_part_elems(nb, 1)), order(P, n_all);
+    pl->locus = DBuf<uint32_t>(P, n_all); pl->edge = DBuf<uint32_t>(P, n_all); pl->aux = DBuf<uint32_t>(P, n_all);
+    pl->attempt = DBuf<uint32_t>(P, n_all);
+    pl->cls = DBuf<uint8_t>(P, n_all); pl->sig = DBuf<uint8_t>(P, n_all); pl->allele = DBuf<uint8_t>(P, n_all);
+    pl->kind = DBuf<uint8_t>(P, n_all); pl->nature = DBuf<uint8_t>(P, n_all);
+    pg::sort_by_locus(o, uint32_t(n_all), e->G, bcnt.p, bfill.p, bpart.p, order.p, pl->view(), st);
+    pl->kernel_ms = timer.stop();
+    ck(cudaGetLastError(), "placement kernels");
+    uint32_t err_h = 0;
+    ck(cudaMemcpy(&err_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost), "error flag");
+    if (err_h & pg::ERR_EMPTY_CLASS) throw std::runtime_error("a drawn mutation class has no indexed positions");
+    if (err_h & pg::ERR_CAPACITY) throw std::runtime_error("internal hash table capacity exceeded");
+    *out = pl.release();
+  });
+}
+
+pg_status pg_placed_destroy(pg_placed* p) {
+  return guarded([&] { if (p) { cudaSetDevice(p->eng->device); delete p; } });
+}
+
+pg_status pg_placed_count(const pg_placed* p, uint64_t* n) {
+  return guarded([&] { require(p && n, "NULL argument"); *n = p->M; });
+}
+
+pg_status pg_placed_kernel_ms(const pg_placed* p, float* ms) {
+  return guarded([&] { require(p && ms, "NULL argument"); *ms = p->kernel_ms; });
+}
+
+pg_status pg_placed_copy(const pg_placed* p, uint32_t* locus, uint32_t* edge, uint32_t* aux, uint8_t* cls,
+                         uint8_t* sig, uint8_t* allele, uint8_t* kind, uint8_t* nature) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    select_device(p->eng);
+    const size_t n = p->M;
+    if (n == 0) return;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+      if (dst) ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, p->eng->st), "copy");
+    };
+    cp(locus, p->locus.p, 4 * n); cp(edge, p->edge.p, 4 * n); cp(aux, p->aux.p, 4 * n);
+    cp(cls, p->cls.p, n); cp(sig, p->sig.p, n); cp(allele, p->allele.p, n); cp(kind, p->kind.p, n);
+    cp(nature, p->nature.p, n);
+    ck(cudaStreamSynchronize(p->eng->st), "copy");
+  });
+}
+
+namespace {
+
+// insert-size CDF table (min insert, thresholds)
+void insert_table(const pg_seq_cfg& c, uint32_t R, uint32_t& ins_min, std::vector<uint32_t>& thr) {
+  const double mean = c.insert_size_mean, sd = c.insert_size_stddev;
+  std::vector<double> w;
+  uint32_t k0 = 0;
+  if (c.insert_model == PG_INSERT_BINOMIAL) {
+    // src/seq_simulation.cpp:431-451: Binomial(t = mean/p, p = 1 - sd^2/mean)
+    const double q = double(c.insert_size_stddev) * double(c.insert_size_stddev) / mean;
+    const double p = 1 - q;
+    if (p < 0) {
+      throw std::runtime_error("The insert size mean (" + std::to_string(c.insert_size_mean) +
+                               ") must be greater than or equal to its variance (" +
+                               std::to_string(c.insert_size_stddev) + "*" + std::to_string(c.insert_size_stddev) +
+                               "=" + std::to_string(c.insert_size_stddev * c.insert_size_stddev) + ").");
+    }
+    require(p > 0, "insert size variance equal to the mean gives an undefined binomial model");
+    const uint32_t t = uint32_t(mean / p);
+    const double lp = std::log(p), lq = q > 0 ? std::log(q) : -INFINITY;
+    std::vector<double> pmf(t + 1);
+    for (uint32_t k = 0; k <= t; ++k) {
+      if (q <= 0) { pmf[k] = (k == t) ? 1.0 : 0.0; continue; }
+      pmf[k] = std::exp(std::lgamma(t + 1.0) - std::lgamma(k + 1.0) - std::lgamma(double(t - k) + 1.0) + k * lp +
+                        double(t - k) * lq);
+    }
+    uint32_t lo = 0, hi = t;
+    double cum = 0;
+    while (lo < t && cum + pmf[lo] < 1e-13) { cum += pmf[lo]; ++lo; }
+    cum = 0;
+    while (hi > lo && cum + pmf[hi] < 1e-13) { cum += pmf[hi]; --hi; }
+    k0 = lo;
+    w.assign(pmf.begin() + lo, pmf.begin() + hi + 1);
+  } else {
+    require(sd > 0, "the normal insert model needs a positive standard deviation");
+    const double a = std::max(1.0, std::floor(mean - 10 * sd)), b = std::ceil(mean + 10 * sd);
+    k0 = uint32_t(a);
+    for (double k = a; k <= b; k += 1) {
+      const double z0 = (k - 0.5 - mean) / (sd * std::sqrt(2.0)), z1 = (k + 0.5 - mean) / (sd * std::sqrt(2.0));
+      w.push_back(0.5 * (std::erfc(z0) - std::erfc(z1)));
+    }
+  }
+  // inserts shorter than a read are clamped to the read size
+  if (k0 < R) {
+    const uint32_t drop = std::min<uint32_t>(R - k0, uint32_t(w.size()) - 1);
+    double mass = 0;
+    for (uint32_t i = 0; i < drop; ++i) mass += w[i];
+    w.erase(w.begin(), w.begin() + drop);
+    w[0] += mass;
+    k0 += drop;
+    if (k0 < R) k0 = R;
+  }
+  ins_min = k0;
+  thr = cdf_thresholds(w);
+}
+
+}  // namespace
+
+pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, pg_seq_result** out) {
+  return guarded([&] {
+    require(pl && c && out, "NULL argument");
+    pg_engine* e = pl->eng;
+    select_device(e);
+    cudaStream_t st = e->st;
+    Pool* P = &e->pool;
+    require(c->coverage >= 0 && std::isfinite(c->coverage), "The coverage must be non-negative");
+    require(c->read_size >= 1 && c->read_size <= 4096, "read_size must be in [1, 4096]");
+    require(c->purity >= 0 && c->purity <= 1, "The purity must be a value in [0,1]");
+    require(c->error_rate >= 0 && c->error_rate <= 1, "The parameter \"error_rate\" must be a positive real number.");
+    const uint32_t R = c->read_size;
+    const bool paired = c->insert_size_mean > 0;
+    uint32_t ins_min = R;
+    std::vector<uint32_t> ins_thr{2147483648u};
+    if (paired) insert_table(*c, R, ins_min, ins_thr);
+    const uint32_t span = std::max<uint32_t>(R, ins_min + uint32_t(ins_thr.size()) - 1);
+    // ---- chromosome selection
+    std::vector<uint32_t> chrs;
+    if (c->n_chr_sel) {
+      require(c->chr_sel != nullptr, "NULL chromosome list");
+      for (uint32_t i = 0; i < c->n_chr_sel; ++i) { require(c->chr_sel[i] < e->n_chr, "unknown chromosome"); chrs.push_back(c->chr_sel[i]); }
+      std::sort(chrs.begin(), chrs.end());
+      chrs.erase(std::unique(chrs.begin(), chrs.end()), chrs.end());
+    } else {
+      for (uint32_t i = 0; i < e->n_chr; ++i) chrs.push_back(i);
+    }
+    // ---- tile size
+    uint32_t T = c->tile_size;
+    if (T == 0) {
+      const double density = double(pl->M) / double(e->G);
+      const double target = 256.0;  // expected records per window
+      double t = density > 0 ? target / density : 65536.0;
+      T = 1024;
+      while (T < 65536 && double(T) * 2 <= t) T <<= 1;
+    }
+    require(T >= 64 && T <= (1u << 24), "tile_size must be in [64, 2^24]");
+    // ---- tiles
+    std::vector<uint32_t> t_start, t_len, t_end, t_slot, t_idx, c_ntiles, c_nstarts, c_id;
+    std::vector<uint64_t> c_pairs;
+    const double mates = paired ? 2.0 : 1.0;
+    uint64_t frags_per_sample = 0;
+    for (uint32_t ci : chrs) {
+      const uint32_t L = e->chr_len[ci];
+      if (L < R) continue;
+      const uint32_t slot = uint32_t(c_id.size());
+      const uint32_t S = L - R + 1;
+      const uint32_t nt = (S + T - 1) / T;
+      const uint64_t pairs = uint64_t(std::floor(c->coverage * double(L) / (double(R) * mates)));
+      c_id.push_back(ci); c_ntiles.push_back(nt); c_nstarts.push_back(S); c_pairs.push_back(pairs);
+      frags_per_sample += pairs;
+      for (uint32_t k = 0; k < nt; ++k) {
+        t_start.push_back(e->chr_off[ci] + k * T);
+        t_len.push_back(std::min<uint32_t>(T, S - k * T));
+        t_end.push_back(e->chr_off[ci] + L);
+        t_slot.push_back(slot);
+        t_idx.push_back(k);
+      }
+    }
+    const uint32_t n_tiles = uint32_t(t_start.size());
+    // ---- samples and Euler numbering of normal cells / preneoplastic edge
+    const uint32_t N = pl->n_nodes;
+    std::vector<pg::SeqSample> samples;
+    std::vector<uint32_t> leaf_tin;
+    if (!c->normal_only) {
+      double nthr = std::floor((1.0 - c->purity) * 4294967296.0);
+      if (nthr > 4294967295.0) nthr = 4294967295.0;
+      for (uint32_t s = 0; s < pl->n_samples; ++s) {
+        require(!pl->leaves[s].empty(), "sample " + std::to_string(s) + " has no sampled cells");
+        pg::SeqSample ss{};
+        ss.n_leaves = uint32_t(pl->leaves[s].size());
+        ss.leaf_off = uint32_t(leaf_tin.size());
+        ss.normal_thr = c->purity >= 1 ? 0u : uint32_t(nthr);
+        ss.all_normal = c->purity <= 0 ? 1u : 0u;
+        leaf_tin.insert(leaf_tin.end(), pl->leaves[s].begin(), pl->leaves[s].end());
+        samples.push_back(ss);
+      }
+    }
+    if (c->normal_only || c->with_normal_sample) {
+      pg::SeqSample ss{};
+      ss.n_leaves = 0; ss.leaf_off = 0; ss.normal_thr = 0; ss.all_normal = 1;
+      samples.push_back(ss);
+    }
+    if (leaf_tin.empty()) leaf_tin.push_back(N);
+    std::vector<uint32_t> etin(N + 2), etout(N + 2);
+    for (uint32_t v = 0; v < N; ++v) { etin[v] = pl->tin[v]; etout[v] = pl->tout[v]; }
+    etin[N] = 0; etout[N] = c->preneoplastic_in_normal ? N + 1 : N;   // preneoplastic edge
+    etin[N + 1] = 0; etout[N + 1] = N + 1;                             // germline
+    // ---- device inputs
+    auto res = std::make_unique<pg_seq_result>();
+    res->eng = e;
+    res->n_samples = uint32_t(samples.size());
+    res->M = pl->M;
+    res->n_reads = frags_per_sample * uint64_t(mates) * samples.size();
+    res->alt = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
+    res->depth = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
+    ck(cudaMemsetAsync(res->alt.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
+    ck(cudaMemsetAsync(res->depth.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
+    if (pl->M == 0 || n_tiles == 0 || samples.empty()) { ck(cudaStreamSynchronize(st), "seq"); *out = res.release(); return; }
+    auto etin_d = upload(P, etin, st), etout_d = upload(P, etout, st);
+    auto ts_d = upload(P, t_start, st), tl_d = upload(P, t_len, st), te_d = upload(P, t_end, st);
+    auto tsl_d = upload(P, t_slot, st), tix_d = upload(P, t_idx, st);
+    auto cnt_d = upload(P, c_ntiles, st), cns_d = upload(P, c_nstarts, st), cid_d = upload(P, c_id, st);
+    auto cp_d = upload(P, c_pairs, st);
+    auto smp_d = upload(P, samples, st);
+    auto leaf_d = upload(P, leaf_tin, st);
+    auto ins_d = upload(P, ins_thr, st);
+    DBuf<pg::SeqRec> recs(P, pl->M);
+    DBuf<uint32_t> pair_cnt(P, uint64_t(n_tiles) * samples.size());
+    pg::seq_build_records(pl->view(), uint32_t(pl->M), etin_d.p, etout_d.p, recs.p, st);
+    pg::seq_tile_counts(uint32_t(samples.size()), n_tiles, tsl_d.p, tix_d.p, cnt_d.p, cns_d.p, cid_d.p, cp_d.p, T,
+                        seed, pair_cnt.p, st);
+    pg::SeqTiles tiles{n_tiles, ts_d.p, tl_d.p, te_d.p, nullptr};
+    pg::SeqParams prm{};
+    prm.read_len = R; prm.paired = paired ? 1u : 0u; prm.span = span;
+    prm.ins_min = ins_min; prm.n_ins = uint32_t(ins_thr.size()); prm.ins_cdf = ins_d.p;
+    double et = std::floor(c->error_rate * 4294967296.0);
+    prm.err_thr = et >= 4294967295.0 ? 0xffffffffu : uint32_t(et);
+    prm.normal_tin = N;
+    prm.n_alleles = 2;
+    Timer timer(st);
+    pg::seq_reads(recs.p, uint32_t(pl->M), tiles, pair_cnt.p, smp_d.p, uint32_t(samples.size()), leaf_d.p, prm, seed,
+                  res->alt.p, res->depth.p, st);
+    res->kernel_ms = timer.stop();
+    ck(cudaGetLastError(), "sequencing kernels");
+    *out = res.release();
+  });
+}
+
+pg_status pg_seq_result_destroy(pg_seq_result* r) {
+  return guarded([&] { if (r) { cudaSetDevice(r->eng->device); delete r; } });
+}
+
+pg_status pg_seq_result_dims(const pg_seq_result* r, uint32_t* n_samples, uint64_t* n_mut, uint64_t* n_reads) {
+  return guarded([&] {
+    require(r != nullptr, "NULL handle");
+    if (n_samples) *n_samples = r->n_samples;
+    if (n_mut) *n_mut = r->M;
+    if (n_reads) *n_reads = r->n_reads;
+  });
+}
+
+pg_status pg_seq_result_copy(const pg_seq_result* r, int32_t* alt, int32_t* depth) {
+  return guarded([&] {
+    require(r != nullptr, "NULL handle");
+    select_device(r->eng);
+    const size_t bytes = sizeof(int32_t) * r->n_samples * r->M;
+    if (bytes == 0) return;
+    if (alt) ck(cudaMemcpyAsync(alt, r->alt.p, bytes, cudaMemcpyDeviceToHost, r->eng->st), "copy alt");
+    if (depth) ck(cudaMemcpyAsync(depth, r->depth.p, bytes, cudaMemcpyDeviceToHost, r->eng->st), "copy depth");
+    ck(cudaStreamSynchronize(r->eng->st), "copy");
+  });
+}
+
+pg_status pg_seq_result_kernel_ms(const pg_seq_result* r, float* ms) {
+  return guarded([&] { require(r && ms, "NULL argument"); *ms = r->kernel_ms; });
+}
+
+}  // extern "C"

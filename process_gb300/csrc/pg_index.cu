@@ -1,0 +1,293 @@
+// Genome storage and the two site indices the placement kernels draw from.
+//
+// Reference behaviour (ProCESS wrapper, RACES internals absent):
+//   * ContextIndex<uint32_t>::build_index(ref, regions_to_avoid, context_sampling)
+//     (src/mutation_engine.cpp:211-275, call :260): positions of the reference
+//     grouped by pyrimidine-centred trinucleotide context, one kept in every
+//     `context_sampling` occurrences (default 100, src/mutations.cpp:945-949).
+//   * RSIndex::build_index(ref, max_motif_size, max_repetition_storage)
+//     (src/mutation_engine.cpp:289-359, call :344): positions of repeated
+//     sequences per ID class, at most `max_repetition_storage` per class.
+//
+// Here both are position lists in HBM, u32 absolute positions sorted
+// ascending within each class, built in two streaming passes over the 2-bit
+// genome: (1) per 1024-base tile, per class counts; (2) after a scan over
+// tiles, every warp walks its tile again and writes the positions whose rank
+// within their class is a multiple of the class stride.  Ranks inside a
+// 32-position step come from __match_any_sync, so the lists are in position
+// order without any sort.
+#include "pg_common.cuh"
+#include "pg_rng.cuh"
+#include "pg_scan.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+constexpr int TILE = 1024;
+constexpr int WIN_BEFORE = 8;
+constexpr int WIN_AFTER = 40;
+constexpr int WIN = TILE + WIN_BEFORE + WIN_AFTER;   // bytes per warp
+constexpr int WARPS = 8;
+
+// ------------------------------------------------------------ genome fill
+__global__ void k_genome_synth(uint32_t* __restrict__ words, uint64_t G, uint64_t nwords,
+                               Key key, uint32_t gc_thr) {
+  const uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= nwords) return;
+  uint32_t out = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const uint64_t blk = w * 4 + q;               // Philox block = 4 bases
+    const U4 r = philox(key.k0, key.k1, uint32_t(blk), uint32_t(blk >> 32), 0u, TAG_GENOME);
+    const uint32_t rw[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint64_t i = blk * 4 + j;
+      if (i < G) {
+        const uint32_t u = rw[j];
+        // GC with probability gc_thr/2^32, then C/G or A/T by the low bit
+        const uint32_t b = (u < gc_thr) ? (1u + (u & 1u)) : ((u & 1u) ? 3u : 0u);
+        out |= b << (2 * (q * 4 + j));
+      }
+    }
+  }
+  words[w] = out;
+}
+
+__global__ void k_genome_pack(uint32_t* __restrict__ words, const uint8_t* __restrict__ codes,
+                              uint64_t G, uint64_t nwords) {
+  const uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= nwords) return;
+  uint32_t out = 0;
+  for (int j = 0; j < 16; ++j) {
+    const uint64_t i = w * 16 + j;
+    if (i < G) out |= uint32_t(codes[i] & 3u) << (2 * j);
+  }
+  words[w] = out;
+}
+
+// ------------------------------------------------------------ class families
+// SBS: one family, the trinucleotide context of p (needs both neighbours in
+// the same chromosome).
+struct SbsFamilies {
+  static constexpr int NF = 1;
+  static constexpr int NC = N_CTX;
+  template <class Get>
+  __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
+    out[0] = -1;
+    if (p <= cs || p + 1 >= ce) return;
+    bool fwd;
+    out[0] = context_of(get(p - 1), get(p), get(p + 1), &fwd);
+  }
+};
+
+// ID83 (COSMIC order).  A position p (the first deleted base, or the base
+// before which bases are inserted; p-1 is the anchor) belongs to at most one
+// class per family:
+//   F0  1-bp deletion at a homopolymer run start, run length 1..6+     (0-11)
+//   F1  1-bp insertion at a run start, run length 1..5+               (12-23, idx 1-5)
+//   F2  1-bp C/G insertion with no adjacent C/G                       (12)
+//   F3  1-bp T/A insertion with no adjacent T/A                       (18)
+//   F4-7  l=2..5 deletion of the unit starting a repeat tract: repeat
+//         count r>=2 -> 24+(l-2)*6+min(r-1,5); r==1 -> microhomology
+//         m = common prefix of the unit and the following l bases:
+//         m==0 -> 24+(l-2)*6, else 72+off(l)+m-1
+//   F8-11 l=2..5 insertion of one more unit at a tract start, r>=1   (48+(l-2)*6+min(r,5))
+//   F12-15 l=2..5 insertion of l random bases at a run start          (48+(l-2)*6)
+struct IdFamilies {
+  static constexpr int NF = 16;
+  static constexpr int NC = N_ID;
+  template <class Get>
+  __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
+#pragma unroll
+    for (int f = 0; f < NF; ++f) out[f] = -1;
+    if (p <= cs || p >= ce) return;
+    const uint32_t b = get(p), prev = get(p - 1);
+    int h = 1;
+    while (h < 6 && get(p + h) == b) ++h;
+    const bool runstart = prev != b;
+    const bool pyrT = (b == 3u || b == 0u);
+    if (runstart) {
+      out[0] = (pyrT ? 6 : 0) + h - 1;
+      out[1] = 12 + (pyrT ? 6 : 0) + (h < 5 ? h : 5);
+#pragma unroll
+      for (int l = 2; l <= 5; ++l) out[12 + l - 2] = 48 + (l - 2) * 6;
+    }
+    if (b != 1u && b != 2u && prev != 1u && prev != 2u) out[2] = 12;
+    if (b != 0u && b != 3u && prev != 0u && prev != 3u) out[3] = 18;
+    const int mh_off[4] = {0, 1, 3, 6};
+#pragma unroll
+    for (int l = 2; l <= 5; ++l) {
+      bool valid = true;
+      for (int i = 0; i < l; ++i) valid = valid && get(p + i) != BASE_INVALID;
+      if (!valid) continue;
+      if (p >= cs + uint32_t(l)) {
+        bool same = true;
+        for (int i = 0; i < l; ++i) same = same && get(p - l + i) == get(p + i);
+        if (same) continue;                       // not the start of the tract
+      }
+      int r = 1;
+      while (r < 6) {
+        bool same = true;
+        for (int i = 0; i < l; ++i) same = same && get(p + r * l + i) == get(p + i);
+        if (!same) break;
+        ++r;
+      }
+      if (r >= 2) {
+        out[4 + l - 2] = 24 + (l - 2) * 6 + (r - 1 < 5 ? r - 1 : 5);
+      } else {
+        int m = 0;
+        while (m < l && get(p + l + m) == get(p + m)) ++m;
+        out[4 + l - 2] = (m == 0) ? 24 + (l - 2) * 6 : 72 + mh_off[l - 2] + m - 1;
+      }
+      out[8 + l - 2] = 48 + (l - 2) * 6 + (r < 5 ? r : 5);
+    }
+  }
+};
+
+// ------------------------------------------------------------ index passes
+struct WarpWindow {
+  uint8_t* s;      // WIN bytes
+  uint32_t start;  // absolute position of s[0]
+};
+
+__device__ __forceinline__ void load_window(const uint32_t* __restrict__ g, uint64_t G, uint32_t tile_start,
+                                            uint8_t* s, int lane) {
+  const int64_t w0 = int64_t(tile_start) - WIN_BEFORE;
+  for (int i = lane; i < WIN; i += 32) {
+    const int64_t q = w0 + i;
+    s[i] = (q >= 0 && uint64_t(q) < G) ? uint8_t(base_at(g, uint32_t(q))) : uint8_t(BASE_INVALID);
+  }
+  __syncwarp();
+}
+
+// mode 0: count; mode 1: emit positions
+template <class F, int MODE>
+__global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__ g, uint64_t G,
+                                                    const uint32_t* __restrict__ chr_off, int n_chr,
+                                                    uint32_t ntiles, uint32_t* __restrict__ cnt,
+                                                    const uint32_t* __restrict__ stride,
+                                                    const uint64_t* __restrict__ list_off,
+                                                    const uint32_t* __restrict__ list_len,
+                                                    uint32_t* __restrict__ lists) {
+  __shared__ uint8_t s_win[WARPS][WIN];
+  __shared__ uint32_t s_run[WARPS][F::NC];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t tile = blockIdx.x * WARPS + warp;
+  if (tile >= ntiles) return;
+  const uint32_t tile_start = tile * TILE;
+  for (int k = lane; k < F::NC; k += 32)
+    s_run[warp][k] = MODE == 0 ? 0u : cnt[uint64_t(k) * ntiles + tile];
+  load_window(g, G, tile_start, s_win[warp], lane);
+  // chromosome of the tile start
+  int c = 0;
+  {
+    int lo = 0, hi = n_chr;            // largest c with chr_off[c] <= tile_start
+    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(chr_off + mid) <= tile_start) lo = mid; else hi = mid; }
+    c = lo;
+  }
+  const uint8_t* s = s_win[warp];
+  for (int step = 0; step < TILE / 32; ++step) {
+    const uint32_t p = tile_start + step * 32 + lane;
+    int cls[F::NF];
+    if (p < G) {
+      while (c + 1 < n_chr && p >= __ldg(chr_off + c + 1)) ++c;
+      const uint32_t cs = __ldg(chr_off + c), ce = __ldg(chr_off + c + 1);
+      auto get = [&](uint32_t q) -> uint32_t {
+        return (q >= cs && q < ce) ? uint32_t(s[q - tile_start + WIN_BEFORE]) : BASE_INVALID;
+      };
+      F::classes(get, p, cs, ce, cls);
+    } else {
+#pragma unroll
+      for (int f = 0; f < F::NF; ++f) cls[f] = -1;
+    }
+#pragma unroll
+    for (int f = 0; f < F::NF; ++f) {
+      const int k = cls[f];
+      const uint32_t peers = __match_any_sync(0xffffffffu, k);
+      if (k >= 0) {
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        const uint32_t leader = __ffs(peers) - 1;
+        if (MODE == 1) {
+          const uint32_t r = s_run[warp][k] + rank;
+          const uint32_t sd = stride[k];
+          if (r % sd == 0) {
+            const uint32_t idx = r / sd;
+            if (idx < list_len[k]) lists[list_off[k] + idx] = p;
+          }
+        }
+        __syncwarp(peers);
+        if (uint32_t(lane) == leader) s_run[warp][k] += __popc(peers);
+      }
+      __syncwarp();
+    }
+  }
+  if (MODE == 0) {
+    for (int k = lane; k < F::NC; k += 32) cnt[uint64_t(k) * ntiles + tile] = s_run[warp][k];
+  }
+}
+
+// ------------------------------------------------------------ host side
+void genome_synth(uint32_t* words, uint64_t G, uint64_t seed, double gc, cudaStream_t st) {
+  const uint64_t nwords = (G + 15) / 16;
+  double t = gc * 4294967296.0;
+  uint32_t thr = t >= 4294967295.0 ? 0xffffffffu : uint32_t(t);
+  k_genome_synth<<<unsigned((nwords + 255) / 256), 256, 0, st>>>(words, G, nwords, make_key(seed), thr); note_launch();
+}
+
+void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t st) {
+  const uint64_t nwords = (G + 15) / 16;
+  k_genome_pack<<<unsigned((nwords + 255) / 256), 256, 0, st>>>(words, codes, G, nwords); note_launch();
+}
+
+uint32_t index_num_tiles(uint64_t G) { return uint32_t((G + TILE - 1) / TILE); }
+
+template <class F>
+static void index_count_t(const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                          uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
+  const uint32_t ntiles = index_num_tiles(G);
+  k_index_pass<F, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles, cnt,
+                                                                  nullptr, nullptr, nullptr, nullptr); note_launch();
+  scan_rows<uint32_t>(cnt, cnt, ntiles, F::NC, part, totals, st);
+}
+
+template <class F>
+static void index_emit_t(const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                         const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
+                         const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
+  const uint32_t ntiles = index_num_tiles(G);
+  k_index_pass<F, 1><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles,
+                                                                  const_cast<uint32_t*>(cnt_scanned),
+                                                                  stride, list_off, list_len, lists); note_launch();
+}
+
+void index_count(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                 uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
+  if (which == 0) index_count_t<SbsFamilies>(g, G, chr_off, n_chr, cnt, part, totals, st);
+  else index_count_t<IdFamilies>(g, G, chr_off, n_chr, cnt, part, totals, st);
+}
+
+void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
+                const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
+  if (which == 0) index_emit_t<SbsFamilies>(g, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+  else index_emit_t<IdFamilies>(g, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+}
+
+int index_num_classes(int which) { return which == 0 ? SbsFamilies::NC : IdFamilies::NC; }
+
+}  // namespace pg
+
+namespace pg {
+
+__global__ void k_gather_bases(const uint32_t* __restrict__ g, const uint32_t* __restrict__ pos, uint64_t n,
+                               uint64_t G, uint8_t* __restrict__ out) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = pos[i] < G ? uint8_t(base_at(g, pos[i])) : uint8_t(BASE_INVALID);
+}
+
+void genome_gather(const uint32_t* g, uint64_t G, const uint32_t* pos, uint64_t n, uint8_t* out, cudaStream_t st) {
+  if (n) { k_gather_bases<<<unsigned((n + 255) / 256), 256, 0, st>>>(g, pos, n, G, out); note_launch(); }
+}
+
+}  // namespace pg

@@ -1,0 +1,138 @@
+// Host-callable launchers of the device kernels and the plain-pointer
+// structures they take.  Everything here is internal to the library; the
+// public boundary is include/process_gb300.h.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pg {
+
+constexpr uint32_t MAX_EPOCHS = 16;
+
+// Counts kernel launches of this library (read with pg_launch_count).
+void note_launch(uint32_t n = 1);
+
+// ---------------------------------------------------------------- index
+void genome_synth(uint32_t* words, uint64_t G, uint64_t seed, double gc, cudaStream_t st);
+void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t st);
+uint32_t index_num_tiles(uint64_t G);
+void genome_gather(const uint32_t* g, uint64_t G, const uint32_t* pos, uint64_t n, uint8_t* out, cudaStream_t st);
+int index_num_classes(int which);  // 0 = SBS contexts (32), 1 = ID classes (83)
+void index_count(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr, uint32_t* cnt,
+                 uint32_t* part, uint32_t* totals, cudaStream_t st);
+void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
+                const uint32_t* list_len, uint32_t* lists, cudaStream_t st);
+
+// ---------------------------------------------------------------- placement
+struct PlaceTables {
+  // forest (device)
+  uint32_t n_nodes;
+  const int32_t* parent;
+  const double* birth;
+  const uint32_t* species;
+  const uint32_t* divisions;
+  // epochs and rates (device); rates are [species][epoch]
+  uint32_t n_epochs;
+  const double* epoch_start;
+  const double* snv_rate;
+  const double* indel_rate;
+  double allelic_size;
+  // signatures: exposure CDFs [(n_epochs+1) rows][n_sigs], class CDFs [n_sigs][classes]
+  uint32_t n_sbs_sigs, n_id_sigs;
+  const uint32_t* sbs_expo_cdf;
+  const uint32_t* sbs_sig_cdf;
+  const uint32_t* id_expo_cdf;
+  const uint32_t* id_sig_cdf;
+  // indices
+  const uint32_t* genome;
+  const uint64_t* ctx_off; const uint32_t* ctx_len; const uint32_t* ctx_lists;
+  const uint64_t* id_off; const uint32_t* id_len; const uint32_t* id_lists;
+};
+
+// SoA of placed mutations (device)
+struct PlaceOut {
+  uint32_t* locus;    // absolute position (SNV) or anchor position (indel)
+  uint32_t* edge;     // node index; n_nodes = preneoplastic edge
+  uint32_t* aux;      // SNV: alt base; indel: descriptor
+  uint8_t* cls;       // SBS96 / ID83 class, 0xff for drivers
+  uint8_t* sig;       // signature index (cause), 0xff for drivers
+  uint8_t* allele;
+  uint8_t* kind;
+  uint8_t* nature;
+  uint32_t* attempt;
+};
+
+struct DriverRec {
+  uint32_t locus, edge, aux, allele;  // allele 0xff = random
+  uint8_t kind, pad[3];
+};
+
+void place_edge_counts(const PlaceTables& t, uint32_t* cnt_snv, uint32_t* cnt_id, uint64_t seed,
+                       uint32_t n_pre_snv, uint32_t n_pre_id, cudaStream_t st);
+void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
+                            const uint32_t* off_id, uint32_t n_snv, uint32_t n_id, const uint32_t* pending,
+                            uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st);
+void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, uint64_t seed,
+                   cudaStream_t st);
+void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st);
+void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
+                 uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
+                 uint32_t* err, cudaStream_t st);
+uint32_t sort_num_buckets(uint64_t G);
+void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,
+                   uint32_t* order, const PlaceOut& sorted, cudaStream_t st);
+
+// ---------------------------------------------------------------- sequencing
+struct SeqRec {            // 16 B, one per placed mutation, sorted by locus
+  uint32_t locus;
+  uint32_t tin, tout;      // Euler interval of the edge that carries it
+  uint32_t info;           // allele | kind << 8
+};
+
+struct SeqTiles {
+  uint32_t n_tiles;        // over all selected chromosomes
+  const uint32_t* start;   // first start position of the tile (absolute)
+  const uint32_t* len;     // number of start positions in the tile
+  const uint32_t* chr_end; // absolute end of the tile's chromosome
+  const uint32_t* tree;    // per tile: (chr slot << 24 | unused) -- see seq_tile_counts
+};
+
+struct SeqSample {
+  uint32_t n_leaves;
+  uint32_t leaf_off;       // into leaf_tin
+  uint32_t normal_thr;     // read from a normal cell iff u < normal_thr
+  uint32_t all_normal;     // the normal sample: every read from a normal cell
+};
+
+struct SeqParams {
+  uint32_t read_len;
+  uint32_t paired;
+  uint32_t span;           // max fragment span past the start (read_len or max insert)
+  uint32_t ins_min, n_ins; // insert size = ins_min + index in the CDF table
+  const uint32_t* ins_cdf;
+  uint32_t err_thr;        // substitution error iff u < err_thr
+  uint32_t normal_tin;     // Euler index of normal cells
+  uint32_t n_alleles;
+};
+
+void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_tin, const uint32_t* edge_tout,
+                       SeqRec* recs, cudaStream_t st);
+// per (sample, tile) pair counts: multinomial split of each chromosome's
+// pair count over its tiles by a binary tree of binomial draws
+void seq_tile_counts(uint32_t n_samples, uint32_t n_tiles, const uint32_t* tile_chr_slot,
+                     const uint32_t* tile_idx_in_chr, const uint32_t* chr_ntiles, const uint32_t* chr_nstarts,
+                     const uint32_t* chr_id, const uint64_t* chr_pairs, uint32_t tile_size, uint64_t seed,
+                     uint32_t* pair_cnt, cudaStream_t st);
+void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
+               const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
+               uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st);
+
+// ---------------------------------------------------------------- calibration
+struct CalibDims {
+  uint32_t K;        // epochs
+  uint32_t J;        // signatures
+  uint32_t C;        // classes
+};
+
+}  // namespace pg

@@ -1,0 +1,357 @@
+// Mutation placement on a samples forest.
+//
+// Reference call site: MutationEngine::place_mutations
+// (src/mutation_engine.cpp:1085-1113) -> RACES
+// MutationEngine<uint32_t, std::mt19937_64>::place_mutations (absent; model
+// restated here and in oracle/).
+//
+// Model (one draw function per decision, all keyed Philox):
+//   * edge v of the forest carries divisions d_v >= 1; division j happens at
+//     t = t_parent + (t_v - t_parent) * (j+1)/d_v (roots: t_v), and belongs to
+//     the exposure epoch whose start time is the last one <= t.
+//   * passenger SNVs (indels) on (v, epoch e):
+//       Poisson(rate[species_v][e] * allelic_size * divisions_in_e)
+//     (per-species passenger rates: src/mutation_engine.cpp:864-1083; timed
+//     exposures: :734-739).  The preneoplastic edge (index N) carries exactly
+//     the requested numbers, drawn from the named signature
+//     (src/mutation_engine.hpp:160-206).
+//   * each mutation draws its signature from the epoch exposure, its class
+//     from the signature, a position uniformly from the class's position list,
+//     and an allele uniformly among the cell's alleles.
+//   * infinite sites (src/mutation_engine.hpp:148-156): loci are unique over
+//     the forest; colliding mutations keep their class and redraw the
+//     position (attempt a uses Philox block 1+a), the lowest slot index wins
+//     a contested locus, rounds repeat until no collision is left.  From
+//     attempt RECLASS_ATTEMPTS on, the class is redrawn too (same signature),
+//     so a class whose positions are all taken cannot stall the rounds.
+#include "pg_common.cuh"
+#include "pg_rng.cuh"
+#include "pg_scan.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+constexpr uint32_t RECLASS_ATTEMPTS = 16;
+
+// ------------------------------------------------------------ per-edge counts
+__global__ void k_edge_counts(PlaceTables t, uint32_t* __restrict__ cnt_snv, uint32_t* __restrict__ cnt_id,
+                              Key key, uint32_t n_pre_snv, uint32_t n_pre_id) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t N = t.n_nodes, E = t.n_epochs;
+  if (v > N) return;
+  if (v == N) {  // preneoplastic edge
+    for (uint32_t e = 0; e < E; ++e) {
+      cnt_snv[uint64_t(v) * E + e] = e == 0 ? n_pre_snv : 0u;
+      cnt_id[uint64_t(v) * E + e] = e == 0 ? n_pre_id : 0u;
+    }
+    return;
+  }
+  const double tv = t.birth[v];
+  const int par = t.parent[v];
+  const double tu = par >= 0 ? t.birth[par] : tv;
+  const uint32_t d = t.divisions[v];
+  const uint32_t sp = t.species[v];
+  uint32_t ndiv[MAX_EPOCHS];
+  for (uint32_t e = 0; e < E; ++e) ndiv[e] = 0;
+  for (uint32_t j = 0; j < d; ++j) {
+    const double tj = tu + (tv - tu) * (double(j + 1) / double(d));
+    uint32_t e = 0;
+    while (e + 1 < E && t.epoch_start[e + 1] <= tj) ++e;
+    ndiv[e] += 1;
+  }
+  for (uint32_t e = 0; e < E; ++e) {
+    const double A = t.allelic_size;
+    const double lam_s = t.snv_rate[sp * E + e] * A * double(ndiv[e]);
+    const double lam_i = t.indel_rate[sp * E + e] * A * double(ndiv[e]);
+    Stream s1{key, e, v, 0u, TAG_EDGE_SNV, 0u};
+    Stream s2{key, e, v, 0u, TAG_EDGE_INDEL, 0u};
+    cnt_snv[uint64_t(v) * E + e] = uint32_t(poisson(s1, lam_s));
+    cnt_id[uint64_t(v) * E + e] = uint32_t(poisson(s2, lam_i));
+  }
+}
+
+// ------------------------------------------------------------ placement
+__device__ __forceinline__ uint32_t find_cell(const uint32_t* __restrict__ off, uint32_t ncell, uint32_t i) {
+  // largest q with off[q] <= i (off is the exclusive scan of the counts)
+  uint32_t lo = 0, hi = ncell;
+  while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (off[mid] <= i) lo = mid; else hi = mid; }
+  return lo;
+}
+
+// Placement of slot i (first placement when redraw==0: class and position;
+// redraw: position only, with attempt+1).  kind 0 = SNV slots [0, n_snv),
+// kind 1 = indel slots [n_snv, n_snv+n_id).
+__global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
+                        const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_id,
+                        const uint32_t* __restrict__ pending, uint32_t n_pending, int redraw,
+                        uint32_t* __restrict__ err) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_pending) return;
+  const uint32_t slot = pending ? pending[tid] : tid;
+  const bool is_id = slot >= n_snv;
+  const uint32_t i = is_id ? slot - n_snv : slot;
+  const uint32_t ncell = (t.n_nodes + 1) * t.n_epochs;
+  const uint32_t* off = is_id ? off_id : off_snv;
+  const uint32_t q = find_cell(off, ncell, i);
+  const uint32_t v = q / t.n_epochs, e = q % t.n_epochs;
+  const uint32_t m = i - off[q];
+  Stream st{key, m, v, e, is_id ? TAG_INDEL : TAG_SNV, 0u};
+  uint32_t cls, sig;
+  if (!redraw) {
+    const U4 r = st.next();
+    const uint32_t row = (v == t.n_nodes) ? t.n_epochs : e;
+    if (!is_id) {
+      sig = cdf_lookup(t.sbs_expo_cdf + row * t.n_sbs_sigs, t.n_sbs_sigs, r.x);
+      cls = cdf_lookup(t.sbs_sig_cdf + sig * N_SBS, N_SBS, r.y);
+    } else {
+      sig = cdf_lookup(t.id_expo_cdf + row * t.n_id_sigs, t.n_id_sigs, r.x);
+      cls = cdf_lookup(t.id_sig_cdf + sig * N_ID, N_ID, r.y);
+    }
+    o.cls[slot] = uint8_t(cls);
+    o.sig[slot] = uint8_t(sig);
+    o.edge[slot] = v;
+    o.nature[slot] = (v == t.n_nodes) ? NATURE_PRENEOPLASTIC : NATURE_PASSENGER;
+    o.kind[slot] = is_id ? KIND_INDEL : KIND_SNV;
+    o.attempt[slot] = 0;
+  } else {
+    cls = o.cls[slot];
+    o.attempt[slot] += 1;
+  }
+  const uint32_t attempt = o.attempt[slot];
+  st.block = 1u + attempt;
+  const U4 r = st.next();
+  if (attempt >= RECLASS_ATTEMPTS) {
+    // the class keeps colliding (its free positions may be exhausted): redraw
+    // the class from the same signature with word w
+    sig = o.sig[slot];
+    cls = is_id ? cdf_lookup(t.id_sig_cdf + sig * N_ID, N_ID, r.w) : cdf_lookup(t.sbs_sig_cdf + sig * N_SBS, N_SBS, r.w);
+    o.cls[slot] = uint8_t(cls);
+  }
+  const uint32_t list = is_id ? cls : uint32_t(sbs_class_context(int(cls)));
+  const uint32_t len = is_id ? t.id_len[list] : t.ctx_len[list];
+  if (len == 0) { atomicOr(err, ERR_EMPTY_CLASS); o.locus[slot] = 0; return; }
+  const uint64_t j = uniform_index64(r.x, r.y, len);
+  const uint32_t p = is_id ? t.id_lists[t.id_off[list] + j] : t.ctx_lists[t.ctx_off[list] + j];
+  o.allele[slot] = uint8_t(uniform_index32(r.z, 2u));
+  if (!is_id) {
+    const uint32_t ref = base_at(t.genome, p);
+    const uint32_t alt_pyr = sbs_class_alt(int(cls));
+    const bool fwd = (ref == 1u || ref == 3u);
+    o.locus[slot] = p;
+    o.aux[slot] = fwd ? alt_pyr : 3u - alt_pyr;
+  } else {
+    // indel descriptor: bit0 insertion, bits1-3 length, bits 8.. inserted bases (2 bits each)
+    uint32_t ins = 0, l = 1, bases = 0;
+    if (cls < 12) { ins = 0; l = 1; }
+    else if (cls < 24) {
+      ins = 1; l = 1;
+      const uint32_t idx = (cls - 12) % 6;
+      if (idx >= 1) bases = base_at(t.genome, p);
+      else bases = (cls < 18) ? ((r.w & 1u) ? 2u : 1u) : ((r.w & 1u) ? 0u : 3u);
+    } else if (cls < 48) { ins = 0; l = (cls - 24) / 6 + 2; }
+    else if (cls < 72) {
+      ins = 1; l = (cls - 48) / 6 + 2;
+      if ((cls - 48) % 6 >= 1) { for (uint32_t k = 0; k < l; ++k) bases |= base_at(t.genome, p + k) << (2 * k); }
+      else bases = r.w & ((1u << (2 * l)) - 1u);
+    } else {
+      ins = 0; l = cls == 72 ? 2 : (cls < 75 ? 3 : (cls < 78 ? 4 : 5));
+    }
+    o.locus[slot] = p - 1;                       // anchor base
+    o.aux[slot] = ins | (l << 1) | (bases << 8);
+  }
+}
+
+// ------------------------------------------------------------ hash sets
+__device__ __forceinline__ uint32_t hash32(uint32_t k) {
+  k ^= k >> 16; k *= 0x7feb352du; k ^= k >> 15; k *= 0x846ca68bu; k ^= k >> 16;
+  return k;
+}
+constexpr uint32_t EMPTY = 0xffffffffu;
+
+__device__ __forceinline__ bool hset_contains(const uint32_t* __restrict__ keys, uint32_t mask, uint32_t k) {
+  uint32_t h = hash32(k) & mask;
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const uint32_t x = keys[h];
+    if (x == k) return true;
+    if (x == EMPTY) return false;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+
+// returns the slot index of key k, inserting it when absent
+__device__ __forceinline__ uint32_t hset_insert(uint32_t* __restrict__ keys, uint32_t mask, uint32_t k) {
+  uint32_t h = hash32(k) & mask;
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const uint32_t prev = atomicCAS(keys + h, EMPTY, k);
+    if (prev == EMPTY || prev == k) return h;
+    h = (h + 1) & mask;
+  }
+  return EMPTY;
+}
+
+__global__ void k_insert_accepted(uint32_t* __restrict__ hkeys, uint32_t hmask, const uint32_t* __restrict__ loci,
+                                  uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) hset_insert(hkeys, hmask, loci[i]);
+}
+
+__global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
+                              const uint32_t* __restrict__ hkeys, uint32_t hmask, uint32_t* __restrict__ ckeys,
+                              uint32_t* __restrict__ cvals, uint32_t cmask, uint8_t* __restrict__ lost,
+                              uint32_t* __restrict__ err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t slot = pending ? pending[i] : i;
+  const uint32_t k = locus[slot];
+  if (hset_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
+  lost[i] = 0;
+  const uint32_t h = hset_insert(ckeys, cmask, k);
+  if (h == EMPTY) { atomicOr(err, ERR_CAPACITY); return; }
+  atomicMin(cvals + h, slot);
+}
+
+__global__ void k_cand_resolve(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
+                               uint32_t* __restrict__ hkeys, uint32_t hmask, const uint32_t* __restrict__ ckeys,
+                               const uint32_t* __restrict__ cvals, uint32_t cmask, const uint8_t* __restrict__ lost,
+                               uint32_t* __restrict__ next, uint32_t* __restrict__ n_next,
+                               uint32_t* __restrict__ err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t slot = pending ? pending[i] : i;
+  const uint32_t k = locus[slot];
+  bool win = false;
+  if (!lost[i]) {
+    uint32_t h = hash32(k) & cmask;
+    for (uint32_t probe = 0; probe <= cmask; ++probe) {
+      const uint32_t x = ckeys[h];
+      if (x == k) { win = cvals[h] == slot; break; }
+      if (x == EMPTY) break;
+      h = (h + 1) & cmask;
+    }
+  }
+  if (win) {
+    if (hset_insert(hkeys, hmask, k) == EMPTY) atomicOr(err, ERR_CAPACITY);
+  } else {
+    next[atomicAdd(n_next, 1u)] = slot;
+  }
+}
+
+// ------------------------------------------------------------ drivers
+// Driver SIDs are applied on the first edge of their mutant; a random allele
+// (RANDOM_ALLELE in src/mutation_engine.cpp:789-848) is drawn per driver.
+__global__ void k_drivers(PlaceOut o, const DriverRec* __restrict__ drv, uint32_t n_drv, uint32_t base_slot, Key key) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_drv) return;
+  const DriverRec d = drv[i];
+  const uint32_t slot = base_slot + i;
+  o.locus[slot] = d.locus;
+  o.edge[slot] = d.edge;
+  o.kind[slot] = d.kind;
+  o.cls[slot] = 0xff;
+  o.sig[slot] = 0xff;
+  o.aux[slot] = d.aux;
+  o.nature[slot] = NATURE_DRIVER;
+  o.attempt[slot] = 0;
+  uint32_t a = d.allele;
+  if (a == 0xffu) {
+    const U4 r = philox(key.k0, key.k1, i, d.edge, 0u, TAG_DRIVER);
+    a = uniform_index32(r.x, 2u);
+  }
+  o.allele[slot] = uint8_t(a);
+}
+
+// ------------------------------------------------------------ locus sort
+constexpr int BUCKET_SHIFT = 10;
+
+__global__ void k_bucket_count(const uint32_t* __restrict__ locus, uint32_t n, uint32_t* __restrict__ bcnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(bcnt + (locus[i] >> BUCKET_SHIFT), 1u);
+}
+__global__ void k_bucket_scatter(const uint32_t* __restrict__ locus, uint32_t n, const uint32_t* __restrict__ boff,
+                                 uint32_t* __restrict__ bfill, uint32_t* __restrict__ order) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t b = locus[i] >> BUCKET_SHIFT;
+  order[boff[b] + atomicAdd(bfill + b, 1u)] = i;
+}
+__global__ void k_bucket_sort(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ boff, uint32_t nb,
+                              uint32_t n, uint32_t* __restrict__ order) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const uint32_t lo = boff[b], hi = (b + 1 < nb) ? boff[b + 1] : n;
+  for (uint32_t i = lo + 1; i < hi; ++i) {
+    const uint32_t x = order[i];
+    const uint64_t kx = (uint64_t(locus[x]) << 32) | x;
+    uint32_t j = i;
+    while (j > lo) {
+      const uint32_t y = order[j - 1];
+      const uint64_t ky = (uint64_t(locus[y]) << 32) | y;
+      if (ky <= kx) break;
+      order[j] = y;
+      --j;
+    }
+    order[j] = x;
+  }
+}
+
+__global__ void k_gather_sorted(PlaceOut o, const uint32_t* __restrict__ order, uint32_t n, PlaceOut s) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t x = order[i];
+  s.locus[i] = o.locus[x]; s.edge[i] = o.edge[x]; s.aux[i] = o.aux[x];
+  s.cls[i] = o.cls[x]; s.sig[i] = o.sig[x]; s.allele[i] = o.allele[x];
+  s.kind[i] = o.kind[x]; s.nature[i] = o.nature[x]; s.attempt[i] = o.attempt[x];
+}
+
+// ------------------------------------------------------------ host launchers
+static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
+
+void place_edge_counts(const PlaceTables& t, uint32_t* cnt_snv, uint32_t* cnt_id, uint64_t seed,
+                       uint32_t n_pre_snv, uint32_t n_pre_id, cudaStream_t st) {
+  k_edge_counts<<<nblk(t.n_nodes + 1, 128), 128, 0, st>>>(t, cnt_snv, cnt_id, make_key(seed), n_pre_snv, n_pre_id); note_launch();
+}
+
+void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
+                            const uint32_t* off_id, uint32_t n_snv, uint32_t n_id, const uint32_t* pending,
+                            uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st) {
+  if (n_pending == 0) return;
+  k_place<<<nblk(n_pending), 256, 0, st>>>(t, o, make_key(seed), off_snv, off_id, n_snv, n_id, pending, n_pending,
+                                           redraw, err); note_launch();
+}
+
+void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, uint64_t seed,
+                   cudaStream_t st) {
+  if (n_drv == 0) return;
+  k_drivers<<<nblk(n_drv), 256, 0, st>>>(o, drv, n_drv, base_slot, make_key(seed)); note_launch();
+}
+
+void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st) {
+  if (n) { k_insert_accepted<<<nblk(n), 256, 0, st>>>(hkeys, hmask, loci, n); note_launch(); }
+}
+
+void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
+                 uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
+                 uint32_t* err, cudaStream_t st) {
+  if (n == 0) return;
+  k_cand_insert<<<nblk(n), 256, 0, st>>>(locus, pending, n, hkeys, hmask, ckeys, cvals, cmask, lost, err); note_launch();
+  k_cand_resolve<<<nblk(n), 256, 0, st>>>(locus, pending, n, hkeys, hmask, ckeys, cvals, cmask, lost, next, n_next,
+                                          err); note_launch();
+}
+
+void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,
+                   uint32_t* order, const PlaceOut& sorted, cudaStream_t st) {
+  const uint32_t nb = uint32_t((G >> BUCKET_SHIFT) + 1);
+  cudaMemsetAsync(bcnt, 0, sizeof(uint32_t) * nb, st);
+  cudaMemsetAsync(bfill, 0, sizeof(uint32_t) * nb, st);
+  if (n == 0) return;
+  k_bucket_count<<<nblk(n), 256, 0, st>>>(o.locus, n, bcnt); note_launch();
+  scan_rows<uint32_t>(bcnt, bcnt, nb, 1, part, nullptr, st);
+  k_bucket_scatter<<<nblk(n), 256, 0, st>>>(o.locus, n, bcnt, bfill, order); note_launch();
+  k_bucket_sort<<<nblk(nb), 256, 0, st>>>(o.locus, bcnt, nb, n, order); note_launch();
+  k_gather_sorted<<<nblk(n), 256, 0, st>>>(o, order, n, sorted); note_launch();
+}
+
+uint32_t sort_num_buckets(uint64_t G) { return uint32_t((G >> BUCKET_SHIFT) + 1); }
+
+}  // namespace pg

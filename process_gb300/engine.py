@@ -1,0 +1,802 @@
+"""Host-side mirror of the ProCESS API for the placement and sequencing path.
+
+Names, arguments, defaults and returned data-frame columns follow the
+reference's Rcpp modules:
+
+* ``MutationEngine`` — ``src/mutations.cpp:392-756`` (methods) and the factory
+  defaults ``:938-951``; ``place_mutations`` overloads
+  ``src/mutation_engine.hpp:160-206``.
+* ``PhylogeneticForest`` getters — ``src/phylogenetic_forest.cpp:57-99, 323-562``.
+* ``simulate_seq`` / ``simulate_normal_seq`` — ``src/sequencing.cpp:193-209, 268-282``
+  and the result flattening of ``src/seq_simulation.cpp:52-181``.
+* ``BasicIlluminaSequencer`` / ``ErrorlessIlluminaSequencer`` —
+  ``src/sequencers.cpp:78-105``.
+
+Data frames are returned as ``dict[str, numpy.ndarray]`` with the reference's
+column names (pandas is not a dependency).  All computation runs in the CUDA
+library through the C-ABI; this module only validates and arranges inputs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+from dataclasses import dataclass, field
+from typing import Iterable, Mapping, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import DomainError, check, lib, ptr
+
+BASES = np.array(list("ACGT"))
+_SUBS = ["C>A", "C>G", "C>T", "T>A", "T>C", "T>G"]
+SBS_CLASSES = [f"{f}[{s}]{t}" for s in _SUBS for f in "ACGT" for t in "ACGT"]
+ID_CLASSES = (
+    [f"1:Del:{b}:{k}" for b in "CT" for k in range(6)]
+    + [f"1:Ins:{b}:{k}" for b in "CT" for k in range(6)]
+    + [f"{ln}:Del:R:{k}" for ln in (2, 3, 4, "5+") for k in range(6)]
+    + [f"{ln}:Ins:R:{k}" for ln in (2, 3, 4, "5+") for k in range(6)]
+    + ["2:Del:M:1", "3:Del:M:1", "3:Del:M:2", "4:Del:M:1", "4:Del:M:2", "4:Del:M:3",
+       "5:Del:M:1", "5:Del:M:2", "5:Del:M:3", "5:Del:M:4", "5:Del:M:5"]
+)
+assert len(SBS_CLASSES) == 96 and len(ID_CLASSES) == 83
+
+NATURES = np.array(["passenger", "driver", "preneoplastic", "germinal"])
+
+
+def _seed(seed) -> int:
+    """Seed semantics of the reference: NULL draws one (src/utility.hpp:41-64)."""
+    if seed is None:
+        return int(np.random.default_rng().integers(0, 2**31 - 1))
+    return int(seed) & 0xFFFFFFFFFFFFFFFF
+
+
+# ---------------------------------------------------------------- genome
+@dataclass
+class GenomeSpec:
+    """Reference genome: chromosome names and lengths plus either explicit base
+    codes (A=0 C=1 G=2 T=3) or a seeded synthetic i.i.d. sequence."""
+
+    chr_names: Sequence[str]
+    chr_lengths: Sequence[int]
+    bases: np.ndarray | None = None
+    seed: int = 0
+    gc: float = 0.5
+
+    @property
+    def total(self) -> int:
+        return int(np.sum(np.asarray(self.chr_lengths, dtype=np.uint64)))
+
+
+# ---------------------------------------------------------------- driver specs
+@dataclass
+class Mutation:
+    """Driver SNV/indel (``Mutation(chr, chr_pos, ref, alt, allele)``, src/mutations.cpp:30-120)."""
+
+    chr: str
+    chr_pos: int
+    ref: str
+    alt: str
+    allele: int | None = None
+
+
+def SNV(chr: str, chr_pos: int, alt: str, ref: str = "?", allele: int | None = None) -> Mutation:
+    """``SNV(chr, chr_pos, alt, ref, allele)``; a "?" ref is read from the genome."""
+    return Mutation(chr, chr_pos, ref, alt, allele)
+
+
+@dataclass
+class CNA:
+    type: str
+    chr: str
+    chr_pos: int
+    len: int
+    allele: int | None = None
+    src_allele: int | None = None
+
+
+class _WGD:
+    def __repr__(self):
+        return "WGD"
+
+
+WGD = _WGD()
+
+
+# ---------------------------------------------------------------- sequencers
+@dataclass
+class ErrorlessIlluminaSequencer:
+    """An error-free Illumina sequencer (src/sequencers.hpp:25-38)."""
+
+    @property
+    def error_rate(self) -> float:
+        return 0.0
+
+
+@dataclass
+class BasicIlluminaSequencer:
+    """Illumina sequencer with a base-, position- and read-independent error
+    rate (src/sequencers.hpp:40-72); validation of src/sequencers.cpp:78-105."""
+
+    error_rate: float
+    random_quality_scores: bool = True
+
+    def __post_init__(self):
+        if not isinstance(self.error_rate, (int, float)) or self.error_rate < 0:
+            raise DomainError(_lib.PG_ERR_DOMAIN, 'The parameter "error_rate" must be a positive real number.')
+        if not isinstance(self.random_quality_scores, bool):
+            raise DomainError(_lib.PG_ERR_DOMAIN, 'The parameter "random_quality_scores" must be a Boolean value.')
+
+
+# ---------------------------------------------------------------- forest
+class SamplesForest:
+    """A samples forest (``DescendantsForest``, node columns of src/forest.hpp:29-68).
+
+    ``divisions`` is the number of cell divisions on the edge into each node
+    (1 for a forest that keeps every division as a node)."""
+
+    def __init__(self, cell_id, ancestor, mutant, epistate, sample, birth_time, divisions=None):
+        cell_id = np.asarray(cell_id, dtype=np.int64)
+        n = len(cell_id)
+        ancestor = np.asarray(ancestor, dtype=np.int64)  # -1 = root (NA)
+        self.mutant = np.asarray(mutant, dtype=object)
+        self.epistate = np.asarray(epistate, dtype=object)
+        sample = np.asarray(sample, dtype=object)
+        self.birth_time = np.asarray(birth_time, dtype=np.float64)
+        self.divisions = (np.ones(n, dtype=np.uint32) if divisions is None
+                          else np.asarray(divisions, dtype=np.uint32))
+        # topological order: parents first
+        pos = {int(c): i for i, c in enumerate(cell_id)}
+        par = np.array([pos.get(int(a), -1) if a >= 0 else -1 for a in ancestor], dtype=np.int64)
+        order, seen = [], np.zeros(n, dtype=bool)
+        kids: dict[int, list[int]] = {}
+        for i, p in enumerate(par):
+            kids.setdefault(int(p), []).append(i)
+        stack = list(reversed(kids.get(-1, [])))
+        while stack:
+            v = stack.pop()
+            if seen[v]:
+                continue
+            seen[v] = True
+            order.append(v)
+            stack.extend(reversed(kids.get(v, [])))
+        if len(order) != n:
+            raise DomainError(_lib.PG_ERR_DOMAIN, "the ancestor relation is not a forest")
+        order = np.asarray(order)
+        inv = np.empty(n, dtype=np.int64)
+        inv[order] = np.arange(n)
+        self.cell_id = cell_id[order]
+        self.parent = np.where(par[order] >= 0, inv[np.maximum(par[order], 0)], -1).astype(np.int32)
+        self.mutant = self.mutant[order]
+        self.epistate = self.epistate[order]
+        self.birth_time = self.birth_time[order]
+        self.divisions = self.divisions[order]
+        sample = sample[order]
+        names = sorted({str(s) for s in sample if s is not None and str(s) != "" and str(s) != "nan"})
+        self.sample_names = list(names)
+        idx = {s: i for i, s in enumerate(names)}
+        self.sample = np.array([idx.get(str(s), -1) if s is not None else -1 for s in sample], dtype=np.int32)
+        is_parent = np.zeros(n, dtype=bool)
+        is_parent[self.parent[self.parent >= 0]] = True
+        self.is_leaf = ~is_parent
+
+    @property
+    def num_of_nodes(self) -> int:
+        return len(self.cell_id)
+
+    def get_nodes(self) -> dict:
+        anc = np.where(self.parent >= 0, self.cell_id[np.maximum(self.parent, 0)], -1)
+        smp = np.array([self.sample_names[s] if s >= 0 else None for s in self.sample], dtype=object)
+        return {"cell_id": self.cell_id.copy(), "ancestor": anc, "mutant": self.mutant.copy(),
+                "epistate": self.epistate.copy(), "sample": smp, "birth_time": self.birth_time.copy()}
+
+    def get_samples_info(self) -> dict:
+        counts = np.bincount(self.sample[self.is_leaf & (self.sample >= 0)], minlength=len(self.sample_names))
+        return {"name": np.array(self.sample_names, dtype=object), "tumour_cells": counts}
+
+
+# ---------------------------------------------------------------- engine
+class MutationEngine:
+    """``MutationEngine`` over a GPU-resident genome and its context / repeat indices.
+
+    The reference downloads a FASTA, signatures and germline data by setup
+    code (src/mutation_engine.cpp:75-185); here the genome, signatures and
+    species are given directly."""
+
+    def __init__(self, genome: GenomeSpec, SBS_signatures: Mapping[str, Sequence[float]] | None = None,
+                 indel_signatures: Mapping[str, Sequence[float]] | None = None, context_sampling: int = 100,
+                 max_motif_size: int = 50, max_repetition_storage: int = 500000,
+                 avoid_homozygous_losses: bool = True):
+        self.genome = genome
+        self.chr_names = [str(c) for c in genome.chr_names]
+        self.chr_lengths = np.asarray(genome.chr_lengths, dtype=np.uint32)
+        self.chr_off = np.concatenate([[0], np.cumsum(self.chr_lengths.astype(np.uint64))]).astype(np.uint64)
+        self.context_sampling = int(context_sampling)
+        self.max_motif_size = int(max_motif_size)
+        self.max_repetition_storage = int(max_repetition_storage)
+        self.avoid_homozygous_losses = bool(avoid_homozygous_losses)
+        d = _lib.GenomeDesc()
+        d.n_chr = len(self.chr_lengths)
+        d.chr_lengths = ptr(self.chr_lengths, C.c_uint32)
+        bases = None
+        if genome.bases is not None:
+            bases = np.ascontiguousarray(genome.bases, dtype=np.uint8)
+            if bases.size != genome.total:
+                raise DomainError(_lib.PG_ERR_DOMAIN, "bases do not match the chromosome lengths")
+            d.bases = ptr(bases, C.c_uint8)
+        d.synthetic_seed = int(genome.seed)
+        d.synthetic_gc = float(genome.gc)
+        d.context_sampling = self.context_sampling
+        d.max_repetition_storage = self.max_repetition_storage
+        h = C.c_void_p()
+        check(lib().pg_engine_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self.sig_names: list[list[str]] = [[], []]
+        self.mutants: list[str] = []
+        self.species: dict[tuple[str, str], int] = {}
+        self.species_rates: dict[tuple[str, str], dict] = {}
+        self._exposures: list[tuple[float, dict]] = []
+        if SBS_signatures:
+            self.set_signatures(0, SBS_signatures)
+        if indel_signatures:
+            self.set_signatures(1, indel_signatures)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._LIB is not None:
+            _lib._LIB.pg_engine_destroy(h)
+            self._h = None
+
+    # -- signatures and exposures ------------------------------------------------
+    def set_signatures(self, type_: int, sigs: Mapping[str, Sequence[float]]) -> None:
+        nc = 96 if type_ == 0 else 83
+        names = list(sigs.keys())
+        mat = np.ascontiguousarray(np.array([np.asarray(sigs[k], dtype=np.float64) for k in names]))
+        if mat.shape != (len(names), nc):
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"signatures must have {nc} classes")
+        check(lib().pg_engine_set_signatures(self._h, type_, len(names), ptr(mat, C.c_double)))
+        self.sig_names[type_] = names
+
+    def add_exposure(self, time: float = 0.0, coefficients: Mapping[str, float] | None = None) -> None:
+        """``add_exposure(time, coefficients)`` (src/mutation_engine.cpp:734-739): one
+        call may set SBS and ID exposures together; names select the type."""
+        if coefficients is None:
+            raise DomainError(_lib.PG_ERR_DOMAIN, "missing exposure coefficients")
+        by_type = [np.zeros(len(self.sig_names[0])), np.zeros(len(self.sig_names[1]))]
+        used = [False, False]
+        for name, c in coefficients.items():
+            if c < 0:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f"{name}: exposure coefficients must be non-negative")
+            for ty in (0, 1):
+                if name in self.sig_names[ty]:
+                    by_type[ty][self.sig_names[ty].index(name)] = c
+                    used[ty] = True
+                    break
+            else:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f"Unknown signature {name}")
+        for ty in (0, 1):
+            if used[ty]:
+                s = by_type[ty].sum()
+                if abs(s - 1.0) > 1e-6:
+                    raise DomainError(_lib.PG_ERR_DOMAIN, "The exposure coefficients must sum up to 1")
+                check(lib().pg_engine_add_exposure(self._h, ty, float(time), ptr(np.ascontiguousarray(by_type[ty]),
+                                                                                    C.c_double)))
+        self._exposures.append((float(time), dict(coefficients)))
+
+    # -- mutants -----------------------------------------------------------------
+    def _species_id(self, mutant: str, epistate: str) -> int:
+        key = (mutant, epistate)
+        if key not in self.species:
+            self.species[key] = len(self.species)
+        return self.species[key]
+
+    def add_mutant(self, mutant_name: str, passenger_rates: Mapping, drivers: Iterable = ()) -> None:
+        """``add_mutant(mutant_name, passenger_rates, drivers)`` (src/mutation_engine.cpp:864-1083).
+
+        ``passenger_rates`` is ``{"SNV": r, "indel": r, "CNA": r}`` or
+        ``{"+": {...}, "-": {...}}``; a rate may be a sequence giving one value
+        per exposure epoch."""
+        if mutant_name in self.mutants:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"mutant {mutant_name} already declared")
+        mut_id = len(self.mutants)
+        self.mutants.append(mutant_name)
+        keys = set(passenger_rates.keys())
+        if keys <= {"SNV", "indel", "CNA"}:
+            per_epi = {"": passenger_rates}
+        elif keys <= {"+", "-"}:
+            per_epi = dict(passenger_rates)
+        else:
+            raise DomainError(_lib.PG_ERR_DOMAIN, "Passenger rates list must be a named list whose names are in "
+                              'the set {"SNV", "indel", "CNA"} or epistates "+"/"-".')
+        for epi, rates in per_epi.items():
+            for k in rates:
+                if k not in ("SNV", "indel", "CNA"):
+                    raise DomainError(_lib.PG_ERR_DOMAIN, f'"{k}" is an unsupported name in passenger rates list.')
+            sid = self._species_id(mutant_name, epi)
+            snv, indel, cna = rates.get("SNV", 0.0), rates.get("indel", 0.0), rates.get("CNA", 0.0)
+            if np.ndim(snv) or np.ndim(indel):
+                n = max(np.size(snv), np.size(indel))
+                s_arr = np.ascontiguousarray(np.broadcast_to(np.asarray(snv, dtype=np.float64), (n,)))
+                i_arr = np.ascontiguousarray(np.broadcast_to(np.asarray(indel, dtype=np.float64), (n,)))
+                check(lib().pg_engine_set_species_epoch_rates(self._h, sid, n, ptr(s_arr, C.c_double),
+                                                              ptr(i_arr, C.c_double)))
+                check(lib().pg_engine_set_species_rates(self._h, sid, float(s_arr[0]), float(i_arr[0]), float(cna)))
+            else:
+                check(lib().pg_engine_set_species_rates(self._h, sid, float(snv), float(indel), float(cna)))
+            check(lib().pg_engine_set_species_mutant(self._h, sid, mut_id))
+            self.species_rates[(mutant_name, epi)] = {"SNV": snv, "indel": indel, "CNA": cna}
+        for d in drivers:
+            if isinstance(d, Mutation):
+                chr_idx = self._chr_index(d.chr)
+                ref = d.ref
+                if ref == "?":
+                    ref = self.get_bases(chr_idx, d.chr_pos, 1)
+                al = -1 if d.allele is None else int(d.allele)
+                check(lib().pg_engine_add_driver_sid(self._h, mut_id, chr_idx, int(d.chr_pos), ref.encode(),
+                                                     d.alt.encode(), al))
+            elif isinstance(d, CNA):
+                al = -1 if d.allele is None else int(d.allele)
+                src = -1 if d.src_allele is None else int(d.src_allele)
+                check(lib().pg_engine_add_driver_cna(self._h, mut_id, 1 if d.type == "A" else 0,
+                                                     self._chr_index(d.chr), int(d.chr_pos), int(d.len), al, src))
+            elif d is WGD:
+                check(lib().pg_engine_add_driver_wgd(self._h, mut_id))
+            else:
+                raise DomainError(_lib.PG_ERR_DOMAIN, "unsupported driver mutation specification")
+
+    def get_species_rates(self) -> dict:
+        rows = list(self.species_rates.items())
+        return {"mutant": np.array([k[0] for k, _ in rows], dtype=object),
+                "epistate": np.array([k[1] for k, _ in rows], dtype=object),
+                "SNV": np.array([np.atleast_1d(v["SNV"])[0] for _, v in rows], dtype=float),
+                "indel": np.array([np.atleast_1d(v["indel"])[0] for _, v in rows], dtype=float),
+                "CNA": np.array([v["CNA"] for _, v in rows], dtype=float)}
+
+    @property
+    def infinite_sites_model(self) -> bool:
+        on = C.c_int(0)
+        check(lib().pg_engine_get_infinite_sites(self._h, C.byref(on)))
+        return bool(on.value)
+
+    @infinite_sites_model.setter
+    def infinite_sites_model(self, value: bool) -> None:
+        check(lib().pg_engine_set_infinite_sites(self._h, 1 if value else 0))
+
+    # -- genome helpers ----------------------------------------------------------------
+    def _chr_index(self, name) -> int:
+        name = str(name)
+        if name not in self.chr_names:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"unknown chromosome {name}")
+        return self.chr_names.index(name)
+
+    def gather_bases(self, positions: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(positions, dtype=np.uint32)
+        out = np.empty(pos.size, dtype=np.uint8)
+        if pos.size:
+            check(lib().pg_engine_gather_bases(self._h, pos.size, ptr(pos, C.c_uint32), ptr(out, C.c_uint8)))
+        return out
+
+    def get_bases(self, chr_idx: int, chr_pos: int, n: int) -> str:
+        start = int(self.chr_off[chr_idx]) + chr_pos - 1
+        return "".join(BASES[self.gather_bases(np.arange(start, start + n, dtype=np.uint32))])
+
+    def read_genome(self, start: int = 0, n: int | None = None) -> np.ndarray:
+        n = self.genome.total - start if n is None else n
+        out = np.empty(n, dtype=np.uint8)
+        check(lib().pg_engine_read_genome(self._h, start, n, ptr(out, C.c_uint8)))
+        return out
+
+    def index_info(self) -> dict:
+        G = C.c_uint64()
+        ct, it = np.zeros(32, np.uint64), np.zeros(83, np.uint64)
+        cs, is_ = np.zeros(32, np.uint32), np.zeros(83, np.uint32)
+        check(lib().pg_engine_genome_info(self._h, C.byref(G), ptr(ct, C.c_uint64), ptr(it, C.c_uint64),
+                                          ptr(cs, C.c_uint32), ptr(is_, C.c_uint32)))
+        return {"length": G.value, "ctx_total": ct, "id_total": it, "ctx_stored": cs, "id_stored": is_}
+
+    def read_index(self, which: int, cls: int) -> np.ndarray:
+        n = C.c_uint32()
+        check(lib().pg_engine_read_index(self._h, which, cls, None, 0, C.byref(n)))
+        out = np.empty(n.value, dtype=np.uint32)
+        check(lib().pg_engine_read_index(self._h, which, cls, ptr(out, C.c_uint32), n.value, C.byref(n)))
+        return out
+
+    def get_genome_info(self) -> dict:
+        return {"chr": np.array(self.chr_names, dtype=object), "length": self.chr_lengths.astype(np.int64)}
+
+    # -- placement ------------------------------------------------------------------
+    def forest_species(self, forest: SamplesForest) -> np.ndarray:
+        out = np.empty(forest.num_of_nodes, dtype=np.uint32)
+        for i, (m, e) in enumerate(zip(forest.mutant, forest.epistate)):
+            key = (str(m), "" if e is None else str(e))
+            if key not in self.species:
+                key2 = (str(m), "")
+                if key2 not in self.species:
+                    raise DomainError(_lib.PG_ERR_DOMAIN, f'unknown species "{m}{e}": add its mutant first')
+                key = key2
+            out[i] = self.species[key]
+        return out
+
+    def place_mutations(self, samples_forest: SamplesForest, num_of_preneoplatic_SNVs: int = 0,
+                        num_of_preneoplatic_indels: int = 0, seed=None,
+                        preneoplatic_SNV_signature_name: str = "SBS1",
+                        preneoplatic_indel_signature_name: str = "ID1") -> "PhylogeneticForest":
+        """``place_mutations(samples_forest, #preneoplastic SNVs, #preneoplastic indels, seed)``."""
+        f = samples_forest
+        species = self.forest_species(f)
+
+        def sig_index(ty, name, count):
+            if count == 0:
+                return 0
+            if name not in self.sig_names[ty]:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f"Unknown signature {name}")
+            return self.sig_names[ty].index(name)
+
+        pre_s = sig_index(0, preneoplatic_SNV_signature_name, num_of_preneoplatic_SNVs)
+        pre_i = sig_index(1, preneoplatic_indel_signature_name, num_of_preneoplatic_indels)
+        fh = C.c_void_p()
+        parent = np.ascontiguousarray(f.parent, dtype=np.int32)
+        birth = np.ascontiguousarray(f.birth_time, dtype=np.float64)
+        sample = np.ascontiguousarray(np.where(f.is_leaf, f.sample, -1), dtype=np.int32)
+        div = np.ascontiguousarray(f.divisions, dtype=np.uint32)
+        check(lib().pg_forest_create(f.num_of_nodes, ptr(parent, C.c_int32), ptr(birth, C.c_double),
+                                     ptr(species, C.c_uint32), ptr(sample, C.c_int32), ptr(div, C.c_uint32),
+                                     len(f.sample_names), C.byref(fh)))
+        try:
+            ph = C.c_void_p()
+            s = _seed(seed)
+            check(lib().pg_place_mutations(self._h, fh, int(num_of_preneoplatic_SNVs), pre_s,
+                                           int(num_of_preneoplatic_indels), pre_i, s, C.byref(ph)))
+        finally:
+            lib().pg_forest_destroy(fh)
+        return PhylogeneticForest(self, f, ph, s)
+
+
+class PhylogeneticForest:
+    """Placement result: the samples forest plus the placed mutations (kept in
+    HBM, sorted by locus) and the getters of src/phylogenetic_forest.cpp."""
+
+    def __init__(self, engine: MutationEngine, forest: SamplesForest, handle: C.c_void_p, seed: int):
+        self.engine = engine
+        self.forest = forest
+        self._h = handle
+        self.seed = seed
+        self._table = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._LIB is not None:
+            _lib._LIB.pg_placed_destroy(h)
+            self._h = None
+
+    @property
+    def num_of_mutations(self) -> int:
+        n = C.c_uint64()
+        check(lib().pg_placed_count(self._h, C.byref(n)))
+        return n.value
+
+    def kernel_ms(self) -> float:
+        v = C.c_float()
+        check(lib().pg_placed_kernel_ms(self._h, C.byref(v)))
+        return v.value
+
+    def table(self) -> dict:
+        """Placed mutations as arrays (sorted by absolute locus)."""
+        if self._table is None:
+            n = self.num_of_mutations
+            t = {k: np.empty(n, dtype=np.uint32) for k in ("locus", "edge", "aux")}
+            t.update({k: np.empty(n, dtype=np.uint8) for k in ("cls", "sig", "allele", "kind", "nature")})
+            check(lib().pg_placed_copy(self._h, *(ptr(t[k], C.c_uint32) for k in ("locus", "edge", "aux")),
+                                       *(ptr(t[k], C.c_uint8) for k in ("cls", "sig", "allele", "kind", "nature"))))
+            self._table = t
+        return self._table
+
+    # -- reference-facing getters ------------------------------------------------------
+    def get_nodes(self) -> dict:
+        return self.forest.get_nodes()
+
+    def _ref_alt(self, t: dict) -> tuple[np.ndarray, np.ndarray]:
+        eng = self.engine
+        n = len(t["locus"])
+        kind, aux, locus = t["kind"], t["aux"], t["locus"].astype(np.int64)
+        ref = np.empty(n, dtype=object)
+        alt = np.empty(n, dtype=object)
+        snv = kind == 0
+        rb = eng.gather_bases(locus[snv])
+        ref[snv] = BASES[np.minimum(rb, 3)]
+        alt[snv] = BASES[aux[snv] & 3]
+        for i in np.nonzero(~snv)[0]:
+            a = int(aux[i])
+            ins, ln, bases = a & 1, (a >> 1) & 7, a >> 8
+            anchor = int(locus[i])
+            if ins:
+                r = "".join(BASES[eng.gather_bases(np.array([anchor], dtype=np.uint32))])
+                alt[i] = r + "".join(BASES[(bases >> (2 * k)) & 3] for k in range(ln))
+                ref[i] = r
+            else:
+                r = "".join(BASES[eng.gather_bases(np.arange(anchor, anchor + ln + 1, dtype=np.uint32))])
+                ref[i], alt[i] = r, r[0]
+        return ref, alt
+
+    def _cause(self, t: dict) -> np.ndarray:
+        out = np.empty(len(t["sig"]), dtype=object)
+        for i, (s, k, nat) in enumerate(zip(t["sig"], t["kind"], t["nature"])):
+            names = self.engine.sig_names[int(k)]
+            out[i] = names[s] if s != 0xFF and s < len(names) else None
+        return out
+
+    def _chr_pos(self, locus: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        off = self.engine.chr_off
+        ci = np.searchsorted(off, locus.astype(np.uint64), side="right") - 1
+        names = np.array(self.engine.chr_names, dtype=object)[ci]
+        return names, (locus.astype(np.int64) - off[ci].astype(np.int64) + 1)
+
+    def leaf_carriers(self, leaf: int) -> np.ndarray:
+        """Mask of the placed mutations carried by node ``leaf``."""
+        f = self.forest
+        path = set()
+        v = int(leaf)
+        while v >= 0:
+            path.add(v)
+            v = int(f.parent[v])
+        t = self.table()
+        e = t["edge"]
+        return np.isin(e, np.fromiter(path, dtype=np.int64)) | (e == f.num_of_nodes)
+
+    def get_sampled_cell_mutations(self, cell_id=None) -> dict:
+        """Columns cell_id, chr, chr_pos, allele, ref, alt, type, cause, class
+        (src/phylogenetic_forest.cpp:452-507)."""
+        f = self.forest
+        t = self.table()
+        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
+        if cell_id is not None:
+            hit = np.nonzero(f.cell_id == int(cell_id))[0]
+            if len(hit) == 0 or not f.is_leaf[hit[0]]:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f'Cell "{cell_id}" is not a leaf')
+            leaves = hit
+        ref, alt = self._ref_alt(t)
+        cause = self._cause(t)
+        chrn, pos = self._chr_pos(t["locus"])
+        cols = {k: [] for k in ("cell_id", "chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
+        for lf in leaves:
+            m = self.leaf_carriers(lf)
+            cols["cell_id"].append(np.full(m.sum(), f.cell_id[lf]))
+            cols["chr"].append(chrn[m]); cols["chr_pos"].append(pos[m]); cols["allele"].append(t["allele"][m])
+            cols["ref"].append(ref[m]); cols["alt"].append(alt[m])
+            cols["type"].append(np.where(t["kind"][m] == 0, "SNV", "indel"))
+            cols["cause"].append(cause[m]); cols["class"].append(NATURES[t["nature"][m]])
+        return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
+
+    def get_samples_info(self) -> dict:
+        """name, tumour_cells, DNA_quantity, equivalent_normal_cells (src/phylogenetic_forest.cpp:57-99)."""
+        info = self.forest.get_samples_info()
+        normal_dna = 2.0 * self.engine.genome.total
+        dna = info["tumour_cells"].astype(np.float64) * normal_dna
+        info["DNA_quantity"] = dna
+        info["equivalent_normal_cells"] = dna / normal_dna
+        return info
+
+    def get_germline_mutations(self) -> dict:
+        return {k: np.array([]) for k in ("chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
+
+
+# ---------------------------------------------------------------- sequencing
+class SeqResult:
+    """Raw sequencing counts kept on the device until read."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._LIB is not None:
+            _lib._LIB.pg_seq_result_destroy(h)
+            self._h = None
+
+    def dims(self) -> tuple[int, int, int]:
+        s, m, r = C.c_uint32(), C.c_uint64(), C.c_uint64()
+        check(lib().pg_seq_result_dims(self._h, C.byref(s), C.byref(m), C.byref(r)))
+        return s.value, m.value, r.value
+
+    def counts(self) -> tuple[np.ndarray, np.ndarray]:
+        s, m, _ = self.dims()
+        alt = np.empty((s, m), dtype=np.int32)
+        dep = np.empty((s, m), dtype=np.int32)
+        check(lib().pg_seq_result_copy(self._h, ptr(alt, C.c_int32), ptr(dep, C.c_int32)))
+        return alt, dep
+
+    def kernel_ms(self) -> float:
+        v = C.c_float()
+        check(lib().pg_seq_result_kernel_ms(self._h, C.byref(v)))
+        return v.value
+
+
+INSERT_MODELS = {"binomial": 0, "normal": 1}
+
+
+def seq_cfg(coverage=10, read_size=150, insert_size_mean=0, insert_size_stddev=10, error_rate=0.0, purity=1.0,
+            with_normal_sample=True, preneoplastic_in_normal=False, normal_only=False, chromosomes=None,
+            tile_size=0, insert_model="binomial", chr_index=None) -> tuple[_lib.SeqCfg, np.ndarray | None]:
+    c = _lib.SeqCfg()
+    c.coverage = float(coverage)
+    c.read_size = int(read_size)
+    c.insert_size_mean = int(insert_size_mean)
+    c.insert_size_stddev = int(insert_size_stddev)
+    c.insert_model = INSERT_MODELS[insert_model]
+    c.error_rate = float(error_rate)
+    c.purity = float(purity)
+    c.with_normal_sample = int(bool(with_normal_sample))
+    c.preneoplastic_in_normal = int(bool(preneoplastic_in_normal))
+    c.normal_only = int(bool(normal_only))
+    c.tile_size = int(tile_size)
+    sel = None
+    if chromosomes is not None:
+        sel = np.ascontiguousarray([chr_index(x) for x in chromosomes], dtype=np.uint32)
+        c.n_chr_sel = len(sel)
+        c.chr_sel = ptr(sel, C.c_uint32)
+    return c, sel
+
+
+def sequence_counts(phylo_forest: PhylogeneticForest, seed: int, **cfg) -> SeqResult:
+    """Runs the read simulator and returns the device-resident counts."""
+    c, _sel = seq_cfg(chr_index=phylo_forest.engine._chr_index, **cfg)
+    h = C.c_void_p()
+    check(lib().pg_simulate_seq(phylo_forest._h, C.byref(c), int(seed), C.byref(h)))
+    return SeqResult(h)
+
+
+def _sequencer_rate(sequencer) -> tuple[float, dict | None]:
+    if sequencer is None:
+        return 0.0, None
+    if isinstance(sequencer, ErrorlessIlluminaSequencer):
+        return 0.0, {"name": "ErrorlessIlluminaSequencer", "error_rate": 0.0}
+    if isinstance(sequencer, BasicIlluminaSequencer):
+        return float(sequencer.error_rate), {"name": "BasicIlluminaSequencer", "error_rate": sequencer.error_rate,
+                                             "random_quality_scores": sequencer.random_quality_scores}
+    raise DomainError(_lib.PG_ERR_DOMAIN, "Unsupported sequencer type")
+
+
+def _result_frame(pf: PhylogeneticForest, alt: np.ndarray, dep: np.ndarray, sample_names: list[str],
+                  include_non_sequenced: bool, present: np.ndarray) -> dict:
+    """The wide data frame of get_result_dataframe (src/seq_simulation.cpp:142-181):
+    rows = mutations observed in some sample (or present, with
+    include_non_sequenced_mutations), merged by (chr, pos, ref, alt)."""
+    t = pf.table()
+    ref, altb = pf._ref_alt(t)
+    cause = pf._cause(t)
+    keep = (alt.sum(axis=0) > 0) | (include_non_sequenced & present)
+    idx = np.nonzero(keep)[0]
+    chrn, pos = pf._chr_pos(t["locus"][idx])
+    # merge records that are the same SID (chr, pos, ref, alt): occurrences add, causes/classes union
+    keys = {}
+    order = []
+    for j, i in enumerate(idx):
+        k = (int(t["locus"][i]), ref[i], altb[i])
+        if k in keys:
+            keys[k].append(i)
+        else:
+            keys[k] = [i]
+            order.append(k)
+    rows = [keys[k] for k in order]
+    first = np.array([r[0] for r in rows], dtype=np.int64)
+    df = {
+        "chr": chrn[np.searchsorted(idx, first)] if len(first) else np.array([], dtype=object),
+        "chr_pos": pos[np.searchsorted(idx, first)] if len(first) else np.array([], dtype=np.int64),
+        "ref": ref[first] if len(first) else np.array([], dtype=object),
+        "alt": altb[first] if len(first) else np.array([], dtype=object),
+        "causes": np.array([";".join(sorted({c for c in cause[r] if c is not None})) or None for r in rows],
+                           dtype=object),
+        "classes": np.array([";".join(sorted(set(NATURES[t["nature"][r]]))) for r in rows], dtype=object),
+    }
+    for s, name in enumerate(sample_names):
+        occ = np.array([alt[s, r].sum() for r in rows], dtype=np.int32)
+        cov = dep[s, first].astype(np.int32) if len(first) else np.array([], dtype=np.int32)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            vaf = np.where(cov > 0, occ / np.maximum(cov, 1), 0.0)
+        df[f"{name}.occurrences"] = occ
+        df[f"{name}.coverage"] = cov
+        df[f"{name}.VAF"] = vaf
+    return df
+
+
+def _presence(pf: PhylogeneticForest, n_samples_seq: int, with_normal: bool, pre_in_normal: bool) -> np.ndarray:
+    """Mutations present in the cells of some sequenced sample."""
+    f = pf.forest
+    t = pf.table()
+    n = f.num_of_nodes
+    # Euler intervals
+    kids = [[] for _ in range(n)]
+    roots = []
+    for v in range(n):
+        (roots if f.parent[v] < 0 else kids[f.parent[v]]).append(v)
+    tin, tout = np.zeros(n, np.int64), np.zeros(n, np.int64)
+    clock = 0
+    for r in roots:
+        stack = [(r, 0)]
+        tin[r] = clock; clock += 1
+        while stack:
+            v, k = stack[-1]
+            if k < len(kids[v]):
+                stack[-1] = (v, k + 1)
+                c = kids[v][k]
+                tin[c] = clock; clock += 1
+                stack.append((c, 0))
+            else:
+                tout[v] = clock
+                stack.pop()
+    leaf_tins = np.sort(tin[f.is_leaf & (f.sample >= 0)])
+    e = t["edge"].astype(np.int64)
+    real = e < n
+    present = np.zeros(len(e), dtype=bool)
+    lo = np.searchsorted(leaf_tins, tin[np.minimum(e, n - 1)], side="left")
+    hi = np.searchsorted(leaf_tins, tout[np.minimum(e, n - 1)], side="left")
+    present[real] = (hi > lo)[real]
+    present[~real] = True
+    return present
+
+
+def simulate_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_genome=None, chromosomes=None,
+                 coverage: float = 10, read_size: int = 150, insert_size_mean: int = 0, insert_size_stddev: int = 10,
+                 output_dir: str = "ProCESS_SAM", write_SAM: bool = False, update_SAM: bool = False,
+                 cell_labelling=None, purity: float = 1, with_normal_sample: bool = True,
+                 preneoplastic_in_normal: bool = False, filename_prefix: str = "chr_",
+                 template_name_prefix: str = "r", include_non_sequenced_mutations: bool = False, seed=None,
+                 insert_model: str = "binomial", tile_size: int = 0) -> dict:
+    """``simulate_seq`` (src/sequencing.cpp:193-209).  Returns
+    ``{"mutations": data frame, "parameters": dict}``.  ``insert_model``
+    "normal" adds a discretised normal insert size next to the reference's
+    binomial model."""
+    if write_SAM:
+        raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "SAM output is not built in this version")
+    if cell_labelling is not None:
+        raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "cell_labelling (FACS) is not built in this version")
+    err, seq_data = _sequencer_rate(sequencer)
+    s = _seed(seed)
+    res = sequence_counts(phylo_forest, s, coverage=coverage, read_size=read_size,
+                          insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
+                          purity=purity, with_normal_sample=with_normal_sample,
+                          preneoplastic_in_normal=preneoplastic_in_normal, chromosomes=chromosomes,
+                          tile_size=tile_size, insert_model=insert_model)
+    alt, dep = res.counts()
+    names = list(phylo_forest.forest.sample_names) + (["normal_sample"] if with_normal_sample else [])
+    present = _presence(phylo_forest, len(names), with_normal_sample, preneoplastic_in_normal)
+    df = _result_frame(phylo_forest, alt, dep, names, include_non_sequenced_mutations, present)
+    params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
+              "coverage": coverage, "read_size": read_size, "insert_size_mean": insert_size_mean,
+              "insert_size_stddev": insert_size_stddev, "output_dir": output_dir, "write_SAM": write_SAM,
+              "update_SAM": update_SAM, "cell_labelling": cell_labelling, "purity": purity,
+              "with_normal_sample": with_normal_sample, "filename_prefix": filename_prefix,
+              "template_name_prefix": template_name_prefix,
+              "include_non_sequenced_mutations": include_non_sequenced_mutations, "seed": s}
+    return {"mutations": df, "parameters": params}
+
+
+def simulate_normal_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_genome=None, chromosomes=None,
+                        coverage: float = 10, read_size: int = 150, insert_size_mean: int = 0,
+                        insert_size_stddev: int = 10, output_dir: str = "ProCESS_normal_SAM",
+                        write_SAM: bool = True, update_SAM: bool = False, with_preneoplastic: bool = False,
+                        filename_prefix: str = "chr_", template_name_prefix: str = "r",
+                        include_non_sequenced_mutations: bool = False, seed=None,
+                        insert_model: str = "binomial", tile_size: int = 0) -> dict:
+    """``simulate_normal_seq`` (src/sequencing.cpp:268-282); ``write_SAM`` must be
+    FALSE in this version (its reference default is TRUE)."""
+    if write_SAM:
+        raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "SAM output is not built in this version; "
+                                    "call with write_SAM=False")
+    err, seq_data = _sequencer_rate(sequencer)
+    s = _seed(seed)
+    res = sequence_counts(phylo_forest, s, coverage=coverage, read_size=read_size,
+                          insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
+                          purity=1.0, with_normal_sample=True, preneoplastic_in_normal=with_preneoplastic,
+                          normal_only=True, chromosomes=chromosomes, tile_size=tile_size, insert_model=insert_model)
+    alt, dep = res.counts()
+    t = phylo_forest.table()
+    present = (t["edge"] == phylo_forest.forest.num_of_nodes) & bool(with_preneoplastic)
+    df = _result_frame(phylo_forest, alt, dep, ["normal_sample"], include_non_sequenced_mutations, present)
+    params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
+              "coverage": coverage, "read_size": read_size, "insert_size_mean": insert_size_mean,
+              "insert_size_stddev": insert_size_stddev, "output_dir": output_dir, "write_SAM": write_SAM,
+              "update_SAM": update_SAM, "with_preneoplastic": with_preneoplastic,
+              "filename_prefix": filename_prefix, "template_name_prefix": template_name_prefix,
+              "include_non_sequenced_mutations": include_non_sequenced_mutations, "seed": s}
+    return {"mutations": df, "parameters": params}

@@ -1,0 +1,227 @@
+"""GPU parity: the CUDA path against the oracle.
+
+* bit-exact (integers) against the Philox replay: genome, index lists,
+  placed mutations (locus, edge, class, signature, allele, alt/indel
+  descriptor, nature) and sequencing alt/depth tables;
+* in distribution against the std::mt19937_64 reference-engine flavour over
+  64 seeds (chi-square on contexts, KS on per-edge counts and on VAF), p > 0.01;
+* edge cases of the reference API.
+"""
+import numpy as np
+import pytest
+from scipy import stats
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(orc, w, **kw):
+    from process_gb300 import synth
+    eng = synth.build_engine(w)
+    o = orc.OracleEngine.like(w, **kw) if kw else orc.OracleEngine.like(w)
+    return eng, o
+
+
+def oracle_species(e, forest):
+    return np.array([e.species[(m, ep)] for m, ep in zip(forest.mutant, forest.epistate)], dtype=np.uint32)
+
+
+def assert_tables_equal(a, b):
+    assert len(a["locus"]) == len(b["locus"])
+    for k in ("locus", "edge", "aux", "cls", "sig", "allele", "kind", "nature"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_genome_and_index_bit_exact(gpu_lib, orc):
+    from process_gb300 import GenomeSpec, MutationEngine
+    g = GenomeSpec(["1", "2", "3", "4"], [70_001, 1_000, 333_333, 5], seed=77, gc=0.41)
+    for cs, cap in ((1, 500000), (7, 300)):
+        eng = MutationEngine(g, context_sampling=cs, max_repetition_storage=cap)
+        o = orc.OracleEngine(g.chr_lengths, None, g.seed, g.gc, context_sampling=cs, max_rep=cap)
+        np.testing.assert_array_equal(eng.read_genome(), o.read_genome())
+        gi, oi = eng.index_info(), o.index_info()
+        np.testing.assert_array_equal(gi["ctx_total"], oi["ctx_total"])
+        np.testing.assert_array_equal(gi["id_total"], oi["id_total"])
+        np.testing.assert_array_equal(gi["ctx_stored"], oi["ctx_stored"])
+        np.testing.assert_array_equal(gi["id_stored"], oi["id_stored"])
+        for c in range(32):
+            np.testing.assert_array_equal(eng.read_index(0, c), o.read_index(0, c))
+        for c in range(83):
+            np.testing.assert_array_equal(eng.read_index(1, c), o.read_index(1, c))
+
+
+def test_explicit_bases_genome(gpu_lib, orc):
+    from process_gb300 import GenomeSpec, MutationEngine
+    rng = np.random.default_rng(5)
+    bases = rng.integers(0, 4, 50_000).astype(np.uint8)
+    bases[1000:1040] = 1            # a long homopolymer run
+    bases[2000:2030] = np.tile([0, 3], 15)   # a dinucleotide repeat
+    g = GenomeSpec(["a", "b"], [20_000, 30_000], bases=bases)
+    eng = MutationEngine(g, context_sampling=1, max_repetition_storage=1000)
+    o = orc.OracleEngine(g.chr_lengths, bases, context_sampling=1, max_rep=1000)
+    np.testing.assert_array_equal(eng.read_genome(), bases)
+    for c in range(83):
+        np.testing.assert_array_equal(eng.read_index(1, c), o.read_index(1, c))
+
+
+@pytest.mark.parametrize("infinite", [True, False])
+def test_placement_bit_exact_config1(gpu_lib, orc, infinite):
+    from process_gb300 import synth
+    w = synth.config1(seed=3, n_leaves=800)
+    eng, o = make_pair(orc, w)
+    eng.infinite_sites_model = infinite
+    o.set_infinite_sites(infinite)
+    for seed in (1, 2, 12345678901):
+        pf = eng.place_mutations(w.forest, 100, 10, seed=seed)
+        ot = o.place(w.forest, oracle_species(o, w.forest), 100, 0, 10, 0, seed=seed).table()
+        assert_tables_equal(pf.table(), ot)
+
+
+def test_placement_bit_exact_epochs_drivers(gpu_lib, orc):
+    """Three exposure epochs with per-epoch rates, compressed edges and drivers."""
+    from process_gb300 import SNV, Mutation, synth
+    w = synth.config2(seed=4, n_leaves_per_sample=300, genome_scale=2e-3)
+    w.mutants = [("A", w.mutants[0][1], []),
+                 ("B", w.mutants[1][1], [SNV("1", 1000, "T", allele=1), Mutation("2", 500, "A", "ACG"),
+                                         SNV("3", 77, "G")])]
+    eng, o = make_pair(orc, w)
+    # the oracle gets the same drivers with the reference base read from the genome
+    g = o.read_genome()
+    off = np.concatenate([[0], np.cumsum(np.asarray(w.genome.chr_lengths, dtype=np.int64))])
+    o.add_driver_sid(1, 0, 1000, "ACGT"[g[off[0] + 999]], "T", 1)
+    o.add_driver_sid(1, 1, 500, "A", "ACG", -1)
+    o.add_driver_sid(1, 2, 77, "ACGT"[g[off[2] + 76]], "G", -1)
+    for seed in (5, 6):
+        pf = eng.place_mutations(w.forest, 1000, 100, seed=seed)
+        ot = o.place(w.forest, oracle_species(o, w.forest), 1000, 0, 100, 0, seed=seed).table()
+        t = pf.table()
+        assert_tables_equal(t, ot)
+        assert (t["nature"] == 1).sum() == 3
+        assert len(np.unique(t["locus"])) == len(t["locus"])
+
+
+SEQ_CASES = [
+    dict(coverage=30, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3, purity=0.7),
+    dict(coverage=20, read_size=100, insert_size_mean=350, insert_size_stddev=30, insert_model="normal",
+         error_rate=0.0, purity=1.0, preneoplastic_in_normal=True),
+    dict(coverage=25, read_size=150, insert_size_mean=0, error_rate=5e-2, purity=0.5, with_normal_sample=False),
+    dict(coverage=15, read_size=150, insert_size_mean=300, insert_size_stddev=5, error_rate=1e-3, purity=0.0,
+         chromosomes=["3", "1"]),
+    dict(coverage=40, read_size=150, insert_size_mean=250, insert_size_stddev=15, error_rate=1e-2,
+         normal_only=True, preneoplastic_in_normal=True),
+]
+
+
+@pytest.mark.parametrize("case", range(len(SEQ_CASES)))
+def test_sequencing_bit_exact(gpu_lib, orc, case):
+    from process_gb300 import synth
+    from process_gb300.engine import seq_cfg, sequence_counts
+    cfg = dict(SEQ_CASES[case])
+    w = synth.config1(seed=8, n_leaves=400)
+    eng, o = make_pair(orc, w)
+    pf = eng.place_mutations(w.forest, 200, 20, seed=21)
+    op = o.place(w.forest, oracle_species(o, w.forest), 200, 0, 20, 0, seed=21)
+    assert_tables_equal(pf.table(), op.table())
+    for tile in (2048, 16384):
+        res = sequence_counts(pf, 99, tile_size=tile, **cfg)
+        alt, dep = res.counts()
+        c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=tile, **cfg)
+        oalt, odep, oreads = op.sequence(c, 99, flavour=0)
+        np.testing.assert_array_equal(dep, odep)
+        np.testing.assert_array_equal(alt, oalt)
+        assert res.dims()[2] == oreads
+
+
+def test_distribution_against_reference_engine(gpu_lib, orc):
+    """64 seeds: chi-square on SBS context counts, KS on per-edge SNV counts
+    and on VAF, GPU vs the std::mt19937_64 flavour; p > 0.01."""
+    from process_gb300 import synth
+    from process_gb300.engine import seq_cfg, sequence_counts
+    w = synth.config1(seed=11, n_leaves=300)
+    w.genome.chr_lengths = [300_000] * 3
+    eng, o = make_pair(orc, w)
+    sp = oracle_species(o, w.forest)
+    n = w.forest.num_of_nodes
+    cfg = dict(coverage=30, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3,
+               purity=0.8, with_normal_sample=False)
+    c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=16384, **cfg)
+    g_ctx, m_ctx = np.zeros(96), np.zeros(96)
+    g_edge, m_edge, g_vaf, m_vaf = [], [], [], []
+    for s in range(64):
+        pf = eng.place_mutations(w.forest, 50, 5, seed=1000 + s)
+        t = pf.table()
+        op = o.place(w.forest, sp, 50, 0, 5, 0, seed=1000 + s, flavour=1)
+        ot = op.table()
+        for tab, ctx, edges in ((t, g_ctx, g_edge), (ot, m_ctx, m_edge)):
+            snv = tab["kind"] == 0
+            ctx += np.bincount(tab["cls"][snv & (tab["nature"] == 0)], minlength=96)
+            edges.append(np.bincount(tab["edge"][snv & (tab["nature"] == 0)], minlength=n))
+        if s < 16:
+            alt, dep = sequence_counts(pf, 500 + s, tile_size=16384, **cfg).counts()
+            oalt, odep, _ = op.sequence(c, 500 + s, flavour=1)
+            for a, d, out, tab in ((alt, dep, g_vaf, t), (oalt, odep, m_vaf, ot)):
+                keep = (d[0] >= 10) & (tab["nature"] == 2)
+                out.append(a[0][keep] / d[0][keep])
+    keep = (g_ctx + m_ctx) > 0
+    assert stats.chi2_contingency(np.vstack([g_ctx[keep], m_ctx[keep]]))[1] > 0.01
+    assert stats.ks_2samp(np.concatenate(g_edge), np.concatenate(m_edge)).pvalue > 0.01
+    assert stats.ks_2samp(np.concatenate(g_vaf), np.concatenate(m_vaf)).pvalue > 0.01
+
+
+def test_edge_cases(gpu_lib, orc):
+    from process_gb300 import (BasicIlluminaSequencer, ErrorlessIlluminaSequencer, ProcessError, simulate_seq,
+                               simulate_normal_seq, synth)
+    from process_gb300.engine import sequence_counts
+    w = synth.config1(seed=2, n_leaves=200)
+    eng, _ = make_pair(orc, w)
+    pf = eng.place_mutations(w.forest, 100, 10, seed=1)
+    # error rate 0 is the error-less sequencer
+    a = simulate_seq(pf, BasicIlluminaSequencer(0.0), coverage=10, seed=3)["mutations"]
+    b = simulate_seq(pf, ErrorlessIlluminaSequencer(), coverage=10, seed=3)["mutations"]
+    for k in b:
+        np.testing.assert_array_equal(a[k], b[k])
+    # purity 0: tumour reads all come from normal cells: no passenger is seen without errors
+    alt, dep = sequence_counts(pf, 4, coverage=10, purity=0.0, error_rate=0.0).counts()
+    assert alt[0].sum() == 0 and dep[0].sum() > 0
+    # single-end reads (insert_size_mean = 0)
+    alt, dep = sequence_counts(pf, 4, coverage=12, insert_size_mean=0).counts()
+    assert abs(dep.mean() - 12) < 1.0
+    # variance above the mean: the reference's binomial insert model throws
+    with pytest.raises(ProcessError, match="variance"):
+        simulate_seq(pf, coverage=1, insert_size_mean=350, insert_size_stddev=30, seed=1)
+    # ... the normal model expresses it
+    df = simulate_seq(pf, coverage=5, insert_size_mean=350, insert_size_stddev=30, insert_model="normal",
+                      seed=1)["mutations"]
+    assert {"chr", "chr_pos", "ref", "alt", "causes", "classes", "S_1.occurrences", "S_1.coverage", "S_1.VAF",
+            "normal_sample.VAF"} <= set(df)
+    # coverage 0: no reads, no observed mutation
+    alt, dep = sequence_counts(pf, 4, coverage=0).counts()
+    assert dep.sum() == 0
+    # normal sequencing sees only preneoplastic mutations (when asked) and errors
+    n = simulate_normal_seq(pf, coverage=20, with_preneoplastic=True, write_SAM=False, seed=2)["mutations"]
+    assert set(n["classes"]) <= {"preneoplastic", "passenger"}
+    assert list(n) == ["chr", "chr_pos", "ref", "alt", "causes", "classes", "normal_sample.occurrences",
+                       "normal_sample.coverage", "normal_sample.VAF"]
+
+
+def test_full_size_properties(gpu_lib):
+    """The full config-2 workload (3.1 Gbp, 3 x 1e4 leaves, 100x): properties
+    that hold at any size — sorted unique loci, mean depth at the coverage,
+    clonal VAF at purity/2, an error-only alt rate in the normal sample."""
+    from process_gb300 import synth
+    from process_gb300.engine import sequence_counts
+    w = synth.config2(seed=2)
+    eng = synth.build_engine(w)
+    pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=7)
+    t = pf.table()
+    assert np.all(np.diff(t["locus"].astype(np.int64)) > 0)
+    assert 2e6 < len(t["locus"]) < 1e8
+    res = sequence_counts(pf, 9, **w.seq)
+    alt, dep = res.counts()
+    assert abs(dep[:3].mean() - 100) < 2
+    pre = (t["nature"] == 2) & (t["kind"] == 0)
+    vaf = alt[0, pre].sum() / dep[0, pre].sum()
+    assert abs(vaf - 0.35) < 0.02
+    # normal sample: tumour passengers only through errors (rate e/3)
+    pas = (t["nature"] == 0) & (t["kind"] == 0)
+    rate = alt[3, pas].sum() / dep[3, pas].sum()
+    assert rate < 1e-3
