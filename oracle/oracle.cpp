@@ -193,7 +193,7 @@ uint64_t binomial(Stream& st, uint64_t n, double p) {
     const double aa = (nd + 1.0) * s;
     double rr = my_exp(nd * my_log(q));
     k = 0;
-    while (u > rr && k < n) { u = u - rr; k = k + 1; rr = rr * (aa / double(k) - s); }
+    while (u > rr && k < n && rr > 0.0) { u = u - rr; k = k + 1; rr = rr * (aa / double(k) - s); }
   } else {
     const double spq = std::sqrt(nd * pp * q);
     const double b = 1.15 + 2.53 * spq;

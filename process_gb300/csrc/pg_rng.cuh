@@ -206,7 +206,8 @@ __device__ __forceinline__ uint64_t binomial(Stream& st, uint64_t n, double p) {
     const double aa = (nd + 1.0) * s;
     double rr = pg_exp(nd * pg_log(q));
     k = 0;
-    while (u > rr && k < n) { u = u - rr; k = k + 1; rr = rr * (aa / double(k) - s); }
+    // rr > 0: once the pmf underflows the remaining mass is below rounding
+    while (u > rr && k < n && rr > 0.0) { u = u - rr; k = k + 1; rr = rr * (aa / double(k) - s); }
   } else {
     const double spq = sqrt(nd * pp * q);
     const double b = 1.15 + 2.53 * spq;
