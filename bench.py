@@ -179,7 +179,7 @@ def gpu_arm(args):
     from process_gb300.engine import sequence_counts
     import ctypes as C
 
-    w = synth.config2(seed=2)
+    w = synth.config2(seed=2, genome_scale=args.genome_scale)
     eng = synth.build_engine(w)
     stream = torch.cuda.current_stream()
     _lib.check(_lib.lib().pg_engine_set_stream(eng._h, C.c_void_p(stream.cuda_stream)))
@@ -311,6 +311,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--genome-scale", type=float, default=1.0,
+                    help="fraction of the 3.1 Gbp genome (profiling runs on smaller cases; 1.0 for the bench)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -803,21 +803,30 @@ SeqSetup seq_setup(const Placed& pl, const SeqCfg& c) {
   return s;
 }
 
+// error word of the visit of mate `mate` of a fragment to `locus`: the
+// MurmurHash3 fmix32 finaliser (A. Appleby, public domain) of the fragment's
+// Philox word (word 1 of its TAG_PAIR2 block) mixed with locus and mate
+uint32_t error_word(uint32_t w, uint32_t locus, uint32_t mate) {
+  uint32_t h = w ^ (locus * 0x9E3779B1u) ^ (mate ? 0x85EBCA77u : 0u);
+  h ^= h >> 16;
+  h *= 0x85EBCA6Bu;
+  h ^= h >> 13;
+  h *= 0xC2B2AE35u;
+  h ^= h >> 16;
+  return h;
+}
+
 void count_mate(const Placed& pl, const Carrier& car, uint32_t a, uint32_t R, int64_t cell, uint32_t allele,
-                uint32_t err_thr, uint64_t seed, uint32_t j, uint32_t t, uint32_t smp, uint32_t& q, W4& eb,
-                uint32_t* alt, uint32_t* dep) {
+                uint32_t err_thr, uint32_t mate, uint32_t w, uint32_t* alt, uint32_t* dep) {
   auto it = std::lower_bound(pl.locus.begin(), pl.locus.end(), a);
   for (size_t i = size_t(it - pl.locus.begin()); i < pl.locus.size() && pl.locus[i] < a + R; ++i) {
     const bool carried = car.ancestor_or_self(pl.edge[i], cell) && pl.allele[i] == allele;
     bool obs;
     if (pl.kind[i] == 1) obs = carried;
     else {
-      if ((q & 1u) == 0) eb = philox(uint32_t(seed), uint32_t(seed >> 32), j, t, smp, TAG_ERR | ((q >> 1) << 8));
-      const uint32_t ew = (q & 1u) ? eb.v[2] : eb.v[0];
-      const uint32_t bw = (q & 1u) ? eb.v[3] : eb.v[1];
-      ++q;
-      const bool err = ew < err_thr;
-      obs = carried ? !err : (err && mulhi32(bw, 3) == 0);
+      const uint32_t e = error_word(w, pl.locus[i], mate);
+      const bool err = e < err_thr;
+      obs = carried ? !err : (err && e % 3 == 0);   // the erroneous base is one of three
     }
     dep[i] += 1;
     if (obs) alt[i] += 1;
@@ -846,21 +855,30 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
     const uint32_t ce = e.g.off[ci + 1];
     for (uint32_t smp = 0; smp < out.n_samples; ++smp) {
       const SampleDesc& sd = s.samples[smp];
-      // multinomial split by the binomial tree, top-down
+      // multinomial split by a binary tree over the padded tile range
+      // [0, 2^D): node h covering [lo, lo+size) sends Binomial(n, w_left/w)
+      // fragments to its left half (w = start positions of covered tiles)
+      uint32_t D = 0;
+      while ((uint64_t(1) << D) < nt) ++D;
+      auto wts = [&](uint64_t a, uint64_t b) {
+        return std::min<uint64_t>(b * T, S) - std::min<uint64_t>(a * T, S);
+      };
       std::vector<uint64_t> tile_pairs(nt, 0);
-      struct Node { uint32_t lo, hi, id; uint64_t n; };
-      std::vector<Node> stack{{0, nt, 1, pairs}};
+      struct Node { uint64_t lo, size; uint32_t id; uint64_t n; };
+      std::vector<Node> stack{{0, uint64_t(1) << D, 1, pairs}};
       while (!stack.empty()) {
         Node nd = stack.back(); stack.pop_back();
-        if (nd.hi - nd.lo == 1) { tile_pairs[nd.lo] = nd.n; continue; }
-        const uint32_t mid = (nd.lo + nd.hi) >> 1;
-        const uint64_t a = uint64_t(nd.lo) * T;
-        const uint64_t bm = std::min<uint64_t>(uint64_t(mid) * T, S), bh = std::min<uint64_t>(uint64_t(nd.hi) * T, S);
-        const double p = double(bm - a) / double(bh - a);
-        Stream st = stream(seed, nd.id, ci, smp, TAG_TILE_SPLIT);
-        const uint64_t nl = binomial(st, nd.n, p);
-        stack.push_back({nd.lo, mid, 2 * nd.id, nl});
-        stack.push_back({mid, nd.hi, 2 * nd.id + 1, nd.n - nl});
+        if (nd.size == 1) { if (nd.lo < nt) tile_pairs[nd.lo] = nd.n; continue; }
+        const uint64_t half = nd.size / 2, mid = nd.lo + half;
+        uint64_t nl = 0;
+        const uint64_t wt = wts(nd.lo, nd.lo + nd.size);
+        if (nd.n > 0 && wt > 0) {
+          const double p = double(wts(nd.lo, mid)) / double(wt);
+          Stream st = stream(seed, nd.id, ci, smp, TAG_TILE_SPLIT);
+          nl = binomial(st, nd.n, p);
+        }
+        stack.push_back({nd.lo, half, 2 * nd.id, nl});
+        stack.push_back({mid, half, 2 * nd.id + 1, nd.n - nl});
       }
       uint32_t* alt = out.alt.data() + uint64_t(smp) * M;
       uint32_t* dep = out.depth.data() + uint64_t(smp) * M;
@@ -873,15 +891,13 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
           const bool normal = sd.all_normal || r.v[1] < sd.normal_thr;
           const int64_t cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[2], uint32_t(sd.leaves.size()))]);
           const uint32_t allele = mulhi32(r.v[3], 2);
-          uint32_t q = 0;
-          W4 eb{{0, 0, 0, 0}};
-          count_mate(pl, car, p0, s.R, cell, allele, s.err_thr, seed, j, t, smp, q, eb, alt, dep);
+          const W4 r2 = philox(uint32_t(seed), uint32_t(seed >> 32), j, t, smp, TAG_PAIR2);
+          count_mate(pl, car, p0, s.R, cell, allele, s.err_thr, 0, r2.v[1], alt, dep);
           if (s.paired) {
-            const W4 r2 = philox(uint32_t(seed), uint32_t(seed >> 32), j, t, smp, TAG_PAIR2);
             const uint32_t ins = s.ins_min + lookup(s.ins_thr.data(), uint32_t(s.ins_thr.size()), r2.v[0]);
             uint32_t p1 = p0 + ins - s.R;
             if (p1 > ce - s.R) p1 = ce - s.R;
-            count_mate(pl, car, p1, s.R, cell, allele, s.err_thr, seed, j, t, smp, q, eb, alt, dep);
+            count_mate(pl, car, p1, s.R, cell, allele, s.err_thr, 1, r2.v[1], alt, dep);
           }
           out.n_reads += s.paired ? 2 : 1;
         }

@@ -42,6 +42,7 @@ void ck(cudaError_t e, const char* what) {
 template <class F>
 pg_status guarded(F&& f) {
   try {
+    cudaGetLastError();   // a stale non-sticky error of an earlier call is not this call's error
     f();
     g_last_error.clear();
     return PG_OK;
@@ -186,6 +187,9 @@ struct pg_engine {
   std::map<uint32_t, Species> species;
   std::map<uint32_t, std::vector<DriverSpec>> drivers;
   bool infinite_sites = true;
+  // the caller's reference plus one per live placed/sequencing handle: the
+  // engine (its pool and stream) outlives every handle that draws from it
+  std::atomic<int> refs{1};
 
   ~pg_engine() {
     genome.reset(); chr_off_d.reset(); ctx_lists.reset(); id_lists.reset();
@@ -203,6 +207,14 @@ struct pg_forest {
   std::vector<uint32_t> tin, tout;             // Euler intervals (preorder)
   std::vector<std::vector<uint32_t>> leaves;   // per sample: tin of its leaves
 };
+
+static void engine_retain(pg_engine* e) { e->refs.fetch_add(1); }
+static void engine_release(pg_engine* e) {
+  if (e->refs.fetch_sub(1) == 1) {
+    cudaSetDevice(e->device);
+    delete e;
+  }
+}
 
 struct pg_placed {
   pg_engine* eng = nullptr;
@@ -411,7 +423,7 @@ pg_status pg_launch_count(uint64_t* n) {
 }
 
 pg_status pg_engine_destroy(pg_engine* eng) {
-  return guarded([&] { if (eng) { cudaSetDevice(eng->device); delete eng; } });
+  return guarded([&] { if (eng) engine_release(eng); });
 }
 
 pg_status pg_engine_genome_info(const pg_engine* e, uint64_t* total_len, uint64_t* ctx_total, uint64_t* id_total,
@@ -822,12 +834,19 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     ck(cudaMemcpy(&err_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost), "error flag");
     if (err_h & pg::ERR_EMPTY_CLASS) throw std::runtime_error("a drawn mutation class has no indexed positions");
     if (err_h & pg::ERR_CAPACITY) throw std::runtime_error("internal hash table capacity exceeded");
+    engine_retain(e);
     *out = pl.release();
   });
 }
 
 pg_status pg_placed_destroy(pg_placed* p) {
-  return guarded([&] { if (p) { cudaSetDevice(p->eng->device); delete p; } });
+  return guarded([&] {
+    if (!p) return;
+    pg_engine* e = p->eng;
+    cudaSetDevice(e->device);
+    delete p;              // device buffers go back to the engine's pool
+    engine_release(e);
+  });
 }
 
 pg_status pg_placed_count(const pg_placed* p, uint64_t* n) {
@@ -943,15 +962,18 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     // ---- tile size
     uint32_t T = c->tile_size;
     if (T == 0) {
+      // about 1024 fragments per tile (one shared-memory batch), at most
+      // 128 records per window, and a window that fits the start buckets
+      const double mates_per_frag = paired ? 2.0 : 1.0;
+      double t = c->coverage > 0 ? 1024.0 * R * mates_per_frag / c->coverage : 8192.0;
       const double density = double(pl->M) / double(e->G);
-      const double target = 256.0;  // expected records per window
-      double t = density > 0 ? target / density : 65536.0;
-      T = 1024;
-      while (T < 65536 && double(T) * 2 <= t) T <<= 1;
+      if (density > 0) t = std::min(t, 128.0 / density);
+      t = std::min(t, double(16384 - 1 - span));
+      T = uint32_t(std::max(256.0, std::floor(t / 64.0) * 64.0));
     }
     require(T >= 64 && T <= (1u << 24), "tile_size must be in [64, 2^24]");
     // ---- tiles
-    std::vector<uint32_t> t_start, t_len, t_end, t_slot, t_idx, c_ntiles, c_nstarts, c_id;
+    std::vector<uint32_t> t_start, t_len, t_end, c_ntiles, c_nstarts, c_id, c_first, c_depth, b_slot, b_index;
     std::vector<uint64_t> c_pairs;
     const double mates = paired ? 2.0 : 1.0;
     uint64_t frags_per_sample = 0;
@@ -962,14 +984,18 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
       const uint32_t S = L - R + 1;
       const uint32_t nt = (S + T - 1) / T;
       const uint64_t pairs = uint64_t(std::floor(c->coverage * double(L) / (double(R) * mates)));
+      require(pairs < (uint64_t(1) << 32), "too many fragments for one chromosome");
+      uint32_t D = 0;
+      while ((uint64_t(1) << D) < nt) ++D;
       c_id.push_back(ci); c_ntiles.push_back(nt); c_nstarts.push_back(S); c_pairs.push_back(pairs);
+      c_first.push_back(uint32_t(t_start.size())); c_depth.push_back(D);
       frags_per_sample += pairs;
+      const uint32_t blk = 1u << std::min<uint32_t>(D, 6);
+      for (uint32_t b = 0; b * blk < nt; ++b) { b_slot.push_back(slot); b_index.push_back(b); }
       for (uint32_t k = 0; k < nt; ++k) {
         t_start.push_back(e->chr_off[ci] + k * T);
         t_len.push_back(std::min<uint32_t>(T, S - k * T));
         t_end.push_back(e->chr_off[ci] + L);
-        t_slot.push_back(slot);
-        t_idx.push_back(k);
       }
     }
     const uint32_t n_tiles = uint32_t(t_start.size());
@@ -1011,24 +1037,40 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     res->depth = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
     ck(cudaMemsetAsync(res->alt.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
     ck(cudaMemsetAsync(res->depth.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
-    if (pl->M == 0 || n_tiles == 0 || samples.empty()) { ck(cudaStreamSynchronize(st), "seq"); *out = res.release(); return; }
+    if (pl->M == 0 || n_tiles == 0 || samples.empty()) {
+      ck(cudaStreamSynchronize(st), "seq");
+      engine_retain(e);
+      *out = res.release();
+      return;
+    }
     auto etin_d = upload(P, etin, st), etout_d = upload(P, etout, st);
     auto ts_d = upload(P, t_start, st), tl_d = upload(P, t_len, st), te_d = upload(P, t_end, st);
-    auto tsl_d = upload(P, t_slot, st), tix_d = upload(P, t_idx, st);
+    auto bs_d = upload(P, b_slot, st), bi_d = upload(P, b_index, st);
     auto cnt_d = upload(P, c_ntiles, st), cns_d = upload(P, c_nstarts, st), cid_d = upload(P, c_id, st);
+    auto cf_d = upload(P, c_first, st), cd_d = upload(P, c_depth, st);
     auto cp_d = upload(P, c_pairs, st);
     auto smp_d = upload(P, samples, st);
     auto leaf_d = upload(P, leaf_tin, st);
     auto ins_d = upload(P, ins_thr, st);
+    // guide table of the insert CDF: first index whose threshold exceeds g * 2^23
+    std::vector<uint16_t> guide(256);
+    for (uint32_t g = 0; g < 256; ++g) {
+      const uint32_t v = g << 23;
+      const uint32_t k = uint32_t(std::upper_bound(ins_thr.begin(), ins_thr.end(), v) - ins_thr.begin());
+      guide[g] = uint16_t(std::min<uint32_t>(k, uint32_t(ins_thr.size()) - 1));
+    }
+    auto guide_d = upload(P, guide, st);
     DBuf<pg::SeqRec> recs(P, pl->M);
-    DBuf<uint32_t> pair_cnt(P, uint64_t(n_tiles) * samples.size());
+    DBuf<uint32_t> pair_cnt(P, uint64_t(n_tiles) * samples.size()), rlo(P, n_tiles), rhi(P, n_tiles);
     pg::seq_build_records(pl->view(), uint32_t(pl->M), etin_d.p, etout_d.p, recs.p, st);
-    pg::seq_tile_counts(uint32_t(samples.size()), n_tiles, tsl_d.p, tix_d.p, cnt_d.p, cns_d.p, cid_d.p, cp_d.p, T,
-                        seed, pair_cnt.p, st);
-    pg::SeqTiles tiles{n_tiles, ts_d.p, tl_d.p, te_d.p, nullptr};
+    pg::seq_tile_counts(uint32_t(samples.size()), uint32_t(b_slot.size()), bs_d.p, bi_d.p, cf_d.p, cnt_d.p, cd_d.p,
+                        cns_d.p, cid_d.p, cp_d.p, T, n_tiles, seed, pair_cnt.p, st);
+    pg::seq_tile_ranges(recs.p, uint32_t(pl->M), ts_d.p, tl_d.p, n_tiles, span, rlo.p, rhi.p, st);
+    pg::SeqTiles tiles{n_tiles, ts_d.p, tl_d.p, te_d.p, rlo.p, rhi.p};
     pg::SeqParams prm{};
     prm.read_len = R; prm.paired = paired ? 1u : 0u; prm.span = span;
     prm.ins_min = ins_min; prm.n_ins = uint32_t(ins_thr.size()); prm.ins_cdf = ins_d.p;
+    prm.ins_guide = guide_d.p;
     double et = std::floor(c->error_rate * 4294967296.0);
     prm.err_thr = et >= 4294967295.0 ? 0xffffffffu : uint32_t(et);
     prm.normal_tin = N;
@@ -1038,12 +1080,19 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
                   res->alt.p, res->depth.p, st);
     res->kernel_ms = timer.stop();
     ck(cudaGetLastError(), "sequencing kernels");
+    engine_retain(e);
     *out = res.release();
   });
 }
 
 pg_status pg_seq_result_destroy(pg_seq_result* r) {
-  return guarded([&] { if (r) { cudaSetDevice(r->eng->device); delete r; } });
+  return guarded([&] {
+    if (!r) return;
+    pg_engine* e = r->eng;
+    cudaSetDevice(e->device);
+    delete r;
+    engine_release(e);
+  });
 }
 
 pg_status pg_seq_result_dims(const pg_seq_result* r, uint32_t* n_samples, uint64_t* n_mut, uint64_t* n_reads) {

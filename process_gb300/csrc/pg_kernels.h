@@ -95,7 +95,8 @@ struct SeqTiles {
   const uint32_t* start;   // first start position of the tile (absolute)
   const uint32_t* len;     // number of start positions in the tile
   const uint32_t* chr_end; // absolute end of the tile's chromosome
-  const uint32_t* tree;    // per tile: (chr slot << 24 | unused) -- see seq_tile_counts
+  const uint32_t* rec_lo;  // records of the tile's window [start, start + len - 1 + span)
+  const uint32_t* rec_hi;
 };
 
 struct SeqSample {
@@ -111,6 +112,7 @@ struct SeqParams {
   uint32_t span;           // max fragment span past the start (read_len or max insert)
   uint32_t ins_min, n_ins; // insert size = ins_min + index in the CDF table
   const uint32_t* ins_cdf;
+  const uint16_t* ins_guide; // 256 entries: first index whose threshold exceeds g * 2^23
   uint32_t err_thr;        // substitution error iff u < err_thr
   uint32_t normal_tin;     // Euler index of normal cells
   uint32_t n_alleles;
@@ -118,12 +120,15 @@ struct SeqParams {
 
 void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_tin, const uint32_t* edge_tout,
                        SeqRec* recs, cudaStream_t st);
+void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start, const uint32_t* len,
+                     uint32_t n_tiles, uint32_t span, uint32_t* rlo, uint32_t* rhi, cudaStream_t st);
 // per (sample, tile) pair counts: multinomial split of each chromosome's
-// pair count over its tiles by a binary tree of binomial draws
-void seq_tile_counts(uint32_t n_samples, uint32_t n_tiles, const uint32_t* tile_chr_slot,
-                     const uint32_t* tile_idx_in_chr, const uint32_t* chr_ntiles, const uint32_t* chr_nstarts,
-                     const uint32_t* chr_id, const uint64_t* chr_pairs, uint32_t tile_size, uint64_t seed,
-                     uint32_t* pair_cnt, cudaStream_t st);
+// pair count over its tiles by a binary tree of binomial draws, one thread
+// per (sample, block of 64 tiles)
+void seq_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* blk_slot, const uint32_t* blk_index,
+                     const uint32_t* chr_first_tile, const uint32_t* chr_ntiles, const uint32_t* chr_depth,
+                     const uint32_t* chr_nstarts, const uint32_t* chr_id, const uint64_t* chr_pairs,
+                     uint32_t tile_size, uint32_t n_tiles, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st);
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
                const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st);

@@ -21,22 +21,37 @@
 //   * a read covering a mutation locus adds 1 to its depth; it adds 1 to alt
 //     when it carries the mutation (edge is an ancestor of the cell, same
 //     allele) and the base is not hit by a substitution error, or when it
-//     does not carry it and an error turns the reference into that alt base
-//     (probability err/3).  Indels are not affected by substitution errors.
+//     does not carry it and an error turns the reference into that alt base.
+//     The error word of a (fragment, mate, locus) visit is the MurmurHash3
+//     fmix32 finaliser of the fragment's Philox word mixed with the locus and
+//     the mate; an error happens when it is below err_thr, and the erroneous
+//     base is one of the three others, word % 3 == 0 being the alt base.
+//     Indels are not affected by substitution errors.
 //
-// Kernel layout: one CTA per (tile, sample).  The CTA stages the sorted
-// mutation records of its window [tile start, tile end + span) in shared
-// memory, keeps alt/depth counters there (block-private bins, shared-memory
-// atomics), and flushes them to HBM once.  Windows larger than the shared
-// capacity run the same loop on the global arrays.
+// Kernel layout (one CTA per (tile, sample); fragments in batches):
+//   phase A  every thread generates fragments (two Philox blocks each) and
+//            writes its two mates to shared memory; mates are bucketed by
+//            start position (16 bp buckets, counting sort);
+//   phase B  work items (mutation record, start bucket) scan the mates of one
+//            bucket that may cover the record and count depth and alt in
+//            registers, one shared-memory atomic per item.
+// Both phases keep every lane busy whatever the number of mutations a read
+// covers.  Windows with more records than shared memory holds run a per-read
+// loop on the global arrays instead.
 #include "pg_common.cuh"
 #include "pg_rng.cuh"
 #include "pg_kernels.h"
+#include "pg_scan.cuh"
 
 namespace pg {
 
 constexpr int SEQ_THREADS = 256;
-constexpr uint32_t SEQ_CAP = 1024;   // mutation records staged per CTA
+constexpr uint32_t SEQ_CAP = 512;        // mutation records staged per CTA
+constexpr uint32_t SEQ_MCAP = 2048;      // mates per batch (SEQ_MCAP / 2 fragments)
+constexpr uint32_t SEQ_BW = 16;          // start bucket width (bp)
+constexpr uint32_t SEQ_NBK = 1024;       // start buckets per window (window <= 16 kbp)
+constexpr uint32_t SEQ_INS_CAP = 1024;   // insert-size CDF entries staged in shared memory
+constexpr uint32_t SEQ_GUIDE = 256;      // guide table of the insert-size CDF
 
 __global__ void k_seq_records(PlaceOut s, uint32_t n, const uint32_t* __restrict__ edge_tin,
                               const uint32_t* __restrict__ edge_tout, SeqRec* __restrict__ recs) {
@@ -51,122 +66,278 @@ __global__ void k_seq_records(PlaceOut s, uint32_t n, const uint32_t* __restrict
   recs[i] = r;
 }
 
-__global__ void k_tile_counts(uint32_t n_samples, uint32_t n_tiles, const uint32_t* __restrict__ tile_slot,
-                              const uint32_t* __restrict__ tile_idx, const uint32_t* __restrict__ chr_ntiles,
+__device__ __forceinline__ uint32_t lower_bound_rec(const SeqRec* __restrict__ recs, uint32_t n, uint32_t key) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) { const uint32_t mid = (lo + hi) >> 1; if (recs[mid].locus < key) lo = mid + 1; else hi = mid; }
+  return lo;
+}
+
+// record range [lo, hi) of every tile's window [start, start + len - 1 + span)
+__global__ void k_tile_ranges(const SeqRec* __restrict__ recs, uint32_t n_recs, const uint32_t* __restrict__ start,
+                              const uint32_t* __restrict__ len, uint32_t n_tiles, uint32_t span,
+                              uint32_t* __restrict__ rlo, uint32_t* __restrict__ rhi) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tiles) return;
+  rlo[t] = lower_bound_rec(recs, n_recs, start[t]);
+  rhi[t] = lower_bound_rec(recs, n_recs, start[t] + len[t] - 1 + span);
+}
+
+// Multinomial split of a chromosome's fragments over its n tiles: a binary
+// tree over the padded range [0, 2^D) of tiles (D = ceil(log2 n)); the node
+// with heap id h at depth d covers tiles [i 2^(D-d), (i+1) 2^(D-d)) and sends
+// Binomial(count, w_left / w_node) fragments to its left half, w being the
+// number of start positions of the covered tiles.  Every node's draw uses
+// Philox counter (h, chromosome, sample, TAG_TILE_SPLIT).
+struct TileSplit {
+  uint64_t S;     // start positions of the chromosome
+  uint32_t T;     // tile size
+  __device__ __forceinline__ uint64_t w(uint64_t a, uint64_t b) const {   // start positions of tiles [a, b)
+    const uint64_t x = a * T < S ? a * T : S, y = b * T < S ? b * T : S;
+    return y - x;
+  }
+  __device__ __forceinline__ uint64_t left(Key key, uint32_t h, uint32_t chr, uint32_t s, uint64_t n, uint64_t lo,
+                                           uint64_t mid, uint64_t hi) const {
+    const uint64_t wt = w(lo, hi);
+    if (n == 0 || wt == 0) return 0;
+    const double p = double(w(lo, mid)) / double(wt);
+    Stream st{key, h, chr, s, TAG_TILE_SPLIT, 0u};
+    return binomial(st, n, p);
+  }
+};
+
+constexpr uint32_t SPLIT_BLOCK_LOG = 6;   // 64 tiles per thread
+
+// one thread per (sample, block of 64 tiles): walk from the root to the
+// block's node, then draw the block's 63 internal splits top-down
+__global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* __restrict__ blk_slot,
+                              const uint32_t* __restrict__ blk_index, const uint32_t* __restrict__ chr_first_tile,
+                              const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
                               const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
-                              const uint64_t* __restrict__ chr_pairs, uint32_t T, Key key,
+                              const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles, Key key,
                               uint32_t* __restrict__ pair_cnt) {
   const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (gid >= uint64_t(n_tiles) * n_samples) return;
-  const uint32_t s = uint32_t(gid / n_tiles), t = uint32_t(gid % n_tiles);
-  const uint32_t slot = tile_slot[t], idx = tile_idx[t];
-  const uint64_t S = chr_nstarts[slot];
-  uint64_t n = chr_pairs[slot];
-  uint32_t lo = 0, hi = chr_ntiles[slot], node = 1;
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) >> 1;
-    const uint64_t a = uint64_t(lo) * T;
-    const uint64_t bm = uint64_t(mid) * T < S ? uint64_t(mid) * T : S;
-    const uint64_t bh = uint64_t(hi) * T < S ? uint64_t(hi) * T : S;
-    const double p = double(bm - a) / double(bh - a);
-    Stream st{key, node, chr_id[slot], s, TAG_TILE_SPLIT, 0u};
-    const uint64_t nl = binomial(st, n, p);
-    if (idx < mid) { n = nl; hi = mid; node = 2 * node; }
-    else { n = n - nl; lo = mid; node = 2 * node + 1; }
+  if (gid >= uint64_t(n_blocks) * n_samples) return;
+  const uint32_t s = uint32_t(gid / n_blocks), bi = uint32_t(gid % n_blocks);
+  const uint32_t slot = blk_slot[bi], b = blk_index[bi];
+  const uint32_t D = chr_depth[slot], chr = chr_id[slot], nt = chr_ntiles[slot];
+  const TileSplit sp{chr_nstarts[slot], T};
+  const uint32_t Db = D < SPLIT_BLOCK_LOG ? D : SPLIT_BLOCK_LOG;   // depth of the block's subtree
+  // root -> block node
+  uint64_t n = chr_pairs[slot], lo = 0, size = uint64_t(1) << D;
+  uint32_t h = 1;
+  for (uint32_t d = 0; d < D - Db; ++d) {
+    const uint64_t half = size >> 1, mid = lo + half;
+    const uint64_t nl = sp.left(key, h, chr, s, n, lo, mid, lo + size);
+    const bool right = (uint64_t(b) << Db) >= mid;   // the block lies in the right half
+    if (right) { n -= nl; lo = mid; h = 2 * h + 1; } else { n = nl; h = 2 * h; }
+    size = half;
   }
-  pair_cnt[gid] = uint32_t(n);
+  // the block's subtree, breadth first (relative heap ids 1 .. 2^Db - 1)
+  uint32_t c[2 << SPLIT_BLOCK_LOG];
+  c[1] = uint32_t(n);
+  const uint32_t nint = (1u << Db) - 1;
+  for (uint32_t r = 1; r <= nint; ++r) {
+    const uint32_t level = 31 - __clz(r);
+    const uint64_t nsz = uint64_t(1) << (Db - level);
+    const uint64_t nlo = lo + uint64_t(r - (1u << level)) * nsz;
+    const uint32_t gh = (h << level) + (r - (1u << level));
+    const uint64_t nl = sp.left(key, gh, chr, s, c[r], nlo, nlo + (nsz >> 1), nlo + nsz);
+    c[2 * r] = uint32_t(nl);
+    c[2 * r + 1] = c[r] - uint32_t(nl);
+  }
+  const uint32_t base = chr_first_tile[slot];
+  for (uint32_t r = 0; r < (1u << Db); ++r) {
+    const uint64_t tile = lo + r;
+    if (tile < nt) pair_cnt[uint64_t(s) * n_tiles + base + tile] = c[(1u << Db) + r];
+  }
 }
 
-template <bool SMEM>
-__device__ __forceinline__ void visit_mate(const SeqRec* __restrict__ recs, uint32_t nw, uint32_t* alt, uint32_t* dep,
-                                           uint32_t a, uint32_t R, uint32_t cell, uint32_t allele,
-                                           uint32_t err_thr, Key key, uint32_t j, uint32_t t, uint32_t s,
-                                           uint32_t& q, U4& eblk) {
-  // first record with locus >= a
-  uint32_t lo = 0, hi = nw;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (recs[mid].locus < a) lo = mid + 1; else hi = mid;
-  }
-  for (uint32_t i = lo; i < nw; ++i) {
-    const SeqRec r = recs[i];
-    if (r.locus >= a + R) break;
-    const bool carried = (r.tin <= cell) && (cell < r.tout) && ((r.info & 0xffu) == allele);
-    bool obs;
-    if ((r.info >> 8) & 1u) {
-      obs = carried;
+// error word of the visit of mate `mate` of a fragment (Philox word w) to `locus`
+__device__ __forceinline__ uint32_t err_word(uint32_t w, uint32_t locus, uint32_t mate) {
+  uint32_t h = w ^ (locus * 0x9E3779B1u) ^ (mate ? 0x85EBCA77u : 0u);
+  h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
+  return h;
+}
+
+// did the visit observe the alt base?
+__device__ __forceinline__ bool observed(uint32_t tin, uint32_t tout, uint32_t info, uint32_t cell, uint32_t allele,
+                                         uint32_t w, uint32_t locus, uint32_t mate, uint32_t err_thr) {
+  const bool carried = (tin <= cell) && (cell < tout) && ((info & 0xffu) == allele);
+  if ((info >> 8) & 1u) return carried;   // indel
+  const uint32_t e = err_word(w, locus, mate);
+  const bool err = e < err_thr;
+  return carried ? !err : (err && (e % 3u) == 0u);
+}
+
+// one fragment's draws: mate starts, source cell, allele and its error word
+struct Fragment {
+  uint32_t p0, p1, cell, allele, w;
+};
+
+template <bool INS_SMEM>
+__device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
+                                                  uint32_t len, uint32_t ce, const SeqSample& sm,
+                                                  const uint32_t* __restrict__ leaf_tin, const SeqParams& prm,
+                                                  const uint32_t* ins, const uint16_t* guide) {
+  const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
+  const U4 r2 = philox(key.k0, key.k1, j, t, s, TAG_PAIR2);
+  Fragment f;
+  const uint32_t R = prm.read_len;
+  f.p0 = start + __umulhi(r.x, len);
+  const bool normal = sm.all_normal || r.y < sm.normal_thr;
+  f.cell = normal ? prm.normal_tin : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.z, sm.n_leaves));
+  f.allele = __umulhi(r.w, prm.n_alleles);
+  f.w = r2.y;
+  f.p1 = f.p0;
+  if (prm.paired) {
+    uint32_t k;
+    if (INS_SMEM) {
+      const uint32_t v = r2.x >> 1;
+      k = guide[v >> 23];
+      while (k + 1 < prm.n_ins && ins[k] <= v) ++k;
     } else {
-      if ((q & 1u) == 0) eblk = philox(key.k0, key.k1, j, t, s, TAG_ERR | ((q >> 1) << 8));
-      const uint32_t ew = (q & 1u) ? eblk.z : eblk.x;
-      const uint32_t bw = (q & 1u) ? eblk.w : eblk.y;
-      ++q;
-      const bool err = ew < err_thr;
-      obs = carried ? !err : (err && __umulhi(bw, 3u) == 0u);
+      k = cdf_lookup(prm.ins_cdf, prm.n_ins, r2.x);
     }
-    atomicAdd(dep + i, 1u);
-    if (obs) atomicAdd(alt + i, 1u);
+    uint32_t p1 = f.p0 + prm.ins_min + k - R;
+    if (p1 > ce - R) p1 = ce - R;
+    f.p1 = p1;
   }
+  return f;
 }
 
-__global__ void __launch_bounds__(SEQ_THREADS) k_reads(const SeqRec* __restrict__ g_recs, uint32_t n_recs,
-                                                       SeqTiles tiles, const uint32_t* __restrict__ pair_cnt,
-                                                       const SeqSample* __restrict__ samples,
-                                                       const uint32_t* __restrict__ leaf_tin, SeqParams prm,
-                                                       Key key, uint32_t* __restrict__ g_alt,
-                                                       uint32_t* __restrict__ g_dep) {
-  __shared__ SeqRec s_rec[SEQ_CAP];
+__global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restrict__ g_recs, SeqTiles tiles,
+                                                          const uint32_t* __restrict__ pair_cnt,
+                                                          const SeqSample* __restrict__ samples,
+                                                          const uint32_t* __restrict__ leaf_tin, SeqParams prm,
+                                                          Key key, uint64_t n_recs, uint32_t* __restrict__ g_alt,
+                                                          uint32_t* __restrict__ g_dep) {
+  __shared__ uint32_t s_locus[SEQ_CAP], s_tin[SEQ_CAP], s_tout[SEQ_CAP], s_info[SEQ_CAP];
   __shared__ uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
-  __shared__ uint32_t s_lo, s_hi;
-  const uint32_t t = blockIdx.x, s = blockIdx.y;
+  __shared__ uint16_t s_mpos[SEQ_MCAP];     // start offset in the window | mate << 15
+  __shared__ uint32_t s_mcell[SEQ_MCAP];    // cell | allele << 30
+  __shared__ uint32_t s_mw[SEQ_MCAP];       // the fragment's error word
+  __shared__ uint16_t s_idx[SEQ_MCAP];      // mates in start-bucket order
+  __shared__ uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
+  __shared__ uint32_t s_bfill[SEQ_NBK];
+  __shared__ uint32_t s_ins[SEQ_INS_CAP];
+  __shared__ uint16_t s_guide[SEQ_GUIDE];
+  __shared__ uint32_t s_scan[8];
+  const uint32_t t = blockIdx.x, s = blockIdx.y, tid = threadIdx.x;
   const uint32_t n_pairs = pair_cnt[uint64_t(s) * tiles.n_tiles + t];
+  const uint32_t lo = tiles.rec_lo[t], nw = tiles.rec_hi[t] - lo;
+  if (nw == 0 || n_pairs == 0) return;       // nothing to count in this window
   const uint32_t start = tiles.start[t], len = tiles.len[t], ce = tiles.chr_end[t];
   const uint32_t R = prm.read_len;
-  if (threadIdx.x < 2) {
-    const uint32_t key_pos = threadIdx.x == 0 ? start : start + len - 1 + prm.span;
-    uint32_t lo = 0, hi = n_recs;
-    while (lo < hi) { const uint32_t mid = (lo + hi) >> 1; if (g_recs[mid].locus < key_pos) lo = mid + 1; else hi = mid; }
-    if (threadIdx.x == 0) s_lo = lo; else s_hi = lo;
-  }
-  __syncthreads();
-  const uint32_t lo = s_lo, nw = s_hi - s_lo;
-  if (nw == 0 || n_pairs == 0) return;       // nothing to count in this window
-  const bool smem = nw <= SEQ_CAP;
-  if (smem) {
-    for (uint32_t i = threadIdx.x; i < nw; i += SEQ_THREADS) { s_rec[i] = g_recs[lo + i]; s_alt[i] = 0; s_dep[i] = 0; }
-  }
-  __syncthreads();
+  const uint32_t wlen = len - 1 + prm.span;   // the window is [start, start + wlen)
+  const uint32_t nbk = (wlen + SEQ_BW - 1) / SEQ_BW;
   const SeqSample sm = samples[s];
-  const uint64_t M = n_recs;
-  uint32_t* galt = g_alt + uint64_t(s) * M + lo;
-  uint32_t* gdep = g_dep + uint64_t(s) * M + lo;
-  for (uint32_t j = threadIdx.x; j < n_pairs; j += SEQ_THREADS) {
-    const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
-    const uint32_t p0 = start + __umulhi(r.x, len);
-    const bool normal = sm.all_normal || r.y < sm.normal_thr;
-    const uint32_t cell = normal ? prm.normal_tin : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.z, sm.n_leaves));
-    const uint32_t allele = __umulhi(r.w, prm.n_alleles);
-    uint32_t q = 0;
-    U4 eblk{0, 0, 0, 0};
-    if (smem) visit_mate<true>(s_rec, nw, s_alt, s_dep, p0, R, cell, allele, prm.err_thr, key, j, t, s, q, eblk);
-    else visit_mate<false>(g_recs + lo, nw, galt, gdep, p0, R, cell, allele, prm.err_thr, key, j, t, s, q, eblk);
-    if (prm.paired) {
-      const U4 r2 = philox(key.k0, key.k1, j, t, s, TAG_PAIR2);
-      const uint32_t ins = prm.ins_min + cdf_lookup(prm.ins_cdf, prm.n_ins, r2.x);
-      uint32_t p1 = p0 + ins - R;
-      if (p1 > ce - R) p1 = ce - R;
-      if (smem) visit_mate<true>(s_rec, nw, s_alt, s_dep, p1, R, cell, allele, prm.err_thr, key, j, t, s, q, eblk);
-      else visit_mate<false>(g_recs + lo, nw, galt, gdep, p1, R, cell, allele, prm.err_thr, key, j, t, s, q, eblk);
-    }
-  }
-  if (smem) {
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nw; i += SEQ_THREADS) {
-      const uint32_t d = s_dep[i];
-      if (d) {
-        atomicAdd(gdep + i, d);
-        const uint32_t a = s_alt[i];
-        if (a) atomicAdd(galt + i, a);
+  uint32_t* galt = g_alt + uint64_t(s) * n_recs + lo;
+  uint32_t* gdep = g_dep + uint64_t(s) * n_recs + lo;
+  const SeqRec* grec = g_recs + lo;
+  const bool ins_smem = prm.paired && prm.n_ins <= SEQ_INS_CAP;
+
+  if (nw > SEQ_CAP || nbk > SEQ_NBK || wlen >= 32768u) {
+    // dense or long window: per-read loop over the global records
+    for (uint32_t j = tid; j < n_pairs; j += SEQ_THREADS) {
+      const Fragment f = make_fragment<false>(key, j, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
+      for (uint32_t mate = 0; mate < (prm.paired ? 2u : 1u); ++mate) {
+        const uint32_t a = mate ? f.p1 : f.p0;
+        for (uint32_t i = lower_bound_rec(grec, nw, a); i < nw; ++i) {
+          const SeqRec r = grec[i];
+          if (r.locus >= a + R) break;
+          atomicAdd(gdep + i, 1u);
+          if (observed(r.tin, r.tout, r.info, f.cell, f.allele, f.w, r.locus, mate, prm.err_thr))
+            atomicAdd(galt + i, 1u);
+        }
       }
+    }
+    return;
+  }
+
+  for (uint32_t i = tid; i < nw; i += SEQ_THREADS) {
+    const SeqRec r = grec[i];
+    s_locus[i] = r.locus; s_tin[i] = r.tin; s_tout[i] = r.tout; s_info[i] = r.info;
+    s_alt[i] = 0; s_dep[i] = 0;
+  }
+  if (ins_smem) {
+    for (uint32_t i = tid; i < prm.n_ins; i += SEQ_THREADS) s_ins[i] = prm.ins_cdf[i];
+    for (uint32_t g = tid; g < SEQ_GUIDE; g += SEQ_THREADS) s_guide[g] = prm.ins_guide[g];
+  }
+  // buckets a record's covering mates may start in: (L-R+1 .. L) - start
+  const uint32_t nbr = (R + SEQ_BW - 2) / SEQ_BW + 1;
+  const uint32_t n_items = nw * nbr;
+  const uint32_t per_batch = SEQ_MCAP / 2;
+
+  for (uint32_t b0 = 0; b0 < n_pairs; b0 += per_batch) {
+    const uint32_t nb_pairs = min(per_batch, n_pairs - b0);
+    for (uint32_t b = tid; b <= nbk; b += SEQ_THREADS) { s_boff[b] = 0; if (b < nbk) s_bfill[b] = 0; }
+    __syncthreads();
+    // phase A: fragments -> mates
+    const uint32_t n_mates = prm.paired ? 2 * nb_pairs : nb_pairs;
+    for (uint32_t k = tid; k < nb_pairs; k += SEQ_THREADS) {
+      const Fragment f = ins_smem
+          ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide)
+          : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
+      const uint32_t ca = f.cell | (f.allele << 30);
+      const uint32_t m0 = prm.paired ? 2 * k : k;
+      const uint32_t o0 = f.p0 - start;
+      s_mpos[m0] = uint16_t(o0); s_mcell[m0] = ca; s_mw[m0] = f.w;
+      atomicAdd(s_boff + o0 / SEQ_BW, 1u);
+      if (prm.paired) {
+        const uint32_t o1 = f.p1 - start;
+        s_mpos[m0 + 1] = uint16_t(o1 | 0x8000u); s_mcell[m0 + 1] = ca; s_mw[m0 + 1] = f.w;
+        atomicAdd(s_boff + o1 / SEQ_BW, 1u);
+      }
+    }
+    __syncthreads();
+    // bucket offsets (exclusive scan of at most 1024 counts)
+    {
+      uint32_t v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { const uint32_t b = tid * 4 + q; v[q] = b < nbk ? s_boff[b] : 0u; }
+      const uint32_t tot = block_excl_scan4(v, s_scan);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { const uint32_t b = tid * 4 + q; if (b < nbk) s_boff[b] = v[q]; }
+      if (tid == 0) s_boff[nbk] = tot;
+    }
+    __syncthreads();
+    for (uint32_t m = tid; m < n_mates; m += SEQ_THREADS) {
+      const uint32_t b = (s_mpos[m] & 0x7fffu) / SEQ_BW;
+      s_idx[s_boff[b] + atomicAdd(s_bfill + b, 1u)] = uint16_t(m);
+    }
+    __syncthreads();
+    // phase B: (record, bucket) items
+    for (uint32_t it = tid; it < n_items; it += SEQ_THREADS) {
+      const uint32_t i = it / nbr, kb = it - i * nbr;
+      const uint32_t L = s_locus[i];
+      const uint32_t off = L - start;                       // >= 0: records lie in the window
+      const uint32_t lo_off = off + 1 >= R ? off + 1 - R : 0u;
+      const uint32_t b = lo_off / SEQ_BW + kb;
+      if (b > off / SEQ_BW || b >= nbk) continue;
+      const uint32_t tin = s_tin[i], tout = s_tout[i], info = s_info[i];
+      uint32_t dep = 0, alt = 0;
+      for (uint32_t x = s_boff[b], xe = s_boff[b + 1]; x < xe; ++x) {
+        const uint32_t m = s_idx[x];
+        const uint32_t pm = s_mpos[m];
+        const uint32_t o = pm & 0x7fffu;
+        if (o > off || o + R <= off) continue;                // the mate does not cover L
+        const uint32_t ca = s_mcell[m];
+        dep += 1;
+        alt += observed(tin, tout, info, ca & 0x3fffffffu, ca >> 30, s_mw[m], L, pm >> 15, prm.err_thr) ? 1u : 0u;
+      }
+      if (dep) {
+        atomicAdd(s_dep + i, dep);
+        if (alt) atomicAdd(s_alt + i, alt);
+      }
+    }
+    __syncthreads();
+  }
+  for (uint32_t i = tid; i < nw; i += SEQ_THREADS) {
+    const uint32_t d = s_dep[i];
+    if (d) {
+      atomicAdd(gdep + i, d);
+      const uint32_t a = s_alt[i];
+      if (a) atomicAdd(galt + i, a);
     }
   }
 }
@@ -178,14 +349,19 @@ void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_
   if (n) { k_seq_records<<<nblk(n), 256, 0, st>>>(sorted, n, edge_tin, edge_tout, recs); note_launch(); }
 }
 
-void seq_tile_counts(uint32_t n_samples, uint32_t n_tiles, const uint32_t* tile_chr_slot,
-                     const uint32_t* tile_idx_in_chr, const uint32_t* chr_ntiles, const uint32_t* chr_nstarts,
-                     const uint32_t* chr_id, const uint64_t* chr_pairs, uint32_t tile_size, uint64_t seed,
-                     uint32_t* pair_cnt, cudaStream_t st) {
-  const uint64_t n = uint64_t(n_samples) * n_tiles;
-  if (n) { k_tile_counts<<<nblk(n, 128), 128, 0, st>>>(n_samples, n_tiles, tile_chr_slot, tile_idx_in_chr, chr_ntiles,
-                                                     chr_nstarts, chr_id, chr_pairs, tile_size, make_key(seed),
-                                                     pair_cnt); note_launch(); }
+void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start, const uint32_t* len,
+                     uint32_t n_tiles, uint32_t span, uint32_t* rlo, uint32_t* rhi, cudaStream_t st) {
+  if (n_tiles) { k_tile_ranges<<<nblk(n_tiles), 256, 0, st>>>(recs, n_recs, start, len, n_tiles, span, rlo, rhi); note_launch(); }
+}
+
+void seq_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* blk_slot, const uint32_t* blk_index,
+                     const uint32_t* chr_first_tile, const uint32_t* chr_ntiles, const uint32_t* chr_depth,
+                     const uint32_t* chr_nstarts, const uint32_t* chr_id, const uint64_t* chr_pairs,
+                     uint32_t tile_size, uint32_t n_tiles, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st) {
+  const uint64_t n = uint64_t(n_samples) * n_blocks;
+  if (n) { k_tile_counts<<<nblk(n, 64), 64, 0, st>>>(n_samples, n_blocks, blk_slot, blk_index, chr_first_tile,
+                                                   chr_ntiles, chr_depth, chr_nstarts, chr_id, chr_pairs, tile_size,
+                                                   n_tiles, make_key(seed), pair_cnt); note_launch(); }
 }
 
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
@@ -193,7 +369,7 @@ void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st) {
   if (tiles.n_tiles == 0 || n_samples == 0 || n_recs == 0) return;
   dim3 grid(tiles.n_tiles, n_samples);
-  k_reads<<<grid, SEQ_THREADS, 0, st>>>(recs, n_recs, tiles, pair_cnt, samples, leaf_tin, prm, make_key(seed), alt,
+  k_reads<<<grid, SEQ_THREADS, 0, st>>>(recs, tiles, pair_cnt, samples, leaf_tin, prm, make_key(seed), n_recs, alt,
                                          depth); note_launch();
 }
 

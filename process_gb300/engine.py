@@ -584,8 +584,9 @@ class PhylogeneticForest:
 class SeqResult:
     """Raw sequencing counts kept on the device until read."""
 
-    def __init__(self, handle: C.c_void_p):
+    def __init__(self, handle: C.c_void_p, source: "PhylogeneticForest | None" = None):
         self._h = handle
+        self.source = source
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -642,7 +643,7 @@ def sequence_counts(phylo_forest: PhylogeneticForest, seed: int, **cfg) -> SeqRe
     c, _sel = seq_cfg(chr_index=phylo_forest.engine._chr_index, **cfg)
     h = C.c_void_p()
     check(lib().pg_simulate_seq(phylo_forest._h, C.byref(c), int(seed), C.byref(h)))
-    return SeqResult(h)
+    return SeqResult(h, phylo_forest)
 
 
 def _sequencer_rate(sequencer) -> tuple[float, dict | None]:
