@@ -962,10 +962,13 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     // ---- tile size
     uint32_t T = c->tile_size;
     if (T == 0) {
-      // about 1024 fragments per tile (one shared-memory batch), at most
-      // 128 records per window, and a window that fits the start buckets
+      // fragments per tile: 4 standard deviations below one shared-memory
+      // batch of the read kernel; at most 128 records per window, and a
+      // window that fits the start buckets
       const double mates_per_frag = paired ? 2.0 : 1.0;
-      double t = c->coverage > 0 ? 1024.0 * R * mates_per_frag / c->coverage : 8192.0;
+      const double cap = double(pg::SEQ_FRAGS_PER_BATCH);
+      const double target = cap - 4.0 * std::sqrt(cap);
+      double t = c->coverage > 0 ? target * R * mates_per_frag / c->coverage : 8192.0;
       const double density = double(pl->M) / double(e->G);
       if (density > 0) t = std::min(t, 128.0 / density);
       t = std::min(t, double(16384 - 1 - span));

@@ -90,6 +90,10 @@ struct SeqRec {            // 16 B, one per placed mutation, sorted by locus
   uint32_t info;           // allele | kind << 8
 };
 
+// fragments the read kernel handles per shared-memory batch (5 per thread);
+// tiles are sized so that their fragment count rarely exceeds one batch
+constexpr uint32_t SEQ_FRAGS_PER_BATCH = 1280;
+
 struct SeqTiles {
   uint32_t n_tiles;        // over all selected chromosomes
   const uint32_t* start;   // first start position of the tile (absolute)

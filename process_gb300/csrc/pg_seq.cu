@@ -47,7 +47,7 @@ namespace pg {
 
 constexpr int SEQ_THREADS = 256;
 constexpr uint32_t SEQ_CAP = 512;        // mutation records staged per CTA
-constexpr uint32_t SEQ_MCAP = 2048;      // mates per batch (SEQ_MCAP / 2 fragments)
+constexpr uint32_t SEQ_MCAP = 2 * SEQ_FRAGS_PER_BATCH;   // mates per batch
 constexpr uint32_t SEQ_BW = 16;          // start bucket width (bp)
 constexpr uint32_t SEQ_NBK = 1024;       // start buckets per window (window <= 16 kbp)
 constexpr uint32_t SEQ_INS_CAP = 1024;   // insert-size CDF entries staged in shared memory
@@ -213,15 +213,17 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
                                                           uint32_t* __restrict__ g_dep) {
   __shared__ uint32_t s_locus[SEQ_CAP], s_tin[SEQ_CAP], s_tout[SEQ_CAP], s_info[SEQ_CAP];
   __shared__ uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
+  // mates of the batch in start-bucket order
   __shared__ uint16_t s_mpos[SEQ_MCAP];     // start offset in the window | mate << 15
   __shared__ uint32_t s_mcell[SEQ_MCAP];    // cell | allele << 30
   __shared__ uint32_t s_mw[SEQ_MCAP];       // the fragment's error word
-  __shared__ uint16_t s_idx[SEQ_MCAP];      // mates in start-bucket order
   __shared__ uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
-  __shared__ uint32_t s_bfill[SEQ_NBK];
   __shared__ uint32_t s_ins[SEQ_INS_CAP];
   __shared__ uint16_t s_guide[SEQ_GUIDE];
+  __shared__ uint16_t s_wstart[SEQ_CAP];    // first candidate mate (sorted position) of each record
+  __shared__ uint32_t s_wpre[SEQ_CAP];      // prefix of the records' candidate counts
   __shared__ uint32_t s_scan[8];
+  __shared__ uint32_t s_wtot;
   const uint32_t t = blockIdx.x, s = blockIdx.y, tid = threadIdx.x;
   const uint32_t n_pairs = pair_cnt[uint64_t(s) * tiles.n_tiles + t];
   const uint32_t lo = tiles.rec_lo[t], nw = tiles.rec_hi[t] - lo;
@@ -263,30 +265,31 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
     for (uint32_t i = tid; i < prm.n_ins; i += SEQ_THREADS) s_ins[i] = prm.ins_cdf[i];
     for (uint32_t g = tid; g < SEQ_GUIDE; g += SEQ_THREADS) s_guide[g] = prm.ins_guide[g];
   }
-  // buckets a record's covering mates may start in: (L-R+1 .. L) - start
-  const uint32_t nbr = (R + SEQ_BW - 2) / SEQ_BW + 1;
-  const uint32_t n_items = nw * nbr;
   const uint32_t per_batch = SEQ_MCAP / 2;
 
+  constexpr uint32_t FPT = SEQ_MCAP / 2 / SEQ_THREADS;   // fragments per thread and batch
   for (uint32_t b0 = 0; b0 < n_pairs; b0 += per_batch) {
     const uint32_t nb_pairs = min(per_batch, n_pairs - b0);
-    for (uint32_t b = tid; b <= nbk; b += SEQ_THREADS) { s_boff[b] = 0; if (b < nbk) s_bfill[b] = 0; }
+    for (uint32_t b = tid; b <= nbk; b += SEQ_THREADS) s_boff[b] = 0;
     __syncthreads();
-    // phase A: fragments -> mates
-    const uint32_t n_mates = prm.paired ? 2 * nb_pairs : nb_pairs;
-    for (uint32_t k = tid; k < nb_pairs; k += SEQ_THREADS) {
-      const Fragment f = ins_smem
-          ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide)
-          : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
-      const uint32_t ca = f.cell | (f.allele << 30);
-      const uint32_t m0 = prm.paired ? 2 * k : k;
-      const uint32_t o0 = f.p0 - start;
-      s_mpos[m0] = uint16_t(o0); s_mcell[m0] = ca; s_mw[m0] = f.w;
-      atomicAdd(s_boff + o0 / SEQ_BW, 1u);
-      if (prm.paired) {
-        const uint32_t o1 = f.p1 - start;
-        s_mpos[m0 + 1] = uint16_t(o1 | 0x8000u); s_mcell[m0 + 1] = ca; s_mw[m0 + 1] = f.w;
-        atomicAdd(s_boff + o1 / SEQ_BW, 1u);
+    // phase A: fragments stay in registers; each mate takes its rank within
+    // its start bucket from the histogram's atomic
+    uint32_t o0[FPT], o1[FPT], ca[FPT], fw[FPT], rk0[FPT], rk1[FPT];
+#pragma unroll
+    for (uint32_t q = 0; q < FPT; ++q) {
+      const uint32_t k = tid + q * SEQ_THREADS;
+      if (k < nb_pairs) {
+        const Fragment f = ins_smem
+            ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide)
+            : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
+        ca[q] = f.cell | (f.allele << 30);
+        fw[q] = f.w;
+        o0[q] = f.p0 - start;
+        rk0[q] = atomicAdd(s_boff + o0[q] / SEQ_BW, 1u);
+        if (prm.paired) {
+          o1[q] = f.p1 - start;
+          rk1[q] = atomicAdd(s_boff + o1[q] / SEQ_BW, 1u);
+        }
       }
     }
     __syncthreads();
@@ -301,33 +304,72 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
       if (tid == 0) s_boff[nbk] = tot;
     }
     __syncthreads();
-    for (uint32_t m = tid; m < n_mates; m += SEQ_THREADS) {
-      const uint32_t b = (s_mpos[m] & 0x7fffu) / SEQ_BW;
-      s_idx[s_boff[b] + atomicAdd(s_bfill + b, 1u)] = uint16_t(m);
+    // scatter the mates in start-bucket order
+#pragma unroll
+    for (uint32_t q = 0; q < FPT; ++q) {
+      const uint32_t k = tid + q * SEQ_THREADS;
+      if (k < nb_pairs) {
+        const uint32_t x0 = s_boff[o0[q] / SEQ_BW] + rk0[q];
+        s_mpos[x0] = uint16_t(o0[q]); s_mcell[x0] = ca[q]; s_mw[x0] = fw[q];
+        if (prm.paired) {
+          const uint32_t x1 = s_boff[o1[q] / SEQ_BW] + rk1[q];
+          s_mpos[x1] = uint16_t(o1[q] | 0x8000u); s_mcell[x1] = ca[q]; s_mw[x1] = fw[q];
+        }
+      }
     }
     __syncthreads();
-    // phase B: (record, bucket) items
-    for (uint32_t it = tid; it < n_items; it += SEQ_THREADS) {
-      const uint32_t i = it / nbr, kb = it - i * nbr;
-      const uint32_t L = s_locus[i];
-      const uint32_t off = L - start;                       // >= 0: records lie in the window
-      const uint32_t lo_off = off + 1 >= R ? off + 1 - R : 0u;
-      const uint32_t b = lo_off / SEQ_BW + kb;
-      if (b > off / SEQ_BW || b >= nbk) continue;
-      const uint32_t tin = s_tin[i], tout = s_tout[i], info = s_info[i];
-      uint32_t dep = 0, alt = 0;
-      for (uint32_t x = s_boff[b], xe = s_boff[b + 1]; x < xe; ++x) {
-        const uint32_t m = s_idx[x];
-        const uint32_t pm = s_mpos[m];
-        const uint32_t o = pm & 0x7fffu;
-        if (o > off || o + R <= off) continue;                // the mate does not cover L
-        const uint32_t ca = s_mcell[m];
-        dep += 1;
-        alt += observed(tin, tout, info, ca & 0x3fffffffu, ca >> 30, s_mw[m], L, pm >> 15, prm.err_thr) ? 1u : 0u;
+    // phase B: a record's candidate mates (those starting in the buckets of
+    // [L-R+1, L]) are one contiguous run of the bucket-sorted mates; the runs
+    // of all records are concatenated and split evenly over the threads
+    {
+      uint32_t v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t i = tid * 4 + q;
+        uint32_t cnt = 0;
+        if (i < nw) {
+          const uint32_t off = s_locus[i] - start;
+          const uint32_t blo = (off + 1 >= R ? off + 1 - R : 0u) / SEQ_BW;
+          const uint32_t bhi = min(off / SEQ_BW, nbk - 1);
+          s_wstart[i] = uint16_t(s_boff[blo]);
+          cnt = s_boff[bhi + 1] - s_boff[blo];
+        }
+        v[q] = cnt;
       }
-      if (dep) {
-        atomicAdd(s_dep + i, dep);
-        if (alt) atomicAdd(s_alt + i, alt);
+      const uint32_t tot = block_excl_scan4(v, s_scan);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { const uint32_t i = tid * 4 + q; if (i < SEQ_CAP) s_wpre[i] = v[q]; }
+      if (tid == 0) s_wtot = tot;
+    }
+    __syncthreads();
+    {
+      const uint32_t W = s_wtot;
+      const uint32_t k0 = uint32_t(uint64_t(W) * tid / SEQ_THREADS);
+      const uint32_t k1 = uint32_t(uint64_t(W) * (tid + 1) / SEQ_THREADS);
+      if (k0 < k1) {
+        uint32_t i = 0, hi = nw;                              // record holding work item k0
+        while (hi - i > 1) { const uint32_t mid = (i + hi) >> 1; if (s_wpre[mid] <= k0) i = mid; else hi = mid; }
+        uint32_t next = i + 1 < nw ? s_wpre[i + 1] : W;
+        uint32_t L = s_locus[i], off = L - start, tin = s_tin[i], tout = s_tout[i], info = s_info[i];
+        uint32_t base = s_wstart[i] - s_wpre[i];
+        uint32_t dep = 0, alt = 0;
+        for (uint32_t k = k0; k < k1; ++k) {
+          while (k >= next) {                                 // the run of the next record starts
+            if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
+            dep = 0; alt = 0;
+            ++i;
+            next = i + 1 < nw ? s_wpre[i + 1] : W;
+            L = s_locus[i]; off = L - start; tin = s_tin[i]; tout = s_tout[i]; info = s_info[i];
+            base = s_wstart[i] - s_wpre[i];
+          }
+          const uint32_t x = base + k;
+          const uint32_t pm = s_mpos[x], ca = s_mcell[x], w = s_mw[x];   // independent loads
+          const uint32_t o = pm & 0x7fffu;
+          if (o > off || o + R <= off) continue;              // the mate does not cover L
+          dep += 1;
+          alt += observed(tin, tout, info, ca & 0x3fffffffu, ca >> 30, w, L, pm >> 15, prm.err_thr) ? 1u : 0u;
+        }
+        if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
       }
     }
     __syncthreads();
