@@ -78,6 +78,34 @@ pg_status pg_engine_set_stream(pg_engine* eng, void* cuda_stream);
 /* Number of kernels this library has launched in the process so far. */
 pg_status pg_launch_count(uint64_t* n);
 
+/* Per-class position counts of a genome the caller already holds in device
+ * memory, computed without allocating any device memory.  No reference
+ * counterpart: it exists for callers that must not call cudaMalloc, such as a
+ * host framework whose pooling allocator owns the device memory, code that
+ * runs while a stream is being captured, or a latency-bound loop that cannot
+ * afford the device-wide synchronisation an allocation can cause.
+ *   which          0: the 32 SBS trinucleotide contexts; 1: the 83 ID classes
+ *   genome_words   device pointer, 2-bit codes (A=0 C=1 G=2 T=3), 16 bases per
+ *                  u32 word, base i in bits 2*(i%16); at least
+ *                  ceil(genome_len/16) words
+ *   genome_len     total bases, at most 8,388,608 (larger genomes are rejected
+ *                  with PG_ERR_DOMAIN)
+ *   chr_off        device pointer, n_chr + 1 chromosome start offsets (the
+ *                  last one is genome_len)
+ *   class_totals   device pointer, 32 or 83 u64 counts (overwritten)
+ *   stream         cudaStream_t the two kernels are queued on (NULL: legacy
+ *                  default stream); the call returns without waiting.
+ * The per-tile counts live in one fixed 2.7 MB array of the library's own
+ * device memory, present on every GPU that loads the library until the
+ * process exits.  The first call on a device looks up that array's device
+ * address; make it before capturing a stream into a CUDA graph.  All calls
+ * share the array: calls whose kernels overlap on the GPU (different
+ * streams, or concurrent host threads) race and return wrong counts;
+ * serialise them on one stream.  The counts equal pg_engine_genome_info's
+ * ctx_total / id_total for the same genome. */
+pg_status pg_index_counts_noalloc(int which, const uint32_t* genome_words, uint64_t genome_len,
+                                  const uint32_t* chr_off, uint32_t n_chr, uint64_t* class_totals, void* stream);
+
 /* Genome size and per-class position counts of the indices (ctx: 32 entries,
  * id: 83 entries; either may be NULL).  get_genome_info, src/mutation_engine.cpp. */
 pg_status pg_engine_genome_info(const pg_engine* eng, uint64_t* total_len, uint64_t* ctx_total,

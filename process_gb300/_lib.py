@@ -60,6 +60,8 @@ _PROTOS = {
     "pg_engine_destroy": (C.c_int, [P]),
     "pg_engine_set_stream": (C.c_int, [P, C.c_void_p]),
     "pg_launch_count": (C.c_int, [u64p]),
+    "pg_index_counts_noalloc": (C.c_int, [C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint32, C.c_void_p,
+                                          C.c_void_p]),
     "pg_engine_genome_info": (C.c_int, [P, u64p, u64p, u64p, u32p, u32p]),
     "pg_engine_read_genome": (C.c_int, [P, C.c_uint64, C.c_uint64, u8p]),
     "pg_engine_gather_bases": (C.c_int, [P, C.c_uint64, u32p, u8p]),

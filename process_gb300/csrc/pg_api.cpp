@@ -418,6 +418,21 @@ pg_status pg_engine_set_stream(pg_engine* e, void* stream) {
   });
 }
 
+pg_status pg_index_counts_noalloc(int which, const uint32_t* genome_words, uint64_t genome_len,
+                                  const uint32_t* chr_off, uint32_t n_chr, uint64_t* class_totals, void* stream) {
+  return guarded([&] {
+    require(which == 0 || which == 1, "which must be 0 (SBS contexts) or 1 (ID classes)");
+    require(genome_words && chr_off && class_totals, "NULL device pointer");
+    require(n_chr >= 1, "at least one chromosome");
+    const char* msg = pg::index_counts_noalloc(which, genome_words, genome_len, chr_off, int(n_chr), class_totals,
+                                               static_cast<cudaStream_t>(stream));
+    if (msg) {
+      if (genome_len == 0 || genome_len > uint64_t(pg::NOALLOC_MAX_TILES) * 1024) throw DomainError(msg);
+      throw CudaError(msg);
+    }
+  });
+}
+
 pg_status pg_launch_count(uint64_t* n) {
   return guarded([&] { require(n != nullptr, "NULL argument"); *n = g_launches.load(); });
 }

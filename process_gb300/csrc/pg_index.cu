@@ -16,6 +16,8 @@
 // within their class is a multiple of the class stride.  Ranks inside a
 // 32-position step come from __match_any_sync, so the lists are in position
 // order without any sort.
+#include <mutex>
+
 #include "pg_common.cuh"
 #include "pg_rng.cuh"
 #include "pg_scan.cuh"
@@ -275,6 +277,70 @@ void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_of
 }
 
 int index_num_classes(int which) { return which == 0 ? SbsFamilies::NC : IdFamilies::NC; }
+
+// ------------------------------------------------------------ allocation-free class counts
+// The count pass above writes one count per (class, tile) into a table the
+// engine allocates.  This variant keeps that table in a fixed array of the
+// library's own device memory, so that a caller who may not allocate device
+// memory can still count the classes of a genome it holds.  The array is
+// sized for genomes up to NOALLOC_MAX_TILES tiles of 1024 bases (8 Mbp);
+// every GPU that loads the library holds it (2.7 MB) until the process ends.
+static __device__ __align__(256) uint32_t g_noalloc_tile_counts[N_ID * NOALLOC_MAX_TILES];
+
+// per-class sum of the tile counts (one block per class)
+__global__ void k_class_totals(const uint32_t* __restrict__ cnt, uint32_t ntiles, uint64_t* __restrict__ totals) {
+  __shared__ uint64_t s_part[8];
+  const uint32_t k = blockIdx.x;
+  uint64_t acc = 0;
+  for (uint32_t t = threadIdx.x; t < ntiles; t += blockDim.x) acc += cnt[uint64_t(k) * ntiles + t];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t tot = 0;
+    for (int w = 0; w < 8; ++w) tot += s_part[w];
+    totals[k] = tot;
+  }
+}
+
+// device address of g_noalloc_tile_counts per device (host code cannot use
+// the symbol itself: on the host it names a stand-in, not device memory)
+static std::mutex g_noalloc_mu;
+static uint32_t* g_noalloc_addr[64] = {};
+
+const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                                 uint64_t* totals, cudaStream_t st) {
+  if (G == 0 || G > uint64_t(NOALLOC_MAX_TILES) * TILE) return "genome length must be in [1, 8388608] bases";
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return "no current CUDA device";
+  uint32_t* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_tile_counts) != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        return "cudaGetSymbolAddress failed for the library's count array";
+      }
+      g_noalloc_addr[dev] = static_cast<uint32_t*>(p);
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  const uint32_t ntiles = index_num_tiles(G);
+  const int nc = index_num_classes(which);
+  // every (class, tile) entry is written by the count pass: nothing to clear
+  if (which == 0)
+    k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles, scratch,
+                                                                              nullptr, nullptr, nullptr, nullptr);
+  else
+    k_index_pass<IdFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles, scratch,
+                                                                             nullptr, nullptr, nullptr, nullptr);
+  k_class_totals<<<nc, 256, 0, st>>>(scratch, ntiles, totals);
+  note_launch(2);
+  if (cudaGetLastError() != cudaSuccess) return "launch of the count kernels failed";
+  return nullptr;
+}
 
 }  // namespace pg
 

@@ -18,6 +18,11 @@ void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t
 uint32_t index_num_tiles(uint64_t G);
 void genome_gather(const uint32_t* g, uint64_t G, const uint32_t* pos, uint64_t n, uint8_t* out, cudaStream_t st);
 int index_num_classes(int which);  // 0 = SBS contexts (32), 1 = ID classes (83)
+// allocation-free per-class totals over a caller-held genome (see pg_index.cu);
+// returns nullptr on success, else a message
+constexpr uint32_t NOALLOC_MAX_TILES = 8192;
+const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+                                 uint64_t* totals, cudaStream_t st);
 void index_count(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr, uint32_t* cnt,
                  uint32_t* part, uint32_t* totals, cudaStream_t st);
 void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
