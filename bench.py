@@ -181,7 +181,10 @@ def gpu_arm(args):
 
     w = synth.config2(seed=2, genome_scale=args.genome_scale)
     eng = synth.build_engine(w)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream: the engine runs on it and the CUDA
+    # events that time the steps are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     _lib.check(_lib.lib().pg_engine_set_stream(eng._h, C.c_void_p(stream.cuda_stream)))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 

@@ -204,6 +204,39 @@ pg_status pg_seq_result_copy(const pg_seq_result* res, int32_t* alt, int32_t* de
 /* Device time of the read kernel of the call (ms). */
 pg_status pg_seq_result_kernel_ms(const pg_seq_result* res, float* ms);
 
+/* ------------------------------------------------------------------ calibration
+ * Expected-VAF binomial-mixture negative log-likelihood of alt/depth tables
+ * and its gradient (no reference counterpart: ProCESS has no calibration
+ * path).  Per replicate r: sites (alt, depth, class) with class in [0, C);
+ * K epochs of relative length L_k (epoch_weight) whose mutations have mean
+ * cellular fraction phi_k; J signatures over the C classes.  Parameters per
+ * replicate (P = K + K*J + 1 floats): log rates lr_k, exposure logits
+ * theta_kj (softmax over j) and the purity logit rho:
+ *   pi_k(c) = e^lr_k L_k sum_j softmax(theta_k)_j S_j(c) / sum_k' e^lr_k' L_k'
+ *   v_k = sigmoid(rho) phi_k / 2
+ *   NLL = -sum_i log sum_k pi_k(c_i) v_k^a_i (1 - v_k)^(d_i - a_i)
+ * Computed in FP32 with compensated sums. */
+typedef struct pg_calib pg_calib;
+pg_status pg_calib_create(uint32_t n_rep, const uint64_t* site_off, const int32_t* alt, const int32_t* depth,
+                          const int32_t* cls, uint32_t K, uint32_t J, uint32_t C, const double* signatures,
+                          const double* epoch_weight, const double* phi, pg_calib** out);
+pg_status pg_calib_destroy(pg_calib* cal);
+pg_status pg_calib_num_params(const pg_calib* cal, uint32_t* P);
+/* every later call of the handle runs on this cudaStream_t (NULL: its own stream) */
+pg_status pg_calib_set_stream(pg_calib* cal, void* cuda_stream);
+/* Batched: NLL and gradient of every replicate in one launch of each kernel.
+ * params, nll and grad are device pointers (n_rep x P, n_rep, n_rep x P);
+ * nll or grad may be NULL.  Asynchronous on the handle's stream. */
+pg_status pg_calib_nll_grad(pg_calib* cal, const float* params, float* nll, float* grad);
+/* One replicate only (the per-instance path): same layout, replicate `rep`. */
+pg_status pg_calib_nll_grad_one(pg_calib* cal, uint32_t rep, const float* params, float* nll, float* grad);
+/* `steps` Adam steps on every replicate's parameters (device, updated in
+ * place), run entirely on the device as one CUDA graph; nll (device, n_rep,
+ * may be NULL) receives the NLL of the last step's parameters before the
+ * update.  The optimizer state restarts at zero on each call. */
+pg_status pg_calib_adam(pg_calib* cal, float* params, uint32_t steps, float lr, float beta1, float beta2, float eps,
+                        float* nll);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1139,3 +1139,183 @@ pg_status pg_seq_result_kernel_ms(const pg_seq_result* r, float* ms) {
 }
 
 }  // extern "C"
+
+// ====================================================================== calibration
+struct pg_calib {
+  int device = 0;
+  cudaStream_t st = nullptr, own_st = nullptr;
+  Pool pool;
+  uint32_t n_rep = 0, K = 0, J = 0, C = 0, P = 0, n_chunks = 0;
+  DBuf<int32_t> alt, depth, cls;
+  DBuf<uint64_t> site_off, chunk_start;
+  DBuf<uint32_t> chunk_rep, rep_first_chunk, step;
+  DBuf<float> sig, epoch_w, phi, partial, m, v;
+  std::vector<uint32_t> rep_first_chunk_h;
+  uint32_t part_stride = 0;
+  cudaGraphExec_t graph = nullptr;
+  struct { float* params = nullptr; uint32_t steps = 0; float lr = 0, b1 = 0, b2 = 0, eps = 0; float* nll = nullptr; cudaStream_t st = nullptr; } gkey;
+  pg::CalibArgs args() const {
+    pg::CalibArgs a{};
+    a.K = K; a.J = J; a.C = C; a.P = P;
+    a.alt = alt.p; a.depth = depth.p; a.cls = cls.p; a.site_off = site_off.p;
+    a.sig = sig.p; a.epoch_w = epoch_w.p; a.phi = phi.p;
+    a.chunk = 4096; a.part_stride = part_stride;
+    return a;
+  }
+  ~pg_calib() {
+    if (graph) cudaGraphExecDestroy(graph);
+    alt.reset(); depth.reset(); cls.reset(); site_off.reset(); chunk_start.reset(); chunk_rep.reset();
+    rep_first_chunk.reset(); step.reset(); sig.reset(); epoch_w.reset(); phi.reset(); partial.reset(); m.reset();
+    v.reset();
+    pool.release_all();
+    if (own_st) cudaStreamDestroy(own_st);
+  }
+};
+
+extern "C" {
+
+pg_status pg_calib_create(uint32_t n_rep, const uint64_t* site_off, const int32_t* alt, const int32_t* depth,
+                          const int32_t* cls, uint32_t K, uint32_t J, uint32_t C, const double* signatures,
+                          const double* epoch_weight, const double* phi, pg_calib** out) {
+  return guarded([&] {
+    require(out && site_off && signatures && epoch_weight && phi, "NULL argument");
+    require(n_rep >= 1, "at least one replicate");
+    require(K >= 1 && K <= 8 && J >= 1 && J <= 8 && C >= 1 && C <= 128, "K and J in [1, 8], C in [1, 128]");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); throw CudaError("no CUDA device"); }
+    const uint64_t n = site_off[n_rep];
+    require(site_off[0] == 0, "site offsets start at 0");
+    for (uint32_t r = 0; r < n_rep; ++r) require(site_off[r + 1] >= site_off[r], "site offsets must not decrease");
+    require(n == 0 || (alt && depth && cls), "NULL site arrays");
+    for (uint64_t i = 0; i < n; ++i) {
+      require(depth[i] >= 0 && alt[i] >= 0 && alt[i] <= depth[i], "sites need 0 <= alt <= depth");
+      require(cls[i] >= 0 && uint32_t(cls[i]) < C, "site class out of range");
+    }
+    for (uint64_t x = 0; x < uint64_t(J) * C; ++x) require(signatures[x] >= 0, "signature probabilities >= 0");
+    for (uint64_t x = 0; x < uint64_t(n_rep) * K; ++x) {
+      require(epoch_weight[x] > 0, "epoch weights must be positive");
+      require(phi[x] > 0 && phi[x] <= 1, "phi must be in (0, 1]");
+    }
+    auto c = std::make_unique<pg_calib>();
+    ck(cudaGetDevice(&c->device), "cudaGetDevice");
+    ck(cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking), "stream");
+    c->st = c->own_st;
+    c->n_rep = n_rep; c->K = K; c->J = J; c->C = C; c->P = K + K * J + 1;
+    Pool* P = &c->pool;
+    cudaStream_t st = c->st;
+    std::vector<int32_t> va(alt, alt + n), vd(depth, depth + n), vc(cls, cls + n);
+    c->alt = upload(P, va, st); c->depth = upload(P, vd, st); c->cls = upload(P, vc, st);
+    c->site_off = upload(P, std::vector<uint64_t>(site_off, site_off + n_rep + 1), st);
+    std::vector<float> fs(uint64_t(J) * C), fw(uint64_t(n_rep) * K), fp(uint64_t(n_rep) * K);
+    for (uint32_t j = 0; j < J; ++j) {   // signatures normalised to sum 1 over the classes
+      double tot = 0;
+      for (uint32_t k = 0; k < C; ++k) tot += signatures[uint64_t(j) * C + k];
+      require(tot > 0, "a signature has no mass");
+      for (uint32_t k = 0; k < C; ++k) fs[uint64_t(j) * C + k] = float(signatures[uint64_t(j) * C + k] / tot);
+    }
+    for (uint64_t x = 0; x < fw.size(); ++x) { fw[x] = float(epoch_weight[x]); fp[x] = float(phi[x]); }
+    c->sig = upload(P, fs, st); c->epoch_w = upload(P, fw, st); c->phi = upload(P, fp, st);
+    // chunks of 4096 sites, never across replicates
+    std::vector<uint32_t> crep;
+    std::vector<uint64_t> cstart;
+    c->rep_first_chunk_h.assign(n_rep + 1, 0);
+    for (uint32_t r = 0; r < n_rep; ++r) {
+      c->rep_first_chunk_h[r] = uint32_t(crep.size());
+      for (uint64_t i = site_off[r]; i < site_off[r + 1]; i += 4096) { crep.push_back(r); cstart.push_back(i); }
+    }
+    c->rep_first_chunk_h[n_rep] = uint32_t(crep.size());
+    c->n_chunks = uint32_t(crep.size());
+    c->chunk_rep = upload(P, crep, st); c->chunk_start = upload(P, cstart, st);
+    c->rep_first_chunk = upload(P, c->rep_first_chunk_h, st);
+    c->part_stride = (1 + 2 * K + K * C + 3) & ~3u;
+    c->partial = DBuf<float>(P, uint64_t(std::max<uint32_t>(c->n_chunks, 1)) * c->part_stride);
+    c->m = DBuf<float>(P, uint64_t(n_rep) * c->P);
+    c->v = DBuf<float>(P, uint64_t(n_rep) * c->P);
+    c->step = DBuf<uint32_t>(P, n_rep);
+    ck(cudaStreamSynchronize(st), "calibration upload");
+    *out = c.release();
+  });
+}
+
+pg_status pg_calib_destroy(pg_calib* c) {
+  return guarded([&] { if (c) { cudaSetDevice(c->device); delete c; } });
+}
+
+pg_status pg_calib_num_params(const pg_calib* c, uint32_t* P) {
+  return guarded([&] { require(c && P, "NULL argument"); *P = c->P; });
+}
+
+pg_status pg_calib_set_stream(pg_calib* c, void* stream) {
+  return guarded([&] {
+    require(c != nullptr, "NULL handle");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    ck(cudaStreamSynchronize(c->st), "stream switch");
+    c->st = stream ? static_cast<cudaStream_t>(stream) : c->own_st;
+  });
+}
+
+pg_status pg_calib_nll_grad(pg_calib* c, const float* params, float* nll, float* grad) {
+  return guarded([&] {
+    require(c && params, "NULL argument");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    pg::AdamArgs no{};
+    pg::calib_launch(c->args(), const_cast<float*>(params), c->chunk_rep.p, c->chunk_start.p, c->n_chunks,
+                     c->rep_first_chunk.p, c->n_rep, c->partial.p, nll, grad, no, c->st);
+    ck(cudaGetLastError(), "calibration kernels");
+  });
+}
+
+pg_status pg_calib_nll_grad_one(pg_calib* c, uint32_t rep, const float* params, float* nll, float* grad) {
+  return guarded([&] {
+    require(c && params, "NULL argument");
+    require(rep < c->n_rep, "replicate out of range");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    pg::CalibArgs a = c->args();
+    a.chunk0 = c->rep_first_chunk_h[rep];
+    a.rep0 = rep;
+    pg::AdamArgs no{};
+    pg::calib_launch(a, const_cast<float*>(params), c->chunk_rep.p, c->chunk_start.p,
+                     c->rep_first_chunk_h[rep + 1] - c->rep_first_chunk_h[rep], c->rep_first_chunk.p, 1,
+                     c->partial.p, nll, grad, no, c->st);
+    ck(cudaGetLastError(), "calibration kernels");
+  });
+}
+
+pg_status pg_calib_adam(pg_calib* c, float* params, uint32_t steps, float lr, float beta1, float beta2, float eps,
+                        float* nll) {
+  return guarded([&] {
+    require(c && params, "NULL argument");
+    require(steps >= 1 && steps <= 100000, "steps in [1, 100000]");
+    require(lr > 0 && beta1 >= 0 && beta1 < 1 && beta2 >= 0 && beta2 < 1 && eps > 0, "invalid Adam hyperparameters");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t st = c->st;
+    ck(cudaMemsetAsync(c->m.p, 0, sizeof(float) * c->n_rep * c->P, st), "memset");
+    ck(cudaMemsetAsync(c->v.p, 0, sizeof(float) * c->n_rep * c->P, st), "memset");
+    ck(cudaMemsetAsync(c->step.p, 0, sizeof(uint32_t) * c->n_rep, st), "memset");
+    const bool same = c->graph && c->gkey.params == params && c->gkey.steps == steps && c->gkey.lr == lr &&
+                      c->gkey.b1 == beta1 && c->gkey.b2 == beta2 && c->gkey.eps == eps && c->gkey.nll == nll &&
+                      c->gkey.st == st;
+    if (!same) {
+      if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+      pg::AdamArgs ad{c->m.p, c->v.p, c->step.p, lr, beta1, beta2, eps};
+      cudaGraph_t g = nullptr;
+      const uint64_t counted = g_launches.load();   // captured kernels are not launches yet
+      ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+      for (uint32_t s = 0; s < steps; ++s)
+        pg::calib_launch(c->args(), params, c->chunk_rep.p, c->chunk_start.p, c->n_chunks, c->rep_first_chunk.p,
+                         c->n_rep, c->partial.p, s + 1 == steps ? nll : nullptr, nullptr, ad, st);
+      const cudaError_t ce = cudaStreamEndCapture(st, &g);
+      ck(ce, "end capture");
+      const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      ck(ie, "graph instantiate");
+      c->gkey = {params, steps, lr, beta1, beta2, eps, nll, st};
+      g_launches.store(counted);
+    }
+    ck(cudaGraphLaunch(c->graph, st), "graph launch");
+    pg::note_launch(2 * steps);
+    ck(cudaGetLastError(), "calibration graph");
+  });
+}
+
+}  // extern "C"

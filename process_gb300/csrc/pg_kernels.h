@@ -143,10 +143,27 @@ void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st);
 
 // ---------------------------------------------------------------- calibration
-struct CalibDims {
-  uint32_t K;        // epochs
-  uint32_t J;        // signatures
-  uint32_t C;        // classes
+struct CalibArgs {
+  uint32_t K, J, C, P;          // epochs, signatures, classes, parameters per replicate
+  const int32_t* alt;           // sites of all replicates, concatenated
+  const int32_t* depth;
+  const int32_t* cls;
+  const uint64_t* site_off;     // n_rep + 1
+  const float* sig;             // J x C
+  const float* epoch_w;         // n_rep x K  (L_k: relative length of epoch k)
+  const float* phi;             // n_rep x K  (mean cellular fraction of epoch-k mutations)
+  uint32_t chunk;               // sites per CTA
+  uint32_t part_stride;         // floats per chunk partial (>= 1 + 2K + K C)
+  uint32_t chunk0, rep0;        // first chunk / replicate of a launch (sub-range launches)
 };
+struct AdamArgs {               // m == nullptr: no optimizer step
+  float* m; float* v; uint32_t* step;
+  float lr, beta1, beta2, eps;
+};
+// k_calib_sites over chunks [a.chunk0, a.chunk0 + n_chunks), then the
+// epilogue for replicates [a.rep0, a.rep0 + n_rep)
+void calib_launch(const CalibArgs& a, float* params, const uint32_t* chunk_rep, const uint64_t* chunk_start,
+                  uint32_t n_chunks, const uint32_t* rep_first_chunk, uint32_t n_rep, float* partial, float* nll,
+                  float* grad, const AdamArgs& adam, cudaStream_t st);
 
 }  // namespace pg
