@@ -161,6 +161,74 @@ def reference_arm(args):
     return 0
 
 
+def calibration_bench(world: int, n_rep: int = 512, n_sites: int = 100_000, steps: int = 200):
+    """Batched calibration (512 replicates x 1e5 sites, Poisson depth means
+    U(30, 200), K=4, 3 exposures): gradient evaluations per second of the
+    batched kernels, of the graph-captured Adam loop, and of the per-instance
+    path (one launch pair per replicate), plus the FP64 CPU oracle."""
+    import torch
+
+    import oracle.calib as oc
+    from process_gb300 import calib
+    rng = np.random.default_rng(5)
+    d = calib.synthetic(n_rep, n_sites, rng.uniform(30, 200, n_rep), seed=5)
+    b = calib.batch_of(d)
+    s = b.stream
+    p0 = torch.tensor(d.true_params + rng.normal(0, 0.3, d.true_params.shape), dtype=torch.float32, device="cuda")
+    # batched gradient evaluations (every replicate per launch pair)
+    for _ in range(3):
+        b.nll_grad(p0)
+    torch.cuda.synchronize()
+    reps = 20
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(s)
+    with torch.cuda.stream(s):
+        for _ in range(reps):
+            b.nll_grad(p0)
+    ev[1].record(s)
+    ev[1].synchronize()
+    t_batched = ev[0].elapsed_time(ev[1]) / 1000.0 / reps
+    # 200 Adam steps under one CUDA graph
+    p = p0.clone()
+    b.adam(p, steps)
+    p = p0.clone()
+    torch.cuda.synchronize()
+    ev[0].record(s)
+    with torch.cuda.stream(s):
+        b.adam(p, steps)
+    ev[1].record(s)
+    ev[1].synchronize()
+    t_adam = ev[0].elapsed_time(ev[1]) / 1000.0
+    # per-instance path: one replicate per call, the caller waiting for each
+    n_one = min(64, n_rep)
+    for r in range(2):
+        b.nll_grad_one(r, p0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in range(n_one):
+        b.nll_grad_one(r, p0)
+        torch.cuda.synchronize()
+    t_one = (time.perf_counter() - t0) / n_one
+    # FP64 CPU oracle, one replicate
+    r0 = (d.alt[: n_sites], d.depth[: n_sites], d.cls[: n_sites], d.signatures, d.epoch_weight[0], d.phi[0], 4, 3)
+    t0 = time.perf_counter()
+    oc.nll_grad(d.true_params[0], *r0)
+    t_cpu = time.perf_counter() - t0
+    n_sites_total = int(d.site_off[-1])
+    peak, _ = peaks()
+    achieved = 12.0 * n_sites_total / t_batched / 1e9
+    return {"workload": f"{n_rep} replicates x {n_sites} sites, depth Poisson(U(30,200)), K=4, J=3",
+            "grad_evals_per_s_batched": world * n_rep / t_batched,
+            "grad_evals_per_s_adam_graph": world * n_rep * steps / t_adam,
+            "grad_evals_per_s_per_instance": world / t_one,
+            "batched_over_per_instance": t_one / (t_batched / n_rep),
+            "adam_200_steps_ms": t_adam * 1000.0,
+            "cpu_fp64_grad_evals_per_s_1core": 1.0 / t_cpu,
+            "roofline": {"kernel": "k_calib_sites+k_calib_epilogue", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "per_unit": "12 B/site (alt, depth, class)"}}
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -265,6 +333,8 @@ def gpu_arm(args):
     e2e_s = time.perf_counter() - t0
     e2e_value = world * e2e_reads / e2e_s
 
+    cal = None if args.no_calibration else calibration_bench(world, args.calib_replicates)
+
     line = None
     if rank == 0:
         cpu = None
@@ -298,6 +368,7 @@ def gpu_arm(args):
             "e2e": {"value": e2e_value, "unit": "reads/s", "h2d_bytes_per_step": forest_bytes,
                     "d2h_bytes_per_step": d2h // max(1, e2e_steps)},
             "gpu_launches": n_launch,
+            "calibration": cal,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
@@ -314,6 +385,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-calibration", action="store_true")
+    ap.add_argument("--calib-replicates", type=int, default=512)
     ap.add_argument("--genome-scale", type=float, default=1.0,
                     help="fraction of the 3.1 Gbp genome (profiling runs on smaller cases; 1.0 for the bench)")
     args = ap.parse_args()

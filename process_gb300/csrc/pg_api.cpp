@@ -1141,6 +1141,8 @@ pg_status pg_seq_result_kernel_ms(const pg_seq_result* r, float* ms) {
 }  // extern "C"
 
 // ====================================================================== calibration
+constexpr uint32_t CALIB_CHUNK = 8192;   // sites per CTA of the site kernel
+
 struct pg_calib {
   int device = 0;
   cudaStream_t st = nullptr, own_st = nullptr;
@@ -1159,7 +1161,7 @@ struct pg_calib {
     a.K = K; a.J = J; a.C = C; a.P = P;
     a.alt = alt.p; a.depth = depth.p; a.cls = cls.p; a.site_off = site_off.p;
     a.sig = sig.p; a.epoch_w = epoch_w.p; a.phi = phi.p;
-    a.chunk = 4096; a.part_stride = part_stride;
+    a.chunk = CALIB_CHUNK; a.part_stride = part_stride;
     return a;
   }
   ~pg_calib() {
@@ -1215,13 +1217,13 @@ pg_status pg_calib_create(uint32_t n_rep, const uint64_t* site_off, const int32_
     }
     for (uint64_t x = 0; x < fw.size(); ++x) { fw[x] = float(epoch_weight[x]); fp[x] = float(phi[x]); }
     c->sig = upload(P, fs, st); c->epoch_w = upload(P, fw, st); c->phi = upload(P, fp, st);
-    // chunks of 4096 sites, never across replicates
+    // chunks of CALIB_CHUNK sites, never across replicates
     std::vector<uint32_t> crep;
     std::vector<uint64_t> cstart;
     c->rep_first_chunk_h.assign(n_rep + 1, 0);
     for (uint32_t r = 0; r < n_rep; ++r) {
       c->rep_first_chunk_h[r] = uint32_t(crep.size());
-      for (uint64_t i = site_off[r]; i < site_off[r + 1]; i += 4096) { crep.push_back(r); cstart.push_back(i); }
+      for (uint64_t i = site_off[r]; i < site_off[r + 1]; i += CALIB_CHUNK) { crep.push_back(r); cstart.push_back(i); }
     }
     c->rep_first_chunk_h[n_rep] = uint32_t(crep.size());
     c->n_chunks = uint32_t(crep.size());

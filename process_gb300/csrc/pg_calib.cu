@@ -61,7 +61,7 @@ __device__ void calib_tables(const CalibArgs& a, uint32_t r, const float* __rest
       num += e * a.sig[j * C + c];
     }
     const float M = num / den;
-    logpi[x] = p[k] + logf(a.epoch_w[r * K + k]) + logf(fmaxf(M, 1e-30f)) - lZ;
+    logpi[c * K + k] = p[k] + logf(a.epoch_w[r * K + k]) + logf(fmaxf(M, 1e-30f)) - lZ;   // class-major
   }
   if (threadIdx.x < K) {
     const float v = sig * a.phi[r * K + threadIdx.x] * 0.5f;
@@ -70,83 +70,120 @@ __device__ void calib_tables(const CalibArgs& a, uint32_t r, const float* __rest
   }
 }
 
+// K floats as one vector access where K is a multiple of 4
+template <uint32_t K, bool V = (K % 4 == 0)> struct KVec {
+  using type = float;
+  __device__ static void load(const float* p, float* v) {
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) v[k] = p[k];
+  }
+  __device__ static void add(float* p, const float* v) {
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) p[k] += v[k];
+  }
+};
+template <uint32_t K> struct KVec<K, true> {
+  using type = float4;
+  __device__ static void load(const float* p, float* v) {
+#pragma unroll
+    for (uint32_t k = 0; k < K; k += 4) {
+      const float4 x = *reinterpret_cast<const float4*>(p + k);
+      v[k] = x.x; v[k + 1] = x.y; v[k + 2] = x.z; v[k + 3] = x.w;
+    }
+  }
+  __device__ static void add(float* p, const float* v) {
+#pragma unroll
+    for (uint32_t k = 0; k < K; k += 4) {
+      float4 x = *reinterpret_cast<float4*>(p + k);
+      x.x += v[k]; x.y += v[k + 1]; x.z += v[k + 2]; x.w += v[k + 3];
+      *reinterpret_cast<float4*>(p + k) = x;
+    }
+  }
+};
+
+// Per-site work: every thread takes sites i0 + tid, i0 + tid + 256, ...
+// (coalesced), keeps plain FP32 sums over its ~32 sites, and adds its
+// responsibilities straight into its warp's class bins; lanes of one warp
+// that share a class add theirs in lane order (deterministic).  The sums are
+// compensated from the warp level on.
+template <uint32_t K>
 __global__ void __launch_bounds__(CAL_THREADS) k_calib_sites(CalibArgs a, const float* __restrict__ params,
                                                              const uint32_t* __restrict__ chunk_rep,
                                                              const uint64_t* __restrict__ chunk_start,
                                                              float* __restrict__ partial) {
-  __shared__ float s_logpi[CAL_MAXK * CAL_MAXC];
-  __shared__ float s_lv[CAL_MAXK], s_l1v[CAL_MAXK];
-  __shared__ float s_bins[CAL_WARPS][CAL_MAXK * CAL_MAXC];
-  __shared__ float s_gam[CAL_WARPS][32][CAL_MAXK];
-  __shared__ float s_red[CAL_WARPS][2 + 4 * CAL_MAXK];
+  __shared__ __align__(16) float s_logpi[K * CAL_MAXC];
+  __shared__ float s_lv[K], s_l1v[K];
+  __shared__ __align__(16) float s_bins[CAL_WARPS][K * CAL_MAXC];
+  __shared__ float s_red[CAL_WARPS][2 + 4 * K];
   const uint32_t chunk = a.chunk0 + blockIdx.x;
   const uint32_t r = chunk_rep[chunk];
   const uint64_t i0 = chunk_start[chunk];
   const uint64_t i1 = min(i0 + a.chunk, a.site_off[r + 1]);
-  const uint32_t K = a.K, C = a.C, P = a.P;
+  const uint32_t C = a.C, P = a.P;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   calib_tables(a, r, params + uint64_t(r) * P, s_logpi, s_lv, s_l1v);
   for (uint32_t x = lane; x < K * C; x += 32) s_bins[warp][x] = 0.f;
   __syncthreads();
-  Neu nll, A[CAL_MAXK], B[CAL_MAXK];
-  for (uint64_t base = i0 + uint64_t(warp) * 32; base < i1; base += uint64_t(CAL_WARPS) * 32) {
+  float lv[K], l1v[K];
+#pragma unroll
+  for (uint32_t k = 0; k < K; ++k) { lv[k] = s_lv[k]; l1v[k] = s_l1v[k]; }
+  float nll = 0.f, A[K], B[K];
+#pragma unroll
+  for (uint32_t k = 0; k < K; ++k) { A[k] = 0.f; B[k] = 0.f; }
+  float* bins = s_bins[warp];
+  // log pi and the bins are class-major ([c][k]): one vector access per site
+  using VecK = typename KVec<K>::type;
+  for (uint64_t base = i0 + (threadIdx.x & ~31u); base < i1; base += CAL_THREADS) {
     const uint64_t i = base + lane;
     const bool act = i < i1;
     int32_t c = -1;
-    float g[CAL_MAXK];
+    float g[K];
     if (act) {
-      const float al = float(a.alt[i]), dl = float(a.depth[i]);
-      c = a.cls[i];
-      float t[CAL_MAXK];
-      float tmax = -INFINITY;
+      const float al = float(__ldg(a.alt + i)), dl = float(__ldg(a.depth + i));
+      c = __ldg(a.cls + i);
+      float t[K], tmax = -INFINITY;
+      KVec<K>::load(s_logpi + c * K, t);
 #pragma unroll
-      for (uint32_t k = 0; k < CAL_MAXK; ++k) {
-        if (k < K) {
-          t[k] = s_logpi[k * C + c] + al * s_lv[k] + (dl - al) * s_l1v[k];
-          tmax = fmaxf(tmax, t[k]);
-        }
+      for (uint32_t k = 0; k < K; ++k) {
+        t[k] += al * lv[k] + (dl - al) * l1v[k];
+        tmax = fmaxf(tmax, t[k]);
       }
       float se = 0.f;
 #pragma unroll
-      for (uint32_t k = 0; k < CAL_MAXK; ++k) {
-        if (k < K) { g[k] = __expf(t[k] - tmax); se += g[k]; }
-      }
+      for (uint32_t k = 0; k < K; ++k) { g[k] = __expf(t[k] - tmax); se += g[k]; }
       const float inv = 1.f / se;
-      nll.add(-(tmax + __logf(se)));
+      nll -= tmax + __logf(se);
 #pragma unroll
-      for (uint32_t k = 0; k < CAL_MAXK; ++k) {
-        if (k < K) {
-          g[k] *= inv;
-          A[k].add(g[k] * al);
-          B[k].add(g[k] * (dl - al));
-        }
-      }
+      for (uint32_t k = 0; k < K; ++k) { g[k] *= inv; A[k] += g[k] * al; B[k] += g[k] * (dl - al); }
     }
-    // class bins: lanes with the same class add their gammas in lane order
-#pragma unroll
-    for (uint32_t k = 0; k < CAL_MAXK; ++k) if (k < K) s_gam[warp][lane][k] = act ? g[k] : 0.f;
-    __syncwarp();
     const uint32_t peers = __match_any_sync(0xffffffffu, c);
-    if (act && lane == uint32_t(__ffs(peers) - 1)) {
-      for (uint32_t k = 0; k < K; ++k) {
-        float sum = 0.f;
-        for (uint32_t m = peers; m; m &= m - 1) sum += s_gam[warp][__ffs(m) - 1][k];
-        s_bins[warp][k * C + c] += sum;
+    if (act) {
+      if ((peers & (peers - 1)) == 0) {              // the only lane with this class
+        KVec<K>::add(bins + c * K, g);
+      } else {                                         // shared class: sum in lane order
+        float sum[K];
+#pragma unroll
+        for (uint32_t k = 0; k < K; ++k) sum[k] = 0.f;
+        for (uint32_t m = peers; m; m &= m - 1) {
+          const int src = __ffs(m) - 1;
+#pragma unroll
+          for (uint32_t k = 0; k < K; ++k) sum[k] += __shfl_sync(peers, g[k], src);
+        }
+        if (lane == uint32_t(__ffs(peers) - 1)) KVec<K>::add(bins + c * K, sum);
       }
     }
     __syncwarp();
+    (void)sizeof(VecK);
   }
-  // block partial: per-thread sums reduced in a fixed order
+  // block partial: warp sums, then a compensated sum over the warps
   float* out = partial + uint64_t(chunk) * a.part_stride;
   {
-    float vals[2 + 4 * CAL_MAXK];
-    vals[0] = nll.s; vals[1] = nll.c;
+    float vals[1 + 2 * K];
+    vals[0] = nll;
 #pragma unroll
-    for (uint32_t k = 0; k < CAL_MAXK; ++k) {
-      vals[2 + 4 * k] = A[k].s; vals[3 + 4 * k] = A[k].c; vals[4 + 4 * k] = B[k].s; vals[5 + 4 * k] = B[k].c;
-    }
-    const uint32_t nv = 2 + 4 * K;
-    for (uint32_t q = 0; q < nv; ++q) {
+    for (uint32_t k = 0; k < K; ++k) { vals[1 + k] = A[k]; vals[1 + K + k] = B[k]; }
+#pragma unroll
+    for (uint32_t q = 0; q < 1 + 2 * K; ++q) {
       float v = vals[q];
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -154,24 +191,16 @@ __global__ void __launch_bounds__(CAL_THREADS) k_calib_sites(CalibArgs a, const 
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    Neu t0;
-    for (uint32_t w = 0; w < CAL_WARPS; ++w) { t0.add(s_red[w][0]); t0.add(s_red[w][1]); }
-    out[0] = t0.value();
-    for (uint32_t k = 0; k < K; ++k) {
-      Neu ta, tb;
-      for (uint32_t w = 0; w < CAL_WARPS; ++w) {
-        ta.add(s_red[w][2 + 4 * k]); ta.add(s_red[w][3 + 4 * k]);
-        tb.add(s_red[w][4 + 4 * k]); tb.add(s_red[w][5 + 4 * k]);
-      }
-      out[1 + k] = ta.value();
-      out[1 + K + k] = tb.value();
-    }
+  if (threadIdx.x < 1 + 2 * K) {
+    Neu t;
+    for (uint32_t w = 0; w < CAL_WARPS; ++w) t.add(s_red[w][threadIdx.x]);
+    out[threadIdx.x] = t.value();
   }
   for (uint32_t x = threadIdx.x; x < K * C; x += blockDim.x) {
-    float sum = 0.f;
-    for (uint32_t w = 0; w < CAL_WARPS; ++w) sum += s_bins[w][x];
-    out[1 + 2 * K + x] = sum;
+    const uint32_t k = x / C, c = x % C;
+    Neu t;
+    for (uint32_t w = 0; w < CAL_WARPS; ++w) t.add(s_bins[w][c * K + k]);
+    out[1 + 2 * K + x] = t.value();
   }
 }
 
@@ -263,7 +292,11 @@ void calib_launch(const CalibArgs& a, float* params, const uint32_t* chunk_rep, 
                   uint32_t n_chunks, const uint32_t* rep_first_chunk, uint32_t n_rep, float* partial, float* nll,
                   float* grad, const AdamArgs& adam, cudaStream_t st) {
   if (n_chunks) {
-    k_calib_sites<<<n_chunks, CAL_THREADS, 0, st>>>(a, params, chunk_rep, chunk_start, partial);
+    switch (a.K) {
+#define PG_CALIB_K(KK) case KK: k_calib_sites<KK><<<n_chunks, CAL_THREADS, 0, st>>>(a, params, chunk_rep, chunk_start, partial); break;
+      PG_CALIB_K(1) PG_CALIB_K(2) PG_CALIB_K(3) PG_CALIB_K(4) PG_CALIB_K(5) PG_CALIB_K(6) PG_CALIB_K(7) PG_CALIB_K(8)
+#undef PG_CALIB_K
+    }
     note_launch();
   }
   if (n_rep) {
