@@ -140,10 +140,20 @@ pg_status pg_engine_set_species_mutant(pg_engine* eng, uint32_t species, uint32_
  * allele < 0 = random allele. */
 pg_status pg_engine_add_driver_sid(pg_engine* eng, uint32_t mutant, uint32_t chr_index, uint32_t chr_pos,
                                    const char* ref, const char* alt, int32_t allele);
-/* Driver CNA (src/cna.cpp:21-138) and whole-genome doubling (src/wg_doubling.hpp). */
+/* Driver CNA (CNA(type, chr, chr_pos, len, allele, src_allele), src/cna.cpp:21-138)
+ * and whole-genome doubling (src/wg_doubling.hpp:28-40), appended to the
+ * mutant's driver list in application order.  Alleles are ordinals among the
+ * allele instances covering the region start (-1 = random). */
 pg_status pg_engine_add_driver_cna(pg_engine* eng, uint32_t mutant, int type_amplification, uint32_t chr_index,
                                    uint32_t begin, uint32_t length, int32_t allele, int32_t src_allele);
 pg_status pg_engine_add_driver_wgd(pg_engine* eng, uint32_t mutant);
+/* Passenger CNA candidate (load_passenger_CNAs, src/mutation_engine.cpp:441-487):
+ * each passenger CNA event draws one candidate uniformly. */
+pg_status pg_engine_add_passenger_cna(pg_engine* eng, uint32_t chr_index, uint32_t begin, uint32_t length,
+                                      int type_amplification);
+/* avoid_homozygous_losses (src/mutation_engine.cpp:1356, src/mutations.cpp:837-840):
+ * passenger deletions never remove the last allele of a region. */
+pg_status pg_engine_set_avoid_homozygous_losses(pg_engine* eng, int on);
 /* infinite_sites_model property (src/mutation_engine.hpp:148-156). */
 pg_status pg_engine_set_infinite_sites(pg_engine* eng, int on);
 pg_status pg_engine_get_infinite_sites(const pg_engine* eng, int* on);
@@ -169,7 +179,20 @@ pg_status pg_placed_count(const pg_placed* placed, uint64_t* n_mutations);
 /* Placed mutations sorted by (absolute locus, slot); any pointer may be NULL.
  * aux: SNV alt base code; indel bit0 = insertion, bits1-3 = length, bits 8.. inserted bases. */
 pg_status pg_placed_copy(const pg_placed* placed, uint32_t* locus, uint32_t* edge, uint32_t* aux, uint8_t* cls,
-                         uint8_t* sig, uint8_t* allele, uint8_t* kind, uint8_t* nature);
+                         uint8_t* sig, uint16_t* allele, uint8_t* kind, uint8_t* nature);
+/* Applied CNA / WGD events (type 0 deletion, 1 amplification, 2 WGD), with
+ * the edge (node) they happened on, their 1-based inclusive region, the
+ * allele instance they created (amplification) or acted on (deletion) and its
+ * source instance, and whether they are drivers: the rows of the reference's
+ * get_sampled_cell_CNAs (src/phylogenetic_forest.cpp:509-562) before they are
+ * expanded per cell. */
+pg_status pg_placed_cna_count(const pg_placed* placed, uint64_t* n);
+pg_status pg_placed_cna_copy(const pg_placed* placed, uint32_t* node, uint8_t* type, uint32_t* chr, uint32_t* begin,
+                             uint32_t* end, uint32_t* allele, uint32_t* src_allele, uint8_t* driver);
+/* Genotype class of every node (n_nodes entries) and the class count / the
+ * largest copy number of any position. */
+pg_status pg_placed_node_classes(const pg_placed* placed, uint32_t* node_class, uint32_t* n_classes,
+                                 uint32_t* cn_max);
 /* Device time of the placement kernels of the last place call (ms). */
 pg_status pg_placed_kernel_ms(const pg_placed* placed, float* ms);
 

@@ -32,8 +32,8 @@ def lib() -> C.CDLL:
             build()
         L = C.CDLL(str(LIB_PATH))
         P = C.c_void_p
-        u8p, u32p, i32p, u64p, f64p = (C.POINTER(t) for t in (C.c_uint8, C.c_uint32, C.c_int32, C.c_uint64,
-                                                                C.c_double))
+        u8p, u16p, u32p, i32p, u64p, f64p = (C.POINTER(t) for t in (C.c_uint8, C.c_uint16, C.c_uint32, C.c_int32,
+                                                                      C.c_uint64, C.c_double))
         sig = {
             "orc_last_error": (C.c_char_p, []),
             "orc_philox": (None, [C.c_uint32] * 6 + [u32p]),
@@ -51,18 +51,26 @@ def lib() -> C.CDLL:
             "orc_engine_read_genome": (None, [P, u8p]),
             "orc_engine_set_signatures": (None, [P, C.c_int, C.c_uint32, f64p]),
             "orc_engine_add_exposure": (None, [P, C.c_int, C.c_double, f64p]),
-            "orc_engine_set_species_rates": (None, [P, C.c_uint32, C.c_double, C.c_double]),
+            "orc_engine_set_species_rates": (None, [P, C.c_uint32, C.c_double, C.c_double, C.c_double]),
             "orc_engine_set_species_epoch_rates": (None, [P, C.c_uint32, C.c_uint32, f64p, f64p]),
             "orc_engine_set_species_mutant": (None, [P, C.c_uint32, C.c_uint32]),
             "orc_engine_add_driver_sid": (None, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_char_p, C.c_char_p,
                                                  C.c_int32]),
             "orc_engine_set_infinite_sites": (None, [P, C.c_int]),
+            "orc_engine_add_driver_cna": (None, [P, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32,
+                                                 C.c_int32, C.c_int32]),
+            "orc_engine_add_driver_wgd": (None, [P, C.c_uint32]),
+            "orc_engine_add_passenger_cna": (None, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
+            "orc_engine_set_avoid_homozygous_losses": (None, [P, C.c_int]),
+            "orc_placed_cna_count": (C.c_uint64, [P]),
+            "orc_placed_cna_copy": (None, [P, u32p, u8p, u32p, u32p, u32p, u32p, u32p, u8p]),
+            "orc_placed_node_classes": (None, [P, u32p, u32p, u32p]),
             "orc_place": (P, [P, C.c_uint32, i32p, f64p, u32p, i32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32,
                               C.c_uint32, C.c_uint32, C.c_uint64, C.c_int]),
             "orc_placed_destroy": (None, [P]),
             "orc_placed_count": (C.c_uint64, [P]),
-            "orc_placed_copy": (None, [P, u32p, u32p, u32p, u8p, u8p, u8p, u8p, u8p]),
-            "orc_placed_set": (None, [P, C.c_uint64, u32p, u32p, u8p, u8p]),
+            "orc_placed_copy": (None, [P, u32p, u32p, u32p, u8p, u8p, u16p, u8p, u8p]),
+            "orc_placed_set": (C.c_int, [P, C.c_uint64, u32p, u32p, u16p, u8p]),
             "orc_seq": (P, [P, C.c_void_p, C.c_uint64, C.c_int, C.c_double, C.c_int]),
             "orc_seq_destroy": (None, [P]),
             "orc_seq_samples": (C.c_uint32, [P]),
@@ -116,13 +124,14 @@ class OracleEngine:
             per_epi = {"": rates} if keys <= {"SNV", "indel", "CNA"} else dict(rates)
             for epi, r in per_epi.items():
                 sid = species.setdefault((name, epi), len(species))
-                snv, indel = r.get("SNV", 0.0), r.get("indel", 0.0)
+                snv, indel, cna = r.get("SNV", 0.0), r.get("indel", 0.0), r.get("CNA", 0.0)
                 if np.ndim(snv) or np.ndim(indel):
                     n = max(np.size(snv), np.size(indel))
                     e.set_epoch_rates(sid, np.broadcast_to(np.asarray(snv, float), (n,)),
                                       np.broadcast_to(np.asarray(indel, float), (n,)))
+                    e.set_rates(sid, np.atleast_1d(snv)[0], np.atleast_1d(indel)[0], cna)
                 else:
-                    e.set_rates(sid, snv, indel)
+                    e.set_rates(sid, snv, indel, cna)
                 lib().orc_engine_set_species_mutant(e._h, sid, mut_id)
         e.species = species
         for t, coeffs in w.exposures:
@@ -146,8 +155,8 @@ class OracleEngine:
             if used:
                 lib().orc_engine_add_exposure(self._h, ty, float(time), _p(np.ascontiguousarray(v), C.c_double))
 
-    def set_rates(self, sid, snv, indel):
-        lib().orc_engine_set_species_rates(self._h, sid, float(snv), float(indel))
+    def set_rates(self, sid, snv, indel, cna=0.0):
+        lib().orc_engine_set_species_rates(self._h, sid, float(snv), float(indel), float(cna))
 
     def set_epoch_rates(self, sid, snv, indel):
         s = np.ascontiguousarray(snv, dtype=np.float64)
@@ -159,6 +168,34 @@ class OracleEngine:
 
     def set_infinite_sites(self, on):
         lib().orc_engine_set_infinite_sites(self._h, 1 if on else 0)
+
+    def add_driver_cna(self, mutant, amp, chr_idx, begin, length, allele=-1, src=-1):
+        lib().orc_engine_add_driver_cna(self._h, mutant, 1 if amp else 0, chr_idx, begin, length, allele, src)
+
+    def add_driver_wgd(self, mutant):
+        lib().orc_engine_add_driver_wgd(self._h, mutant)
+
+    def add_passenger_cna(self, chr_idx, begin, length, amp):
+        lib().orc_engine_add_passenger_cna(self._h, chr_idx, begin, length, 1 if amp else 0)
+
+    def set_avoid_homozygous_losses(self, on):
+        lib().orc_engine_set_avoid_homozygous_losses(self._h, 1 if on else 0)
+
+    def add_drivers(self, mutant, drivers, chr_index):
+        """Driver lists as given to process_gb300.MutationEngine.add_mutant
+        (SNV/Mutation with explicit ref, CNA, WGD); chr_index maps names."""
+        for d in drivers:
+            kind = type(d).__name__
+            if kind == "Mutation":
+                al = -1 if d.allele is None else int(d.allele)
+                lib().orc_engine_add_driver_sid(self._h, mutant, chr_index(d.chr), int(d.chr_pos), d.ref.encode(),
+                                                d.alt.encode(), al)
+            elif kind == "CNA":
+                self.add_driver_cna(mutant, d.type == "A", chr_index(d.chr), int(d.chr_pos), int(d.len),
+                                    -1 if d.allele is None else int(d.allele),
+                                    -1 if d.src_allele is None else int(d.src_allele))
+            else:
+                self.add_driver_wgd(mutant)
 
     def index_info(self):
         ct, it = np.zeros(32, np.uint64), np.zeros(83, np.uint64)
@@ -204,16 +241,34 @@ class OraclePlaced:
     def table(self) -> dict:
         n = lib().orc_placed_count(self._h)
         t = {k: np.empty(n, dtype=np.uint32) for k in ("locus", "edge", "aux")}
-        t.update({k: np.empty(n, dtype=np.uint8) for k in ("cls", "sig", "allele", "kind", "nature")})
+        t.update({k: np.empty(n, dtype=np.uint8) for k in ("cls", "sig", "kind", "nature")})
+        t["allele"] = np.empty(n, dtype=np.uint16)
         lib().orc_placed_copy(self._h, *(_p(t[k], C.c_uint32) for k in ("locus", "edge", "aux")),
-                              *(_p(t[k], C.c_uint8) for k in ("cls", "sig", "allele", "kind", "nature")))
+                              _p(t["cls"], C.c_uint8), _p(t["sig"], C.c_uint8), _p(t["allele"], C.c_uint16),
+                              _p(t["kind"], C.c_uint8), _p(t["nature"], C.c_uint8))
         return t
+
+    def cna_table(self) -> dict:
+        m = lib().orc_placed_cna_count(self._h)
+        t = {k: np.empty(m, dtype=np.uint32) for k in ("node", "chr", "begin", "end", "allele", "src")}
+        t.update({k: np.empty(m, dtype=np.uint8) for k in ("type", "driver")})
+        lib().orc_placed_cna_copy(self._h, _p(t["node"], C.c_uint32), _p(t["type"], C.c_uint8),
+                                  _p(t["chr"], C.c_uint32), _p(t["begin"], C.c_uint32), _p(t["end"], C.c_uint32),
+                                  _p(t["allele"], C.c_uint32), _p(t["src"], C.c_uint32), _p(t["driver"], C.c_uint8))
+        return t
+
+    def node_classes(self, n_nodes):
+        out = np.empty(n_nodes, dtype=np.uint32)
+        nc, cm = C.c_uint32(), C.c_uint32()
+        lib().orc_placed_node_classes(self._h, _p(out, C.c_uint32), C.byref(nc), C.byref(cm))
+        return out, nc.value, cm.value
 
     def set_table(self, t: dict):
         arrs = [np.ascontiguousarray(t[k], dtype=d) for k, d in
-                (("locus", np.uint32), ("edge", np.uint32), ("allele", np.uint8), ("kind", np.uint8))]
-        lib().orc_placed_set(self._h, len(arrs[0]), _p(arrs[0], C.c_uint32), _p(arrs[1], C.c_uint32),
-                             _p(arrs[2], C.c_uint8), _p(arrs[3], C.c_uint8))
+                (("locus", np.uint32), ("edge", np.uint32), ("allele", np.uint16), ("kind", np.uint8))]
+        if lib().orc_placed_set(self._h, len(arrs[0]), _p(arrs[0], C.c_uint32), _p(arrs[1], C.c_uint32),
+                                _p(arrs[2], C.c_uint16), _p(arrs[3], C.c_uint8)):
+            raise RuntimeError(_err())
 
     def sequence(self, cfg, seed, flavour=0, fraction=1.0, threads=1):
         """cfg: a process_gb300._lib.SeqCfg (same layout as the oracle's)."""

@@ -64,8 +64,8 @@ W4 philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint3
 }
 
 enum : uint32_t {
-  TAG_EDGE_SNV = 1, TAG_EDGE_INDEL = 2, TAG_SNV = 4, TAG_INDEL = 5, TAG_DRIVER = 6,
-  TAG_TILE_SPLIT = 7, TAG_PAIR = 8, TAG_PAIR2 = 9, TAG_ERR = 10, TAG_GENOME = 11
+  TAG_EDGE_SNV = 1, TAG_EDGE_INDEL = 2, TAG_EDGE_CNA = 3, TAG_SNV = 4, TAG_INDEL = 5, TAG_DRIVER = 6,
+  TAG_TILE_SPLIT = 7, TAG_PAIR = 8, TAG_PAIR2 = 9, TAG_ERR = 10, TAG_GENOME = 11, TAG_CNA = 12
 };
 
 static inline uint64_t index64(uint32_t hi, uint32_t lo, uint64_t n) {
@@ -312,8 +312,10 @@ void id_classes(const Genome& g, uint32_t p, int out[16]) {
 }
 
 // ------------------------------------------------------------ engine
-struct Species { double snv = 0, indel = 0; std::vector<double> snv_e, indel_e; uint32_t mutant = 0; bool has = false; };
+struct Species { double snv = 0, indel = 0, cna = 0; std::vector<double> snv_e, indel_e; uint32_t mutant = 0; bool has = false; };
 struct Driver { uint32_t chr, pos; std::string ref, alt; int32_t allele; };
+struct Cna { bool amp; uint32_t chr, begin, len; int32_t allele, src; };   // 1-based begin
+struct DriverEvent { int kind; Driver sid; Cna cna; };                      // 0 SID, 1 CNA, 2 WGD
 
 struct Engine {
   Genome g;
@@ -324,8 +326,10 @@ struct Engine {
   std::vector<double> sigs[2];
   std::map<double, std::vector<double>> expo[2];
   std::map<uint32_t, Species> species;
-  std::map<uint32_t, std::vector<Driver>> drivers;
+  std::map<uint32_t, std::vector<DriverEvent>> drivers;
+  std::vector<Cna> cands;                 // passenger CNA candidates
   bool infinite_sites = true;
+  bool avoid_losses = true;
 };
 
 void build_index(Engine& e) {
@@ -361,12 +365,73 @@ struct Forest {
   std::vector<uint8_t> is_leaf;
 };
 
+// ---- copy-number state.  A cell's genome maps every allele instance it
+// holds to the sorted, disjoint intervals [b, e) (absolute positions) the
+// instance still covers.  Instances 0 and 1 are the germline alleles; every
+// amplification or WGD copy creates the next instance id, in the order the
+// events are applied (nodes in index order, each node's events in order).
+using Ivl = std::vector<std::pair<uint32_t, uint32_t>>;
+using CellGenome = std::map<uint32_t, Ivl>;
+
+bool ivl_has(const Ivl& v, uint32_t p) {
+  auto it = std::upper_bound(v.begin(), v.end(), std::make_pair(p, 0xffffffffu));
+  return it != v.begin() && std::prev(it)->first <= p && p < std::prev(it)->second;
+}
+Ivl ivl_minus(const Ivl& v, uint32_t b, uint32_t e) {
+  Ivl out;
+  for (auto [x, y] : v) {
+    if (y <= b || x >= e) { out.push_back({x, y}); continue; }
+    if (x < b) out.push_back({x, b});
+    if (y > e) out.push_back({e, y});
+  }
+  return out;
+}
+Ivl ivl_within(const Ivl& v, uint32_t b, uint32_t e) {
+  Ivl out;
+  for (auto [x, y] : v) if (y > b && x < e) out.push_back({std::max(x, b), std::min(y, e)});
+  return out;
+}
+// instances covering p, ascending
+std::vector<uint32_t> covering(const CellGenome& g, uint32_t p) {
+  std::vector<uint32_t> out;
+  for (const auto& [inst, v] : g) if (ivl_has(v, p)) out.push_back(inst);
+  return out;
+}
+uint64_t genome_size(const CellGenome& g) {
+  uint64_t n = 0;
+  for (const auto& kv : g) for (auto [x, y] : kv.second) n += y - x;
+  return n;
+}
+// largest number of instances covering one position
+uint32_t max_copies(const CellGenome& g) {
+  std::vector<std::pair<uint32_t, int>> ev;
+  for (const auto& kv : g) for (auto [x, y] : kv.second) { ev.push_back({x, 1}); ev.push_back({y, -1}); }
+  std::sort(ev.begin(), ev.end());   // at equal positions ends (-1) come first
+  int cur = 0, best = 0;
+  for (auto [p, d] : ev) { cur += d; best = std::max(best, cur); }
+  return uint32_t(best);
+}
+
+// a copy made on edge `edge` by its event `event` (instance `made` from `from`)
+struct CopyRec { uint32_t edge, event, made, from; };
+
+struct CnaRec { uint32_t node; uint8_t type; uint32_t chr, begin, end, allele, src; uint8_t driver; };
+
 struct Placed {
   std::vector<uint32_t> locus, edge, aux;
-  std::vector<uint8_t> cls, sig, allele, kind, nature;
+  std::vector<uint8_t> cls, sig, kind, nature;
+  std::vector<uint16_t> allele;
+  std::vector<int32_t> order;      // position among the edge's events: driver index, -1 preneoplastic,
+                                   // INT32_MAX passengers (after every event of the edge)
   const Forest* forest = nullptr;
   const Engine* eng = nullptr;
   Forest forest_copy;
+  std::vector<CellGenome> classes{1};   // genotype classes, class 0 = germline
+  std::vector<uint32_t> node_class;     // per node (+ the preneoplastic edge: class 0)
+  std::vector<CopyRec> copies;
+  std::vector<CnaRec> cnas;
+  uint32_t n_inst = 2, cn_max = 2;
+  bool has_cna = false;
 };
 
 struct Tables {
@@ -439,35 +504,165 @@ uint32_t code(char c) {
   return 0;
 }
 
-struct DriverRec { uint32_t locus, edge, aux, allele; uint8_t kind; };
+struct DriverRec { uint32_t locus, edge, aux, allele; int32_t order; uint8_t kind; };
 
-std::vector<DriverRec> driver_records(const Engine& e, const Forest& f) {
-  std::vector<DriverRec> out;
-  auto mut_of = [&](uint32_t node) {
-    auto it = e.species.find(f.species[node]);
-    return it == e.species.end() ? 0u : it->second.mutant;
-  };
-  for (uint32_t v = 0; v < f.n; ++v) {
-    const uint32_t m = mut_of(v);
-    if (f.parent[v] >= 0 && mut_of(uint32_t(f.parent[v])) == m) continue;
-    auto it = e.drivers.find(m);
-    if (it == e.drivers.end()) continue;
-    for (const auto& d : it->second) {
-      DriverRec r{};
-      r.edge = v;
-      r.locus = e.g.off[d.chr] + d.pos - 1;
-      r.allele = d.allele < 0 ? 0xffu : uint32_t(d.allele);
-      if (d.ref.size() == 1 && d.alt.size() == 1) { r.kind = 0; r.aux = code(d.alt[0]); }
-      else {
-        r.kind = 1;
-        if (d.alt.size() > 1) {
-          uint32_t bases = 0;
-          for (size_t k = 1; k < d.alt.size(); ++k) bases |= code(d.alt[k]) << (2 * (k - 1));
-          r.aux = 1u | (uint32_t(d.alt.size() - 1) << 1) | (bases << 8);
-        } else {
-          r.aux = uint32_t(d.ref.size() - 1) << 1;
-        }
+// locus and descriptor of a driver SNV/indel (allele left to the caller)
+DriverRec driver_site(const Engine& e, const Driver& d, uint32_t edge) {
+  DriverRec r{};
+  r.edge = edge;
+  r.locus = e.g.off[d.chr] + d.pos - 1;
+  if (d.ref.size() == 1 && d.alt.size() == 1) { r.kind = 0; r.aux = code(d.alt[0]); }
+  else {
+    r.kind = 1;
+    if (d.alt.size() > 1) {
+      uint32_t bases = 0;
+      for (size_t k = 1; k < d.alt.size(); ++k) bases |= code(d.alt[k]) << (2 * (k - 1));
+      r.aux = 1u | (uint32_t(d.alt.size() - 1) << 1) | (bases << 8);
+    } else {
+      r.aux = uint32_t(d.ref.size() - 1) << 1;
+    }
+  }
+  return r;
+}
+
+uint32_t mutant_of(const Engine& e, const Forest& f, uint32_t node) {
+  auto it = e.species.find(f.species[node]);
+  return it == e.species.end() ? 0u : it->second.mutant;
+}
+// the driver list applied on edge v: the mutant's, on the first edge of its clone
+const std::vector<DriverEvent>* drivers_of(const Engine& e, const Forest& f, uint32_t v) {
+  const uint32_t m = mutant_of(e, f, v);
+  if (f.parent[v] >= 0 && mutant_of(e, f, uint32_t(f.parent[v])) == m) return nullptr;
+  auto it = e.drivers.find(m);
+  return it == e.drivers.end() ? nullptr : &it->second;
+}
+
+bool has_copy_number_events(const Engine& e) {
+  for (const auto& kv : e.drivers) for (const auto& d : kv.second) if (d.kind != 0) return true;
+  if (e.cands.empty()) return false;
+  for (const auto& kv : e.species) if (kv.second.cna > 0) return true;
+  return false;
+}
+
+// Applies every node's driver list (SNVs/indels, CNAs, WGD in declaration
+// order; src/mutation_engine.cpp:789-862, vignettes/mutations.Rmd:159-177)
+// and then its passenger CNAs (candidates of src/mutation_engine.cpp:441-487
+// at the species' CNA rate; with avoid_homozygous_losses a passenger deletion
+// never removes the last allele of a region, :1356) to the genome inherited
+// from the parent.  Fills the genotype classes, copies and CNA records of
+// `pl` and returns the driver SNVs/indels in node then event order.
+std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t seed, Placed& pl) {
+  const uint32_t N = f.n, k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
+  const uint32_t n_chr = uint32_t(e.g.off.size() - 1);
+  CellGenome germ;
+  for (uint32_t c = 0; c < n_chr; ++c)
+    if (e.g.off[c] < e.g.off[c + 1])
+      for (uint32_t a = 0; a < 2; ++a) germ[a].push_back({e.g.off[c], e.g.off[c + 1]});
+  pl.classes.assign(1, germ);
+  pl.node_class.assign(N + 1, 0);
+  pl.copies.clear(); pl.cnas.clear();
+  uint32_t n_inst = 2, n_sid = 0;
+  // passenger CNA counts: Poisson(rate * germline allelic size * divisions)
+  std::vector<uint64_t> n_pcna(N, 0);
+  if (!e.cands.empty()) {
+    const double germline = 2.0 * double(e.g.b.size());
+    for (uint32_t v = 0; v < N; ++v) {
+      auto it = e.species.find(f.species[v]);
+      const double rate = it == e.species.end() ? 0.0 : it->second.cna;
+      Stream st = stream(seed, 0, v, 0, TAG_EDGE_CNA);
+      n_pcna[v] = poisson(st, rate * germline * double(f.divisions[v]));
+    }
+  }
+  std::vector<DriverRec> drv;
+  for (uint32_t v = 0; v < N; ++v) {
+    const uint32_t base = f.parent[v] >= 0 ? pl.node_class[f.parent[v]] : 0u;
+    CellGenome g = pl.classes[base];
+    bool changed = false;
+    const auto* list = drivers_of(e, f, v);
+    const uint32_t nd = list ? uint32_t(list->size()) : 0u;
+    if (uint64_t(nd) + n_pcna[v] > 0x7ffd) throw std::runtime_error("too many driver and CNA events on one edge");
+    auto cna = [&](const Cna& c, uint32_t event, uint32_t word, bool passenger) {
+      const uint32_t b = e.g.off[c.chr] + c.begin - 1;
+      const uint32_t end = uint32_t(std::min<uint64_t>(uint64_t(b) + c.len, e.g.off[c.chr + 1]));
+      if (b >= end) return;
+      const auto cov = covering(g, b);
+      if (cov.empty()) return;
+      const uint32_t last = c.begin + (end - b) - 1;
+      if (c.amp) {
+        const uint32_t ord = c.src >= 0 ? uint32_t(c.src) : mulhi32(word, uint32_t(cov.size()));
+        if (ord >= cov.size()) throw std::runtime_error("CNA source allele does not cover the region");
+        const uint32_t x = cov[ord], made = n_inst++;
+        g[made] = ivl_within(g[x], b, end);
+        pl.copies.push_back({v, event, made, x});
+        pl.cnas.push_back({v, 1, c.chr, c.begin, last, made, x, uint8_t(passenger ? 0 : 1)});
+      } else {
+        if (passenger && e.avoid_losses && cov.size() <= 1) return;
+        const uint32_t ord = c.allele >= 0 ? uint32_t(c.allele) : mulhi32(word, uint32_t(cov.size()));
+        if (ord >= cov.size()) throw std::runtime_error("CNA allele does not cover the region");
+        const uint32_t x = cov[ord];
+        g[x] = ivl_minus(g[x], b, end);
+        if (g[x].empty()) g.erase(x);
+        pl.cnas.push_back({v, 0, c.chr, c.begin, last, x, x, uint8_t(passenger ? 0 : 1)});
       }
+      changed = true;
+    };
+    for (uint32_t j = 0; j < nd; ++j) {
+      const DriverEvent& de = (*list)[j];
+      if (de.kind == 0) {
+        DriverRec r = driver_site(e, de.sid, v);
+        const auto cov = covering(g, r.locus);
+        if (cov.empty()) throw std::runtime_error("a driver mutation lies where the cell has no allele left");
+        uint32_t ord;
+        if (de.sid.allele >= 0) {
+          ord = uint32_t(de.sid.allele);
+          if (ord >= cov.size()) throw std::runtime_error("driver allele does not exist there");
+        } else {
+          ord = mulhi32(philox(k0, k1, n_sid, v, 0, TAG_DRIVER).v[0], uint32_t(cov.size()));
+        }
+        r.allele = cov[ord];
+        r.order = int32_t(j);
+        drv.push_back(r);
+        ++n_sid;
+      } else if (de.kind == 1) {
+        cna(de.cna, j, philox(k0, k1, j, v, 1, TAG_CNA).v[1], false);
+      } else {
+        std::vector<uint32_t> present;
+        for (const auto& kv : g) present.push_back(kv.first);
+        for (uint32_t x : present) {
+          const uint32_t made = n_inst++;
+          g[made] = g[x];
+          pl.copies.push_back({v, j, made, x});
+        }
+        pl.cnas.push_back({v, 2, 0, 0, 0, 0, 0, 1});
+        changed = true;
+      }
+    }
+    for (uint64_t k = 0; k < n_pcna[v]; ++k) {
+      const W4 r = philox(k0, k1, uint32_t(k), v, 0, TAG_CNA);
+      cna(e.cands[mulhi32(r.v[0], uint32_t(e.cands.size()))], nd + uint32_t(k), r.v[1], true);
+    }
+    if (changed) { pl.classes.push_back(std::move(g)); pl.node_class[v] = uint32_t(pl.classes.size() - 1); }
+    else pl.node_class[v] = base;
+  }
+  if (n_inst >= 0xffff) throw std::runtime_error("too many allele instances");
+  pl.n_inst = n_inst;
+  pl.has_cna = pl.classes.size() > 1 || n_inst > 2;
+  pl.cn_max = 2;
+  for (const auto& g : pl.classes) pl.cn_max = std::max(pl.cn_max, max_copies(g));
+  return drv;
+}
+
+// driver SNVs/indels of a forest without copy-number events (random alleles
+// marked 0xff, for the std::mt19937_64 flavour)
+std::vector<DriverRec> driver_sites(const Engine& e, const Forest& f) {
+  std::vector<DriverRec> out;
+  for (uint32_t v = 0; v < f.n; ++v) {
+    const auto* list = drivers_of(e, f, v);
+    if (!list) continue;
+    for (uint32_t j = 0; j < list->size(); ++j) {
+      DriverRec r = driver_site(e, (*list)[j].sid, v);
+      r.allele = (*list)[j].sid.allele < 0 ? 0xffu : uint32_t((*list)[j].sid.allele);
+      r.order = int32_t(j);
       out.push_back(r);
     }
   }
@@ -509,15 +704,20 @@ uint32_t indel_aux(const Engine& e, uint32_t cls, uint32_t p, uint32_t w) {
 }
 
 // ---- flavour 0: Philox replay
+constexpr uint32_t LOCUS_NONE = 0xffffffffu;   // drawn where the cell has no allele left
+
 void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre_sbs, uint32_t n_pre_id,
                   uint32_t pre_id, uint64_t seed, Placed& out) {
   const Tables t = make_tables(e, f, n_pre_snv, pre_sbs, n_pre_id, pre_id);
   const uint32_t N = f.n, E = t.E;
-  const double A = 2.0 * double(e.g.b.size());
+  const auto drv = replay_events(e, f, seed, out);
+  std::vector<double> class_size(out.classes.size());
+  for (size_t c = 0; c < class_size.size(); ++c) class_size[c] = double(genome_size(out.classes[c]));
   std::vector<uint32_t> cnt_snv(uint64_t(N + 1) * E, 0), cnt_id(uint64_t(N + 1) * E, 0);
   for (uint32_t v = 0; v < N; ++v) {
     const auto nd = divisions_per_epoch(f, t, v);
     const uint32_t sp = f.species[v];
+    const double A = class_size[out.node_class[v]];   // allelic size of the edge's genome
     for (uint32_t ep = 0; ep < E; ++ep) {
       const double ls = t.snv_rate[uint64_t(sp) * E + ep] * A * double(nd[ep]);
       const double li = t.id_rate[uint64_t(sp) * E + ep] * A * double(nd[ep]);
@@ -537,10 +737,11 @@ void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t
       for (uint32_t ep = 0; ep < E; ++ep)
         for (uint32_t m = 0; m < cnt[uint64_t(v) * E + ep]; ++m) slots.push_back({v, ep, m, ty == 1});
   }
-  const auto drv = driver_records(e, f);
   const size_t n_pass = slots.size(), n_all = n_pass + drv.size();
   std::vector<uint32_t> locus(n_all), aux(n_all), edge(n_all), attempt(n_all, 0);
-  std::vector<uint8_t> cls(n_all), sig(n_all), allele(n_all), kind(n_all), nature(n_all);
+  std::vector<uint8_t> cls(n_all), sig(n_all), kind(n_all), nature(n_all);
+  std::vector<uint16_t> allele(n_all);
+  std::vector<int32_t> order(n_all);
   auto draw_pos = [&](size_t i) {
     const Slot& sl = slots[i];
     Stream st = stream(seed, sl.m, sl.edge, sl.epoch, sl.indel ? TAG_INDEL : TAG_SNV);
@@ -553,14 +754,16 @@ void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t
     }
     const std::vector<uint32_t>& list = sl.indel ? e.id[cls[i]] : e.ctx[sbs_ctx(cls[i])];
     const uint32_t p = list[index64(r.v[0], r.v[1], list.size())];
-    allele[i] = uint8_t(mulhi32(r.v[2], 2));
+    const uint32_t loc = sl.indel ? p - 1 : p;
+    const auto cov = covering(out.classes[out.node_class[sl.edge]], loc);
+    if (cov.empty()) { locus[i] = LOCUS_NONE; return; }
+    allele[i] = uint16_t(cov[mulhi32(r.v[2], uint32_t(cov.size()))]);
+    locus[i] = loc;
     if (!sl.indel) {
       const int ref = e.g.b[p];
       const int ap = sbs_alt(cls[i]);
-      locus[i] = p;
       aux[i] = uint32_t((ref == 1 || ref == 3) ? ap : 3 - ap);
     } else {
-      locus[i] = p - 1;
       aux[i] = indel_aux(e, cls[i], p, r.v[3]);
     }
   };
@@ -576,52 +779,58 @@ void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t
     sig[i] = uint8_t(s); cls[i] = uint8_t(k); edge[i] = sl.edge;
     kind[i] = sl.indel ? 1 : 0;
     nature[i] = sl.edge == N ? 2 : 0;
+    order[i] = sl.edge == N ? -1 : INT32_MAX;
     draw_pos(i);
   }
   for (size_t d = 0; d < drv.size(); ++d) {
     const size_t i = n_pass + d;
     locus[i] = drv[d].locus; edge[i] = drv[d].edge; aux[i] = drv[d].aux; kind[i] = drv[d].kind;
     cls[i] = 0xff; sig[i] = 0xff; nature[i] = 1;
-    uint32_t a = drv[d].allele;
-    if (a == 0xffu) { const W4 r = philox(uint32_t(seed), uint32_t(seed >> 32), uint32_t(d), drv[d].edge, 0, TAG_DRIVER); a = mulhi32(r.v[0], 2); }
-    allele[i] = uint8_t(a);
+    allele[i] = uint16_t(drv[d].allele);
+    order[i] = drv[d].order;
   }
-  if (e.infinite_sites && n_pass > 0) {
+  // redraw rounds: colliding loci under infinite sites (lowest slot wins), and
+  // loci drawn where the edge's genome has no allele left
+  if ((e.infinite_sites || out.has_cna) && n_pass > 0) {
     std::unordered_set<uint32_t> accepted;
-    for (size_t d = 0; d < drv.size(); ++d) accepted.insert(drv[d].locus);
+    if (e.infinite_sites) for (size_t d = 0; d < drv.size(); ++d) accepted.insert(drv[d].locus);
     std::vector<size_t> pending(n_pass);
     for (size_t i = 0; i < n_pass; ++i) pending[i] = i;
     int round = 0;
     while (!pending.empty()) {
-      if (round >= 256) throw std::runtime_error("infinite sites: no free locus");
-      std::unordered_map<uint32_t, size_t> best;
-      std::vector<uint8_t> lost(pending.size(), 0);
-      for (size_t q = 0; q < pending.size(); ++q) {
-        const size_t i = pending[q];
-        if (accepted.count(locus[i])) { lost[q] = 1; continue; }
-        auto it = best.find(locus[i]);
-        if (it == best.end() || i < it->second) best[locus[i]] = i;
-      }
+      if (round >= 256) throw std::runtime_error("no free locus left for some mutations");
       std::vector<size_t> next;
-      for (size_t q = 0; q < pending.size(); ++q) {
-        const size_t i = pending[q];
-        if (!lost[q] && best[locus[i]] == i) accepted.insert(locus[i]);
-        else next.push_back(i);
+      if (e.infinite_sites) {
+        std::unordered_map<uint32_t, size_t> best;
+        std::vector<uint8_t> lost(pending.size(), 0);
+        for (size_t q = 0; q < pending.size(); ++q) {
+          const size_t i = pending[q];
+          if (locus[i] == LOCUS_NONE || accepted.count(locus[i])) { lost[q] = 1; continue; }
+          auto it = best.find(locus[i]);
+          if (it == best.end() || i < it->second) best[locus[i]] = i;
+        }
+        for (size_t q = 0; q < pending.size(); ++q) {
+          const size_t i = pending[q];
+          if (!lost[q] && best[locus[i]] == i) accepted.insert(locus[i]);
+          else next.push_back(i);
+        }
+      } else {
+        for (size_t i : pending) if (locus[i] == LOCUS_NONE) next.push_back(i);
       }
       for (size_t i : next) { attempt[i] += 1; draw_pos(i); }
       pending.swap(next);
       ++round;
     }
   }
-  std::vector<size_t> order(n_all);
-  for (size_t i = 0; i < n_all; ++i) order[i] = i;
-  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+  std::vector<size_t> ord(n_all);
+  for (size_t i = 0; i < n_all; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
     return locus[a] != locus[b] ? locus[a] < locus[b] : a < b;
   });
-  auto perm = [&](auto& v) { auto c = v; for (size_t i = 0; i < n_all; ++i) v[i] = c[order[i]]; };
-  perm(locus); perm(edge); perm(aux); perm(cls); perm(sig); perm(allele); perm(kind); perm(nature);
+  auto perm = [&](auto& v) { auto c = v; for (size_t i = 0; i < n_all; ++i) v[i] = c[ord[i]]; };
+  perm(locus); perm(edge); perm(aux); perm(cls); perm(sig); perm(allele); perm(kind); perm(nature); perm(order);
   out.locus = locus; out.edge = edge; out.aux = aux; out.cls = cls; out.sig = sig;
-  out.allele = allele; out.kind = kind; out.nature = nature;
+  out.allele = allele; out.kind = kind; out.nature = nature; out.order = order;
 }
 
 // ---- flavour 1: sequential std::mt19937_64 engine
@@ -632,16 +841,18 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
   const uint32_t N = f.n, E = t.E;
   const double A = 2.0 * double(e.g.b.size());
   std::unordered_set<uint32_t> used;
-  const auto drv = driver_records(e, f);
-  auto push = [&](uint32_t loc, uint32_t ed, uint32_t ax, int c, int s, int al, int k, int nat) {
+  if (has_copy_number_events(e))
+    throw std::runtime_error("the std::mt19937_64 flavour models no copy-number events");
+  const auto drv = driver_sites(e, f);
+  auto push = [&](uint32_t loc, uint32_t ed, uint32_t ax, int c, int s, int al, int k, int nat, int32_t o) {
     out.locus.push_back(loc); out.edge.push_back(ed); out.aux.push_back(ax); out.cls.push_back(uint8_t(c));
-    out.sig.push_back(uint8_t(s)); out.allele.push_back(uint8_t(al)); out.kind.push_back(uint8_t(k));
-    out.nature.push_back(uint8_t(nat));
+    out.sig.push_back(uint8_t(s)); out.allele.push_back(uint16_t(al)); out.kind.push_back(uint8_t(k));
+    out.nature.push_back(uint8_t(nat)); out.order.push_back(o);
   };
   for (const auto& d : drv) {
     used.insert(d.locus);
     const int al = d.allele == 0xffu ? int(std::uniform_int_distribution<int>(0, 1)(rng)) : int(d.allele);
-    push(d.locus, d.edge, d.aux, 0xff, 0xff, al, d.kind, 1);
+    push(d.locus, d.edge, d.aux, 0xff, 0xff, al, d.kind, 1, d.order);
   }
   auto place_one = [&](uint32_t v, uint32_t row, int ty) {
     const uint32_t NC = ty == 0 ? 96 : 83;
@@ -664,7 +875,7 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
     uint32_t ax;
     if (ty == 0) { const int ref = e.g.b[p]; const int ap = sbs_alt(int(k)); ax = uint32_t((ref == 1 || ref == 3) ? ap : 3 - ap); }
     else ax = indel_aux(e, k, p, uint32_t(rng()));
-    push(loc, v, ax, int(k), int(s), al, ty, v == N ? 2 : 0);
+    push(loc, v, ax, int(k), int(s), al, ty, v == N ? 2 : 0, v == N ? -1 : INT32_MAX);
   };
   for (uint32_t m = 0; m < n_pre_snv; ++m) place_one(N, E, 0);
   for (uint32_t m = 0; m < n_pre_id; ++m) place_one(N, E, 1);
@@ -686,7 +897,8 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return out.locus[a] < out.locus[b]; });
   auto perm = [&](auto& v) { auto c = v; for (size_t i = 0; i < n; ++i) v[i] = c[order[i]]; };
   perm(out.locus); perm(out.edge); perm(out.aux); perm(out.cls); perm(out.sig); perm(out.allele);
-  perm(out.kind); perm(out.nature);
+  perm(out.kind); perm(out.nature); perm(out.order);
+  out.node_class.assign(N + 1, 0);
 }
 
 // ------------------------------------------------------------ sequencing
@@ -816,11 +1028,39 @@ uint32_t error_word(uint32_t w, uint32_t locus, uint32_t mate) {
   return h;
 }
 
-void count_mate(const Placed& pl, const Carrier& car, uint32_t a, uint32_t R, int64_t cell, uint32_t allele,
-                uint32_t err_thr, uint32_t mate, uint32_t w, uint32_t* alt, uint32_t* dep) {
+// Allele instances carrying mutation i: its own instance and every copy made
+// from a carrier after the mutation (later on its edge, or on an edge below
+// it; preneoplastic mutations precede every copy).  Copies are visited in the
+// order they were made, so a copy's source is settled before it.
+std::vector<std::vector<uint32_t>> carrier_sets(const Placed& pl) {
+  const Forest& f = *pl.forest;
+  const size_t M = pl.locus.size();
+  std::vector<std::vector<uint32_t>> out(M);
+  auto below = [&](uint32_t u, uint32_t e) {
+    for (int32_t x = f.parent[u]; x >= 0; x = f.parent[x]) if (uint32_t(x) == e) return true;
+    return false;
+  };
+  for (size_t i = 0; i < M; ++i) {
+    std::vector<uint32_t>& c = out[i];
+    c.push_back(pl.allele[i]);
+    const uint32_t ei = pl.edge[i];
+    for (const CopyRec& cp : pl.copies) {
+      if (std::find(c.begin(), c.end(), cp.from) == c.end()) continue;
+      const bool after = ei >= f.n || (cp.edge == ei && int64_t(cp.event) > int64_t(pl.order[i])) ||
+                         below(cp.edge, ei);
+      if (after) c.push_back(cp.made);
+    }
+  }
+  return out;
+}
+
+void count_mate(const Placed& pl, const Carrier& car, const std::vector<std::vector<uint32_t>>& carriers,
+                uint32_t a, uint32_t R, int64_t cell, uint32_t allele, uint32_t err_thr, uint32_t mate, uint32_t w,
+                uint32_t* alt, uint32_t* dep) {
   auto it = std::lower_bound(pl.locus.begin(), pl.locus.end(), a);
   for (size_t i = size_t(it - pl.locus.begin()); i < pl.locus.size() && pl.locus[i] < a + R; ++i) {
-    const bool carried = car.ancestor_or_self(pl.edge[i], cell) && pl.allele[i] == allele;
+    const auto& cs = carriers[i];
+    const bool carried = car.ancestor_or_self(pl.edge[i], cell) && std::find(cs.begin(), cs.end(), allele) != cs.end();
     bool obs;
     if (pl.kind[i] == 1) obs = carried;
     else {
@@ -831,6 +1071,25 @@ void count_mate(const Placed& pl, const Carrier& car, uint32_t a, uint32_t R, in
     dep[i] += 1;
     if (obs) alt[i] += 1;
   }
+}
+
+// copies of genome g summed over positions [a, b), and the largest copy
+// number there
+void copies_in(const CellGenome& g, uint32_t a, uint32_t b, uint64_t& sum, uint32_t& mx) {
+  std::vector<std::pair<uint32_t, int>> ev;
+  sum = 0;
+  for (const auto& kv : g)
+    for (auto [x, y] : kv.second) {
+      const uint32_t lo = std::max(x, a), hi = std::min(y, b);
+      if (lo >= hi) continue;
+      sum += hi - lo;
+      ev.push_back({lo, 1});
+      ev.push_back({hi, -1});
+    }
+  std::sort(ev.begin(), ev.end());
+  int cur = 0, best = 0;
+  for (auto [p, d] : ev) { cur += d; best = std::max(best, cur); }
+  mx = uint32_t(best);
 }
 
 // ---- flavour 0: replay of the tiled read generation
@@ -845,7 +1104,9 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
   out.alt.assign(out.n_samples * M, 0);
   out.depth.assign(out.n_samples * M, 0);
   Carrier car{f, c.preneoplastic_in_normal != 0};
+  const auto carriers = carrier_sets(pl);
   const double mates = s.paired ? 2.0 : 1.0;
+  const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
   uint32_t tile_base = 0;   // global tile index of the chromosome's first tile
   for (uint32_t ci : s.chrs) {
     const uint32_t L = e.g.off[ci + 1] - e.g.off[ci];
@@ -855,14 +1116,49 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
     const uint32_t ce = e.g.off[ci + 1];
     for (uint32_t smp = 0; smp < out.n_samples; ++smp) {
       const SampleDesc& sd = s.samples[smp];
+      // with copy-number events: the DNA mass of each tile in this sample
+      // (cells drawn as normal with probability wn, else a uniform leaf;
+      // mass = wn * copies of the germline + (1 - wn) / leaves * the leaves'
+      // copies, copies summed over the tile's start positions) and the copy
+      // slots of the tile's rejection draw (largest copy number there)
+      std::vector<double> cum(nt, 0.0);
+      std::vector<uint32_t> tile_cn(nt, 1);
+      double tot = 0.0;
+      if (pl.has_cna) {
+        const double wn = sd.all_normal ? 1.0 : double(sd.normal_thr) * (1.0 / 4294967296.0);
+        const double wt = 1.0 - wn;
+        const bool tumour = wt > 0 && !sd.leaves.empty();
+        for (uint32_t k = 0; k < nt; ++k) {
+          const uint32_t a = e.g.off[ci] + k * T, b = a + std::min<uint32_t>(T, S - k * T);
+          uint64_t i0 = 0, sum = 0;
+          uint32_t m0 = 0, mx = 0;
+          copies_in(pl.classes[0], a, b, i0, m0);
+          if (wn > 0) mx = m0;
+          if (tumour)
+            for (uint32_t leaf : sd.leaves) {
+              uint64_t x = 0;
+              uint32_t m = 0;
+              copies_in(pl.classes[pl.node_class[leaf]], a, b, x, m);
+              sum += x;
+              mx = std::max(mx, m);
+            }
+          cum[k] = tot;
+          double m = wn * double(i0);
+          if (tumour) m = m + (wt / double(sd.leaves.size())) * double(sum);
+          tot = tot + m;
+          tile_cn[k] = std::max<uint32_t>(1, mx);
+        }
+      }
       // multinomial split by a binary tree over the padded tile range
       // [0, 2^D): node h covering [lo, lo+size) sends Binomial(n, w_left/w)
-      // fragments to its left half (w = start positions of covered tiles)
+      // fragments to its left half (w = start positions of covered tiles, or
+      // their mass)
       uint32_t D = 0;
       while ((uint64_t(1) << D) < nt) ++D;
       auto wts = [&](uint64_t a, uint64_t b) {
         return std::min<uint64_t>(b * T, S) - std::min<uint64_t>(a * T, S);
       };
+      auto mass_at = [&](uint64_t a) { return a < nt ? cum[a] : tot; };
       std::vector<uint64_t> tile_pairs(nt, 0);
       struct Node { uint64_t lo, size; uint32_t id; uint64_t n; };
       std::vector<Node> stack{{0, uint64_t(1) << D, 1, pairs}};
@@ -871,11 +1167,20 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
         if (nd.size == 1) { if (nd.lo < nt) tile_pairs[nd.lo] = nd.n; continue; }
         const uint64_t half = nd.size / 2, mid = nd.lo + half;
         uint64_t nl = 0;
-        const uint64_t wt = wts(nd.lo, nd.lo + nd.size);
-        if (nd.n > 0 && wt > 0) {
-          const double p = double(wts(nd.lo, mid)) / double(wt);
-          Stream st = stream(seed, nd.id, ci, smp, TAG_TILE_SPLIT);
-          nl = binomial(st, nd.n, p);
+        if (!pl.has_cna) {
+          const uint64_t wt = wts(nd.lo, nd.lo + nd.size);
+          if (nd.n > 0 && wt > 0) {
+            const double p = double(wts(nd.lo, mid)) / double(wt);
+            Stream st = stream(seed, nd.id, ci, smp, TAG_TILE_SPLIT);
+            nl = binomial(st, nd.n, p);
+          }
+        } else {
+          const double lo_m = mass_at(nd.lo), wt = mass_at(nd.lo + nd.size) - lo_m;
+          if (nd.n > 0 && wt > 0) {
+            const double p = (mass_at(mid) - lo_m) / wt;
+            Stream st = stream(seed, nd.id, ci, smp, TAG_TILE_SPLIT);
+            nl = binomial(st, nd.n, p);
+          }
         }
         stack.push_back({nd.lo, half, 2 * nd.id, nl});
         stack.push_back({mid, half, 2 * nd.id + 1, nd.n - nl});
@@ -886,20 +1191,33 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
         const uint32_t t = tile_base + k;
         const uint32_t start = e.g.off[ci] + k * T, len = std::min<uint32_t>(T, S - k * T);
         for (uint32_t j = 0; j < tile_pairs[k]; ++j) {
-          const W4 r = philox(uint32_t(seed), uint32_t(seed >> 32), j, t, smp, TAG_PAIR);
-          const uint32_t p0 = start + mulhi32(r.v[0], len);
-          const bool normal = sd.all_normal || r.v[1] < sd.normal_thr;
-          const int64_t cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[2], uint32_t(sd.leaves.size()))]);
-          const uint32_t allele = mulhi32(r.v[3], 2);
-          const W4 r2 = philox(uint32_t(seed), uint32_t(seed >> 32), j, t, smp, TAG_PAIR2);
-          count_mate(pl, car, p0, s.R, cell, allele, s.err_thr, 0, r2.v[1], alt, dep);
+          out.n_reads += s.paired ? 2 : 1;
+          // start, cell and allele instance; with copy-number events drawn
+          // by rejection (copy slot u < cn_max kept when the cell has more
+          // than u instances at the start), attempt a on Philox tag
+          // TAG_PAIR | a << 8, the fragment dropped after 256 attempts
+          uint32_t p0 = 0, allele = 0;
+          int64_t cell = -1;
+          bool found = false;
+          for (uint32_t att = 0; att < (pl.has_cna ? 256u : 1u) && !found; ++att) {
+            const W4 r = philox(k0, k1, j, t, smp, TAG_PAIR | (att << 8));
+            p0 = start + mulhi32(r.v[0], len);
+            const bool normal = sd.all_normal || r.v[1] < sd.normal_thr;
+            cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[2], uint32_t(sd.leaves.size()))]);
+            if (!pl.has_cna) { allele = mulhi32(r.v[3], 2); found = true; break; }
+            const uint32_t u = mulhi32(r.v[3], tile_cn[k]);
+            const auto cov = covering(pl.classes[cell < 0 ? 0u : pl.node_class[cell]], p0);
+            if (u < cov.size()) { allele = cov[u]; found = true; }
+          }
+          if (!found) continue;
+          const W4 r2 = philox(k0, k1, j, t, smp, TAG_PAIR2);
+          count_mate(pl, car, carriers, p0, s.R, cell, allele, s.err_thr, 0, r2.v[1], alt, dep);
           if (s.paired) {
             const uint32_t ins = s.ins_min + lookup(s.ins_thr.data(), uint32_t(s.ins_thr.size()), r2.v[0]);
             uint32_t p1 = p0 + ins - s.R;
             if (p1 > ce - s.R) p1 = ce - s.R;
-            count_mate(pl, car, p1, s.R, cell, allele, s.err_thr, 1, r2.v[1], alt, dep);
+            count_mate(pl, car, carriers, p1, s.R, cell, allele, s.err_thr, 1, r2.v[1], alt, dep);
           }
-          out.n_reads += s.paired ? 2 : 1;
         }
       }
     }
@@ -912,6 +1230,7 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
 // bounded sample for the timed CPU baseline); `threads` splits the samples
 // and chromosomes over host threads, each with its own engine.
 void seq_mt(const Placed& pl, const SeqCfg& c, uint64_t seed, double fraction, int threads, SeqOut& out) {
+  if (pl.has_cna) throw std::runtime_error("the std::mt19937_64 flavour models no copy-number events");
   const Engine& e = *pl.eng;
   const Forest& f = *pl.forest;
   const SeqSetup s = seq_setup(pl, c);
@@ -1080,9 +1399,9 @@ void orc_engine_add_exposure(void* ep, int type, double time, const double* coef
   auto* e = static_cast<Engine*>(ep);
   e->expo[type][time] = std::vector<double>(coeffs, coeffs + e->n_sig[type]);
 }
-void orc_engine_set_species_rates(void* ep, uint32_t sp, double snv, double indel) {
+void orc_engine_set_species_rates(void* ep, uint32_t sp, double snv, double indel, double cna) {
   auto& s = static_cast<Engine*>(ep)->species[sp];
-  s.snv = snv; s.indel = indel; s.has = true;
+  s.snv = snv; s.indel = indel; s.cna = cna; s.has = true;
 }
 void orc_engine_set_species_epoch_rates(void* ep, uint32_t sp, uint32_t n, const double* snv, const double* indel) {
   auto& s = static_cast<Engine*>(ep)->species[sp];
@@ -1093,8 +1412,27 @@ void orc_engine_set_species_mutant(void* ep, uint32_t sp, uint32_t mutant) {
 }
 void orc_engine_add_driver_sid(void* ep, uint32_t mutant, uint32_t chr, uint32_t pos, const char* ref, const char* alt,
                                int32_t allele) {
-  static_cast<Engine*>(ep)->drivers[mutant].push_back({chr, pos, ref, alt, allele});
+  DriverEvent d{};
+  d.kind = 0;
+  d.sid = {chr, pos, ref, alt, allele};
+  static_cast<Engine*>(ep)->drivers[mutant].push_back(d);
 }
+void orc_engine_add_driver_cna(void* ep, uint32_t mutant, int amp, uint32_t chr, uint32_t begin, uint32_t len,
+                               int32_t allele, int32_t src) {
+  DriverEvent d{};
+  d.kind = 1;
+  d.cna = {amp != 0, chr, begin, len, allele, src};
+  static_cast<Engine*>(ep)->drivers[mutant].push_back(d);
+}
+void orc_engine_add_driver_wgd(void* ep, uint32_t mutant) {
+  DriverEvent d{};
+  d.kind = 2;
+  static_cast<Engine*>(ep)->drivers[mutant].push_back(d);
+}
+void orc_engine_add_passenger_cna(void* ep, uint32_t chr, uint32_t begin, uint32_t len, int amp) {
+  static_cast<Engine*>(ep)->cands.push_back({amp != 0, chr, begin, len, -1, -1});
+}
+void orc_engine_set_avoid_homozygous_losses(void* ep, int on) { static_cast<Engine*>(ep)->avoid_losses = on != 0; }
 void orc_engine_set_infinite_sites(void* ep, int on) { static_cast<Engine*>(ep)->infinite_sites = on != 0; }
 
 void* orc_place(void* ep, uint32_t n, const int32_t* parent, const double* birth, const uint32_t* species,
@@ -1123,7 +1461,7 @@ void* orc_place(void* ep, uint32_t n, const int32_t* parent, const double* birth
 void orc_placed_destroy(void* p) { delete static_cast<Placed*>(p); }
 uint64_t orc_placed_count(void* pp) { return static_cast<Placed*>(pp)->locus.size(); }
 void orc_placed_copy(void* pp, uint32_t* locus, uint32_t* edge, uint32_t* aux, uint8_t* cls, uint8_t* sig,
-                     uint8_t* allele, uint8_t* kind, uint8_t* nature) {
+                     uint16_t* allele, uint8_t* kind, uint8_t* nature) {
   auto* p = static_cast<Placed*>(pp);
   const size_t n = p->locus.size();
   if (locus) std::copy(p->locus.begin(), p->locus.end(), locus);
@@ -1136,13 +1474,34 @@ void orc_placed_copy(void* pp, uint32_t* locus, uint32_t* edge, uint32_t* aux, u
   if (nature) std::copy(p->nature.begin(), p->nature.end(), nature);
   (void)n;
 }
-// Replace the placed mutations (used to sequence the same table the GPU placed)
-void orc_placed_set(void* pp, uint64_t n, const uint32_t* locus, const uint32_t* edge, const uint8_t* allele,
-                    const uint8_t* kind) {
+// Replace the placed mutations of a table without copy-number events (used
+// to sequence the same table the GPU placed)
+int orc_placed_set(void* pp, uint64_t n, const uint32_t* locus, const uint32_t* edge, const uint16_t* allele,
+                   const uint8_t* kind) {
   auto* p = static_cast<Placed*>(pp);
+  if (p->has_cna) { orc_err = "orc_placed_set: the table has copy-number events"; return 1; }
   p->locus.assign(locus, locus + n); p->edge.assign(edge, edge + n);
   p->allele.assign(allele, allele + n); p->kind.assign(kind, kind + n);
   p->aux.assign(n, 0); p->cls.assign(n, 0); p->sig.assign(n, 0); p->nature.assign(n, 0);
+  p->order.assign(n, 0);
+  for (uint64_t i = 0; i < n; ++i) p->order[i] = edge[i] >= p->forest->n ? -1 : INT32_MAX;
+  return 0;
+}
+uint64_t orc_placed_cna_count(void* pp) { return static_cast<Placed*>(pp)->cnas.size(); }
+void orc_placed_cna_copy(void* pp, uint32_t* node, uint8_t* type, uint32_t* chr, uint32_t* begin, uint32_t* end,
+                         uint32_t* allele, uint32_t* src, uint8_t* driver) {
+  const auto& c = static_cast<Placed*>(pp)->cnas;
+  for (size_t i = 0; i < c.size(); ++i) {
+    node[i] = c[i].node; type[i] = c[i].type; chr[i] = c[i].chr; begin[i] = c[i].begin; end[i] = c[i].end;
+    allele[i] = c[i].allele; src[i] = c[i].src; driver[i] = c[i].driver;
+  }
+}
+// node classes (n nodes), number of classes, largest copy number
+void orc_placed_node_classes(void* pp, uint32_t* node_class, uint32_t* n_classes, uint32_t* cn_max) {
+  auto* p = static_cast<Placed*>(pp);
+  if (node_class) std::copy(p->node_class.begin(), p->node_class.begin() + p->forest->n, node_class);
+  if (n_classes) *n_classes = uint32_t(p->classes.size());
+  if (cn_max) *cn_max = p->cn_max;
 }
 
 void* orc_seq(void* pp, const void* cfg, uint64_t seed, int flavour, double fraction, int threads) {

@@ -84,7 +84,12 @@ _PROTOS = {
                                      C.POINTER(P)]),
     "pg_placed_destroy": (C.c_int, [P]),
     "pg_placed_count": (C.c_int, [P, u64p]),
-    "pg_placed_copy": (C.c_int, [P, u32p, u32p, u32p, u8p, u8p, u8p, u8p, u8p]),
+    "pg_placed_copy": (C.c_int, [P, u32p, u32p, u32p, u8p, u8p, C.POINTER(C.c_uint16), u8p, u8p]),
+    "pg_placed_cna_count": (C.c_int, [P, u64p]),
+    "pg_placed_cna_copy": (C.c_int, [P, u32p, u8p, u32p, u32p, u32p, u32p, u32p, u8p]),
+    "pg_placed_node_classes": (C.c_int, [P, u32p, u32p, u32p]),
+    "pg_engine_add_passenger_cna": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
+    "pg_engine_set_avoid_homozygous_losses": (C.c_int, [P, C.c_int]),
     "pg_placed_kernel_ms": (C.c_int, [P, f32p]),
     "pg_simulate_seq": (C.c_int, [P, C.POINTER(SeqCfg), C.c_uint64, C.POINTER(P)]),
     "pg_seq_result_destroy": (C.c_int, [P]),

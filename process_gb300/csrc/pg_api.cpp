@@ -4,6 +4,7 @@
 #include "pg_common.cuh"
 #include "pg_kernels.h"
 #include "pg_scan.cuh"
+#include "pg_genome.h"
 
 #include <cuda_runtime.h>
 
@@ -164,6 +165,38 @@ struct DriverSpec {
   int32_t allele;
 };
 
+struct CnaSpec {      // a driver CNA or a passenger CNA candidate
+  bool amp;           // amplification (else deletion)
+  uint32_t chr, begin, len;   // 0-based chr index, 1-based first position, length
+  int32_t allele, src;        // allele ordinal among the covering instances, -1 = random
+};
+
+struct DriverEvent {  // one entry of a mutant's driver list, in application order
+  int kind;           // 0 SNV/indel, 1 CNA, 2 whole-genome doubling
+  DriverSpec sid;
+  CnaSpec cna;
+};
+
+struct CnaOut {       // an applied CNA/WGD event (for the phylogenetic-forest getters)
+  uint32_t node;
+  uint8_t type;       // 0 deletion, 1 amplification, 2 WGD
+  uint32_t chr, begin, end;   // 1-based inclusive region
+  uint32_t allele, src;       // instance acted on / created, source instance
+  uint8_t driver;
+};
+
+static void philox_host(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t out[4]) {
+  uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
+  for (int i = 0; i < 10; ++i) {
+    const uint64_t p0 = uint64_t(0xD2511F53u) * c0, p1 = uint64_t(0xCD9E8D57u) * c2;
+    const uint32_t n0 = uint32_t(p1 >> 32) ^ c1 ^ k0, n2 = uint32_t(p0 >> 32) ^ c3 ^ k1;
+    c0 = n0; c1 = uint32_t(p1); c2 = n2; c3 = uint32_t(p0);
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+static inline uint32_t mulhi32(uint32_t a, uint32_t b) { return uint32_t((uint64_t(a) * b) >> 32); }
+
 struct pg_engine {
   int device = 0;
   cudaStream_t st = nullptr;         // the stream every call of the engine runs on
@@ -185,8 +218,10 @@ struct pg_engine {
   std::vector<double> sigs[2];
   std::map<double, std::vector<double>> expo[2];
   std::map<uint32_t, Species> species;
-  std::map<uint32_t, std::vector<DriverSpec>> drivers;
+  std::map<uint32_t, std::vector<DriverEvent>> drivers;   // per mutant, application order
+  std::vector<CnaSpec> cna_cands;                          // passenger CNA candidates
   bool infinite_sites = true;
+  bool avoid_homozygous_losses = true;
   // the caller's reference plus one per live placed/sequencing handle: the
   // engine (its pool and stream) outlives every handle that draws from it
   std::atomic<int> refs{1};
@@ -223,10 +258,24 @@ struct pg_placed {
   std::vector<std::vector<uint32_t>> leaves;
   uint64_t M = 0;
   DBuf<uint32_t> locus, edge, aux, attempt;
-  DBuf<uint8_t> cls, sig, allele, kind, nature;
+  DBuf<uint8_t> cls, sig, kind, nature;
+  DBuf<uint16_t> allele, seq;
   float kernel_ms = 0;
+  // genotype classes (copy-number state) and allele-instance lineage
+  bool has_cna = false;
+  uint32_t cn_max = 2, n_classes = 1;
+  std::vector<uint32_t> node_class_h;
+  std::vector<std::vector<uint32_t>> leaf_cls;   // per sample, parallel to leaves
+  std::vector<uint32_t> seg_off_h, seg_start_h, seg_end_h, seg_icnt_h;   // class segments (host copy)
+  DBuf<uint32_t> node_class, seg_off, seg_start, seg_end, seg_ioff, seg_icnt, chain_off;
+  DBuf<uint16_t> inst_list, chain_anc;
+  DBuf<uint64_t> chain_key;
+  std::vector<CnaOut> cnas;
   pg::PlaceOut view() const {
-    return {locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, kind.p, nature.p, attempt.p};
+    return {locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, seq.p, kind.p, nature.p, attempt.p};
+  }
+  pg::GenomeClasses classes_view() const {
+    return {n_classes, node_class.p, seg_off.p, seg_start.p, seg_end.p, seg_ioff.p, seg_icnt.p, inst_list.p};
   }
 };
 
@@ -574,22 +623,50 @@ pg_status pg_engine_add_driver_sid(pg_engine* e, uint32_t mutant, uint32_t chr, 
     for (char c : r) code_of(c);
     for (char c : a) code_of(c);
     require(allele >= -1 && allele <= 1, "allele must be 0, 1 or random (-1)");
-    e->drivers[mutant].push_back({chr, pos, r, a, allele});
+    DriverEvent ev{};
+    ev.kind = 0;
+    ev.sid = {chr, pos, r, a, allele};
+    e->drivers[mutant].push_back(ev);
   });
 }
 
-pg_status pg_engine_add_driver_cna(pg_engine* e, uint32_t, int, uint32_t, uint32_t, uint32_t, int32_t, int32_t) {
+pg_status pg_engine_add_driver_cna(pg_engine* e, uint32_t mutant, int type_amplification, uint32_t chr,
+                                   uint32_t begin, uint32_t length, int32_t allele, int32_t src_allele) {
   return guarded([&] {
     require(e != nullptr, "NULL engine");
-    throw Unsupported("driver CNAs are not built in this version of process_gb300");
+    require(chr < e->n_chr, "unknown chromosome");
+    require(begin >= 1 && length >= 1 && uint64_t(begin) + length - 1 <= e->chr_len[chr],
+            "the CNA region must lie inside the chromosome");
+    require(allele >= -1 && src_allele >= -1, "alleles are ordinals (>= 0) or random (-1)");
+    DriverEvent ev{};
+    ev.kind = 1;
+    ev.cna = {type_amplification != 0, chr, begin, length, allele, src_allele};
+    e->drivers[mutant].push_back(ev);
   });
 }
 
-pg_status pg_engine_add_driver_wgd(pg_engine* e, uint32_t) {
+pg_status pg_engine_add_driver_wgd(pg_engine* e, uint32_t mutant) {
   return guarded([&] {
     require(e != nullptr, "NULL engine");
-    throw Unsupported("whole-genome doubling is not built in this version of process_gb300");
+    DriverEvent ev{};
+    ev.kind = 2;
+    e->drivers[mutant].push_back(ev);
   });
+}
+
+pg_status pg_engine_add_passenger_cna(pg_engine* e, uint32_t chr, uint32_t begin, uint32_t length,
+                                      int type_amplification) {
+  return guarded([&] {
+    require(e != nullptr, "NULL engine");
+    require(chr < e->n_chr, "unknown chromosome");
+    require(begin >= 1 && length >= 1 && uint64_t(begin) + length - 1 <= e->chr_len[chr],
+            "the CNA region must lie inside the chromosome");
+    e->cna_cands.push_back({type_amplification != 0, chr, begin, length, -1, -1});
+  });
+}
+
+pg_status pg_engine_set_avoid_homozygous_losses(pg_engine* e, int on) {
+  return guarded([&] { require(e != nullptr, "NULL engine"); e->avoid_homozygous_losses = on != 0; });
 }
 
 pg_status pg_engine_set_infinite_sites(pg_engine* e, int on) {
@@ -733,49 +810,201 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     auto id_sig_d = upload(P, sig_cdf[1], st);
     auto sbs_expo_d = upload(P, expo_cdf[0], st);
     auto id_expo_d = upload(P, expo_cdf[1], st);
+    std::vector<double> cna_rate(S, 0.0);
+    bool passenger_cnas = false;
+    for (uint32_t s2 = 0; s2 < S; ++s2) {
+      auto it = e->species.find(s2);
+      if (used[s2] && it != e->species.end()) cna_rate[s2] = it->second.cna;
+      passenger_cnas = passenger_cnas || (used[s2] && cna_rate[s2] > 0);
+    }
+    passenger_cnas = passenger_cnas && !e->cna_cands.empty();
+    auto cna_d = upload(P, cna_rate, st);
     pg::PlaceTables t{};
     t.n_nodes = f->n; t.parent = parent_d.p; t.birth = birth_d.p; t.species = species_d.p; t.divisions = div_d.p;
-    t.n_epochs = E; t.epoch_start = times_d.p; t.snv_rate = snv_d.p; t.indel_rate = id_d.p;
-    t.allelic_size = 2.0 * double(e->G);
+    t.n_epochs = E; t.epoch_start = times_d.p; t.snv_rate = snv_d.p; t.indel_rate = id_d.p; t.cna_rate = cna_d.p;
     t.n_sbs_sigs = std::max<uint32_t>(e->n_sig[0], 1); t.n_id_sigs = std::max<uint32_t>(e->n_sig[1], 1);
     t.sbs_expo_cdf = sbs_expo_d.p; t.sbs_sig_cdf = sbs_sig_d.p; t.id_expo_cdf = id_expo_d.p; t.id_sig_cdf = id_sig_d.p;
     t.genome = e->genome.p;
     t.ctx_off = e->ctx_off_d.p; t.ctx_len = e->ctx_len_d.p; t.ctx_lists = e->ctx_lists.p;
     t.id_off = e->id_off_d.p; t.id_len = e->id_len_d.p; t.id_lists = e->id_lists.p;
 
-    // ---- drivers: first edge of each mutant
+    Timer timer(st);
+    // ---- passenger CNA counts (germline-size rate, so they do not depend on the events)
+    std::vector<uint32_t> cnt_cna(f->n, 0);
+    if (passenger_cnas) {
+      DBuf<uint32_t> cc(P, f->n);
+      pg::place_cna_counts(t, cc.p, seed, 2.0 * double(e->G), st);
+      ck(cudaMemcpyAsync(cnt_cna.data(), cc.p, sizeof(uint32_t) * f->n, cudaMemcpyDeviceToHost, st), "cna counts");
+      ck(cudaStreamSynchronize(st), "cna counts");
+    }
+    // ---- replay drivers and CNA/WGD events into genotype classes (host)
+    auto pl = std::make_unique<pg_placed>();
+    std::vector<pg::GenomeFrags> classes(1);
+    for (uint32_t c = 0; c < e->n_chr; ++c) {
+      classes[0].push_back({0u, e->chr_off[c], e->chr_off[c + 1]});
+      classes[0].push_back({1u, e->chr_off[c], e->chr_off[c + 1]});
+    }
+    std::vector<pg::InstInfo> insts{{-1, 0}, {-1, 0}};
+    std::vector<uint32_t> node_class(f->n + 1, 0);
     std::vector<pg::DriverRec> drv;
+    uint32_t drv_index = 0;
+    auto mut_of = [&](uint32_t node) {
+      auto it = e->species.find(f->species[node]);
+      return it == e->species.end() ? 0u : it->second.mutant;
+    };
+    // order key of the copy made by event j on edge v (see SEQ_PASSENGER)
+    auto key_of = [&](uint32_t v, uint32_t j) { return (uint64_t(f->tin[v]) << 16) | (j + 1u); };
     for (uint32_t v = 0; v < f->n; ++v) {
-      auto mut_of = [&](uint32_t node) {
-        auto it = e->species.find(f->species[node]);
-        return it == e->species.end() ? 0u : it->second.mutant;
-      };
+      const uint32_t base = f->parent[v] >= 0 ? node_class[f->parent[v]] : 0u;
+      const std::vector<DriverEvent>* devs = nullptr;
       const uint32_t m = mut_of(v);
-      if (f->parent[v] >= 0 && mut_of(uint32_t(f->parent[v])) == m) continue;
-      auto it = e->drivers.find(m);
-      if (it == e->drivers.end()) continue;
-      for (const auto& d : it->second) {
-        pg::DriverRec r{};
-        const uint32_t abs = e->chr_off[d.chr] + d.pos - 1;
-        r.edge = v;
-        r.allele = d.allele < 0 ? 0xffu : uint32_t(d.allele);
-        if (d.ref.size() == 1 && d.alt.size() == 1) {
-          r.kind = pg::KIND_SNV; r.locus = abs; r.aux = code_of(d.alt[0]);
+      if (f->parent[v] < 0 || mut_of(uint32_t(f->parent[v])) != m) {
+        auto it = e->drivers.find(m);
+        if (it != e->drivers.end()) devs = &it->second;
+      }
+      const uint32_t nd = devs ? uint32_t(devs->size()) : 0u;
+      require(uint64_t(nd) + cnt_cna[v] <= pg::SEQ_MAX_EVENTS, "too many driver and CNA events on one edge");
+      bool touches = cnt_cna[v] > 0;
+      for (uint32_t j = 0; j < nd; ++j) touches = touches || (*devs)[j].kind != 0;
+      if (!touches && nd == 0) { node_class[v] = base; continue; }
+      pg::GenomeFrags g = touches ? classes[base] : pg::GenomeFrags();
+      const pg::GenomeFrags& gv = touches ? g : classes[base];
+      bool changed = false;
+      auto apply_cna = [&](const CnaSpec& c, uint32_t seq, uint32_t r_word, bool passenger) {
+        const uint32_t b = e->chr_off[c.chr] + c.begin - 1;
+        const uint32_t end = uint32_t(std::min<uint64_t>(uint64_t(b) + c.len, e->chr_off[c.chr + 1]));
+        if (b >= end) return;
+        const auto cov = pg::covering_insts(g, b);
+        if (cov.empty()) return;
+        CnaOut rec{v, uint8_t(c.amp ? 1 : 0), c.chr, c.begin, c.begin + (end - b) - 1, 0, 0, uint8_t(passenger ? 0 : 1)};
+        if (c.amp) {
+          const uint32_t ord = c.src >= 0 ? uint32_t(c.src) : mulhi32(r_word, uint32_t(cov.size()));
+          if (ord >= cov.size()) throw DomainError("CNA source allele " + std::to_string(ord) + " does not cover the region");
+          const uint32_t x = cov[ord], xn = uint32_t(insts.size());
+          insts.push_back({int32_t(x), key_of(v, seq)});
+          pg::frag_amplify(g, x, xn, b, end);
+          rec.allele = xn; rec.src = x;
         } else {
-          r.kind = pg::KIND_INDEL; r.locus = abs;  // the shared first base is the anchor
-          if (d.alt.size() > 1) {
-            uint32_t bases = 0;
-            for (size_t k = 1; k < d.alt.size(); ++k) bases |= code_of(d.alt[k]) << (2 * (k - 1));
-            r.aux = 1u | (uint32_t(d.alt.size() - 1) << 1) | (bases << 8);
-          } else {
-            r.aux = 0u | (uint32_t(d.ref.size() - 1) << 1);
-          }
+          if (passenger && e->avoid_homozygous_losses && cov.size() <= 1) return;
+          const uint32_t ord = c.allele >= 0 ? uint32_t(c.allele) : mulhi32(r_word, uint32_t(cov.size()));
+          if (ord >= cov.size()) throw DomainError("CNA allele " + std::to_string(ord) + " does not cover the region");
+          pg::frag_delete(g, cov[ord], b, end);
+          rec.allele = cov[ord]; rec.src = cov[ord];
         }
-        drv.push_back(r);
+        changed = true;
+        pl->cnas.push_back(rec);
+      };
+      for (uint32_t j = 0; j < nd; ++j) {
+        const DriverEvent& de = (*devs)[j];
+        if (de.kind == 0) {
+          const DriverSpec& d = de.sid;
+          pg::DriverRec r{};
+          r.locus = e->chr_off[d.chr] + d.pos - 1;   // SNV site, or the shared first base of an indel
+          r.edge = v;
+          r.seq = j;
+          const auto cov = pg::covering_insts(gv, r.locus);
+          if (cov.empty()) throw DomainError("a driver mutation lies where the cell has no allele left");
+          uint32_t ord;
+          if (d.allele >= 0) {
+            ord = uint32_t(d.allele);
+            if (ord >= cov.size()) throw DomainError("driver allele " + std::to_string(ord) + " does not exist there");
+          } else {
+            uint32_t w[4];
+            philox_host(seed, drv_index, v, 0u, 6u /* TAG_DRIVER */, w);
+            ord = mulhi32(w[0], uint32_t(cov.size()));
+          }
+          r.allele = cov[ord];
+          if (d.ref.size() == 1 && d.alt.size() == 1) {
+            r.kind = pg::KIND_SNV; r.aux = code_of(d.alt[0]);
+          } else {
+            r.kind = pg::KIND_INDEL;
+            if (d.alt.size() > 1) {
+              uint32_t bases = 0;
+              for (size_t k = 1; k < d.alt.size(); ++k) bases |= code_of(d.alt[k]) << (2 * (k - 1));
+              r.aux = 1u | (uint32_t(d.alt.size() - 1) << 1) | (bases << 8);
+            } else {
+              r.aux = 0u | (uint32_t(d.ref.size() - 1) << 1);
+            }
+          }
+          drv.push_back(r);
+          ++drv_index;
+        } else if (de.kind == 1) {
+          uint32_t w[4];
+          philox_host(seed, j, v, 1u, 12u /* TAG_CNA */, w);
+          apply_cna(de.cna, j, w[1], false);
+        } else {                                  // whole-genome doubling
+          std::vector<uint32_t> present;
+          for (const auto& fr : g) present.push_back(fr.inst);
+          std::sort(present.begin(), present.end());
+          present.erase(std::unique(present.begin(), present.end()), present.end());
+          for (uint32_t x : present) {
+            const uint32_t xn = uint32_t(insts.size());
+            insts.push_back({int32_t(x), key_of(v, j)});
+            pg::frag_amplify(g, x, xn, 0u, 0xffffffffu);
+          }
+          pl->cnas.push_back({v, 2, 0, 0, 0, 0, 0, 1});
+          changed = true;
+        }
+      }
+      for (uint32_t k = 0; k < cnt_cna[v]; ++k) {
+        uint32_t w[4];
+        philox_host(seed, k, v, 0u, 12u /* TAG_CNA */, w);
+        const CnaSpec& cand = e->cna_cands[mulhi32(w[0], uint32_t(e->cna_cands.size()))];
+        apply_cna(cand, nd + k, w[1], true);
+      }
+      if (changed) {
+        require(classes.size() < (1u << 24), "too many genotype classes");
+        classes.push_back(std::move(g));
+        node_class[v] = uint32_t(classes.size() - 1);
+      } else {
+        node_class[v] = base;
       }
     }
+    require(insts.size() < 0xffff, "too many allele instances");
+    // ---- class tables (segments), node sizes, instance lineage chains
+    std::vector<uint32_t> seg_off{0}, seg_start, seg_end, seg_ioff, seg_icnt;
+    std::vector<uint16_t> inst_list;
+    std::vector<double> class_size(classes.size());
+    uint32_t cn_max = 0;
+    for (size_t c = 0; c < classes.size(); ++c) {
+      for (const auto& sg : pg::segments_of(classes[c])) {
+        seg_start.push_back(sg.b); seg_end.push_back(sg.e);
+        seg_ioff.push_back(uint32_t(inst_list.size())); seg_icnt.push_back(uint32_t(sg.insts.size()));
+        for (uint32_t x : sg.insts) inst_list.push_back(uint16_t(x));
+        cn_max = std::max<uint32_t>(cn_max, uint32_t(sg.insts.size()));
+      }
+      seg_off.push_back(uint32_t(seg_start.size()));
+      class_size[c] = double(pg::frag_size(classes[c]));
+    }
+    std::vector<double> node_size(f->n + 1);
+    for (uint32_t v = 0; v < f->n; ++v) node_size[v] = class_size[node_class[v]];
+    node_size[f->n] = class_size[0];
+    std::vector<uint32_t> chain_off{0};
+    std::vector<uint16_t> chain_anc;
+    std::vector<uint64_t> chain_key;
+    for (size_t y = 0; y < insts.size(); ++y) {
+      for (int32_t cur = int32_t(y); insts[cur].parent >= 0; cur = insts[cur].parent) {
+        chain_anc.push_back(uint16_t(insts[cur].parent));
+        chain_key.push_back(insts[cur].key);
+      }
+      chain_off.push_back(uint32_t(chain_anc.size()));
+    }
+    pl->has_cna = classes.size() > 1 || insts.size() > 2;
+    pl->cn_max = std::max<uint32_t>(cn_max, 2);
+    pl->n_classes = uint32_t(classes.size());
+    pl->node_class_h = node_class;
+    pl->node_class = upload(P, node_class, st);
+    pl->seg_off_h = seg_off; pl->seg_start_h = seg_start; pl->seg_end_h = seg_end; pl->seg_icnt_h = seg_icnt;
+    pl->seg_off = upload(P, seg_off, st); pl->seg_start = upload(P, seg_start, st); pl->seg_end = upload(P, seg_end, st);
+    pl->seg_ioff = upload(P, seg_ioff, st); pl->seg_icnt = upload(P, seg_icnt, st);
+    if (inst_list.empty()) inst_list.push_back(0);
+    pl->inst_list = upload(P, inst_list, st);
+    if (chain_anc.empty()) { chain_anc.push_back(0); chain_key.push_back(0); }
+    pl->chain_off = upload(P, chain_off, st); pl->chain_anc = upload(P, chain_anc, st); pl->chain_key = upload(P, chain_key, st);
+    auto node_size_d = upload(P, node_size, st);
+    t.node_size = node_size_d.p;
+    t.gc = pl->classes_view();
 
-    Timer timer(st);
     // ---- per-edge counts and offsets
     const uint64_t ncell = uint64_t(f->n + 1) * E;
     DBuf<uint32_t> cnt_snv(P, ncell), cnt_id(P, ncell), off_snv(P, ncell), off_id(P, ncell);
@@ -790,43 +1019,59 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     const uint64_t n_all = n_snv + n_id + drv.size();
     require(n_all < (1ull << 31), "too many mutations for one placement call");
     // ---- outputs
-    auto pl = std::make_unique<pg_placed>();
     pl->eng = e; pl->n_nodes = f->n; pl->n_samples = f->n_samples;
     pl->tin = f->tin; pl->tout = f->tout; pl->leaves = f->leaves;
+    pl->leaf_cls.assign(f->n_samples, {});
+    {
+      std::vector<uint8_t> has_kid(f->n, 0);
+      for (uint32_t v = 0; v < f->n; ++v) if (f->parent[v] >= 0) has_kid[f->parent[v]] = 1;
+      for (uint32_t v = 0; v < f->n; ++v)
+        if (!has_kid[v] && f->sample[v] >= 0) pl->leaf_cls[f->sample[v]].push_back(node_class[v]);
+    }
     pl->M = n_all;
     DBuf<uint32_t> locus(P, n_all), edge(P, n_all), aux(P, n_all), attempt(P, n_all);
-    DBuf<uint8_t> cls(P, n_all), sig(P, n_all), allele(P, n_all), kind(P, n_all), nature(P, n_all);
-    pg::PlaceOut o{locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, kind.p, nature.p, attempt.p};
+    DBuf<uint8_t> cls(P, n_all), sig(P, n_all), kind(P, n_all), nature(P, n_all);
+    DBuf<uint16_t> allele(P, n_all), seqv(P, n_all);
+    pg::PlaceOut o{locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, seqv.p, kind.p, nature.p, attempt.p};
     DBuf<uint32_t> err(P, 1);
     ck(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st), "memset");
     pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), nullptr,
                                uint32_t(n_snv + n_id), 0, err.p, st);
     auto drv_d = upload(P, drv, st);
-    pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), uint32_t(n_snv + n_id), seed, st);
-    // ---- infinite sites
-    if (e->infinite_sites && n_snv + n_id > 0) {
+    pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), uint32_t(n_snv + n_id), st);
+    // ---- infinite sites, and loci drawn where the cell has no allele left
+    if ((e->infinite_sites || pl->has_cna) && n_snv + n_id > 0) {
       uint32_t cap = 1024;
       while (cap < 2 * n_all) cap <<= 1;
-      DBuf<uint32_t> hkeys(P, cap), ckeys(P, cap), cvals(P, cap), pend_a(P, n_snv + n_id), pend_b(P, n_snv + n_id);
+      const bool unique = e->infinite_sites;
+      DBuf<uint32_t> hkeys(P, unique ? cap : 1), ckeys(P, unique ? cap : 1), cvals(P, unique ? cap : 1);
+      DBuf<uint32_t> pend_a(P, n_snv + n_id), pend_b(P, n_snv + n_id);
       DBuf<uint8_t> lost(P, n_snv + n_id);
       DBuf<uint32_t> n_next(P, 1);
-      ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-      // drivers occupy their loci first
-      pg::sites_insert_accepted(hkeys.p, cap - 1, locus.p + n_snv + n_id, uint32_t(drv.size()), st);
+      if (unique) {
+        ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        // drivers occupy their loci first
+        pg::sites_insert_accepted(hkeys.p, cap - 1, locus.p + n_snv + n_id, uint32_t(drv.size()), st);
+      }
       const uint32_t* pending = nullptr;
       uint32_t n_pend = uint32_t(n_snv + n_id);
       uint32_t* next = pend_a.p;
       int round = 0;
       while (n_pend > 0) {
-        require(round < 256, "infinite sites model: no free locus left for some mutations");
-        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        require(round < 256, unique ? "infinite sites model: no free locus left for some mutations"
+                                    : "no allele left where some mutations were drawn");
         ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-        pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
-                        n_next.p, err.p, st);
+        if (unique) {
+          ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+          ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+          pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
+                          n_next.p, err.p, st);
+        } else {
+          pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_next.p, st);
+        }
         uint32_t nn = 0;
         ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-        ck(cudaStreamSynchronize(st), "infinite sites round");
+        ck(cudaStreamSynchronize(st), "redraw round");
         if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, nn,
                                            1, err.p, st);
         pending = next;
@@ -840,7 +1085,8 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     DBuf<uint32_t> bcnt(P, nb), bfill(P, nb), bpart(P, pg::scan_part_elems(nb, 1)), order(P, n_all);
     pl->locus = DBuf<uint32_t>(P, n_all); pl->edge = DBuf<uint32_t>(P, n_all); pl->aux = DBuf<uint32_t>(P, n_all);
     pl->attempt = DBuf<uint32_t>(P, n_all);
-    pl->cls = DBuf<uint8_t>(P, n_all); pl->sig = DBuf<uint8_t>(P, n_all); pl->allele = DBuf<uint8_t>(P, n_all);
+    pl->cls = DBuf<uint8_t>(P, n_all); pl->sig = DBuf<uint8_t>(P, n_all); pl->allele = DBuf<uint16_t>(P, n_all);
+    pl->seq = DBuf<uint16_t>(P, n_all);
     pl->kind = DBuf<uint8_t>(P, n_all); pl->nature = DBuf<uint8_t>(P, n_all);
     pg::sort_by_locus(o, uint32_t(n_all), e->G, bcnt.p, bfill.p, bpart.p, order.p, pl->view(), st);
     pl->kernel_ms = timer.stop();
@@ -868,12 +1114,43 @@ pg_status pg_placed_count(const pg_placed* p, uint64_t* n) {
   return guarded([&] { require(p && n, "NULL argument"); *n = p->M; });
 }
 
+pg_status pg_placed_cna_count(const pg_placed* p, uint64_t* n) {
+  return guarded([&] { require(p && n, "NULL argument"); *n = p->cnas.size(); });
+}
+
+pg_status pg_placed_cna_copy(const pg_placed* p, uint32_t* node, uint8_t* type, uint32_t* chr, uint32_t* begin,
+                             uint32_t* end, uint32_t* allele, uint32_t* src_allele, uint8_t* driver) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    for (size_t i = 0; i < p->cnas.size(); ++i) {
+      const CnaOut& c = p->cnas[i];
+      if (node) node[i] = c.node;
+      if (type) type[i] = c.type;
+      if (chr) chr[i] = c.chr;
+      if (begin) begin[i] = c.begin;
+      if (end) end[i] = c.end;
+      if (allele) allele[i] = c.allele;
+      if (src_allele) src_allele[i] = c.src;
+      if (driver) driver[i] = c.driver;
+    }
+  });
+}
+
+pg_status pg_placed_node_classes(const pg_placed* p, uint32_t* node_class, uint32_t* n_classes, uint32_t* cn_max) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    if (node_class) std::copy(p->node_class_h.begin(), p->node_class_h.begin() + p->n_nodes, node_class);
+    if (n_classes) *n_classes = p->n_classes;
+    if (cn_max) *cn_max = p->cn_max;
+  });
+}
+
 pg_status pg_placed_kernel_ms(const pg_placed* p, float* ms) {
   return guarded([&] { require(p && ms, "NULL argument"); *ms = p->kernel_ms; });
 }
 
 pg_status pg_placed_copy(const pg_placed* p, uint32_t* locus, uint32_t* edge, uint32_t* aux, uint8_t* cls,
-                         uint8_t* sig, uint8_t* allele, uint8_t* kind, uint8_t* nature) {
+                         uint8_t* sig, uint16_t* allele, uint8_t* kind, uint8_t* nature) {
   return guarded([&] {
     require(p != nullptr, "NULL handle");
     select_device(p->eng);
@@ -883,7 +1160,7 @@ pg_status pg_placed_copy(const pg_placed* p, uint32_t* locus, uint32_t* edge, ui
       if (dst) ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, p->eng->st), "copy");
     };
     cp(locus, p->locus.p, 4 * n); cp(edge, p->edge.p, 4 * n); cp(aux, p->aux.p, 4 * n);
-    cp(cls, p->cls.p, n); cp(sig, p->sig.p, n); cp(allele, p->allele.p, n); cp(kind, p->kind.p, n);
+    cp(cls, p->cls.p, n); cp(sig, p->sig.p, n); cp(allele, p->allele.p, 2 * n); cp(kind, p->kind.p, n);
     cp(nature, p->nature.p, n);
     ck(cudaStreamSynchronize(p->eng->st), "copy");
   });
@@ -1020,6 +1297,7 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     // ---- samples and Euler numbering of normal cells / preneoplastic edge
     const uint32_t N = pl->n_nodes;
     std::vector<pg::SeqSample> samples;
+    std::vector<int32_t> sample_src;   // forest sample of each sequenced sample, -1 for the normal one
     std::vector<uint32_t> leaf_tin;
     if (!c->normal_only) {
       double nthr = std::floor((1.0 - c->purity) * 4294967296.0);
@@ -1033,14 +1311,79 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
         ss.all_normal = c->purity <= 0 ? 1u : 0u;
         leaf_tin.insert(leaf_tin.end(), pl->leaves[s].begin(), pl->leaves[s].end());
         samples.push_back(ss);
+        sample_src.push_back(int32_t(s));
       }
     }
     if (c->normal_only || c->with_normal_sample) {
       pg::SeqSample ss{};
       ss.n_leaves = 0; ss.leaf_off = 0; ss.normal_thr = 0; ss.all_normal = 1;
       samples.push_back(ss);
+      sample_src.push_back(-1);
+    }
+    // ---- with copy-number events: DNA mass of every (sample, tile) and the
+    // copy slots of its rejection draw.  A cell is normal with probability
+    // wn = normal_thr / 2^32 (1 for the normal sample), else one of the
+    // sample's n leaves; mass(tile) = wn * I_0 + (1 - wn) / n * sum over the
+    // leaves' classes c of n_c * I_c, I_c being the copies of class c summed
+    // over the tile's start positions (integers, exact), accumulated in tile
+    // order per chromosome.
+    std::vector<double> mass_cum, mass_tot;
+    std::vector<uint32_t> tile_cn;
+    if (pl->has_cna) {
+      const size_t NS = samples.size(), NT = n_tiles, NSL = c_id.size();
+      mass_cum.assign(NS * NT, 0.0); mass_tot.assign(NS * NSL, 0.0); tile_cn.assign(NS * NT, 1u);
+      auto class_tiles = [&](uint32_t cls, std::vector<uint64_t>& sum, std::vector<uint32_t>& mx) {
+        sum.assign(NT, 0); mx.assign(NT, 0);
+        uint32_t j = pl->seg_off_h[cls];
+        const uint32_t je = pl->seg_off_h[cls + 1];
+        for (size_t t = 0; t < NT; ++t) {
+          const uint32_t a = t_start[t], b = t_start[t] + t_len[t];
+          while (j < je && pl->seg_end_h[j] <= a) ++j;
+          for (uint32_t q = j; q < je && pl->seg_start_h[q] < b; ++q) {
+            const uint32_t x = std::max(a, pl->seg_start_h[q]), y = std::min(b, pl->seg_end_h[q]);
+            if (x < y) { sum[t] += uint64_t(y - x) * pl->seg_icnt_h[q]; mx[t] = std::max(mx[t], pl->seg_icnt_h[q]); }
+          }
+        }
+      };
+      std::vector<uint64_t> s0, sc;
+      std::vector<uint32_t> m0, mc;
+      class_tiles(0, s0, m0);
+      for (size_t s = 0; s < NS; ++s) {
+        const double wn = samples[s].all_normal ? 1.0 : double(samples[s].normal_thr) * (1.0 / 4294967296.0);
+        const double wt = 1.0 - wn;
+        std::vector<uint64_t> S(NT, 0);
+        std::vector<uint32_t> mx(NT, 0);
+        if (wn > 0) mx = m0;
+        uint64_t nl = 0;
+        if (wt > 0 && sample_src[s] >= 0) {
+          std::map<uint32_t, uint64_t> per_class;
+          for (uint32_t k : pl->leaf_cls[sample_src[s]]) per_class[k] += 1;
+          for (const auto& kv : per_class) {
+            class_tiles(kv.first, sc, mc);
+            for (size_t t = 0; t < NT; ++t) { S[t] += kv.second * sc[t]; mx[t] = std::max(mx[t], mc[t]); }
+            nl += kv.second;
+          }
+        }
+        for (size_t slot = 0; slot < NSL; ++slot) {
+          double acc = 0.0;
+          for (uint32_t k = 0; k < c_ntiles[slot]; ++k) {
+            const size_t t = c_first[slot] + k;
+            mass_cum[s * NT + t] = acc;
+            double m = wn * double(s0[t]);
+            if (nl > 0) m = m + (wt / double(nl)) * double(S[t]);
+            acc = acc + m;
+            tile_cn[s * NT + t] = std::max<uint32_t>(1u, mx[t]);
+          }
+          mass_tot[s * NSL + slot] = acc;
+        }
+      }
     }
     if (leaf_tin.empty()) leaf_tin.push_back(N);
+    std::vector<uint32_t> leaf_cls;
+    if (!c->normal_only)
+      for (uint32_t s2 = 0; s2 < pl->n_samples; ++s2)
+        leaf_cls.insert(leaf_cls.end(), pl->leaf_cls[s2].begin(), pl->leaf_cls[s2].end());
+    if (leaf_cls.empty()) leaf_cls.push_back(0);
     std::vector<uint32_t> etin(N + 2), etout(N + 2);
     for (uint32_t v = 0; v < N; ++v) { etin[v] = pl->tin[v]; etout[v] = pl->tout[v]; }
     etin[N] = 0; etout[N] = c->preneoplastic_in_normal ? N + 1 : N;   // preneoplastic edge
@@ -1081,8 +1424,12 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     DBuf<pg::SeqRec> recs(P, pl->M);
     DBuf<uint32_t> pair_cnt(P, uint64_t(n_tiles) * samples.size()), rlo(P, n_tiles), rhi(P, n_tiles);
     pg::seq_build_records(pl->view(), uint32_t(pl->M), etin_d.p, etout_d.p, recs.p, st);
+    DBuf<double> mcum_d, mtot_d;
+    DBuf<uint32_t> tcn_d;
+    if (pl->has_cna) { mcum_d = upload(P, mass_cum, st); mtot_d = upload(P, mass_tot, st); tcn_d = upload(P, tile_cn, st); }
     pg::seq_tile_counts(uint32_t(samples.size()), uint32_t(b_slot.size()), bs_d.p, bi_d.p, cf_d.p, cnt_d.p, cd_d.p,
-                        cns_d.p, cid_d.p, cp_d.p, T, n_tiles, seed, pair_cnt.p, st);
+                        cns_d.p, cid_d.p, cp_d.p, T, n_tiles, pl->has_cna ? mcum_d.p : nullptr,
+                        pl->has_cna ? mtot_d.p : nullptr, uint32_t(c_id.size()), seed, pair_cnt.p, st);
     pg::seq_tile_ranges(recs.p, uint32_t(pl->M), ts_d.p, tl_d.p, n_tiles, span, rlo.p, rhi.p, st);
     pg::SeqTiles tiles{n_tiles, ts_d.p, tl_d.p, te_d.p, rlo.p, rhi.p};
     pg::SeqParams prm{};
@@ -1093,6 +1440,14 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     prm.err_thr = et >= 4294967295.0 ? 0xffffffffu : uint32_t(et);
     prm.normal_tin = N;
     prm.n_alleles = 2;
+    auto leaf_cls_d = upload(P, leaf_cls, st);
+    prm.has_cna = pl->has_cna ? 1u : 0u;
+    prm.cn_max = pl->cn_max;
+    prm.gc = pl->classes_view();
+    prm.leaf_cls = leaf_cls_d.p;
+    prm.chain_off = pl->chain_off.p; prm.chain_anc = pl->chain_anc.p; prm.chain_key = pl->chain_key.p;
+    prm.tile_cn = pl->has_cna ? tcn_d.p : nullptr;
+    prm.n_tiles = n_tiles;
     Timer timer(st);
     pg::seq_reads(recs.p, uint32_t(pl->M), tiles, pair_cnt.p, smp_d.p, uint32_t(samples.size()), leaf_d.p, prm, seed,
                   res->alt.p, res->depth.p, st);

@@ -56,4 +56,38 @@ enum : uint32_t {
 enum : uint8_t { KIND_SNV = 0, KIND_INDEL = 1 };
 enum : uint8_t { NATURE_PASSENGER = 0, NATURE_DRIVER = 1, NATURE_PRENEOPLASTIC = 2, NATURE_GERMINAL = 3 };
 
+constexpr uint32_t LOCUS_INVALID = 0xffffffffu;   // a drawn position no allele of the cell covers
+// Order of a mutation among the events of its edge.  Copy events (CNA
+// amplifications, WGD) at event index j have order j + 1 and drivers at event
+// index j have order j, so a copy follows a driver exactly when its index is
+// larger; passengers follow every event of their edge; preneoplastic
+// mutations precede every event of the forest (their edge shares preorder
+// index 0 with the first root).
+constexpr uint16_t SEQ_PASSENGER = 0x7fff;
+constexpr uint16_t SEQ_PRENEOPLASTIC = 0;
+constexpr uint32_t SEQ_MAX_EVENTS = 0x7ffd;       // events per edge (orders 1..0x7ffe)
+
+}  // namespace pg
+
+#include "pg_kernels.h"
+
+namespace pg {
+
+// allele instances of genotype class `cls` covering absolute position `pos`:
+// returns their number and sets *ioff (their first index in inst_list)
+__device__ __forceinline__ uint32_t covering(const GenomeClasses& g, uint32_t cls, uint32_t pos, uint32_t* ioff) {
+  const uint32_t b = __ldg(g.seg_off + cls), e = __ldg(g.seg_off + cls + 1);
+  if (b == e) return 0;
+  uint32_t lo = b, hi = e;                 // last segment starting at or before pos
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(g.seg_start + mid) <= pos) lo = mid; else hi = mid;
+  }
+  if (__ldg(g.seg_start + lo) <= pos && pos < __ldg(g.seg_end + lo)) {
+    *ioff = __ldg(g.seg_ioff + lo);
+    return __ldg(g.seg_icnt + lo);
+  }
+  return 0;
+}
+
 }  // namespace pg

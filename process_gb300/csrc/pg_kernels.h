@@ -29,6 +29,23 @@ void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_of
                 const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
                 const uint32_t* list_len, uint32_t* lists, cudaStream_t st);
 
+// ---------------------------------------------------------------- genome classes
+// Copy-number events are rare, so the cells of a forest fall into few
+// genotype classes: the genome below each CNA/WGD event edge.  A class is a
+// list of segments (absolute [start, end), ascending) with the sorted ids of
+// the allele instances covering each segment.  Class 0 is the germline:
+// instances 0 and 1 over every chromosome.
+struct GenomeClasses {
+  uint32_t n_classes;
+  const uint32_t* node_class;   // class of each edge's genome after its own events (n_nodes + 1 entries)
+  const uint32_t* seg_off;      // n_classes + 1
+  const uint32_t* seg_start;
+  const uint32_t* seg_end;
+  const uint32_t* seg_ioff;     // covering instances: inst_list[seg_ioff, seg_ioff + seg_icnt)
+  const uint32_t* seg_icnt;
+  const uint16_t* inst_list;
+};
+
 // ---------------------------------------------------------------- placement
 struct PlaceTables {
   // forest (device)
@@ -42,7 +59,9 @@ struct PlaceTables {
   const double* epoch_start;
   const double* snv_rate;
   const double* indel_rate;
-  double allelic_size;
+  const double* cna_rate;       // per species (passenger CNAs per base per division)
+  const double* node_size;      // allelic size of each edge's genome (n_nodes + 1 entries)
+  GenomeClasses gc;
   // signatures: exposure CDFs [(n_epochs+1) rows][n_sigs], class CDFs [n_sigs][classes]
   uint32_t n_sbs_sigs, n_id_sigs;
   const uint32_t* sbs_expo_cdf;
@@ -62,24 +81,28 @@ struct PlaceOut {
   uint32_t* aux;      // SNV: alt base; indel: descriptor
   uint8_t* cls;       // SBS96 / ID83 class, 0xff for drivers
   uint8_t* sig;       // signature index (cause), 0xff for drivers
-  uint8_t* allele;
+  uint16_t* allele;   // allele instance
+  uint16_t* seq;      // order on the edge: driver event index, 0x7fff passengers, 0 preneoplastic
   uint8_t* kind;
   uint8_t* nature;
   uint32_t* attempt;
 };
 
 struct DriverRec {
-  uint32_t locus, edge, aux, allele;  // allele 0xff = random
+  uint32_t locus, edge, aux, allele, seq;   // allele: the instance, chosen on the host
   uint8_t kind, pad[3];
 };
 
+void place_cna_counts(const PlaceTables& t, uint32_t* cnt_cna, uint64_t seed, double germline_size, cudaStream_t st);
 void place_edge_counts(const PlaceTables& t, uint32_t* cnt_snv, uint32_t* cnt_id, uint64_t seed,
                        uint32_t n_pre_snv, uint32_t n_pre_id, cudaStream_t st);
 void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
                             const uint32_t* off_id, uint32_t n_snv, uint32_t n_id, const uint32_t* pending,
                             uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st);
-void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, uint64_t seed,
-                   cudaStream_t st);
+void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, cudaStream_t st);
+// slots whose locus is invalid (no allele covers the drawn position) -> next list
+void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
+                           uint32_t* n_next, cudaStream_t st);
 void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st);
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
                  uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
@@ -92,7 +115,7 @@ void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, ui
 struct SeqRec {            // 16 B, one per placed mutation, sorted by locus
   uint32_t locus;
   uint32_t tin, tout;      // Euler interval of the edge that carries it
-  uint32_t info;           // allele | kind << 8
+  uint32_t info;           // instance | (order on the edge & 0x7fff) << 16 | kind << 31
 };
 
 // fragments the read kernel handles per shared-memory batch (5 per thread);
@@ -125,6 +148,17 @@ struct SeqParams {
   uint32_t err_thr;        // substitution error iff u < err_thr
   uint32_t normal_tin;     // Euler index of normal cells
   uint32_t n_alleles;
+  // copy-number state (has_cna == 0: every cell has instances 0 and 1 everywhere)
+  uint32_t has_cna;
+  uint32_t cn_max;         // largest number of instances covering a position
+  GenomeClasses gc;
+  const uint32_t* leaf_cls;   // class of each leaf, parallel to leaf_tin
+  const uint32_t* chain_off;  // instance lineage: for instance y, ancestors chain_anc[chain_off[y]..]
+  const uint16_t* chain_anc;  //   with the order key (tin << 16 | seq) of the copy that led towards y
+  const uint64_t* chain_key;
+  const uint32_t* tile_cn;    // per (sample, tile): copy slots of the rejection draw (>= the largest
+                              //   copy number of the tile's starts in the sample's cells)
+  uint32_t n_tiles;
 };
 
 void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_tin, const uint32_t* edge_tout,
@@ -133,11 +167,15 @@ void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start,
                      uint32_t n_tiles, uint32_t span, uint32_t* rlo, uint32_t* rhi, cudaStream_t st);
 // per (sample, tile) pair counts: multinomial split of each chromosome's
 // pair count over its tiles by a binary tree of binomial draws, one thread
-// per (sample, block of 64 tiles)
+// per (sample, block of 64 tiles).  Tiles weigh their number of start
+// positions, or (mass_cum != NULL) their DNA mass: mass_cum[s * n_tiles + t]
+// is the sample's mass of the chromosome's tiles before t and
+// mass_tot[s * n_slots + slot] the chromosome's total.
 void seq_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* blk_slot, const uint32_t* blk_index,
                      const uint32_t* chr_first_tile, const uint32_t* chr_ntiles, const uint32_t* chr_depth,
                      const uint32_t* chr_nstarts, const uint32_t* chr_id, const uint64_t* chr_pairs,
-                     uint32_t tile_size, uint32_t n_tiles, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st);
+                     uint32_t tile_size, uint32_t n_tiles, const double* mass_cum, const double* mass_tot,
+                     uint32_t n_slots, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st);
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
                const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st);

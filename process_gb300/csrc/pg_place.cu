@@ -59,8 +59,8 @@ __global__ void k_edge_counts(PlaceTables t, uint32_t* __restrict__ cnt_snv, uin
     while (e + 1 < E && t.epoch_start[e + 1] <= tj) ++e;
     ndiv[e] += 1;
   }
+  const double A = t.node_size[v];   // allelic size of the edge's genome
   for (uint32_t e = 0; e < E; ++e) {
-    const double A = t.allelic_size;
     const double lam_s = t.snv_rate[sp * E + e] * A * double(ndiv[e]);
     const double lam_i = t.indel_rate[sp * E + e] * A * double(ndiv[e]);
     Stream s1{key, e, v, 0u, TAG_EDGE_SNV, 0u};
@@ -68,6 +68,17 @@ __global__ void k_edge_counts(PlaceTables t, uint32_t* __restrict__ cnt_snv, uin
     cnt_snv[uint64_t(v) * E + e] = uint32_t(poisson(s1, lam_s));
     cnt_id[uint64_t(v) * E + e] = uint32_t(poisson(s2, lam_i));
   }
+}
+
+// passenger CNA events per edge: Poisson(rate_cna[species] * 2G * divisions);
+// the germline size is used so that the counts do not depend on the copy
+// number the events themselves create
+__global__ void k_cna_counts(PlaceTables t, uint32_t* __restrict__ cnt_cna, Key key, double germline_size) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= t.n_nodes) return;
+  const double lam = t.cna_rate[t.species[v]] * germline_size * double(t.divisions[v]);
+  Stream st{key, 0u, v, 0u, TAG_EDGE_CNA, 0u};
+  cnt_cna[v] = uint32_t(poisson(st, lam));
 }
 
 // ------------------------------------------------------------ placement
@@ -112,6 +123,7 @@ __global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __re
     o.edge[slot] = v;
     o.nature[slot] = (v == t.n_nodes) ? NATURE_PRENEOPLASTIC : NATURE_PASSENGER;
     o.kind[slot] = is_id ? KIND_INDEL : KIND_SNV;
+    o.seq[slot] = (v == t.n_nodes) ? SEQ_PRENEOPLASTIC : SEQ_PASSENGER;
     o.attempt[slot] = 0;
   } else {
     cls = o.cls[slot];
@@ -132,7 +144,14 @@ __global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __re
   if (len == 0) { atomicOr(err, ERR_EMPTY_CLASS); o.locus[slot] = 0; return; }
   const uint64_t j = uniform_index64(r.x, r.y, len);
   const uint32_t p = is_id ? t.id_lists[t.id_off[list] + j] : t.ctx_lists[t.ctx_off[list] + j];
-  o.allele[slot] = uint8_t(uniform_index32(r.z, 2u));
+  // the allele: uniform among the instances of the edge's genome covering the locus
+  {
+    const uint32_t loc = is_id ? p - 1 : p;
+    uint32_t ioff = 0;
+    const uint32_t n = covering(t.gc, t.gc.node_class[v], loc, &ioff);
+    if (n == 0) { o.locus[slot] = LOCUS_INVALID; return; }   // deleted here: redrawn next round
+    o.allele[slot] = t.gc.inst_list[ioff + uniform_index32(r.z, n)];
+  }
   if (!is_id) {
     const uint32_t ref = base_at(t.genome, p);
     const uint32_t alt_pyr = sbs_class_alt(int(cls));
@@ -204,7 +223,7 @@ __global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t
   if (i >= n) return;
   const uint32_t slot = pending ? pending[i] : i;
   const uint32_t k = locus[slot];
-  if (hset_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
+  if (k == LOCUS_INVALID || hset_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
   lost[i] = 0;
   const uint32_t h = hset_insert(ckeys, cmask, k);
   if (h == EMPTY) { atomicOr(err, ERR_CAPACITY); return; }
@@ -238,9 +257,10 @@ __global__ void k_cand_resolve(const uint32_t* __restrict__ locus, const uint32_
 }
 
 // ------------------------------------------------------------ drivers
-// Driver SIDs are applied on the first edge of their mutant; a random allele
-// (RANDOM_ALLELE in src/mutation_engine.cpp:789-848) is drawn per driver.
-__global__ void k_drivers(PlaceOut o, const DriverRec* __restrict__ drv, uint32_t n_drv, uint32_t base_slot, Key key) {
+// Driver SIDs are applied on the first edge of their mutant, in application
+// order with the mutant's CNAs and WGDs; their instance and order on the edge
+// come from the host, which replays those events.
+__global__ void k_drivers(PlaceOut o, const DriverRec* __restrict__ drv, uint32_t n_drv, uint32_t base_slot) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_drv) return;
   const DriverRec d = drv[i];
@@ -253,12 +273,16 @@ __global__ void k_drivers(PlaceOut o, const DriverRec* __restrict__ drv, uint32_
   o.aux[slot] = d.aux;
   o.nature[slot] = NATURE_DRIVER;
   o.attempt[slot] = 0;
-  uint32_t a = d.allele;
-  if (a == 0xffu) {
-    const U4 r = philox(key.k0, key.k1, i, d.edge, 0u, TAG_DRIVER);
-    a = uniform_index32(r.x, 2u);
-  }
-  o.allele[slot] = uint8_t(a);
+  o.allele[slot] = uint16_t(d.allele);
+  o.seq[slot] = uint16_t(d.seq);
+}
+
+__global__ void k_collect_invalid(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending,
+                                  uint32_t n, uint32_t* __restrict__ next, uint32_t* __restrict__ n_next) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t slot = pending ? pending[i] : i;
+  if (locus[slot] == LOCUS_INVALID) next[atomicAdd(n_next, 1u)] = slot;
 }
 
 // ------------------------------------------------------------ locus sort
@@ -300,12 +324,16 @@ __global__ void k_gather_sorted(PlaceOut o, const uint32_t* __restrict__ order, 
   if (i >= n) return;
   const uint32_t x = order[i];
   s.locus[i] = o.locus[x]; s.edge[i] = o.edge[x]; s.aux[i] = o.aux[x];
-  s.cls[i] = o.cls[x]; s.sig[i] = o.sig[x]; s.allele[i] = o.allele[x];
+  s.cls[i] = o.cls[x]; s.sig[i] = o.sig[x]; s.allele[i] = o.allele[x]; s.seq[i] = o.seq[x];
   s.kind[i] = o.kind[x]; s.nature[i] = o.nature[x]; s.attempt[i] = o.attempt[x];
 }
 
 // ------------------------------------------------------------ host launchers
 static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
+
+void place_cna_counts(const PlaceTables& t, uint32_t* cnt_cna, uint64_t seed, double germline_size, cudaStream_t st) {
+  if (t.n_nodes) { k_cna_counts<<<nblk(t.n_nodes, 128), 128, 0, st>>>(t, cnt_cna, make_key(seed), germline_size); note_launch(); }
+}
 
 void place_edge_counts(const PlaceTables& t, uint32_t* cnt_snv, uint32_t* cnt_id, uint64_t seed,
                        uint32_t n_pre_snv, uint32_t n_pre_id, cudaStream_t st) {
@@ -320,10 +348,14 @@ void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t se
                                            redraw, err); note_launch();
 }
 
-void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, uint64_t seed,
-                   cudaStream_t st) {
+void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, cudaStream_t st) {
   if (n_drv == 0) return;
-  k_drivers<<<nblk(n_drv), 256, 0, st>>>(o, drv, n_drv, base_slot, make_key(seed)); note_launch();
+  k_drivers<<<nblk(n_drv), 256, 0, st>>>(o, drv, n_drv, base_slot); note_launch();
+}
+
+void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
+                           uint32_t* n_next, cudaStream_t st) {
+  if (n) { k_collect_invalid<<<nblk(n), 256, 0, st>>>(locus, pending, n, next, n_next); note_launch(); }
 }
 
 void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st) {

@@ -62,7 +62,7 @@ __global__ void k_seq_records(PlaceOut s, uint32_t n, const uint32_t* __restrict
   r.locus = s.locus[i];
   r.tin = edge_tin[e];
   r.tout = edge_tout[e];
-  r.info = uint32_t(s.allele[i]) | (uint32_t(s.kind[i]) << 8);
+  r.info = uint32_t(s.allele[i]) | ((uint32_t(s.seq[i]) & 0x7fffu) << 16) | (uint32_t(s.kind[i]) << 31);
   recs[i] = r;
 }
 
@@ -86,20 +86,34 @@ __global__ void k_tile_ranges(const SeqRec* __restrict__ recs, uint32_t n_recs, 
 // tree over the padded range [0, 2^D) of tiles (D = ceil(log2 n)); the node
 // with heap id h at depth d covers tiles [i 2^(D-d), (i+1) 2^(D-d)) and sends
 // Binomial(count, w_left / w_node) fragments to its left half, w being the
-// number of start positions of the covered tiles.  Every node's draw uses
-// Philox counter (h, chromosome, sample, TAG_TILE_SPLIT).
+// number of start positions of the covered tiles or, with copy-number
+// events, their DNA mass in the sample (so that fragments are proportional
+// to copy number across tiles; the rejection draw of the start makes them so
+// within a tile).  Every node's draw uses Philox counter
+// (h, chromosome, sample, TAG_TILE_SPLIT).
 struct TileSplit {
-  uint64_t S;     // start positions of the chromosome
-  uint32_t T;     // tile size
+  uint64_t S;            // start positions of the chromosome
+  uint32_t T;            // tile size
+  uint32_t nt;           // tiles of the chromosome
+  const double* cum;     // mass before each tile (NULL: weigh start positions)
+  double tot;            // mass of the chromosome
   __device__ __forceinline__ uint64_t w(uint64_t a, uint64_t b) const {   // start positions of tiles [a, b)
     const uint64_t x = a * T < S ? a * T : S, y = b * T < S ? b * T : S;
     return y - x;
   }
+  __device__ __forceinline__ double c(uint64_t a) const { return a < nt ? cum[a] : tot; }
   __device__ __forceinline__ uint64_t left(Key key, uint32_t h, uint32_t chr, uint32_t s, uint64_t n, uint64_t lo,
                                            uint64_t mid, uint64_t hi) const {
-    const uint64_t wt = w(lo, hi);
-    if (n == 0 || wt == 0) return 0;
-    const double p = double(w(lo, mid)) / double(wt);
+    double p;
+    if (cum == nullptr) {
+      const uint64_t wt = w(lo, hi);
+      if (n == 0 || wt == 0) return 0;
+      p = double(w(lo, mid)) / double(wt);
+    } else {
+      const double base = c(lo), wt = c(hi) - base;
+      if (n == 0 || !(wt > 0.0)) return 0;
+      p = (c(mid) - base) / wt;
+    }
     Stream st{key, h, chr, s, TAG_TILE_SPLIT, 0u};
     return binomial(st, n, p);
   }
@@ -113,14 +127,17 @@ __global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint3
                               const uint32_t* __restrict__ blk_index, const uint32_t* __restrict__ chr_first_tile,
                               const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
                               const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
-                              const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles, Key key,
-                              uint32_t* __restrict__ pair_cnt) {
+                              const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles,
+                              const double* __restrict__ mass_cum, const double* __restrict__ mass_tot,
+                              uint32_t n_slots, Key key, uint32_t* __restrict__ pair_cnt) {
   const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (gid >= uint64_t(n_blocks) * n_samples) return;
   const uint32_t s = uint32_t(gid / n_blocks), bi = uint32_t(gid % n_blocks);
   const uint32_t slot = blk_slot[bi], b = blk_index[bi];
   const uint32_t D = chr_depth[slot], chr = chr_id[slot], nt = chr_ntiles[slot];
-  const TileSplit sp{chr_nstarts[slot], T};
+  const uint32_t base = chr_first_tile[slot];
+  const TileSplit sp{chr_nstarts[slot], T, nt, mass_cum ? mass_cum + uint64_t(s) * n_tiles + base : nullptr,
+                     mass_cum ? mass_tot[uint64_t(s) * n_slots + slot] : 0.0};
   const uint32_t Db = D < SPLIT_BLOCK_LOG ? D : SPLIT_BLOCK_LOG;   // depth of the block's subtree
   // root -> block node
   uint64_t n = chr_pairs[slot], lo = 0, size = uint64_t(1) << D;
@@ -145,7 +162,6 @@ __global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint3
     c[2 * r] = uint32_t(nl);
     c[2 * r + 1] = c[r] - uint32_t(nl);
   }
-  const uint32_t base = chr_first_tile[slot];
   for (uint32_t r = 0; r < (1u << Db); ++r) {
     const uint64_t tile = lo + r;
     if (tile < nt) pair_cnt[uint64_t(s) * n_tiles + base + tile] = c[(1u << Db) + r];
@@ -159,34 +175,77 @@ __device__ __forceinline__ uint32_t err_word(uint32_t w, uint32_t locus, uint32_
   return h;
 }
 
+// does allele instance y of the read's cell carry the mutation placed on
+// instance x with order key key_m (tin of its edge << 16 | order on the edge)?
+// y carries it when y is x, or when y descends from x through copies made
+// after the mutation (a copy's key exceeds the mutation's: both lie on the
+// cell's root path, where tin grows with depth)
+__device__ __forceinline__ bool inst_carries(const SeqParams& prm, uint32_t y, uint32_t x, uint64_t key_m) {
+  if (y == x) return true;
+  if (!prm.has_cna) return false;
+  for (uint32_t q = __ldg(prm.chain_off + y), e = __ldg(prm.chain_off + y + 1); q < e; ++q)
+    if (__ldg(prm.chain_anc + q) == x) return __ldg(prm.chain_key + q) > key_m;
+  return false;
+}
+
 // did the visit observe the alt base?
-__device__ __forceinline__ bool observed(uint32_t tin, uint32_t tout, uint32_t info, uint32_t cell, uint32_t allele,
-                                         uint32_t w, uint32_t locus, uint32_t mate, uint32_t err_thr) {
-  const bool carried = (tin <= cell) && (cell < tout) && ((info & 0xffu) == allele);
-  if ((info >> 8) & 1u) return carried;   // indel
+__device__ __forceinline__ bool observed(const SeqParams& prm, uint32_t tin, uint32_t tout, uint32_t info,
+                                         uint32_t cell, uint32_t inst, uint32_t w, uint32_t locus, uint32_t mate) {
+  const bool carried = (tin <= cell) && (cell < tout) &&
+                       inst_carries(prm, inst, info & 0xffffu, (uint64_t(tin) << 16) | ((info >> 16) & 0x7fffu));
+  if (info >> 31) return carried;   // indel
   const uint32_t e = err_word(w, locus, mate);
-  const bool err = e < err_thr;
+  const bool err = e < prm.err_thr;
   return carried ? !err : (err && (e % 3u) == 0u);
 }
 
-// one fragment's draws: mate starts, source cell, allele and its error word
+// one fragment's draws: mate starts, source cell, allele instance and its
+// error word.  With copy-number events the (start, cell, instance) triple is
+// drawn by rejection within the tile: slot u in [0, tile_cn) is kept when
+// more than u instances of the cell cover the start, which makes starts
+// proportional to copy number; attempt a >= 1 uses Philox block a of the
+// fragment's TAG_PAIR stream.  A fragment that finds no covering instance in
+// 256 attempts is dropped (inst = 0xffff).
 struct Fragment {
-  uint32_t p0, p1, cell, allele, w;
+  uint32_t p0, p1, cell, inst, w;
 };
+
+constexpr uint32_t FRAG_ATTEMPTS = 256;
 
 template <bool INS_SMEM>
 __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
                                                   uint32_t len, uint32_t ce, const SeqSample& sm,
                                                   const uint32_t* __restrict__ leaf_tin, const SeqParams& prm,
                                                   const uint32_t* ins, const uint16_t* guide) {
-  const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
+  U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
   const U4 r2 = philox(key.k0, key.k1, j, t, s, TAG_PAIR2);
   Fragment f;
   const uint32_t R = prm.read_len;
-  f.p0 = start + __umulhi(r.x, len);
-  const bool normal = sm.all_normal || r.y < sm.normal_thr;
-  f.cell = normal ? prm.normal_tin : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.z, sm.n_leaves));
-  f.allele = __umulhi(r.w, prm.n_alleles);
+  if (!prm.has_cna) {
+    f.p0 = start + __umulhi(r.x, len);
+    const bool normal = sm.all_normal || r.y < sm.normal_thr;
+    f.cell = normal ? prm.normal_tin : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.z, sm.n_leaves));
+    f.inst = __umulhi(r.w, prm.n_alleles);
+  } else {
+    f.inst = 0xffffu;
+    for (uint32_t att = 0; att < FRAG_ATTEMPTS; ++att) {
+      if (att) r = philox(key.k0, key.k1, j, t, s, TAG_PAIR | (att << 8));
+      f.p0 = start + __umulhi(r.x, len);
+      const bool normal = sm.all_normal || r.y < sm.normal_thr;
+      uint32_t cls = 0;
+      if (normal) {
+        f.cell = prm.normal_tin;
+      } else {
+        const uint32_t li = sm.leaf_off + __umulhi(r.z, sm.n_leaves);
+        f.cell = __ldg(leaf_tin + li);
+        cls = __ldg(prm.leaf_cls + li);
+      }
+      const uint32_t slot = __umulhi(r.w, __ldg(prm.tile_cn + uint64_t(s) * prm.n_tiles + t));
+      uint32_t ioff = 0;
+      const uint32_t n = covering(prm.gc, cls, f.p0, &ioff);
+      if (slot < n) { f.inst = __ldg(prm.gc.inst_list + ioff + slot); break; }
+    }
+  }
   f.w = r2.y;
   f.p1 = f.p0;
   if (prm.paired) {
@@ -215,7 +274,8 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
   __shared__ uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
   // mates of the batch in start-bucket order
   __shared__ uint16_t s_mpos[SEQ_MCAP];     // start offset in the window | mate << 15
-  __shared__ uint32_t s_mcell[SEQ_MCAP];    // cell | allele << 30
+  __shared__ uint32_t s_mcell[SEQ_MCAP];    // source cell (Euler index)
+  __shared__ uint16_t s_minst[SEQ_MCAP];    // allele instance (0xffff: dropped fragment)
   __shared__ uint32_t s_mw[SEQ_MCAP];       // the fragment's error word
   __shared__ uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
   __shared__ uint32_t s_ins[SEQ_INS_CAP];
@@ -242,13 +302,14 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
     // dense or long window: per-read loop over the global records
     for (uint32_t j = tid; j < n_pairs; j += SEQ_THREADS) {
       const Fragment f = make_fragment<false>(key, j, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
+      if (f.inst == 0xffffu) continue;   // dropped: no covering instance
       for (uint32_t mate = 0; mate < (prm.paired ? 2u : 1u); ++mate) {
         const uint32_t a = mate ? f.p1 : f.p0;
         for (uint32_t i = lower_bound_rec(grec, nw, a); i < nw; ++i) {
           const SeqRec r = grec[i];
           if (r.locus >= a + R) break;
           atomicAdd(gdep + i, 1u);
-          if (observed(r.tin, r.tout, r.info, f.cell, f.allele, f.w, r.locus, mate, prm.err_thr))
+          if (observed(prm, r.tin, r.tout, r.info, f.cell, f.inst, f.w, r.locus, mate))
             atomicAdd(galt + i, 1u);
         }
       }
@@ -274,7 +335,7 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
     __syncthreads();
     // phase A: fragments stay in registers; each mate takes its rank within
     // its start bucket from the histogram's atomic
-    uint32_t o0[FPT], o1[FPT], ca[FPT], fw[FPT], rk0[FPT], rk1[FPT];
+    uint32_t o0[FPT], o1[FPT], ca[FPT], fi[FPT], fw[FPT], rk0[FPT], rk1[FPT];
 #pragma unroll
     for (uint32_t q = 0; q < FPT; ++q) {
       const uint32_t k = tid + q * SEQ_THREADS;
@@ -282,7 +343,8 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
         const Fragment f = ins_smem
             ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide)
             : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
-        ca[q] = f.cell | (f.allele << 30);
+        ca[q] = f.cell;
+        fi[q] = f.inst;
         fw[q] = f.w;
         o0[q] = f.p0 - start;
         rk0[q] = atomicAdd(s_boff + o0[q] / SEQ_BW, 1u);
@@ -310,10 +372,11 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
       const uint32_t k = tid + q * SEQ_THREADS;
       if (k < nb_pairs) {
         const uint32_t x0 = s_boff[o0[q] / SEQ_BW] + rk0[q];
-        s_mpos[x0] = uint16_t(o0[q]); s_mcell[x0] = ca[q]; s_mw[x0] = fw[q];
+        s_mpos[x0] = uint16_t(o0[q]); s_mcell[x0] = ca[q]; s_minst[x0] = uint16_t(fi[q]); s_mw[x0] = fw[q];
         if (prm.paired) {
           const uint32_t x1 = s_boff[o1[q] / SEQ_BW] + rk1[q];
-          s_mpos[x1] = uint16_t(o1[q] | 0x8000u); s_mcell[x1] = ca[q]; s_mw[x1] = fw[q];
+          s_mpos[x1] = uint16_t(o1[q] | 0x8000u); s_mcell[x1] = ca[q]; s_minst[x1] = uint16_t(fi[q]);
+          s_mw[x1] = fw[q];
         }
       }
     }
@@ -363,11 +426,11 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
             base = s_wstart[i] - s_wpre[i];
           }
           const uint32_t x = base + k;
-          const uint32_t pm = s_mpos[x], ca = s_mcell[x], w = s_mw[x];   // independent loads
+          const uint32_t pm = s_mpos[x], ca = s_mcell[x], mi = s_minst[x], w = s_mw[x];   // independent loads
           const uint32_t o = pm & 0x7fffu;
-          if (o > off || o + R <= off) continue;              // the mate does not cover L
+          if (o > off || o + R <= off || mi == 0xffffu) continue;   // the mate does not cover L (or was dropped)
           dep += 1;
-          alt += observed(tin, tout, info, ca & 0x3fffffffu, ca >> 30, w, L, pm >> 15, prm.err_thr) ? 1u : 0u;
+          alt += observed(prm, tin, tout, info, ca, mi, w, L, pm >> 15) ? 1u : 0u;
         }
         if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
       }
@@ -399,11 +462,13 @@ void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start,
 void seq_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* blk_slot, const uint32_t* blk_index,
                      const uint32_t* chr_first_tile, const uint32_t* chr_ntiles, const uint32_t* chr_depth,
                      const uint32_t* chr_nstarts, const uint32_t* chr_id, const uint64_t* chr_pairs,
-                     uint32_t tile_size, uint32_t n_tiles, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st) {
+                     uint32_t tile_size, uint32_t n_tiles, const double* mass_cum, const double* mass_tot,
+                     uint32_t n_slots, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st) {
   const uint64_t n = uint64_t(n_samples) * n_blocks;
   if (n) { k_tile_counts<<<nblk(n, 64), 64, 0, st>>>(n_samples, n_blocks, blk_slot, blk_index, chr_first_tile,
                                                    chr_ntiles, chr_depth, chr_nstarts, chr_id, chr_pairs, tile_size,
-                                                   n_tiles, make_key(seed), pair_cnt); note_launch(); }
+                                                   n_tiles, mass_cum, mass_tot, n_slots, make_key(seed), pair_cnt);
+           note_launch(); }
 }
 
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,

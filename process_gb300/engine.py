@@ -95,6 +95,43 @@ class CNA:
     src_allele: int | None = None
 
 
+def load_passenger_CNAs(path, tumour_type: str = "", tumour_study: str = "") -> list[CNA]:
+    """Passenger CNA candidates from a tab-separated table with a header row
+    and the columns chr, begin, end, major, minor, tumour type, study
+    (load_passenger_CNAs, src/mutation_engine.cpp:441-487): rows of the
+    requested tumour type and study ("" = any) give an amplification when
+    major is NA or above 1 and a deletion when minor is NA or below 1, over
+    [begin, end]; duplicates are dropped."""
+    out = set()
+    with open(path) as fh:
+        rows = [ln.rstrip("\n").split("\t") for ln in fh]
+    for num, row in enumerate(rows[1:], start=2):
+        if not row or row == [""]:
+            continue
+        if len(row) < 7:
+            raise RuntimeError("The CNA CSV must contains at least 7 columns")
+        if (tumour_type and row[5] != tumour_type) or (tumour_study and row[6] != tumour_study):
+            continue
+        try:
+            begin, end = int(row[1]), int(row[2])
+        except ValueError:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"Unknown begin/end specification in row number {num}.")
+        if begin > end:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"The CNA begin lays after the end in row number {num}")
+        for col, amp in ((3, True), (4, False)):
+            v = row[col]
+            try:
+                hit = v == "NA" or (int(v) > 1 if amp else int(v) < 1)
+            except ValueError:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f"Unknown major/minor specification {v} in row number {num}.")
+            if hit:
+                out.add(("A" if amp else "D", row[0], begin, end + 1 - begin))
+
+    def key(c):
+        return (0, int(c[1]), "") if c[1].isdigit() else (1, 0, c[1])
+    return [CNA(t, ch, b, ln) for t, ch, b, ln in sorted(out, key=lambda c: (key(c), c[2], c[3], c[0]))]
+
+
 class _WGD:
     def __repr__(self):
         return "WGD"
@@ -206,7 +243,7 @@ class MutationEngine:
     def __init__(self, genome: GenomeSpec, SBS_signatures: Mapping[str, Sequence[float]] | None = None,
                  indel_signatures: Mapping[str, Sequence[float]] | None = None, context_sampling: int = 100,
                  max_motif_size: int = 50, max_repetition_storage: int = 500000,
-                 avoid_homozygous_losses: bool = True):
+                 avoid_homozygous_losses: bool = True, passenger_CNAs: Iterable | None = None):
         self.genome = genome
         self.chr_names = [str(c) for c in genome.chr_names]
         self.chr_lengths = np.asarray(genome.chr_lengths, dtype=np.uint32)
@@ -214,7 +251,6 @@ class MutationEngine:
         self.context_sampling = int(context_sampling)
         self.max_motif_size = int(max_motif_size)
         self.max_repetition_storage = int(max_repetition_storage)
-        self.avoid_homozygous_losses = bool(avoid_homozygous_losses)
         d = _lib.GenomeDesc()
         d.n_chr = len(self.chr_lengths)
         d.chr_lengths = ptr(self.chr_lengths, C.c_uint32)
@@ -236,10 +272,38 @@ class MutationEngine:
         self.species: dict[tuple[str, str], int] = {}
         self.species_rates: dict[tuple[str, str], dict] = {}
         self._exposures: list[tuple[float, dict]] = []
+        self.passenger_CNAs: list[CNA] = []
+        self.avoid_homozygous_losses = bool(avoid_homozygous_losses)
         if SBS_signatures:
             self.set_signatures(0, SBS_signatures)
         if indel_signatures:
             self.set_signatures(1, indel_signatures)
+        if passenger_CNAs:
+            self.add_passenger_CNAs(passenger_CNAs)
+
+    @property
+    def avoid_homozygous_losses(self) -> bool:
+        """Passenger deletions never remove the last allele of a region
+        (``avoid_homozygous_losses``, src/mutations.cpp:837-840, default TRUE)."""
+        return self._avoid_losses
+
+    @avoid_homozygous_losses.setter
+    def avoid_homozygous_losses(self, value: bool) -> None:
+        check(lib().pg_engine_set_avoid_homozygous_losses(self._h, 1 if value else 0))
+        self._avoid_losses = bool(value)
+
+    def add_passenger_CNAs(self, cnas: Iterable) -> None:
+        """Appends passenger CNA candidates (``CNA`` objects; the reference
+        loads them from its passenger-CNA table, src/mutation_engine.cpp:441-487,
+        see :func:`load_passenger_CNAs`).  A species with CNA rate r draws
+        Poisson(r * 2G * divisions) of them per edge, uniformly."""
+        for c in cnas:
+            if not isinstance(c, CNA) or c.type not in ("A", "D"):
+                raise DomainError(_lib.PG_ERR_DOMAIN, "passenger CNA candidates are CNA(\"A\"|\"D\", ...) objects")
+            ci = self._chr_index(c.chr)
+            check(lib().pg_engine_add_passenger_cna(self._h, ci, int(c.chr_pos), int(c.len),
+                                                    1 if c.type == "A" else 0))
+            self.passenger_CNAs.append(c)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -485,9 +549,12 @@ class PhylogeneticForest:
         if self._table is None:
             n = self.num_of_mutations
             t = {k: np.empty(n, dtype=np.uint32) for k in ("locus", "edge", "aux")}
-            t.update({k: np.empty(n, dtype=np.uint8) for k in ("cls", "sig", "allele", "kind", "nature")})
+            t.update({k: np.empty(n, dtype=np.uint8) for k in ("cls", "sig", "kind", "nature")})
+            t["allele"] = np.empty(n, dtype=np.uint16)
             check(lib().pg_placed_copy(self._h, *(ptr(t[k], C.c_uint32) for k in ("locus", "edge", "aux")),
-                                       *(ptr(t[k], C.c_uint8) for k in ("cls", "sig", "allele", "kind", "nature"))))
+                                       ptr(t["cls"], C.c_uint8), ptr(t["sig"], C.c_uint8),
+                                       ptr(t["allele"], C.c_uint16), ptr(t["kind"], C.c_uint8),
+                                       ptr(t["nature"], C.c_uint8)))
             self._table = t
         return self._table
 
@@ -565,6 +632,62 @@ class PhylogeneticForest:
             cols["ref"].append(ref[m]); cols["alt"].append(alt[m])
             cols["type"].append(np.where(t["kind"][m] == 0, "SNV", "indel"))
             cols["cause"].append(cause[m]); cols["class"].append(NATURES[t["nature"][m]])
+        return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
+
+    def cna_table(self) -> dict:
+        """Applied CNA / WGD events: node, type (0 deletion, 1 amplification,
+        2 WGD), chr index, 1-based begin/end, allele instance, source instance,
+        driver flag."""
+        n = C.c_uint64()
+        check(lib().pg_placed_cna_count(self._h, C.byref(n)))
+        m = n.value
+        t = {k: np.empty(m, dtype=np.uint32) for k in ("node", "chr", "begin", "end", "allele", "src")}
+        t.update({k: np.empty(m, dtype=np.uint8) for k in ("type", "driver")})
+        check(lib().pg_placed_cna_copy(self._h, ptr(t["node"], C.c_uint32), ptr(t["type"], C.c_uint8),
+                                       ptr(t["chr"], C.c_uint32), ptr(t["begin"], C.c_uint32),
+                                       ptr(t["end"], C.c_uint32), ptr(t["allele"], C.c_uint32),
+                                       ptr(t["src"], C.c_uint32), ptr(t["driver"], C.c_uint8)))
+        return t
+
+    def node_classes(self) -> tuple[np.ndarray, int, int]:
+        """Genotype class of every node, the number of classes and the largest copy number."""
+        f = self.forest
+        out = np.empty(f.num_of_nodes, dtype=np.uint32)
+        nc, cm = C.c_uint32(), C.c_uint32()
+        check(lib().pg_placed_node_classes(self._h, ptr(out, C.c_uint32), C.byref(nc), C.byref(cm)))
+        return out, nc.value, cm.value
+
+    def get_sampled_cell_CNAs(self, cell_id=None) -> dict:
+        """Columns cell_id, type ("A", "D"; "WGD" for a whole-genome doubling,
+        whose chr/begin/end are empty), chr, begin, end, allele, src allele
+        (NA, i.e. -1, for deletions) and class (src/phylogenetic_forest.cpp:509-562)."""
+        f = self.forest
+        c = self.cna_table()
+        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
+        if cell_id is not None:
+            hit = np.nonzero(f.cell_id == int(cell_id))[0]
+            if len(hit) == 0 or not f.is_leaf[hit[0]]:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f'Cell "{cell_id}" is not a leaf')
+            leaves = hit
+        names = np.array(self.engine.chr_names + [""], dtype=object)
+        tname = np.array(["D", "A", "WGD"], dtype=object)
+        cols = {k: [] for k in ("cell_id", "type", "chr", "begin", "end", "allele", "src allele", "class")}
+        for lf in leaves:
+            path = set()
+            v = int(lf)
+            while v >= 0:
+                path.add(v)
+                v = int(f.parent[v])
+            m = np.isin(c["node"], np.fromiter(path, dtype=np.int64))
+            wgd = c["type"][m] == 2
+            cols["cell_id"].append(np.full(m.sum(), f.cell_id[lf]))
+            cols["type"].append(tname[c["type"][m]])
+            cols["chr"].append(names[np.where(wgd, len(names) - 1, c["chr"][m])])
+            cols["begin"].append(np.where(wgd, -1, c["begin"][m].astype(np.int64)))
+            cols["end"].append(np.where(wgd, -1, c["end"][m].astype(np.int64)))
+            cols["allele"].append(np.where(wgd, -1, c["allele"][m].astype(np.int64)))
+            cols["src allele"].append(np.where(c["type"][m] == 1, c["src"][m].astype(np.int64), -1))
+            cols["class"].append(np.where(c["driver"][m] == 1, "driver", "passenger"))
         return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
 
     def get_samples_info(self) -> dict:

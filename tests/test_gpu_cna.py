@@ -1,0 +1,127 @@
+"""GPU parity with copy-number events: driver CNAs, whole-genome doubling,
+passenger CNAs drawn from candidates, avoid_homozygous_losses.  Bit-exact
+against the oracle's Philox replay: genotype classes, applied CNA records,
+placed mutations and sequencing alt/depth tables."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(seed, n_leaves, cna_rate=3e-9):
+    from process_gb300 import CNA, SNV, WGD, synth
+    w = synth.config1(seed=seed, n_leaves=n_leaves)
+    w.genome.chr_lengths = [600_000] * 3
+    (na, ra, _), (nb, rb, _) = w.mutants
+    w.mutants = [
+        (na, dict(ra, CNA=cna_rate), [SNV("1", 1000, "T", allele=0), CNA("A", "2", 100_001, 200_000),
+                                      WGD, CNA("D", "3", 500_001, 50_000, allele=1)]),
+        (nb, dict(rb, CNA=cna_rate), [CNA("D", "1", 1, 300_000), SNV("2", 150_000, "G"),
+                                      CNA("A", "2", 120_001, 10_000, src_allele=2)]),
+    ]
+    cands = [CNA("A", "1", 200_001, 30_000), CNA("D", "1", 400_001, 80_000), CNA("D", "2", 1, 50_000),
+             CNA("A", "3", 10_001, 100_000), CNA("D", "3", 300_001, 5_000)]
+    return w, cands
+
+
+def _pair(orc, w, cands, avoid, infinite):
+    from process_gb300 import synth
+    eng = synth.build_engine(w)
+    eng.add_passenger_CNAs(cands)
+    eng.avoid_homozygous_losses = avoid
+    eng.infinite_sites_model = infinite
+    o = orc.OracleEngine.like(w)
+    g = o.read_genome()
+    off = np.concatenate([[0], np.cumsum(np.asarray(w.genome.chr_lengths, dtype=np.int64))])
+    idx = {n: i for i, n in enumerate(w.genome.chr_names)}
+
+    def explicit(drivers):
+        out = []
+        for d in drivers:
+            if type(d).__name__ == "Mutation" and d.ref == "?":
+                d = type(d)(d.chr, d.chr_pos, "ACGT"[g[off[idx[d.chr]] + d.chr_pos - 1]], d.alt, d.allele)
+            out.append(d)
+        return out
+    for m, (_, _, drivers) in enumerate(w.mutants):
+        o.add_drivers(m, explicit(drivers), idx.__getitem__)
+    for c in cands:
+        o.add_passenger_cna(idx[c.chr], c.chr_pos, c.len, c.type == "A")
+    o.set_avoid_homozygous_losses(avoid)
+    o.set_infinite_sites(infinite)
+    return eng, o
+
+
+def _species(o, forest):
+    return np.array([o.species[(m, ep)] for m, ep in zip(forest.mutant, forest.epistate)], dtype=np.uint32)
+
+
+def _tables_equal(a, b):
+    assert len(a["locus"]) == len(b["locus"])
+    for k in ("locus", "edge", "aux", "cls", "sig", "allele", "kind", "nature"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+@pytest.mark.parametrize("avoid,infinite", [(True, True), (False, True), (True, False)])
+def test_cna_placement_bit_exact(gpu_lib, orc, avoid, infinite):
+    w, cands = _workload(seed=3, n_leaves=500)
+    eng, o = _pair(orc, w, cands, avoid, infinite)
+    f = w.forest
+    for seed in (1, 77):
+        pf = eng.place_mutations(f, 100, 10, seed=seed)
+        op = o.place(f, _species(o, f), 100, 0, 10, 0, seed=seed)
+        gcls, gn, gcn = pf.node_classes()
+        ocls, on, ocn = op.node_classes(f.num_of_nodes)
+        np.testing.assert_array_equal(gcls, ocls)
+        assert (gn, gcn) == (on, ocn)
+        assert gn > 3 and gcn >= 4
+        gc, oc = pf.cna_table(), op.cna_table()
+        for k in oc:
+            np.testing.assert_array_equal(gc[k], oc[k], err_msg=k)
+        assert (gc["driver"] == 0).sum() > 0          # some passenger CNAs were applied
+        _tables_equal(pf.table(), op.table())
+        t = pf.table()
+        assert t["allele"].max() > 1                  # mutations on copied instances
+
+
+SEQ = [
+    dict(coverage=25, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3, purity=0.7),
+    dict(coverage=20, read_size=100, insert_size_mean=0, error_rate=0.0, purity=1.0, with_normal_sample=False),
+]
+
+
+@pytest.mark.parametrize("case", range(len(SEQ)))
+def test_cna_sequencing_bit_exact(gpu_lib, orc, case):
+    from process_gb300.engine import seq_cfg, sequence_counts
+    w, cands = _workload(seed=4, n_leaves=300)
+    eng, o = _pair(orc, w, cands, True, True)
+    f = w.forest
+    pf = eng.place_mutations(f, 200, 20, seed=5)
+    op = o.place(f, _species(o, f), 200, 0, 20, 0, seed=5)
+    _tables_equal(pf.table(), op.table())
+    for tile in (2048, 16384):
+        res = sequence_counts(pf, 31, tile_size=tile, **SEQ[case])
+        alt, dep = res.counts()
+        c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=tile, **SEQ[case])
+        oalt, odep, oreads = op.sequence(c, 31, flavour=0)
+        np.testing.assert_array_equal(dep, odep)
+        np.testing.assert_array_equal(alt, oalt)
+        assert res.dims()[2] == oreads
+
+
+def test_wgd_order_vaf_gpu(gpu_lib, orc):
+    """The driver SNV before the doubling is on two of four alleles, after it on one."""
+    from process_gb300 import SNV, WGD, synth
+    from process_gb300.engine import sequence_counts
+    vafs = []
+    for drivers in ([SNV("1", 50_000, "T", allele=0), WGD], [WGD, SNV("1", 50_000, "T", allele=0)]):
+        w = synth.config1(seed=6, n_leaves=100)
+        w.genome.chr_lengths = [200_000] * 3
+        w.mutants = [(w.mutants[0][0], w.mutants[0][1], drivers), w.mutants[1]]
+        eng = synth.build_engine(w)
+        pf = eng.place_mutations(w.forest, 0, 0, seed=9)
+        t = pf.table()
+        d = np.nonzero(t["nature"] == 1)[0][0]
+        alt, dep = sequence_counts(pf, 4, coverage=400, read_size=150, insert_size_mean=350, insert_size_stddev=10,
+                                   error_rate=0.0, purity=1.0, with_normal_sample=False).counts()
+        vafs.append(alt[0, d] / dep[0, d])
+    assert abs(vafs[0] - 0.5) < 0.09 and abs(vafs[1] - 0.25) < 0.09
