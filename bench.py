@@ -32,7 +32,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "reads/s + mutations placed/s on 1 GB300 vs host CPU; batched calib grad-evals/s"
 WORKLOAD = ("config2 full scale: 3.1 Gbp/24 chr GC 41%, 3 samples x 1e4 leaves, 3 epochs "
-            "SNV {1.5e-8,3e-8,5e-8} indel 0.1x, 3 SBS + 2 ID signatures, 100x paired 150 bp, "
+            "SNV {1.5e-8,3e-8,5e-8} indel 0.1x, 3 SBS + 2 ID signatures, 20 driver CNAs (1-50 Mbp, "
+            "CN 0-4) + 1 WGD branch, 100x paired 150 bp, "
             "insert binomial(350, 10), purity 0.7, error 1e-3, + normal sample")
 # algorithmic bytes of one simulated read and of one read-locus visit (alt+depth
 # read-modify-write), the per-unit contract of the read kernel

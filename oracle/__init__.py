@@ -136,6 +136,19 @@ class OracleEngine:
         e.species = species
         for t, coeffs in w.exposures:
             e.add_exposure(t, coeffs)
+        idx = {str(n): i for i, n in enumerate(g.chr_names)}
+        off = np.concatenate([[0], np.cumsum(np.asarray(g.chr_lengths, dtype=np.int64))])
+        genome = None
+        for mut_id, (_, _, drivers) in enumerate(w.mutants):
+            resolved = []
+            for d in drivers:
+                if type(d).__name__ == "Mutation" and d.ref == "?":
+                    if genome is None:
+                        genome = e.read_genome()
+                    ref = "ACGT"[genome[off[idx[d.chr]] + d.chr_pos - 1]]
+                    d = type(d)(d.chr, d.chr_pos, ref, d.alt, d.allele)
+                resolved.append(d)
+            e.add_drivers(mut_id, resolved, idx.__getitem__)
         return e
 
     def set_signatures(self, ty, sigs: dict):

@@ -412,6 +412,34 @@ uint32_t max_copies(const CellGenome& g) {
   return uint32_t(best);
 }
 
+// Positions of a genome grouped into maximal runs covered by the same
+// (ascending) instance list, for O(log) lookups
+struct ClassIndex {
+  std::vector<uint32_t> b, e;
+  std::vector<std::vector<uint32_t>> insts;
+};
+ClassIndex class_index(const CellGenome& g) {
+  std::vector<uint32_t> cuts;
+  for (const auto& kv : g) for (auto [x, y] : kv.second) { cuts.push_back(x); cuts.push_back(y); }
+  std::sort(cuts.begin(), cuts.end());
+  cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+  ClassIndex ix;
+  for (size_t i = 0; i + 1 < cuts.size(); ++i) {
+    auto cov = covering(g, cuts[i]);
+    if (cov.empty()) continue;
+    if (!ix.b.empty() && ix.e.back() == cuts[i] && ix.insts.back() == cov) { ix.e.back() = cuts[i + 1]; continue; }
+    ix.b.push_back(cuts[i]); ix.e.push_back(cuts[i + 1]); ix.insts.push_back(std::move(cov));
+  }
+  return ix;
+}
+const std::vector<uint32_t>& covering(const ClassIndex& ix, uint32_t p) {
+  static const std::vector<uint32_t> none;
+  auto it = std::upper_bound(ix.b.begin(), ix.b.end(), p);
+  if (it == ix.b.begin()) return none;
+  const size_t i = size_t(it - ix.b.begin()) - 1;
+  return p < ix.e[i] ? ix.insts[i] : none;
+}
+
 // a copy made on edge `edge` by its event `event` (instance `made` from `from`)
 struct CopyRec { uint32_t edge, event, made, from; };
 
@@ -427,6 +455,7 @@ struct Placed {
   const Engine* eng = nullptr;
   Forest forest_copy;
   std::vector<CellGenome> classes{1};   // genotype classes, class 0 = germline
+  std::vector<ClassIndex> index;        // per class
   std::vector<uint32_t> node_class;     // per node (+ the preneoplastic edge: class 0)
   std::vector<CopyRec> copies;
   std::vector<CnaRec> cnas;
@@ -537,12 +566,6 @@ const std::vector<DriverEvent>* drivers_of(const Engine& e, const Forest& f, uin
   return it == e.drivers.end() ? nullptr : &it->second;
 }
 
-bool has_copy_number_events(const Engine& e) {
-  for (const auto& kv : e.drivers) for (const auto& d : kv.second) if (d.kind != 0) return true;
-  if (e.cands.empty()) return false;
-  for (const auto& kv : e.species) if (kv.second.cna > 0) return true;
-  return false;
-}
 
 // Applies every node's driver list (SNVs/indels, CNAs, WGD in declaration
 // order; src/mutation_engine.cpp:789-862, vignettes/mutations.Rmd:159-177)
@@ -551,8 +574,37 @@ bool has_copy_number_events(const Engine& e) {
 // never removes the last allele of a region, :1356) to the genome inherited
 // from the parent.  Fills the genotype classes, copies and CNA records of
 // `pl` and returns the driver SNVs/indels in node then event order.
-std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t seed, Placed& pl) {
-  const uint32_t N = f.n, k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
+// The random choices of the event replay.  PhiloxDraws uses the keyed
+// counters of the GPU path; MtDraws draws them in sequence from the
+// std::mt19937_64 engine of the reference-engine flavour.
+struct PhiloxDraws {
+  uint64_t seed;
+  uint32_t k0() const { return uint32_t(seed); }
+  uint32_t k1() const { return uint32_t(seed >> 32); }
+  uint64_t pcna_count(uint32_t v, double lambda) {
+    Stream st = stream(seed, 0, v, 0, TAG_EDGE_CNA);
+    return poisson(st, lambda);
+  }
+  uint32_t pcna_cand(uint32_t v, uint32_t k, uint32_t n) { return mulhi32(philox(k0(), k1(), k, v, 0, TAG_CNA).v[0], n); }
+  uint32_t pcna_ord(uint32_t v, uint32_t k, uint32_t n) { return mulhi32(philox(k0(), k1(), k, v, 0, TAG_CNA).v[1], n); }
+  uint32_t cna_ord(uint32_t v, uint32_t j, uint32_t n) { return mulhi32(philox(k0(), k1(), j, v, 1, TAG_CNA).v[1], n); }
+  uint32_t sid_ord(uint32_t idx, uint32_t v, uint32_t n) { return mulhi32(philox(k0(), k1(), idx, v, 0, TAG_DRIVER).v[0], n); }
+};
+struct MtDraws {
+  std::mt19937_64& rng;
+  uint64_t pcna_count(uint32_t, double lambda) {
+    return lambda > 0 ? std::poisson_distribution<uint64_t>(lambda)(rng) : 0;
+  }
+  uint32_t pick(uint32_t n) { return std::uniform_int_distribution<uint32_t>(0, n - 1)(rng); }
+  uint32_t pcna_cand(uint32_t, uint32_t, uint32_t n) { return pick(n); }
+  uint32_t pcna_ord(uint32_t, uint32_t, uint32_t n) { return pick(n); }
+  uint32_t cna_ord(uint32_t, uint32_t, uint32_t n) { return pick(n); }
+  uint32_t sid_ord(uint32_t, uint32_t, uint32_t n) { return pick(n); }
+};
+
+template <class Draws>
+std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, Draws& draws, Placed& pl) {
+  const uint32_t N = f.n;
   const uint32_t n_chr = uint32_t(e.g.off.size() - 1);
   CellGenome germ;
   for (uint32_t c = 0; c < n_chr; ++c)
@@ -569,8 +621,7 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
     for (uint32_t v = 0; v < N; ++v) {
       auto it = e.species.find(f.species[v]);
       const double rate = it == e.species.end() ? 0.0 : it->second.cna;
-      Stream st = stream(seed, 0, v, 0, TAG_EDGE_CNA);
-      n_pcna[v] = poisson(st, rate * germline * double(f.divisions[v]));
+      n_pcna[v] = draws.pcna_count(v, rate * germline * double(f.divisions[v]));
     }
   }
   std::vector<DriverRec> drv;
@@ -581,7 +632,8 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
     const auto* list = drivers_of(e, f, v);
     const uint32_t nd = list ? uint32_t(list->size()) : 0u;
     if (uint64_t(nd) + n_pcna[v] > 0x7ffd) throw std::runtime_error("too many driver and CNA events on one edge");
-    auto cna = [&](const Cna& c, uint32_t event, uint32_t word, bool passenger) {
+    // ord(n): ordinal among the n covering instances when the event names none
+    auto cna = [&](const Cna& c, uint32_t event, auto ord_of, bool passenger) {
       const uint32_t b = e.g.off[c.chr] + c.begin - 1;
       const uint32_t end = uint32_t(std::min<uint64_t>(uint64_t(b) + c.len, e.g.off[c.chr + 1]));
       if (b >= end) return;
@@ -589,7 +641,7 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
       if (cov.empty()) return;
       const uint32_t last = c.begin + (end - b) - 1;
       if (c.amp) {
-        const uint32_t ord = c.src >= 0 ? uint32_t(c.src) : mulhi32(word, uint32_t(cov.size()));
+        const uint32_t ord = c.src >= 0 ? uint32_t(c.src) : ord_of(uint32_t(cov.size()));
         if (ord >= cov.size()) throw std::runtime_error("CNA source allele does not cover the region");
         const uint32_t x = cov[ord], made = n_inst++;
         g[made] = ivl_within(g[x], b, end);
@@ -597,7 +649,7 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
         pl.cnas.push_back({v, 1, c.chr, c.begin, last, made, x, uint8_t(passenger ? 0 : 1)});
       } else {
         if (passenger && e.avoid_losses && cov.size() <= 1) return;
-        const uint32_t ord = c.allele >= 0 ? uint32_t(c.allele) : mulhi32(word, uint32_t(cov.size()));
+        const uint32_t ord = c.allele >= 0 ? uint32_t(c.allele) : ord_of(uint32_t(cov.size()));
         if (ord >= cov.size()) throw std::runtime_error("CNA allele does not cover the region");
         const uint32_t x = cov[ord];
         g[x] = ivl_minus(g[x], b, end);
@@ -617,14 +669,14 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
           ord = uint32_t(de.sid.allele);
           if (ord >= cov.size()) throw std::runtime_error("driver allele does not exist there");
         } else {
-          ord = mulhi32(philox(k0, k1, n_sid, v, 0, TAG_DRIVER).v[0], uint32_t(cov.size()));
+          ord = draws.sid_ord(n_sid, v, uint32_t(cov.size()));
         }
         r.allele = cov[ord];
         r.order = int32_t(j);
         drv.push_back(r);
         ++n_sid;
       } else if (de.kind == 1) {
-        cna(de.cna, j, philox(k0, k1, j, v, 1, TAG_CNA).v[1], false);
+        cna(de.cna, j, [&](uint32_t n) { return draws.cna_ord(v, j, n); }, false);
       } else {
         std::vector<uint32_t> present;
         for (const auto& kv : g) present.push_back(kv.first);
@@ -638,8 +690,9 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
       }
     }
     for (uint64_t k = 0; k < n_pcna[v]; ++k) {
-      const W4 r = philox(k0, k1, uint32_t(k), v, 0, TAG_CNA);
-      cna(e.cands[mulhi32(r.v[0], uint32_t(e.cands.size()))], nd + uint32_t(k), r.v[1], true);
+      const uint32_t kk = uint32_t(k);
+      cna(e.cands[draws.pcna_cand(v, kk, uint32_t(e.cands.size()))], nd + kk,
+          [&](uint32_t n) { return draws.pcna_ord(v, kk, n); }, true);
     }
     if (changed) { pl.classes.push_back(std::move(g)); pl.node_class[v] = uint32_t(pl.classes.size() - 1); }
     else pl.node_class[v] = base;
@@ -649,25 +702,11 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, uint64_t 
   pl.has_cna = pl.classes.size() > 1 || n_inst > 2;
   pl.cn_max = 2;
   for (const auto& g : pl.classes) pl.cn_max = std::max(pl.cn_max, max_copies(g));
+  pl.index.clear();
+  for (const auto& g : pl.classes) pl.index.push_back(class_index(g));
   return drv;
 }
 
-// driver SNVs/indels of a forest without copy-number events (random alleles
-// marked 0xff, for the std::mt19937_64 flavour)
-std::vector<DriverRec> driver_sites(const Engine& e, const Forest& f) {
-  std::vector<DriverRec> out;
-  for (uint32_t v = 0; v < f.n; ++v) {
-    const auto* list = drivers_of(e, f, v);
-    if (!list) continue;
-    for (uint32_t j = 0; j < list->size(); ++j) {
-      DriverRec r = driver_site(e, (*list)[j].sid, v);
-      r.allele = (*list)[j].sid.allele < 0 ? 0xffu : uint32_t((*list)[j].sid.allele);
-      r.order = int32_t(j);
-      out.push_back(r);
-    }
-  }
-  return out;
-}
 
 // number of divisions of edge v per epoch
 std::vector<uint32_t> divisions_per_epoch(const Forest& f, const Tables& t, uint32_t v) {
@@ -710,7 +749,8 @@ void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t
                   uint32_t pre_id, uint64_t seed, Placed& out) {
   const Tables t = make_tables(e, f, n_pre_snv, pre_sbs, n_pre_id, pre_id);
   const uint32_t N = f.n, E = t.E;
-  const auto drv = replay_events(e, f, seed, out);
+  PhiloxDraws draws{seed};
+  const auto drv = replay_events(e, f, draws, out);
   std::vector<double> class_size(out.classes.size());
   for (size_t c = 0; c < class_size.size(); ++c) class_size[c] = double(genome_size(out.classes[c]));
   std::vector<uint32_t> cnt_snv(uint64_t(N + 1) * E, 0), cnt_id(uint64_t(N + 1) * E, 0);
@@ -755,7 +795,7 @@ void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t
     const std::vector<uint32_t>& list = sl.indel ? e.id[cls[i]] : e.ctx[sbs_ctx(cls[i])];
     const uint32_t p = list[index64(r.v[0], r.v[1], list.size())];
     const uint32_t loc = sl.indel ? p - 1 : p;
-    const auto cov = covering(out.classes[out.node_class[sl.edge]], loc);
+    const auto& cov = covering(out.index[out.node_class[sl.edge]], loc);
     if (cov.empty()) { locus[i] = LOCUS_NONE; return; }
     allele[i] = uint16_t(cov[mulhi32(r.v[2], uint32_t(cov.size()))]);
     locus[i] = loc;
@@ -839,11 +879,11 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
   const Tables t = make_tables(e, f, n_pre_snv, pre_sbs, n_pre_id, pre_id);
   std::mt19937_64 rng(seed);
   const uint32_t N = f.n, E = t.E;
-  const double A = 2.0 * double(e.g.b.size());
   std::unordered_set<uint32_t> used;
-  if (has_copy_number_events(e))
-    throw std::runtime_error("the std::mt19937_64 flavour models no copy-number events");
-  const auto drv = driver_sites(e, f);
+  MtDraws draws{rng};
+  const auto drv = replay_events(e, f, draws, out);   // drivers carry their alleles
+  std::vector<double> class_size(out.classes.size());
+  for (size_t c = 0; c < class_size.size(); ++c) class_size[c] = double(genome_size(out.classes[c]));
   auto push = [&](uint32_t loc, uint32_t ed, uint32_t ax, int c, int s, int al, int k, int nat, int32_t o) {
     out.locus.push_back(loc); out.edge.push_back(ed); out.aux.push_back(ax); out.cls.push_back(uint8_t(c));
     out.sig.push_back(uint8_t(s)); out.allele.push_back(uint16_t(al)); out.kind.push_back(uint8_t(k));
@@ -851,8 +891,7 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
   };
   for (const auto& d : drv) {
     used.insert(d.locus);
-    const int al = d.allele == 0xffu ? int(std::uniform_int_distribution<int>(0, 1)(rng)) : int(d.allele);
-    push(d.locus, d.edge, d.aux, 0xff, 0xff, al, d.kind, 1, d.order);
+    push(d.locus, d.edge, d.aux, 0xff, 0xff, int(d.allele), d.kind, 1, d.order);
   }
   auto place_one = [&](uint32_t v, uint32_t row, int ty) {
     const uint32_t NC = ty == 0 ? 96 : 83;
@@ -862,16 +901,20 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
     uint32_t k = dc(rng);
     (void)NC;
     uint32_t p = 0, loc = 0;
-    for (int tries = 0; tries < 100000; ++tries) {
+    const ClassIndex& ix = out.index[out.node_class[v]];
+    const std::vector<uint32_t>* cov = nullptr;
+    for (int tries = 0;; ++tries) {
+      if (tries >= 100000) throw std::runtime_error("no free locus left for some mutations");
       if (tries >= 16) k = dc(rng);   // class redrawn after 16 collisions
       const std::vector<uint32_t>& list = ty == 1 ? e.id[k] : e.ctx[sbs_ctx(int(k))];
       std::uniform_int_distribution<uint64_t> dp(0, list.size() - 1);
       p = list[dp(rng)];
       loc = ty == 0 ? p : p - 1;
-      if (!e.infinite_sites || !used.count(loc)) break;
+      cov = &covering(ix, loc);        // no allele left there: draw again
+      if (!cov->empty() && (!e.infinite_sites || !used.count(loc))) break;
     }
     if (e.infinite_sites) used.insert(loc);
-    const int al = std::uniform_int_distribution<int>(0, 1)(rng);
+    const int al = int((*cov)[std::uniform_int_distribution<size_t>(0, cov->size() - 1)(rng)]);
     uint32_t ax;
     if (ty == 0) { const int ref = e.g.b[p]; const int ap = sbs_alt(int(k)); ax = uint32_t((ref == 1 || ref == 3) ? ap : 3 - ap); }
     else ax = indel_aux(e, k, p, uint32_t(rng()));
@@ -883,6 +926,7 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
     const auto nd = divisions_per_epoch(f, t, v);
     const uint32_t sp = f.species[v];
     for (uint32_t ep = 0; ep < E; ++ep) {
+      const double A = class_size[out.node_class[v]];
       const double ls = t.snv_rate[uint64_t(sp) * E + ep] * A * double(nd[ep]);
       const double li = t.id_rate[uint64_t(sp) * E + ep] * A * double(nd[ep]);
       const uint64_t ns = ls > 0 ? std::poisson_distribution<uint64_t>(ls)(rng) : 0;
@@ -898,7 +942,6 @@ void place_mt(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t pre
   auto perm = [&](auto& v) { auto c = v; for (size_t i = 0; i < n; ++i) v[i] = c[order[i]]; };
   perm(out.locus); perm(out.edge); perm(out.aux); perm(out.cls); perm(out.sig); perm(out.allele);
   perm(out.kind); perm(out.nature); perm(out.order);
-  out.node_class.assign(N + 1, 0);
 }
 
 // ------------------------------------------------------------ sequencing
@@ -1206,7 +1249,7 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
             cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[2], uint32_t(sd.leaves.size()))]);
             if (!pl.has_cna) { allele = mulhi32(r.v[3], 2); found = true; break; }
             const uint32_t u = mulhi32(r.v[3], tile_cn[k]);
-            const auto cov = covering(pl.classes[cell < 0 ? 0u : pl.node_class[cell]], p0);
+            const auto& cov = covering(pl.index[cell < 0 ? 0u : pl.node_class[cell]], p0);
             if (u < cov.size()) { allele = cov[u]; found = true; }
           }
           if (!found) continue;
@@ -1230,7 +1273,6 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
 // bounded sample for the timed CPU baseline); `threads` splits the samples
 // and chromosomes over host threads, each with its own engine.
 void seq_mt(const Placed& pl, const SeqCfg& c, uint64_t seed, double fraction, int threads, SeqOut& out) {
-  if (pl.has_cna) throw std::runtime_error("the std::mt19937_64 flavour models no copy-number events");
   const Engine& e = *pl.eng;
   const Forest& f = *pl.forest;
   const SeqSetup s = seq_setup(pl, c);
@@ -1239,6 +1281,7 @@ void seq_mt(const Placed& pl, const SeqCfg& c, uint64_t seed, double fraction, i
   out.alt.assign(out.n_samples * M, 0);
   out.depth.assign(out.n_samples * M, 0);
   Carrier car{f, c.preneoplastic_in_normal != 0};
+  const auto carriers = carrier_sets(pl);
   const double mates = s.paired ? 2.0 : 1.0;
   // insert distribution of the reference: std::binomial_distribution(t, p)
   uint32_t bin_t = 0;
@@ -1268,21 +1311,45 @@ void seq_mt(const Placed& pl, const SeqCfg& c, uint64_t seed, double fraction, i
       std::uniform_int_distribution<uint32_t> dstart(0, L - s.R);
       std::uniform_real_distribution<double> dunit(0.0, 1.0);
       std::uniform_int_distribution<uint32_t> dleaf(0, sd.leaves.empty() ? 0 : uint32_t(sd.leaves.size()) - 1);
-      std::uniform_int_distribution<uint32_t> dallele(0, 1), dbase(0, 2);
+      // copy slots: the largest copy number on the chromosome in any class
+      uint32_t cn_chr = 1;
+      if (pl.has_cna)
+        for (const auto& g : pl.classes) {
+          uint64_t unused = 0;
+          uint32_t m = 0;
+          copies_in(g, cs, ce, unused, m);
+          cn_chr = std::max(cn_chr, m);
+        }
+      std::uniform_int_distribution<uint32_t> dallele(0, 1), dbase(0, 2), dslot(0, cn_chr - 1);
       std::binomial_distribution<uint32_t> dbin(bin_t, bin_p);
       std::normal_distribution<double> dnorm(double(c.insert_size_mean), double(c.insert_size_stddev));
       std::bernoulli_distribution derr(c.error_rate);
       uint32_t* alt = alt_t[w].data() + uint64_t(jb.smp) * M;
       uint32_t* dep = dep_t[w].data() + uint64_t(jb.smp) * M;
       for (uint64_t j = 0; j < pairs; ++j) {
-        const uint32_t p0 = cs + dstart(rng);
-        const bool normal = sd.all_normal || dunit(rng) < 1.0 - c.purity;
-        const int64_t cell = normal ? -1 : int64_t(sd.leaves[dleaf(rng)]);
-        const uint32_t allele = dallele(rng);
+        // (start, cell, allele instance) uniform over the DNA of the mixture:
+        // with copy-number events by rejection over the whole chromosome
+        // (copy slot u < cn_chr kept when the cell has more than u instances
+        // at the start)
+        uint32_t p0 = 0, allele = 0;
+        int64_t cell = -1;
+        bool found = false;
+        for (uint32_t att = 0; att < (1u << 20) && !found; ++att) {
+          p0 = cs + dstart(rng);
+          const bool normal = sd.all_normal || dunit(rng) < 1.0 - c.purity;
+          cell = normal ? -1 : int64_t(sd.leaves[dleaf(rng)]);
+          if (!pl.has_cna) { allele = dallele(rng); found = true; break; }
+          const uint32_t u = dslot(rng);
+          const auto& cov = covering(pl.index[cell < 0 ? 0u : pl.node_class[cell]], p0);
+          if (u < cov.size()) { allele = cov[u]; found = true; }
+        }
+        if (!found) continue;
         auto mate = [&](uint32_t a) {
           auto it = std::lower_bound(pl.locus.begin(), pl.locus.end(), a);
           for (size_t i = size_t(it - pl.locus.begin()); i < M && pl.locus[i] < a + s.R; ++i) {
-            const bool carried = car.ancestor_or_self(pl.edge[i], cell) && pl.allele[i] == allele;
+            const auto& cs_i = carriers[i];
+            const bool carried = car.ancestor_or_self(pl.edge[i], cell) &&
+                                 std::find(cs_i.begin(), cs_i.end(), allele) != cs_i.end();
             bool obs;
             if (pl.kind[i] == 1) obs = carried;
             else {

@@ -133,6 +133,44 @@ def config1(seed: int = 1, n_leaves: int = 2500) -> Workload:
                              insert_model="normal", error_rate=1e-3, purity=1.0))
 
 
+def config2_cnas(rng: np.random.Generator, genome: GenomeSpec, scale: float) -> tuple[list, list]:
+    """20 driver CNAs of 1-50 Mbp (times the genome scale) and one WGD branch.
+
+    The founder clone A carries 10: four single-allele deletions (copy
+    number 1), two regions deleted on both alleles (0), three amplifications
+    (3) and one region amplified twice (4).  The subclone B starts with a
+    whole-genome doubling followed by five deletions and five
+    amplifications of random alleles."""
+    from .engine import CNA, WGD
+    names = list(genome.chr_names)
+    lengths = np.asarray(genome.chr_lengths, dtype=np.int64)
+    p_chr = lengths / lengths.sum()
+
+    def region():
+        c = int(rng.choice(len(names), p=p_chr))
+        ln = int(max(1000, rng.uniform(1e6, 50e6) * scale))
+        ln = int(min(ln, max(1, lengths[c] // 2)))
+        begin = int(rng.integers(1, max(2, lengths[c] - ln + 1)))
+        return names[c], begin, ln
+
+    a = []
+    for kind in ("D1", "D1", "D1", "D1", "D0", "D0", "A3", "A3", "A3", "A4"):
+        ch, b, ln = region()
+        if kind == "D1":
+            a.append(CNA("D", ch, b, ln, allele=0))
+        elif kind == "D0":
+            a += [CNA("D", ch, b, ln, allele=0), CNA("D", ch, b, ln, allele=0)]
+        elif kind == "A3":
+            a.append(CNA("A", ch, b, ln))
+        else:
+            a += [CNA("A", ch, b, ln, src_allele=0), CNA("A", ch, b, ln, src_allele=0)]
+    bl = [WGD]
+    for kind in ("D",) * 5 + ("A",) * 5:
+        ch, b2, ln = region()
+        bl.append(CNA(kind, ch, b2, ln))
+    return a, bl
+
+
 def config2(seed: int = 2, n_leaves_per_sample: int = 10_000, genome_scale: float = 1.0) -> Workload:
     rng = np.random.default_rng(seed)
     total = int(3.1e9 * genome_scale)
@@ -152,8 +190,10 @@ def config2(seed: int = 2, n_leaves_per_sample: int = 10_000, genome_scale: floa
                               **{f"ID{i + 1}": float(e_i[i]) for i in range(2)}}))
     snv = [1.5e-8, 3e-8, 5e-8]
     rates = {"SNV": snv, "indel": [0.1 * x for x in snv]}
-    return Workload("config2: 3.1 Gbp/24 chr, 3x1e4 leaves, 3 epochs, 100x paired 150 bp, purity 0.7",
-                    genome, sbs, ids, exposures, [("A", rates, []), ("B", rates, [])], forest,
+    cna_a, cna_b = config2_cnas(rng, genome, genome_scale)
+    return Workload("config2: 3.1 Gbp/24 chr, 3x1e4 leaves, 3 epochs, 20 CNAs + 1 WGD branch, "
+                    "100x paired 150 bp, purity 0.7",
+                    genome, sbs, ids, exposures, [("A", rates, cna_a), ("B", rates, cna_b)], forest,
                     n_pre_snv=1000, n_pre_indel=100,
                     seq=dict(coverage=100, read_size=150, insert_size_mean=350, insert_size_stddev=10,
                              insert_model="binomial", error_rate=1e-3, purity=0.7))

@@ -30,20 +30,8 @@ def _pair(orc, w, cands, avoid, infinite):
     eng.add_passenger_CNAs(cands)
     eng.avoid_homozygous_losses = avoid
     eng.infinite_sites_model = infinite
-    o = orc.OracleEngine.like(w)
-    g = o.read_genome()
-    off = np.concatenate([[0], np.cumsum(np.asarray(w.genome.chr_lengths, dtype=np.int64))])
+    o = orc.OracleEngine.like(w)    # drivers included
     idx = {n: i for i, n in enumerate(w.genome.chr_names)}
-
-    def explicit(drivers):
-        out = []
-        for d in drivers:
-            if type(d).__name__ == "Mutation" and d.ref == "?":
-                d = type(d)(d.chr, d.chr_pos, "ACGT"[g[off[idx[d.chr]] + d.chr_pos - 1]], d.alt, d.allele)
-            out.append(d)
-        return out
-    for m, (_, _, drivers) in enumerate(w.mutants):
-        o.add_drivers(m, explicit(drivers), idx.__getitem__)
     for c in cands:
         o.add_passenger_cna(idx[c.chr], c.chr_pos, c.len, c.type == "A")
     o.set_avoid_homozygous_losses(avoid)

@@ -83,13 +83,7 @@ def test_placement_bit_exact_epochs_drivers(gpu_lib, orc):
     w.mutants = [("A", w.mutants[0][1], []),
                  ("B", w.mutants[1][1], [SNV("1", 1000, "T", allele=1), Mutation("2", 500, "A", "ACG"),
                                          SNV("3", 77, "G")])]
-    eng, o = make_pair(orc, w)
-    # the oracle gets the same drivers with the reference base read from the genome
-    g = o.read_genome()
-    off = np.concatenate([[0], np.cumsum(np.asarray(w.genome.chr_lengths, dtype=np.int64))])
-    o.add_driver_sid(1, 0, 1000, "ACGT"[g[off[0] + 999]], "T", 1)
-    o.add_driver_sid(1, 1, 500, "A", "ACG", -1)
-    o.add_driver_sid(1, 2, 77, "ACGT"[g[off[2] + 76]], "G", -1)
+    eng, o = make_pair(orc, w)   # the oracle reads the "?" reference bases from its genome
     for seed in (5, 6):
         pf = eng.place_mutations(w.forest, 1000, 100, seed=seed)
         ot = o.place(w.forest, oracle_species(o, w.forest), 1000, 0, 100, 0, seed=seed).table()
@@ -210,6 +204,7 @@ def test_full_size_properties(gpu_lib):
     from process_gb300 import synth
     from process_gb300.engine import sequence_counts
     w = synth.config2(seed=2)
+    w.mutants = [(n, r, []) for n, r, _ in w.mutants]     # copy number 2 everywhere
     eng = synth.build_engine(w)
     pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=7)
     t = pf.table()
@@ -225,3 +220,33 @@ def test_full_size_properties(gpu_lib):
     pas = (t["nature"] == 0) & (t["kind"] == 0)
     rate = alt[3, pas].sum() / dep[3, pas].sum()
     assert rate < 1e-3
+
+
+def test_full_size_copy_number_properties(gpu_lib):
+    """The full config-2 workload with its 20 CNAs and WGD branch: three
+    genotype classes, one WGD record, passengers per edge scaled by the
+    allelic size of the edge's genome (about 2x on the WGD branch), sorted
+    unique loci and depth near the coverage."""
+    from process_gb300 import synth
+    from process_gb300.engine import sequence_counts
+    w = synth.config2(seed=2)
+    eng = synth.build_engine(w)
+    pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=7)
+    t = pf.table()
+    assert np.all(np.diff(t["locus"].astype(np.int64)) > 0)
+    _, n_cls, cn_max = pf.node_classes()
+    assert n_cls == 3 and cn_max >= 4
+    c = pf.cna_table()
+    assert (c["type"] == 2).sum() == 1 and len(c["type"]) <= 24
+    w0 = synth.config2(seed=2)
+    w0.mutants = [(n, r, []) for n, r, _ in w0.mutants]
+    t0 = synth.build_engine(w0).place_mutations(w0.forest, w0.n_pre_snv, w0.n_pre_indel, seed=7).table()
+    n = w.forest.num_of_nodes
+    per = np.bincount(t["edge"][t["nature"] == 0], minlength=n)[:n].astype(float)
+    per0 = np.bincount(t0["edge"][t0["nature"] == 0], minlength=n)[:n].astype(float)
+    b = np.asarray(w.forest.mutant) == "B"
+    assert 1.7 < per[b].sum() / per0[b].sum() < 2.3
+    assert 0.85 < per[~b].sum() / per0[~b].sum() < 1.15
+    res = sequence_counts(pf, 9, **w.seq)
+    alt, dep = res.counts()
+    assert 80 < dep[:3].mean() < 130
