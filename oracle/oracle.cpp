@@ -440,6 +440,9 @@ const std::vector<uint32_t>& covering(const ClassIndex& ix, uint32_t p) {
   return p < ix.e[i] ? ix.insts[i] : none;
 }
 
+struct Placed;
+void build_atoms(Placed& pl, uint32_t G);
+
 // a copy made on edge `edge` by its event `event` (instance `made` from `from`)
 struct CopyRec { uint32_t edge, event, made, from; };
 
@@ -456,12 +459,32 @@ struct Placed {
   Forest forest_copy;
   std::vector<CellGenome> classes{1};   // genotype classes, class 0 = germline
   std::vector<ClassIndex> index;        // per class
+  // atoms: the coarsest partition of the genome into intervals on which
+  // every class's covering instances are constant, with those instances
+  std::vector<uint32_t> atom_start;
+  std::vector<std::vector<std::vector<uint32_t>>> atom_cov;   // [atom][class]
   std::vector<uint32_t> node_class;     // per node (+ the preneoplastic edge: class 0)
   std::vector<CopyRec> copies;
   std::vector<CnaRec> cnas;
   uint32_t n_inst = 2, cn_max = 2;
   bool has_cna = false;
 };
+
+void build_atoms(Placed& pl, uint32_t G) {
+  std::vector<uint32_t> cuts{0u, G};
+  for (const auto& g : pl.classes)
+    for (const auto& kv : g) for (auto [x, y] : kv.second) { cuts.push_back(x); cuts.push_back(y); }
+  std::sort(cuts.begin(), cuts.end());
+  cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+  pl.atom_start.clear(); pl.atom_cov.clear();
+  for (size_t i = 0; i + 1 < cuts.size(); ++i) {
+    std::vector<std::vector<uint32_t>> tuple;
+    for (const auto& ix : pl.index) tuple.push_back(covering(ix, cuts[i]));
+    if (!pl.atom_cov.empty() && pl.atom_cov.back() == tuple) continue;
+    pl.atom_start.push_back(cuts[i]);
+    pl.atom_cov.push_back(std::move(tuple));
+  }
+}
 
 struct Tables {
   std::vector<double> times;
@@ -704,6 +727,7 @@ std::vector<DriverRec> replay_events(const Engine& e, const Forest& f, Draws& dr
   for (const auto& g : pl.classes) pl.cn_max = std::max(pl.cn_max, max_copies(g));
   pl.index.clear();
   for (const auto& g : pl.classes) pl.index.push_back(class_index(g));
+  build_atoms(pl, uint32_t(e.g.b.size()));
   return drv;
 }
 
@@ -1150,6 +1174,53 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
   const auto carriers = carrier_sets(pl);
   const double mates = s.paired ? 2.0 : 1.0;
   const uint32_t k0 = uint32_t(seed), k1 = uint32_t(seed >> 32);
+  // With copy-number events, (start, cell, instance) follows the DNA of the
+  // sample's cells: a cell is normal with probability wn (normal_thr / 2^32,
+  // 1 for the normal sample), else one of the nl leaves.  Options: the
+  // normal cells (class 0), then the leaf classes ascending, each with its
+  // leaves in node order.  Over atom a an option weighs wn * copies(a, 0) or
+  // (1 - wn) / nl * (n_c * copies(a, c)); a stretch of starts weighs
+  // wn * I0 + (1 - wn) / nl * S with the integer copy sums I0 and S.
+  struct Opt { uint32_t cls; std::vector<uint32_t> leaves; };
+  struct SampleCn {
+    double wn, wt;
+    uint64_t nl;
+    std::vector<Opt> opts;
+    std::vector<std::vector<uint32_t>> opt_thr;    // per atom
+    std::vector<uint64_t> icnt0, S;                 // per atom
+    double mass(uint64_t i0, uint64_t sum) const {
+      double m = wn * double(i0);
+      if (nl > 0) m = m + (wt / double(nl)) * double(sum);
+      return m;
+    }
+  };
+  std::vector<SampleCn> scn(s.samples.size());
+  if (pl.has_cna) {
+    const size_t NA = pl.atom_start.size();
+    for (size_t smp = 0; smp < s.samples.size(); ++smp) {
+      const SampleDesc& sd = s.samples[smp];
+      SampleCn& q = scn[smp];
+      q.wn = sd.all_normal ? 1.0 : double(sd.normal_thr) * (1.0 / 4294967296.0);
+      q.wt = 1.0 - q.wn;
+      q.opts.push_back({0u, {}});
+      std::map<uint32_t, std::vector<uint32_t>> by_class;
+      if (q.wt > 0) for (uint32_t leaf : sd.leaves) by_class[pl.node_class[leaf]].push_back(leaf);
+      q.nl = 0;
+      for (auto& kv : by_class) { q.nl += kv.second.size(); q.opts.push_back({kv.first, kv.second}); }
+      q.icnt0.assign(NA, 0); q.S.assign(NA, 0);
+      for (size_t a = 0; a < NA; ++a) {
+        const auto& cov = pl.atom_cov[a];
+        std::vector<double> w{q.wn * double(cov[0].size())};
+        for (size_t o = 1; o < q.opts.size(); ++o) {
+          const uint64_t n = q.opts[o].leaves.size(), x = n * cov[q.opts[o].cls].size();
+          w.push_back((q.wt / double(q.nl)) * double(x));
+          q.S[a] += x;
+        }
+        q.icnt0[a] = cov[0].size();
+        q.opt_thr.push_back(thresholds(w));
+      }
+    }
+  }
   uint32_t tile_base = 0;   // global tile index of the chromosome's first tile
   for (uint32_t ci : s.chrs) {
     const uint32_t L = e.g.off[ci + 1] - e.g.off[ci];
@@ -1159,37 +1230,33 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
     const uint32_t ce = e.g.off[ci + 1];
     for (uint32_t smp = 0; smp < out.n_samples; ++smp) {
       const SampleDesc& sd = s.samples[smp];
-      // with copy-number events: the DNA mass of each tile in this sample
-      // (cells drawn as normal with probability wn, else a uniform leaf;
-      // mass = wn * copies of the germline + (1 - wn) / leaves * the leaves'
-      // copies, copies summed over the tile's start positions) and the copy
-      // slots of the tile's rejection draw (largest copy number there)
+      // with copy-number events: the parts of each tile (one per atom it
+      // meets), the part thresholds and the tile masses of this sample
+      struct Part { uint32_t start, len, atom; };
+      std::vector<std::vector<Part>> parts(nt);
+      std::vector<std::vector<uint32_t>> part_thr(nt);
       std::vector<double> cum(nt, 0.0);
-      std::vector<uint32_t> tile_cn(nt, 1);
       double tot = 0.0;
       if (pl.has_cna) {
-        const double wn = sd.all_normal ? 1.0 : double(sd.normal_thr) * (1.0 / 4294967296.0);
-        const double wt = 1.0 - wn;
-        const bool tumour = wt > 0 && !sd.leaves.empty();
+        const SampleCn& q = scn[smp];
+        const auto& as = pl.atom_start;
         for (uint32_t k = 0; k < nt; ++k) {
           const uint32_t a = e.g.off[ci] + k * T, b = a + std::min<uint32_t>(T, S - k * T);
+          size_t x = size_t(std::upper_bound(as.begin(), as.end(), a) - as.begin()) - 1;
           uint64_t i0 = 0, sum = 0;
-          uint32_t m0 = 0, mx = 0;
-          copies_in(pl.classes[0], a, b, i0, m0);
-          if (wn > 0) mx = m0;
-          if (tumour)
-            for (uint32_t leaf : sd.leaves) {
-              uint64_t x = 0;
-              uint32_t m = 0;
-              copies_in(pl.classes[pl.node_class[leaf]], a, b, x, m);
-              sum += x;
-              mx = std::max(mx, m);
-            }
+          std::vector<double> pw;
+          for (; x < as.size() && as[x] < b; ++x) {
+            const uint32_t lo = std::max(a, as[x]);
+            const uint32_t hi = std::min<uint32_t>(b, x + 1 < as.size() ? as[x + 1] : uint32_t(e.g.b.size()));
+            parts[k].push_back({lo, hi - lo, uint32_t(x)});
+            const uint64_t len = hi - lo;
+            i0 += len * q.icnt0[x];
+            sum += len * q.S[x];
+            pw.push_back(q.mass(len * q.icnt0[x], len * q.S[x]));
+          }
+          if (pw.size() > 1) part_thr[k] = thresholds(pw);
           cum[k] = tot;
-          double m = wn * double(i0);
-          if (tumour) m = m + (wt / double(sd.leaves.size())) * double(sum);
-          tot = tot + m;
-          tile_cn[k] = std::max<uint32_t>(1, mx);
+          tot = tot + q.mass(i0, sum);
         }
       }
       // multinomial split by a binary tree over the padded tile range
@@ -1235,25 +1302,31 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
         const uint32_t start = e.g.off[ci] + k * T, len = std::min<uint32_t>(T, S - k * T);
         for (uint32_t j = 0; j < tile_pairs[k]; ++j) {
           out.n_reads += s.paired ? 2 : 1;
-          // start, cell and allele instance; with copy-number events drawn
-          // by rejection (copy slot u < cn_max kept when the cell has more
-          // than u instances at the start), attempt a on Philox tag
-          // TAG_PAIR | a << 8, the fragment dropped after 256 attempts
-          uint32_t p0 = 0, allele = 0;
-          int64_t cell = -1;
-          bool found = false;
-          for (uint32_t att = 0; att < (pl.has_cna ? 256u : 1u) && !found; ++att) {
-            const W4 r = philox(k0, k1, j, t, smp, TAG_PAIR | (att << 8));
+          // start, cell and allele instance
+          const W4 r = philox(k0, k1, j, t, smp, TAG_PAIR);
+          const W4 r2 = philox(k0, k1, j, t, smp, TAG_PAIR2);
+          uint32_t p0, allele;
+          int64_t cell;
+          if (!pl.has_cna) {
             p0 = start + mulhi32(r.v[0], len);
             const bool normal = sd.all_normal || r.v[1] < sd.normal_thr;
             cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[2], uint32_t(sd.leaves.size()))]);
-            if (!pl.has_cna) { allele = mulhi32(r.v[3], 2); found = true; break; }
-            const uint32_t u = mulhi32(r.v[3], tile_cn[k]);
-            const auto& cov = covering(pl.index[cell < 0 ? 0u : pl.node_class[cell]], p0);
-            if (u < cov.size()) { allele = cov[u]; found = true; }
+            allele = mulhi32(r.v[3], 2);
+          } else {
+            // part (word z of TAG_PAIR2 when the tile meets several atoms),
+            // start in the part, option, leaf of the option, instance
+            const SampleCn& q = scn[smp];
+            const auto& pk = parts[k];
+            const size_t pi = pk.size() > 1 ? lookup(part_thr[k].data(), uint32_t(pk.size()), r2.v[2]) : 0;
+            const Part& pt = pk[pi];
+            p0 = pt.start + mulhi32(r.v[0], pt.len);
+            const uint32_t o = lookup(q.opt_thr[pt.atom].data(), uint32_t(q.opts.size()), r.v[1]);
+            const Opt& op = q.opts[o];
+            cell = op.leaves.empty() ? -1 : int64_t(op.leaves[mulhi32(r.v[2], uint32_t(op.leaves.size()))]);
+            const auto& cov = pl.atom_cov[pt.atom][op.cls];
+            if (cov.empty()) continue;     // an option without DNA here is never drawn
+            allele = cov[mulhi32(r.v[3], uint32_t(cov.size()))];
           }
-          if (!found) continue;
-          const W4 r2 = philox(k0, k1, j, t, smp, TAG_PAIR2);
           count_mate(pl, car, carriers, p0, s.R, cell, allele, s.err_thr, 0, r2.v[1], alt, dep);
           if (s.paired) {
             const uint32_t ins = s.ins_min + lookup(s.ins_thr.data(), uint32_t(s.ins_thr.size()), r2.v[0]);

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <thread>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -266,7 +267,11 @@ struct pg_placed {
   uint32_t cn_max = 2, n_classes = 1;
   std::vector<uint32_t> node_class_h;
   std::vector<std::vector<uint32_t>> leaf_cls;   // per sample, parallel to leaves
-  std::vector<uint32_t> seg_off_h, seg_start_h, seg_end_h, seg_icnt_h;   // class segments (host copy)
+  // atoms: the coarsest partition of [0, G) on which every class's covering
+  // instances are constant; per (atom, class) the covering instances as
+  // (offset into inst_list, count)
+  std::vector<uint32_t> atom_start_h, atom_icnt_h;
+  DBuf<uint32_t> atom_start, atom_ioff, atom_icnt;
   DBuf<uint32_t> node_class, seg_off, seg_start, seg_end, seg_ioff, seg_icnt, chain_off;
   DBuf<uint16_t> inst_list, chain_anc;
   DBuf<uint64_t> chain_key;
@@ -994,7 +999,37 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     pl->n_classes = uint32_t(classes.size());
     pl->node_class_h = node_class;
     pl->node_class = upload(P, node_class, st);
-    pl->seg_off_h = seg_off; pl->seg_start_h = seg_start; pl->seg_end_h = seg_end; pl->seg_icnt_h = seg_icnt;
+    {
+      // atoms: cut at every segment boundary of every class, then merge
+      // neighbours on which every class sits in the same segment
+      const uint32_t C = uint32_t(classes.size());
+      std::vector<uint32_t> cuts{0u, uint32_t(e->G)};
+      cuts.insert(cuts.end(), seg_start.begin(), seg_start.end());
+      cuts.insert(cuts.end(), seg_end.begin(), seg_end.end());
+      std::sort(cuts.begin(), cuts.end());
+      cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+      std::vector<uint32_t> cur(C), prev, ptr(seg_off.begin(), seg_off.end() - 1);
+      std::vector<uint32_t> atom_ioff;
+      for (size_t i = 0; i + 1 < cuts.size(); ++i) {
+        const uint32_t b = cuts[i];
+        for (uint32_t c = 0; c < C; ++c) {
+          uint32_t& q = ptr[c];
+          while (q < seg_off[c + 1] && seg_end[q] <= b) ++q;
+          cur[c] = (q < seg_off[c + 1] && seg_start[q] <= b) ? q : 0xffffffffu;
+        }
+        if (!prev.empty() && cur == prev) continue;
+        prev = cur;
+        pl->atom_start_h.push_back(b);
+        for (uint32_t c = 0; c < C; ++c) {
+          const bool in = cur[c] != 0xffffffffu;
+          atom_ioff.push_back(in ? seg_ioff[cur[c]] : 0u);
+          pl->atom_icnt_h.push_back(in ? seg_icnt[cur[c]] : 0u);
+        }
+      }
+      pl->atom_start = upload(P, pl->atom_start_h, st);
+      pl->atom_ioff = upload(P, atom_ioff, st);
+      pl->atom_icnt = upload(P, pl->atom_icnt_h, st);
+    }
     pl->seg_off = upload(P, seg_off, st); pl->seg_start = upload(P, seg_start, st); pl->seg_end = upload(P, seg_end, st);
     pl->seg_ioff = upload(P, seg_ioff, st); pl->seg_icnt = upload(P, seg_icnt, st);
     if (inst_list.empty()) inst_list.push_back(0);
@@ -1268,8 +1303,10 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     }
     require(T >= 64 && T <= (1u << 24), "tile_size must be in [64, 2^24]");
     // ---- tiles
-    std::vector<uint32_t> t_start, t_len, t_end, c_ntiles, c_nstarts, c_id, c_first, c_depth, b_slot, b_index;
+    // tiles are laid out on the device from the per-chromosome table
+    std::vector<uint32_t> c_ntiles, c_nstarts, c_id, c_first, c_depth, c_start, c_end, b_slot, b_index;
     std::vector<uint64_t> c_pairs;
+    uint32_t n_tiles = 0;
     const double mates = paired ? 2.0 : 1.0;
     uint64_t frags_per_sample = 0;
     for (uint32_t ci : chrs) {
@@ -1283,17 +1320,14 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
       uint32_t D = 0;
       while ((uint64_t(1) << D) < nt) ++D;
       c_id.push_back(ci); c_ntiles.push_back(nt); c_nstarts.push_back(S); c_pairs.push_back(pairs);
-      c_first.push_back(uint32_t(t_start.size())); c_depth.push_back(D);
+      c_first.push_back(n_tiles); c_depth.push_back(D);
+      c_start.push_back(e->chr_off[ci]); c_end.push_back(e->chr_off[ci] + L);
       frags_per_sample += pairs;
       const uint32_t blk = 1u << std::min<uint32_t>(D, 6);
       for (uint32_t b = 0; b * blk < nt; ++b) { b_slot.push_back(slot); b_index.push_back(b); }
-      for (uint32_t k = 0; k < nt; ++k) {
-        t_start.push_back(e->chr_off[ci] + k * T);
-        t_len.push_back(std::min<uint32_t>(T, S - k * T));
-        t_end.push_back(e->chr_off[ci] + L);
-      }
+      require(uint64_t(n_tiles) + nt < (uint64_t(1) << 31), "too many tiles");
+      n_tiles += nt;
     }
-    const uint32_t n_tiles = uint32_t(t_start.size());
     // ---- samples and Euler numbering of normal cells / preneoplastic edge
     const uint32_t N = pl->n_nodes;
     std::vector<pg::SeqSample> samples;
@@ -1320,70 +1354,66 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
       samples.push_back(ss);
       sample_src.push_back(-1);
     }
-    // ---- with copy-number events: DNA mass of every (sample, tile) and the
-    // copy slots of its rejection draw.  A cell is normal with probability
-    // wn = normal_thr / 2^32 (1 for the normal sample), else one of the
-    // sample's n leaves; mass(tile) = wn * I_0 + (1 - wn) / n * sum over the
-    // leaves' classes c of n_c * I_c, I_c being the copies of class c summed
-    // over the tile's start positions (integers, exact), accumulated in tile
-    // order per chromosome.
-    std::vector<double> mass_cum, mass_tot;
-    std::vector<uint32_t> tile_cn;
+    // ---- with copy-number events: the draws of (start, cell, instance)
+    // follow the DNA of the sample's cells.  A cell is normal with
+    // probability wn = normal_thr / 2^32 (1 for the normal sample), else one
+    // of the sample's nl leaves; leaf class c holds n_c of them.  Over an
+    // atom a, option o (the normal cells: class 0; leaf class c) weighs
+    // wn * icnt(a, 0) or (1 - wn) / nl * (n_c * icnt(a, c)).  A stretch of
+    // starts weighs wn * I0 + (1 - wn) / nl * S, where I0 sums icnt(a, 0) and
+    // S sums n_c * icnt(a, c) over its positions (integers, exact); a tile's
+    // mass is that expression over the whole tile, accumulated in tile order
+    // per chromosome for the split (on the device, seq_tile_mass).
+    std::vector<uint32_t> opt_class, opt_leaf_off, opt_nleaf, cls_leaf_tin, opt_cdf;
+    std::vector<double> s_wn, s_wt;
+    std::vector<uint64_t> s_nl, s_icnt0, s_copy;
     if (pl->has_cna) {
-      const size_t NS = samples.size(), NT = n_tiles, NSL = c_id.size();
-      mass_cum.assign(NS * NT, 0.0); mass_tot.assign(NS * NSL, 0.0); tile_cn.assign(NS * NT, 1u);
-      auto class_tiles = [&](uint32_t cls, std::vector<uint64_t>& sum, std::vector<uint32_t>& mx) {
-        sum.assign(NT, 0); mx.assign(NT, 0);
-        uint32_t j = pl->seg_off_h[cls];
-        const uint32_t je = pl->seg_off_h[cls + 1];
-        for (size_t t = 0; t < NT; ++t) {
-          const uint32_t a = t_start[t], b = t_start[t] + t_len[t];
-          while (j < je && pl->seg_end_h[j] <= a) ++j;
-          for (uint32_t q = j; q < je && pl->seg_start_h[q] < b; ++q) {
-            const uint32_t x = std::max(a, pl->seg_start_h[q]), y = std::min(b, pl->seg_end_h[q]);
-            if (x < y) { sum[t] += uint64_t(y - x) * pl->seg_icnt_h[q]; mx[t] = std::max(mx[t], pl->seg_icnt_h[q]); }
-          }
-        }
-      };
-      std::vector<uint64_t> s0, sc;
-      std::vector<uint32_t> m0, mc;
-      class_tiles(0, s0, m0);
+      const size_t NS = samples.size();
+      const uint32_t C = pl->n_classes, NA = uint32_t(pl->atom_start_h.size());
+      s_icnt0.assign(NS * NA, 0); s_copy.assign(NS * NA, 0);
       for (size_t s = 0; s < NS; ++s) {
-        const double wn = samples[s].all_normal ? 1.0 : double(samples[s].normal_thr) * (1.0 / 4294967296.0);
+        pg::SeqSample& sm = samples[s];
+        const double wn = sm.all_normal ? 1.0 : double(sm.normal_thr) * (1.0 / 4294967296.0);
         const double wt = 1.0 - wn;
-        std::vector<uint64_t> S(NT, 0);
-        std::vector<uint32_t> mx(NT, 0);
-        if (wn > 0) mx = m0;
+        // options: the normal cells, then the leaf classes (leaves grouped by class)
+        std::map<uint32_t, std::vector<uint32_t>> by_class;
+        if (sample_src[s] >= 0 && wt > 0) {
+          const auto& lv = pl->leaves[sample_src[s]];
+          const auto& lc = pl->leaf_cls[sample_src[s]];
+          for (size_t i = 0; i < lv.size(); ++i) by_class[lc[i]].push_back(lv[i]);
+        }
+        sm.opt_off = uint32_t(opt_class.size());
+        sm.n_opt = uint32_t(1 + by_class.size());
+        sm.opt_cdf_off = uint32_t(opt_cdf.size());
+        opt_class.push_back(0); opt_leaf_off.push_back(0); opt_nleaf.push_back(0);
         uint64_t nl = 0;
-        if (wt > 0 && sample_src[s] >= 0) {
-          std::map<uint32_t, uint64_t> per_class;
-          for (uint32_t k : pl->leaf_cls[sample_src[s]]) per_class[k] += 1;
-          for (const auto& kv : per_class) {
-            class_tiles(kv.first, sc, mc);
-            for (size_t t = 0; t < NT; ++t) { S[t] += kv.second * sc[t]; mx[t] = std::max(mx[t], mc[t]); }
-            nl += kv.second;
-          }
+        std::vector<std::pair<uint32_t, uint64_t>> ncls;
+        for (const auto& kv : by_class) {
+          opt_class.push_back(kv.first); opt_leaf_off.push_back(uint32_t(cls_leaf_tin.size()));
+          opt_nleaf.push_back(uint32_t(kv.second.size()));
+          cls_leaf_tin.insert(cls_leaf_tin.end(), kv.second.begin(), kv.second.end());
+          ncls.push_back({kv.first, kv.second.size()});
+          nl += kv.second.size();
         }
-        for (size_t slot = 0; slot < NSL; ++slot) {
-          double acc = 0.0;
-          for (uint32_t k = 0; k < c_ntiles[slot]; ++k) {
-            const size_t t = c_first[slot] + k;
-            mass_cum[s * NT + t] = acc;
-            double m = wn * double(s0[t]);
-            if (nl > 0) m = m + (wt / double(nl)) * double(S[t]);
-            acc = acc + m;
-            tile_cn[s * NT + t] = std::max<uint32_t>(1u, mx[t]);
+        // per atom: option thresholds and the integer copy sums
+        for (uint32_t a = 0; a < NA; ++a) {
+          const uint32_t* ic = &pl->atom_icnt_h[uint64_t(a) * C];
+          std::vector<double> w{wn * double(ic[0])};
+          uint64_t S = 0;
+          for (const auto& [cls, n] : ncls) {
+            w.push_back((wt / double(nl)) * double(n * ic[cls]));
+            S += n * ic[cls];
           }
-          mass_tot[s * NSL + slot] = acc;
+          s_icnt0[s * NA + a] = ic[0];
+          s_copy[s * NA + a] = S;
+          const auto thr = cdf_thresholds(w);
+          opt_cdf.insert(opt_cdf.end(), thr.begin(), thr.end());
         }
+        s_wn.push_back(wn); s_wt.push_back(wt); s_nl.push_back(nl);
       }
+      if (cls_leaf_tin.empty()) cls_leaf_tin.push_back(N);
     }
     if (leaf_tin.empty()) leaf_tin.push_back(N);
-    std::vector<uint32_t> leaf_cls;
-    if (!c->normal_only)
-      for (uint32_t s2 = 0; s2 < pl->n_samples; ++s2)
-        leaf_cls.insert(leaf_cls.end(), pl->leaf_cls[s2].begin(), pl->leaf_cls[s2].end());
-    if (leaf_cls.empty()) leaf_cls.push_back(0);
     std::vector<uint32_t> etin(N + 2), etout(N + 2);
     for (uint32_t v = 0; v < N; ++v) { etin[v] = pl->tin[v]; etout[v] = pl->tout[v]; }
     etin[N] = 0; etout[N] = c->preneoplastic_in_normal ? N + 1 : N;   // preneoplastic edge
@@ -1405,7 +1435,13 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
       return;
     }
     auto etin_d = upload(P, etin, st), etout_d = upload(P, etout, st);
-    auto ts_d = upload(P, t_start, st), tl_d = upload(P, t_len, st), te_d = upload(P, t_end, st);
+    DBuf<uint32_t> ts_d(P, n_tiles), tl_d(P, n_tiles), te_d(P, n_tiles);
+    {
+      auto cf = upload(P, c_first, st), cn = upload(P, c_ntiles, st), cs = upload(P, c_start, st);
+      auto cns = upload(P, c_nstarts, st), cen = upload(P, c_end, st);
+      pg::seq_make_tiles(uint32_t(c_first.size()), cf.p, cn.p, cs.p, cns.p, cen.p, T, n_tiles, ts_d.p, tl_d.p,
+                         te_d.p, st);
+    }
     auto bs_d = upload(P, b_slot, st), bi_d = upload(P, b_index, st);
     auto cnt_d = upload(P, c_ntiles, st), cns_d = upload(P, c_nstarts, st), cid_d = upload(P, c_id, st);
     auto cf_d = upload(P, c_first, st), cd_d = upload(P, c_depth, st);
@@ -1425,8 +1461,29 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     DBuf<uint32_t> pair_cnt(P, uint64_t(n_tiles) * samples.size()), rlo(P, n_tiles), rhi(P, n_tiles);
     pg::seq_build_records(pl->view(), uint32_t(pl->M), etin_d.p, etout_d.p, recs.p, st);
     DBuf<double> mcum_d, mtot_d;
-    DBuf<uint32_t> tcn_d;
-    if (pl->has_cna) { mcum_d = upload(P, mass_cum, st); mtot_d = upload(P, mass_tot, st); tcn_d = upload(P, tile_cn, st); }
+    DBuf<uint32_t> poff_d, pstart_d, plen_d, patom_d, pcdf_d, ocls_d, oloff_d, onl_d, cltin_d, ocdf_d;
+    uint32_t n_parts_cap = 0;
+    if (pl->has_cna) {
+      const uint32_t NS = uint32_t(samples.size()), NA = uint32_t(pl->atom_start_h.size());
+      n_parts_cap = n_tiles + NA;   // each atom boundary splits at most one tile
+      poff_d = DBuf<uint32_t>(P, uint64_t(n_tiles) + 1);
+      pstart_d = DBuf<uint32_t>(P, n_parts_cap); plen_d = DBuf<uint32_t>(P, n_parts_cap);
+      patom_d = DBuf<uint32_t>(P, n_parts_cap); pcdf_d = DBuf<uint32_t>(P, uint64_t(NS) * n_parts_cap);
+      DBuf<uint32_t> scan_part(P, pg::scan_part_elems(n_tiles, 1));
+      pg::seq_tile_parts(n_tiles, ts_d.p, tl_d.p, pl->atom_start.p, NA, uint32_t(e->G), poff_d.p, scan_part.p,
+                         pstart_d.p, plen_d.p, patom_d.p, st);
+      auto wn_d = upload(P, s_wn, st), wt_d = upload(P, s_wt, st);
+      auto nl_d = upload(P, s_nl, st), i0_d = upload(P, s_icnt0, st), cs_d = upload(P, s_copy, st);
+      auto cf_d2 = upload(P, c_first, st), cn_d2 = upload(P, c_ntiles, st);
+      mcum_d = DBuf<double>(P, uint64_t(NS) * n_tiles);
+      mtot_d = DBuf<double>(P, uint64_t(NS) * c_id.size());
+      DBuf<double> tmass(P, uint64_t(NS) * n_tiles);
+      pg::seq_tile_mass(NS, uint32_t(c_id.size()), cf_d2.p, cn_d2.p, poff_d.p, plen_d.p, patom_d.p, NA, wn_d.p,
+                        wt_d.p, nl_d.p, i0_d.p, cs_d.p, n_tiles, n_parts_cap, tmass.p, mcum_d.p, mtot_d.p, pcdf_d.p,
+                        st);
+      ocls_d = upload(P, opt_class, st); oloff_d = upload(P, opt_leaf_off, st); onl_d = upload(P, opt_nleaf, st);
+      cltin_d = upload(P, cls_leaf_tin, st); ocdf_d = upload(P, opt_cdf, st);
+    }
     pg::seq_tile_counts(uint32_t(samples.size()), uint32_t(b_slot.size()), bs_d.p, bi_d.p, cf_d.p, cnt_d.p, cd_d.p,
                         cns_d.p, cid_d.p, cp_d.p, T, n_tiles, pl->has_cna ? mcum_d.p : nullptr,
                         pl->has_cna ? mtot_d.p : nullptr, uint32_t(c_id.size()), seed, pair_cnt.p, st);
@@ -1440,14 +1497,17 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     prm.err_thr = et >= 4294967295.0 ? 0xffffffffu : uint32_t(et);
     prm.normal_tin = N;
     prm.n_alleles = 2;
-    auto leaf_cls_d = upload(P, leaf_cls, st);
     prm.has_cna = pl->has_cna ? 1u : 0u;
-    prm.cn_max = pl->cn_max;
     prm.gc = pl->classes_view();
-    prm.leaf_cls = leaf_cls_d.p;
     prm.chain_off = pl->chain_off.p; prm.chain_anc = pl->chain_anc.p; prm.chain_key = pl->chain_key.p;
-    prm.tile_cn = pl->has_cna ? tcn_d.p : nullptr;
-    prm.n_tiles = n_tiles;
+    if (pl->has_cna) {
+      prm.n_classes = pl->n_classes;
+      prm.atom_ioff = pl->atom_ioff.p; prm.atom_icnt = pl->atom_icnt.p;
+      prm.part_off = poff_d.p; prm.part_start = pstart_d.p; prm.part_len = plen_d.p; prm.part_atom = patom_d.p;
+      prm.part_cdf = pcdf_d.p; prm.n_parts = n_parts_cap;
+      prm.opt_class = ocls_d.p; prm.opt_leaf_off = oloff_d.p; prm.opt_nleaf = onl_d.p;
+      prm.cls_leaf_tin = cltin_d.p; prm.opt_cdf = ocdf_d.p;
+    }
     Timer timer(st);
     pg::seq_reads(recs.p, uint32_t(pl->M), tiles, pair_cnt.p, smp_d.p, uint32_t(samples.size()), leaf_d.p, prm, seed,
                   res->alt.p, res->depth.p, st);

@@ -136,6 +136,10 @@ struct SeqSample {
   uint32_t leaf_off;       // into leaf_tin
   uint32_t normal_thr;     // read from a normal cell iff u < normal_thr
   uint32_t all_normal;     // the normal sample: every read from a normal cell
+  // with copy-number events: the sample's cell options (option 0 its normal
+  // cells, then the genotype classes of its leaves, ascending) and, per atom,
+  // the thresholds of the option draw (rows of n_opt at opt_cdf_off)
+  uint32_t opt_off, n_opt, opt_cdf_off;
 };
 
 struct SeqParams {
@@ -150,17 +154,53 @@ struct SeqParams {
   uint32_t n_alleles;
   // copy-number state (has_cna == 0: every cell has instances 0 and 1 everywhere)
   uint32_t has_cna;
-  uint32_t cn_max;         // largest number of instances covering a position
   GenomeClasses gc;
-  const uint32_t* leaf_cls;   // class of each leaf, parallel to leaf_tin
   const uint32_t* chain_off;  // instance lineage: for instance y, ancestors chain_anc[chain_off[y]..]
-  const uint16_t* chain_anc;  //   with the order key (tin << 16 | seq) of the copy that led towards y
+  const uint16_t* chain_anc;  //   with the order key (tin << 16 | seq + 1) of the copy that led towards y
   const uint64_t* chain_key;
-  const uint32_t* tile_cn;    // per (sample, tile): copy slots of the rejection draw (>= the largest
-                              //   copy number of the tile's starts in the sample's cells)
-  uint32_t n_tiles;
+  // Atoms: the coarsest partition of the genome into intervals on which every
+  // class's covering instances are constant.  A tile's start range is cut
+  // into parts, one per atom it meets.
+  uint32_t n_classes;         // row length of atom_ioff / atom_icnt
+  const uint32_t* atom_ioff;  // [atom * n_classes + class]: first covering instance in gc.inst_list
+  const uint32_t* atom_icnt;  //   and their number (0: the class has no allele there)
+  const uint32_t* part_off;   // parts of tile t: [part_off[t], part_off[t + 1])
+  const uint32_t* part_start; // absolute first start position of the part
+  const uint32_t* part_len;
+  const uint32_t* part_atom;
+  const uint32_t* part_cdf;   // [sample * n_parts + part]: thresholds of the part draw within its tile
+  uint32_t n_parts;
+  const uint32_t* opt_class;  // per cell option: genotype class
+  const uint32_t* opt_leaf_off;   // its leaves in cls_leaf_tin
+  const uint32_t* opt_nleaf;      // 0: the normal cells
+  const uint32_t* cls_leaf_tin;   // every sample's leaves grouped by class (Euler indices)
+  const uint32_t* opt_cdf;        // option thresholds (see SeqSample)
 };
 
+// tile t of chromosome slot c (c_first[c] <= t < c_first[c] + c_ntiles[c],
+// k = t - c_first[c]) covers the starts [c_start + k T, + min(T, S - k T))
+void seq_make_tiles(uint32_t n_slots, const uint32_t* c_first, const uint32_t* c_ntiles, const uint32_t* c_start,
+                    const uint32_t* c_nstarts, const uint32_t* c_end, uint32_t T, uint32_t n_tiles, uint32_t* start,
+                    uint32_t* len, uint32_t* end, cudaStream_t st);
+// Copy-number tables of a sequencing call.  Parts: tile t's start range cut
+// at atom boundaries, at part_off[t] .. part_off[t + 1] (part_off holds
+// n_tiles + 1 entries; `part` is scan scratch of scan_part_elems(n_tiles, 1)).
+void seq_tile_parts(uint32_t n_tiles, const uint32_t* tile_start, const uint32_t* tile_len,
+                    const uint32_t* atom_start, uint32_t n_atoms, uint32_t genome_len, uint32_t* part_off,
+                    uint32_t* scan_part, uint32_t* part_start, uint32_t* part_len, uint32_t* part_atom,
+                    cudaStream_t st);
+// Per (sample, tile) its mass (scratch tile_mass, n_samples * n_tiles) and,
+// for tiles of several parts, the thresholds of the part draw
+// (part_cdf[s * n_parts + part]); then per (sample, chromosome slot),
+// summed in tile order, the mass before each tile (mass_cum[s * n_tiles + t])
+// and the slot's total (mass_tot[s * n_slots + slot]).  A stretch with integer
+// copy sums (I0, S) weighs wn * I0 + (wt / nl) * S (the second term when
+// nl > 0); icnt0 / copy_sum are per (sample, atom).
+void seq_tile_mass(uint32_t n_samples, uint32_t n_slots, const uint32_t* c_first, const uint32_t* c_ntiles,
+                   const uint32_t* part_off, const uint32_t* part_len, const uint32_t* part_atom, uint32_t n_atoms,
+                   const double* wn, const double* wt, const uint64_t* nl, const uint64_t* icnt0,
+                   const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, double* tile_mass, double* mass_cum,
+                   double* mass_tot, uint32_t* part_cdf, cudaStream_t st);
 void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_tin, const uint32_t* edge_tout,
                        SeqRec* recs, cudaStream_t st);
 void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start, const uint32_t* len,

@@ -200,24 +200,56 @@ __device__ __forceinline__ bool observed(const SeqParams& prm, uint32_t tin, uin
 }
 
 // one fragment's draws: mate starts, source cell, allele instance and its
-// error word.  With copy-number events the (start, cell, instance) triple is
-// drawn by rejection within the tile: slot u in [0, tile_cn) is kept when
-// more than u instances of the cell cover the start, which makes starts
-// proportional to copy number; attempt a >= 1 uses Philox block a of the
-// fragment's TAG_PAIR stream.  A fragment that finds no covering instance in
-// 256 attempts is dropped (inst = 0xffff).
+// error word.  Without copy-number events: start uniform in the tile, cell
+// normal with probability normal_thr / 2^32 else a uniform leaf, allele 0 or
+// 1.  With them, (start, cell, instance) is uniform over the DNA of the
+// sample's cells: the part of the tile (word z of the TAG_PAIR2 block, when
+// the tile meets more than one atom) with probability proportional to its
+// mass, the start uniform in the part, the cell option (normal cells or a
+// leaf class) proportional to its copies in the part's atom, a uniform leaf
+// of the class and a uniform covering instance.
 struct Fragment {
   uint32_t p0, p1, cell, inst, w;
 };
 
-constexpr uint32_t FRAG_ATTEMPTS = 256;
+// The copy-number draw tables of one (tile, sample) staged in shared memory:
+// the tile's parts with their thresholds and, per part, the option
+// thresholds of its atom and each option's covering instances there.
+constexpr uint32_t SEQ_CN_PARTS = 4, SEQ_CN_OPTS = 8;
+struct CnCache {
+  uint32_t pstart[SEQ_CN_PARTS], plen[SEQ_CN_PARTS], pthr[SEQ_CN_PARTS];
+  uint32_t othr[SEQ_CN_PARTS][SEQ_CN_OPTS], oioff[SEQ_CN_PARTS][SEQ_CN_OPTS], oicnt[SEQ_CN_PARTS][SEQ_CN_OPTS];
+  uint32_t onl[SEQ_CN_OPTS], oloff[SEQ_CN_OPTS];
+  uint32_t n_parts, n_opt;
+};
+
+__device__ __forceinline__ void fill_cn_cache(CnCache& c, const SeqParams& prm, const SeqSample& sm, uint32_t t,
+                                              uint32_t s, uint32_t tid) {
+  const uint32_t pb = prm.part_off[t], pn = prm.part_off[t + 1] - pb, no = sm.n_opt;
+  if (tid == 0) { c.n_parts = pn; c.n_opt = no; }
+  if (tid < pn) {
+    c.pstart[tid] = prm.part_start[pb + tid];
+    c.plen[tid] = prm.part_len[pb + tid];
+    c.pthr[tid] = prm.part_cdf[uint64_t(s) * prm.n_parts + pb + tid];
+  }
+  if (tid < no) { c.onl[tid] = prm.opt_nleaf[sm.opt_off + tid]; c.oloff[tid] = prm.opt_leaf_off[sm.opt_off + tid]; }
+  if (tid < pn * no) {
+    const uint32_t p = tid / no, o = tid % no;
+    const uint32_t atom = prm.part_atom[pb + p];
+    c.othr[p][o] = prm.opt_cdf[sm.opt_cdf_off + atom * no + o];
+    const uint32_t ai = atom * prm.n_classes + prm.opt_class[sm.opt_off + o];
+    c.oioff[p][o] = prm.atom_ioff[ai];
+    c.oicnt[p][o] = prm.atom_icnt[ai];
+  }
+}
 
 template <bool INS_SMEM>
 __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
                                                   uint32_t len, uint32_t ce, const SeqSample& sm,
                                                   const uint32_t* __restrict__ leaf_tin, const SeqParams& prm,
-                                                  const uint32_t* ins, const uint16_t* guide) {
-  U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
+                                                  const uint32_t* ins, const uint16_t* guide,
+                                                  const CnCache* cc = nullptr) {
+  const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
   const U4 r2 = philox(key.k0, key.k1, j, t, s, TAG_PAIR2);
   Fragment f;
   const uint32_t R = prm.read_len;
@@ -226,25 +258,25 @@ __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t 
     const bool normal = sm.all_normal || r.y < sm.normal_thr;
     f.cell = normal ? prm.normal_tin : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.z, sm.n_leaves));
     f.inst = __umulhi(r.w, prm.n_alleles);
+  } else if (cc) {
+    const uint32_t part = cc->n_parts > 1 ? cdf_lookup(cc->pthr, cc->n_parts, r2.z) : 0u;
+    f.p0 = cc->pstart[part] + __umulhi(r.x, cc->plen[part]);
+    const uint32_t o = cdf_lookup(cc->othr[part], cc->n_opt, r.y);
+    const uint32_t nl = cc->onl[o];
+    f.cell = nl ? __ldg(prm.cls_leaf_tin + cc->oloff[o] + __umulhi(r.z, nl)) : prm.normal_tin;
+    const uint32_t icnt = cc->oicnt[part][o];
+    f.inst = icnt ? uint32_t(__ldg(prm.gc.inst_list + cc->oioff[part][o] + __umulhi(r.w, icnt))) : 0xffffu;
   } else {
-    f.inst = 0xffffu;
-    for (uint32_t att = 0; att < FRAG_ATTEMPTS; ++att) {
-      if (att) r = philox(key.k0, key.k1, j, t, s, TAG_PAIR | (att << 8));
-      f.p0 = start + __umulhi(r.x, len);
-      const bool normal = sm.all_normal || r.y < sm.normal_thr;
-      uint32_t cls = 0;
-      if (normal) {
-        f.cell = prm.normal_tin;
-      } else {
-        const uint32_t li = sm.leaf_off + __umulhi(r.z, sm.n_leaves);
-        f.cell = __ldg(leaf_tin + li);
-        cls = __ldg(prm.leaf_cls + li);
-      }
-      const uint32_t slot = __umulhi(r.w, __ldg(prm.tile_cn + uint64_t(s) * prm.n_tiles + t));
-      uint32_t ioff = 0;
-      const uint32_t n = covering(prm.gc, cls, f.p0, &ioff);
-      if (slot < n) { f.inst = __ldg(prm.gc.inst_list + ioff + slot); break; }
-    }
+    const uint32_t pb = __ldg(prm.part_off + t), pn = __ldg(prm.part_off + t + 1) - pb;
+    const uint32_t part = pb + (pn > 1 ? cdf_lookup(prm.part_cdf + uint64_t(s) * prm.n_parts + pb, pn, r2.z) : 0u);
+    const uint32_t atom = __ldg(prm.part_atom + part);
+    f.p0 = __ldg(prm.part_start + part) + __umulhi(r.x, __ldg(prm.part_len + part));
+    const uint32_t o = sm.opt_off + cdf_lookup(prm.opt_cdf + sm.opt_cdf_off + atom * sm.n_opt, sm.n_opt, r.y);
+    const uint32_t nl = __ldg(prm.opt_nleaf + o);
+    f.cell = nl ? __ldg(prm.cls_leaf_tin + __ldg(prm.opt_leaf_off + o) + __umulhi(r.z, nl)) : prm.normal_tin;
+    const uint32_t ai = atom * prm.n_classes + __ldg(prm.opt_class + o);
+    const uint32_t icnt = __ldg(prm.atom_icnt + ai);
+    f.inst = icnt ? uint32_t(__ldg(prm.gc.inst_list + __ldg(prm.atom_ioff + ai) + __umulhi(r.w, icnt))) : 0xffffu;
   }
   f.w = r2.y;
   f.p1 = f.p0;
@@ -284,6 +316,7 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
   __shared__ uint32_t s_wpre[SEQ_CAP];      // prefix of the records' candidate counts
   __shared__ uint32_t s_scan[8];
   __shared__ uint32_t s_wtot;
+  __shared__ CnCache s_cn;
   const uint32_t t = blockIdx.x, s = blockIdx.y, tid = threadIdx.x;
   const uint32_t n_pairs = pair_cnt[uint64_t(s) * tiles.n_tiles + t];
   const uint32_t lo = tiles.rec_lo[t], nw = tiles.rec_hi[t] - lo;
@@ -326,6 +359,12 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
     for (uint32_t i = tid; i < prm.n_ins; i += SEQ_THREADS) s_ins[i] = prm.ins_cdf[i];
     for (uint32_t g = tid; g < SEQ_GUIDE; g += SEQ_THREADS) s_guide[g] = prm.ins_guide[g];
   }
+  // copy-number draws from shared memory when the tile's tables fit
+  // (the first barrier of the batch loop publishes them)
+  const bool cn_smem = prm.has_cna && prm.part_off[t + 1] - prm.part_off[t] <= SEQ_CN_PARTS &&
+                       sm.n_opt <= SEQ_CN_OPTS;
+  if (cn_smem) fill_cn_cache(s_cn, prm, sm, t, s, tid);
+  const CnCache* cc = cn_smem ? &s_cn : nullptr;
   const uint32_t per_batch = SEQ_MCAP / 2;
 
   constexpr uint32_t FPT = SEQ_MCAP / 2 / SEQ_THREADS;   // fragments per thread and batch
@@ -341,8 +380,8 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
       const uint32_t k = tid + q * SEQ_THREADS;
       if (k < nb_pairs) {
         const Fragment f = ins_smem
-            ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide)
-            : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
+            ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide, cc)
+            : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr, cc);
         ca[q] = f.cell;
         fi[q] = f.inst;
         fw[q] = f.w;
@@ -448,6 +487,174 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
 }
 
 static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
+
+__global__ void k_make_tiles(uint32_t n_slots, const uint32_t* __restrict__ c_first,
+                             const uint32_t* __restrict__ c_ntiles, const uint32_t* __restrict__ c_start,
+                             const uint32_t* __restrict__ c_nstarts, const uint32_t* __restrict__ c_end, uint32_t T,
+                             uint32_t n_tiles, uint32_t* __restrict__ start, uint32_t* __restrict__ len,
+                             uint32_t* __restrict__ end) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tiles) return;
+  uint32_t lo = 0, hi = n_slots;          // last slot whose first tile is <= t
+  while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (c_first[mid] <= t) lo = mid; else hi = mid; }
+  const uint32_t k = t - c_first[lo];
+  start[t] = c_start[lo] + k * T;
+  len[t] = min(T, c_nstarts[lo] - k * T);
+  end[t] = c_end[lo];
+  (void)c_ntiles;
+}
+
+// last atom starting at or before position a
+__device__ __forceinline__ uint32_t atom_of(const uint32_t* __restrict__ atom_start, uint32_t n_atoms, uint32_t a) {
+  uint32_t lo = 0, hi = n_atoms;
+  while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (atom_start[mid] <= a) lo = mid; else hi = mid; }
+  return lo;
+}
+
+__global__ void k_part_counts(uint32_t n_tiles, const uint32_t* __restrict__ tile_start,
+                              const uint32_t* __restrict__ tile_len, const uint32_t* __restrict__ atom_start,
+                              uint32_t n_atoms, uint32_t* __restrict__ cnt) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tiles) return;
+  const uint32_t a = tile_start[t], b = a + tile_len[t];
+  uint32_t x = atom_of(atom_start, n_atoms, a), n = 0;
+  for (; x < n_atoms && atom_start[x] < b; ++x) ++n;
+  cnt[t] = n;
+}
+
+__global__ void k_part_emit(uint32_t n_tiles, const uint32_t* __restrict__ tile_start,
+                            const uint32_t* __restrict__ tile_len, const uint32_t* __restrict__ atom_start,
+                            uint32_t n_atoms, uint32_t genome_len, const uint32_t* __restrict__ part_off,
+                            uint32_t* __restrict__ part_start, uint32_t* __restrict__ part_len,
+                            uint32_t* __restrict__ part_atom) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tiles) return;
+  const uint32_t a = tile_start[t], b = a + tile_len[t];
+  uint32_t q = part_off[t];
+  for (uint32_t x = atom_of(atom_start, n_atoms, a); x < n_atoms && atom_start[x] < b; ++x, ++q) {
+    const uint32_t lo = max(a, atom_start[x]);
+    const uint32_t hi = min(b, x + 1 < n_atoms ? atom_start[x + 1] : genome_len);
+    part_start[q] = lo; part_len[q] = hi - lo; part_atom[q] = x;
+  }
+}
+
+// mass of one stretch of starts with integer copy sums (i0, sum)
+__device__ __forceinline__ double stretch_mass(double wn, double wt, uint64_t nl, uint64_t i0, uint64_t sum) {
+  double m = wn * double(i0);
+  if (nl > 0) m = m + (wt / double(nl)) * double(sum);
+  return m;
+}
+
+// one thread per (sample, tile): the tile's mass and, for tiles of several
+// parts, the thresholds floor(CDF * 2^31) of the part draw with the last
+// part of positive mass at 2^31 (the host's cdf_thresholds)
+__global__ void k_tile_mass(uint32_t n_samples, uint32_t n_tiles, const uint32_t* __restrict__ part_off,
+                            const uint32_t* __restrict__ part_len, const uint32_t* __restrict__ part_atom,
+                            uint32_t n_atoms, const double* __restrict__ wn_s, const double* __restrict__ wt_s,
+                            const uint64_t* __restrict__ nl_s, const uint64_t* __restrict__ icnt0,
+                            const uint64_t* __restrict__ copy_sum, uint32_t n_parts, double* __restrict__ tile_mass,
+                            uint32_t* __restrict__ part_cdf) {
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= uint64_t(n_samples) * n_tiles) return;
+  const uint32_t s = uint32_t(gid / n_tiles), t = uint32_t(gid % n_tiles);
+  const double wn = wn_s[s], wt = wt_s[s];
+  const uint64_t nl = nl_s[s];
+  const uint64_t* i0a = icnt0 + uint64_t(s) * n_atoms;
+  const uint64_t* sa = copy_sum + uint64_t(s) * n_atoms;
+  const uint32_t pb = part_off[t], pe = part_off[t + 1];
+  uint64_t i0 = 0, sum = 0;
+  for (uint32_t q = pb; q < pe; ++q) {
+    const uint64_t len = part_len[q], x = part_atom[q];
+    i0 += len * i0a[x];
+    sum += len * sa[x];
+  }
+  if (pe - pb > 1) {
+    double tot = 0.0;
+    uint32_t last = pb;
+    for (uint32_t q = pb; q < pe; ++q) {
+      const uint64_t len = part_len[q], x = part_atom[q];
+      const double w = stretch_mass(wn, wt, nl, len * i0a[x], len * sa[x]);
+      tot += w;
+      if (w > 0) last = q;
+    }
+    uint32_t* thr = part_cdf + uint64_t(s) * n_parts;
+    double c = 0.0;
+    for (uint32_t q = pb; q < pe; ++q) {
+      const uint64_t len = part_len[q], x = part_atom[q];
+      c += stretch_mass(wn, wt, nl, len * i0a[x], len * sa[x]);
+      if (!(tot > 0)) { thr[q] = 0u; continue; }
+      double v = floor(c / tot * 2147483648.0);
+      if (v > 2147483648.0) v = 2147483648.0;
+      thr[q] = (q >= last) ? 2147483648u : uint32_t(v);
+    }
+  }
+  tile_mass[gid] = stretch_mass(wn, wt, nl, i0, sum);
+}
+
+// one CTA per (sample, chromosome slot): the masses before each tile,
+// summed in tile order by one thread over chunks staged in shared memory
+// (the order fixes the rounding), and the slot's total
+constexpr uint32_t MASS_CHUNK = 2048;
+__global__ void __launch_bounds__(256) k_mass_prefix(uint32_t n_slots, const uint32_t* __restrict__ c_first,
+                                                     const uint32_t* __restrict__ c_ntiles, uint32_t n_tiles,
+                                                     const double* __restrict__ tile_mass,
+                                                     double* __restrict__ mass_cum, double* __restrict__ mass_tot) {
+  __shared__ double buf[MASS_CHUNK];
+  __shared__ double acc_s;
+  const uint32_t s = blockIdx.x / n_slots, slot = blockIdx.x % n_slots;
+  const uint32_t first = c_first[slot], nt = c_ntiles[slot];
+  const double* in = tile_mass + uint64_t(s) * n_tiles + first;
+  double* out = mass_cum + uint64_t(s) * n_tiles + first;
+  if (threadIdx.x == 0) acc_s = 0.0;
+  for (uint32_t c0 = 0; c0 < nt; c0 += MASS_CHUNK) {
+    const uint32_t n = min(MASS_CHUNK, nt - c0);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) buf[i] = in[c0 + i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double acc = acc_s;
+      for (uint32_t i = 0; i < n; ++i) { const double m = buf[i]; buf[i] = acc; acc = acc + m; }
+      acc_s = acc;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[c0 + i] = buf[i];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mass_tot[uint64_t(s) * n_slots + slot] = acc_s;
+}
+
+void seq_tile_parts(uint32_t n_tiles, const uint32_t* tile_start, const uint32_t* tile_len,
+                    const uint32_t* atom_start, uint32_t n_atoms, uint32_t genome_len, uint32_t* part_off,
+                    uint32_t* scan_part, uint32_t* part_start, uint32_t* part_len, uint32_t* part_atom,
+                    cudaStream_t st) {
+  if (!n_tiles) return;
+  k_part_counts<<<nblk(n_tiles), 256, 0, st>>>(n_tiles, tile_start, tile_len, atom_start, n_atoms, part_off);
+  note_launch();
+  scan_rows<uint32_t>(part_off, part_off, n_tiles, 1, scan_part, part_off + n_tiles, st);
+  k_part_emit<<<nblk(n_tiles), 256, 0, st>>>(n_tiles, tile_start, tile_len, atom_start, n_atoms, genome_len,
+                                             part_off, part_start, part_len, part_atom);
+  note_launch();
+}
+
+void seq_tile_mass(uint32_t n_samples, uint32_t n_slots, const uint32_t* c_first, const uint32_t* c_ntiles,
+                   const uint32_t* part_off, const uint32_t* part_len, const uint32_t* part_atom, uint32_t n_atoms,
+                   const double* wn, const double* wt, const uint64_t* nl, const uint64_t* icnt0,
+                   const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, double* tile_mass, double* mass_cum,
+                   double* mass_tot, uint32_t* part_cdf, cudaStream_t st) {
+  const uint64_t n = uint64_t(n_samples) * n_tiles;
+  if (!n) return;
+  k_tile_mass<<<nblk(n), 256, 0, st>>>(n_samples, n_tiles, part_off, part_len, part_atom, n_atoms, wn, wt, nl, icnt0,
+                                       copy_sum, n_parts, tile_mass, part_cdf);
+  k_mass_prefix<<<n_samples * n_slots, 256, 0, st>>>(n_slots, c_first, c_ntiles, n_tiles, tile_mass, mass_cum,
+                                                     mass_tot);
+  note_launch(2);
+}
+
+void seq_make_tiles(uint32_t n_slots, const uint32_t* c_first, const uint32_t* c_ntiles, const uint32_t* c_start,
+                    const uint32_t* c_nstarts, const uint32_t* c_end, uint32_t T, uint32_t n_tiles, uint32_t* start,
+                    uint32_t* len, uint32_t* end, cudaStream_t st) {
+  if (n_tiles) { k_make_tiles<<<nblk(n_tiles), 256, 0, st>>>(n_slots, c_first, c_ntiles, c_start, c_nstarts, c_end, T,
+                                                             n_tiles, start, len, end); note_launch(); }
+}
 
 void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_tin, const uint32_t* edge_tout,
                        SeqRec* recs, cudaStream_t st) {

@@ -217,6 +217,20 @@ class SamplesForest:
         is_parent[self.parent[self.parent >= 0]] = True
         self.is_leaf = ~is_parent
 
+    def species_codes(self) -> tuple[list[tuple[str, str]], np.ndarray]:
+        """The distinct (mutant, epistate) pairs and each node's index among
+        them (computed once per pair of mutant/epistate arrays)."""
+        cache = getattr(self, "_codes", None)
+        if cache is not None and cache[0] is self.mutant and cache[1] is self.epistate:
+            return cache[2], cache[3]
+        table: dict[tuple[str, str], int] = {}
+        code = np.fromiter((table.setdefault((str(m), "" if e is None else str(e)), len(table))
+                            for m, e in zip(self.mutant.tolist(), self.epistate.tolist())),
+                           dtype=np.int64, count=len(self.mutant))
+        names = list(table)
+        self._codes = (self.mutant, self.epistate, names, code)
+        return names, code
+
     @property
     def num_of_nodes(self) -> int:
         return len(self.cell_id)
@@ -470,16 +484,16 @@ class MutationEngine:
 
     # -- placement ------------------------------------------------------------------
     def forest_species(self, forest: SamplesForest) -> np.ndarray:
-        out = np.empty(forest.num_of_nodes, dtype=np.uint32)
-        for i, (m, e) in enumerate(zip(forest.mutant, forest.epistate)):
-            key = (str(m), "" if e is None else str(e))
+        """Species id of every node: its (mutant, epistate), else the mutant's
+        epistate-free species."""
+        names, code = forest.species_codes()
+        ids = np.empty(len(names), dtype=np.uint32)
+        for k, (m, e) in enumerate(names):
+            key = (m, e) if (m, e) in self.species else (m, "")
             if key not in self.species:
-                key2 = (str(m), "")
-                if key2 not in self.species:
-                    raise DomainError(_lib.PG_ERR_DOMAIN, f'unknown species "{m}{e}": add its mutant first')
-                key = key2
-            out[i] = self.species[key]
-        return out
+                raise DomainError(_lib.PG_ERR_DOMAIN, f'unknown species "{m}{e}": add its mutant first')
+            ids[k] = self.species[key]
+        return ids[code]
 
     def place_mutations(self, samples_forest: SamplesForest, num_of_preneoplatic_SNVs: int = 0,
                         num_of_preneoplatic_indels: int = 0, seed=None,

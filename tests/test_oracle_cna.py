@@ -77,7 +77,8 @@ def _sid(chr_, pos, ref, alt, allele):
     return Mutation(chr_, pos, ref, alt, allele)
 
 
-def test_deletion_halves_depth_and_hides_mutations(orc):
+@pytest.mark.parametrize("flavour", [0, 1])
+def test_deletion_halves_depth_and_hides_mutations(orc, flavour):
     from process_gb300 import synth
     w = synth.config1(seed=7, n_leaves=100)
     w.genome.chr_lengths = [300_000] * 3
@@ -85,7 +86,7 @@ def test_deletion_halves_depth_and_hides_mutations(orc):
     # delete allele 0 of [100001, 200000] of chromosome 2 in every tumour cell
     o.add_driver_cna(0, False, 1, 100_001, 100_000, allele=0)
     f = w.forest
-    p = o.place(f, _species(o, f), 200, 0, 0, 0, seed=2)
+    p = o.place(f, _species(o, f), 200, 0, 0, 0, seed=2, flavour=flavour)
     t = p.table()
     lo, hi = 300_000 + 100_000, 300_000 + 200_000
     inside = (t["locus"] >= lo) & (t["locus"] < hi)
@@ -93,7 +94,7 @@ def test_deletion_halves_depth_and_hides_mutations(orc):
     passenger = t["nature"] == 0
     assert inside.any() and (t["allele"][inside & passenger] == 1).all()
     _, dep, _ = p.sequence(_cfg(coverage=60, read_size=150, insert_size_mean=0, error_rate=0.0, purity=1.0,
-                                with_normal_sample=False), 5)
+                                with_normal_sample=False), 5, flavour=flavour)
     d_in = dep[0][inside & passenger].mean()
     d_out = dep[0][~inside & passenger & (t["locus"] >= 300_000) & (t["locus"] < 600_000)].mean()
     assert 0.35 < d_in / d_out < 0.65
