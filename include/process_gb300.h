@@ -260,6 +260,50 @@ pg_status pg_calib_nll_grad_one(pg_calib* cal, uint32_t rep, const float* params
 pg_status pg_calib_adam(pg_calib* cal, float* params, uint32_t steps, float lr, float beta1, float beta2, float eps,
                         float* nll);
 
+/* ------------------------------------------------------------------ batches
+ * Many independent instances on one engine's genome and signatures (no
+ * reference counterpart: the reference places and sequences one instance per
+ * MutationEngine$place_mutations / simulate_seq call).  Instance i has its own
+ * forest (every node of species 0), passenger rates snv_rate[i] /
+ * indel_rate[i] per base per division, one exposure (row i of sbs_expo over
+ * the engine's SBS signatures and of id_expo over its ID signatures; NULL =
+ * zero), preneoplastic counts (NULL = none) of the signatures pre_sbs_sig /
+ * pre_id_sig, and a sequencing configuration (cfgs[i].tile_size 0 = the
+ * analytic size).  A run computes for every instance exactly what the plain
+ * path computes for it alone (pg_place_mutations then pg_simulate_seq on an
+ * engine whose species 0 has those rates and that exposure at time 0, with
+ * the same seeds and the instance's tile size).  Placement runs as single
+ * launches over all instances; sequencing as one persistent kernel over every
+ * (instance, sample, tile), captured into a CUDA graph on the first run and
+ * replayed afterwards. */
+typedef struct pg_batch pg_batch;
+pg_status pg_batch_create(pg_engine* eng, uint32_t n_inst, const pg_forest* const* forests, const double* snv_rate,
+                          const double* indel_rate, const double* sbs_expo, const double* id_expo,
+                          const uint32_t* n_pre_snv, uint32_t pre_sbs_sig, const uint32_t* n_pre_indel,
+                          uint32_t pre_id_sig, const pg_seq_cfg* cfgs, pg_batch** out);
+pg_status pg_batch_destroy(pg_batch* batch);
+/* place and sequence every instance with its placement and sequencing seed */
+pg_status pg_batch_run(pg_batch* batch, const uint64_t* place_seed, const uint64_t* seq_seed);
+/* The autotuner: places once with these seeds, then times the whole
+ * persistent read launch for candidate tile sizes (multiples 0.5, 0.75, 1,
+ * 1.25 of every instance's analytic size) and keeps the fastest; tile_sizes
+ * (may be NULL) receives the choice. */
+pg_status pg_batch_autotune(pg_batch* batch, const uint64_t* place_seed, const uint64_t* seq_seed,
+                            uint32_t* tile_sizes);
+pg_status pg_batch_tile_sizes(const pg_batch* batch, uint32_t* tile_sizes);
+pg_status pg_batch_set_tile_sizes(pg_batch* batch, const uint32_t* tile_sizes);
+/* after a run: instance inst's mutations, sequenced samples and reads */
+pg_status pg_batch_dims(const pg_batch* batch, uint32_t inst, uint64_t* n_mutations, uint32_t* n_samples,
+                        uint64_t* n_reads);
+/* instance inst's placed mutations (sorted by locus, the columns of
+ * pg_placed_copy) and its alt/depth tables [sample][mutation]; any pointer may
+ * be NULL */
+pg_status pg_batch_copy(const pg_batch* batch, uint32_t inst, uint32_t* locus, uint32_t* edge, uint32_t* aux,
+                        uint8_t* cls, uint8_t* sig, uint16_t* allele, uint8_t* kind, uint8_t* nature, int32_t* alt,
+                        int32_t* depth);
+/* device time of the last run's placement and sequencing stages (ms) */
+pg_status pg_batch_kernel_ms(const pg_batch* batch, float* place_ms, float* seq_ms);
+
 #ifdef __cplusplus
 }
 #endif

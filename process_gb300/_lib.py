@@ -96,6 +96,17 @@ _PROTOS = {
     "pg_seq_result_dims": (C.c_int, [P, u32p, u64p, u64p]),
     "pg_seq_result_copy": (C.c_int, [P, i32p, i32p]),
     "pg_seq_result_kernel_ms": (C.c_int, [P, f32p]),
+    "pg_batch_create": (C.c_int, [P, C.c_uint32, C.POINTER(P), f64p, f64p, f64p, f64p, u32p, C.c_uint32, u32p,
+                                  C.c_uint32, C.POINTER(SeqCfg), C.POINTER(P)]),
+    "pg_batch_destroy": (C.c_int, [P]),
+    "pg_batch_run": (C.c_int, [P, u64p, u64p]),
+    "pg_batch_autotune": (C.c_int, [P, u64p, u64p, u32p]),
+    "pg_batch_tile_sizes": (C.c_int, [P, u32p]),
+    "pg_batch_set_tile_sizes": (C.c_int, [P, u32p]),
+    "pg_batch_dims": (C.c_int, [P, C.c_uint32, u64p, u32p, u64p]),
+    "pg_batch_copy": (C.c_int, [P, C.c_uint32, u32p, u32p, u32p, u8p, u8p, C.POINTER(C.c_uint16), u8p, u8p, i32p,
+                                i32p]),
+    "pg_batch_kernel_ms": (C.c_int, [P, f32p, f32p]),
 }
 
 # symbols added by later additions to the ABI are bound when present

@@ -1736,3 +1736,5 @@ pg_status pg_calib_adam(pg_calib* c, float* params, uint32_t steps, float lr, fl
 }
 
 }  // extern "C"
+
+#include "pg_batch_impl.h"

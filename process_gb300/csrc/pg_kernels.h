@@ -7,6 +7,12 @@
 
 namespace pg {
 
+// Philox key of a call (the seed's two words)
+struct Key { uint32_t k0, k1; };
+__host__ __device__ inline Key make_key(uint64_t seed) {
+  return {uint32_t(seed), uint32_t(seed >> 32)};
+}
+
 constexpr uint32_t MAX_EPOCHS = 16;
 
 // Counts kernel launches of this library (read with pg_launch_count).
@@ -201,6 +207,68 @@ void seq_tile_mass(uint32_t n_samples, uint32_t n_slots, const uint32_t* c_first
                    const double* wn, const double* wt, const uint64_t* nl, const uint64_t* icnt0,
                    const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, double* tile_mass, double* mass_cum,
                    double* mass_tot, uint32_t* part_cdf, cudaStream_t st);
+// ---------------------------------------------------------------- batched sequencing
+// Per-instance descriptor of a batch.  The work items of instance i are its
+// (sample, tile) pairs, sample-major; every table row below is relative to
+// the instance's offsets, so each instance computes exactly what the plain
+// path computes for it alone with the same tile size and seed.
+struct SeqInst {
+  SeqParams prm;
+  uint32_t n_samples, sample_off;   // rows of the batch's SeqSample array
+  uint32_t n_tiles, tile_off;       // rows of the batch's tile arrays
+  uint32_t T;                       // tile size
+  uint32_t slot_off;                // chromosome tables
+  uint32_t n_blocks, blk_off;       // tile-split blocks of 64 tiles
+  uint32_t etin_off;                // edge Euler table rows (n_nodes + 2)
+  uint64_t pair_off;                // pair counts [sample][tile]
+  uint64_t count_off;               // alt/depth of sample s: count_off + s * count_stride + record
+  uint32_t count_stride;            // >= the instance's mutations
+};
+struct SeqBatch {
+  uint32_t n_inst;
+  const SeqInst* inst;
+  const Key* keys;                  // sequencing key of each instance
+  const uint32_t* rec_off;          // n_inst + 1: records of instance i (filled by placement)
+  const uint32_t* item_off;         // n_inst + 1: first work item of each instance
+  const uint32_t* cnt_off;          // n_inst + 1: first tile-split thread of each instance
+  uint32_t n_items, n_cnt, n_tiles_all;
+  const uint32_t *tile_start, *tile_len, *tile_end, *tile_inst;
+  uint32_t *rec_lo, *rec_hi;        // per tile, relative to the instance's first record
+  const uint32_t *c_first, *c_ntiles, *c_depth, *c_nstarts, *c_id;
+  const uint64_t* c_pairs;
+  const uint32_t *blk_slot, *blk_index;
+  uint32_t* pair_cnt;
+  const SeqSample* samples;
+  const uint32_t* leaf_tin;
+  const uint32_t *etin, *etout;
+  uint32_t* counter;                // work-item counter of the persistent read kernel
+  uint32_t *alt, *depth;
+};
+// batched placement (launchers in pg_place.cu): cells of instance i are
+// [cell_off[i], cell_off[i+1]); node_off counts each instance's nodes plus its
+// preneoplastic edge
+void place_edge_counts_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* node_off, uint32_t n_nodes_all,
+                             const uint32_t* cell_off, const Key* keys, const uint32_t* pre_snv, const uint32_t* pre_id,
+                             uint32_t* cnt_snv, uint32_t* cnt_id, cudaStream_t st);
+void place_mutations_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* cell_off, const Key* keys,
+                           const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
+                           uint32_t n_snv, const uint32_t* pending, uint32_t n_pending, int redraw, uint32_t* err,
+                           cudaStream_t st);
+void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uint32_t* pending, uint32_t n,
+                       uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
+                       uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st);
+// sort by (instance, locus); bcnt holds n_inst * sort_num_buckets(G) + 1
+// entries and ends as the exclusive scan of the bucket counts
+void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t n_inst, uint64_t G, uint32_t* bcnt,
+                uint32_t* bfill, uint32_t* part, uint32_t* order, const PlaceOut& sorted, uint16_t* inst_sorted,
+                cudaStream_t st);
+// resident CTAs per SM of the persistent read kernel
+int seq_reads_batch_occupancy();
+// records of the first *n_dev sorted mutations of a batch (cap >= *n_dev)
+void seq_batch_records(const PlaceOut& sorted, const uint16_t* inst_sorted, const uint32_t* n_dev, uint32_t cap,
+                       const SeqBatch& b, SeqRec* recs, cudaStream_t st);
+// tile split, record ranges and the persistent read kernel over every work item
+void seq_batch_reads(const SeqBatch& b, const SeqRec* recs, uint32_t grid, cudaStream_t st);
 void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_tin, const uint32_t* edge_tout,
                        SeqRec* recs, cudaStream_t st);
 void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start, const uint32_t* len,

@@ -34,11 +34,12 @@ namespace pg {
 constexpr uint32_t RECLASS_ATTEMPTS = 16;
 
 // ------------------------------------------------------------ per-edge counts
-__global__ void k_edge_counts(PlaceTables t, uint32_t* __restrict__ cnt_snv, uint32_t* __restrict__ cnt_id,
-                              Key key, uint32_t n_pre_snv, uint32_t n_pre_id) {
-  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+// counts of edge v (v == n_nodes: the preneoplastic edge) into
+// cnt_*[v * n_epochs + e]
+__device__ __forceinline__ void edge_counts_one(const PlaceTables& t, uint32_t v, Key key, uint32_t* __restrict__ cnt_snv,
+                                                uint32_t* __restrict__ cnt_id, uint32_t n_pre_snv,
+                                                uint32_t n_pre_id) {
   const uint32_t N = t.n_nodes, E = t.n_epochs;
-  if (v > N) return;
   if (v == N) {  // preneoplastic edge
     for (uint32_t e = 0; e < E; ++e) {
       cnt_snv[uint64_t(v) * E + e] = e == 0 ? n_pre_snv : 0u;
@@ -70,6 +71,13 @@ __global__ void k_edge_counts(PlaceTables t, uint32_t* __restrict__ cnt_snv, uin
   }
 }
 
+__global__ void k_edge_counts(PlaceTables t, uint32_t* __restrict__ cnt_snv, uint32_t* __restrict__ cnt_id,
+                              Key key, uint32_t n_pre_snv, uint32_t n_pre_id) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v > t.n_nodes) return;
+  edge_counts_one(t, v, key, cnt_snv, cnt_id, n_pre_snv, n_pre_id);
+}
+
 // passenger CNA events per edge: Poisson(rate_cna[species] * 2G * divisions);
 // the germline size is used so that the counts do not depend on the copy
 // number the events themselves create
@@ -92,20 +100,10 @@ __device__ __forceinline__ uint32_t find_cell(const uint32_t* __restrict__ off, 
 // Placement of slot i (first placement when redraw==0: class and position;
 // redraw: position only, with attempt+1).  kind 0 = SNV slots [0, n_snv),
 // kind 1 = indel slots [n_snv, n_snv+n_id).
-__global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
-                        const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_id,
-                        const uint32_t* __restrict__ pending, uint32_t n_pending, int redraw,
-                        uint32_t* __restrict__ err) {
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= n_pending) return;
-  const uint32_t slot = pending ? pending[tid] : tid;
-  const bool is_id = slot >= n_snv;
-  const uint32_t i = is_id ? slot - n_snv : slot;
-  const uint32_t ncell = (t.n_nodes + 1) * t.n_epochs;
-  const uint32_t* off = is_id ? off_id : off_snv;
-  const uint32_t q = find_cell(off, ncell, i);
-  const uint32_t v = q / t.n_epochs, e = q % t.n_epochs;
-  const uint32_t m = i - off[q];
+// Mutation m of (edge v, epoch e), SNV or indel, written at `slot` of o.
+__device__ __forceinline__ void place_one(const PlaceTables& t, const PlaceOut& o, Key key, uint32_t slot, bool is_id,
+                                          uint32_t v, uint32_t e, uint32_t m, int redraw,
+                                          uint32_t* __restrict__ err) {
   Stream st{key, m, v, e, is_id ? TAG_INDEL : TAG_SNV, 0u};
   uint32_t cls, sig;
   if (!redraw) {
@@ -178,6 +176,21 @@ __global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __re
     o.locus[slot] = p - 1;                       // anchor base
     o.aux[slot] = ins | (l << 1) | (bases << 8);
   }
+}
+
+__global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
+                        const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_id,
+                        const uint32_t* __restrict__ pending, uint32_t n_pending, int redraw,
+                        uint32_t* __restrict__ err) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_pending) return;
+  const uint32_t slot = pending ? pending[tid] : tid;
+  const bool is_id = slot >= n_snv;
+  const uint32_t i = is_id ? slot - n_snv : slot;
+  const uint32_t ncell = (t.n_nodes + 1) * t.n_epochs;
+  const uint32_t* off = is_id ? off_id : off_snv;
+  const uint32_t q = find_cell(off, ncell, i);
+  place_one(t, o, key, slot, is_id, q / t.n_epochs, q % t.n_epochs, i - off[q], redraw, err);
 }
 
 // ------------------------------------------------------------ hash sets
@@ -328,6 +341,144 @@ __global__ void k_gather_sorted(PlaceOut o, const uint32_t* __restrict__ order, 
   s.kind[i] = o.kind[x]; s.nature[i] = o.nature[x]; s.attempt[i] = o.attempt[x];
 }
 
+__global__ void k_gather_u16(const uint16_t* __restrict__ in, const uint32_t* __restrict__ order, uint32_t n,
+                             uint16_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[order[i]];
+}
+
+// ------------------------------------------------------------ batched placement
+// A batch places the forests of many instances on one genome in single
+// launches.  Cells (edge, epoch) of instance i occupy [cell_off[i],
+// cell_off[i+1]) of the count arrays; the global slot space is every SNV of
+// every instance (cells in order) followed by every indel, so the slots of
+// one instance keep their relative order and every per-instance decision
+// (Philox counters, lowest-slot wins, ties of the sort) is that of the plain
+// path for the instance alone.
+__device__ __forceinline__ uint32_t upper_index(const uint32_t* __restrict__ off, uint32_t n, uint32_t x) {
+  // largest i < n with off[i] <= x
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (off[mid] <= x) lo = mid; else hi = mid; }
+  return lo;
+}
+
+__global__ void k_edge_counts_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst,
+                                const uint32_t* __restrict__ node_off, const uint32_t* __restrict__ cell_off,
+                                const Key* __restrict__ keys, const uint32_t* __restrict__ pre_snv,
+                                const uint32_t* __restrict__ pre_id, uint32_t* __restrict__ cnt_snv,
+                                uint32_t* __restrict__ cnt_id) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= node_off[n_inst]) return;
+  const uint32_t i = upper_index(node_off, n_inst, g);
+  const PlaceTables& t = tabs[i];
+  edge_counts_one(t, g - node_off[i], keys[i], cnt_snv + cell_off[i], cnt_id + cell_off[i], pre_snv[i], pre_id[i]);
+}
+
+__global__ void k_place_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst, const uint32_t* __restrict__ cell_off,
+                          const Key* __restrict__ keys, PlaceOut o, uint16_t* __restrict__ inst_of,
+                          const uint32_t* __restrict__ off_snv, const uint32_t* __restrict__ off_id, uint32_t n_snv,
+                          const uint32_t* __restrict__ pending, uint32_t n_pending, int redraw,
+                          uint32_t* __restrict__ err) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= n_pending) return;
+  const uint32_t slot = pending ? pending[tid] : tid;
+  const bool is_id = slot >= n_snv;
+  const uint32_t j = is_id ? slot - n_snv : slot;
+  const uint32_t n_cells = cell_off[n_inst];
+  const uint32_t* off = is_id ? off_id : off_snv;
+  const uint32_t q = find_cell(off, n_cells, j);        // global cell
+  const uint32_t i = upper_index(cell_off, n_inst, q);
+  const PlaceTables& t = tabs[i];
+  const uint32_t lq = q - cell_off[i];
+  if (!redraw) inst_of[slot] = uint16_t(i);
+  place_one(t, o, keys[i], slot, is_id, lq / t.n_epochs, lq % t.n_epochs, j - off[q], redraw, err);
+}
+
+// infinite-sites rounds of a batch: loci are unique per instance, so the
+// hash keys are (instance << 32 | locus)
+__device__ __forceinline__ uint64_t hash64(uint64_t k) {
+  k ^= k >> 33; k *= 0xff51afd7ed558ccdull; k ^= k >> 33; k *= 0xc4ceb9fe1a85ec53ull; k ^= k >> 33;
+  return k;
+}
+constexpr uint64_t EMPTY64 = ~0ull;
+__device__ __forceinline__ bool hset64_contains(const uint64_t* __restrict__ keys, uint64_t mask, uint64_t k) {
+  uint64_t h = hash64(k) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    const uint64_t x = keys[h];
+    if (x == k) return true;
+    if (x == EMPTY64) return false;
+    h = (h + 1) & mask;
+  }
+  return false;
+}
+__device__ __forceinline__ uint64_t hset64_insert(unsigned long long* __restrict__ keys, uint64_t mask, uint64_t k) {
+  uint64_t h = hash64(k) & mask;
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    const unsigned long long prev = atomicCAS(keys + h, (unsigned long long)EMPTY64, (unsigned long long)k);
+    if (prev == EMPTY64 || prev == k) return h;
+    h = (h + 1) & mask;
+  }
+  return EMPTY64;
+}
+
+__global__ void k_cand_insert_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
+                                const uint32_t* __restrict__ pending, uint32_t n, const uint64_t* __restrict__ hkeys,
+                                uint64_t hmask, unsigned long long* __restrict__ ckeys, uint32_t* __restrict__ cvals,
+                                uint64_t cmask, uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t slot = pending ? pending[i] : i;
+  const uint32_t l = locus[slot];
+  const uint64_t k = (uint64_t(inst_of[slot]) << 32) | l;
+  if (l == LOCUS_INVALID || hset64_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
+  lost[i] = 0;
+  const uint64_t h = hset64_insert(ckeys, cmask, k);
+  if (h == EMPTY64) { atomicOr(err, ERR_CAPACITY); return; }
+  atomicMin(cvals + h, slot);
+}
+
+__global__ void k_cand_resolve_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
+                                 const uint32_t* __restrict__ pending, uint32_t n,
+                                 unsigned long long* __restrict__ hkeys, uint64_t hmask,
+                                 const uint64_t* __restrict__ ckeys, const uint32_t* __restrict__ cvals,
+                                 uint64_t cmask, const uint8_t* __restrict__ lost, uint32_t* __restrict__ next,
+                                 uint32_t* __restrict__ n_next, uint32_t* __restrict__ err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t slot = pending ? pending[i] : i;
+  const uint64_t k = (uint64_t(inst_of[slot]) << 32) | locus[slot];
+  bool win = false;
+  if (!lost[i]) {
+    uint64_t h = hash64(k) & cmask;
+    for (uint64_t probe = 0; probe <= cmask; ++probe) {
+      const uint64_t x = ckeys[h];
+      if (x == k) { win = cvals[h] == slot; break; }
+      if (x == EMPTY64) break;
+      h = (h + 1) & cmask;
+    }
+  }
+  if (win) {
+    if (hset64_insert(hkeys, hmask, k) == EMPTY64) atomicOr(err, ERR_CAPACITY);
+  } else {
+    next[atomicAdd(n_next, 1u)] = slot;
+  }
+}
+
+// sort of a batch by (instance, locus): bucket = instance * nb + locus >> 10
+__global__ void k_bucket_count_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of, uint32_t n,
+                                 uint32_t nb, uint32_t* __restrict__ bcnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(bcnt + uint64_t(inst_of[i]) * nb + (locus[i] >> BUCKET_SHIFT), 1u);
+}
+__global__ void k_bucket_scatter_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
+                                   uint32_t n, uint32_t nb, const uint32_t* __restrict__ boff,
+                                   uint32_t* __restrict__ bfill, uint32_t* __restrict__ order) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t b = uint64_t(inst_of[i]) * nb + (locus[i] >> BUCKET_SHIFT);
+  order[boff[b] + atomicAdd(bfill + b, 1u)] = i;
+}
+
 // ------------------------------------------------------------ host launchers
 static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
 
@@ -385,5 +536,48 @@ void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, ui
 }
 
 uint32_t sort_num_buckets(uint64_t G) { return uint32_t((G >> BUCKET_SHIFT) + 1); }
+
+void place_edge_counts_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* node_off, uint32_t n_nodes_all,
+                             const uint32_t* cell_off, const Key* keys, const uint32_t* pre_snv, const uint32_t* pre_id,
+                             uint32_t* cnt_snv, uint32_t* cnt_id, cudaStream_t st) {
+  if (n_nodes_all) { k_edge_counts_b<<<nblk(n_nodes_all, 128), 128, 0, st>>>(tabs, n_inst, node_off, cell_off, keys,
+                                                                          pre_snv, pre_id, cnt_snv, cnt_id); note_launch(); }
+}
+
+void place_mutations_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* cell_off, const Key* keys,
+                           const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
+                           uint32_t n_snv, const uint32_t* pending, uint32_t n_pending, int redraw, uint32_t* err,
+                           cudaStream_t st) {
+  if (n_pending == 0) return;
+  k_place_b<<<nblk(n_pending), 256, 0, st>>>(tabs, n_inst, cell_off, keys, o, inst_of, off_snv, off_id, n_snv, pending,
+                                             n_pending, redraw, err); note_launch();
+}
+
+void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uint32_t* pending, uint32_t n,
+                       uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
+                       uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st) {
+  if (n == 0) return;
+  k_cand_insert_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, hkeys, hmask,
+                                           reinterpret_cast<unsigned long long*>(ckeys), cvals, cmask, lost, err);
+  k_cand_resolve_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, reinterpret_cast<unsigned long long*>(hkeys),
+                                            hmask, ckeys, cvals, cmask, lost, next, n_next, err);
+  note_launch(2);
+}
+
+void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t n_inst, uint64_t G, uint32_t* bcnt,
+                uint32_t* bfill, uint32_t* part, uint32_t* order, const PlaceOut& sorted, uint16_t* inst_sorted,
+                cudaStream_t st) {
+  const uint32_t nb = uint32_t((G >> BUCKET_SHIFT) + 1);
+  const uint64_t nbt = uint64_t(nb) * n_inst;
+  cudaMemsetAsync(bcnt, 0, sizeof(uint32_t) * (nbt + 1), st);
+  cudaMemsetAsync(bfill, 0, sizeof(uint32_t) * nbt, st);
+  if (n == 0) return;
+  k_bucket_count_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt); note_launch();
+  scan_rows<uint32_t>(bcnt, bcnt, nbt, 1, part, bcnt + nbt, st);
+  k_bucket_scatter_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt, bfill, order); note_launch();
+  k_bucket_sort<<<nblk(nbt), 256, 0, st>>>(o.locus, bcnt, uint32_t(nbt), n, order); note_launch();
+  k_gather_sorted<<<nblk(n), 256, 0, st>>>(o, order, n, sorted); note_launch();
+  k_gather_u16<<<nblk(n), 256, 0, st>>>(inst_of, order, n, inst_sorted); note_launch();
+}
 
 }  // namespace pg

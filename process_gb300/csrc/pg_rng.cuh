@@ -14,6 +14,7 @@
 // contract anything, and log is computed by our own routine (below), never by
 // the CUDA math library.
 #pragma once
+#include "pg_kernels.h"
 #include <cstdint>
 
 namespace pg {
@@ -43,10 +44,6 @@ enum : uint32_t {
   TAG_GENOME = 11, TAG_CNA = 12
 };
 
-struct Key { uint32_t k0, k1; };
-__host__ __device__ inline Key make_key(uint64_t seed) {
-  return {uint32_t(seed), uint32_t(seed >> 32)};
-}
 
 // uniform index in [0, n) from one 32-bit word (floor(u * n / 2^32))
 __device__ __forceinline__ uint32_t uniform_index32(uint32_t u, uint32_t n) {

@@ -123,16 +123,17 @@ constexpr uint32_t SPLIT_BLOCK_LOG = 6;   // 64 tiles per thread
 
 // one thread per (sample, block of 64 tiles): walk from the root to the
 // block's node, then draw the block's 63 internal splits top-down
-__global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* __restrict__ blk_slot,
-                              const uint32_t* __restrict__ blk_index, const uint32_t* __restrict__ chr_first_tile,
-                              const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
-                              const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
-                              const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles,
-                              const double* __restrict__ mass_cum, const double* __restrict__ mass_tot,
-                              uint32_t n_slots, Key key, uint32_t* __restrict__ pair_cnt) {
-  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (gid >= uint64_t(n_blocks) * n_samples) return;
-  const uint32_t s = uint32_t(gid / n_blocks), bi = uint32_t(gid % n_blocks);
+__device__ __forceinline__ void tile_counts_one(uint32_t s, uint32_t bi, const uint32_t* __restrict__ blk_slot,
+                                                const uint32_t* __restrict__ blk_index,
+                                                const uint32_t* __restrict__ chr_first_tile,
+                                                const uint32_t* __restrict__ chr_ntiles,
+                                                const uint32_t* __restrict__ chr_depth,
+                                                const uint32_t* __restrict__ chr_nstarts,
+                                                const uint32_t* __restrict__ chr_id,
+                                                const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles,
+                                                const double* __restrict__ mass_cum,
+                                                const double* __restrict__ mass_tot, uint32_t n_slots, Key key,
+                                                uint32_t* __restrict__ pair_cnt) {
   const uint32_t slot = blk_slot[bi], b = blk_index[bi];
   const uint32_t D = chr_depth[slot], chr = chr_id[slot], nt = chr_ntiles[slot];
   const uint32_t base = chr_first_tile[slot];
@@ -166,6 +167,19 @@ __global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint3
     const uint64_t tile = lo + r;
     if (tile < nt) pair_cnt[uint64_t(s) * n_tiles + base + tile] = c[(1u << Db) + r];
   }
+}
+
+__global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* __restrict__ blk_slot,
+                              const uint32_t* __restrict__ blk_index, const uint32_t* __restrict__ chr_first_tile,
+                              const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
+                              const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
+                              const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles,
+                              const double* __restrict__ mass_cum, const double* __restrict__ mass_tot,
+                              uint32_t n_slots, Key key, uint32_t* __restrict__ pair_cnt) {
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (gid >= uint64_t(n_blocks) * n_samples) return;
+  tile_counts_one(uint32_t(gid / n_blocks), uint32_t(gid % n_blocks), blk_slot, blk_index, chr_first_tile, chr_ntiles,
+                  chr_depth, chr_nstarts, chr_id, chr_pairs, T, n_tiles, mass_cum, mass_tot, n_slots, key, pair_cnt);
 }
 
 // error word of the visit of mate `mate` of a fragment (Philox word w) to `locus`
@@ -296,38 +310,48 @@ __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t 
   return f;
 }
 
-__global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restrict__ g_recs, SeqTiles tiles,
-                                                          const uint32_t* __restrict__ pair_cnt,
-                                                          const SeqSample* __restrict__ samples,
-                                                          const uint32_t* __restrict__ leaf_tin, SeqParams prm,
-                                                          Key key, uint64_t n_recs, uint32_t* __restrict__ g_alt,
-                                                          uint32_t* __restrict__ g_dep) {
-  __shared__ uint32_t s_locus[SEQ_CAP], s_tin[SEQ_CAP], s_tout[SEQ_CAP], s_info[SEQ_CAP];
-  __shared__ uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
+// shared memory of one read CTA
+struct ReadSmem {
+  uint32_t s_locus[SEQ_CAP], s_tin[SEQ_CAP], s_tout[SEQ_CAP], s_info[SEQ_CAP];
+  uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
   // mates of the batch in start-bucket order
-  __shared__ uint16_t s_mpos[SEQ_MCAP];     // start offset in the window | mate << 15
-  __shared__ uint32_t s_mcell[SEQ_MCAP];    // source cell (Euler index)
-  __shared__ uint16_t s_minst[SEQ_MCAP];    // allele instance (0xffff: dropped fragment)
-  __shared__ uint32_t s_mw[SEQ_MCAP];       // the fragment's error word
-  __shared__ uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
-  __shared__ uint32_t s_ins[SEQ_INS_CAP];
-  __shared__ uint16_t s_guide[SEQ_GUIDE];
-  __shared__ uint16_t s_wstart[SEQ_CAP];    // first candidate mate (sorted position) of each record
-  __shared__ uint32_t s_wpre[SEQ_CAP];      // prefix of the records' candidate counts
-  __shared__ uint32_t s_scan[8];
-  __shared__ uint32_t s_wtot;
-  __shared__ CnCache s_cn;
-  const uint32_t t = blockIdx.x, s = blockIdx.y, tid = threadIdx.x;
-  const uint32_t n_pairs = pair_cnt[uint64_t(s) * tiles.n_tiles + t];
-  const uint32_t lo = tiles.rec_lo[t], nw = tiles.rec_hi[t] - lo;
+  uint16_t s_mpos[SEQ_MCAP];     // start offset in the window | mate << 15
+  uint32_t s_mcell[SEQ_MCAP];    // source cell (Euler index)
+  uint16_t s_minst[SEQ_MCAP];    // allele instance (0xffff: dropped fragment)
+  uint32_t s_mw[SEQ_MCAP];       // the fragment's error word
+  uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
+  uint32_t s_ins[SEQ_INS_CAP];
+  uint16_t s_guide[SEQ_GUIDE];
+  uint16_t s_wstart[SEQ_CAP];    // first candidate mate (sorted position) of each record
+  uint32_t s_wpre[SEQ_CAP];      // prefix of the records' candidate counts
+  uint32_t s_scan[8];
+  uint32_t s_wtot;
+  CnCache s_cn;
+};
+
+// One work item: the n_pairs fragments of tile t (window [start, ...),
+// records [lo, lo + nw) of g_recs) for sample s, counted into the rows
+// g_alt_row / g_dep_row (indexed by record).  Called by every thread of the
+// CTA with the same arguments.
+__device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict__ g_recs, uint32_t t, uint32_t s,
+                                          uint32_t n_pairs, uint32_t lo, uint32_t nw, uint32_t start, uint32_t len,
+                                          uint32_t ce, const SeqSample& sm, const uint32_t* __restrict__ leaf_tin,
+                                          const SeqParams& prm, Key key, uint32_t* __restrict__ g_alt_row,
+                                          uint32_t* __restrict__ g_dep_row) {
+  auto& s_locus = sh.s_locus; auto& s_tin = sh.s_tin; auto& s_tout = sh.s_tout; auto& s_info = sh.s_info;
+  auto& s_alt = sh.s_alt; auto& s_dep = sh.s_dep;
+  auto& s_mpos = sh.s_mpos; auto& s_mcell = sh.s_mcell; auto& s_minst = sh.s_minst; auto& s_mw = sh.s_mw;
+  auto& s_boff = sh.s_boff; auto& s_ins = sh.s_ins; auto& s_guide = sh.s_guide;
+  auto& s_wstart = sh.s_wstart; auto& s_wpre = sh.s_wpre; auto& s_scan = sh.s_scan;
+  uint32_t& s_wtot = sh.s_wtot;
+  CnCache& s_cn = sh.s_cn;
+  const uint32_t tid = threadIdx.x;
   if (nw == 0 || n_pairs == 0) return;       // nothing to count in this window
-  const uint32_t start = tiles.start[t], len = tiles.len[t], ce = tiles.chr_end[t];
   const uint32_t R = prm.read_len;
   const uint32_t wlen = len - 1 + prm.span;   // the window is [start, start + wlen)
   const uint32_t nbk = (wlen + SEQ_BW - 1) / SEQ_BW;
-  const SeqSample sm = samples[s];
-  uint32_t* galt = g_alt + uint64_t(s) * n_recs + lo;
-  uint32_t* gdep = g_dep + uint64_t(s) * n_recs + lo;
+  uint32_t* galt = g_alt_row + lo;
+  uint32_t* gdep = g_dep_row + lo;
   const SeqRec* grec = g_recs + lo;
   const bool ins_smem = prm.paired && prm.n_ins <= SEQ_INS_CAP;
 
@@ -486,7 +510,92 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
   }
 }
 
+
+__global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restrict__ g_recs, SeqTiles tiles,
+                                                          const uint32_t* __restrict__ pair_cnt,
+                                                          const SeqSample* __restrict__ samples,
+                                                          const uint32_t* __restrict__ leaf_tin, SeqParams prm,
+                                                          Key key, uint64_t n_recs, uint32_t* __restrict__ g_alt,
+                                                          uint32_t* __restrict__ g_dep) {
+  __shared__ ReadSmem sh;
+  const uint32_t t = blockIdx.x, s = blockIdx.y;
+  const uint32_t lo = tiles.rec_lo[t];
+  const SeqSample sm = samples[s];
+  read_tile(sh, g_recs, t, s, pair_cnt[uint64_t(s) * tiles.n_tiles + t], lo, tiles.rec_hi[t] - lo, tiles.start[t],
+            tiles.len[t], tiles.chr_end[t], sm, leaf_tin, prm, key, g_alt + uint64_t(s) * n_recs,
+            g_dep + uint64_t(s) * n_recs);
+}
+
 static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
+
+// ------------------------------------------------------------ batched sequencing
+__device__ __forceinline__ uint32_t batch_index(const uint32_t* __restrict__ off, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;          // largest i < n with off[i] <= x
+  while (hi - lo > 1) { const uint32_t mid = (lo + hi) >> 1; if (off[mid] <= x) lo = mid; else hi = mid; }
+  return lo;
+}
+
+__global__ void k_seq_records_b(PlaceOut s, const uint16_t* __restrict__ inst_sorted, const uint32_t* __restrict__ n_dev,
+                                uint32_t cap, SeqBatch b, SeqRec* __restrict__ recs) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cap || i >= *n_dev) return;
+  const uint32_t e = b.inst[inst_sorted[i]].etin_off + s.edge[i];
+  SeqRec r;
+  r.locus = s.locus[i];
+  r.tin = b.etin[e];
+  r.tout = b.etout[e];
+  r.info = uint32_t(s.allele[i]) | ((uint32_t(s.seq[i]) & 0x7fffu) << 16) | (uint32_t(s.kind[i]) << 31);
+  recs[i] = r;
+}
+
+__global__ void k_tile_ranges_b(SeqBatch b, const SeqRec* __restrict__ recs) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.n_tiles_all) return;
+  const uint32_t i = b.tile_inst[t];
+  const uint32_t r0 = b.rec_off[i], nr = b.rec_off[i + 1] - r0;
+  const uint32_t start = b.tile_start[t];
+  b.rec_lo[t] = lower_bound_rec(recs + r0, nr, start);
+  b.rec_hi[t] = lower_bound_rec(recs + r0, nr, start + b.tile_len[t] - 1 + b.inst[i].prm.span);
+}
+
+__global__ void k_tile_counts_b(SeqBatch b) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= b.n_cnt) return;
+  const uint32_t i = batch_index(b.cnt_off, b.n_inst, gid);
+  const SeqInst& in = b.inst[i];
+  const uint32_t local = gid - b.cnt_off[i];
+  tile_counts_one(local / in.n_blocks, local % in.n_blocks, b.blk_slot + in.blk_off, b.blk_index + in.blk_off,
+                  b.c_first + in.slot_off, b.c_ntiles + in.slot_off, b.c_depth + in.slot_off,
+                  b.c_nstarts + in.slot_off, b.c_id + in.slot_off, b.c_pairs + in.slot_off, in.T, in.n_tiles,
+                  nullptr, nullptr, 0, b.keys[i], b.pair_cnt + in.pair_off);
+}
+
+// Persistent read kernel of a batch: each CTA takes work items from a global
+// counter until none is left; an item is one (instance, sample, tile).
+__global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads_batch(SeqBatch b, const SeqRec* __restrict__ g_recs) {
+  __shared__ ReadSmem sh;
+  __shared__ uint32_t s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    __syncthreads();
+    if (item >= b.n_items) return;
+    const uint32_t i = batch_index(b.item_off, b.n_inst, item);
+    const SeqInst& in = b.inst[i];
+    const uint32_t local = item - b.item_off[i];
+    const uint32_t s = local / in.n_tiles, t = local % in.n_tiles, gt = in.tile_off + t;
+    const uint32_t lo = b.rec_lo[gt];
+    const SeqSample sm = b.samples[in.sample_off + s];
+    const uint64_t row = in.count_off + uint64_t(s) * in.count_stride;
+    read_tile(sh, g_recs + b.rec_off[i], t, s, b.pair_cnt[in.pair_off + uint64_t(s) * in.n_tiles + t], lo,
+              b.rec_hi[gt] - lo, b.tile_start[gt], b.tile_len[gt], b.tile_end[gt], sm, b.leaf_tin, in.prm,
+              b.keys[i], b.alt + row, b.depth + row);
+    __syncthreads();
+  }
+}
+
+
 
 __global__ void k_make_tiles(uint32_t n_slots, const uint32_t* __restrict__ c_first,
                              const uint32_t* __restrict__ c_ntiles, const uint32_t* __restrict__ c_start,
@@ -687,4 +796,21 @@ void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const
                                          depth); note_launch();
 }
 
+void seq_batch_records(const PlaceOut& sorted, const uint16_t* inst_sorted, const uint32_t* n_dev, uint32_t cap,
+                       const SeqBatch& b, SeqRec* recs, cudaStream_t st) {
+  if (cap) { k_seq_records_b<<<nblk(cap), 256, 0, st>>>(sorted, inst_sorted, n_dev, cap, b, recs); note_launch(); }
+}
+
+int seq_reads_batch_occupancy() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_reads_batch, SEQ_THREADS, 0) != cudaSuccess) return 1;
+  return n;
+}
+
+void seq_batch_reads(const SeqBatch& b, const SeqRec* recs, uint32_t grid, cudaStream_t st) {
+  if (b.n_cnt) { k_tile_counts_b<<<nblk(b.n_cnt, 64), 64, 0, st>>>(b); note_launch(); }
+  if (b.n_tiles_all) { k_tile_ranges_b<<<nblk(b.n_tiles_all), 256, 0, st>>>(b, recs); note_launch(); }
+  cudaMemsetAsync(b.counter, 0, sizeof(uint32_t), st);
+  if (b.n_items) { k_reads_batch<<<grid, SEQ_THREADS, 0, st>>>(b, recs); note_launch(); }
+}
 }  // namespace pg

@@ -717,6 +717,130 @@ class PhylogeneticForest:
         return {k: np.array([]) for k in ("chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
 
 
+# ---------------------------------------------------------------- batches
+class Batch:
+    """Many independent instances placed and sequenced together (no
+    reference counterpart; ``pg_batch_*`` of include/process_gb300.h).
+
+    Instance i: ``forests[i]`` (one species), passenger rates
+    ``snv_rates[i]`` / ``indel_rates[i]``, exposure rows ``sbs_exposures[i]``
+    / ``id_exposures[i]`` over the engine's signatures (in ``sig_names``
+    order), preneoplastic counts and the sequencing keywords
+    ``seq_cfgs[i]`` of :func:`sequence_counts`.  Each instance computes what
+    the plain path computes for it alone (same seeds and tile size)."""
+
+    def __init__(self, engine: MutationEngine, forests: Sequence[SamplesForest], snv_rates, indel_rates,
+                 sbs_exposures, id_exposures, seq_cfgs: Sequence[Mapping], n_pre_snv=None, n_pre_indel=None,
+                 preneoplatic_SNV_signature_name: str = "SBS1", preneoplatic_indel_signature_name: str = "ID1"):
+        n = len(forests)
+        self.engine, self.forests = engine, list(forests)
+        self._h = None
+        fh = []
+        try:
+            for f in forests:
+                h = C.c_void_p()
+                parent = np.ascontiguousarray(f.parent, dtype=np.int32)
+                birth = np.ascontiguousarray(f.birth_time, dtype=np.float64)
+                zeros = np.zeros(f.num_of_nodes, dtype=np.uint32)
+                sample = np.ascontiguousarray(np.where(f.is_leaf, f.sample, -1), dtype=np.int32)
+                div = np.ascontiguousarray(f.divisions, dtype=np.uint32)
+                check(lib().pg_forest_create(f.num_of_nodes, ptr(parent, C.c_int32), ptr(birth, C.c_double),
+                                             ptr(zeros, C.c_uint32), ptr(sample, C.c_int32), ptr(div, C.c_uint32),
+                                             len(f.sample_names), C.byref(h)))
+                fh.append(h)
+            arr = (C.c_void_p * n)(*[h.value for h in fh])
+            snv = np.ascontiguousarray(snv_rates, dtype=np.float64)
+            ind = np.ascontiguousarray(indel_rates, dtype=np.float64)
+            sbs = None if sbs_exposures is None else np.ascontiguousarray(sbs_exposures, dtype=np.float64)
+            ids = None if id_exposures is None else np.ascontiguousarray(id_exposures, dtype=np.float64)
+            pre_s = None if n_pre_snv is None else np.ascontiguousarray(n_pre_snv, dtype=np.uint32)
+            pre_i = None if n_pre_indel is None else np.ascontiguousarray(n_pre_indel, dtype=np.uint32)
+
+            def sig_index(ty, name, counts):
+                if counts is None or not np.any(counts):
+                    return 0
+                if name not in engine.sig_names[ty]:
+                    raise DomainError(_lib.PG_ERR_DOMAIN, f"Unknown signature {name}")
+                return engine.sig_names[ty].index(name)
+            cfgs = (_lib.SeqCfg * n)()
+            self._chr_keep = []
+            for i, kw in enumerate(seq_cfgs):
+                c, sel = seq_cfg(chr_index=engine._chr_index, **kw)
+                cfgs[i] = c
+                self._chr_keep.append(sel)
+            self.n = n
+            h = C.c_void_p()
+            check(lib().pg_batch_create(engine._h, n, C.cast(arr, C.POINTER(C.c_void_p)), ptr(snv, C.c_double),
+                                        ptr(ind, C.c_double), ptr(sbs, C.c_double), ptr(ids, C.c_double),
+                                        ptr(pre_s, C.c_uint32), sig_index(0, preneoplatic_SNV_signature_name, pre_s),
+                                        ptr(pre_i, C.c_uint32), sig_index(1, preneoplatic_indel_signature_name, pre_i),
+                                        cfgs, C.byref(h)))
+            self._h = h
+        finally:
+            for h in fh:
+                lib().pg_forest_destroy(h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib._LIB is not None:
+            _lib._LIB.pg_batch_destroy(h)
+            self._h = None
+
+    @staticmethod
+    def _seeds(seeds, n):
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(seeds, dtype=np.uint64), (n,)))
+
+    def run(self, place_seeds, seq_seeds) -> None:
+        ps, ss = self._seeds(place_seeds, self.n), self._seeds(seq_seeds, self.n)
+        check(lib().pg_batch_run(self._h, ptr(ps, C.c_uint64), ptr(ss, C.c_uint64)))
+
+    def autotune(self, place_seeds, seq_seeds) -> np.ndarray:
+        ps, ss = self._seeds(place_seeds, self.n), self._seeds(seq_seeds, self.n)
+        out = np.empty(self.n, dtype=np.uint32)
+        check(lib().pg_batch_autotune(self._h, ptr(ps, C.c_uint64), ptr(ss, C.c_uint64), ptr(out, C.c_uint32)))
+        return out
+
+    @property
+    def tile_sizes(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.uint32)
+        check(lib().pg_batch_tile_sizes(self._h, ptr(out, C.c_uint32)))
+        return out
+
+    @tile_sizes.setter
+    def tile_sizes(self, value) -> None:
+        v = np.ascontiguousarray(np.broadcast_to(np.asarray(value, dtype=np.uint32), (self.n,)))
+        check(lib().pg_batch_set_tile_sizes(self._h, ptr(v, C.c_uint32)))
+
+    def dims(self, i: int) -> tuple[int, int, int]:
+        m, s, r = C.c_uint64(), C.c_uint32(), C.c_uint64()
+        check(lib().pg_batch_dims(self._h, i, C.byref(m), C.byref(s), C.byref(r)))
+        return m.value, s.value, r.value
+
+    def table(self, i: int) -> dict:
+        m, _, _ = self.dims(i)
+        t = {k: np.empty(m, dtype=np.uint32) for k in ("locus", "edge", "aux")}
+        t.update({k: np.empty(m, dtype=np.uint8) for k in ("cls", "sig", "kind", "nature")})
+        t["allele"] = np.empty(m, dtype=np.uint16)
+        check(lib().pg_batch_copy(self._h, i, ptr(t["locus"], C.c_uint32), ptr(t["edge"], C.c_uint32),
+                                  ptr(t["aux"], C.c_uint32), ptr(t["cls"], C.c_uint8), ptr(t["sig"], C.c_uint8),
+                                  ptr(t["allele"], C.c_uint16), ptr(t["kind"], C.c_uint8),
+                                  ptr(t["nature"], C.c_uint8), None, None))
+        return t
+
+    def counts(self, i: int) -> tuple[np.ndarray, np.ndarray]:
+        m, s, _ = self.dims(i)
+        alt = np.empty((s, m), dtype=np.int32)
+        dep = np.empty((s, m), dtype=np.int32)
+        check(lib().pg_batch_copy(self._h, i, None, None, None, None, None, None, None, None,
+                                  ptr(alt, C.c_int32), ptr(dep, C.c_int32)))
+        return alt, dep
+
+    def kernel_ms(self) -> tuple[float, float]:
+        a, b = C.c_float(), C.c_float()
+        check(lib().pg_batch_kernel_ms(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+
 # ---------------------------------------------------------------- sequencing
 class SeqResult:
     """Raw sequencing counts kept on the device until read."""
