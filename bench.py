@@ -162,6 +162,69 @@ def reference_arm(args):
     return 0
 
 
+def batch_bench(stream, n_inst: int, steps: int, warmup: int):
+    """Batched replicates (config 3): every instance placed and sequenced in
+    one batch run (fused placement launches, one persistent read kernel under
+    a CUDA graph, tile sizes from the autotuner).  Reads/s and placed
+    mutations/s of whole runs, timed with CUDA events on the engine stream;
+    beside them the plain path run instance by instance on the first 16."""
+    import ctypes as C
+
+    import torch
+
+    from process_gb300 import _lib, synth
+    from process_gb300.engine import sequence_counts
+    w = synth.config3(seed=3, n_inst=n_inst)
+    eng, b = synth.build_batch(w)
+    _lib.check(_lib.lib().pg_engine_set_stream(eng._h, C.c_void_p(stream.cuda_stream)))
+    seeds = np.arange(n_inst, dtype=np.uint64)
+    tiles = b.autotune(seeds + 1, seeds + 2)
+    for s in range(warmup):
+        b.run(seeds + 100 * (s + 1), seeds + 100 * (s + 1) + 50)
+    torch.cuda.synchronize()
+    ms = place = seq = 0.0
+    reads = muts = 0
+    for s in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(seeds + 10_000 * (s + 1), seeds + 10_000 * (s + 1) + 77)
+        e1.record(stream)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        p_ms, s_ms = b.kernel_ms()
+        place += p_ms
+        seq += s_ms
+        for i in range(n_inst):
+            m, _, r = b.dims(i)
+            reads += r
+            muts += m
+    # the plain path, instance by instance, on the first instances
+    k = min(16, n_inst)
+    from process_gb300 import MutationEngine
+    torch.cuda.synchronize()
+    plain_reads, plain_ms = 0, 0.0
+    for i in range(k):
+        e = MutationEngine(w.genome, w.sbs, w.ids, context_sampling=w.context_sampling)
+        _lib.check(_lib.lib().pg_engine_set_stream(e._h, C.c_void_p(stream.cuda_stream)))
+        e.add_mutant("A", {"SNV": float(w.snv[i]), "indel": float(w.indel[i])})
+        e.add_exposure(0.0, {**{f"SBS{j + 1}": float(w.sbs_expo[i][j]) for j in range(3)},
+                             **{f"ID{j + 1}": float(w.id_expo[i][j]) for j in range(2)}})
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        pf = e.place_mutations(w.forests[i], 0, 0, seed=int(seeds[i]) + 5)
+        r = sequence_counts(pf, int(seeds[i]) + 6, tile_size=int(tiles[i]), **w.seq[i])
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+        plain_reads += r.dims()[2]
+    return {"workload": w.name, "instances": n_inst, "steps": steps, "warmup": warmup,
+            "reads_per_s": reads / (ms / 1000.0), "mutations_placed_per_s": muts / (place / 1000.0),
+            "ms_per_run": ms / steps, "place_ms_per_run": place / steps, "seq_ms_per_run": seq / steps,
+            "reads_per_run": reads // steps, "mutations_per_run": muts // steps,
+            "tile_sizes": {"min": int(tiles.min()), "median": int(np.median(tiles)), "max": int(tiles.max())},
+            "plain_path_reads_per_s_first16": plain_reads / (plain_ms / 1000.0)}
+
+
 def calibration_bench(world: int, n_rep: int = 512, n_sites: int = 100_000, steps: int = 200):
     """Batched calibration (512 replicates x 1e5 sites, Poisson depth means
     U(30, 200), K=4, 3 exposures): gradient evaluations per second of the
@@ -335,6 +398,8 @@ def gpu_arm(args):
     e2e_value = world * e2e_reads / e2e_s
 
     cal = None if args.no_calibration else calibration_bench(world, args.calib_replicates)
+    batch = None if args.no_batch else batch_bench(stream, args.batch_instances, max(1, min(args.steps, 3)),
+                                                   max(1, min(args.warmup, 2)))
 
     line = None
     if rank == 0:
@@ -370,6 +435,7 @@ def gpu_arm(args):
                     "d2h_bytes_per_step": d2h // max(1, e2e_steps)},
             "gpu_launches": n_launch,
             "calibration": cal,
+            "batched": batch,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
@@ -388,6 +454,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-calibration", action="store_true")
     ap.add_argument("--calib-replicates", type=int, default=512)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--genome-scale", type=float, default=1.0,
                     help="fraction of the 3.1 Gbp genome (profiling runs on smaller cases; 1.0 for the bench)")
     args = ap.parse_args()

@@ -166,6 +166,49 @@ class BasicIlluminaSequencer:
 
 
 # ---------------------------------------------------------------- forest
+def preorder(par: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Depth-first preorder of a forest given parent indices (-1 for roots;
+    roots and children visited in index order): the order and each node's
+    position in it.  Level by level with numpy; raises on a cycle."""
+    par = np.asarray(par, dtype=np.int64)
+    n = len(par)
+    root = par < 0
+    kids = np.argsort(np.where(root, n, par), kind="stable")[: n - int(root.sum())]
+    ptr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(ptr, par[~root] + 1, 1)
+    ptr = np.cumsum(ptr)
+    roots = np.nonzero(root)[0]
+    levels, frontier, seen = [roots], roots, len(roots)
+    while True:
+        cnt = ptr[frontier + 1] - ptr[frontier]
+        tot = int(cnt.sum())
+        if tot == 0:
+            break
+        first = np.cumsum(cnt) - cnt
+        frontier = kids[np.repeat(ptr[frontier], cnt) + np.arange(tot) - np.repeat(first, cnt)]
+        levels.append(frontier)
+        seen += tot
+        if seen > n:
+            break
+    if seen != n:
+        raise DomainError(_lib.PG_ERR_DOMAIN, "the ancestor relation is not a forest")
+    size = np.ones(n, dtype=np.int64)
+    for lvl in reversed(levels[1:]):
+        np.add.at(size, par[lvl], size[lvl])
+    pos = np.empty(n, dtype=np.int64)
+    pos[roots] = np.cumsum(size[roots]) - size[roots]
+    for lvl in levels[1:]:
+        p = par[lvl]
+        sz = size[lvl]
+        cs = np.cumsum(sz)
+        start = np.r_[True, p[1:] != p[:-1]]
+        head = np.maximum.accumulate(np.where(start, np.arange(len(lvl)), 0))
+        pos[lvl] = pos[p] + 1 + (cs - sz) - (cs[head] - sz[head])
+    order = np.empty(n, dtype=np.int64)
+    order[pos] = np.arange(n)
+    return order, pos
+
+
 class SamplesForest:
     """A samples forest (``DescendantsForest``, node columns of src/forest.hpp:29-68).
 
@@ -182,24 +225,20 @@ class SamplesForest:
         self.birth_time = np.asarray(birth_time, dtype=np.float64)
         self.divisions = (np.ones(n, dtype=np.uint32) if divisions is None
                           else np.asarray(divisions, dtype=np.uint32))
-        # topological order: parents first
-        pos = {int(c): i for i, c in enumerate(cell_id)}
-        par = np.array([pos.get(int(a), -1) if a >= 0 else -1 for a in ancestor], dtype=np.int64)
-        order, seen = [], np.zeros(n, dtype=bool)
-        kids: dict[int, list[int]] = {}
-        for i, p in enumerate(par):
-            kids.setdefault(int(p), []).append(i)
-        stack = list(reversed(kids.get(-1, [])))
-        while stack:
-            v = stack.pop()
-            if seen[v]:
-                continue
-            seen[v] = True
-            order.append(v)
-            stack.extend(reversed(kids.get(v, [])))
-        if len(order) != n:
-            raise DomainError(_lib.PG_ERR_DOMAIN, "the ancestor relation is not a forest")
-        order = np.asarray(order)
+        # depth-first preorder (parents first, children in the given order)
+        if np.array_equal(cell_id, np.arange(n)):
+            par = np.where(ancestor >= 0, ancestor, -1)
+            if np.any(par >= n):
+                raise DomainError(_lib.PG_ERR_DOMAIN, "unknown ancestor id")
+        else:
+            srt = np.argsort(cell_id, kind="stable")
+            at = np.searchsorted(cell_id[srt], ancestor)
+            at = np.minimum(at, n - 1)
+            found = (ancestor >= 0) & (cell_id[srt][at] == ancestor)
+            if np.any((ancestor >= 0) & ~found):
+                raise DomainError(_lib.PG_ERR_DOMAIN, "unknown ancestor id")
+            par = np.where(found, srt[at], -1)
+        order, _ = preorder(par)
         inv = np.empty(n, dtype=np.int64)
         inv[order] = np.arange(n)
         self.cell_id = cell_id[order]

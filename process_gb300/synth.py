@@ -37,53 +37,48 @@ def birth_forest(n_leaves: int, n_samples: int, seed: int, birth_rate: float = 0
     divisions on an edge is its duration times the birth rate (at least 1).
     ``subclone=(species, fraction)`` marks the clade closest to that fraction
     of the leaves as the driver species."""
+    from .engine import preorder
     rng = np.random.default_rng(seed)
     n_nodes = 2 * n_leaves - 1
     parent = np.full(n_nodes, -1, dtype=np.int64)
     birth = np.zeros(n_nodes, dtype=np.float64)
-    alive = [0]
     birth[0] = t0
-    nxt = 1
-    t = t0
-    while len(alive) < n_leaves:
-        k = len(alive)
-        t += rng.exponential(1.0 / (birth_rate * k))
-        i = int(rng.integers(k))
-        v = alive[i]
-        a, b = nxt, nxt + 1
-        nxt += 2
-        parent[a] = parent[b] = v
-        birth[a] = birth[b] = t
-        alive[i] = a
-        alive.append(b)
-    t_end = t + rng.exponential(1.0 / (birth_rate * len(alive)))
-    # leaves are born at the end of the sampled time window
-    div = np.ones(n_nodes, dtype=np.uint32)
+    # split j (k = j + 1 lineages alive) happens after an Exp(rate * k) wait
+    # and splits a uniform lineage into nodes 2j+1 and 2j+2
+    k = np.arange(1, n_leaves, dtype=np.float64)
+    times = t0 + np.cumsum(rng.exponential(1.0, n_leaves - 1) / (birth_rate * k))
+    picks = (rng.random(n_leaves - 1) * k).astype(np.int64).tolist()
+    alive = [0]
+    split_parent = [0] * (n_leaves - 1)
+    for j, i in enumerate(picks):
+        split_parent[j] = alive[i]
+        alive[i] = 2 * j + 1
+        alive.append(2 * j + 2)
+    if n_leaves > 1:
+        sp = np.asarray(split_parent, dtype=np.int64)
+        parent[1::2] = sp
+        parent[2::2] = sp
+        birth[1::2] = times
+        birth[2::2] = times
+    t_end = (times[-1] if n_leaves > 1 else t0) + rng.exponential(1.0 / (birth_rate * n_leaves))
     leaf = np.zeros(n_nodes, dtype=bool)
     leaf[alive] = True
-    birth_leaf_end = birth.copy()
-    birth_leaf_end[leaf] = t_end
-    for v in range(1, n_nodes):
-        dt = birth_leaf_end[v] - birth[parent[v]]
-        div[v] = max(1, int(round(dt * birth_rate)))
-    birth = birth_leaf_end
-    # depth-first order of the leaves
-    kids = [[] for _ in range(n_nodes)]
-    for v in range(1, n_nodes):
-        kids[parent[v]].append(v)
-    order, stack = [], [0]
-    size = np.zeros(n_nodes, dtype=np.int64)
-    while stack:
-        v = stack.pop()
-        order.append(v)
-        stack.extend(reversed(kids[v]))
-    for v in reversed(order):
-        size[v] = 1 if leaf[v] else sum(size[c] for c in kids[v])
-    dfs_leaves = [v for v in order if leaf[v]]
+    # leaves are born at the end of the sampled time window
+    birth[leaf] = t_end
+    div = np.ones(n_nodes, dtype=np.uint32)
+    if n_nodes > 1:
+        dt = birth[1:] - birth[parent[1:]]
+        div[1:] = np.maximum(1, np.rint(dt * birth_rate)).astype(np.uint32)
+    # depth-first order of the leaves, and leaves below every node
+    order, pos = preorder(parent)
+    size = leaf.astype(np.int64)
+    for v in range(n_nodes - 1, 0, -1):           # children have larger ids than parents
+        size[parent[v]] += size[v]
+    dfs_leaves = order[leaf[order]]
     sample = np.full(n_nodes, None, dtype=object)
     per = int(np.ceil(n_leaves / n_samples))
-    for j, v in enumerate(dfs_leaves):
-        sample[v] = f"S_{j // per + 1}"
+    names = np.array([f"S_{j + 1}" for j in range(n_samples)], dtype=object)
+    sample[dfs_leaves] = names[np.arange(len(dfs_leaves)) // per]
     mut = np.full(n_nodes, mutant, dtype=object)
     epi = np.full(n_nodes, "", dtype=object)
     if subclone is not None:
@@ -91,16 +86,13 @@ def birth_forest(n_leaves: int, n_samples: int, seed: int, birth_rate: float = 0
         target = frac * n_leaves
         cand = np.nonzero(~leaf)[0]
         best = cand[np.argmin(np.abs(size[cand] - target))] if len(cand) else 0
-        stack = [best]
+        # the clade of `best` (2 L - 1 nodes for L leaves in a binary tree)
+        # is the preorder block starting at it
+        block = np.zeros(n_nodes, dtype=bool)
+        block[order[pos[best]:pos[best] + 2 * size[best] - 1]] = True
         sub_mut = name.rstrip("+-")
-        sub_epi = name[len(sub_mut):]
-        while stack:
-            v = stack.pop()
-            mut[v] = sub_mut
-            epi[v] = sub_epi
-            stack.extend(kids[v])
-        if sub_mut == mutant:  # only the epistate differs
-            pass
+        mut[block] = sub_mut
+        epi[block] = name[len(sub_mut):]
     return SamplesForest(np.arange(n_nodes), parent, mut, epi, sample, birth, div)
 
 
@@ -197,6 +189,57 @@ def config2(seed: int = 2, n_leaves_per_sample: int = 10_000, genome_scale: floa
                     n_pre_snv=1000, n_pre_indel=100,
                     seq=dict(coverage=100, read_size=150, insert_size_mean=350, insert_size_stddev=10,
                              insert_model="binomial", error_rate=1e-3, purity=0.7))
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    genome: GenomeSpec
+    sbs: dict
+    ids: dict
+    forests: list
+    snv: np.ndarray
+    indel: np.ndarray
+    sbs_expo: np.ndarray
+    id_expo: np.ndarray
+    seq: list                  # per-instance sequencing keywords
+    context_sampling: int = 1
+
+
+def config3(seed: int = 3, n_inst: int = 256, leaves=(1_000, 50_000), genome_len: int = 100_000_000) -> BatchWorkload:
+    """Batched replicates: n_inst forests with log-uniform leaf counts on one
+    synthetic genome (4 chromosomes); per instance an SNV rate log-uniform in
+    [1e-8, 1e-7] (indels at 0.1x), exposures Dirichlet(1) over 3 SBS and 2 ID
+    signatures, coverage uniform in [30, 200]x, paired 150 bp reads.  The
+    engine indexes every position (context_sampling 1): the busiest instances
+    place ~3 M mutations under the infinite-sites model, more than a
+    1-in-100 index of 100 Mbp holds."""
+    rng = np.random.default_rng(seed)
+    w = rng.dirichlet(np.full(4, 20.0))
+    lengths = np.maximum((w * genome_len).astype(np.int64), 1000)
+    genome = GenomeSpec(["1", "2", "3", "4"], lengths.tolist(), seed=seed, gc=0.41)
+    sbs = dirichlet_signatures(rng, 3, 96, 0.5, "SBS")
+    ids = dirichlet_signatures(rng, 2, 83, 0.5, "ID")
+    lo, hi = np.log(leaves[0]), np.log(leaves[1])
+    n_leaves = np.exp(rng.uniform(lo, hi, n_inst)).astype(np.int64)
+    forests = [birth_forest(int(n_leaves[i]), 1, seed * 100_003 + i, subclone=None, mutant="A")
+               for i in range(n_inst)]
+    snv = 10 ** rng.uniform(-8, -7, n_inst)
+    seq = [dict(coverage=float(rng.uniform(30, 200)), read_size=150, insert_size_mean=350, insert_size_stddev=10,
+                error_rate=1e-3, purity=1.0, with_normal_sample=False) for _ in range(n_inst)]
+    return BatchWorkload(f"config3: {n_inst} forests of {leaves[0]}-{leaves[1]} leaves (log-uniform) on a "
+                         f"{genome_len / 1e6:.0f} Mbp genome, SNV 1e-8-1e-7 (log-uniform), indel 0.1x, "
+                         "exposures Dirichlet(1), coverage U(30, 200)x paired 150 bp",
+                         genome, sbs, ids, forests, snv, 0.1 * snv, rng.dirichlet(np.ones(3), n_inst),
+                         rng.dirichlet(np.ones(2), n_inst), seq)
+
+
+def build_batch(w: BatchWorkload, engine=None):
+    """(engine, Batch) for a batched workload."""
+    from .engine import Batch, MutationEngine
+    eng = engine if engine is not None else MutationEngine(w.genome, w.sbs, w.ids,
+                                                           context_sampling=w.context_sampling)
+    return eng, Batch(eng, w.forests, w.snv, w.indel, w.sbs_expo, w.id_expo, w.seq)
 
 
 def build_engine(w: Workload):
