@@ -572,25 +572,49 @@ __global__ void k_tile_counts_b(SeqBatch b) {
 
 // Persistent read kernel of a batch: each CTA takes work items from a global
 // counter until none is left; an item is one (instance, sample, tile).
+static_assert(sizeof(SeqParams) % 4 == 0 && sizeof(SeqParams) / 4 <= SEQ_THREADS, "SeqParams staging");
+
 __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads_batch(SeqBatch b, const SeqRec* __restrict__ g_recs) {
   __shared__ ReadSmem sh;
-  __shared__ uint32_t s_item;
+  __shared__ SeqParams s_prm;        // the item's instance parameters, staged once per instance change
+  __shared__ SeqSample s_sm;
+  __shared__ Key s_key;
+  __shared__ uint32_t s_item, s_inst, s_t, s_s, s_pairs, s_lo, s_nw, s_start, s_len, s_ce;
+  __shared__ const SeqRec* s_recs;
+  __shared__ uint64_t s_row;
+  uint32_t cur = 0xffffffffu;        // instance whose parameters s_prm holds
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(b.counter, 1u);
+    if (threadIdx.x == 0) {
+      // decode the next work item once for the CTA
+      const uint32_t item = atomicAdd(b.counter, 1u);
+      s_item = item;
+      if (item < b.n_items) {
+        const uint32_t i = batch_index(b.item_off, b.n_inst, item);
+        const SeqInst& in = b.inst[i];
+        const uint32_t local = item - b.item_off[i];
+        const uint32_t s = local / in.n_tiles, t = local % in.n_tiles, gt = in.tile_off + t;
+        s_inst = i; s_t = t; s_s = s;
+        s_lo = b.rec_lo[gt]; s_nw = b.rec_hi[gt] - s_lo;
+        s_pairs = b.pair_cnt[in.pair_off + uint64_t(s) * in.n_tiles + t];
+        s_start = b.tile_start[gt]; s_len = b.tile_len[gt]; s_ce = b.tile_end[gt];
+        s_sm = b.samples[in.sample_off + s];
+        s_key = b.keys[i];
+        s_recs = g_recs + b.rec_off[i];
+        s_row = in.count_off + uint64_t(s) * in.count_stride;
+      }
+    }
     __syncthreads();
-    const uint32_t item = s_item;
-    __syncthreads();
-    if (item >= b.n_items) return;
-    const uint32_t i = batch_index(b.item_off, b.n_inst, item);
-    const SeqInst& in = b.inst[i];
-    const uint32_t local = item - b.item_off[i];
-    const uint32_t s = local / in.n_tiles, t = local % in.n_tiles, gt = in.tile_off + t;
-    const uint32_t lo = b.rec_lo[gt];
-    const SeqSample sm = b.samples[in.sample_off + s];
-    const uint64_t row = in.count_off + uint64_t(s) * in.count_stride;
-    read_tile(sh, g_recs + b.rec_off[i], t, s, b.pair_cnt[in.pair_off + uint64_t(s) * in.n_tiles + t], lo,
-              b.rec_hi[gt] - lo, b.tile_start[gt], b.tile_len[gt], b.tile_end[gt], sm, b.leaf_tin, in.prm,
-              b.keys[i], b.alt + row, b.depth + row);
+    if (s_item >= b.n_items) return;
+    const uint32_t i = s_inst;
+    if (i != cur) {                  // block-uniform
+      if (threadIdx.x < sizeof(SeqParams) / 4)
+        reinterpret_cast<uint32_t*>(&s_prm)[threadIdx.x] =
+            reinterpret_cast<const uint32_t*>(&b.inst[i].prm)[threadIdx.x];
+      cur = i;
+      __syncthreads();
+    }
+    read_tile(sh, s_recs, s_t, s_s, s_pairs, s_lo, s_nw, s_start, s_len, s_ce, s_sm, b.leaf_tin, s_prm, s_key,
+              b.alt + s_row, b.depth + s_row);
     __syncthreads();
   }
 }
