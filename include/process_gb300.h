@@ -227,6 +227,29 @@ pg_status pg_seq_result_copy(const pg_seq_result* res, int32_t* alt, int32_t* de
 /* Device time of the read kernel of the call (ms). */
 pg_status pg_seq_result_kernel_ms(const pg_seq_result* res, float* ms);
 
+/* simulate_seq with write_SAM = TRUE (src/seq_simulation.cpp:540-564; files
+ * and naming of vignettes/sequencing.Rmd:137-180, 282-317): the counts of
+ * pg_simulate_seq, and one SAM file per chromosome,
+ * <output_dir>/<filename_prefix><chromosome name>.sam, holding the reads of
+ * every sequenced sample as read groups named after the samples.  The
+ * directory is created; when it exists the call fails unless `update` is set,
+ * and then a chromosome whose file exists goes to the first free
+ * <filename_prefix><chromosome name>_<n>.sam, n = 1, 2, ...  A read's bases
+ * are the reference with the mutations its allele carries and its
+ * substitution errors (the same draws as the counts); template names are
+ * template_name_prefix followed by a number per file; qualities are the
+ * Phred value of the error rate. */
+typedef struct pg_sam_cfg {
+  const char* output_dir;
+  const char* filename_prefix;        /* R default "chr_" */
+  const char* template_name_prefix;   /* R default "r" */
+  int update;                         /* update_SAM */
+  const char* const* sample_names;    /* one per sequenced sample (normal last) */
+  const char* const* chr_names;       /* one per chromosome of the engine */
+} pg_sam_cfg;
+pg_status pg_simulate_seq_sam(const pg_placed* placed, const pg_seq_cfg* cfg, uint64_t seed, const pg_sam_cfg* sam,
+                              pg_seq_result** out);
+
 /* ------------------------------------------------------------------ calibration
  * Expected-VAF binomial-mixture negative log-likelihood of alt/depth tables
  * and its gradient (no reference counterpart: ProCESS has no calibration

@@ -40,6 +40,13 @@ class SeqCfg(C.Structure):
     ]
 
 
+class SamCfg(C.Structure):
+    _fields_ = [
+        ("output_dir", C.c_char_p), ("filename_prefix", C.c_char_p), ("template_name_prefix", C.c_char_p),
+        ("update", C.c_int), ("sample_names", C.POINTER(C.c_char_p)), ("chr_names", C.POINTER(C.c_char_p)),
+    ]
+
+
 class GenomeDesc(C.Structure):
     _fields_ = [
         ("n_chr", C.c_uint32), ("chr_lengths", C.POINTER(C.c_uint32)), ("bases", C.POINTER(C.c_uint8)),
@@ -96,6 +103,7 @@ _PROTOS = {
     "pg_seq_result_dims": (C.c_int, [P, u32p, u64p, u64p]),
     "pg_seq_result_copy": (C.c_int, [P, i32p, i32p]),
     "pg_seq_result_kernel_ms": (C.c_int, [P, f32p]),
+    "pg_simulate_seq_sam": (C.c_int, [P, C.POINTER(SeqCfg), C.c_uint64, C.POINTER(SamCfg), C.POINTER(P)]),
     "pg_batch_create": (C.c_int, [P, C.c_uint32, C.POINTER(P), f64p, f64p, f64p, f64p, u32p, C.c_uint32, u32p,
                                   C.c_uint32, C.POINTER(SeqCfg), C.POINTER(P)]),
     "pg_batch_destroy": (C.c_int, [P]),

@@ -13,6 +13,8 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <filesystem>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -1259,8 +1261,147 @@ void insert_table(const pg_seq_cfg& c, uint32_t R, uint32_t& ins_min, std::vecto
 
 }  // namespace
 
+namespace {
+
+// SAM files of a sequencing call (see pg_sam_cfg): one per chromosome, the
+// reads of every sample as read groups, built on the device chunk by chunk
+void write_sam(pg_engine* e, const pg_placed* pl, const pg_sam_cfg& sam, uint64_t seed, const pg::SeqRec* recs,
+               const pg::SeqTiles& tiles, const uint32_t* pair_cnt_d, const pg::SeqSample* samples_d,
+               uint32_t n_samples, const uint32_t* leaf_d, const pg::SeqParams& prm,
+               const std::vector<uint32_t>& c_id, const std::vector<uint32_t>& c_first,
+               const std::vector<uint32_t>& c_ntiles, double error_rate) {
+  namespace fs = std::filesystem;
+  require(sam.output_dir && sam.filename_prefix && sam.template_name_prefix && sam.sample_names && sam.chr_names,
+          "NULL SAM argument");
+  cudaStream_t st = e->st;
+  Pool* P = &e->pool;
+  const fs::path dir(sam.output_dir);
+  if (fs::exists(dir)) {
+    require(sam.update != 0, "The output directory \"" + dir.string() + "\" already exists: set update_SAM to write into it");
+    require(fs::is_directory(dir), "\"" + dir.string() + "\" is not a directory");
+  } else {
+    fs::create_directories(dir);
+  }
+  const uint32_t n_tiles = tiles.n_tiles, mates = prm.paired ? 2u : 1u, R = prm.read_len;
+  std::vector<uint32_t> pc(uint64_t(n_samples) * n_tiles);
+  ck(cudaMemcpyAsync(pc.data(), pair_cnt_d, sizeof(uint32_t) * pc.size(), cudaMemcpyDeviceToHost, st), "pair counts");
+  ck(cudaStreamSynchronize(st), "pair counts");
+  // Phred quality of the substitution rate (constant, as the reference's
+  // constant-quality Illumina model)
+  int q = error_rate > 0 ? int(std::lround(-10.0 * std::log10(error_rate))) : 41;
+  q = std::max(2, std::min(41, q));
+  const char qual = char('!' + q);
+  uint64_t cap = uint64_t(1) << 22;   // reads per chunk
+  DBuf<pg::SamRead> out(P, cap);
+  DBuf<char> seq(P, cap * R);
+  std::vector<pg::SamRead> h_out;
+  std::vector<char> h_seq;
+  std::string line;
+  for (size_t slot = 0; slot < c_id.size(); ++slot) {
+    const uint32_t chr = c_id[slot];
+    const std::string name = sam.chr_names[chr];
+    const std::string stem = std::string(sam.filename_prefix) + name;
+    fs::path path = dir / (stem + ".sam");
+    for (uint32_t n = 1; fs::exists(path); ++n) path = dir / (stem + "_" + std::to_string(n) + ".sam");
+    std::ofstream f(path, std::ios::binary);
+    require(bool(f), "cannot write " + path.string());
+    const uint32_t off = e->chr_off[chr];
+    f << "@HD\tVN:1.6\tSO:unsorted\n@SQ\tSN:" << name << "\tLN:" << e->chr_len[chr] << "\n";
+    for (uint32_t s = 0; s < n_samples; ++s) f << "@RG\tID:" << sam.sample_names[s] << "\tSM:" << sam.sample_names[s] << "\n";
+    uint64_t tmpl = 0;
+    const uint32_t t_end = c_first[slot] + c_ntiles[slot];
+    for (uint32_t k = c_first[slot]; k < t_end;) {
+      // a chunk of whole tiles whose reads fit the buffers
+      uint32_t k2 = k;
+      uint64_t frags = 0;
+      while (k2 < t_end) {
+        uint64_t add = 0;
+        for (uint32_t s = 0; s < n_samples; ++s) add += pc[uint64_t(s) * n_tiles + k2];
+        if (k2 > k && (frags + add) * mates > cap) break;
+        frags += add;
+        ++k2;
+      }
+      if (frags * mates > cap) {        // one tile alone exceeds the buffers
+        cap = frags * mates;
+        out = DBuf<pg::SamRead>(P, cap);
+        seq = DBuf<char>(P, cap * R);
+      }
+      const uint32_t n_chunk = k2 - k;
+      std::vector<uint64_t> off_h(uint64_t(n_samples) * n_chunk);
+      uint64_t acc = 0;
+      for (uint32_t s = 0; s < n_samples; ++s)
+        for (uint32_t x = 0; x < n_chunk; ++x) { off_h[uint64_t(s) * n_chunk + x] = acc; acc += pc[uint64_t(s) * n_tiles + k + x]; }
+      auto off_d = upload(P, off_h, st);
+      pg::seq_sam_reads(recs, uint32_t(pl->M), pl->aux.p, e->genome.p, tiles, k, n_chunk, pair_cnt_d, samples_d,
+                        n_samples, leaf_d, prm, seed, off_d.p, out.p, seq.p, R, st);
+      const uint64_t nr = acc * mates;
+      h_out.resize(nr);
+      h_seq.resize(nr * R);
+      if (nr) {
+        ck(cudaMemcpyAsync(h_out.data(), out.p, sizeof(pg::SamRead) * nr, cudaMemcpyDeviceToHost, st), "SAM reads");
+        ck(cudaMemcpyAsync(h_seq.data(), seq.p, nr * R, cudaMemcpyDeviceToHost, st), "SAM reads");
+      }
+      ck(cudaStreamSynchronize(st), "SAM reads");
+      static const char ops[3] = {'M', 'I', 'D'};
+      for (uint32_t s = 0; s < n_samples; ++s) {
+        const std::string rg = std::string("\tRG:Z:") + sam.sample_names[s] + "\n";
+        for (uint32_t x = 0; x < n_chunk; ++x) {
+          const uint64_t o = off_h[uint64_t(s) * n_chunk + x];
+          const uint32_t np = pc[uint64_t(s) * n_tiles + k + x];
+          for (uint32_t j = 0; j < np; ++j) {
+            const std::string qname = std::string(sam.template_name_prefix) + std::to_string(tmpl + o + j);
+            for (uint32_t m = 0; m < mates; ++m) {
+              const uint64_t r = (o + j) * mates + m;
+              const pg::SamRead& a = h_out[r];
+              line.clear();
+              line += qname; line += '\t';
+              line += std::to_string(a.flag); line += '\t';
+              if (a.flag & 4) { line += "*\t0\t0\t*\t*\t0\t0\t*\t*"; line += rg; f << line; continue; }
+              line += name; line += '\t';
+              line += std::to_string(a.pos - off + 1); line += "\t60\t";
+              if (a.n_cigar == 0) line += '*';
+              for (uint32_t c = 0; c < a.n_cigar; ++c) { line += std::to_string(a.cigar[c] >> 4); line += ops[a.cigar[c] & 15u]; }
+              line += '\t';
+              if (prm.paired) { line += "=\t"; line += std::to_string(a.mate_pos - off + 1); }
+              else line += "*\t0";
+              line += '\t'; line += std::to_string(a.tlen); line += '\t';
+              line.append(h_seq.data() + r * R, a.seq_len); line += '\t';
+              line.append(a.seq_len, qual);
+              line += rg;
+              f << line;
+            }
+          }
+        }
+      }
+      tmpl += acc;
+      k = k2;
+    }
+    require(bool(f), "error writing " + path.string());
+  }
+}
+
+void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, const pg_sam_cfg* sam,
+                       pg_seq_result** out);
+
+}  // namespace
+
 pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, pg_seq_result** out) {
+  return guarded([&] { simulate_seq_impl(pl, c, seed, nullptr, out); });
+}
+
+pg_status pg_simulate_seq_sam(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, const pg_sam_cfg* sam,
+                              pg_seq_result** out) {
   return guarded([&] {
+    require(sam != nullptr, "NULL SAM configuration");
+    simulate_seq_impl(pl, c, seed, sam, out);
+  });
+}
+
+namespace {
+
+void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, const pg_sam_cfg* sam,
+                       pg_seq_result** out) {
+  {
     require(pl && c && out, "NULL argument");
     pg_engine* e = pl->eng;
     select_device(e);
@@ -1428,7 +1569,7 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
     res->depth = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
     ck(cudaMemsetAsync(res->alt.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
     ck(cudaMemsetAsync(res->depth.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
-    if (pl->M == 0 || n_tiles == 0 || samples.empty()) {
+    if ((pl->M == 0 && !sam) || n_tiles == 0 || samples.empty()) {
       ck(cudaStreamSynchronize(st), "seq");
       engine_retain(e);
       *out = res.release();
@@ -1513,10 +1654,17 @@ pg_status pg_simulate_seq(const pg_placed* pl, const pg_seq_cfg* c, uint64_t see
                   res->alt.p, res->depth.p, st);
     res->kernel_ms = timer.stop();
     ck(cudaGetLastError(), "sequencing kernels");
+    if (sam) {
+      write_sam(e, pl, *sam, seed, recs.p, tiles, pair_cnt.p, smp_d.p, uint32_t(samples.size()), leaf_d.p, prm, c_id,
+                c_first, c_ntiles, c->error_rate);
+      ck(cudaGetLastError(), "SAM kernels");
+    }
     engine_retain(e);
     *out = res.release();
-  });
+  }
 }
+
+}  // namespace
 
 pg_status pg_seq_result_destroy(pg_seq_result* r) {
   return guarded([&] {

@@ -207,6 +207,31 @@ void seq_tile_mass(uint32_t n_samples, uint32_t n_slots, const uint32_t* c_first
                    const double* wn, const double* wt, const uint64_t* nl, const uint64_t* icnt0,
                    const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, double* tile_mass, double* mass_cum,
                    double* mass_tot, uint32_t* part_cdf, cudaStream_t st);
+// ---------------------------------------------------------------- SAM records
+// One aligned read as the SAM writer needs it; the host formats the text.
+constexpr uint32_t SAM_MAX_CIGAR = 16;
+struct SamRead {
+  uint32_t pos;             // absolute first aligned reference position
+  uint32_t mate_pos;        // absolute first position of the mate (paired reads)
+  int32_t tlen;             // signed template length (0 for single-end reads)
+  uint16_t flag;            // SAM FLAG
+  uint16_t n_cigar;
+  uint32_t seq_len;
+  uint32_t cigar[SAM_MAX_CIGAR];   // op length << 4 | op (0 M, 1 I, 2 D)
+};
+// Reads of tiles [t0, t0 + n_chunk) (global tile indices, for the draws) of
+// every sample: the fragment draws of the read kernel, each mate's bases
+// built from the genome with the mutations its allele instance carries and
+// the substitution errors of its error words.  Read r of the fragment j of
+// (sample s, tile t0 + k) is written at 2 * (out_off[s * n_chunk + k] + j) +
+// mate (one slot per fragment for single-end reads); seq holds max_len
+// bytes per read.
+void seq_sam_reads(const SeqRec* recs, uint32_t n_recs, const uint32_t* aux, const uint32_t* genome,
+                   const SeqTiles& tiles, uint32_t t0, uint32_t n_chunk, const uint32_t* pair_cnt,
+                   const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
+                   uint64_t seed, const uint64_t* out_off, SamRead* out, char* seq, uint32_t max_len,
+                   cudaStream_t st);
+
 // ---------------------------------------------------------------- batched sequencing
 // Per-instance descriptor of a batch.  The work items of instance i are its
 // (sample, tile) pairs, sample-major; every table row below is relative to

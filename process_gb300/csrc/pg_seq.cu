@@ -528,6 +528,126 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
 
 static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 1) / b); }
 
+// ------------------------------------------------------------ SAM reads
+// The bases of one mate starting at reference position p: the reference with
+// the carried SNVs (alt base) and indels (inserted bases; skipped deleted
+// bases, anchored at the base before them), and a substitution wherever the
+// visit's error word is below the threshold.  A substitution picks one of the
+// three other bases with (word % 3); at an SNV site the first of them is the
+// counterpart allele (the alt base when the read shows the reference, the
+// reference when it shows the alt), so that the bases agree with the alt
+// counts of the read kernel.  Inserted bases draw their errors from the word
+// mixed with their rank.  Indels anchored before p are not applied.
+__device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ genome, const SeqRec* __restrict__ recs,
+                           uint32_t n_recs, const uint32_t* __restrict__ aux, uint32_t p, uint32_t ce, uint32_t cell,
+                           uint32_t inst, uint32_t w, uint32_t mate, SamRead& out, char* __restrict__ seq) {
+  const char* ACGT = "ACGT";
+  const uint32_t R = prm.read_len;
+  uint32_t i = lower_bound_rec(recs, n_recs, p);
+  uint32_t q = p, n = 0, nc = 0;
+  auto push = [&](uint32_t op, uint32_t len) {
+    if (nc > 0 && (out.cigar[nc - 1] & 15u) == op) { out.cigar[nc - 1] += len << 4; return; }
+    if (nc < SAM_MAX_CIGAR) out.cigar[nc++] = (len << 4) | op;
+  };
+  auto others = [](uint32_t tb, int first, uint32_t k) {   // k-th base other than tb (first: preferred one)
+    uint32_t o[3] = {0, 0, 0}, m = 0;
+    if (first >= 0 && uint32_t(first) != tb) o[m++] = uint32_t(first);
+    for (uint32_t x = 0; x < 4 && m < 3; ++x) if (x != tb && (m == 0 || x != o[0])) o[m++] = x;
+    return o[k];
+  };
+  bool indels_open = true;
+  while (n < R && q < ce) {
+    const uint32_t b = base_at(genome, q);
+    while (i < n_recs && recs[i].locus < q) ++i;
+    bool site = false, carried_snv = false;
+    uint32_t alt = 0, indel = 0;
+    bool has_indel = false;
+    for (uint32_t k = i; k < n_recs && recs[k].locus == q; ++k) {
+      const SeqRec r = recs[k];
+      const bool carried = (r.tin <= cell) && (cell < r.tout) &&
+                           inst_carries(prm, inst, r.info & 0xffffu, (uint64_t(r.tin) << 16) | ((r.info >> 16) & 0x7fffu));
+      if (!(r.info >> 31)) {
+        if (!site) { site = true; alt = aux[k] & 3u; }
+        if (carried && !carried_snv) { carried_snv = true; alt = aux[k] & 3u; }
+      } else if (carried && !has_indel) {
+        has_indel = true;
+        indel = aux[k];
+      }
+    }
+    uint32_t tb = carried_snv ? alt : b;
+    const uint32_t e = err_word(w, q, mate);
+    if (e < prm.err_thr) tb = others(tb, site ? int(carried_snv ? b : alt) : -1, e % 3u);
+    seq[n++] = ACGT[tb];
+    push(0u, 1u);
+    ++q;
+    if (has_indel && indels_open && nc < SAM_MAX_CIGAR - 2) {
+      const uint32_t l = (indel >> 1) & 7u;
+      if (indel & 1u) {
+        for (uint32_t k = 0; k < l && n < R; ++k) {
+          uint32_t ib = (indel >> (8 + 2 * k)) & 3u;
+          const uint32_t ei = err_word(w ^ (0x9E3779B1u * (k + 1)), q - 1, mate);
+          if (ei < prm.err_thr) ib = others(ib, -1, ei % 3u);
+          seq[n++] = ACGT[ib];
+          push(1u, 1u);
+        }
+      } else if (n < R) {
+        push(2u, l);
+        q += l;
+      }
+    } else if (has_indel) {
+      indels_open = false;       // the CIGAR is full: later indels are not applied
+    }
+  }
+  out.pos = p;
+  out.n_cigar = uint16_t(nc);
+  out.seq_len = n;
+}
+
+__global__ void k_sam_reads(const SeqRec* __restrict__ recs, uint32_t n_recs, const uint32_t* __restrict__ aux,
+                            const uint32_t* __restrict__ genome, SeqTiles tiles, uint32_t t0, uint32_t n_chunk,
+                            const uint32_t* __restrict__ pair_cnt, const SeqSample* __restrict__ samples,
+                            const uint32_t* __restrict__ leaf_tin, SeqParams prm, Key key,
+                            const uint64_t* __restrict__ out_off, SamRead* __restrict__ out, char* __restrict__ seq,
+                            uint32_t max_len) {
+  const uint32_t k = blockIdx.x, s = blockIdx.y, t = t0 + k;
+  const uint32_t n_pairs = pair_cnt[uint64_t(s) * tiles.n_tiles + t];
+  const uint32_t start = tiles.start[t], len = tiles.len[t], ce = tiles.chr_end[t];
+  const SeqSample sm = samples[s];
+  const uint64_t base = out_off[uint64_t(s) * n_chunk + k];
+  const uint32_t mates = prm.paired ? 2u : 1u;
+  for (uint32_t j = threadIdx.x; j < n_pairs; j += blockDim.x) {
+    const Fragment f = make_fragment<false>(key, j, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr);
+    for (uint32_t m = 0; m < mates; ++m) {
+      const uint64_t r = (base + j) * mates + m;
+      SamRead& o = out[r];
+      char* sq = seq + r * max_len;
+      if (f.inst == 0xffffu) { o.pos = f.p0; o.mate_pos = f.p0; o.tlen = 0; o.flag = 4; o.n_cigar = 0; o.seq_len = 0; continue; }
+      const uint32_t p = m ? f.p1 : f.p0;
+      build_read(prm, genome, recs, n_recs, aux, p, ce, f.cell, f.inst, f.w, m, o, sq);
+      if (prm.paired) {
+        o.mate_pos = m ? f.p0 : f.p1;
+        const int32_t span = int32_t(f.p1 + prm.read_len - f.p0);
+        o.tlen = m ? -span : span;
+        o.flag = uint16_t(0x1 | 0x2 | (m ? (0x80 | 0x10) : (0x40 | 0x20)));
+      } else {
+        o.mate_pos = 0; o.tlen = 0; o.flag = 0;
+      }
+    }
+  }
+}
+
+void seq_sam_reads(const SeqRec* recs, uint32_t n_recs, const uint32_t* aux, const uint32_t* genome,
+                   const SeqTiles& tiles, uint32_t t0, uint32_t n_chunk, const uint32_t* pair_cnt,
+                   const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
+                   uint64_t seed, const uint64_t* out_off, SamRead* out, char* seq, uint32_t max_len,
+                   cudaStream_t st) {
+  if (n_chunk == 0 || n_samples == 0) return;
+  dim3 grid(n_chunk, n_samples);
+  k_sam_reads<<<grid, 128, 0, st>>>(recs, n_recs, aux, genome, tiles, t0, n_chunk, pair_cnt, samples, leaf_tin, prm,
+                                    make_key(seed), out_off, out, seq, max_len);
+  note_launch();
+}
+
 // ------------------------------------------------------------ batched sequencing
 __device__ __forceinline__ uint32_t batch_index(const uint32_t* __restrict__ off, uint32_t n, uint32_t x) {
   uint32_t lo = 0, hi = n;          // largest i < n with off[i] <= x

@@ -938,11 +938,23 @@ def seq_cfg(coverage=10, read_size=150, insert_size_mean=0, insert_size_stddev=1
     return c, sel
 
 
-def sequence_counts(phylo_forest: PhylogeneticForest, seed: int, **cfg) -> SeqResult:
-    """Runs the read simulator and returns the device-resident counts."""
+def sequence_counts(phylo_forest: PhylogeneticForest, seed: int, sam: Mapping | None = None, **cfg) -> SeqResult:
+    """Runs the read simulator and returns the device-resident counts.
+    ``sam`` (keys output_dir, update, filename_prefix, template_name_prefix,
+    sample_names) also writes the reads as SAM files."""
     c, _sel = seq_cfg(chr_index=phylo_forest.engine._chr_index, **cfg)
     h = C.c_void_p()
-    check(lib().pg_simulate_seq(phylo_forest._h, C.byref(c), int(seed), C.byref(h)))
+    if sam is None:
+        check(lib().pg_simulate_seq(phylo_forest._h, C.byref(c), int(seed), C.byref(h)))
+    else:
+        names = [str(x).encode() for x in sam["sample_names"]]
+        chrs = [str(x).encode() for x in phylo_forest.engine.chr_names]
+        sn = (C.c_char_p * len(names))(*names)
+        cn = (C.c_char_p * len(chrs))(*chrs)
+        sc = _lib.SamCfg(str(sam["output_dir"]).encode(), str(sam.get("filename_prefix", "chr_")).encode(),
+                         str(sam.get("template_name_prefix", "r")).encode(), int(bool(sam.get("update", False))),
+                         sn, cn)
+        check(lib().pg_simulate_seq_sam(phylo_forest._h, C.byref(c), int(seed), C.byref(sc), C.byref(h)))
     return SeqResult(h, phylo_forest)
 
 
@@ -1047,19 +1059,19 @@ def simulate_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_gen
     ``{"mutations": data frame, "parameters": dict}``.  ``insert_model``
     "normal" adds a discretised normal insert size next to the reference's
     binomial model."""
-    if write_SAM:
-        raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "SAM output is not built in this version")
     if cell_labelling is not None:
         raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "cell_labelling (FACS) is not built in this version")
     err, seq_data = _sequencer_rate(sequencer)
     s = _seed(seed)
-    res = sequence_counts(phylo_forest, s, coverage=coverage, read_size=read_size,
+    names = list(phylo_forest.forest.sample_names) + (["normal_sample"] if with_normal_sample else [])
+    sam = (dict(output_dir=output_dir, update=update_SAM, filename_prefix=filename_prefix,
+                template_name_prefix=template_name_prefix, sample_names=names) if write_SAM else None)
+    res = sequence_counts(phylo_forest, s, sam=sam, coverage=coverage, read_size=read_size,
                           insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
                           purity=purity, with_normal_sample=with_normal_sample,
                           preneoplastic_in_normal=preneoplastic_in_normal, chromosomes=chromosomes,
                           tile_size=tile_size, insert_model=insert_model)
     alt, dep = res.counts()
-    names = list(phylo_forest.forest.sample_names) + (["normal_sample"] if with_normal_sample else [])
     present = _presence(phylo_forest, len(names), with_normal_sample, preneoplastic_in_normal)
     df = _result_frame(phylo_forest, alt, dep, names, include_non_sequenced_mutations, present)
     params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
@@ -1079,14 +1091,12 @@ def simulate_normal_seq(phylo_forest: PhylogeneticForest, sequencer=None, refere
                         filename_prefix: str = "chr_", template_name_prefix: str = "r",
                         include_non_sequenced_mutations: bool = False, seed=None,
                         insert_model: str = "binomial", tile_size: int = 0) -> dict:
-    """``simulate_normal_seq`` (src/sequencing.cpp:268-282); ``write_SAM`` must be
-    FALSE in this version (its reference default is TRUE)."""
-    if write_SAM:
-        raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "SAM output is not built in this version; "
-                                    "call with write_SAM=False")
+    """``simulate_normal_seq`` (src/sequencing.cpp:268-282)."""
     err, seq_data = _sequencer_rate(sequencer)
     s = _seed(seed)
-    res = sequence_counts(phylo_forest, s, coverage=coverage, read_size=read_size,
+    sam = (dict(output_dir=output_dir, update=update_SAM, filename_prefix=filename_prefix,
+                template_name_prefix=template_name_prefix, sample_names=["normal_sample"]) if write_SAM else None)
+    res = sequence_counts(phylo_forest, s, sam=sam, coverage=coverage, read_size=read_size,
                           insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
                           purity=1.0, with_normal_sample=True, preneoplastic_in_normal=with_preneoplastic,
                           normal_only=True, chromosomes=chromosomes, tile_size=tile_size, insert_model=insert_model)
