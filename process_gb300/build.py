@@ -77,6 +77,10 @@ def build(verbose: bool = False) -> Path:
     units = {u: f for u, f in UNITS.items() if (CSRC / u).exists()}
     with cf.ThreadPoolExecutor(max_workers=min(8, len(units))) as ex:
         objs = list(ex.map(lambda kv: _compile(*kv), units.items()))
+    keep = {o.name for o in objs}
+    for old in BUILD.glob("*.o"):            # objects of earlier sources
+        if old.name not in keep:
+            old.unlink()
     lib = LIBDIR / LIBNAME
     tag = _digest(objs, "link")
     stamp = LIBDIR / f".{LIBNAME}.{tag}"
