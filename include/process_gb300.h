@@ -193,6 +193,16 @@ pg_status pg_placed_cna_copy(const pg_placed* placed, uint32_t* node, uint8_t* t
  * largest copy number of any position. */
 pg_status pg_placed_node_classes(const pg_placed* placed, uint32_t* node_class, uint32_t* n_classes,
                                  uint32_t* cn_max);
+/* Genotype classes as segments (for the allelic fragmentation getters,
+ * src/phylogenetic_forest.cpp:767-927): class c covers the absolute 0-based
+ * intervals [seg_start, seg_end) of its segments seg_off[c] .. seg_off[c+1]-1,
+ * each with the allele instances inst_list[seg_ioff .. seg_ioff + seg_icnt);
+ * inst_root gives the germline allele (0 or 1) every instance descends from.
+ * Sizes: n_classes + 1, n_segments (x4), n_list, n_instances. */
+pg_status pg_placed_class_dims(const pg_placed* placed, uint32_t* n_classes, uint32_t* n_segments, uint32_t* n_list,
+                               uint32_t* n_instances);
+pg_status pg_placed_class_copy(const pg_placed* placed, uint32_t* seg_off, uint32_t* seg_start, uint32_t* seg_end,
+                               uint32_t* seg_ioff, uint32_t* seg_icnt, uint16_t* inst_list, uint8_t* inst_root);
 /* Device time of the placement kernels of the last place call (ms). */
 pg_status pg_placed_kernel_ms(const pg_placed* placed, float* ms);
 

@@ -65,6 +65,8 @@ def lib() -> C.CDLL:
             "orc_placed_cna_count": (C.c_uint64, [P]),
             "orc_placed_cna_copy": (None, [P, u32p, u8p, u32p, u32p, u32p, u32p, u32p, u8p]),
             "orc_placed_node_classes": (None, [P, u32p, u32p, u32p]),
+            "orc_placed_class_pieces": (C.c_uint64, [P, C.c_uint32, u32p, u32p, u32p]),
+            "orc_placed_inst_roots": (C.c_uint32, [P, u8p]),
             "orc_place": (P, [P, C.c_uint32, i32p, f64p, u32p, i32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32,
                               C.c_uint32, C.c_uint32, C.c_uint64, C.c_int]),
             "orc_placed_destroy": (None, [P]),
@@ -275,6 +277,18 @@ class OraclePlaced:
         nc, cm = C.c_uint32(), C.c_uint32()
         lib().orc_placed_node_classes(self._h, _p(out, C.c_uint32), C.byref(nc), C.byref(cm))
         return out, nc.value, cm.value
+
+    def class_pieces(self, c):
+        n = lib().orc_placed_class_pieces(self._h, c, None, None, None)
+        inst, b, e = (np.empty(n, dtype=np.uint32) for _ in range(3))
+        lib().orc_placed_class_pieces(self._h, c, _p(inst, C.c_uint32), _p(b, C.c_uint32), _p(e, C.c_uint32))
+        return inst, b, e
+
+    def inst_roots(self):
+        n = lib().orc_placed_inst_roots(self._h, None)
+        r = np.empty(n, dtype=np.uint8)
+        lib().orc_placed_inst_roots(self._h, _p(r, C.c_uint8))
+        return r
 
     def set_table(self, t: dict):
         arrs = [np.ascontiguousarray(t[k], dtype=d) for k, d in

@@ -1636,6 +1636,29 @@ void orc_placed_cna_copy(void* pp, uint32_t* node, uint8_t* type, uint32_t* chr,
     allele[i] = c[i].allele; src[i] = c[i].src; driver[i] = c[i].driver;
   }
 }
+// pieces (instance, [b, e)) of class c, and the germline allele of every instance
+uint64_t orc_placed_class_pieces(void* pp, uint32_t c, uint32_t* inst, uint32_t* b, uint32_t* e) {
+  auto* p = static_cast<Placed*>(pp);
+  uint64_t n = 0;
+  for (const auto& kv : p->classes[c])
+    for (auto [x, y] : kv.second) {
+      if (inst) { inst[n] = kv.first; b[n] = x; e[n] = y; }
+      ++n;
+    }
+  return n;
+}
+uint32_t orc_placed_inst_roots(void* pp, uint8_t* root) {
+  auto* p = static_cast<Placed*>(pp);
+  std::vector<uint32_t> from(p->n_inst);
+  for (uint32_t y = 0; y < p->n_inst; ++y) from[y] = y;
+  for (const CopyRec& c : p->copies) from[c.made] = c.from;
+  for (uint32_t y = 0; y < p->n_inst && root; ++y) {
+    uint32_t r = y;
+    while (from[r] != r) r = from[r];
+    root[y] = uint8_t(r);
+  }
+  return p->n_inst;
+}
 // node classes (n nodes), number of classes, largest copy number
 void orc_placed_node_classes(void* pp, uint32_t* node_class, uint32_t* n_classes, uint32_t* cn_max) {
   auto* p = static_cast<Placed*>(pp);

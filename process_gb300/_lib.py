@@ -95,6 +95,8 @@ _PROTOS = {
     "pg_placed_cna_count": (C.c_int, [P, u64p]),
     "pg_placed_cna_copy": (C.c_int, [P, u32p, u8p, u32p, u32p, u32p, u32p, u32p, u8p]),
     "pg_placed_node_classes": (C.c_int, [P, u32p, u32p, u32p]),
+    "pg_placed_class_dims": (C.c_int, [P, u32p, u32p, u32p, u32p]),
+    "pg_placed_class_copy": (C.c_int, [P, u32p, u32p, u32p, u32p, u32p, C.POINTER(C.c_uint16), u8p]),
     "pg_engine_add_passenger_cna": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
     "pg_engine_set_avoid_homozygous_losses": (C.c_int, [P, C.c_int]),
     "pg_placed_kernel_ms": (C.c_int, [P, f32p]),

@@ -273,6 +273,10 @@ struct pg_placed {
   // instances are constant; per (atom, class) the covering instances as
   // (offset into inst_list, count)
   std::vector<uint32_t> atom_start_h, atom_icnt_h;
+  // host copy of the class segments and each instance's germline allele
+  std::vector<uint32_t> seg_off_h, seg_start_h, seg_end_h, seg_ioff_h, seg_icnt_h;
+  std::vector<uint16_t> inst_list_h;
+  std::vector<uint8_t> inst_root_h;
   DBuf<uint32_t> atom_start, atom_ioff, atom_icnt;
   DBuf<uint32_t> node_class, seg_off, seg_start, seg_end, seg_ioff, seg_icnt, chain_off;
   DBuf<uint16_t> inst_list, chain_anc;
@@ -997,6 +1001,14 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
       chain_off.push_back(uint32_t(chain_anc.size()));
     }
     pl->has_cna = classes.size() > 1 || insts.size() > 2;
+    pl->seg_off_h = seg_off; pl->seg_start_h = seg_start; pl->seg_end_h = seg_end;
+    pl->seg_ioff_h = seg_ioff; pl->seg_icnt_h = seg_icnt; pl->inst_list_h = inst_list;
+    pl->inst_root_h.resize(insts.size());
+    for (size_t y = 0; y < insts.size(); ++y) {
+      int32_t r = int32_t(y);
+      while (insts[r].parent >= 0) r = insts[r].parent;
+      pl->inst_root_h[y] = uint8_t(r);
+    }
     pl->cn_max = std::max<uint32_t>(cn_max, 2);
     pl->n_classes = uint32_t(classes.size());
     pl->node_class_h = node_class;
@@ -1170,6 +1182,28 @@ pg_status pg_placed_cna_copy(const pg_placed* p, uint32_t* node, uint8_t* type, 
       if (src_allele) src_allele[i] = c.src;
       if (driver) driver[i] = c.driver;
     }
+  });
+}
+
+pg_status pg_placed_class_dims(const pg_placed* p, uint32_t* n_classes, uint32_t* n_segments, uint32_t* n_list,
+                               uint32_t* n_instances) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    if (n_classes) *n_classes = p->n_classes;
+    if (n_segments) *n_segments = uint32_t(p->seg_start_h.size());
+    if (n_list) *n_list = uint32_t(p->inst_list_h.size());
+    if (n_instances) *n_instances = uint32_t(p->inst_root_h.size());
+  });
+}
+
+pg_status pg_placed_class_copy(const pg_placed* p, uint32_t* seg_off, uint32_t* seg_start, uint32_t* seg_end,
+                               uint32_t* seg_ioff, uint32_t* seg_icnt, uint16_t* inst_list, uint8_t* inst_root) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    auto cp = [](auto* dst, const auto& v) { if (dst) std::copy(v.begin(), v.end(), dst); };
+    cp(seg_off, p->seg_off_h); cp(seg_start, p->seg_start_h); cp(seg_end, p->seg_end_h);
+    cp(seg_ioff, p->seg_ioff_h); cp(seg_icnt, p->seg_icnt_h); cp(inst_list, p->inst_list_h);
+    cp(inst_root, p->inst_root_h);
   });
 }
 

@@ -743,11 +743,134 @@ class PhylogeneticForest:
             cols["class"].append(np.where(c["driver"][m] == 1, "driver", "passenger"))
         return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
 
+    # -- copy-number getters (allelic fragmentation) ------------------------------------
+    def _classes(self) -> dict:
+        """Genotype classes as segments with each instance's germline allele."""
+        if getattr(self, "_cls_cache", None) is None:
+            nc, ns, nl, ni = (C.c_uint32() for _ in range(4))
+            check(lib().pg_placed_class_dims(self._h, C.byref(nc), C.byref(ns), C.byref(nl), C.byref(ni)))
+            d = {"seg_off": np.empty(nc.value + 1, np.uint32), "start": np.empty(ns.value, np.uint32),
+                 "end": np.empty(ns.value, np.uint32), "ioff": np.empty(ns.value, np.uint32),
+                 "icnt": np.empty(ns.value, np.uint32), "list": np.empty(max(nl.value, 1), np.uint16),
+                 "root": np.empty(max(ni.value, 1), np.uint8)}
+            check(lib().pg_placed_class_copy(self._h, ptr(d["seg_off"], C.c_uint32), ptr(d["start"], C.c_uint32),
+                                             ptr(d["end"], C.c_uint32), ptr(d["ioff"], C.c_uint32),
+                                             ptr(d["icnt"], C.c_uint32), ptr(d["list"], C.c_uint16),
+                                             ptr(d["root"], C.c_uint8)))
+            # copies of germline allele 1 per segment (the rest descend from allele 0)
+            roots = d["root"][d["list"][:max(nl.value, 1)]].astype(np.int64)
+            csum = np.concatenate([[0], np.cumsum(roots)])
+            d["a1"] = (csum[d["ioff"] + d["icnt"]] - csum[d["ioff"]]).astype(np.int64)
+            d["a0"] = d["icnt"].astype(np.int64) - d["a1"]
+            d["n_classes"] = nc.value
+            self._cls_cache = d
+        return self._cls_cache
+
+    def _class_fragments(self, c: int) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+        """(absolute begin, end (half-open), copies of allele 0, of allele 1) of
+        the maximal stretches of class c with one allelic type, chromosome by
+        chromosome (uncovered stretches have type (0, 0))."""
+        d = self._classes()
+        lo, hi = int(d["seg_off"][c]), int(d["seg_off"][c + 1])
+        st, en = d["start"][lo:hi].astype(np.int64), d["end"][lo:hi].astype(np.int64)
+        off = self.engine.chr_off.astype(np.int64)
+        cuts = np.unique(np.concatenate([off, st, en]))
+        b, e = cuts[:-1], cuts[1:]
+        k = np.searchsorted(st, b, side="right") - 1
+        inside = (k >= 0) & (b < en[np.maximum(k, 0)])
+        a0 = np.where(inside, d["a0"][lo:hi][np.maximum(k, 0)] if hi > lo else 0, 0)
+        a1 = np.where(inside, d["a1"][lo:hi][np.maximum(k, 0)] if hi > lo else 0, 0)
+        chrom = np.searchsorted(off, b, side="right") - 1
+        new = np.r_[True, (chrom[1:] != chrom[:-1]) | (a0[1:] != a0[:-1]) | (a1[1:] != a1[:-1])]
+        first = np.nonzero(new)[0]
+        last = np.r_[first[1:], len(b)] - 1
+        return b[first], e[last], a0[first], a1[first]
+
+    def _frag_rows(self, b, e, a0, a1):
+        off = self.engine.chr_off.astype(np.int64)
+        ci = np.searchsorted(off, b, side="right") - 1
+        names = np.array(self.engine.chr_names, dtype=object)[ci]
+        return names, b - off[ci] + 1, e - off[ci], np.maximum(a0, a1), np.minimum(a0, a1)
+
+    def get_cell_allelic_fragmentation(self) -> dict:
+        """Columns cell_id, chr, begin, end, major, minor: every sampled cell's
+        genome cut into stretches of one allelic type (copies of the two
+        germline alleles; major = the larger), src/phylogenetic_forest.cpp:867-927."""
+        f = self.forest
+        cls, _, _ = self.node_classes()
+        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
+        per = {}
+        cols = {k: [] for k in ("cell_id", "chr", "begin", "end", "major", "minor")}
+        for lf in leaves:
+            c = int(cls[lf])
+            if c not in per:
+                per[c] = self._frag_rows(*self._class_fragments(c))
+            names, b, e, mj, mn = per[c]
+            cols["cell_id"].append(np.full(len(b), f.cell_id[lf]))
+            cols["chr"].append(names); cols["begin"].append(b); cols["end"].append(e)
+            cols["major"].append(mj); cols["minor"].append(mn)
+        return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
+
+    def get_bulk_allelic_fragmentation(self, sample_name: str | None = None) -> dict:
+        """Columns chr, begin, end, major, minor, ratio: for every stretch of
+        the genome on which the sampled cells (of one sample, or all) keep
+        their allelic types, each type with the fraction of cells showing it
+        (src/phylogenetic_forest.cpp:767-820)."""
+        f = self.forest
+        cls, _, _ = self.node_classes()
+        sel = f.is_leaf & (f.sample >= 0)
+        if sample_name is not None:
+            if sample_name not in f.sample_names:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f'Unknown sample "{sample_name}".')
+            sel &= f.sample == f.sample_names.index(sample_name)
+        leaf_cls, counts = np.unique(cls[sel], return_counts=True)
+        n_cells = float(counts.sum())
+        frags = [self._class_fragments(int(c)) for c in leaf_cls]
+        cuts = np.unique(np.concatenate([fr[0] for fr in frags] + [fr[1] for fr in frags]))
+        b, e = cuts[:-1], cuts[1:]
+        keep = np.ones(len(b), dtype=bool)
+        types = []
+        for (fb, fe, f0, f1) in frags:
+            k = np.searchsorted(fb, b, side="right") - 1
+            types.append((f0[k], f1[k]))
+        # merge neighbouring stretches with the same type in every class and chromosome
+        off = self.engine.chr_off.astype(np.int64)
+        chrom = np.searchsorted(off, b, side="right") - 1
+        same = np.ones(len(b) - 1, dtype=bool) if len(b) > 1 else np.zeros(0, dtype=bool)
+        for t0, t1 in types:
+            same &= (t0[1:] == t0[:-1]) & (t1[1:] == t1[:-1])
+        same &= chrom[1:] == chrom[:-1]
+        start = np.r_[True, ~same]
+        first = np.nonzero(start)[0]
+        last = np.r_[first[1:], len(b)] - 1
+        cols = {k: [] for k in ("chr", "begin", "end", "major", "minor", "ratio")}
+        for i0, i1 in zip(first, last):
+            agg = {}
+            for (t0, t1), n in zip(types, counts):
+                key = (int(t0[i0]), int(t1[i0]))
+                agg[key] = agg.get(key, 0) + int(n)
+            names, bb, ee, _, _ = self._frag_rows(np.array([b[i0]]), np.array([e[i1]]), np.zeros(1), np.zeros(1))
+            for (x0, x1), n in sorted(agg.items()):
+                cols["chr"].append(names[0]); cols["begin"].append(int(bb[0])); cols["end"].append(int(ee[0]))
+                cols["major"].append(max(x0, x1)); cols["minor"].append(min(x0, x1)); cols["ratio"].append(n / n_cells)
+        return {k: np.array(v, dtype=object if k == "chr" else None) for k, v in cols.items()}
+
     def get_samples_info(self) -> dict:
-        """name, tumour_cells, DNA_quantity, equivalent_normal_cells (src/phylogenetic_forest.cpp:57-99)."""
+        """name, tumour_cells, DNA_quantity, equivalent_normal_cells
+        (src/phylogenetic_forest.cpp:57-99): the DNA of a sample is the summed
+        allelic size of its sampled cells' genomes."""
         info = self.forest.get_samples_info()
         normal_dna = 2.0 * self.engine.genome.total
-        dna = info["tumour_cells"].astype(np.float64) * normal_dna
+        f = self.forest
+        d = self._classes()
+        size = np.zeros(d["n_classes"], dtype=np.float64)
+        seg_cls = np.repeat(np.arange(d["n_classes"]), np.diff(d["seg_off"].astype(np.int64)))
+        np.add.at(size, seg_cls, (d["end"].astype(np.float64) - d["start"]) * d["icnt"])
+        cls, _, _ = self.node_classes()
+        dna = np.zeros(len(info["name"]), dtype=np.float64)
+        for i, name in enumerate(info["name"]):
+            j = f.sample_names.index(name)
+            dna[i] = size[cls[f.is_leaf & (f.sample == j)]].sum()
         info["DNA_quantity"] = dna
         info["equivalent_normal_cells"] = dna / normal_dna
         return info

@@ -113,3 +113,51 @@ def test_wgd_order_vaf_gpu(gpu_lib, orc):
                                    error_rate=0.0, purity=1.0, with_normal_sample=False).counts()
         vafs.append(alt[0, d] / dep[0, d])
     assert abs(vafs[0] - 0.5) < 0.09 and abs(vafs[1] - 0.25) < 0.09
+
+
+def _oracle_fragments(op, c, chr_off, roots):
+    """Allelic-type stretches of oracle class c (an independent restatement)."""
+    inst, b, e = op.class_pieces(c)
+    cuts = np.unique(np.concatenate([chr_off, b, e]).astype(np.int64))
+    rows = []
+    for lo, hi in zip(cuts[:-1], cuts[1:]):
+        cover = (b <= lo) & (lo < e)
+        r = roots[inst[cover]]
+        t = (int((r == 0).sum()), int((r == 1).sum()))
+        ch = int(np.searchsorted(chr_off, lo, side="right") - 1)
+        if rows and rows[-1][0] == ch and rows[-1][3] == t and rows[-1][2] == lo:
+            rows[-1][2] = hi
+        else:
+            rows.append([ch, lo, hi, t])
+    return [(ch, lo - chr_off[ch] + 1, hi - chr_off[ch], max(t), min(t)) for ch, lo, hi, t in rows]
+
+
+def test_allelic_fragmentation_getters(gpu_lib, orc):
+    w, cands = _workload(seed=6, n_leaves=200)
+    eng, o = _pair(orc, w, cands, True, True)
+    f = w.forest
+    pf = eng.place_mutations(f, 50, 5, seed=8)
+    op = o.place(f, _species(o, f), 50, 0, 5, 0, seed=8)
+    chr_off = eng.chr_off.astype(np.int64)
+    roots = op.inst_roots()
+    cls, n_cls, _ = pf.node_classes()
+    cell = pf.get_cell_allelic_fragmentation()
+    leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
+    assert len(np.unique(cell["cell_id"])) == len(leaves)
+    for lf in leaves[:: max(1, len(leaves) // 25)]:
+        m = cell["cell_id"] == f.cell_id[lf]
+        got = [(eng.chr_names.index(c), int(b), int(e), int(mj), int(mn))
+               for c, b, e, mj, mn in zip(cell["chr"][m], cell["begin"][m], cell["end"][m], cell["major"][m],
+                                          cell["minor"][m])]
+        assert got == _oracle_fragments(op, int(cls[lf]), chr_off, roots)
+    bulk = pf.get_bulk_allelic_fragmentation()
+    # every stretch's ratios sum to 1 and the stretches tile every chromosome
+    keys = list(zip(bulk["chr"], bulk["begin"], bulk["end"]))
+    for k in set(keys):
+        assert abs(sum(r for kk, r in zip(keys, bulk["ratio"]) if kk == k) - 1.0) < 1e-12
+    for ci, name in enumerate(eng.chr_names):
+        spans = sorted({(b, e) for c, b, e in keys if c == name})
+        assert spans[0][0] == 1 and spans[-1][1] == eng.chr_lengths[ci]
+        assert all(spans[i][1] + 1 == spans[i + 1][0] for i in range(len(spans) - 1))
+    info = pf.get_samples_info()
+    assert np.all(info["DNA_quantity"] > 0) and np.any(info["equivalent_normal_cells"] != info["tumour_cells"])
