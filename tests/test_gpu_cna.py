@@ -161,3 +161,44 @@ def test_allelic_fragmentation_getters(gpu_lib, orc):
         assert all(spans[i][1] + 1 == spans[i + 1][0] for i in range(len(spans) - 1))
     info = pf.get_samples_info()
     assert np.all(info["DNA_quantity"] > 0) and np.any(info["equivalent_normal_cells"] != info["tumour_cells"])
+
+
+def test_cna_distribution_against_reference_engine(gpu_lib, orc):
+    """Copy-number events, 48 seeds: the GPU path against the std::mt19937_64
+    flavour (which replays the events with sequential draws and draws reads by
+    rejection over whole chromosomes): chi-square on SBS contexts, KS on
+    per-edge passenger counts, on VAF and on depth; p > 0.01."""
+    from scipy import stats
+
+    from process_gb300.engine import seq_cfg, sequence_counts
+    w, cands = _workload(seed=12, n_leaves=150, cna_rate=5e-9)
+    eng, o = _pair(orc, w, cands, True, True)
+    f = w.forest
+    sp = _species(o, f)
+    n = f.num_of_nodes
+    cfg = dict(coverage=40, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3,
+               purity=0.8, with_normal_sample=False)
+    c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=4096, **cfg)
+    g_ctx, m_ctx = np.zeros(96), np.zeros(96)
+    g_edge, m_edge, g_vaf, m_vaf, g_dep, m_dep = [], [], [], [], [], []
+    for s in range(48):
+        pf = eng.place_mutations(f, 40, 4, seed=3000 + s)
+        t = pf.table()
+        op = o.place(f, sp, 40, 0, 4, 0, seed=3000 + s, flavour=1)
+        ot = op.table()
+        for tab, ctx, edges in ((t, g_ctx, g_edge), (ot, m_ctx, m_edge)):
+            snv = (tab["kind"] == 0) & (tab["nature"] == 0)
+            ctx += np.bincount(tab["cls"][snv], minlength=96)
+            edges.append(np.bincount(tab["edge"][snv], minlength=n)[:n])
+        if s < 16:
+            alt, dep = sequence_counts(pf, 700 + s, tile_size=4096, **cfg).counts()
+            oalt, odep, _ = op.sequence(c, 700 + s, flavour=1)
+            for a, d, vafs, deps, tab in ((alt, dep, g_vaf, g_dep, t), (oalt, odep, m_vaf, m_dep, ot)):
+                keep = d[0] >= 10
+                vafs.append(a[0][keep] / d[0][keep])
+                deps.append(d[0])
+    keep = (g_ctx + m_ctx) > 0
+    assert stats.chi2_contingency(np.vstack([g_ctx[keep], m_ctx[keep]]))[1] > 0.01
+    assert stats.ks_2samp(np.concatenate(g_edge), np.concatenate(m_edge)).pvalue > 0.01
+    assert stats.ks_2samp(np.concatenate(g_vaf), np.concatenate(m_vaf)).pvalue > 0.01
+    assert stats.ks_2samp(np.concatenate(g_dep), np.concatenate(m_dep)).pvalue > 0.01
