@@ -325,6 +325,8 @@ class MutationEngine:
         self.species: dict[tuple[str, str], int] = {}
         self.species_rates: dict[tuple[str, str], dict] = {}
         self._exposures: list[tuple[float, dict]] = []
+        self._sigs: list[dict] = [{}, {}]
+        self._mutant_specs: list[tuple[str, dict, list]] = []   # add_mutant calls, in order
         self.passenger_CNAs: list[CNA] = []
         self.avoid_homozygous_losses = bool(avoid_homozygous_losses)
         if SBS_signatures:
@@ -373,6 +375,7 @@ class MutationEngine:
             raise DomainError(_lib.PG_ERR_DOMAIN, f"signatures must have {nc} classes")
         check(lib().pg_engine_set_signatures(self._h, type_, len(names), ptr(mat, C.c_double)))
         self.sig_names[type_] = names
+        self._sigs[type_] = {k: mat[i].tolist() for i, k in enumerate(names)}
 
     def add_exposure(self, time: float = 0.0, coefficients: Mapping[str, float] | None = None) -> None:
         """``add_exposure(time, coefficients)`` (src/mutation_engine.cpp:734-739): one
@@ -413,6 +416,7 @@ class MutationEngine:
         ``passenger_rates`` is ``{"SNV": r, "indel": r, "CNA": r}`` or
         ``{"+": {...}, "-": {...}}``; a rate may be a sequence giving one value
         per exposure epoch."""
+        drivers = list(drivers)
         if mutant_name in self.mutants:
             raise DomainError(_lib.PG_ERR_DOMAIN, f"mutant {mutant_name} already declared")
         mut_id = len(self.mutants)
@@ -460,6 +464,7 @@ class MutationEngine:
                 check(lib().pg_engine_add_driver_wgd(self._h, mut_id))
             else:
                 raise DomainError(_lib.PG_ERR_DOMAIN, "unsupported driver mutation specification")
+        self._mutant_specs.append((mutant_name, passenger_rates, drivers))
 
     def get_species_rates(self) -> dict:
         rows = list(self.species_rates.items())
@@ -566,7 +571,12 @@ class MutationEngine:
                                            int(num_of_preneoplatic_indels), pre_i, s, C.byref(ph)))
         finally:
             lib().pg_forest_destroy(fh)
-        return PhylogeneticForest(self, f, ph, s)
+        pf = PhylogeneticForest(self, f, ph, s)
+        pf._place_args = dict(num_of_preneoplatic_SNVs=int(num_of_preneoplatic_SNVs),
+                              num_of_preneoplatic_indels=int(num_of_preneoplatic_indels), seed=s,
+                              preneoplatic_SNV_signature_name=preneoplatic_SNV_signature_name,
+                              preneoplatic_indel_signature_name=preneoplatic_indel_signature_name)
+        return pf
 
 
 class PhylogeneticForest:
@@ -875,8 +885,131 @@ class PhylogeneticForest:
         info["equivalent_normal_cells"] = dna / normal_dna
         return info
 
+    def save(self, filename: str, quiet: bool = False) -> None:
+        """``PhylogeneticForest$save(filename, quiet)``; see :func:`save_phylogenetic_forest`."""
+        save_phylogenetic_forest(self, filename)
+
     def get_germline_mutations(self) -> dict:
         return {k: np.array([]) for k in ("chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
+
+
+# ---------------------------------------------------------------- save / load
+FOREST_FORMAT = "process_gb300.phylogenetic_forest"
+FOREST_VERSION = 1
+
+
+def _plain(x):
+    """JSON-ready copy of rates, exposures and driver specifications."""
+    if isinstance(x, dict):
+        return {str(k): _plain(v) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_plain(v) for v in x]
+    if isinstance(x, np.ndarray):
+        return x.tolist()
+    if isinstance(x, np.generic):
+        return x.item()
+    if isinstance(x, Mutation):
+        return {"kind": "SID", "chr": x.chr, "chr_pos": int(x.chr_pos), "ref": x.ref, "alt": x.alt,
+                "allele": x.allele}
+    if isinstance(x, CNA):
+        return {"kind": "CNA", "type": x.type, "chr": x.chr, "chr_pos": int(x.chr_pos), "len": int(x.len),
+                "allele": x.allele, "src_allele": x.src_allele}
+    if x is WGD:
+        return {"kind": "WGD"}
+    return x
+
+
+def _driver(d):
+    if d["kind"] == "SID":
+        return Mutation(d["chr"], d["chr_pos"], d["ref"], d["alt"], d["allele"])
+    if d["kind"] == "CNA":
+        return CNA(d["type"], d["chr"], d["chr_pos"], d["len"], d["allele"], d["src_allele"])
+    return WGD
+
+
+def _table_digest(t: dict) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for k in ("locus", "edge", "aux", "cls", "sig", "allele", "kind", "nature"):
+        h.update(np.ascontiguousarray(t[k]).tobytes())
+    return h.hexdigest()
+
+
+def save_phylogenetic_forest(pf: "PhylogeneticForest", filename: str) -> None:
+    """``PhylogeneticForest$save`` (src/phylogenetic_forest.cpp:940-955).  The
+    RACES binary archive layout is unavailable, so the file is a versioned
+    native archive (numpy .npz): the engine's configuration, the samples
+    forest, the placement call and a digest of the placed mutations.  Loading
+    places again (placement is a function of these inputs) and checks the
+    digest."""
+    import json
+    e, f = pf.engine, pf.forest
+    args = getattr(pf, "_place_args", None)
+    if args is None:
+        raise DomainError(_lib.PG_ERR_DOMAIN, "this phylogenetic forest was not made by place_mutations")
+    meta = {
+        "format": FOREST_FORMAT, "version": FOREST_VERSION,
+        "genome": {"chr_names": list(e.chr_names), "chr_lengths": [int(x) for x in e.chr_lengths],
+                   "seed": int(e.genome.seed), "gc": float(e.genome.gc), "bases": e.genome.bases is not None},
+        "engine": {"context_sampling": e.context_sampling, "max_motif_size": e.max_motif_size,
+                   "max_repetition_storage": e.max_repetition_storage,
+                   "avoid_homozygous_losses": e.avoid_homozygous_losses,
+                   "infinite_sites_model": e.infinite_sites_model,
+                   "SBS_signatures": _plain(e._sigs[0]), "indel_signatures": _plain(e._sigs[1]),
+                   "exposures": _plain(e._exposures), "mutants": _plain(e._mutant_specs),
+                   "passenger_CNAs": _plain(e.passenger_CNAs)},
+        "place": _plain(args),
+        "digest": _table_digest(pf.table()),
+    }
+    ancestor = np.where(f.parent >= 0, f.cell_id[np.maximum(f.parent, 0)], -1)
+    sample = np.array([f.sample_names[s] if s >= 0 else "" for s in f.sample], dtype=object)
+    arrays = {"meta": np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8),
+              "cell_id": f.cell_id, "ancestor": ancestor, "mutant": f.mutant.astype(str),
+              "epistate": np.array(["" if x is None else str(x) for x in f.epistate]),
+              "sample": sample.astype(str), "birth_time": f.birth_time, "divisions": f.divisions}
+    if e.genome.bases is not None:
+        arrays["bases"] = np.asarray(e.genome.bases, dtype=np.uint8)
+    with open(filename, "wb") as fh:
+        np.savez_compressed(fh, **arrays)
+
+
+def load_phylogenetic_forest(filename: str, quiet: bool = False) -> "PhylogeneticForest":
+    """``load_phylogenetic_forest(filename, quiet)`` (src/mutations.cpp:1466-1480):
+    rebuilds the engine and the samples forest of a saved file, places the
+    mutations again and checks them against the saved digest."""
+    import json
+    import os
+    if not os.path.exists(filename):
+        raise DomainError(_lib.PG_ERR_DOMAIN, f'The file "{filename}" does not exist.')
+    if not os.path.isfile(filename):
+        raise DomainError(_lib.PG_ERR_DOMAIN, f'The file "{filename}" is not a regular file.')
+    with np.load(filename, allow_pickle=False) as z:
+        meta = json.loads(bytes(z["meta"]).decode())
+        if meta.get("format") != FOREST_FORMAT:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f'"{filename}" is not a phylogenetic forest file')
+        if meta.get("version") != FOREST_VERSION:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f'"{filename}" has format version {meta.get("version")}, '
+                              f"this library reads version {FOREST_VERSION}")
+        g = meta["genome"]
+        genome = GenomeSpec(g["chr_names"], g["chr_lengths"], z["bases"] if g["bases"] else None, g["seed"], g["gc"])
+        em = meta["engine"]
+        eng = MutationEngine(genome, em["SBS_signatures"], em["indel_signatures"],
+                             context_sampling=em["context_sampling"], max_motif_size=em["max_motif_size"],
+                             max_repetition_storage=em["max_repetition_storage"],
+                             avoid_homozygous_losses=em["avoid_homozygous_losses"],
+                             passenger_CNAs=[_driver(c) for c in em["passenger_CNAs"]])
+        for name, rates, drivers in em["mutants"]:
+            eng.add_mutant(name, rates, [_driver(d) for d in drivers])
+        for t, coeffs in em["exposures"]:
+            eng.add_exposure(t, coeffs)
+        eng.infinite_sites_model = em["infinite_sites_model"]
+        sample = np.array([s if s != "" else None for s in z["sample"]], dtype=object)
+        forest = SamplesForest(z["cell_id"], z["ancestor"], z["mutant"].astype(object),
+                               z["epistate"].astype(object), sample, z["birth_time"], z["divisions"])
+    pf = eng.place_mutations(forest, **meta["place"])
+    if _table_digest(pf.table()) != meta["digest"]:
+        raise _lib.ProcessError(_lib.PG_ERR_RUNTIME, f'"{filename}": the placed mutations differ from the saved ones')
+    return pf
 
 
 # ---------------------------------------------------------------- batches

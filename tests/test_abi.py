@@ -101,3 +101,24 @@ def test_synthetic_workloads_shapes():
     w2 = synth.config2(seed=3, n_leaves_per_sample=50, genome_scale=1e-3)
     assert len(w2.genome.chr_lengths) == 24 and len(w2.exposures) == 3
     assert sorted(set(w2.forest.sample_names)) == ["S_1", "S_2", "S_3"]
+
+
+def test_load_phylogenetic_forest_errors(tmp_path):
+    """File checks of load_phylogenetic_forest happen before any device work."""
+    import numpy as np
+    from process_gb300 import DomainError, load_phylogenetic_forest
+    with pytest.raises(DomainError, match="does not exist"):
+        load_phylogenetic_forest(str(tmp_path / "missing.sff"))
+    with pytest.raises(DomainError, match="not a regular file"):
+        load_phylogenetic_forest(str(tmp_path))
+    bad = tmp_path / "bad.sff"
+    with open(bad, "wb") as fh:
+        np.savez(fh, meta=np.frombuffer(b'{"format": "other", "version": 1}', dtype=np.uint8))
+    with pytest.raises(DomainError, match="not a phylogenetic forest"):
+        load_phylogenetic_forest(str(bad))
+    newer = tmp_path / "newer.sff"
+    with open(newer, "wb") as fh:
+        np.savez(fh, meta=np.frombuffer(b'{"format": "process_gb300.phylogenetic_forest", "version": 99}',
+                                        dtype=np.uint8))
+    with pytest.raises(DomainError, match="format version 99"):
+        load_phylogenetic_forest(str(newer))

@@ -1,0 +1,37 @@
+"""PhylogeneticForest save / load (versioned native archive): a loaded forest
+places the same mutations (digest-checked) and sequences identically."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_save_load_round_trip(gpu_lib, tmp_path):
+    from process_gb300 import CNA, SNV, WGD, load_phylogenetic_forest, synth
+    from process_gb300.engine import sequence_counts
+    w = synth.config1(seed=4, n_leaves=150)
+    w.genome.chr_lengths = [200_000, 100_000, 100_000]
+    (na, ra, _), (nb, rb, _) = w.mutants
+    w.mutants = [(na, dict(ra, CNA=1e-8), [SNV("1", 5000, "T"), CNA("A", "2", 10_001, 20_000)]),
+                 (nb, rb, [WGD])]
+    eng = synth.build_engine(w)
+    eng.add_passenger_CNAs([CNA("D", "3", 1001, 5000)])
+    eng.infinite_sites_model = False
+    pf = eng.place_mutations(w.forest, 20, 3, seed=11)
+    path = tmp_path / "phylo_forest.sff"
+    pf.save(str(path))
+    pf2 = load_phylogenetic_forest(str(path))
+    for k, v in pf.table().items():
+        np.testing.assert_array_equal(pf2.table()[k], v, err_msg=k)
+    np.testing.assert_array_equal(pf2.forest.parent, pf.forest.parent)
+    np.testing.assert_array_equal(pf2.forest.cell_id, pf.forest.cell_id)
+    assert pf2.forest.sample_names == pf.forest.sample_names
+    assert not pf2.engine.infinite_sites_model
+    cfg = dict(coverage=10, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3)
+    a1, d1 = sequence_counts(pf, 5, **cfg).counts()
+    a2, d2 = sequence_counts(pf2, 5, **cfg).counts()
+    np.testing.assert_array_equal(a1, a2)
+    np.testing.assert_array_equal(d1, d2)
+    c1, c2 = pf.cna_table(), pf2.cna_table()
+    for k in c1:
+        np.testing.assert_array_equal(c1[k], c2[k], err_msg=k)
