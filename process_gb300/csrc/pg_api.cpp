@@ -1105,28 +1105,62 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
       const uint32_t* pending = nullptr;
       uint32_t n_pend = uint32_t(n_snv + n_id);
       uint32_t* next = pend_a.p;
+      // Rounds with many pending slots read their count on the host; below
+      // ROUND_TAIL pending slots, groups of ROUND_GROUP rounds run with the
+      // counts in device memory (the grids sized by the group's first count,
+      // which later rounds never exceed), with one host read per group.
+      constexpr uint32_t ROUND_TAIL = 1u << 20;
+      constexpr int ROUND_GROUP = 16;
+      DBuf<uint32_t> counts(P, ROUND_GROUP);
       int round = 0;
       while (n_pend > 0) {
         require(round < 256, unique ? "infinite sites model: no free locus left for some mutations"
                                     : "no allele left where some mutations were drawn");
-        ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-        if (unique) {
-          ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-          ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-          pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
-                          n_next.p, err.p, st);
-        } else {
-          pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_next.p, st);
+        if (n_pend > ROUND_TAIL) {
+          ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
+          if (unique) {
+            ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+            ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+            pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
+                            n_next.p, err.p, st);
+          } else {
+            pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_next.p, st);
+          }
+          uint32_t nn = 0;
+          ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+          ck(cudaStreamSynchronize(st), "redraw round");
+          if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next,
+                                             nn, 1, err.p, st);
+          pending = next;
+          next = (next == pend_a.p) ? pend_b.p : pend_a.p;
+          n_pend = nn;
+          ++round;
+          continue;
+        }
+        uint32_t ctail = 1024;                 // candidate table of the group, in the full table's buffers
+        while (ctail < 2 * n_pend) ctail <<= 1;
+        ck(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * ROUND_GROUP, st), "memset");
+        for (int g = 0; g < ROUND_GROUP; ++g) {
+          const uint32_t* n_dev = g == 0 ? nullptr : counts.p + g - 1;
+          uint32_t* n_out = counts.p + g;
+          if (unique) {
+            ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
+            ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
+            pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, ctail - 1, lost.p, next,
+                            n_out, err.p, st, n_dev);
+          } else {
+            pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_out, st, n_dev);
+          }
+          pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, n_pend,
+                                     1, err.p, st, n_out);
+          pending = next;
+          next = (next == pend_a.p) ? pend_b.p : pend_a.p;
         }
         uint32_t nn = 0;
-        ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-        ck(cudaStreamSynchronize(st), "redraw round");
-        if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, nn,
-                                           1, err.p, st);
-        pending = next;
-        next = (next == pend_a.p) ? pend_b.p : pend_a.p;
+        ck(cudaMemcpyAsync(&nn, counts.p + ROUND_GROUP - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+        ck(cudaStreamSynchronize(st), "redraw rounds");
         n_pend = nn;
-        ++round;
+        round += ROUND_GROUP;
       }
     }
     // ---- sort by locus

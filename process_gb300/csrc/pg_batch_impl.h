@@ -153,21 +153,50 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
     const uint32_t* pending = nullptr;
     uint32_t n_pend = uint32_t(n_all);
     uint32_t* next = pend_a.p;
-    for (int round = 0; n_pend > 0; ++round) {
+    // as the plain path: host-read rounds while many slots are pending, then
+    // groups of rounds with the counts in device memory
+    constexpr uint32_t ROUND_TAIL = 1u << 20;
+    constexpr int ROUND_GROUP = 16;
+    DBuf<uint32_t> counts(P, ROUND_GROUP);
+    for (int round = 0; n_pend > 0;) {
       require(round < 256, "infinite sites model: no free locus left for some mutations");
-      ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-      ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
-      ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-      pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1,
-                            lost.p, next, n_next.p, err.p, st);
+      if (n_pend > ROUND_TAIL) {
+        ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
+        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
+        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1,
+                              lost.p, next, n_next.p, err.p, st);
+        uint32_t nn = 0;
+        ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+        ck(cudaStreamSynchronize(st), "redraw round");
+        if (nn) pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p,
+                                          cnt_id.p, uint32_t(n_snv), next, nn, 1, err.p, st);
+        pending = next;
+        next = (next == pend_a.p) ? pend_b.p : pend_a.p;
+        n_pend = nn;
+        ++round;
+        continue;
+      }
+      uint64_t ctail = 1024;
+      while (ctail < 2ull * n_pend) ctail <<= 1;
+      ck(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * ROUND_GROUP, st), "memset");
+      for (int g = 0; g < ROUND_GROUP; ++g) {
+        const uint32_t* n_dev = g == 0 ? nullptr : counts.p + g - 1;
+        uint32_t* n_out = counts.p + g;
+        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * ctail, st), "memset");
+        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
+        pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p,
+                              ctail - 1, lost.p, next, n_out, err.p, st, n_dev);
+        pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p, cnt_id.p,
+                                  uint32_t(n_snv), next, n_pend, 1, err.p, st, n_out);
+        pending = next;
+        next = (next == pend_a.p) ? pend_b.p : pend_a.p;
+      }
       uint32_t nn = 0;
-      ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-      ck(cudaStreamSynchronize(st), "redraw round");
-      if (nn) pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p,
-                                        cnt_id.p, uint32_t(n_snv), next, nn, 1, err.p, st);
-      pending = next;
-      next = (next == pend_a.p) ? pend_b.p : pend_a.p;
+      ck(cudaMemcpyAsync(&nn, counts.p + ROUND_GROUP - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+      ck(cudaStreamSynchronize(st), "redraw rounds");
       n_pend = nn;
+      round += ROUND_GROUP;
     }
   }
   // sort by (instance, locus); the instance's first record is the exclusive

@@ -102,17 +102,20 @@ struct DriverRec {
 void place_cna_counts(const PlaceTables& t, uint32_t* cnt_cna, uint64_t seed, double germline_size, cudaStream_t st);
 void place_edge_counts(const PlaceTables& t, uint32_t* cnt_snv, uint32_t* cnt_id, uint64_t seed,
                        uint32_t n_pre_snv, uint32_t n_pre_id, cudaStream_t st);
+// n_dev (optional): the number of pending slots in device memory (<= n_pending,
+// which sizes the grid); the redraw rounds run without reading it on the host
 void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
                             const uint32_t* off_id, uint32_t n_snv, uint32_t n_id, const uint32_t* pending,
-                            uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st);
+                            uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st,
+                            const uint32_t* n_dev = nullptr);
 void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, cudaStream_t st);
 // slots whose locus is invalid (no allele covers the drawn position) -> next list
 void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
-                           uint32_t* n_next, cudaStream_t st);
+                           uint32_t* n_next, cudaStream_t st, const uint32_t* n_dev = nullptr);
 void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st);
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
                  uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                 uint32_t* err, cudaStream_t st);
+                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev = nullptr);
 uint32_t sort_num_buckets(uint64_t G);
 void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,
                    uint32_t* order, const PlaceOut& sorted, cudaStream_t st);
@@ -278,10 +281,11 @@ void place_edge_counts_batch(const PlaceTables* tabs, uint32_t n_inst, const uin
 void place_mutations_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* cell_off, const Key* keys,
                            const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
                            uint32_t n_snv, const uint32_t* pending, uint32_t n_pending, int redraw, uint32_t* err,
-                           cudaStream_t st);
+                           cudaStream_t st, const uint32_t* n_dev = nullptr);
 void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uint32_t* pending, uint32_t n,
                        uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
-                       uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st);
+                       uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st,
+                       const uint32_t* n_dev = nullptr);
 // sort by (instance, locus); bcnt holds n_inst * sort_num_buckets(G) + 1
 // entries and ends as the exclusive scan of the bucket counts
 void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t n_inst, uint64_t G, uint32_t* bcnt,

@@ -180,10 +180,10 @@ __device__ __forceinline__ void place_one(const PlaceTables& t, const PlaceOut& 
 
 __global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
                         const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_id,
-                        const uint32_t* __restrict__ pending, uint32_t n_pending, int redraw,
-                        uint32_t* __restrict__ err) {
+                        const uint32_t* __restrict__ pending, uint32_t n_pending,
+                        const uint32_t* __restrict__ n_dev, int redraw, uint32_t* __restrict__ err) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= n_pending) return;
+  if (tid >= (n_dev ? *n_dev : n_pending)) return;
   const uint32_t slot = pending ? pending[tid] : tid;
   const bool is_id = slot >= n_snv;
   const uint32_t i = is_id ? slot - n_snv : slot;
@@ -229,11 +229,11 @@ __global__ void k_insert_accepted(uint32_t* __restrict__ hkeys, uint32_t hmask, 
 }
 
 __global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
-                              const uint32_t* __restrict__ hkeys, uint32_t hmask, uint32_t* __restrict__ ckeys,
-                              uint32_t* __restrict__ cvals, uint32_t cmask, uint8_t* __restrict__ lost,
-                              uint32_t* __restrict__ err) {
+                              const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ hkeys, uint32_t hmask,
+                              uint32_t* __restrict__ ckeys, uint32_t* __restrict__ cvals, uint32_t cmask,
+                              uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (n_dev ? *n_dev : n)) return;
   const uint32_t slot = pending ? pending[i] : i;
   const uint32_t k = locus[slot];
   if (k == LOCUS_INVALID || hset_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
@@ -244,12 +244,12 @@ __global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t
 }
 
 __global__ void k_cand_resolve(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
-                               uint32_t* __restrict__ hkeys, uint32_t hmask, const uint32_t* __restrict__ ckeys,
-                               const uint32_t* __restrict__ cvals, uint32_t cmask, const uint8_t* __restrict__ lost,
-                               uint32_t* __restrict__ next, uint32_t* __restrict__ n_next,
-                               uint32_t* __restrict__ err) {
+                               const uint32_t* __restrict__ n_dev, uint32_t* __restrict__ hkeys, uint32_t hmask,
+                               const uint32_t* __restrict__ ckeys, const uint32_t* __restrict__ cvals, uint32_t cmask,
+                               const uint8_t* __restrict__ lost, uint32_t* __restrict__ next,
+                               uint32_t* __restrict__ n_next, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (n_dev ? *n_dev : n)) return;
   const uint32_t slot = pending ? pending[i] : i;
   const uint32_t k = locus[slot];
   bool win = false;
@@ -291,9 +291,10 @@ __global__ void k_drivers(PlaceOut o, const DriverRec* __restrict__ drv, uint32_
 }
 
 __global__ void k_collect_invalid(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending,
-                                  uint32_t n, uint32_t* __restrict__ next, uint32_t* __restrict__ n_next) {
+                                  uint32_t n, const uint32_t* __restrict__ n_dev, uint32_t* __restrict__ next,
+                                  uint32_t* __restrict__ n_next) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (n_dev ? *n_dev : n)) return;
   const uint32_t slot = pending ? pending[i] : i;
   if (locus[slot] == LOCUS_INVALID) next[atomicAdd(n_next, 1u)] = slot;
 }
@@ -377,10 +378,10 @@ __global__ void k_edge_counts_b(const PlaceTables* __restrict__ tabs, uint32_t n
 __global__ void k_place_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst, const uint32_t* __restrict__ cell_off,
                           const Key* __restrict__ keys, PlaceOut o, uint16_t* __restrict__ inst_of,
                           const uint32_t* __restrict__ off_snv, const uint32_t* __restrict__ off_id, uint32_t n_snv,
-                          const uint32_t* __restrict__ pending, uint32_t n_pending, int redraw,
-                          uint32_t* __restrict__ err) {
+                          const uint32_t* __restrict__ pending, uint32_t n_pending,
+                          const uint32_t* __restrict__ n_dev, int redraw, uint32_t* __restrict__ err) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= n_pending) return;
+  if (tid >= (n_dev ? *n_dev : n_pending)) return;
   const uint32_t slot = pending ? pending[tid] : tid;
   const bool is_id = slot >= n_snv;
   const uint32_t j = is_id ? slot - n_snv : slot;
@@ -422,11 +423,12 @@ __device__ __forceinline__ uint64_t hset64_insert(unsigned long long* __restrict
 }
 
 __global__ void k_cand_insert_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
-                                const uint32_t* __restrict__ pending, uint32_t n, const uint64_t* __restrict__ hkeys,
-                                uint64_t hmask, unsigned long long* __restrict__ ckeys, uint32_t* __restrict__ cvals,
-                                uint64_t cmask, uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
+                                const uint32_t* __restrict__ pending, uint32_t n, const uint32_t* __restrict__ n_dev,
+                                const uint64_t* __restrict__ hkeys, uint64_t hmask,
+                                unsigned long long* __restrict__ ckeys, uint32_t* __restrict__ cvals, uint64_t cmask,
+                                uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (n_dev ? *n_dev : n)) return;
   const uint32_t slot = pending ? pending[i] : i;
   const uint32_t l = locus[slot];
   const uint64_t k = (uint64_t(inst_of[slot]) << 32) | l;
@@ -438,13 +440,13 @@ __global__ void k_cand_insert_b(const uint32_t* __restrict__ locus, const uint16
 }
 
 __global__ void k_cand_resolve_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
-                                 const uint32_t* __restrict__ pending, uint32_t n,
+                                 const uint32_t* __restrict__ pending, uint32_t n, const uint32_t* __restrict__ n_dev,
                                  unsigned long long* __restrict__ hkeys, uint64_t hmask,
                                  const uint64_t* __restrict__ ckeys, const uint32_t* __restrict__ cvals,
                                  uint64_t cmask, const uint8_t* __restrict__ lost, uint32_t* __restrict__ next,
                                  uint32_t* __restrict__ n_next, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= (n_dev ? *n_dev : n)) return;
   const uint32_t slot = pending ? pending[i] : i;
   const uint64_t k = (uint64_t(inst_of[slot]) << 32) | locus[slot];
   bool win = false;
@@ -493,10 +495,10 @@ void place_edge_counts(const PlaceTables& t, uint32_t* cnt_snv, uint32_t* cnt_id
 
 void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
                             const uint32_t* off_id, uint32_t n_snv, uint32_t n_id, const uint32_t* pending,
-                            uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st) {
+                            uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st, const uint32_t* n_dev) {
   if (n_pending == 0) return;
   k_place<<<nblk(n_pending), 256, 0, st>>>(t, o, make_key(seed), off_snv, off_id, n_snv, n_id, pending, n_pending,
-                                           redraw, err); note_launch();
+                                           n_dev, redraw, err); note_launch();
 }
 
 void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, cudaStream_t st) {
@@ -505,8 +507,8 @@ void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint
 }
 
 void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
-                           uint32_t* n_next, cudaStream_t st) {
-  if (n) { k_collect_invalid<<<nblk(n), 256, 0, st>>>(locus, pending, n, next, n_next); note_launch(); }
+                           uint32_t* n_next, cudaStream_t st, const uint32_t* n_dev) {
+  if (n) { k_collect_invalid<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, next, n_next); note_launch(); }
 }
 
 void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st) {
@@ -515,11 +517,12 @@ void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci
 
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
                  uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                 uint32_t* err, cudaStream_t st) {
+                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev) {
   if (n == 0) return;
-  k_cand_insert<<<nblk(n), 256, 0, st>>>(locus, pending, n, hkeys, hmask, ckeys, cvals, cmask, lost, err); note_launch();
-  k_cand_resolve<<<nblk(n), 256, 0, st>>>(locus, pending, n, hkeys, hmask, ckeys, cvals, cmask, lost, next, n_next,
-                                          err); note_launch();
+  k_cand_insert<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, ckeys, cvals, cmask, lost, err);
+  k_cand_resolve<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, ckeys, cvals, cmask, lost, next,
+                                          n_next, err);
+  note_launch(2);
 }
 
 void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,
@@ -547,20 +550,22 @@ void place_edge_counts_batch(const PlaceTables* tabs, uint32_t n_inst, const uin
 void place_mutations_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* cell_off, const Key* keys,
                            const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
                            uint32_t n_snv, const uint32_t* pending, uint32_t n_pending, int redraw, uint32_t* err,
-                           cudaStream_t st) {
+                           cudaStream_t st, const uint32_t* n_dev) {
   if (n_pending == 0) return;
   k_place_b<<<nblk(n_pending), 256, 0, st>>>(tabs, n_inst, cell_off, keys, o, inst_of, off_snv, off_id, n_snv, pending,
-                                             n_pending, redraw, err); note_launch();
+                                             n_pending, n_dev, redraw, err); note_launch();
 }
 
 void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uint32_t* pending, uint32_t n,
                        uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
-                       uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st) {
+                       uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st,
+                       const uint32_t* n_dev) {
   if (n == 0) return;
-  k_cand_insert_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, hkeys, hmask,
+  k_cand_insert_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, n_dev, hkeys, hmask,
                                            reinterpret_cast<unsigned long long*>(ckeys), cvals, cmask, lost, err);
-  k_cand_resolve_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, reinterpret_cast<unsigned long long*>(hkeys),
-                                            hmask, ckeys, cvals, cmask, lost, next, n_next, err);
+  k_cand_resolve_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, n_dev,
+                                            reinterpret_cast<unsigned long long*>(hkeys), hmask, ckeys, cvals, cmask,
+                                            lost, next, n_next, err);
   note_launch(2);
 }
 
