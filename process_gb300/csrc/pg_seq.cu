@@ -315,10 +315,9 @@ struct ReadSmem {
   uint32_t s_locus[SEQ_CAP], s_tin[SEQ_CAP], s_tout[SEQ_CAP], s_info[SEQ_CAP];
   uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
   // mates of the batch in start-bucket order
-  uint16_t s_mpos[SEQ_MCAP];     // start offset in the window | mate << 15
-  uint32_t s_mcell[SEQ_MCAP];    // source cell (Euler index)
-  uint16_t s_minst[SEQ_MCAP];    // allele instance (0xffff: dropped fragment)
-  uint32_t s_mw[SEQ_MCAP];       // the fragment's error word
+  uint32_t s_mpi[SEQ_MCAP];      // start offset in the window | mate << 15 | allele instance << 16
+                                 //   (instance 0xffff: dropped fragment)
+  uint2 s_mcw[SEQ_MCAP];         // source cell (Euler index), the fragment's error word
   uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
   uint32_t s_ins[SEQ_INS_CAP];
   uint16_t s_guide[SEQ_GUIDE];
@@ -340,7 +339,7 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
                                           uint32_t* __restrict__ g_dep_row) {
   auto& s_locus = sh.s_locus; auto& s_tin = sh.s_tin; auto& s_tout = sh.s_tout; auto& s_info = sh.s_info;
   auto& s_alt = sh.s_alt; auto& s_dep = sh.s_dep;
-  auto& s_mpos = sh.s_mpos; auto& s_mcell = sh.s_mcell; auto& s_minst = sh.s_minst; auto& s_mw = sh.s_mw;
+  auto& s_mpi = sh.s_mpi; auto& s_mcw = sh.s_mcw;
   auto& s_boff = sh.s_boff; auto& s_ins = sh.s_ins; auto& s_guide = sh.s_guide;
   auto& s_wstart = sh.s_wstart; auto& s_wpre = sh.s_wpre; auto& s_scan = sh.s_scan;
   uint32_t& s_wtot = sh.s_wtot;
@@ -396,9 +395,10 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
     const uint32_t nb_pairs = min(per_batch, n_pairs - b0);
     for (uint32_t b = tid; b <= nbk; b += SEQ_THREADS) s_boff[b] = 0;
     __syncthreads();
-    // phase A: fragments stay in registers; each mate takes its rank within
-    // its start bucket from the histogram's atomic
-    uint32_t o0[FPT], o1[FPT], ca[FPT], fi[FPT], fw[FPT], rk0[FPT], rk1[FPT];
+    // phase A: fragments stay in registers (mate offsets, both < 2^15, and
+    // bucket ranks, both < 2^16, packed in pairs); each mate takes its rank
+    // within its start bucket from the histogram's atomic
+    uint32_t o01[FPT], ca[FPT], fi[FPT], fw[FPT], rk01[FPT];
 #pragma unroll
     for (uint32_t q = 0; q < FPT; ++q) {
       const uint32_t k = tid + q * SEQ_THREADS;
@@ -409,12 +409,15 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
         ca[q] = f.cell;
         fi[q] = f.inst;
         fw[q] = f.w;
-        o0[q] = f.p0 - start;
-        rk0[q] = atomicAdd(s_boff + o0[q] / SEQ_BW, 1u);
+        const uint32_t o0 = f.p0 - start;
+        uint32_t rk = atomicAdd(s_boff + o0 / SEQ_BW, 1u);
+        uint32_t o1 = 0;
         if (prm.paired) {
-          o1[q] = f.p1 - start;
-          rk1[q] = atomicAdd(s_boff + o1[q] / SEQ_BW, 1u);
+          o1 = f.p1 - start;
+          rk |= atomicAdd(s_boff + o1 / SEQ_BW, 1u) << 16;
         }
+        o01[q] = o0 | (o1 << 16);
+        rk01[q] = rk;
       }
     }
     __syncthreads();
@@ -434,12 +437,12 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
     for (uint32_t q = 0; q < FPT; ++q) {
       const uint32_t k = tid + q * SEQ_THREADS;
       if (k < nb_pairs) {
-        const uint32_t x0 = s_boff[o0[q] / SEQ_BW] + rk0[q];
-        s_mpos[x0] = uint16_t(o0[q]); s_mcell[x0] = ca[q]; s_minst[x0] = uint16_t(fi[q]); s_mw[x0] = fw[q];
+        const uint32_t o0 = o01[q] & 0xffffu, o1 = o01[q] >> 16;
+        const uint32_t x0 = s_boff[o0 / SEQ_BW] + (rk01[q] & 0xffffu);
+        s_mpi[x0] = o0 | (fi[q] << 16); s_mcw[x0] = make_uint2(ca[q], fw[q]);
         if (prm.paired) {
-          const uint32_t x1 = s_boff[o1[q] / SEQ_BW] + rk1[q];
-          s_mpos[x1] = uint16_t(o1[q] | 0x8000u); s_mcell[x1] = ca[q]; s_minst[x1] = uint16_t(fi[q]);
-          s_mw[x1] = fw[q];
+          const uint32_t x1 = s_boff[o1 / SEQ_BW] + (rk01[q] >> 16);
+          s_mpi[x1] = o1 | 0x8000u | (fi[q] << 16); s_mcw[x1] = make_uint2(ca[q], fw[q]);
         }
       }
     }
@@ -489,7 +492,9 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
             base = s_wstart[i] - s_wpre[i];
           }
           const uint32_t x = base + k;
-          const uint32_t pm = s_mpos[x], ca = s_mcell[x], mi = s_minst[x], w = s_mw[x];   // independent loads
+          const uint32_t pi = s_mpi[x];
+          const uint2 cw = s_mcw[x];                          // one 32-bit and one 64-bit load
+          const uint32_t pm = pi & 0xffffu, mi = pi >> 16, ca = cw.x, w = cw.y;
           const uint32_t o = pm & 0x7fffu;
           if (o > off || o + R <= off || mi == 0xffffu) continue;   // the mate does not cover L (or was dropped)
           dep += 1;
