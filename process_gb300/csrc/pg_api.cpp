@@ -1772,7 +1772,7 @@ pg_status pg_seq_result_kernel_ms(const pg_seq_result* r, float* ms) {
 }  // extern "C"
 
 // ====================================================================== calibration
-constexpr uint32_t CALIB_CHUNK = 8192;   // sites per CTA of the site kernel
+constexpr uint32_t CALIB_CHUNK = 16384;   // sites per CTA of the site kernel
 
 struct pg_calib {
   int device = 0;
@@ -1782,9 +1782,9 @@ struct pg_calib {
   DBuf<int32_t> alt, depth, cls;
   DBuf<uint64_t> site_off, chunk_start;
   DBuf<uint32_t> chunk_rep, rep_first_chunk, step;
-  DBuf<float> sig, epoch_w, phi, partial, m, v;
+  DBuf<float> sig, sig_rows, epoch_w, phi, partial, m, v, tab;
   std::vector<uint32_t> rep_first_chunk_h;
-  uint32_t part_stride = 0;
+  uint32_t part_stride = 0, tab_stride = 0;
   cudaGraphExec_t graph = nullptr;
   struct { float* params = nullptr; uint32_t steps = 0; float lr = 0, b1 = 0, b2 = 0, eps = 0; float* nll = nullptr; cudaStream_t st = nullptr; } gkey;
   pg::CalibArgs args() const {
@@ -1793,13 +1793,14 @@ struct pg_calib {
     a.alt = alt.p; a.depth = depth.p; a.cls = cls.p; a.site_off = site_off.p;
     a.sig = sig.p; a.epoch_w = epoch_w.p; a.phi = phi.p;
     a.chunk = CALIB_CHUNK; a.part_stride = part_stride;
+    a.sig_rows = sig_rows.p; a.tab = tab.p; a.tab_stride = tab_stride;
     return a;
   }
   ~pg_calib() {
     if (graph) cudaGraphExecDestroy(graph);
     alt.reset(); depth.reset(); cls.reset(); site_off.reset(); chunk_start.reset(); chunk_rep.reset();
     rep_first_chunk.reset(); step.reset(); sig.reset(); epoch_w.reset(); phi.reset(); partial.reset(); m.reset();
-    v.reset();
+    v.reset(); tab.reset(); sig_rows.reset();
     pool.release_all();
     if (own_st) cudaStreamDestroy(own_st);
   }
@@ -1848,6 +1849,13 @@ pg_status pg_calib_create(uint32_t n_rep, const uint64_t* site_off, const int32_
     }
     for (uint64_t x = 0; x < fw.size(); ++x) { fw[x] = float(epoch_weight[x]); fp[x] = float(phi[x]); }
     c->sig = upload(P, fs, st); c->epoch_w = upload(P, fw, st); c->phi = upload(P, fp, st);
+    {   // signatures by class, rows of 4 or 8 floats
+      const uint32_t JP = J > 4 ? 8 : 4;
+      std::vector<float> rows(size_t(C) * JP, 0.f);
+      for (uint32_t j = 0; j < J; ++j)
+        for (uint32_t cl = 0; cl < C; ++cl) rows[size_t(cl) * JP + j] = fs[size_t(j) * C + cl];
+      c->sig_rows = upload(P, rows, st);
+    }
     // chunks of CALIB_CHUNK sites, never across replicates
     std::vector<uint32_t> crep;
     std::vector<uint64_t> cstart;
@@ -1860,7 +1868,10 @@ pg_status pg_calib_create(uint32_t n_rep, const uint64_t* site_off, const int32_
     c->n_chunks = uint32_t(crep.size());
     c->chunk_rep = upload(P, crep, st); c->chunk_start = upload(P, cstart, st);
     c->rep_first_chunk = upload(P, c->rep_first_chunk_h, st);
-    c->part_stride = (1 + 2 * K + K * C + 3) & ~3u;
+    c->part_stride = (1 + 3 * K + K * J + 3) & ~3u;
+    // per replicate: log(exp(lr_k) L_k / Z), log v_k, log(1 - v_k) (K each), w_kj (K J)
+    c->tab_stride = (3 * K + K * J + 3) & ~3u;
+    c->tab = DBuf<float>(P, uint64_t(n_rep) * c->tab_stride);
     c->partial = DBuf<float>(P, uint64_t(std::max<uint32_t>(c->n_chunks, 1)) * c->part_stride);
     c->m = DBuf<float>(P, uint64_t(n_rep) * c->P);
     c->v = DBuf<float>(P, uint64_t(n_rep) * c->P);

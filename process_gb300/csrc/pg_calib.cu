@@ -12,14 +12,24 @@
 // (the binomial coefficient, constant in the parameters, is left out).
 // Parameters per replicate, in order: lr_0..K-1, theta_00..theta_K-1,J-1, rho.
 //
-// Kernels: k_calib_sites (one CTA per (replicate, chunk of sites)) computes
-// per-site log-likelihoods and responsibilities gamma_k in FP32 and reduces
-//   G_k(c) = sum_{i: c_i = c} gamma_ik,  A_k = sum gamma_ik a_i,
-//   B_k = sum gamma_ik (d_i - a_i),  NLL
-// with per-thread Neumaier-compensated sums and deterministic per-warp class
-// bins; k_calib_epilogue (one CTA per replicate) adds the chunk partials in a
-// fixed order (compensated) and applies the chain rule, optionally followed
-// by an Adam step on the parameters.
+// Kernels: k_calib_tables (one CTA per replicate) derives the replicate's
+// constants; k_calib_sites (one CTA per (replicate, chunk of sites))
+// computes per-site log-likelihoods and responsibilities in FP32 with the
+// mixture weights in registers and only the site class's signature row
+// S(c) gathered from shared memory:
+//   u_k = log(exp(lr_k) L_k / Z) + a log v_k + (d - a) log(1 - v_k)
+//   e_k = exp(u_k - max u),  q_k = M_k(c) e_k,  s = sum_k q_k
+//   gamma_k = q_k / s,  log-likelihood = max u + log s
+// and reduces
+//   G_k = sum_i gamma_ik,  A_k = sum gamma_ik a_i,  B_k = sum gamma_ik (d_i - a_i),
+//   H_kj = sum_i gamma_ik S_j(c_i) / M_k(c_i) = sum_i e_ik S_j(c_i) / s_i,  NLL
+// (H carries the class dependence of the exposure gradient, so no per-class
+// bins are needed) with per-thread FP32 sums over the thread's sites in
+// order, a fixed warp tree and a Neumaier-compensated sum over the warps;
+// k_calib_epilogue (one CTA per replicate) adds the chunk partials in a fixed
+// order (compensated) and applies the chain rule, optionally followed by an
+// Adam step on the parameters.  Every sum has a fixed order: results are
+// deterministic.
 #include <cstdint>
 
 #include "pg_kernels.h"
@@ -40,167 +50,133 @@ struct Neu {   // Neumaier-compensated FP32 sum
   __device__ __forceinline__ float value() const { return s + c; }
 };
 
-// per-replicate derived tables: log pi_k(c), log v_k, log(1 - v_k)
-__device__ void calib_tables(const CalibArgs& a, uint32_t r, const float* __restrict__ p, float* logpi, float* lv,
-                             float* l1v) {
-  const uint32_t K = a.K, J = a.J, C = a.C;
-  // Z and softmax are tiny: every thread recomputes them
+// Per-replicate constants, once per evaluation, in the replicate's row of
+// a.tab: log(exp(lr_k) L_k / Z) (K), log v_k (K), log(1 - v_k) (K), then the
+// exposures w_kj (K x J).
+__global__ void __launch_bounds__(32) k_calib_tables(CalibArgs a, const float* __restrict__ params) {
+  const uint32_t r = a.rep0 + blockIdx.x;
+  const uint32_t K = a.K, J = a.J, k = threadIdx.x;
+  const float* p = params + uint64_t(r) * a.P;
+  float* row = a.tab + uint64_t(r) * a.tab_stride;
   float Z = 0.f;
-  for (uint32_t k = 0; k < K; ++k) Z += expf(p[k]) * a.epoch_w[r * K + k];
-  const float lZ = logf(Z);
+  for (uint32_t q = 0; q < K; ++q) Z += expf(p[q]) * a.epoch_w[r * K + q];
+  if (k >= K) return;
   const float sig = 1.f / (1.f + expf(-p[K + K * J]));
-  for (uint32_t x = threadIdx.x; x < K * C; x += blockDim.x) {
-    const uint32_t k = x / C, c = x % C;
-    const float* th = p + K + k * J;
-    float mx = th[0];
-    for (uint32_t j = 1; j < J; ++j) mx = fmaxf(mx, th[j]);
-    float den = 0.f, num = 0.f;
-    for (uint32_t j = 0; j < J; ++j) {
-      const float e = expf(th[j] - mx);
-      den += e;
-      num += e * a.sig[j * C + c];
-    }
-    const float M = num / den;
-    logpi[c * K + k] = p[k] + logf(a.epoch_w[r * K + k]) + logf(fmaxf(M, 1e-30f)) - lZ;   // class-major
-  }
-  if (threadIdx.x < K) {
-    const float v = sig * a.phi[r * K + threadIdx.x] * 0.5f;
-    lv[threadIdx.x] = logf(v);
-    l1v[threadIdx.x] = log1pf(-v);
-  }
+  const float v = sig * a.phi[r * K + k] * 0.5f;
+  row[k] = p[k] + logf(a.epoch_w[r * K + k]) - logf(Z);
+  row[K + k] = logf(v);
+  row[2 * K + k] = log1pf(-v);
+  const float* th = p + K + k * J;
+  float mx = th[0];
+  for (uint32_t j = 1; j < J; ++j) mx = fmaxf(mx, th[j]);
+  float den = 0.f;
+  for (uint32_t j = 0; j < J; ++j) den += expf(th[j] - mx);
+  for (uint32_t j = 0; j < J; ++j) row[3 * K + k * J + j] = expf(th[j] - mx) / den;
 }
 
-// K floats as one vector access where K is a multiple of 4
-template <uint32_t K, bool V = (K % 4 == 0)> struct KVec {
-  using type = float;
-  __device__ static void load(const float* p, float* v) {
-#pragma unroll
-    for (uint32_t k = 0; k < K; ++k) v[k] = p[k];
-  }
-  __device__ static void add(float* p, const float* v) {
-#pragma unroll
-    for (uint32_t k = 0; k < K; ++k) p[k] += v[k];
-  }
-};
-template <uint32_t K> struct KVec<K, true> {
-  using type = float4;
-  __device__ static void load(const float* p, float* v) {
-#pragma unroll
-    for (uint32_t k = 0; k < K; k += 4) {
-      const float4 x = *reinterpret_cast<const float4*>(p + k);
-      v[k] = x.x; v[k + 1] = x.y; v[k + 2] = x.z; v[k + 3] = x.w;
-    }
-  }
-  __device__ static void add(float* p, const float* v) {
-#pragma unroll
-    for (uint32_t k = 0; k < K; k += 4) {
-      float4 x = *reinterpret_cast<float4*>(p + k);
-      x.x += v[k]; x.y += v[k + 1]; x.z += v[k + 2]; x.w += v[k + 3];
-      *reinterpret_cast<float4*>(p + k) = x;
-    }
-  }
-};
-
 // Per-site work: every thread takes sites i0 + tid, i0 + tid + 256, ...
-// (coalesced), keeps plain FP32 sums over its ~32 sites, and adds its
-// responsibilities straight into its warp's class bins; lanes of one warp
-// that share a class add theirs in lane order (deterministic).  The sums are
-// compensated from the warp level on.
-template <uint32_t K>
-__global__ void __launch_bounds__(CAL_THREADS) k_calib_sites(CalibArgs a, const float* __restrict__ params,
-                                                             const uint32_t* __restrict__ chunk_rep,
-                                                             const uint64_t* __restrict__ chunk_start,
-                                                             float* __restrict__ partial) {
-  __shared__ __align__(16) float s_logpi[K * CAL_MAXC];
-  __shared__ float s_lv[K], s_l1v[K];
-  __shared__ __align__(16) float s_bins[CAL_WARPS][K * CAL_MAXC];
-  __shared__ float s_red[CAL_WARPS][2 + 4 * K];
+// (coalesced, four sites' loads in flight at a time) and keeps plain FP32
+// sums over its sites, in site order.  The signature rows in shared memory
+// are JP floats (J rounded up to 4 or 8, zero beyond J).
+// CTAs per SM asked of the register allocator: the per-thread constants and
+// sums take about 1 + 6K + 2KJ registers, plus K of per-site temporaries
+constexpr uint32_t calib_min_blocks(uint32_t K, uint32_t J) {
+  return 1 + 7 * K + 2 * K * J <= 53 ? 3 : 1 + 7 * K + 2 * K * J <= 96 ? 2 : 1;
+}
+
+template <uint32_t K, uint32_t J>
+__global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_sites(
+    CalibArgs a, const float* __restrict__ params, const uint32_t* __restrict__ chunk_rep,
+    const uint64_t* __restrict__ chunk_start, float* __restrict__ partial) {
+  constexpr uint32_t JP = J > 4 ? 8 : 4;
+  constexpr uint32_t NV = 1 + 3 * K + K * J;   // nll, A, B, G, H
+  constexpr uint32_t U = 4;
+  __shared__ __align__(16) float s_sig[JP * CAL_MAXC];
+  __shared__ float s_row[3 * CAL_MAXK + CAL_MAXK * CAL_MAXJ];
+  __shared__ float s_red[CAL_WARPS][NV];
   const uint32_t chunk = a.chunk0 + blockIdx.x;
   const uint32_t r = chunk_rep[chunk];
   const uint64_t i0 = chunk_start[chunk];
   const uint64_t i1 = min(i0 + a.chunk, a.site_off[r + 1]);
-  const uint32_t C = a.C, P = a.P;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  calib_tables(a, r, params + uint64_t(r) * P, s_logpi, s_lv, s_l1v);
-  for (uint32_t x = lane; x < K * C; x += 32) s_bins[warp][x] = 0.f;
+  for (uint32_t x = threadIdx.x; x < JP * a.C / 4; x += CAL_THREADS)
+    reinterpret_cast<float4*>(s_sig)[x] = reinterpret_cast<const float4*>(a.sig_rows)[x];
+  for (uint32_t x = threadIdx.x; x < 3 * K + K * J; x += CAL_THREADS) s_row[x] = a.tab[uint64_t(r) * a.tab_stride + x];
   __syncthreads();
-  float lv[K], l1v[K];
+  float cst[K], lv[K], l1v[K], w[K * J];
 #pragma unroll
-  for (uint32_t k = 0; k < K; ++k) { lv[k] = s_lv[k]; l1v[k] = s_l1v[k]; }
-  float nll = 0.f, A[K], B[K];
+  for (uint32_t k = 0; k < K; ++k) {
+    cst[k] = s_row[k]; lv[k] = s_row[K + k]; l1v[k] = s_row[2 * K + k];
 #pragma unroll
-  for (uint32_t k = 0; k < K; ++k) { A[k] = 0.f; B[k] = 0.f; }
-  float* bins = s_bins[warp];
-  // log pi and the bins are class-major ([c][k]): one vector access per site
-  using VecK = typename KVec<K>::type;
-  for (uint64_t base = i0 + (threadIdx.x & ~31u); base < i1; base += CAL_THREADS) {
-    const uint64_t i = base + lane;
-    const bool act = i < i1;
-    int32_t c = -1;
-    float g[K];
-    if (act) {
-      const float al = float(__ldg(a.alt + i)), dl = float(__ldg(a.depth + i));
-      c = __ldg(a.cls + i);
-      float t[K], tmax = -INFINITY;
-      KVec<K>::load(s_logpi + c * K, t);
-#pragma unroll
-      for (uint32_t k = 0; k < K; ++k) {
-        t[k] += al * lv[k] + (dl - al) * l1v[k];
-        tmax = fmaxf(tmax, t[k]);
-      }
-      float se = 0.f;
-#pragma unroll
-      for (uint32_t k = 0; k < K; ++k) { g[k] = __expf(t[k] - tmax); se += g[k]; }
-      const float inv = 1.f / se;
-      nll -= tmax + __logf(se);
-#pragma unroll
-      for (uint32_t k = 0; k < K; ++k) { g[k] *= inv; A[k] += g[k] * al; B[k] += g[k] * (dl - al); }
-    }
-    const uint32_t peers = __match_any_sync(0xffffffffu, c);
-    if (act) {
-      if ((peers & (peers - 1)) == 0) {              // the only lane with this class
-        KVec<K>::add(bins + c * K, g);
-      } else {                                         // shared class: sum in lane order
-        float sum[K];
-#pragma unroll
-        for (uint32_t k = 0; k < K; ++k) sum[k] = 0.f;
-        for (uint32_t m = peers; m; m &= m - 1) {
-          const int src = __ffs(m) - 1;
-#pragma unroll
-          for (uint32_t k = 0; k < K; ++k) sum[k] += __shfl_sync(peers, g[k], src);
-        }
-        if (lane == uint32_t(__ffs(peers) - 1)) KVec<K>::add(bins + c * K, sum);
-      }
-    }
-    __syncwarp();
-    (void)sizeof(VecK);
+    for (uint32_t j = 0; j < J; ++j) w[k * J + j] = s_row[3 * K + k * J + j];
   }
-  // block partial: warp sums, then a compensated sum over the warps
+  float acc[NV];
+#pragma unroll
+  for (uint32_t q = 0; q < NV; ++q) acc[q] = 0.f;
+  auto site = [&](float al, float dl, int32_t c) {
+    float sg[JP];
+#pragma unroll
+    for (uint32_t j = 0; j < JP; j += 4) {
+      const float4 x = *reinterpret_cast<const float4*>(s_sig + c * JP + j);
+      sg[j] = x.x; sg[j + 1] = x.y; sg[j + 2] = x.z; sg[j + 3] = x.w;
+    }
+    float u[K], umax = -INFINITY;
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) {
+      u[k] = cst[k] + al * lv[k] + (dl - al) * l1v[k];
+      umax = fmaxf(umax, u[k]);
+    }
+    float e[K], q[K], sum = 0.f;
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) {
+      float m = 0.f;
+#pragma unroll
+      for (uint32_t j = 0; j < J; ++j) m += w[k * J + j] * sg[j];
+      e[k] = __expf(u[k] - umax);
+      q[k] = fmaxf(m, 1e-30f) * e[k];
+      sum += q[k];
+    }
+    const float inv = __fdividef(1.f, sum);
+    acc[0] -= umax + __logf(sum);
+#pragma unroll
+    for (uint32_t k = 0; k < K; ++k) {
+      const float g = q[k] * inv, h = e[k] * inv;
+      acc[1 + k] += g * al;
+      acc[1 + K + k] += g * (dl - al);
+      acc[1 + 2 * K + k] += g;
+#pragma unroll
+      for (uint32_t j = 0; j < J; ++j) acc[1 + 3 * K + k * J + j] += h * sg[j];
+    }
+  };
+  uint64_t i = i0 + threadIdx.x;
+  for (; i + (U - 1) * CAL_THREADS < i1; i += U * CAL_THREADS) {
+    float al[U], dl[U];
+    int32_t c[U];
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) {
+      al[u] = float(__ldg(a.alt + i + u * CAL_THREADS));
+      dl[u] = float(__ldg(a.depth + i + u * CAL_THREADS));
+      c[u] = __ldg(a.cls + i + u * CAL_THREADS);
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < U; ++u) site(al[u], dl[u], c[u]);
+  }
+  for (; i < i1; i += CAL_THREADS) site(float(__ldg(a.alt + i)), float(__ldg(a.depth + i)), __ldg(a.cls + i));
+  // block partial: warp trees, then a compensated sum over the warps
+#pragma unroll
+  for (uint32_t q = 0; q < NV; ++q) {
+    float v = acc[q];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[warp][q] = v;
+  }
+  __syncthreads();
+  // partial layout: nll, A_k, B_k, G_k, H_kj (j < J)
   float* out = partial + uint64_t(chunk) * a.part_stride;
-  {
-    float vals[1 + 2 * K];
-    vals[0] = nll;
-#pragma unroll
-    for (uint32_t k = 0; k < K; ++k) { vals[1 + k] = A[k]; vals[1 + K + k] = B[k]; }
-#pragma unroll
-    for (uint32_t q = 0; q < 1 + 2 * K; ++q) {
-      float v = vals[q];
-#pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (lane == 0) s_red[warp][q] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 1 + 2 * K) {
+  for (uint32_t x = threadIdx.x; x < NV; x += blockDim.x) {
     Neu t;
-    for (uint32_t w = 0; w < CAL_WARPS; ++w) t.add(s_red[w][threadIdx.x]);
-    out[threadIdx.x] = t.value();
-  }
-  for (uint32_t x = threadIdx.x; x < K * C; x += blockDim.x) {
-    const uint32_t k = x / C, c = x % C;
-    Neu t;
-    for (uint32_t w = 0; w < CAL_WARPS; ++w) t.add(s_bins[w][c * K + k]);
-    out[1 + 2 * K + x] = t.value();
+    for (uint32_t w = 0; w < CAL_WARPS; ++w) t.add(s_red[w][x]);
+    out[x] = t.value();
   }
 }
 
@@ -210,14 +186,12 @@ __global__ void __launch_bounds__(CAL_THREADS) k_calib_epilogue(CalibArgs a, flo
                                                                 const float* __restrict__ partial,
                                                                 float* __restrict__ nll_out,
                                                                 float* __restrict__ grad_out, AdamArgs adam) {
-  __shared__ float s_tot[1 + 2 * CAL_MAXK + CAL_MAXK * CAL_MAXC];
-  __shared__ float s_M[CAL_MAXK * CAL_MAXC];
+  __shared__ float s_tot[1 + 3 * CAL_MAXK + CAL_MAXK * CAL_MAXJ];
   __shared__ float s_w[CAL_MAXK * CAL_MAXJ];
   __shared__ float s_grad[CAL_MAXK + CAL_MAXK * CAL_MAXJ + 1];
-  __shared__ float s_Gk[CAL_MAXK];
   const uint32_t r = a.rep0 + blockIdx.x;
-  const uint32_t K = a.K, J = a.J, C = a.C, P = a.P;
-  const uint32_t nval = 1 + 2 * K + K * C;
+  const uint32_t K = a.K, J = a.J, P = a.P;
+  const uint32_t nval = 1 + 3 * K + K * J;
   const uint32_t c0 = rep_first_chunk[r], c1 = rep_first_chunk[r + 1];
   for (uint32_t x = threadIdx.x; x < nval; x += blockDim.x) {
     Neu t;
@@ -225,7 +199,7 @@ __global__ void __launch_bounds__(CAL_THREADS) k_calib_epilogue(CalibArgs a, flo
     s_tot[x] = t.value();
   }
   float* p = params + uint64_t(r) * P;
-  // exposures and mixtures
+  // exposures
   for (uint32_t k = threadIdx.x; k < K; k += blockDim.x) {
     const float* th = p + K + k * J;
     float mx = th[0];
@@ -235,24 +209,13 @@ __global__ void __launch_bounds__(CAL_THREADS) k_calib_epilogue(CalibArgs a, flo
     for (uint32_t j = 0; j < J; ++j) s_w[k * J + j] = expf(th[j] - mx) / den;
   }
   __syncthreads();
-  for (uint32_t x = threadIdx.x; x < K * C; x += blockDim.x) {
-    const uint32_t k = x / C, c = x % C;
-    float m = 0.f;
-    for (uint32_t j = 0; j < J; ++j) m += s_w[k * J + j] * a.sig[j * C + c];
-    s_M[x] = fmaxf(m, 1e-30f);
-  }
-  if (threadIdx.x < K) {
-    Neu g;
-    for (uint32_t c = 0; c < C; ++c) g.add(s_tot[1 + 2 * K + threadIdx.x * C + c]);
-    s_Gk[threadIdx.x] = g.value();
-  }
-  __syncthreads();
   const float* G = s_tot + 1 + 2 * K;
+  const float* H = s_tot + 1 + 3 * K;
   if (threadIdx.x == 0) {
     // d/d lr_k = -G_k + N r_k L_k / Z   (N = sum_k G_k = number of sites)
     float Z = 0.f, N = 0.f;
-    for (uint32_t k = 0; k < K; ++k) { Z += expf(p[k]) * a.epoch_w[r * K + k]; N += s_Gk[k]; }
-    for (uint32_t k = 0; k < K; ++k) s_grad[k] = -s_Gk[k] + N * expf(p[k]) * a.epoch_w[r * K + k] / Z;
+    for (uint32_t k = 0; k < K; ++k) { Z += expf(p[k]) * a.epoch_w[r * K + k]; N += G[k]; }
+    for (uint32_t k = 0; k < K; ++k) s_grad[k] = -G[k] + N * expf(p[k]) * a.epoch_w[r * K + k] / Z;
     // d/d rho = -(1 - sigma) sum_k (A_k - B_k v_k / (1 - v_k))
     const float sig = 1.f / (1.f + expf(-p[K + K * J]));
     float acc = 0.f;
@@ -262,13 +225,8 @@ __global__ void __launch_bounds__(CAL_THREADS) k_calib_epilogue(CalibArgs a, flo
     }
     s_grad[K + K * J] = -(1.f - sig) * acc;
   }
-  // d/d theta_kj = -w_kj (sum_c G_k(c) S_j(c) / M_k(c) - G_k)
-  for (uint32_t x = threadIdx.x; x < K * J; x += blockDim.x) {
-    const uint32_t k = x / J, j = x % J;
-    Neu s;
-    for (uint32_t c = 0; c < C; ++c) s.add(G[k * C + c] * a.sig[j * C + c] / s_M[k * C + c]);
-    s_grad[K + x] = -s_w[x] * (s.value() - s_Gk[k]);
-  }
+  // d/d theta_kj = -w_kj (sum_i gamma_ik S_j(c_i) / M_k(c_i) - G_k) = -w_kj (H_kj - G_k)
+  for (uint32_t x = threadIdx.x; x < K * J; x += blockDim.x) s_grad[K + x] = -s_w[x] * (H[x] - G[x / J]);
   __syncthreads();
   if (threadIdx.x == 0 && nll_out) nll_out[r] = s_tot[0];
   for (uint32_t q = threadIdx.x; q < P; q += blockDim.x) {
@@ -291,10 +249,18 @@ __global__ void __launch_bounds__(CAL_THREADS) k_calib_epilogue(CalibArgs a, flo
 void calib_launch(const CalibArgs& a, float* params, const uint32_t* chunk_rep, const uint64_t* chunk_start,
                   uint32_t n_chunks, const uint32_t* rep_first_chunk, uint32_t n_rep, float* partial, float* nll,
                   float* grad, const AdamArgs& adam, cudaStream_t st) {
+  if (n_rep) {
+    k_calib_tables<<<n_rep, 32, 0, st>>>(a, params);
+    note_launch();
+  }
   if (n_chunks) {
-    switch (a.K) {
-#define PG_CALIB_K(KK) case KK: k_calib_sites<KK><<<n_chunks, CAL_THREADS, 0, st>>>(a, params, chunk_rep, chunk_start, partial); break;
+    switch (a.K * 8 + a.J - 9) {
+#define PG_CALIB_J(KK, JJ) \
+  case KK * 8 + JJ - 9: k_calib_sites<KK, JJ><<<n_chunks, CAL_THREADS, 0, st>>>(a, params, chunk_rep, chunk_start, partial); break;
+#define PG_CALIB_K(KK) PG_CALIB_J(KK, 1) PG_CALIB_J(KK, 2) PG_CALIB_J(KK, 3) PG_CALIB_J(KK, 4) \
+                       PG_CALIB_J(KK, 5) PG_CALIB_J(KK, 6) PG_CALIB_J(KK, 7) PG_CALIB_J(KK, 8)
       PG_CALIB_K(1) PG_CALIB_K(2) PG_CALIB_K(3) PG_CALIB_K(4) PG_CALIB_K(5) PG_CALIB_K(6) PG_CALIB_K(7) PG_CALIB_K(8)
+#undef PG_CALIB_J
 #undef PG_CALIB_K
     }
     note_launch();

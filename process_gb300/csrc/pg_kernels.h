@@ -328,8 +328,11 @@ struct CalibArgs {
   const float* epoch_w;         // n_rep x K  (L_k: relative length of epoch k)
   const float* phi;             // n_rep x K  (mean cellular fraction of epoch-k mutations)
   uint32_t chunk;               // sites per CTA
-  uint32_t part_stride;         // floats per chunk partial (>= 1 + 2K + K C)
+  uint32_t part_stride;         // floats per chunk partial (>= 1 + 3K + K J)
   uint32_t chunk0, rep0;        // first chunk / replicate of a launch (sub-range launches)
+  const float* sig_rows;        // C x JP: S_j(c) by class, JP = 4 (J <= 4) or 8 floats, zero beyond J
+  float* tab;                   // per replicate: log(exp(lr_k) L_k / Z), log v_k, log(1 - v_k), w_kj
+  uint32_t tab_stride;          // floats per replicate in tab
 };
 struct AdamArgs {               // m == nullptr: no optimizer step
   float* m; float* v; uint32_t* step;

@@ -1155,10 +1155,19 @@ class SeqResult:
         check(lib().pg_seq_result_dims(self._h, C.byref(s), C.byref(m), C.byref(r)))
         return s.value, m.value, r.value
 
-    def counts(self) -> tuple[np.ndarray, np.ndarray]:
+    def counts(self, out: tuple[np.ndarray, np.ndarray] | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """alt and depth tables (samples x mutations, int32).  ``out`` takes
+        two preallocated C-contiguous int32 arrays of that shape, e.g. views
+        of page-locked host memory, which the device copies straight into."""
         s, m, _ = self.dims()
-        alt = np.empty((s, m), dtype=np.int32)
-        dep = np.empty((s, m), dtype=np.int32)
+        if out is None:
+            alt = np.empty((s, m), dtype=np.int32)
+            dep = np.empty((s, m), dtype=np.int32)
+        else:
+            alt, dep = out
+            for a in (alt, dep):
+                if a.dtype != np.int32 or a.shape != (s, m) or not a.flags.c_contiguous or not a.flags.writeable:
+                    raise ValueError(f"out arrays must be writable C-contiguous int32 of shape {(s, m)}")
         check(lib().pg_seq_result_copy(self._h, ptr(alt, C.c_int32), ptr(dep, C.c_int32)))
         return alt, dep
 

@@ -35,3 +35,27 @@ def test_save_load_round_trip(gpu_lib, tmp_path):
     c1, c2 = pf.cna_table(), pf2.cna_table()
     for k in c1:
         np.testing.assert_array_equal(c1[k], c2[k], err_msg=k)
+
+
+def test_counts_into_page_locked_buffers(gpu_lib):
+    """counts(out=...) fills caller-owned (here page-locked) arrays with the
+    same tables as the allocating form, and rejects wrong shapes and types."""
+    import torch
+    from process_gb300 import synth
+    from process_gb300.engine import sequence_counts
+    w = synth.config1(seed=12, n_leaves=100)
+    w.genome.chr_lengths = [100_000, 50_000, 50_000]
+    eng = synth.build_engine(w)
+    pf = eng.place_mutations(w.forest, 10, 2, seed=2)
+    r = sequence_counts(pf, 3, coverage=12, read_size=100, insert_size_mean=250, insert_size_stddev=10)
+    s, m, _ = r.dims()
+    a1, d1 = r.counts()
+    bufs = [torch.empty((s, m), dtype=torch.int32, pin_memory=True).numpy() for _ in range(2)]
+    a2, d2 = r.counts(tuple(bufs))
+    assert a2 is bufs[0] and d2 is bufs[1]
+    np.testing.assert_array_equal(a1, a2)
+    np.testing.assert_array_equal(d1, d2)
+    with pytest.raises(ValueError, match="C-contiguous int32"):
+        r.counts((np.empty((s, m), np.int64), bufs[1]))
+    with pytest.raises(ValueError, match="C-contiguous int32"):
+        r.counts((bufs[0][:, :-1], bufs[1]))
