@@ -78,6 +78,29 @@ __global__ void __launch_bounds__(32) k_calib_tables(CalibArgs a, const float* _
 // (coalesced, four sites' loads in flight at a time) and keeps plain FP32
 // sums over its sites, in site order.  The signature rows in shared memory
 // are JP floats (J rounded up to 4 or 8, zero beyond J).
+// packed f32x2 arithmetic (two lanes of one 64-bit register pair, each
+// rounded as the scalar operation)
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+#define PG_F2OP(NAME, OP)                                                                                        \
+  __device__ __forceinline__ float2 NAME(float2 a, float2 b) {                                                \
+    float2 d;                                                                                                  \
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" OP " rd, ra, rb;\n\t" \
+        "mov.b64 {%0, %1}, rd;\n\t}"                                                                          \
+        : "=f"(d.x), "=f"(d.y)                                                                                 \
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                             \
+    return d;                                                                                                  \
+  }
+PG_F2OP(f2mul, "mul.rn.f32x2")
+PG_F2OP(f2add, "add.rn.f32x2")
+#undef PG_F2OP
+
 // CTAs per SM asked of the register allocator: the per-thread constants and
 // sums take about 1 + 6K + 2KJ registers, plus K of per-site temporaries
 constexpr uint32_t calib_min_blocks(uint32_t K, uint32_t J) {
@@ -103,16 +126,28 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
     reinterpret_cast<float4*>(s_sig)[x] = reinterpret_cast<const float4*>(a.sig_rows)[x];
   for (uint32_t x = threadIdx.x; x < 3 * K + K * J; x += CAL_THREADS) s_row[x] = a.tab[uint64_t(r) * a.tab_stride + x];
   __syncthreads();
-  float cst[K], lv[K], l1v[K], w[K * J];
+  // epochs in pairs (packed f32x2 arithmetic); an odd K gets a padding
+  // epoch of weight exp(-inf) = 0
+  constexpr uint32_t KH = (K + 1) / 2;
+  float2 cst[KH], lv[KH], l1v[KH], w[J][KH];
+  auto at = [&](uint32_t k, uint32_t off, float pad) { return k < K ? s_row[off + k] : pad; };
 #pragma unroll
-  for (uint32_t k = 0; k < K; ++k) {
-    cst[k] = s_row[k]; lv[k] = s_row[K + k]; l1v[k] = s_row[2 * K + k];
+  for (uint32_t h = 0; h < KH; ++h) {
+    cst[h] = make_float2(at(2 * h, 0, 0.f), at(2 * h + 1, 0, -INFINITY));
+    lv[h] = make_float2(at(2 * h, K, 0.f), at(2 * h + 1, K, 0.f));
+    l1v[h] = make_float2(at(2 * h, 2 * K, 0.f), at(2 * h + 1, 2 * K, 0.f));
 #pragma unroll
-    for (uint32_t j = 0; j < J; ++j) w[k * J + j] = s_row[3 * K + k * J + j];
+    for (uint32_t j = 0; j < J; ++j)
+      w[j][h] = make_float2(s_row[3 * K + 2 * h * J + j], 2 * h + 1 < K ? s_row[3 * K + (2 * h + 1) * J + j] : 0.f);
   }
-  float acc[NV];
+  float nll = 0.f;
+  float2 A[KH], B[KH], G[KH], H[J][KH];
 #pragma unroll
-  for (uint32_t q = 0; q < NV; ++q) acc[q] = 0.f;
+  for (uint32_t h = 0; h < KH; ++h) {
+    A[h] = B[h] = G[h] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (uint32_t j = 0; j < J; ++j) H[j][h] = make_float2(0.f, 0.f);
+  }
   auto site = [&](float al, float dl, int32_t c) {
     float sg[JP];
 #pragma unroll
@@ -120,32 +155,37 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
       const float4 x = *reinterpret_cast<const float4*>(s_sig + c * JP + j);
       sg[j] = x.x; sg[j + 1] = x.y; sg[j + 2] = x.z; sg[j + 3] = x.w;
     }
-    float u[K], umax = -INFINITY;
+    const float2 al2 = make_float2(al, al), dal2 = make_float2(dl - al, dl - al);
+    float2 u[KH], m[KH];
+    float umax = -INFINITY;
 #pragma unroll
-    for (uint32_t k = 0; k < K; ++k) {
-      u[k] = cst[k] + al * lv[k] + (dl - al) * l1v[k];
-      umax = fmaxf(umax, u[k]);
+    for (uint32_t h = 0; h < KH; ++h) {
+      u[h] = f2fma(dal2, l1v[h], f2fma(al2, lv[h], cst[h]));
+      umax = fmaxf(umax, fmaxf(u[h].x, u[h].y));
+      m[h] = f2mul(w[0][h], make_float2(sg[0], sg[0]));
+#pragma unroll
+      for (uint32_t j = 1; j < J; ++j) m[h] = f2fma(w[j][h], make_float2(sg[j], sg[j]), m[h]);
     }
-    float e[K], q[K], sum = 0.f;
+    float2 e[KH], q[KH];
+    float sum = 0.f;
 #pragma unroll
-    for (uint32_t k = 0; k < K; ++k) {
-      float m = 0.f;
-#pragma unroll
-      for (uint32_t j = 0; j < J; ++j) m += w[k * J + j] * sg[j];
-      e[k] = __expf(u[k] - umax);
-      q[k] = fmaxf(m, 1e-30f) * e[k];
-      sum += q[k];
+    for (uint32_t h = 0; h < KH; ++h) {
+      e[h] = make_float2(__expf(u[h].x - umax), __expf(u[h].y - umax));
+      q[h] = f2mul(make_float2(fmaxf(m[h].x, 1e-30f), fmaxf(m[h].y, 1e-30f)), e[h]);
+      sum += q[h].x;
+      sum += q[h].y;
     }
     const float inv = __fdividef(1.f, sum);
-    acc[0] -= umax + __logf(sum);
+    nll -= umax + __logf(sum);
+    const float2 inv2 = make_float2(inv, inv);
 #pragma unroll
-    for (uint32_t k = 0; k < K; ++k) {
-      const float g = q[k] * inv, h = e[k] * inv;
-      acc[1 + k] += g * al;
-      acc[1 + K + k] += g * (dl - al);
-      acc[1 + 2 * K + k] += g;
+    for (uint32_t h = 0; h < KH; ++h) {
+      const float2 g = f2mul(q[h], inv2), r = f2mul(e[h], inv2);
+      A[h] = f2fma(g, al2, A[h]);
+      B[h] = f2fma(g, dal2, B[h]);
+      G[h] = f2add(G[h], g);
 #pragma unroll
-      for (uint32_t j = 0; j < J; ++j) acc[1 + 3 * K + k * J + j] += h * sg[j];
+      for (uint32_t j = 0; j < J; ++j) H[j][h] = f2fma(r, make_float2(sg[j], sg[j]), H[j][h]);
     }
   };
   uint64_t i = i0 + threadIdx.x;
@@ -163,6 +203,17 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
   }
   for (; i < i1; i += CAL_THREADS) site(float(__ldg(a.alt + i)), float(__ldg(a.depth + i)), __ldg(a.cls + i));
   // block partial: warp trees, then a compensated sum over the warps
+  float acc[NV];
+  acc[0] = nll;
+#pragma unroll
+  for (uint32_t k = 0; k < K; ++k) {
+    const bool hi = k & 1;
+    acc[1 + k] = hi ? A[k / 2].y : A[k / 2].x;
+    acc[1 + K + k] = hi ? B[k / 2].y : B[k / 2].x;
+    acc[1 + 2 * K + k] = hi ? G[k / 2].y : G[k / 2].x;
+#pragma unroll
+    for (uint32_t j = 0; j < J; ++j) acc[1 + 3 * K + k * J + j] = hi ? H[j][k / 2].y : H[j][k / 2].x;
+  }
 #pragma unroll
   for (uint32_t q = 0; q < NV; ++q) {
     float v = acc[q];
