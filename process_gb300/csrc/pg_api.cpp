@@ -59,6 +59,8 @@ pg_status guarded(F&& f) {
 }
 
 void require(bool c, const std::string& msg) { if (!c) throw DomainError(msg); }
+// literal messages: no string is built unless the check fails
+void require(bool c, const char* msg) { if (!c) throw DomainError(msg); }
 
 // ---------------------------------------------------------------- device memory
 // A small caching pool: freed blocks are kept per engine and reused by size,
@@ -374,23 +376,28 @@ uint32_t code_of(char c) {
 
 // Euler intervals of the forest (preorder index, subtree end)
 void euler(pg_forest& f) {
-  std::vector<std::vector<uint32_t>> kids(f.n);
+  // children in CSR form, each node's in increasing index order
+  std::vector<uint32_t> koff(f.n + 1, 0), kids(f.n), fill;
   std::vector<uint32_t> roots;
   for (uint32_t v = 0; v < f.n; ++v) {
-    if (f.parent[v] < 0) roots.push_back(v); else kids[f.parent[v]].push_back(v);
+    if (f.parent[v] < 0) roots.push_back(v); else ++koff[f.parent[v] + 1];
   }
+  for (uint32_t v = 0; v < f.n; ++v) koff[v + 1] += koff[v];
+  fill.assign(koff.begin(), koff.end() - 1);
+  for (uint32_t v = 0; v < f.n; ++v)
+    if (f.parent[v] >= 0) kids[fill[f.parent[v]]++] = v;
   f.tin.assign(f.n, 0); f.tout.assign(f.n, 0);
   uint32_t clock = 0;
-  std::vector<std::pair<uint32_t, uint32_t>> stack;  // node, next child
+  std::vector<std::pair<uint32_t, uint32_t>> stack;  // node, next child position
   for (uint32_t r : roots) {
-    stack.push_back({r, 0});
+    stack.push_back({r, koff[r]});
     f.tin[r] = clock++;
     while (!stack.empty()) {
       auto& top = stack.back();
-      if (top.second < kids[top.first].size()) {
-        const uint32_t c = kids[top.first][top.second++];
+      if (top.second < koff[top.first + 1]) {
+        const uint32_t c = kids[top.second++];
         f.tin[c] = clock++;
-        stack.push_back({c, 0});
+        stack.push_back({c, koff[c]});
       } else {
         f.tout[top.first] = clock;
         stack.pop_back();
@@ -399,7 +406,7 @@ void euler(pg_forest& f) {
   }
   f.leaves.assign(f.n_samples, {});
   for (uint32_t v = 0; v < f.n; ++v) {
-    if (kids[v].empty() && f.sample[v] >= 0) f.leaves[f.sample[v]].push_back(f.tin[v]);
+    if (koff[v] == koff[v + 1] && f.sample[v] >= 0) f.leaves[f.sample[v]].push_back(f.tin[v]);
   }
 }
 
@@ -1513,8 +1520,10 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
     require(T >= 64 && T <= (1u << 24), "tile_size must be in [64, 2^24]");
     // ---- tiles
     // tiles are laid out on the device from the per-chromosome table
-    std::vector<uint32_t> c_ntiles, c_nstarts, c_id, c_first, c_depth, c_start, c_end, b_slot, b_index;
-    std::vector<uint64_t> c_pairs;
+    std::vector<uint32_t> c_ntiles, c_nstarts, c_id, c_first, c_depth, c_start, c_end;
+    std::vector<uint64_t> c_pairs, heap_base;   // per chromosome: its split tree's heap (2^(depth + 1) entries)
+    uint64_t heap_total = 0;
+    uint32_t max_depth = 0;
     uint32_t n_tiles = 0;
     const double mates = paired ? 2.0 : 1.0;
     uint64_t frags_per_sample = 0;
@@ -1532,8 +1541,9 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
       c_first.push_back(n_tiles); c_depth.push_back(D);
       c_start.push_back(e->chr_off[ci]); c_end.push_back(e->chr_off[ci] + L);
       frags_per_sample += pairs;
-      const uint32_t blk = 1u << std::min<uint32_t>(D, 6);
-      for (uint32_t b = 0; b * blk < nt; ++b) { b_slot.push_back(slot); b_index.push_back(b); }
+      heap_base.push_back(heap_total);
+      heap_total += uint64_t(2) << D;
+      max_depth = std::max(max_depth, D);
       require(uint64_t(n_tiles) + nt < (uint64_t(1) << 31), "too many tiles");
       n_tiles += nt;
     }
@@ -1651,7 +1661,7 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
       pg::seq_make_tiles(uint32_t(c_first.size()), cf.p, cn.p, cs.p, cns.p, cen.p, T, n_tiles, ts_d.p, tl_d.p,
                          te_d.p, st);
     }
-    auto bs_d = upload(P, b_slot, st), bi_d = upload(P, b_index, st);
+    auto hb_d = upload(P, heap_base, st);
     auto cnt_d = upload(P, c_ntiles, st), cns_d = upload(P, c_nstarts, st), cid_d = upload(P, c_id, st);
     auto cf_d = upload(P, c_first, st), cd_d = upload(P, c_depth, st);
     auto cp_d = upload(P, c_pairs, st);
@@ -1693,9 +1703,10 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
       ocls_d = upload(P, opt_class, st); oloff_d = upload(P, opt_leaf_off, st); onl_d = upload(P, opt_nleaf, st);
       cltin_d = upload(P, cls_leaf_tin, st); ocdf_d = upload(P, opt_cdf, st);
     }
-    pg::seq_tile_counts(uint32_t(samples.size()), uint32_t(b_slot.size()), bs_d.p, bi_d.p, cf_d.p, cnt_d.p, cd_d.p,
-                        cns_d.p, cid_d.p, cp_d.p, T, n_tiles, pl->has_cna ? mcum_d.p : nullptr,
-                        pl->has_cna ? mtot_d.p : nullptr, uint32_t(c_id.size()), seed, pair_cnt.p, st);
+    DBuf<uint32_t> heap(P, heap_total * samples.size());
+    pg::seq_tile_counts(uint32_t(samples.size()), uint32_t(c_id.size()), max_depth, cf_d.p, cnt_d.p, cd_d.p, cns_d.p,
+                        cid_d.p, cp_d.p, hb_d.p, heap_total, heap.p, T, n_tiles, pl->has_cna ? mcum_d.p : nullptr,
+                        pl->has_cna ? mtot_d.p : nullptr, seed, pair_cnt.p, st);
     pg::seq_tile_ranges(recs.p, uint32_t(pl->M), ts_d.p, tl_d.p, n_tiles, span, rlo.p, rhi.p, st);
     pg::SeqTiles tiles{n_tiles, ts_d.p, tl_d.p, te_d.p, rlo.p, rhi.p};
     pg::SeqParams prm{};

@@ -303,16 +303,19 @@ void seq_build_records(const PlaceOut& sorted, uint32_t n, const uint32_t* edge_
 void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start, const uint32_t* len,
                      uint32_t n_tiles, uint32_t span, uint32_t* rlo, uint32_t* rhi, cudaStream_t st);
 // per (sample, tile) pair counts: multinomial split of each chromosome's
-// pair count over its tiles by a binary tree of binomial draws, one thread
-// per (sample, block of 64 tiles).  Tiles weigh their number of start
-// positions, or (mass_cum != NULL) their DNA mass: mass_cum[s * n_tiles + t]
-// is the sample's mass of the chromosome's tiles before t and
+// pair count over its tiles by a binary tree of binomial draws, one launch
+// per tree level (max_depth of them) with the node counts in `heap`
+// (heap_total entries per sample; chromosome slot's heap at heap_base[slot],
+// 2^(depth + 1) entries).  Tiles weigh their number of start positions, or
+// (mass_cum != NULL) their DNA mass: mass_cum[s * n_tiles + t] is the
+// sample's mass of the chromosome's tiles before t and
 // mass_tot[s * n_slots + slot] the chromosome's total.
-void seq_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* blk_slot, const uint32_t* blk_index,
-                     const uint32_t* chr_first_tile, const uint32_t* chr_ntiles, const uint32_t* chr_depth,
-                     const uint32_t* chr_nstarts, const uint32_t* chr_id, const uint64_t* chr_pairs,
-                     uint32_t tile_size, uint32_t n_tiles, const double* mass_cum, const double* mass_tot,
-                     uint32_t n_slots, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st);
+void seq_tile_counts(uint32_t n_samples, uint32_t n_slots, uint32_t max_depth, const uint32_t* chr_first_tile,
+                     const uint32_t* chr_ntiles, const uint32_t* chr_depth, const uint32_t* chr_nstarts,
+                     const uint32_t* chr_id, const uint64_t* chr_pairs, const uint64_t* heap_base,
+                     uint64_t heap_total, uint32_t* heap, uint32_t tile_size, uint32_t n_tiles,
+                     const double* mass_cum, const double* mass_tot, uint64_t seed, uint32_t* pair_cnt,
+                     cudaStream_t st);
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
                const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st);

@@ -169,17 +169,42 @@ __device__ __forceinline__ void tile_counts_one(uint32_t s, uint32_t bi, const u
   }
 }
 
-__global__ void k_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* __restrict__ blk_slot,
-                              const uint32_t* __restrict__ blk_index, const uint32_t* __restrict__ chr_first_tile,
-                              const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
-                              const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
-                              const uint64_t* __restrict__ chr_pairs, uint32_t T, uint32_t n_tiles,
-                              const double* __restrict__ mass_cum, const double* __restrict__ mass_tot,
-                              uint32_t n_slots, Key key, uint32_t* __restrict__ pair_cnt) {
-  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (gid >= uint64_t(n_blocks) * n_samples) return;
-  tile_counts_one(uint32_t(gid / n_blocks), uint32_t(gid % n_blocks), blk_slot, blk_index, chr_first_tile, chr_ntiles,
-                  chr_depth, chr_nstarts, chr_id, chr_pairs, T, n_tiles, mass_cum, mass_tot, n_slots, key, pair_cnt);
+// Level-synchronous form of the same tree (the plain path): one launch per
+// level, one thread per (sample, chromosome, node of the level) whose range
+// meets the chromosome's tiles; node counts live in a per-(sample,
+// chromosome) heap in global memory.  Every node draws with its own heap id,
+// as in tile_counts_one, so the counts are the same.
+__global__ void k_tile_split_level(uint32_t level, uint32_t n_slots, const uint32_t* __restrict__ chr_first_tile,
+                                   const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
+                                   const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
+                                   const uint64_t* __restrict__ chr_pairs, const uint64_t* __restrict__ heap_base,
+                                   uint64_t heap_total, uint32_t T, uint32_t n_tiles,
+                                   const double* __restrict__ mass_cum, const double* __restrict__ mass_tot, Key key,
+                                   uint32_t* __restrict__ heap, uint32_t* __restrict__ pair_cnt) {
+  const uint32_t s = blockIdx.z, slot = blockIdx.y;
+  const uint32_t D = chr_depth[slot], nt = chr_ntiles[slot], first = chr_first_tile[slot];
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint32_t* cnt = pair_cnt + uint64_t(s) * n_tiles + first;
+  if (D == 0) {   // one tile: it takes every pair
+    if (level == 0 && i == 0) cnt[0] = uint32_t(chr_pairs[slot]);
+    return;
+  }
+  if (level >= D || i >= (uint64_t(1) << level)) return;
+  const uint64_t size = uint64_t(1) << (D - level), lo = i * size;
+  if (lo >= nt) return;
+  const TileSplit sp{chr_nstarts[slot], T, nt, mass_cum ? mass_cum + uint64_t(s) * n_tiles + first : nullptr,
+                     mass_cum ? mass_tot[uint64_t(s) * n_slots + slot] : 0.0};
+  uint32_t* hp = heap + uint64_t(s) * heap_total + heap_base[slot];
+  const uint32_t h = uint32_t((uint64_t(1) << level) + i);
+  const uint64_t n = level == 0 ? chr_pairs[slot] : hp[h];
+  const uint64_t nl = sp.left(key, h, chr_id[slot], s, n, lo, lo + (size >> 1), lo + size);
+  if (level + 1 == D) {   // the children are tiles lo and lo + 1
+    cnt[lo] = uint32_t(nl);
+    if (lo + 1 < nt) cnt[lo + 1] = uint32_t(n - nl);
+  } else {
+    hp[2 * h] = uint32_t(nl);
+    hp[2 * h + 1] = uint32_t(n - nl);
+  }
 }
 
 // error word of the visit of mate `mate` of a fragment (Philox word w) to `locus`
@@ -924,16 +949,21 @@ void seq_tile_ranges(const SeqRec* recs, uint32_t n_recs, const uint32_t* start,
   if (n_tiles) { k_tile_ranges<<<nblk(n_tiles), 256, 0, st>>>(recs, n_recs, start, len, n_tiles, span, rlo, rhi); note_launch(); }
 }
 
-void seq_tile_counts(uint32_t n_samples, uint32_t n_blocks, const uint32_t* blk_slot, const uint32_t* blk_index,
-                     const uint32_t* chr_first_tile, const uint32_t* chr_ntiles, const uint32_t* chr_depth,
-                     const uint32_t* chr_nstarts, const uint32_t* chr_id, const uint64_t* chr_pairs,
-                     uint32_t tile_size, uint32_t n_tiles, const double* mass_cum, const double* mass_tot,
-                     uint32_t n_slots, uint64_t seed, uint32_t* pair_cnt, cudaStream_t st) {
-  const uint64_t n = uint64_t(n_samples) * n_blocks;
-  if (n) { k_tile_counts<<<nblk(n, 64), 64, 0, st>>>(n_samples, n_blocks, blk_slot, blk_index, chr_first_tile,
-                                                   chr_ntiles, chr_depth, chr_nstarts, chr_id, chr_pairs, tile_size,
-                                                   n_tiles, mass_cum, mass_tot, n_slots, make_key(seed), pair_cnt);
-           note_launch(); }
+void seq_tile_counts(uint32_t n_samples, uint32_t n_slots, uint32_t max_depth, const uint32_t* chr_first_tile,
+                     const uint32_t* chr_ntiles, const uint32_t* chr_depth, const uint32_t* chr_nstarts,
+                     const uint32_t* chr_id, const uint64_t* chr_pairs, const uint64_t* heap_base,
+                     uint64_t heap_total, uint32_t* heap, uint32_t tile_size, uint32_t n_tiles,
+                     const double* mass_cum, const double* mass_tot, uint64_t seed, uint32_t* pair_cnt,
+                     cudaStream_t st) {
+  if (n_samples == 0 || n_slots == 0) return;
+  const Key key = make_key(seed);
+  for (uint32_t level = 0; level < std::max<uint32_t>(max_depth, 1); ++level) {
+    const dim3 grid(nblk(uint64_t(1) << level, 128), n_slots, n_samples);
+    k_tile_split_level<<<grid, 128, 0, st>>>(level, n_slots, chr_first_tile, chr_ntiles, chr_depth, chr_nstarts,
+                                             chr_id, chr_pairs, heap_base, heap_total, tile_size, n_tiles, mass_cum,
+                                             mass_tot, key, heap, pair_cnt);
+    note_launch();
+  }
 }
 
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
