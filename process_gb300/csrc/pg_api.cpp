@@ -1097,21 +1097,43 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), uint32_t(n_snv + n_id), st);
     // ---- infinite sites, and loci drawn where the cell has no allele left
     if ((e->infinite_sites || pl->has_cna) && n_snv + n_id > 0) {
-      uint32_t cap = 1024;
-      while (cap < 2 * n_all) cap <<= 1;
       const bool unique = e->infinite_sites;
-      DBuf<uint32_t> hkeys(P, unique ? cap : 1), ckeys(P, unique ? cap : 1), cvals(P, unique ? cap : 1);
       DBuf<uint32_t> pend_a(P, n_snv + n_id), pend_b(P, n_snv + n_id);
       DBuf<uint8_t> lost(P, n_snv + n_id);
       DBuf<uint32_t> n_next(P, 1);
-      if (unique) {
-        ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-        // drivers occupy their loci first
-        pg::sites_insert_accepted(hkeys.p, cap - 1, locus.p + n_snv + n_id, uint32_t(drv.size()), st);
-      }
       const uint32_t* pending = nullptr;
       uint32_t n_pend = uint32_t(n_snv + n_id);
       uint32_t* next = pend_a.p;
+      int round = 0;
+      // infinite sites: the first round over all slots against one table of
+      // its candidates (drivers first); the later rounds' tables are sized
+      // by what it leaves pending
+      DBuf<unsigned long long> first;
+      uint32_t fmask = 0;
+      if (unique) {
+        uint64_t fcap = 1024;
+        while (fcap < 2 * n_all) fcap <<= 1;
+        require(fcap <= (uint64_t(1) << 32), "too many mutations for one placement call");
+        first = DBuf<unsigned long long>(P, fcap);
+        fmask = uint32_t(fcap - 1);
+        ck(cudaMemsetAsync(first.p, 0xff, sizeof(unsigned long long) * fcap, st), "memset");
+        ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
+        pg::sites_first_round(locus.p, n_pend, locus.p + n_snv + n_id, uint32_t(drv.size()), first.p, fmask, next,
+                              n_next.p, err.p, st);
+        uint32_t nn = 0;
+        ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+        ck(cudaStreamSynchronize(st), "first round");
+        if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, nn, 1,
+                                           err.p, st);
+        pending = next;
+        next = pend_b.p;
+        n_pend = nn;
+        round = 1;
+      }
+      uint32_t cap = 1024;
+      while (cap < 2 * uint64_t(n_pend)) cap <<= 1;
+      DBuf<uint32_t> hkeys(P, unique ? cap : 1), ckeys(P, unique ? cap : 1), cvals(P, unique ? cap : 1);
+      if (unique) ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
       // Rounds with many pending slots read their count on the host; below
       // ROUND_TAIL pending slots, groups of ROUND_GROUP rounds run with the
       // counts in device memory (the grids sized by the group's first count,
@@ -1119,7 +1141,6 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
       constexpr uint32_t ROUND_TAIL = 1u << 20;
       constexpr int ROUND_GROUP = 16;
       DBuf<uint32_t> counts(P, ROUND_GROUP);
-      int round = 0;
       while (n_pend > 0) {
         require(round < 256, unique ? "infinite sites model: no free locus left for some mutations"
                                     : "no allele left where some mutations were drawn");
@@ -1129,7 +1150,7 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
             ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
             ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
             pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
-                            n_next.p, err.p, st);
+                            n_next.p, err.p, st, nullptr, first.p, fmask);
           } else {
             pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_next.p, st);
           }
@@ -1154,7 +1175,7 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
             ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
             ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
             pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, ctail - 1, lost.p, next,
-                            n_out, err.p, st, n_dev);
+                            n_out, err.p, st, n_dev, first.p, fmask);
           } else {
             pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_out, st, n_dev);
           }

@@ -112,10 +112,18 @@ void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint
 // slots whose locus is invalid (no allele covers the drawn position) -> next list
 void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
                            uint32_t* n_next, cudaStream_t st, const uint32_t* n_dev = nullptr);
-void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st);
+// first infinite-sites round over slots [0, n) and the drivers' loci:
+// `first` (fmask + 1 entries of 64 bits, all ones) ends holding the taken
+// loci; the losing slots go to next
+void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
+                       unsigned long long* first, uint32_t fmask, uint32_t* next, uint32_t* n_next, uint32_t* err,
+                       cudaStream_t st);
+// a later round: a locus is taken when it is in the accepted set hkeys or
+// (first != NULL) in the first round's table
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
                  uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev = nullptr);
+                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev = nullptr,
+                 const unsigned long long* first = nullptr, uint32_t fmask = 0);
 uint32_t sort_num_buckets(uint64_t G);
 void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,
                    uint32_t* order, const PlaceOut& sorted, cudaStream_t st);

@@ -222,21 +222,79 @@ __device__ __forceinline__ uint32_t hset_insert(uint32_t* __restrict__ keys, uin
   return EMPTY;
 }
 
-__global__ void k_insert_accepted(uint32_t* __restrict__ hkeys, uint32_t hmask, const uint32_t* __restrict__ loci,
-                                  uint32_t n) {
+
+// The first infinite-sites round over every slot, against one table of all
+// its candidates: an entry is (locus << 32 | code), code 0 for a driver's
+// locus and slot + 1 for a passenger's, and a locus keeps the smallest code.
+// A passenger wins its locus when the entry holds its own code, i.e. when no
+// driver and no smaller slot drew it: the rule of the later rounds (the
+// smallest pending slot wins a free locus).  The table then holds exactly
+// the taken loci (drivers and the round's winners), so the later rounds test
+// it instead of inserting the winners into the accepted set.
+constexpr unsigned long long FIRST_EMPTY = ~0ull;
+
+__device__ __forceinline__ void first_insert(unsigned long long* __restrict__ tab, uint32_t mask, uint32_t k,
+                                             uint32_t code, uint32_t* __restrict__ err) {
+  const unsigned long long mine = (static_cast<unsigned long long>(k) << 32) | code;
+  uint32_t h = hash32(k) & mask;
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    unsigned long long x = tab[h];
+    if (x == FIRST_EMPTY) {
+      x = atomicCAS(tab + h, FIRST_EMPTY, mine);
+      if (x == FIRST_EMPTY) return;
+    }
+    if (uint32_t(x >> 32) == k) { if (x > mine) atomicMin(tab + h, mine); return; }
+    h = (h + 1) & mask;
+  }
+  atomicOr(err, ERR_CAPACITY);
+}
+
+// the entry of locus k, or FIRST_EMPTY
+__device__ __forceinline__ unsigned long long first_find(const unsigned long long* __restrict__ tab, uint32_t mask,
+                                                         uint32_t k) {
+  uint32_t h = hash32(k) & mask;
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const unsigned long long x = tab[h];
+    if (x == FIRST_EMPTY || uint32_t(x >> 32) == k) return x;
+    h = (h + 1) & mask;
+  }
+  return FIRST_EMPTY;
+}
+
+__global__ void k_first_insert(const uint32_t* __restrict__ locus, uint32_t n, const uint32_t* __restrict__ drv_locus,
+                               uint32_t n_drv, unsigned long long* __restrict__ tab, uint32_t mask,
+                               uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) hset_insert(hkeys, hmask, loci[i]);
+  if (i < n_drv) first_insert(tab, mask, drv_locus[i], 0u, err);
+  if (i >= n) return;
+  const uint32_t k = locus[i];
+  if (k != LOCUS_INVALID) first_insert(tab, mask, k, i + 1, err);
+}
+
+__global__ void k_first_resolve(const uint32_t* __restrict__ locus, uint32_t n,
+                                const unsigned long long* __restrict__ tab, uint32_t mask,
+                                uint32_t* __restrict__ next, uint32_t* __restrict__ n_next) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = locus[i];
+  const bool win = k != LOCUS_INVALID && uint32_t(first_find(tab, mask, k)) == i + 1;
+  if (!win) next[atomicAdd(n_next, 1u)] = i;
 }
 
 __global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
                               const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ hkeys, uint32_t hmask,
+                              const unsigned long long* __restrict__ first, uint32_t fmask,
                               uint32_t* __restrict__ ckeys, uint32_t* __restrict__ cvals, uint32_t cmask,
                               uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (n_dev ? *n_dev : n)) return;
   const uint32_t slot = pending ? pending[i] : i;
   const uint32_t k = locus[slot];
-  if (k == LOCUS_INVALID || hset_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
+  if (k == LOCUS_INVALID || hset_contains(hkeys, hmask, k) ||
+      (first && first_find(first, fmask, k) != FIRST_EMPTY)) {
+    lost[i] = 1;
+    return;
+  }
   lost[i] = 0;
   const uint32_t h = hset_insert(ckeys, cmask, k);
   if (h == EMPTY) { atomicOr(err, ERR_CAPACITY); return; }
@@ -511,15 +569,22 @@ void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint3
   if (n) { k_collect_invalid<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, next, n_next); note_launch(); }
 }
 
-void sites_insert_accepted(uint32_t* hkeys, uint32_t hmask, const uint32_t* loci, uint32_t n, cudaStream_t st) {
-  if (n) { k_insert_accepted<<<nblk(n), 256, 0, st>>>(hkeys, hmask, loci, n); note_launch(); }
+void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
+                       unsigned long long* first, uint32_t fmask, uint32_t* next, uint32_t* n_next, uint32_t* err,
+                       cudaStream_t st) {
+  if (n == 0 && n_drv == 0) return;
+  k_first_insert<<<nblk(std::max(n, n_drv)), 256, 0, st>>>(locus, n, drv_locus, n_drv, first, fmask, err);
+  note_launch();
+  if (n) { k_first_resolve<<<nblk(n), 256, 0, st>>>(locus, n, first, fmask, next, n_next); note_launch(); }
 }
 
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
                  uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev) {
+                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev, const unsigned long long* first,
+                 uint32_t fmask) {
   if (n == 0) return;
-  k_cand_insert<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, ckeys, cvals, cmask, lost, err);
+  k_cand_insert<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, first, fmask, ckeys, cvals, cmask,
+                                         lost, err);
   k_cand_resolve<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, ckeys, cvals, cmask, lost, next,
                                           n_next, err);
   note_launch(2);
