@@ -1235,8 +1235,11 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
       struct Part { uint32_t start, len, atom; };
       std::vector<std::vector<Part>> parts(nt);
       std::vector<std::vector<uint32_t>> part_thr(nt);
+      // the mass before each tile is the mass of the exact integer copy sums
+      // before it
       std::vector<double> cum(nt, 0.0);
       double tot = 0.0;
+      uint64_t cum_i0 = 0, cum_s = 0;
       if (pl.has_cna) {
         const SampleCn& q = scn[smp];
         const auto& as = pl.atom_start;
@@ -1255,9 +1258,11 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
             pw.push_back(q.mass(len * q.icnt0[x], len * q.S[x]));
           }
           if (pw.size() > 1) part_thr[k] = thresholds(pw);
-          cum[k] = tot;
-          tot = tot + q.mass(i0, sum);
+          cum[k] = q.mass(cum_i0, cum_s);
+          cum_i0 += i0;
+          cum_s += sum;
         }
+        tot = q.mass(cum_i0, cum_s);
       }
       // multinomial split by a binary tree over the padded tile range
       // [0, 2^D): node h covering [lo, lo+size) sends Binomial(n, w_left/w)

@@ -1199,7 +1199,9 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     pl->cls = DBuf<uint8_t>(P, n_all); pl->sig = DBuf<uint8_t>(P, n_all); pl->allele = DBuf<uint16_t>(P, n_all);
     pl->seq = DBuf<uint16_t>(P, n_all);
     pl->kind = DBuf<uint8_t>(P, n_all); pl->nature = DBuf<uint8_t>(P, n_all);
-    pg::sort_by_locus(o, uint32_t(n_all), e->G, bcnt.p, bfill.p, bpart.p, order.p, pl->view(), st);
+    DBuf<unsigned long long> skeys(P, n_all);
+    DBuf<uint4> recs(P, 2 * n_all);   // 32-byte records of the gather
+    pg::sort_by_locus(o, uint32_t(n_all), e->G, bcnt.p, bfill.p, bpart.p, order.p, pl->view(), skeys.p, recs.p, st);
     pl->kernel_ms = timer.stop();
     ck(cudaGetLastError(), "placement kernels");
     uint32_t err_h = 0;
@@ -1717,9 +1719,9 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
       auto cf_d2 = upload(P, c_first, st), cn_d2 = upload(P, c_ntiles, st);
       mcum_d = DBuf<double>(P, uint64_t(NS) * n_tiles);
       mtot_d = DBuf<double>(P, uint64_t(NS) * c_id.size());
-      DBuf<double> tmass(P, uint64_t(NS) * n_tiles);
+      DBuf<uint64_t> tsums(P, 2 * uint64_t(NS) * n_tiles);
       pg::seq_tile_mass(NS, uint32_t(c_id.size()), cf_d2.p, cn_d2.p, poff_d.p, plen_d.p, patom_d.p, NA, wn_d.p,
-                        wt_d.p, nl_d.p, i0_d.p, cs_d.p, n_tiles, n_parts_cap, tmass.p, mcum_d.p, mtot_d.p, pcdf_d.p,
+                        wt_d.p, nl_d.p, i0_d.p, cs_d.p, n_tiles, n_parts_cap, tsums.p, mcum_d.p, mtot_d.p, pcdf_d.p,
                         st);
       ocls_d = upload(P, opt_class, st); oloff_d = upload(P, opt_leaf_off, st); onl_d = upload(P, opt_nleaf, st);
       cltin_d = upload(P, cls_leaf_tin, st); ocdf_d = upload(P, opt_cdf, st);

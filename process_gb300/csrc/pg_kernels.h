@@ -125,8 +125,11 @@ void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uin
                  uint32_t* err, cudaStream_t st, const uint32_t* n_dev = nullptr,
                  const unsigned long long* first = nullptr, uint32_t fmask = 0);
 uint32_t sort_num_buckets(uint64_t G);
+// sort by (locus, slot) into `sorted`; keys: n 64-bit keys, recs: 2n
+// 16-byte words (the 32-byte records of the gather)
 void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,
-                   uint32_t* order, const PlaceOut& sorted, cudaStream_t st);
+                   uint32_t* order, const PlaceOut& sorted, unsigned long long* keys, uint4* recs,
+                   cudaStream_t st);
 
 // ---------------------------------------------------------------- sequencing
 struct SeqRec {            // 16 B, one per placed mutation, sorted by locus
@@ -206,18 +209,19 @@ void seq_tile_parts(uint32_t n_tiles, const uint32_t* tile_start, const uint32_t
                     const uint32_t* atom_start, uint32_t n_atoms, uint32_t genome_len, uint32_t* part_off,
                     uint32_t* scan_part, uint32_t* part_start, uint32_t* part_len, uint32_t* part_atom,
                     cudaStream_t st);
-// Per (sample, tile) its mass (scratch tile_mass, n_samples * n_tiles) and,
-// for tiles of several parts, the thresholds of the part draw
-// (part_cdf[s * n_parts + part]); then per (sample, chromosome slot),
-// summed in tile order, the mass before each tile (mass_cum[s * n_tiles + t])
-// and the slot's total (mass_tot[s * n_slots + slot]).  A stretch with integer
-// copy sums (I0, S) weighs wn * I0 + (wt / nl) * S (the second term when
-// nl > 0); icnt0 / copy_sum are per (sample, atom).
+// Per (sample, tile) its integer copy sums (I0, S) (scratch tile_sums,
+// 2 * n_samples * n_tiles) and, for tiles of several parts, the thresholds
+// of the part draw (part_cdf[s * n_parts + part]); then per (sample,
+// chromosome slot) the mass before each tile (mass_cum[s * n_tiles + t]) and
+// the slot's total (mass_tot[s * n_slots + slot]), each the mass of the
+// exact integer sums before it.  A stretch with integer copy sums (I0, S)
+// weighs wn * I0 + (wt / nl) * S (the second term when nl > 0);
+// icnt0 / copy_sum are per (sample, atom).
 void seq_tile_mass(uint32_t n_samples, uint32_t n_slots, const uint32_t* c_first, const uint32_t* c_ntiles,
                    const uint32_t* part_off, const uint32_t* part_len, const uint32_t* part_atom, uint32_t n_atoms,
                    const double* wn, const double* wt, const uint64_t* nl, const uint64_t* icnt0,
-                   const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, double* tile_mass, double* mass_cum,
-                   double* mass_tot, uint32_t* part_cdf, cudaStream_t st);
+                   const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, uint64_t* tile_sums,
+                   double* mass_cum, double* mass_tot, uint32_t* part_cdf, cudaStream_t st);
 // ---------------------------------------------------------------- SAM records
 // One aligned read as the SAM writer needs it; the host formats the text.
 constexpr uint32_t SAM_MAX_CIGAR = 16;

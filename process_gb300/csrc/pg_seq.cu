@@ -835,8 +835,8 @@ __global__ void k_tile_mass(uint32_t n_samples, uint32_t n_tiles, const uint32_t
                             const uint32_t* __restrict__ part_len, const uint32_t* __restrict__ part_atom,
                             uint32_t n_atoms, const double* __restrict__ wn_s, const double* __restrict__ wt_s,
                             const uint64_t* __restrict__ nl_s, const uint64_t* __restrict__ icnt0,
-                            const uint64_t* __restrict__ copy_sum, uint32_t n_parts, double* __restrict__ tile_mass,
-                            uint32_t* __restrict__ part_cdf) {
+                            const uint64_t* __restrict__ copy_sum, uint32_t n_parts, uint64_t* __restrict__ tile_i0,
+                            uint64_t* __restrict__ tile_s, uint32_t* __restrict__ part_cdf) {
   const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (gid >= uint64_t(n_samples) * n_tiles) return;
   const uint32_t s = uint32_t(gid / n_tiles), t = uint32_t(gid % n_tiles);
@@ -871,38 +871,67 @@ __global__ void k_tile_mass(uint32_t n_samples, uint32_t n_tiles, const uint32_t
       thr[q] = (q >= last) ? 2147483648u : uint32_t(v);
     }
   }
-  tile_mass[gid] = stretch_mass(wn, wt, nl, i0, sum);
+  tile_i0[gid] = i0;
+  tile_s[gid] = sum;
 }
 
-// one CTA per (sample, chromosome slot): the masses before each tile,
-// summed in tile order by one thread over chunks staged in shared memory
-// (the order fixes the rounding), and the slot's total
-constexpr uint32_t MASS_CHUNK = 2048;
+// one CTA per (sample, chromosome slot): the integer copy sums before each
+// tile by an exclusive block scan (exact, so independent of the order of
+// the additions), and the mass before each tile as the mass of those sums
+constexpr uint32_t MASS_PER_THREAD = 4;
 __global__ void __launch_bounds__(256) k_mass_prefix(uint32_t n_slots, const uint32_t* __restrict__ c_first,
                                                      const uint32_t* __restrict__ c_ntiles, uint32_t n_tiles,
-                                                     const double* __restrict__ tile_mass,
+                                                     const double* __restrict__ wn_s, const double* __restrict__ wt_s,
+                                                     const uint64_t* __restrict__ nl_s,
+                                                     const uint64_t* __restrict__ tile_i0,
+                                                     const uint64_t* __restrict__ tile_s,
                                                      double* __restrict__ mass_cum, double* __restrict__ mass_tot) {
-  __shared__ double buf[MASS_CHUNK];
-  __shared__ double acc_s;
+  __shared__ uint64_t w_i0[8], w_s[8];
+  __shared__ uint64_t carry_i0, carry_s;
   const uint32_t s = blockIdx.x / n_slots, slot = blockIdx.x % n_slots;
   const uint32_t first = c_first[slot], nt = c_ntiles[slot];
-  const double* in = tile_mass + uint64_t(s) * n_tiles + first;
-  double* out = mass_cum + uint64_t(s) * n_tiles + first;
-  if (threadIdx.x == 0) acc_s = 0.0;
-  for (uint32_t c0 = 0; c0 < nt; c0 += MASS_CHUNK) {
-    const uint32_t n = min(MASS_CHUNK, nt - c0);
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) buf[i] = in[c0 + i];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double wn = wn_s[s], wt = wt_s[s];
+  const uint64_t nl = nl_s[s];
+  const uint64_t base = uint64_t(s) * n_tiles + first;
+  if (threadIdx.x == 0) { carry_i0 = 0; carry_s = 0; }
+  __syncthreads();
+  constexpr uint32_t CH = 256 * MASS_PER_THREAD;
+  for (uint32_t c0 = 0; c0 < nt; c0 += CH) {
+    uint64_t a[MASS_PER_THREAD], b[MASS_PER_THREAD], ta = 0, tb = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < MASS_PER_THREAD; ++q) {
+      const uint32_t t = c0 + threadIdx.x * MASS_PER_THREAD + q;
+      a[q] = t < nt ? tile_i0[base + t] : 0;
+      b[q] = t < nt ? tile_s[base + t] : 0;
+      ta += a[q];
+      tb += b[q];
+    }
+    // exclusive scan of the threads' sums: warp, then warps
+    uint64_t ia = ta, ib = tb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+      if (lane >= uint32_t(o)) { ia += xa; ib += xb; }
+    }
+    if (lane == 31) { w_i0[warp] = ia; w_s[warp] = ib; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double acc = acc_s;
-      for (uint32_t i = 0; i < n; ++i) { const double m = buf[i]; buf[i] = acc; acc = acc + m; }
-      acc_s = acc;
+    uint64_t pa = carry_i0, pb = carry_s;
+    for (uint32_t w = 0; w < warp; ++w) { pa += w_i0[w]; pb += w_s[w]; }
+    pa += ia - ta;
+    pb += ib - tb;
+#pragma unroll
+    for (uint32_t q = 0; q < MASS_PER_THREAD; ++q) {
+      const uint32_t t = c0 + threadIdx.x * MASS_PER_THREAD + q;
+      if (t < nt) mass_cum[base + t] = stretch_mass(wn, wt, nl, pa, pb);
+      pa += a[q];
+      pb += b[q];
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[c0 + i] = buf[i];
+    if (threadIdx.x == 255) { carry_i0 = pa; carry_s = pb; }
     __syncthreads();
   }
-  if (threadIdx.x == 0) mass_tot[uint64_t(s) * n_slots + slot] = acc_s;
+  if (threadIdx.x == 0) mass_tot[uint64_t(s) * n_slots + slot] = stretch_mass(wn, wt, nl, carry_i0, carry_s);
 }
 
 void seq_tile_parts(uint32_t n_tiles, const uint32_t* tile_start, const uint32_t* tile_len,
@@ -921,14 +950,14 @@ void seq_tile_parts(uint32_t n_tiles, const uint32_t* tile_start, const uint32_t
 void seq_tile_mass(uint32_t n_samples, uint32_t n_slots, const uint32_t* c_first, const uint32_t* c_ntiles,
                    const uint32_t* part_off, const uint32_t* part_len, const uint32_t* part_atom, uint32_t n_atoms,
                    const double* wn, const double* wt, const uint64_t* nl, const uint64_t* icnt0,
-                   const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, double* tile_mass, double* mass_cum,
-                   double* mass_tot, uint32_t* part_cdf, cudaStream_t st) {
+                   const uint64_t* copy_sum, uint32_t n_tiles, uint32_t n_parts, uint64_t* tile_sums,
+                   double* mass_cum, double* mass_tot, uint32_t* part_cdf, cudaStream_t st) {
   const uint64_t n = uint64_t(n_samples) * n_tiles;
   if (!n) return;
   k_tile_mass<<<nblk(n), 256, 0, st>>>(n_samples, n_tiles, part_off, part_len, part_atom, n_atoms, wn, wt, nl, icnt0,
-                                       copy_sum, n_parts, tile_mass, part_cdf);
-  k_mass_prefix<<<n_samples * n_slots, 256, 0, st>>>(n_slots, c_first, c_ntiles, n_tiles, tile_mass, mass_cum,
-                                                     mass_tot);
+                                       copy_sum, n_parts, tile_sums, tile_sums + n, part_cdf);
+  k_mass_prefix<<<n_samples * n_slots, 256, 0, st>>>(n_slots, c_first, c_ntiles, n_tiles, wn, wt, nl, tile_sums,
+                                                     tile_sums + n, mass_cum, mass_tot);
   note_launch(2);
 }
 
