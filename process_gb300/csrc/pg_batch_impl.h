@@ -204,8 +204,10 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
   const uint32_t nb = pg::sort_num_buckets(e->G);
   const uint64_t nbt = uint64_t(nb) * B;
   DBuf<uint32_t> bcnt(P, nbt + 1), bfill(P, nbt), bpart(P, pg::scan_part_elems(nbt, 1)), order(P, n_all);
+  DBuf<unsigned long long> skeys(P, n_all);
+  DBuf<uint4> recs(P, 2 * n_all);
   pg::sort_batch(o, b->inst_of.p, uint32_t(n_all), B, e->G, bcnt.p, bfill.p, bpart.p, order.p, b->sorted_view(),
-                 b->s_inst.p, st);
+                 b->s_inst.p, skeys.p, recs.p, st);
   if (n_all > 0) {
     ck(cudaMemcpy2DAsync(b->rec_off_d.p, sizeof(uint32_t), bcnt.p, sizeof(uint32_t) * nb, sizeof(uint32_t), B,
                          cudaMemcpyDeviceToDevice, st), "record offsets");

@@ -298,11 +298,12 @@ void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uin
                        uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
                        uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st,
                        const uint32_t* n_dev = nullptr);
-// sort by (instance, locus); bcnt holds n_inst * sort_num_buckets(G) + 1
-// entries and ends as the exclusive scan of the bucket counts
+// sort by (instance, locus, slot); bcnt holds n_inst * sort_num_buckets(G)
+// + 1 entries and ends as the exclusive scan of the bucket counts; keys: n
+// 64-bit keys, recs: 2n 16-byte words
 void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t n_inst, uint64_t G, uint32_t* bcnt,
                 uint32_t* bfill, uint32_t* part, uint32_t* order, const PlaceOut& sorted, uint16_t* inst_sorted,
-                cudaStream_t st);
+                unsigned long long* keys, uint4* recs, cudaStream_t st);
 // resident CTAs per SM of the persistent read kernel
 int seq_reads_batch_occupancy();
 // records of the first *n_dev sorted mutations of a batch (cap >= *n_dev)

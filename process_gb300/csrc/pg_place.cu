@@ -364,30 +364,9 @@ __global__ void k_bucket_count(const uint32_t* __restrict__ locus, uint32_t n, u
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) atomicAdd(bcnt + (locus[i] >> BUCKET_SHIFT), 1u);
 }
-__global__ void k_bucket_sort(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ boff, uint32_t nb,
-                              uint32_t n, uint32_t* __restrict__ order) {
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  const uint32_t lo = boff[b], hi = (b + 1 < nb) ? boff[b + 1] : n;
-  for (uint32_t i = lo + 1; i < hi; ++i) {
-    const uint32_t x = order[i];
-    const uint64_t kx = (uint64_t(locus[x]) << 32) | x;
-    uint32_t j = i;
-    while (j > lo) {
-      const uint32_t y = order[j - 1];
-      const uint64_t ky = (uint64_t(locus[y]) << 32) | y;
-      if (ky <= kx) break;
-      order[j] = y;
-      --j;
-    }
-    order[j] = x;
-  }
-}
-
-// The plain path's bucket sort on 64-bit keys (locus << 32 | slot) written
-// by the scatter, so the in-bucket insertion sort reads its bucket's keys
-// contiguously instead of looking each slot's locus up; the key order is
-// that of k_bucket_sort.
+// Bucket sort on 64-bit keys (locus << 32 | slot) written by the scatter:
+// the in-bucket insertion sort reads its bucket's keys contiguously, and
+// ties of a locus fall in slot order.
 __global__ void k_bucket_scatter_keys(const uint32_t* __restrict__ locus, uint32_t n, const uint32_t* __restrict__ boff,
                                       uint32_t* __restrict__ bfill, unsigned long long* __restrict__ keys) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -414,30 +393,22 @@ __global__ void k_bucket_sort_keys(const uint32_t* __restrict__ boff, uint32_t n
   for (uint32_t i = lo; i < hi; ++i) order[i] = uint32_t(keys[i]);
 }
 
-__global__ void k_gather_sorted(PlaceOut o, const uint32_t* __restrict__ order, uint32_t n, PlaceOut s) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t x = order[i];
-  s.locus[i] = o.locus[x]; s.edge[i] = o.edge[x]; s.aux[i] = o.aux[x];
-  s.cls[i] = o.cls[x]; s.sig[i] = o.sig[x]; s.allele[i] = o.allele[x]; s.seq[i] = o.seq[x];
-  s.kind[i] = o.kind[x]; s.nature[i] = o.nature[x]; s.attempt[i] = o.attempt[x];
-}
-
-// The same gather through 32-byte records: every slot's columns packed by a
-// coalesced pass, so the gather reads one 32-byte sector per mutation
-// instead of one per column.
-__global__ void k_pack_records(PlaceOut o, uint32_t n, uint4* __restrict__ rec) {
+// The gather of the sorted columns through 32-byte records: every slot's
+// columns packed by a coalesced pass, so the gather reads one 32-byte sector
+// per mutation instead of one per column.
+// (inst: the batched form's instance of each slot, carried along; may be NULL)
+__global__ void k_pack_records(PlaceOut o, const uint16_t* __restrict__ inst, uint32_t n, uint4* __restrict__ rec) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   rec[2 * uint64_t(i)] = make_uint4(o.locus[i], o.edge[i], o.aux[i], o.attempt[i]);
   rec[2 * uint64_t(i) + 1] = make_uint4(uint32_t(o.allele[i]) | (uint32_t(o.seq[i]) << 16),
                                         uint32_t(o.cls[i]) | (uint32_t(o.sig[i]) << 8) | (uint32_t(o.kind[i]) << 16) |
                                             (uint32_t(o.nature[i]) << 24),
-                                        0u, 0u);
+                                        inst ? uint32_t(inst[i]) : 0u, 0u);
 }
 
 __global__ void k_gather_records(const uint4* __restrict__ rec, const uint32_t* __restrict__ order, uint32_t n,
-                                 PlaceOut s) {
+                                 PlaceOut s, uint16_t* __restrict__ inst_sorted) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint64_t x = order[i];
@@ -445,12 +416,7 @@ __global__ void k_gather_records(const uint4* __restrict__ rec, const uint32_t* 
   s.locus[i] = a.x; s.edge[i] = a.y; s.aux[i] = a.z; s.attempt[i] = a.w;
   s.allele[i] = uint16_t(b.x); s.seq[i] = uint16_t(b.x >> 16);
   s.cls[i] = uint8_t(b.y); s.sig[i] = uint8_t(b.y >> 8); s.kind[i] = uint8_t(b.y >> 16); s.nature[i] = uint8_t(b.y >> 24);
-}
-
-__global__ void k_gather_u16(const uint16_t* __restrict__ in, const uint32_t* __restrict__ order, uint32_t n,
-                             uint16_t* __restrict__ out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = in[order[i]];
+  if (inst_sorted) inst_sorted[i] = uint16_t(b.z);
 }
 
 // ------------------------------------------------------------ batched placement
@@ -579,11 +545,12 @@ __global__ void k_bucket_count_b(const uint32_t* __restrict__ locus, const uint1
 }
 __global__ void k_bucket_scatter_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
                                    uint32_t n, uint32_t nb, const uint32_t* __restrict__ boff,
-                                   uint32_t* __restrict__ bfill, uint32_t* __restrict__ order) {
+                                   uint32_t* __restrict__ bfill, unsigned long long* __restrict__ keys) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint64_t b = uint64_t(inst_of[i]) * nb + (locus[i] >> BUCKET_SHIFT);
-  order[boff[b] + atomicAdd(bfill + b, 1u)] = i;
+  const uint32_t k = locus[i];
+  const uint64_t b = uint64_t(inst_of[i]) * nb + (k >> BUCKET_SHIFT);
+  keys[boff[b] + atomicAdd(bfill + b, 1u)] = (static_cast<unsigned long long>(k) << 32) | i;
 }
 
 // ------------------------------------------------------------ host launchers
@@ -648,8 +615,8 @@ void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, ui
   scan_rows<uint32_t>(bcnt, bcnt, nb, 1, part, nullptr, st);
   k_bucket_scatter_keys<<<nblk(n), 256, 0, st>>>(o.locus, n, bcnt, bfill, keys); note_launch();
   k_bucket_sort_keys<<<nblk(nb), 256, 0, st>>>(bcnt, nb, n, keys, order); note_launch();
-  k_pack_records<<<nblk(n), 256, 0, st>>>(o, n, recs); note_launch();
-  k_gather_records<<<nblk(n), 256, 0, st>>>(recs, order, n, sorted); note_launch();
+  k_pack_records<<<nblk(n), 256, 0, st>>>(o, nullptr, n, recs); note_launch();
+  k_gather_records<<<nblk(n), 256, 0, st>>>(recs, order, n, sorted, nullptr); note_launch();
 }
 
 uint32_t sort_num_buckets(uint64_t G) { return uint32_t((G >> BUCKET_SHIFT) + 1); }
@@ -685,7 +652,7 @@ void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uin
 
 void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t n_inst, uint64_t G, uint32_t* bcnt,
                 uint32_t* bfill, uint32_t* part, uint32_t* order, const PlaceOut& sorted, uint16_t* inst_sorted,
-                cudaStream_t st) {
+                unsigned long long* keys, uint4* recs, cudaStream_t st) {
   const uint32_t nb = uint32_t((G >> BUCKET_SHIFT) + 1);
   const uint64_t nbt = uint64_t(nb) * n_inst;
   cudaMemsetAsync(bcnt, 0, sizeof(uint32_t) * (nbt + 1), st);
@@ -693,10 +660,10 @@ void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t
   if (n == 0) return;
   k_bucket_count_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt); note_launch();
   scan_rows<uint32_t>(bcnt, bcnt, nbt, 1, part, bcnt + nbt, st);
-  k_bucket_scatter_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt, bfill, order); note_launch();
-  k_bucket_sort<<<nblk(nbt), 256, 0, st>>>(o.locus, bcnt, uint32_t(nbt), n, order); note_launch();
-  k_gather_sorted<<<nblk(n), 256, 0, st>>>(o, order, n, sorted); note_launch();
-  k_gather_u16<<<nblk(n), 256, 0, st>>>(inst_of, order, n, inst_sorted); note_launch();
+  k_bucket_scatter_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt, bfill, keys); note_launch();
+  k_bucket_sort_keys<<<nblk(nbt), 256, 0, st>>>(bcnt, uint32_t(nbt), n, keys, order); note_launch();
+  k_pack_records<<<nblk(n), 256, 0, st>>>(o, inst_of, n, recs); note_launch();
+  k_gather_records<<<nblk(n), 256, 0, st>>>(recs, order, n, sorted, inst_sorted); note_launch();
 }
 
 }  // namespace pg
