@@ -144,28 +144,52 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
   pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p, cnt_id.p,
                             uint32_t(n_snv), nullptr, uint32_t(n_all), 0, err.p, st);
   if (e->infinite_sites && n_all > 0) {
-    uint64_t cap = 1024;
-    while (cap < 2 * n_all) cap <<= 1;
-    DBuf<uint64_t> hkeys(P, cap), ckeys(P, cap);
-    DBuf<uint32_t> cvals(P, cap), pend_a(P, n_all), pend_b(P, n_all), n_next(P, 1);
+    DBuf<uint32_t> pend_a(P, n_all), pend_b(P, n_all), n_next(P, 1);
     DBuf<uint8_t> lost(P, n_all);
-    ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
     const uint32_t* pending = nullptr;
     uint32_t n_pend = uint32_t(n_all);
     uint32_t* next = pend_a.p;
+    // the first round (no drivers in a batch, so nothing is taken yet) keeps
+    // its candidate table, which then holds exactly the taken keys; the
+    // later rounds test it beside their own accepted set, sized by what the
+    // first round leaves
+    uint64_t fcap = 1024;
+    while (fcap < 2 * n_all) fcap <<= 1;
+    DBuf<uint64_t> fkeys(P, fcap);
+    {
+      DBuf<uint32_t> fvals(P, fcap);
+      ck(cudaMemsetAsync(fkeys.p, 0xff, sizeof(uint64_t) * fcap, st), "memset");
+      ck(cudaMemsetAsync(fvals.p, 0xff, sizeof(uint32_t) * fcap, st), "memset");
+      ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
+      pg::sites_round_batch(b->locus.p, b->inst_of.p, nullptr, n_pend, nullptr, 0, fkeys.p, fvals.p, fcap - 1, lost.p,
+                            next, n_next.p, err.p, st);
+      uint32_t nn = 0;
+      ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+      ck(cudaStreamSynchronize(st), "first round");
+      if (nn) pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p,
+                                        cnt_id.p, uint32_t(n_snv), next, nn, 1, err.p, st);
+      pending = next;
+      next = pend_b.p;
+      n_pend = nn;
+    }
+    uint64_t cap = 1024;
+    while (cap < 2 * uint64_t(n_pend)) cap <<= 1;
+    DBuf<uint64_t> hkeys(P, cap), ckeys(P, cap);
+    DBuf<uint32_t> cvals(P, cap);
+    ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
     // as the plain path: host-read rounds while many slots are pending, then
     // groups of rounds with the counts in device memory
     constexpr uint32_t ROUND_TAIL = 1u << 20;
     constexpr int ROUND_GROUP = 16;
     DBuf<uint32_t> counts(P, ROUND_GROUP);
-    for (int round = 0; n_pend > 0;) {
+    for (int round = 1; n_pend > 0;) {
       require(round < 256, "infinite sites model: no free locus left for some mutations");
       if (n_pend > ROUND_TAIL) {
         ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
         ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
         ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
         pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1,
-                              lost.p, next, n_next.p, err.p, st);
+                              lost.p, next, n_next.p, err.p, st, nullptr, fkeys.p, fcap - 1);
         uint32_t nn = 0;
         ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
         ck(cudaStreamSynchronize(st), "redraw round");
@@ -186,7 +210,7 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
         ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * ctail, st), "memset");
         ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
         pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p,
-                              ctail - 1, lost.p, next, n_out, err.p, st, n_dev);
+                              ctail - 1, lost.p, next, n_out, err.p, st, n_dev, fkeys.p, fcap - 1);
         pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p, cnt_id.p,
                                   uint32_t(n_snv), next, n_pend, 1, err.p, st, n_out);
         pending = next;

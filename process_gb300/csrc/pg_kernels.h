@@ -294,10 +294,13 @@ void place_mutations_batch(const PlaceTables* tabs, uint32_t n_inst, const uint3
                            const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
                            uint32_t n_snv, const uint32_t* pending, uint32_t n_pending, int redraw, uint32_t* err,
                            cudaStream_t st, const uint32_t* n_dev = nullptr);
+// hkeys NULL: no accepted set (the first round, whose candidate table then
+// holds the taken keys); fkeys (optional): that first round's table, tested
+// as taken by the later rounds
 void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uint32_t* pending, uint32_t n,
                        uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
                        uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st,
-                       const uint32_t* n_dev = nullptr);
+                       const uint32_t* n_dev = nullptr, const uint64_t* fkeys = nullptr, uint64_t fmask = 0);
 // sort by (instance, locus, slot); bcnt holds n_inst * sort_num_buckets(G)
 // + 1 entries and ends as the exclusive scan of the bucket counts; keys: n
 // 64-bit keys, recs: 2n 16-byte words

@@ -496,6 +496,7 @@ __device__ __forceinline__ uint64_t hset64_insert(unsigned long long* __restrict
 __global__ void k_cand_insert_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of,
                                 const uint32_t* __restrict__ pending, uint32_t n, const uint32_t* __restrict__ n_dev,
                                 const uint64_t* __restrict__ hkeys, uint64_t hmask,
+                                const uint64_t* __restrict__ fkeys, uint64_t fmask,
                                 unsigned long long* __restrict__ ckeys, uint32_t* __restrict__ cvals, uint64_t cmask,
                                 uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -503,7 +504,11 @@ __global__ void k_cand_insert_b(const uint32_t* __restrict__ locus, const uint16
   const uint32_t slot = pending ? pending[i] : i;
   const uint32_t l = locus[slot];
   const uint64_t k = (uint64_t(inst_of[slot]) << 32) | l;
-  if (l == LOCUS_INVALID || hset64_contains(hkeys, hmask, k)) { lost[i] = 1; return; }
+  if (l == LOCUS_INVALID || (hkeys && hset64_contains(hkeys, hmask, k)) ||
+      (fkeys && hset64_contains(fkeys, fmask, k))) {
+    lost[i] = 1;
+    return;
+  }
   lost[i] = 0;
   const uint64_t h = hset64_insert(ckeys, cmask, k);
   if (h == EMPTY64) { atomicOr(err, ERR_CAPACITY); return; }
@@ -531,7 +536,7 @@ __global__ void k_cand_resolve_b(const uint32_t* __restrict__ locus, const uint1
     }
   }
   if (win) {
-    if (hset64_insert(hkeys, hmask, k) == EMPTY64) atomicOr(err, ERR_CAPACITY);
+    if (hkeys && hset64_insert(hkeys, hmask, k) == EMPTY64) atomicOr(err, ERR_CAPACITY);
   } else {
     next[atomicAdd(n_next, 1u)] = slot;
   }
@@ -640,9 +645,9 @@ void place_mutations_batch(const PlaceTables* tabs, uint32_t n_inst, const uint3
 void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uint32_t* pending, uint32_t n,
                        uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
                        uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st,
-                       const uint32_t* n_dev) {
+                       const uint32_t* n_dev, const uint64_t* fkeys, uint64_t fmask) {
   if (n == 0) return;
-  k_cand_insert_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, n_dev, hkeys, hmask,
+  k_cand_insert_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, n_dev, hkeys, hmask, fkeys, fmask,
                                            reinterpret_cast<unsigned long long*>(ckeys), cvals, cmask, lost, err);
   k_cand_resolve_b<<<nblk(n), 256, 0, st>>>(locus, inst_of, pending, n, n_dev,
                                             reinterpret_cast<unsigned long long*>(hkeys), hmask, ckeys, cvals, cmask,
