@@ -138,6 +138,25 @@ def run_cpu(steps: int, warmup: int, threads: int, sample_desc: str):
             "seconds": t_place + t_seq, "threads": threads, "sample": sample_desc}
 
 
+def cpu_model() -> str:
+    """The host CPU's model name as the OS reports it (lscpu, else
+    /proc/cpuinfo), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def reference_arm(args):
     rank = env_int("RANK", 0)
     if rank != 0:
@@ -155,7 +174,7 @@ def reference_arm(args):
             "secondary": {"mutations_placed_per_s": r["mutations_placed_per_s"],
                           "sequencing_reads_per_s": r["seq_reads_per_s"]},
             "cpu_baseline": {"value": r["reads_per_s"], "unit": "reads/s", "cores": threads, "kind": "port",
-                             "sample": desc},
+                             "sample": desc, "cpu_model": cpu_model()},
             "e2e": {"value": r["reads_per_s"], "unit": "reads/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -419,7 +438,7 @@ def gpu_arm(args):
             r1 = run_cpu(1, 0, 1, desc)
             cpu = {"value": r["reads_per_s"], "unit": "reads/s", "cores": threads, "kind": "port", "sample": desc,
                    "single_core_value": r1["reads_per_s"],
-                   "mutations_placed_per_s": r["mutations_placed_per_s"]}
+                   "mutations_placed_per_s": r["mutations_placed_per_s"], "cpu_model": cpu_model()}
         clocks = clk.summary()
         line = {
             "metric": METRIC, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
