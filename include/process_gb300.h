@@ -236,6 +236,15 @@ pg_status pg_seq_result_dims(const pg_seq_result* res, uint32_t* n_samples, uint
 pg_status pg_seq_result_copy(const pg_seq_result* res, int32_t* alt, int32_t* depth);
 /* Device time of the read kernel of the call (ms). */
 pg_status pg_seq_result_kernel_ms(const pg_seq_result* res, float* ms);
+/* The observed rows: mutations with an alt read in some sample, the rows the
+ * reference's result data frame keeps by default (include_non_sequenced_
+ * mutations = FALSE; src/seq_simulation.cpp:52-90, 142-181).  Built on the
+ * device on the first call; n_active = their number. */
+pg_status pg_seq_result_active(pg_seq_result* res, uint64_t* n_active);
+/* Their mutation indices (n_active, ascending, in the order of
+ * pg_placed_copy) and alt / depth as [n_samples][n_active] int32; any
+ * pointer may be NULL.  Requires pg_seq_result_active first. */
+pg_status pg_seq_result_copy_active(const pg_seq_result* res, uint32_t* index, int32_t* alt, int32_t* depth);
 
 /* simulate_seq with write_SAM = TRUE (src/seq_simulation.cpp:540-564; files
  * and naming of vignettes/sequencing.Rmd:137-180, 282-317): the counts of

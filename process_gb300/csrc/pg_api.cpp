@@ -298,6 +298,10 @@ struct pg_seq_result {
   uint64_t M = 0, n_reads = 0;
   DBuf<uint32_t> alt, depth;
   float kernel_ms = 0;
+  // observed rows (built on the first request)
+  bool active_done = false;
+  uint32_t n_active = 0;
+  DBuf<uint32_t> a_index, a_alt, a_depth;
 };
 
 namespace {
@@ -1796,6 +1800,49 @@ pg_status pg_seq_result_copy(const pg_seq_result* r, int32_t* alt, int32_t* dept
     if (alt) ck(cudaMemcpyAsync(alt, r->alt.p, bytes, cudaMemcpyDeviceToHost, r->eng->st), "copy alt");
     if (depth) ck(cudaMemcpyAsync(depth, r->depth.p, bytes, cudaMemcpyDeviceToHost, r->eng->st), "copy depth");
     ck(cudaStreamSynchronize(r->eng->st), "copy");
+  });
+}
+
+pg_status pg_seq_result_active(pg_seq_result* r, uint64_t* n_active) {
+  return guarded([&] {
+    require(r != nullptr && n_active != nullptr, "NULL argument");
+    select_device(r->eng);
+    if (!r->active_done) {
+      require(r->M < (uint64_t(1) << 32), "too many mutations for the observed-row tables");
+      cudaStream_t st = r->eng->st;
+      Pool* P = &r->eng->pool;
+      DBuf<uint32_t> pos(P, r->M), part(P, pg::scan_part_elems(r->M, 1)), tot(P, 1);
+      pg::seq_active_flags(r->alt.p, r->n_samples, r->M, pos.p, st);
+      pg::scan_rows<uint32_t>(pos.p, pos.p, r->M, 1, part.p, tot.p, st);
+      uint32_t na = 0;
+      ck(cudaMemcpyAsync(&na, tot.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "observed rows");
+      ck(cudaStreamSynchronize(st), "observed rows");
+      r->a_index = DBuf<uint32_t>(P, na);
+      r->a_alt = DBuf<uint32_t>(P, uint64_t(na) * r->n_samples);
+      r->a_depth = DBuf<uint32_t>(P, uint64_t(na) * r->n_samples);
+      pg::seq_active_gather(r->alt.p, r->depth.p, r->n_samples, r->M, pos.p, na, r->a_index.p, r->a_alt.p,
+                            r->a_depth.p, st);
+      ck(cudaGetLastError(), "observed rows");
+      ck(cudaStreamSynchronize(st), "observed rows");
+      r->n_active = na;
+      r->active_done = true;
+    }
+    *n_active = r->n_active;
+  });
+}
+
+pg_status pg_seq_result_copy_active(const pg_seq_result* r, uint32_t* index, int32_t* alt, int32_t* depth) {
+  return guarded([&] {
+    require(r != nullptr, "NULL handle");
+    require(r->active_done, "pg_seq_result_active has not been called on this result");
+    select_device(r->eng);
+    cudaStream_t st = r->eng->st;
+    const uint64_t na = r->n_active, nb = sizeof(uint32_t) * na * r->n_samples;
+    if (na == 0) return;
+    if (index) ck(cudaMemcpyAsync(index, r->a_index.p, sizeof(uint32_t) * na, cudaMemcpyDeviceToHost, st), "copy");
+    if (alt) ck(cudaMemcpyAsync(alt, r->a_alt.p, nb, cudaMemcpyDeviceToHost, st), "copy alt");
+    if (depth) ck(cudaMemcpyAsync(depth, r->a_depth.p, nb, cudaMemcpyDeviceToHost, st), "copy depth");
+    ck(cudaStreamSynchronize(st), "copy");
   });
 }
 

@@ -332,6 +332,12 @@ void seq_tile_counts(uint32_t n_samples, uint32_t n_slots, uint32_t max_depth, c
                      uint64_t heap_total, uint32_t* heap, uint32_t tile_size, uint32_t n_tiles,
                      const double* mass_cum, const double* mass_tot, uint64_t seed, uint32_t* pair_cnt,
                      cudaStream_t st);
+// observed rows: flag[m] = 1 when some sample has an alt read of mutation m;
+// with pos the exclusive scan of the flags (n_active rows), the compact
+// [sample][row] alt / depth tables and each row's mutation index
+void seq_active_flags(const uint32_t* alt, uint32_t n_samples, uint64_t M, uint32_t* flag, cudaStream_t st);
+void seq_active_gather(const uint32_t* alt, const uint32_t* depth, uint32_t n_samples, uint64_t M, const uint32_t* pos,
+                       uint32_t n_active, uint32_t* index, uint32_t* a_out, uint32_t* d_out, cudaStream_t st);
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
                const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st);

@@ -995,6 +995,47 @@ void seq_tile_counts(uint32_t n_samples, uint32_t n_slots, uint32_t max_depth, c
   }
 }
 
+// ------------------------------------------------------------ observed rows
+// The rows of the result a caller reads by default: mutations with an alt
+// read in some sample (src/seq_simulation.cpp:52-90 keeps those unless
+// include_non_sequenced_mutations).  Flags, their exclusive scan, then the
+// compact [sample][row] tables and the rows' mutation indices.
+__global__ void k_active_flags(const uint32_t* __restrict__ alt, uint32_t n_samples, uint64_t M,
+                               uint32_t* __restrict__ flag) {
+  const uint64_t m = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  uint32_t any = 0;
+  for (uint32_t s = 0; s < n_samples; ++s) any |= alt[uint64_t(s) * M + m];
+  flag[m] = any ? 1u : 0u;
+}
+
+__global__ void k_active_gather(const uint32_t* __restrict__ alt, const uint32_t* __restrict__ depth,
+                                uint32_t n_samples, uint64_t M, const uint32_t* __restrict__ pos, uint32_t n_active,
+                                uint32_t* __restrict__ index, uint32_t* __restrict__ a_out,
+                                uint32_t* __restrict__ d_out) {
+  const uint64_t m = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  const uint32_t p = pos[m];
+  if ((m + 1 < M ? pos[m + 1] : n_active) == p) return;   // not observed
+  index[p] = uint32_t(m);
+  for (uint32_t s = 0; s < n_samples; ++s) {
+    a_out[uint64_t(s) * n_active + p] = alt[uint64_t(s) * M + m];
+    d_out[uint64_t(s) * n_active + p] = depth[uint64_t(s) * M + m];
+  }
+}
+
+void seq_active_flags(const uint32_t* alt, uint32_t n_samples, uint64_t M, uint32_t* flag, cudaStream_t st) {
+  if (M) { k_active_flags<<<nblk(M), 256, 0, st>>>(alt, n_samples, M, flag); note_launch(); }
+}
+
+void seq_active_gather(const uint32_t* alt, const uint32_t* depth, uint32_t n_samples, uint64_t M, const uint32_t* pos,
+                       uint32_t n_active, uint32_t* index, uint32_t* a_out, uint32_t* d_out, cudaStream_t st) {
+  if (M && n_active) {
+    k_active_gather<<<nblk(M), 256, 0, st>>>(alt, depth, n_samples, M, pos, n_active, index, a_out, d_out);
+    note_launch();
+  }
+}
+
 void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const uint32_t* pair_cnt,
                const SeqSample* samples, uint32_t n_samples, const uint32_t* leaf_tin, const SeqParams& prm,
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st) {

@@ -1171,6 +1171,35 @@ class SeqResult:
         check(lib().pg_seq_result_copy(self._h, ptr(alt, C.c_int32), ptr(dep, C.c_int32)))
         return alt, dep
 
+    def observed(self, out: tuple[np.ndarray, np.ndarray, np.ndarray] | None = None
+                 ) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """The rows of mutations with an alt read in some sample (the rows
+        the result data frame keeps by default), compacted on the device:
+        (mutation indices (uint32, ascending), alt, depth ([samples][rows],
+        int32)).  ``out`` takes three preallocated C-contiguous arrays of
+        at least that size (e.g. page-locked host memory); views of their
+        first rows are returned."""
+        n = C.c_uint64()
+        check(lib().pg_seq_result_active(self._h, C.byref(n)))
+        s, _, _ = self.dims()
+        na = n.value
+        if out is None:
+            idx = np.empty(na, dtype=np.uint32)
+            alt = np.empty((s, na), dtype=np.int32)
+            dep = np.empty((s, na), dtype=np.int32)
+        else:
+            bi, ba, bd = out
+            for b, dt, need in ((bi, np.uint32, na), (ba, np.int32, s * na), (bd, np.int32, s * na)):
+                if b.dtype != dt or not b.flags.c_contiguous or not b.flags.writeable or b.size < need:
+                    raise ValueError(f"out arrays must be writable C-contiguous {np.dtype(dt).name} "
+                                     f"with at least {need} elements")
+            idx = bi.reshape(-1)[:na]
+            alt = ba.reshape(-1)[:s * na].reshape(s, na)
+            dep = bd.reshape(-1)[:s * na].reshape(s, na)
+        check(lib().pg_seq_result_copy_active(self._h, ptr(idx, C.c_uint32), ptr(alt, C.c_int32),
+                                              ptr(dep, C.c_int32)))
+        return idx, alt, dep
+
     def kernel_ms(self) -> float:
         v = C.c_float()
         check(lib().pg_seq_result_kernel_ms(self._h, C.byref(v)))
@@ -1234,16 +1263,15 @@ def _sequencer_rate(sequencer) -> tuple[float, dict | None]:
     raise DomainError(_lib.PG_ERR_DOMAIN, "Unsupported sequencer type")
 
 
-def _result_frame(pf: PhylogeneticForest, alt: np.ndarray, dep: np.ndarray, sample_names: list[str],
-                  include_non_sequenced: bool, present: np.ndarray) -> dict:
-    """The wide data frame of get_result_dataframe (src/seq_simulation.cpp:142-181):
-    rows = mutations observed in some sample (or present, with
-    include_non_sequenced_mutations), merged by (chr, pos, ref, alt)."""
+def _result_frame(pf: PhylogeneticForest, idx: np.ndarray, alt: np.ndarray, dep: np.ndarray,
+                  sample_names: list[str]) -> dict:
+    """The wide data frame of get_result_dataframe (src/seq_simulation.cpp:142-181)
+    over the rows idx (mutation indices, ascending; alt / dep are their
+    [sample][row] tables), merged by (chr, pos, ref, alt)."""
     t = pf.table()
     ref, altb = pf._ref_alt(t)
     cause = pf._cause(t)
-    keep = (alt.sum(axis=0) > 0) | (include_non_sequenced & present)
-    idx = np.nonzero(keep)[0]
+    idx = np.asarray(idx, dtype=np.int64)
     chrn, pos = pf._chr_pos(t["locus"][idx])
     # merge records that are the same SID (chr, pos, ref, alt): occurrences add, causes/classes union
     keys = {}
@@ -1251,20 +1279,21 @@ def _result_frame(pf: PhylogeneticForest, alt: np.ndarray, dep: np.ndarray, samp
     for j, i in enumerate(idx):
         k = (int(t["locus"][i]), ref[i], altb[i])
         if k in keys:
-            keys[k].append(i)
+            keys[k].append(j)
         else:
-            keys[k] = [i]
+            keys[k] = [j]
             order.append(k)
-    rows = [keys[k] for k in order]
+    rows = [keys[k] for k in order]                 # columns of alt / dep
     first = np.array([r[0] for r in rows], dtype=np.int64)
+    firsti = idx[first] if len(first) else first
     df = {
-        "chr": chrn[np.searchsorted(idx, first)] if len(first) else np.array([], dtype=object),
-        "chr_pos": pos[np.searchsorted(idx, first)] if len(first) else np.array([], dtype=np.int64),
-        "ref": ref[first] if len(first) else np.array([], dtype=object),
-        "alt": altb[first] if len(first) else np.array([], dtype=object),
-        "causes": np.array([";".join(sorted({c for c in cause[r] if c is not None})) or None for r in rows],
+        "chr": chrn[first] if len(first) else np.array([], dtype=object),
+        "chr_pos": pos[first] if len(first) else np.array([], dtype=np.int64),
+        "ref": ref[firsti] if len(first) else np.array([], dtype=object),
+        "alt": altb[firsti] if len(first) else np.array([], dtype=object),
+        "causes": np.array([";".join(sorted({c for c in cause[idx[r]] if c is not None})) or None for r in rows],
                            dtype=object),
-        "classes": np.array([";".join(sorted(set(NATURES[t["nature"][r]]))) for r in rows], dtype=object),
+        "classes": np.array([";".join(sorted(set(NATURES[t["nature"][idx[r]]]))) for r in rows], dtype=object),
     }
     for s, name in enumerate(sample_names):
         occ = np.array([alt[s, r].sum() for r in rows], dtype=np.int32)
@@ -1275,6 +1304,17 @@ def _result_frame(pf: PhylogeneticForest, alt: np.ndarray, dep: np.ndarray, samp
         df[f"{name}.coverage"] = cov
         df[f"{name}.VAF"] = vaf
     return df
+
+
+def _result_rows(res: "SeqResult", include_non_sequenced: bool, present: np.ndarray):
+    """Rows of the result frame: the observed rows compacted on the device,
+    or (include_non_sequenced_mutations) those plus every mutation present
+    in a sequenced sample's cells, from the full tables."""
+    if not include_non_sequenced:
+        return res.observed()
+    alt, dep = res.counts()
+    idx = np.nonzero((alt.sum(axis=0) > 0) | present)[0]
+    return idx, alt[:, idx], dep[:, idx]
 
 
 def _presence(pf: PhylogeneticForest, n_samples_seq: int, with_normal: bool, pre_in_normal: bool) -> np.ndarray:
@@ -1336,9 +1376,9 @@ def simulate_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_gen
                           purity=purity, with_normal_sample=with_normal_sample,
                           preneoplastic_in_normal=preneoplastic_in_normal, chromosomes=chromosomes,
                           tile_size=tile_size, insert_model=insert_model)
-    alt, dep = res.counts()
-    present = _presence(phylo_forest, len(names), with_normal_sample, preneoplastic_in_normal)
-    df = _result_frame(phylo_forest, alt, dep, names, include_non_sequenced_mutations, present)
+    present = (_presence(phylo_forest, len(names), with_normal_sample, preneoplastic_in_normal)
+               if include_non_sequenced_mutations else None)
+    df = _result_frame(phylo_forest, *_result_rows(res, include_non_sequenced_mutations, present), names)
     params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
               "coverage": coverage, "read_size": read_size, "insert_size_mean": insert_size_mean,
               "insert_size_stddev": insert_size_stddev, "output_dir": output_dir, "write_SAM": write_SAM,
@@ -1365,10 +1405,9 @@ def simulate_normal_seq(phylo_forest: PhylogeneticForest, sequencer=None, refere
                           insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
                           purity=1.0, with_normal_sample=True, preneoplastic_in_normal=with_preneoplastic,
                           normal_only=True, chromosomes=chromosomes, tile_size=tile_size, insert_model=insert_model)
-    alt, dep = res.counts()
     t = phylo_forest.table()
     present = (t["edge"] == phylo_forest.forest.num_of_nodes) & bool(with_preneoplastic)
-    df = _result_frame(phylo_forest, alt, dep, ["normal_sample"], include_non_sequenced_mutations, present)
+    df = _result_frame(phylo_forest, *_result_rows(res, include_non_sequenced_mutations, present), ["normal_sample"])
     params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
               "coverage": coverage, "read_size": read_size, "insert_size_mean": insert_size_mean,
               "insert_size_stddev": insert_size_stddev, "output_dir": output_dir, "write_SAM": write_SAM,

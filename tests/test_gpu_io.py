@@ -59,3 +59,45 @@ def test_counts_into_page_locked_buffers(gpu_lib):
         r.counts((np.empty((s, m), np.int64), bufs[1]))
     with pytest.raises(ValueError, match="C-contiguous int32"):
         r.counts((bufs[0][:, :-1], bufs[1]))
+
+
+def test_observed_rows(gpu_lib):
+    """observed() compacts, on the device, the rows with an alt read in some
+    sample: the same indices and tables as filtering the full tables; the
+    default result frame (those rows) and the include_non_sequenced frame
+    carry the same occurrences."""
+    import torch
+    from process_gb300 import simulate_seq, synth
+    from process_gb300.engine import sequence_counts
+    w = synth.config1(seed=13, n_leaves=200)
+    w.genome.chr_lengths = [120_000, 60_000, 60_000]
+    eng = synth.build_engine(w)
+    pf = eng.place_mutations(w.forest, 20, 4, seed=6)
+    r = sequence_counts(pf, 5, coverage=25, read_size=120, insert_size_mean=300, insert_size_stddev=10,
+                        error_rate=1e-3, purity=0.8)
+    a, d = r.counts()
+    keep = np.nonzero(a.sum(axis=0) > 0)[0]
+    assert 0 < len(keep) < a.shape[1]
+    idx, ao, do = r.observed()
+    np.testing.assert_array_equal(idx, keep)
+    np.testing.assert_array_equal(ao, a[:, keep])
+    np.testing.assert_array_equal(do, d[:, keep])
+    s = a.shape[0]
+    bufs = (torch.empty(a.shape[1], dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+            torch.empty(s * a.shape[1], dtype=torch.int32, pin_memory=True).numpy(),
+            torch.empty(s * a.shape[1], dtype=torch.int32, pin_memory=True).numpy())
+    i2, a2, d2 = r.observed(bufs)
+    np.testing.assert_array_equal(i2, keep)
+    np.testing.assert_array_equal(a2, a[:, keep])
+    np.testing.assert_array_equal(d2, d[:, keep])
+    with pytest.raises(ValueError, match="at least"):
+        r.observed((bufs[0][:1], bufs[1], bufs[2]))
+    f0 = simulate_seq(pf, coverage=25, insert_size_mean=300, insert_size_stddev=10, seed=7)["mutations"]
+    f1 = simulate_seq(pf, coverage=25, insert_size_mean=300, insert_size_stddev=10, seed=7,
+                      include_non_sequenced_mutations=True)["mutations"]
+    assert len(f1["chr"]) > len(f0["chr"])
+    occ = [k for k in f0 if k.endswith(".occurrences")]
+    assert occ and all(int(f0[k].sum()) == int(f1[k].sum()) for k in occ)
+    rows0 = set(zip(f0["chr"], f0["chr_pos"], f0["ref"], f0["alt"]))
+    rows1 = set(zip(f1["chr"], f1["chr_pos"], f1["ref"], f1["alt"]))
+    assert rows0 <= rows1
