@@ -625,34 +625,54 @@ class PhylogeneticForest:
     def get_nodes(self) -> dict:
         return self.forest.get_nodes()
 
-    def _ref_alt(self, t: dict) -> tuple[np.ndarray, np.ndarray]:
+    def _ref_alt(self, t: dict, rows: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """ref / alt strings of the rows (all when None): one base gather for
+        the SNVs and one for the indels' anchor windows."""
         eng = self.engine
-        n = len(t["locus"])
-        kind, aux, locus = t["kind"], t["aux"], t["locus"].astype(np.int64)
+        rows = np.arange(len(t["locus"])) if rows is None else np.asarray(rows, dtype=np.int64)
+        n = len(rows)
+        kind, aux = t["kind"][rows], t["aux"][rows].astype(np.int64)
+        locus = t["locus"][rows].astype(np.int64)
         ref = np.empty(n, dtype=object)
         alt = np.empty(n, dtype=object)
         snv = kind == 0
         rb = eng.gather_bases(locus[snv])
         ref[snv] = BASES[np.minimum(rb, 3)]
         alt[snv] = BASES[aux[snv] & 3]
-        for i in np.nonzero(~snv)[0]:
-            a = int(aux[i])
-            ins, ln, bases = a & 1, (a >> 1) & 7, a >> 8
-            anchor = int(locus[i])
-            if ins:
-                r = "".join(BASES[eng.gather_bases(np.array([anchor], dtype=np.uint32))])
-                alt[i] = r + "".join(BASES[(bases >> (2 * k)) & 3] for k in range(ln))
-                ref[i] = r
-            else:
-                r = "".join(BASES[eng.gather_bases(np.arange(anchor, anchor + ln + 1, dtype=np.uint32))])
-                ref[i], alt[i] = r, r[0]
+        ind = np.nonzero(~snv)[0]
+        if len(ind):
+            a = aux[ind]
+            ins, ln, bases = (a & 1).astype(bool), (a >> 1) & 7, a >> 8
+            # the anchor and the 7 bases after it (a deletion spans at most 7)
+            win = np.minimum(locus[ind][:, None] + np.arange(8)[None, :], eng.genome.total - 1)
+            gch = BASES[np.minimum(eng.gather_bases(win.ravel()).reshape(-1, 8), 3)]
+            added = BASES[(bases[:, None] >> (2 * np.arange(7))[None, :]) & 3]
+            for length in np.unique(ln):
+                L = int(length)
+                # insertion: ref = anchor, alt = anchor + L inserted bases
+                sel = np.nonzero(ins & (ln == L))[0]
+                if len(sel):
+                    ref[ind[sel]] = gch[sel, 0]
+                    chars = np.ascontiguousarray(np.concatenate([gch[sel, :1], added[sel, :L]], axis=1))
+                    alt[ind[sel]] = chars.view(f"<U{L + 1}").ravel()
+                # deletion: ref = anchor + L deleted bases, alt = anchor
+                sel = np.nonzero(~ins & (ln == L))[0]
+                if len(sel):
+                    ref[ind[sel]] = np.ascontiguousarray(gch[sel, :L + 1]).view(f"<U{L + 1}").ravel()
+                    alt[ind[sel]] = gch[sel, 0]
         return ref, alt
 
-    def _cause(self, t: dict) -> np.ndarray:
-        out = np.empty(len(t["sig"]), dtype=object)
-        for i, (s, k, nat) in enumerate(zip(t["sig"], t["kind"], t["nature"])):
-            names = self.engine.sig_names[int(k)]
-            out[i] = names[s] if s != 0xFF and s < len(names) else None
+    def _cause(self, t: dict, rows: np.ndarray | None = None) -> np.ndarray:
+        """Signature name of each row (None for drivers and unknown indices)."""
+        rows = np.arange(len(t["sig"])) if rows is None else np.asarray(rows, dtype=np.int64)
+        sig, kind = t["sig"][rows].astype(np.int64), t["kind"][rows]
+        out = np.full(len(rows), None, dtype=object)
+        for k in np.unique(kind):
+            names = list(self.engine.sig_names[int(k)]) if int(k) < len(self.engine.sig_names) else []
+            table = np.array(names + [None], dtype=object)
+            m = kind == k
+            sk = sig[m]
+            out[m] = table[np.where((sk == 0xFF) | (sk >= len(names)), len(names), sk)]
         return out
 
     def _chr_pos(self, locus: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
@@ -1267,37 +1287,48 @@ def _result_frame(pf: PhylogeneticForest, idx: np.ndarray, alt: np.ndarray, dep:
                   sample_names: list[str]) -> dict:
     """The wide data frame of get_result_dataframe (src/seq_simulation.cpp:142-181)
     over the rows idx (mutation indices, ascending; alt / dep are their
-    [sample][row] tables), merged by (chr, pos, ref, alt)."""
+    [sample][row] tables), merged by (chr, pos, ref, alt) in the order of
+    each SID's first row: occurrences add, the coverage is the first row's,
+    causes and classes are the sorted unions."""
     t = pf.table()
-    ref, altb = pf._ref_alt(t)
-    cause = pf._cause(t)
     idx = np.asarray(idx, dtype=np.int64)
-    chrn, pos = pf._chr_pos(t["locus"][idx])
-    # merge records that are the same SID (chr, pos, ref, alt): occurrences add, causes/classes union
-    keys = {}
-    order = []
-    for j, i in enumerate(idx):
-        k = (int(t["locus"][i]), ref[i], altb[i])
-        if k in keys:
-            keys[k].append(j)
-        else:
-            keys[k] = [j]
-            order.append(k)
-    rows = [keys[k] for k in order]                 # columns of alt / dep
-    first = np.array([r[0] for r in rows], dtype=np.int64)
-    firsti = idx[first] if len(first) else first
-    df = {
-        "chr": chrn[first] if len(first) else np.array([], dtype=object),
-        "chr_pos": pos[first] if len(first) else np.array([], dtype=np.int64),
-        "ref": ref[firsti] if len(first) else np.array([], dtype=object),
-        "alt": altb[firsti] if len(first) else np.array([], dtype=object),
-        "causes": np.array([";".join(sorted({c for c in cause[idx[r]] if c is not None})) or None for r in rows],
-                           dtype=object),
-        "classes": np.array([";".join(sorted(set(NATURES[t["nature"][idx[r]]]))) for r in rows], dtype=object),
-    }
+    ref, altb = pf._ref_alt(t, idx)
+    cause = pf._cause(t, idx)
+    nat = NATURES[t["nature"][idx]]
+    loc = t["locus"][idx].astype(np.int64)
+    n = len(idx)
+    # group the rows by SID: a stable sort on (locus, ref, alt) keeps each
+    # group's rows in index order
+    _, rc = np.unique(ref.astype(str), return_inverse=True) if n else (None, np.zeros(0, np.int64))
+    _, ac = np.unique(altb.astype(str), return_inverse=True) if n else (None, np.zeros(0, np.int64))
+    order = np.lexsort((ac, rc, loc))
+    if n:
+        ks = np.stack([loc[order], rc[order], ac[order]], axis=1)
+        new = np.ones(n, dtype=bool)
+        new[1:] = np.any(ks[1:] != ks[:-1], axis=1)
+    else:
+        new = np.zeros(0, dtype=bool)
+    gsorted = np.cumsum(new) - 1                     # group of each sorted row
+    first_sorted = order[new]                        # each group's first row (smallest index)
+    gorder = np.argsort(first_sorted, kind="stable")  # groups in the order of their first row
+    rank = np.empty(len(gorder), dtype=np.int64)
+    rank[gorder] = np.arange(len(gorder))
+    group = np.empty(n, dtype=np.int64)
+    group[order] = rank[gsorted]                     # output row of every input row
+    first = first_sorted[gorder]
+    ng = len(first)
+    sizes = np.bincount(group, minlength=ng)
+    chrn, pos = pf._chr_pos(loc[first] if ng else loc[:0])
+    causes = cause[first].copy()
+    classes = nat[first].astype(object)
+    for g in np.nonzero(sizes > 1)[0]:
+        members = np.nonzero(group == g)[0]
+        causes[g] = ";".join(sorted({c for c in cause[members] if c is not None})) or None
+        classes[g] = ";".join(sorted(set(nat[members])))
+    df = {"chr": chrn, "chr_pos": pos, "ref": ref[first], "alt": altb[first], "causes": causes, "classes": classes}
     for s, name in enumerate(sample_names):
-        occ = np.array([alt[s, r].sum() for r in rows], dtype=np.int32)
-        cov = dep[s, first].astype(np.int32) if len(first) else np.array([], dtype=np.int32)
+        occ = np.bincount(group, weights=alt[s], minlength=ng).astype(np.int32) if n else np.zeros(0, np.int32)
+        cov = dep[s, first].astype(np.int32)
         with np.errstate(divide="ignore", invalid="ignore"):
             vaf = np.where(cov > 0, occ / np.maximum(cov, 1), 0.0)
         df[f"{name}.occurrences"] = occ

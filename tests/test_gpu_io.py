@@ -101,3 +101,67 @@ def test_observed_rows(gpu_lib):
     rows0 = set(zip(f0["chr"], f0["chr_pos"], f0["ref"], f0["alt"]))
     rows1 = set(zip(f1["chr"], f1["chr_pos"], f1["ref"], f1["alt"]))
     assert rows0 <= rows1
+
+
+def _naive_frame(pf, alt, dep, names):
+    """The result frame built row by row (the definition the vectorised
+    builder must match): SIDs (locus, ref, alt) in order of first row."""
+    from process_gb300.engine import BASES, NATURES
+    t = pf.table()
+    eng = pf.engine
+    g = eng.read_genome()
+    keep = np.nonzero(alt.sum(axis=0) > 0)[0]
+    groups, order = {}, []
+    for i in keep:
+        a, k, loc = int(t["aux"][i]), int(t["kind"][i]), int(t["locus"][i])
+        if k == 0:
+            r, x = BASES[g[loc]], BASES[a & 3]
+        else:
+            ins, ln, b = a & 1, (a >> 1) & 7, a >> 8
+            if ins:
+                r = BASES[g[loc]]
+                x = r + "".join(BASES[(b >> (2 * q)) & 3] for q in range(ln))
+            else:
+                r = "".join(BASES[g[loc:loc + ln + 1]])
+                x = r[0]
+        key = (loc, r, x)
+        if key not in groups:
+            groups[key] = []
+            order.append(key)
+        groups[key].append(i)
+    out = {"ref": [k[1] for k in order], "alt": [k[2] for k in order], "locus": [k[0] for k in order]}
+    for s, name in enumerate(names):
+        out[f"{name}.occurrences"] = [int(alt[s, groups[k]].sum()) for k in order]
+        out[f"{name}.coverage"] = [int(dep[s, groups[k][0]]) for k in order]
+    out["classes"] = [";".join(sorted(set(NATURES[t["nature"][groups[k]]]))) for k in order]
+    return out
+
+
+def test_result_frame_matches_row_by_row(gpu_lib):
+    """The vectorised result frame equals the row-by-row definition, with
+    indels and (infinite sites off) several SIDs on one locus."""
+    from process_gb300 import synth
+    from process_gb300.engine import _result_frame, sequence_counts
+    w = synth.config1(seed=14, n_leaves=150)
+    w.genome.chr_lengths = [40_000, 20_000, 20_000]
+    w.mutants = [(n, dict(r, SNV=r["SNV"] * 20, indel=2e-6), d) for n, r, d in w.mutants]
+    eng = synth.build_engine(w)
+    eng.infinite_sites_model = False
+    pf = eng.place_mutations(w.forest, 50, 10, seed=8)
+    t = pf.table()
+    assert len(np.unique(t["locus"])) < len(t["locus"])        # repeated loci
+    r = sequence_counts(pf, 9, coverage=60, read_size=100, insert_size_mean=250, insert_size_stddev=10,
+                        error_rate=1e-3, purity=0.9)
+    a, d = r.counts()
+    names = [f"s{q}" for q in range(a.shape[0])]
+    df = _result_frame(pf, *r.observed(), names)
+    ref = _naive_frame(pf, a, d, names)
+    assert list(df["ref"]) == ref["ref"] and list(df["alt"]) == ref["alt"]
+    assert (t["kind"][np.nonzero(a.sum(axis=0) > 0)[0]] == 1).any()   # some indels observed
+    off = eng.chr_off.astype(np.int64)
+    loc = np.array([off[eng.chr_names.index(c)] for c in df["chr"]]) + df["chr_pos"] - 1
+    assert loc.tolist() == ref["locus"]
+    assert list(df["classes"]) == ref["classes"]
+    for name in names:
+        assert df[f"{name}.occurrences"].tolist() == ref[f"{name}.occurrences"]
+        assert df[f"{name}.coverage"].tolist() == ref[f"{name}.coverage"]
