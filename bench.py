@@ -157,6 +157,23 @@ def cpu_model() -> str:
     return "unknown"
 
 
+def replica_rate(units: float, ms: list[float], world: int, device) -> tuple[float, float, list[float]]:
+    """Whole-job throughput of independent replicas (no data-path
+    collective): the units all ranks processed over the slowest rank's time.
+    ``ms`` are this rank's timed spans (the first is the whole timed region);
+    returns (rate per second, total units, the spans' maxima over ranks)."""
+    import torch
+    import torch.distributed as dist
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    t = torch.tensor([float(x) for x in ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    spans = t.tolist()
+    total = float(u[0])
+    return total / (spans[0] / 1000.0), total, spans
+
+
 def reference_arm(args):
     rank = env_int("RANK", 0)
     if rank != 0:
@@ -376,12 +393,9 @@ def gpu_arm(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
         n_launch = launches() - n0
-    step_ms = (place_ms + seq_ms) / args.steps
-    t = torch.tensor([place_ms + seq_ms, place_ms, seq_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t[0])
-    value = world * reads / (total_ms / 1000.0)
+    value, _, t = replica_rate(reads, [place_ms + seq_ms, place_ms, seq_ms], world, "cuda")
+    _, all_muts, _ = replica_rate(muts, [1.0], world, "cuda")
+    step_ms = t[0] / args.steps
     # read-locus visits of the last step, for the roofline's algorithmic bytes
     pf, res = last
     alt, dep = res.counts()
@@ -428,7 +442,8 @@ def gpu_arm(args):
             n_reads += n_r
             n_bytes += sum(x.nbytes for x in arrays)
         torch.cuda.synchronize()
-        return world * n_reads / (time.perf_counter() - t0), n_bytes // max(1, e2e_steps)
+        rate, _, _ = replica_rate(n_reads, [1000.0 * (time.perf_counter() - t0)], world, "cuda")
+        return rate, n_bytes // max(1, e2e_steps)
 
     e2e_value, d2h_step = e2e_run(False, seed0 + 30_000)
     e2e_full_value, d2h_full_step = e2e_run(True, seed0 + 50_000)
@@ -458,8 +473,8 @@ def gpu_arm(args):
                        "mutations_per_step_per_gpu": muts // args.steps,
                        "l2": "flushed between steps (256 MiB write); record and count tables exceed L2",
                        "parallelism": f"replicas x{world}"},
-            "secondary": {"mutations_placed_per_s": world * muts / (float(t[1]) / 1000.0),
-                          "sequencing_reads_per_s": world * reads / (float(t[2]) / 1000.0),
+            "secondary": {"mutations_placed_per_s": all_muts / (t[1] / 1000.0),
+                          "sequencing_reads_per_s": value * t[0] / t[2],
                           "place_ms_per_step": float(t[1]) / args.steps, "seq_ms_per_step": float(t[2]) / args.steps,
                           "bracket_wall_s": wall,
                           "e2e_full_tables": {"value": e2e_full_value, "unit": "reads/s",
