@@ -1532,12 +1532,14 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
     // ---- tile size
     uint32_t T = c->tile_size;
     if (T == 0) {
-      // fragments per tile: 4 standard deviations below one shared-memory
-      // batch of the read kernel; at most 128 records per window, and a
-      // window that fits the start buckets
+      // fragments per tile: two shared-memory batches of the read kernel,
+      // each 4 standard deviations below its capacity (one batch per tile
+      // measured 1-3% slower: the per-tile set-up is paid twice as often);
+      // at most 128 records per window, and a window that fits the start
+      // buckets
       const double mates_per_frag = paired ? 2.0 : 1.0;
       const double cap = double(pg::SEQ_FRAGS_PER_BATCH);
-      const double target = cap - 4.0 * std::sqrt(cap);
+      const double target = 2.0 * (cap - 4.0 * std::sqrt(cap));
       double t = c->coverage > 0 ? target * R * mates_per_frag / c->coverage : 8192.0;
       const double density = double(pl->M) / double(e->G);
       if (density > 0) t = std::min(t, 128.0 / density);
