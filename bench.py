@@ -31,7 +31,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "reads/s + mutations placed/s on 1 GB300 vs host CPU; batched calib grad-evals/s"
-WORKLOAD = ("config2 full scale: 3.1 Gbp/24 chr GC 41%, 3 samples x 1e4 leaves, 3 epochs "
+WORKLOAD = ("full scale: 3.1 Gbp/24 chr GC 41%, 3 samples x 1e4 leaves, 3 epochs "
             "SNV {1.5e-8,3e-8,5e-8} indel 0.1x, 3 SBS + 2 ID signatures, 20 driver CNAs (1-50 Mbp, "
             "CN 0-4) + 1 WGD branch, 100x paired 150 bp, "
             "insert binomial(350, 10), purity 0.7, error 1e-3, + normal sample")
@@ -106,7 +106,7 @@ class ClockSampler:
 
 def cpu_sample_workload():
     from process_gb300 import synth
-    return synth.config2(seed=2, genome_scale=CPU_SAMPLE_SCALE)
+    return synth.full_scale(seed=2, genome_scale=CPU_SAMPLE_SCALE)
 
 
 def run_cpu(steps: int, warmup: int, threads: int, sample_desc: str):
@@ -199,7 +199,7 @@ def reference_arm(args):
 
 
 def batch_bench(stream, n_inst: int, steps: int, warmup: int):
-    """Batched replicates (config 3): every instance placed and sequenced in
+    """Batched replicates (256 forests on 100 Mbp): every instance placed and sequenced in
     one batch run (fused placement launches, one persistent read kernel under
     a CUDA graph, tile sizes from the autotuner).  Reads/s and placed
     mutations/s of whole runs, timed with CUDA events on the engine stream;
@@ -210,7 +210,7 @@ def batch_bench(stream, n_inst: int, steps: int, warmup: int):
 
     from process_gb300 import _lib, synth
     from process_gb300.engine import sequence_counts
-    w = synth.config3(seed=3, n_inst=n_inst)
+    w = synth.batch_256(seed=3, n_inst=n_inst)
     eng, b = synth.build_batch(w)
     _lib.check(_lib.lib().pg_engine_set_stream(eng._h, C.c_void_p(stream.cuda_stream)))
     seeds = np.arange(n_inst, dtype=np.uint64)
@@ -347,7 +347,7 @@ def gpu_arm(args):
     from process_gb300.engine import sequence_counts
     import ctypes as C
 
-    w = synth.config2(seed=2, genome_scale=args.genome_scale)
+    w = synth.full_scale(seed=2, genome_scale=args.genome_scale)
     eng = synth.build_engine(w)
     # a dedicated (non-default) stream: the engine runs on it and the CUDA
     # events that time the steps are recorded on it

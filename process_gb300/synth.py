@@ -6,11 +6,11 @@ simulation (SpatialSimulation, src/simulation.cpp); neither is available, so
 the workloads use seeded synthetic genomes, Dirichlet signatures and
 birth-process forests with the shapes of each configuration:
 
-* ``config1``: 3 x 1 Mbp uniform ACGT, ~2.5k leaves in one sample with a
+* ``plain_3mbp``: 3 x 1 Mbp uniform ACGT, ~2.5k leaves in one sample with a
   driver subclone (species A and A+), SNV 1e-6 and indel 1e-7 per base per
   division, one Dirichlet(0.5) SBS and one ID signature; 80x paired 150 bp,
   insert Normal(350, 30), error 1e-3.
-* ``config2``: 3.1 Gbp in 24 chromosomes at GC 41%, 3 samples x 1e4 leaves,
+* ``full_scale``: 3.1 Gbp in 24 chromosomes at GC 41%, 3 samples x 1e4 leaves,
   3 epochs with SNV {1.5e-8, 3e-8, 5e-8} and indels at 0.1x, 3 SBS + 2 ID
   Dirichlet(0.5) signatures with per-epoch exposures; 100x paired 150 bp,
   purity 0.7, error 1e-3.
@@ -111,21 +111,21 @@ class Workload:
     context_sampling: int = 1
 
 
-def config1(seed: int = 1, n_leaves: int = 2500) -> Workload:
+def plain_3mbp(seed: int = 1, n_leaves: int = 2500) -> Workload:
     rng = np.random.default_rng(seed)
     genome = GenomeSpec(["1", "2", "3"], [1_000_000] * 3, seed=seed, gc=0.5)
     sbs = dirichlet_signatures(rng, 1, 96, 0.5, "SBS")
     ids = dirichlet_signatures(rng, 1, 83, 0.5, "ID")
     forest = birth_forest(n_leaves, 1, seed, birth_rate=0.2, subclone=("B", 0.6), mutant="A")
     rates = {"SNV": 1e-6, "indel": 1e-7}
-    return Workload("config1: 3x1 Mbp, ~2.5k leaves, 80x paired 150 bp", genome, sbs, ids,
+    return Workload("plain_3mbp: 3x1 Mbp, ~2.5k leaves, 80x paired 150 bp", genome, sbs, ids,
                     [(0.0, {"SBS1": 1.0, "ID1": 1.0})], [("A", rates, []), ("B", rates, [])], forest,
                     n_pre_snv=100, n_pre_indel=10,
                     seq=dict(coverage=80, read_size=150, insert_size_mean=350, insert_size_stddev=30,
                              insert_model="normal", error_rate=1e-3, purity=1.0))
 
 
-def config2_cnas(rng: np.random.Generator, genome: GenomeSpec, scale: float) -> tuple[list, list]:
+def full_scale_cnas(rng: np.random.Generator, genome: GenomeSpec, scale: float) -> tuple[list, list]:
     """20 driver CNAs of 1-50 Mbp (times the genome scale) and one WGD branch.
 
     The founder clone A carries 10: four single-allele deletions (copy
@@ -163,7 +163,7 @@ def config2_cnas(rng: np.random.Generator, genome: GenomeSpec, scale: float) -> 
     return a, bl
 
 
-def config2(seed: int = 2, n_leaves_per_sample: int = 10_000, genome_scale: float = 1.0) -> Workload:
+def full_scale(seed: int = 2, n_leaves_per_sample: int = 10_000, genome_scale: float = 1.0) -> Workload:
     rng = np.random.default_rng(seed)
     total = int(3.1e9 * genome_scale)
     w = rng.dirichlet(np.full(24, 20.0))
@@ -182,8 +182,8 @@ def config2(seed: int = 2, n_leaves_per_sample: int = 10_000, genome_scale: floa
                               **{f"ID{i + 1}": float(e_i[i]) for i in range(2)}}))
     snv = [1.5e-8, 3e-8, 5e-8]
     rates = {"SNV": snv, "indel": [0.1 * x for x in snv]}
-    cna_a, cna_b = config2_cnas(rng, genome, genome_scale)
-    return Workload("config2: 3.1 Gbp/24 chr, 3x1e4 leaves, 3 epochs, 20 CNAs + 1 WGD branch, "
+    cna_a, cna_b = full_scale_cnas(rng, genome, genome_scale)
+    return Workload("full_scale: 3.1 Gbp/24 chr, 3x1e4 leaves, 3 epochs, 20 CNAs + 1 WGD branch, "
                     "100x paired 150 bp, purity 0.7",
                     genome, sbs, ids, exposures, [("A", rates, cna_a), ("B", rates, cna_b)], forest,
                     n_pre_snv=1000, n_pre_indel=100,
@@ -206,7 +206,7 @@ class BatchWorkload:
     context_sampling: int = 1
 
 
-def config3(seed: int = 3, n_inst: int = 256, leaves=(1_000, 50_000), genome_len: int = 100_000_000) -> BatchWorkload:
+def batch_256(seed: int = 3, n_inst: int = 256, leaves=(1_000, 50_000), genome_len: int = 100_000_000) -> BatchWorkload:
     """Batched replicates: n_inst forests with log-uniform leaf counts on one
     synthetic genome (4 chromosomes); per instance an SNV rate log-uniform in
     [1e-8, 1e-7] (indels at 0.1x), exposures Dirichlet(1) over 3 SBS and 2 ID
@@ -227,7 +227,7 @@ def config3(seed: int = 3, n_inst: int = 256, leaves=(1_000, 50_000), genome_len
     snv = 10 ** rng.uniform(-8, -7, n_inst)
     seq = [dict(coverage=float(rng.uniform(30, 200)), read_size=150, insert_size_mean=350, insert_size_stddev=10,
                 error_rate=1e-3, purity=1.0, with_normal_sample=False) for _ in range(n_inst)]
-    return BatchWorkload(f"config3: {n_inst} forests of {leaves[0]}-{leaves[1]} leaves (log-uniform) on a "
+    return BatchWorkload(f"batch_256: {n_inst} forests of {leaves[0]}-{leaves[1]} leaves (log-uniform) on a "
                          f"{genome_len / 1e6:.0f} Mbp genome, SNV 1e-8-1e-7 (log-uniform), indel 0.1x, "
                          "exposures Dirichlet(1), coverage U(30, 200)x paired 150 bp",
                          genome, sbs, ids, forests, snv, 0.1 * snv, rng.dirichlet(np.ones(3), n_inst),

@@ -94,11 +94,11 @@ def test_samples_forest_topological_order():
 
 def test_synthetic_workloads_shapes():
     from process_gb300 import synth
-    w = synth.config1(seed=3, n_leaves=200)
+    w = synth.plain_3mbp(seed=3, n_leaves=200)
     assert w.forest.num_of_nodes == 399
     assert w.forest.is_leaf.sum() == 200
     assert w.genome.total == 3_000_000
-    w2 = synth.config2(seed=3, n_leaves_per_sample=50, genome_scale=1e-3)
+    w2 = synth.full_scale(seed=3, n_leaves_per_sample=50, genome_scale=1e-3)
     assert len(w2.genome.chr_lengths) == 24 and len(w2.exposures) == 3
     assert sorted(set(w2.forest.sample_names)) == ["S_1", "S_2", "S_3"]
 

@@ -32,7 +32,7 @@ def test_synthetic_tables_shape():
 
 
 @pytest.mark.gpu
-def test_adjoint_matches_fp64_gradient_config4(gpu_lib):
+def test_adjoint_matches_fp64_gradient_2e5_sites(gpu_lib):
     """2e5 sites, depth ~ Poisson(100), K=4, 3 exposures per epoch: FP32 adjoint
     against the FP64 gradient and FP64 central differences (h = 1e-5),
     relative error < 1e-4."""

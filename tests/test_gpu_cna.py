@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 def _workload(seed, n_leaves, cna_rate=3e-9):
     from process_gb300 import CNA, SNV, WGD, synth
-    w = synth.config1(seed=seed, n_leaves=n_leaves)
+    w = synth.plain_3mbp(seed=seed, n_leaves=n_leaves)
     w.genome.chr_lengths = [600_000] * 3
     (na, ra, _), (nb, rb, _) = w.mutants
     w.mutants = [
@@ -102,7 +102,7 @@ def test_wgd_order_vaf_gpu(gpu_lib, orc):
     from process_gb300.engine import sequence_counts
     vafs = []
     for drivers in ([SNV("1", 50_000, "T", allele=0), WGD], [WGD, SNV("1", 50_000, "T", allele=0)]):
-        w = synth.config1(seed=6, n_leaves=100)
+        w = synth.plain_3mbp(seed=6, n_leaves=100)
         w.genome.chr_lengths = [200_000] * 3
         w.mutants = [(w.mutants[0][0], w.mutants[0][1], drivers), w.mutants[1]]
         eng = synth.build_engine(w)

@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 def test_save_load_round_trip(gpu_lib, tmp_path):
     from process_gb300 import CNA, SNV, WGD, load_phylogenetic_forest, synth
     from process_gb300.engine import sequence_counts
-    w = synth.config1(seed=4, n_leaves=150)
+    w = synth.plain_3mbp(seed=4, n_leaves=150)
     w.genome.chr_lengths = [200_000, 100_000, 100_000]
     (na, ra, _), (nb, rb, _) = w.mutants
     w.mutants = [(na, dict(ra, CNA=1e-8), [SNV("1", 5000, "T"), CNA("A", "2", 10_001, 20_000)]),
@@ -43,7 +43,7 @@ def test_counts_into_page_locked_buffers(gpu_lib):
     import torch
     from process_gb300 import synth
     from process_gb300.engine import sequence_counts
-    w = synth.config1(seed=12, n_leaves=100)
+    w = synth.plain_3mbp(seed=12, n_leaves=100)
     w.genome.chr_lengths = [100_000, 50_000, 50_000]
     eng = synth.build_engine(w)
     pf = eng.place_mutations(w.forest, 10, 2, seed=2)
@@ -69,7 +69,7 @@ def test_observed_rows(gpu_lib):
     import torch
     from process_gb300 import simulate_seq, synth
     from process_gb300.engine import sequence_counts
-    w = synth.config1(seed=13, n_leaves=200)
+    w = synth.plain_3mbp(seed=13, n_leaves=200)
     w.genome.chr_lengths = [120_000, 60_000, 60_000]
     eng = synth.build_engine(w)
     pf = eng.place_mutations(w.forest, 20, 4, seed=6)
@@ -142,7 +142,7 @@ def test_result_frame_matches_row_by_row(gpu_lib):
     indels and (infinite sites off) several SIDs on one locus."""
     from process_gb300 import synth
     from process_gb300.engine import _result_frame, sequence_counts
-    w = synth.config1(seed=14, n_leaves=150)
+    w = synth.plain_3mbp(seed=14, n_leaves=150)
     w.genome.chr_lengths = [40_000, 20_000, 20_000]
     w.mutants = [(n, dict(r, SNV=r["SNV"] * 20, indel=2e-6), d) for n, r, d in w.mutants]
     eng = synth.build_engine(w)

@@ -64,9 +64,9 @@ def test_explicit_bases_genome(gpu_lib, orc):
 
 
 @pytest.mark.parametrize("infinite", [True, False])
-def test_placement_bit_exact_config1(gpu_lib, orc, infinite):
+def test_placement_bit_exact_3mbp(gpu_lib, orc, infinite):
     from process_gb300 import synth
-    w = synth.config1(seed=3, n_leaves=800)
+    w = synth.plain_3mbp(seed=3, n_leaves=800)
     eng, o = make_pair(orc, w)
     eng.infinite_sites_model = infinite
     o.set_infinite_sites(infinite)
@@ -79,7 +79,7 @@ def test_placement_bit_exact_config1(gpu_lib, orc, infinite):
 def test_placement_bit_exact_epochs_drivers(gpu_lib, orc):
     """Three exposure epochs with per-epoch rates, compressed edges and drivers."""
     from process_gb300 import SNV, Mutation, synth
-    w = synth.config2(seed=4, n_leaves_per_sample=300, genome_scale=2e-3)
+    w = synth.full_scale(seed=4, n_leaves_per_sample=300, genome_scale=2e-3)
     w.mutants = [("A", w.mutants[0][1], []),
                  ("B", w.mutants[1][1], [SNV("1", 1000, "T", allele=1), Mutation("2", 500, "A", "ACG"),
                                          SNV("3", 77, "G")])]
@@ -110,7 +110,7 @@ def test_sequencing_bit_exact(gpu_lib, orc, case):
     from process_gb300 import synth
     from process_gb300.engine import seq_cfg, sequence_counts
     cfg = dict(SEQ_CASES[case])
-    w = synth.config1(seed=8, n_leaves=400)
+    w = synth.plain_3mbp(seed=8, n_leaves=400)
     eng, o = make_pair(orc, w)
     pf = eng.place_mutations(w.forest, 200, 20, seed=21)
     op = o.place(w.forest, oracle_species(o, w.forest), 200, 0, 20, 0, seed=21)
@@ -130,7 +130,7 @@ def test_distribution_against_reference_engine(gpu_lib, orc):
     and on VAF, GPU vs the std::mt19937_64 flavour; p > 0.01."""
     from process_gb300 import synth
     from process_gb300.engine import seq_cfg, sequence_counts
-    w = synth.config1(seed=11, n_leaves=300)
+    w = synth.plain_3mbp(seed=11, n_leaves=300)
     w.genome.chr_lengths = [300_000] * 3
     eng, o = make_pair(orc, w)
     sp = oracle_species(o, w.forest)
@@ -165,7 +165,7 @@ def test_edge_cases(gpu_lib, orc):
     from process_gb300 import (BasicIlluminaSequencer, ErrorlessIlluminaSequencer, ProcessError, simulate_seq,
                                simulate_normal_seq, synth)
     from process_gb300.engine import sequence_counts
-    w = synth.config1(seed=2, n_leaves=200)
+    w = synth.plain_3mbp(seed=2, n_leaves=200)
     eng, _ = make_pair(orc, w)
     pf = eng.place_mutations(w.forest, 100, 10, seed=1)
     # error rate 0 is the error-less sequencer
@@ -198,12 +198,12 @@ def test_edge_cases(gpu_lib, orc):
 
 
 def test_full_size_properties(gpu_lib):
-    """The full config-2 workload (3.1 Gbp, 3 x 1e4 leaves, 100x): properties
+    """The full-scale workload (3.1 Gbp, 3 x 1e4 leaves, 100x): properties
     that hold at any size — sorted unique loci, mean depth at the coverage,
     clonal VAF at purity/2, an error-only alt rate in the normal sample."""
     from process_gb300 import synth
     from process_gb300.engine import sequence_counts
-    w = synth.config2(seed=2)
+    w = synth.full_scale(seed=2)
     w.mutants = [(n, r, []) for n, r, _ in w.mutants]     # copy number 2 everywhere
     eng = synth.build_engine(w)
     pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=7)
@@ -223,13 +223,13 @@ def test_full_size_properties(gpu_lib):
 
 
 def test_full_size_copy_number_properties(gpu_lib):
-    """The full config-2 workload with its 20 CNAs and WGD branch: three
+    """The full-scale workload with its 20 CNAs and WGD branch: three
     genotype classes, one WGD record, passengers per edge scaled by the
     allelic size of the edge's genome (about 2x on the WGD branch), sorted
     unique loci and depth near the coverage."""
     from process_gb300 import synth
     from process_gb300.engine import sequence_counts
-    w = synth.config2(seed=2)
+    w = synth.full_scale(seed=2)
     eng = synth.build_engine(w)
     pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=7)
     t = pf.table()
@@ -238,7 +238,7 @@ def test_full_size_copy_number_properties(gpu_lib):
     assert n_cls == 3 and cn_max >= 4
     c = pf.cna_table()
     assert (c["type"] == 2).sum() == 1 and len(c["type"]) <= 24
-    w0 = synth.config2(seed=2)
+    w0 = synth.full_scale(seed=2)
     w0.mutants = [(n, r, []) for n, r, _ in w0.mutants]
     t0 = synth.build_engine(w0).place_mutations(w0.forest, w0.n_pre_snv, w0.n_pre_indel, seed=7).table()
     n = w.forest.num_of_nodes

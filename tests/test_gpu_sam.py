@@ -86,7 +86,7 @@ def _check_against_counts(pf, eng, tmp_path, cfg, names, seed=17):
 
 def test_sam_reads_match_counts(gpu_lib, tmp_path):
     from process_gb300 import synth
-    w = synth.config1(seed=9, n_leaves=150)
+    w = synth.plain_3mbp(seed=9, n_leaves=150)
     w.genome.chr_lengths = [120_000, 80_000, 60_000]
     w.mutants = [(n, dict(r, indel=0.0), d) for n, r, d in w.mutants]
     eng = synth.build_engine(w)
@@ -99,7 +99,7 @@ def test_sam_reads_match_counts(gpu_lib, tmp_path):
 
 def test_sam_with_copy_number_and_single_end(gpu_lib, tmp_path):
     from process_gb300 import CNA, WGD, synth
-    w = synth.config1(seed=10, n_leaves=120)
+    w = synth.plain_3mbp(seed=10, n_leaves=120)
     w.genome.chr_lengths = [150_000, 100_000, 50_000]
     (na, ra, _), (nb, rb, _) = w.mutants
     w.mutants = [(na, dict(ra, indel=0.0), [CNA("A", "1", 20_001, 40_000), CNA("D", "2", 10_001, 30_000, allele=0)]),
@@ -114,7 +114,7 @@ def test_sam_with_copy_number_and_single_end(gpu_lib, tmp_path):
 
 def test_sam_indels_naming_and_update(gpu_lib, tmp_path):
     from process_gb300 import DomainError, simulate_seq, synth
-    w = synth.config1(seed=11, n_leaves=100)
+    w = synth.plain_3mbp(seed=11, n_leaves=100)
     w.genome.chr_lengths = [100_000, 50_000, 50_000]
     w.mutants = [(n, dict(r, indel=2e-6), d) for n, r, d in w.mutants]
     eng = synth.build_engine(w)

@@ -61,7 +61,7 @@ def test_binomial_sampler(orc, n, p):
 
 def small_workload(seed=1, leaves=300):
     from process_gb300 import synth
-    return synth.config1(seed=seed, n_leaves=leaves)
+    return synth.plain_3mbp(seed=seed, n_leaves=leaves)
 
 
 def species_of(e, forest):

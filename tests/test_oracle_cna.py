@@ -21,7 +21,7 @@ def _cfg(**kw):
 
 def test_wgd_classes_and_copy_number(orc):
     from process_gb300 import synth
-    w = synth.config1(seed=5, n_leaves=200)
+    w = synth.plain_3mbp(seed=5, n_leaves=200)
     o = _engine(orc, w)
     o.add_driver_wgd(0)                      # mutant A: every tumour cell
     f = w.forest
@@ -47,7 +47,7 @@ def test_driver_then_wgd_vaf(orc, snv_first):
     """SNV then WGD: both copies of the mutated allele carry it (VAF 1/2 in a
     pure tumour); WGD then SNV: one allele of four (VAF 1/4)."""
     from process_gb300 import synth
-    w = synth.config1(seed=6, n_leaves=100)
+    w = synth.plain_3mbp(seed=6, n_leaves=100)
     w.genome.chr_lengths = [200_000] * 3
     o = _engine(orc, w)
     g = o.read_genome()
@@ -80,7 +80,7 @@ def _sid(chr_, pos, ref, alt, allele):
 @pytest.mark.parametrize("flavour", [0, 1])
 def test_deletion_halves_depth_and_hides_mutations(orc, flavour):
     from process_gb300 import synth
-    w = synth.config1(seed=7, n_leaves=100)
+    w = synth.plain_3mbp(seed=7, n_leaves=100)
     w.genome.chr_lengths = [300_000] * 3
     o = _engine(orc, w)
     # delete allele 0 of [100001, 200000] of chromosome 2 in every tumour cell
@@ -103,7 +103,7 @@ def test_deletion_halves_depth_and_hides_mutations(orc, flavour):
 @pytest.mark.parametrize("avoid", [True, False])
 def test_avoid_homozygous_losses(orc, avoid):
     from process_gb300 import synth
-    w = synth.config1(seed=8, n_leaves=300)
+    w = synth.plain_3mbp(seed=8, n_leaves=300)
     w.genome.chr_lengths = [100_000] * 3
     w.mutants = [(n, dict(r, CNA=2e-6), d) for n, r, d in w.mutants]
     o = _engine(orc, w)
