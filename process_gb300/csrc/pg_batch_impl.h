@@ -667,9 +667,10 @@ pg_status pg_batch_autotune(pg_batch* b, const uint64_t* place_seed, const uint6
     for (uint32_t i = 0; i < B; ++i) keys[i] = pg::make_key(seq_seed[i]);
     ck(cudaMemcpyAsync(b->skeys.p, keys.data(), sizeof(pg::Key) * B, cudaMemcpyHostToDevice, st), "keys");
     // candidates: multiples of each instance's analytic size (the fragment
-    // count of a tile 4 sigma below one shared-memory batch), timed as one
-    // whole persistent launch; the best of two repetitions counts
-    const double mult[] = {0.5, 0.75, 1.0, 1.25};
+    // count of a tile 4 sigma below one shared-memory batch; 1.5 and 2 give
+    // tiles of two batches), timed as one whole persistent launch; the best
+    // of two repetitions counts
+    const double mult[] = {0.5, 0.75, 1.0, 1.25, 1.5, 2.0};
     double best = 1e300;
     std::vector<uint32_t> best_T(B);
     for (double m : mult) {
