@@ -193,6 +193,13 @@ pg_status pg_placed_cna_copy(const pg_placed* placed, uint32_t* node, uint8_t* t
  * largest copy number of any position. */
 pg_status pg_placed_node_classes(const pg_placed* placed, uint32_t* node_class, uint32_t* n_classes,
                                  uint32_t* cn_max);
+/* The samples the next pg_simulate_seq calls sequence: sample_of_node[v] in
+ * [0, n_samples) puts leaf v (a sampled cell) in that sample, -1 leaves it
+ * out.  This is how the FACS labelling of simulate_seq(cell_labelling = f)
+ * (src/seq_simulation.cpp:183-243, split_by_labels / apply_FACS_labels)
+ * arrives: the shim evaluates f on each sampled cell before the call and
+ * passes the partition; sample names stay with the caller. */
+pg_status pg_placed_set_samples(pg_placed* placed, uint32_t n_samples, const int32_t* sample_of_node);
 /* Genotype classes as segments (for the allelic fragmentation getters,
  * src/phylogenetic_forest.cpp:767-927): class c covers the absolute 0-based
  * intervals [seg_start, seg_end) of its segments seg_off[c] .. seg_off[c+1]-1,

@@ -1284,6 +1284,24 @@ pg_status pg_placed_node_classes(const pg_placed* p, uint32_t* node_class, uint3
   });
 }
 
+pg_status pg_placed_set_samples(pg_placed* p, uint32_t n_samples, const int32_t* sample_of_node) {
+  return guarded([&] {
+    require(p != nullptr && sample_of_node != nullptr, "NULL argument");
+    std::vector<std::vector<uint32_t>> leaves(n_samples), leaf_cls(n_samples);
+    for (uint32_t v = 0; v < p->n_nodes; ++v) {
+      const int32_t s = sample_of_node[v];
+      if (s < 0) continue;
+      require(uint32_t(s) < n_samples, "sample index out of range");
+      require(p->tout[v] == p->tin[v] + 1, "only leaves (sampled cells) can be assigned to a sample");
+      leaves[s].push_back(p->tin[v]);
+      leaf_cls[s].push_back(p->node_class_h.empty() ? 0u : p->node_class_h[v]);
+    }
+    p->leaves = std::move(leaves);
+    p->leaf_cls = std::move(leaf_cls);
+    p->n_samples = n_samples;
+  });
+}
+
 pg_status pg_placed_kernel_ms(const pg_placed* p, float* ms) {
   return guarded([&] { require(p && ms, "NULL argument"); *ms = p->kernel_ms; });
 }

@@ -1384,6 +1384,72 @@ def _presence(pf: PhylogeneticForest, n_samples_seq: int, with_normal: bool, pre
     return present
 
 
+class SampledCell:
+    """A sampled cell as a ``cell_labelling`` function sees it (``SampledCell``
+    of src/sequencing.cpp:284-330): its epistate, mutant, species, birth time
+    and, on request, its mutations (the columns of
+    ``get_sampled_cell_mutations``)."""
+
+    def __init__(self, pf: "PhylogeneticForest", node: int):
+        self._pf = pf
+        self._node = int(node)
+
+    @property
+    def cell_id(self) -> int:
+        return int(self._pf.forest.cell_id[self._node])
+
+    @property
+    def epistate(self) -> str:
+        return str(self._pf.forest.epistate[self._node] or "")
+
+    @property
+    def mutant(self) -> str:
+        return str(self._pf.forest.mutant[self._node])
+
+    @property
+    def species(self) -> str:
+        return self.mutant + self.epistate
+
+    @property
+    def birth_time(self) -> float:
+        return float(self._pf.forest.birth_time[self._node])
+
+    @property
+    def mutations(self) -> dict:
+        return self._pf.get_sampled_cell_mutations(self.cell_id)
+
+
+def _forest_partition(pf: "PhylogeneticForest") -> np.ndarray:
+    f = pf.forest
+    return np.ascontiguousarray(np.where(f.is_leaf & (f.sample >= 0), f.sample, -1), dtype=np.int32)
+
+
+def _facs_partition(pf: "PhylogeneticForest", labelling) -> tuple[np.ndarray, list[str]]:
+    """FACS split of every sample by the label of each of its cells
+    (src/seq_simulation.cpp:183-243): the cells of a sample with one label
+    form the sample "<sample>_<label>" ("<sample>" for the empty label), in
+    the order the labels first appear, cells taken by identifier."""
+    if not callable(labelling):
+        raise DomainError(_lib.PG_ERR_DOMAIN, "The FACs_labelling_function must be a function.")
+    f = pf.forest
+    base = _forest_partition(pf)
+    part = np.full(f.num_of_nodes, -1, dtype=np.int32)
+    names: list[str] = []
+    for s, sname in enumerate(f.sample_names):
+        cells = np.nonzero(base == s)[0]
+        cells = cells[np.argsort(f.cell_id[cells], kind="stable")]
+        index: dict[str, int] = {}
+        for v in cells:
+            label = labelling(SampledCell(pf, v))
+            if not isinstance(label, str):
+                raise DomainError(_lib.PG_ERR_DOMAIN, "The FACS labelling function must return a string.")
+            if label not in index:
+                index[label] = len(names)
+                names.append(sname if label == "" else f"{sname}_{label}")
+            part[v] = index[label]
+    return part, names
+
+
 def simulate_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_genome=None, chromosomes=None,
                  coverage: float = 10, read_size: int = 150, insert_size_mean: int = 0, insert_size_stddev: int = 10,
                  output_dir: str = "ProCESS_SAM", write_SAM: bool = False, update_SAM: bool = False,
@@ -1395,18 +1461,28 @@ def simulate_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_gen
     ``{"mutations": data frame, "parameters": dict}``.  ``insert_model``
     "normal" adds a discretised normal insert size next to the reference's
     binomial model."""
-    if cell_labelling is not None:
-        raise _lib.UnsupportedError(_lib.PG_ERR_UNSUPPORTED, "cell_labelling (FACS) is not built in this version")
     err, seq_data = _sequencer_rate(sequencer)
     s = _seed(seed)
-    names = list(phylo_forest.forest.sample_names) + (["normal_sample"] if with_normal_sample else [])
+    samples = list(phylo_forest.forest.sample_names)
+    part = None
+    if cell_labelling is not None:
+        part, samples = _facs_partition(phylo_forest, cell_labelling)
+    names = samples + (["normal_sample"] if with_normal_sample else [])
     sam = (dict(output_dir=output_dir, update=update_SAM, filename_prefix=filename_prefix,
                 template_name_prefix=template_name_prefix, sample_names=names) if write_SAM else None)
-    res = sequence_counts(phylo_forest, s, sam=sam, coverage=coverage, read_size=read_size,
-                          insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
-                          purity=purity, with_normal_sample=with_normal_sample,
-                          preneoplastic_in_normal=preneoplastic_in_normal, chromosomes=chromosomes,
-                          tile_size=tile_size, insert_model=insert_model)
+    if part is not None:
+        check(lib().pg_placed_set_samples(phylo_forest._h, len(samples), ptr(part, C.c_int32)))
+    try:
+        res = sequence_counts(phylo_forest, s, sam=sam, coverage=coverage, read_size=read_size,
+                              insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev,
+                              error_rate=err, purity=purity, with_normal_sample=with_normal_sample,
+                              preneoplastic_in_normal=preneoplastic_in_normal, chromosomes=chromosomes,
+                              tile_size=tile_size, insert_model=insert_model)
+    finally:
+        if part is not None:
+            base = _forest_partition(phylo_forest)
+            check(lib().pg_placed_set_samples(phylo_forest._h, len(phylo_forest.forest.sample_names),
+                                              ptr(base, C.c_int32)))
     present = (_presence(phylo_forest, len(names), with_normal_sample, preneoplastic_in_normal)
                if include_non_sequenced_mutations else None)
     df = _result_frame(phylo_forest, *_result_rows(res, include_non_sequenced_mutations, present), names)
