@@ -62,7 +62,8 @@ pg_status pg_device_count(int* n);
 typedef struct {
   uint32_t n_chr;
   const uint32_t* chr_lengths;      /* bases per chromosome */
-  const uint8_t* bases;             /* concatenated codes A=0 C=1 G=2 T=3, or NULL: synthetic genome */
+  const uint8_t* bases;             /* concatenated codes A=0 C=1 G=2 T=3, above 3 an unknown base (N,
+                                       not indexed, read as 4 and as N in SAM), or NULL: synthetic genome */
   uint64_t synthetic_seed;          /* seeded i.i.d. bases when bases == NULL */
   double synthetic_gc;              /* GC fraction of the synthetic genome */
   uint32_t context_sampling;        /* keep 1 in N occurrences per context (reference default 100) */

@@ -272,6 +272,7 @@ void id_classes(const Genome& g, uint32_t p, int out[16]) {
   if (p <= cs || p >= ce) return;
   auto get = [&](int64_t q) -> int { return (q >= int64_t(cs) && q < int64_t(ce)) ? g.b[q] : 4; };
   const int b = get(p), prev = get(int64_t(p) - 1);
+  if (b == 4 || prev == 4) return;     // the site or its anchor is unknown (N)
   int h = 1;
   while (h < 6 && get(int64_t(p) + h) == b) ++h;
   const bool runstart = prev != b;
@@ -338,7 +339,9 @@ void build_index(Engine& e) {
   for (uint64_t p = 0; p < G; ++p) {
     const uint32_t c = e.g.chr_of(uint32_t(p));
     const uint32_t cs = e.g.off[c], ce = e.g.off[c + 1];
-    if (p > cs && p + 1 < ce) all_ctx[context_of(e.g.b[p - 1], e.g.b[p], e.g.b[p + 1])].push_back(uint32_t(p));
+    // a context with an unknown base (code 4, N) is not indexed
+    if (p > cs && p + 1 < ce && e.g.b[p - 1] < 4 && e.g.b[p] < 4 && e.g.b[p + 1] < 4)
+      all_ctx[context_of(e.g.b[p - 1], e.g.b[p], e.g.b[p + 1])].push_back(uint32_t(p));
     int cl[16];
     id_classes(e.g, uint32_t(p), cl);
     for (int f = 0; f < 16; ++f) if (cl[f] >= 0) all_id[cl[f]].push_back(uint32_t(p));
@@ -1509,7 +1512,9 @@ void* orc_engine_create(uint32_t n_chr, const uint32_t* chr_len, const uint8_t* 
     for (uint32_t c = 0; c < n_chr; ++c) { e->g.off[c] = uint32_t(G); G += chr_len[c]; }
     e->g.off[n_chr] = uint32_t(G);
     e->g.b.resize(G);
-    if (bases) std::memcpy(e->g.b.data(), bases, G);
+    if (bases) {   // codes above 3 (N and the other ambiguity codes) are unknown: 4
+      for (uint64_t i = 0; i < G; ++i) e->g.b[i] = bases[i] > 3 ? uint8_t(4) : bases[i];
+    }
     else orc_genome_synth(G, seed, gc, e->g.b.data());
     e->context_sampling = context_sampling;
     e->max_rep = max_rep;

@@ -211,6 +211,7 @@ struct pg_engine {
   std::vector<uint32_t> chr_len, chr_off;  // chr_off: n_chr + 1 entries
   uint64_t G = 0;
   DBuf<uint32_t> genome, chr_off_d;
+  DBuf<uint32_t> nmask;              // unknown bases (N), one bit each; empty when the genome has none
   uint32_t context_sampling = 100, max_rep = 500000;
   // index
   std::vector<uint64_t> ctx_total, id_total;
@@ -332,7 +333,7 @@ void build_indices(pg_engine* e) {
     DBuf<uint32_t> cnt(&e->pool, uint64_t(NC) * ntiles);
     DBuf<uint32_t> part(&e->pool, pg::scan_part_elems(ntiles, NC));
     DBuf<uint32_t> tot(&e->pool, NC);
-    pg::index_count(which, e->genome.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, part.p, tot.p, e->st);
+    pg::index_count(which, e->genome.p, e->nmask.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, part.p, tot.p, e->st);
     std::vector<uint32_t> tot_h(NC);
     ck(cudaMemcpyAsync(tot_h.data(), tot.p, sizeof(uint32_t) * NC, cudaMemcpyDeviceToHost, e->st), "index totals");
     ck(cudaStreamSynchronize(e->st), "index count");
@@ -354,7 +355,8 @@ void build_indices(pg_engine* e) {
     std::vector<uint64_t> off_k(off.begin(), off.begin() + NC);
     auto off_d = upload(&e->pool, off_k, e->st);
     DBuf<uint32_t> lists(&e->pool, off[NC]);
-    pg::index_emit(which, e->genome.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p, off_d.p, len_d.p,
+    pg::index_emit(which, e->genome.p, e->nmask.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p, off_d.p,
+                   len_d.p,
                    lists.p, e->st);
     ck(cudaStreamSynchronize(e->st), "index emit");
     ck(cudaGetLastError(), "index kernels");
@@ -469,7 +471,15 @@ pg_status pg_engine_create(const pg_genome_desc* gd, pg_engine** out) {
       DBuf<uint8_t> codes(&e->pool, G);
       ck(cudaMemcpyAsync(codes.p, gd->bases, G, cudaMemcpyHostToDevice, e->st), "genome upload");
       pg::genome_pack(e->genome.p, codes.p, G, e->st);
+      // codes above 3 (N and the other ambiguity codes) are unknown bases
+      e->nmask = DBuf<uint32_t>(&e->pool, (G + 31) / 32 + 1);
+      DBuf<uint32_t> any(&e->pool, 1);
+      ck(cudaMemsetAsync(any.p, 0, sizeof(uint32_t), e->st), "memset");
+      pg::genome_nmask(codes.p, G, e->nmask.p, any.p, e->st);
+      uint32_t any_h = 0;
+      ck(cudaMemcpyAsync(&any_h, any.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->st), "unknown bases");
       ck(cudaStreamSynchronize(e->st), "genome pack");
+      if (!any_h) e->nmask.reset();
     } else {
       require(gd->synthetic_gc >= 0 && gd->synthetic_gc <= 1, "synthetic_gc must be in [0,1]");
       pg::genome_synth(e->genome.p, G, gd->synthetic_seed, gd->synthetic_gc, e->st);
@@ -533,9 +543,15 @@ pg_status pg_engine_read_genome(const pg_engine* e, uint64_t start, uint64_t n, 
     std::vector<uint32_t> words(w1 - w0);
     if (!words.empty())
       ck(cudaMemcpy(words.data(), e->genome.p + w0, sizeof(uint32_t) * words.size(), cudaMemcpyDeviceToHost), "read");
+    // unknown bases read as 4
+    const uint64_t m0 = start / 32, m1 = (start + n + 31) / 32;
+    std::vector<uint32_t> mask(e->nmask.p ? m1 - m0 : 0);
+    if (!mask.empty())
+      ck(cudaMemcpy(mask.data(), e->nmask.p + m0, sizeof(uint32_t) * mask.size(), cudaMemcpyDeviceToHost), "read");
     for (uint64_t i = 0; i < n; ++i) {
       const uint64_t p = start + i;
-      out[i] = uint8_t((words[p / 16 - w0] >> (2 * (p % 16))) & 3u);
+      const bool unknown = !mask.empty() && ((mask[p / 32 - m0] >> (p % 32)) & 1u);
+      out[i] = unknown ? uint8_t(4) : uint8_t((words[p / 16 - w0] >> (2 * (p % 16))) & 3u);
     }
   });
 }
@@ -549,7 +565,7 @@ pg_status pg_engine_gather_bases(const pg_engine* e, uint64_t n, const uint32_t*
     DBuf<uint32_t> pd(P, n);
     DBuf<uint8_t> od(P, n);
     ck(cudaMemcpyAsync(pd.p, pos, 4 * n, cudaMemcpyHostToDevice, e->st), "upload");
-    pg::genome_gather(e->genome.p, e->G, pd.p, n, od.p, e->st);
+    pg::genome_gather(e->genome.p, e->nmask.p, e->G, pd.p, n, od.p, e->st);
     ck(cudaMemcpyAsync(out, od.p, n, cudaMemcpyDeviceToHost, e->st), "download");
     ck(cudaStreamSynchronize(e->st), "gather");
   });
@@ -1767,6 +1783,7 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
     prm.has_cna = pl->has_cna ? 1u : 0u;
     prm.gc = pl->classes_view();
     prm.chain_off = pl->chain_off.p; prm.chain_anc = pl->chain_anc.p; prm.chain_key = pl->chain_key.p;
+    prm.nmask = e->nmask.p;
     if (pl->has_cna) {
       prm.n_classes = pl->n_classes;
       prm.atom_ioff = pl->atom_ioff.p; prm.atom_icnt = pl->atom_icnt.p;

@@ -78,8 +78,10 @@ struct SbsFamilies {
   __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
     out[0] = -1;
     if (p <= cs || p + 1 >= ce) return;
+    const uint32_t x = get(p - 1), y = get(p), z = get(p + 1);
+    if (x > 3u || y > 3u || z > 3u) return;          // an unknown base (N) in the context
     bool fwd;
-    out[0] = context_of(get(p - 1), get(p), get(p + 1), &fwd);
+    out[0] = context_of(x, y, z, &fwd);
   }
 };
 
@@ -105,6 +107,7 @@ struct IdFamilies {
     for (int f = 0; f < NF; ++f) out[f] = -1;
     if (p <= cs || p >= ce) return;
     const uint32_t b = get(p), prev = get(p - 1);
+    if (b > 3u || prev > 3u) return;                 // the site or its anchor is unknown (N)
     int h = 1;
     while (h < 6 && get(p + h) == b) ++h;
     const bool runstart = prev != b;
@@ -153,19 +156,26 @@ struct WarpWindow {
   uint32_t start;  // absolute position of s[0]
 };
 
-__device__ __forceinline__ void load_window(const uint32_t* __restrict__ g, uint64_t G, uint32_t tile_start,
-                                            uint8_t* s, int lane) {
+// unknown bases (N) are bits of nmask (NULL: none), one bit per position
+__device__ __forceinline__ bool base_unknown(const uint32_t* __restrict__ nmask, uint32_t q) {
+  return nmask && ((__ldg(nmask + (q >> 5)) >> (q & 31u)) & 1u);
+}
+
+__device__ __forceinline__ void load_window(const uint32_t* __restrict__ g, const uint32_t* __restrict__ nmask,
+                                            uint64_t G, uint32_t tile_start, uint8_t* s, int lane) {
   const int64_t w0 = int64_t(tile_start) - WIN_BEFORE;
   for (int i = lane; i < WIN; i += 32) {
     const int64_t q = w0 + i;
-    s[i] = (q >= 0 && uint64_t(q) < G) ? uint8_t(base_at(g, uint32_t(q))) : uint8_t(BASE_INVALID);
+    s[i] = (q >= 0 && uint64_t(q) < G && !base_unknown(nmask, uint32_t(q))) ? uint8_t(base_at(g, uint32_t(q)))
+                                                                           : uint8_t(BASE_INVALID);
   }
   __syncwarp();
 }
 
 // mode 0: count; mode 1: emit positions
 template <class F, int MODE>
-__global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__ g, uint64_t G,
+__global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__ g,
+                                                    const uint32_t* __restrict__ nmask, uint64_t G,
                                                     const uint32_t* __restrict__ chr_off, int n_chr,
                                                     uint32_t ntiles, uint32_t* __restrict__ cnt,
                                                     const uint32_t* __restrict__ stride,
@@ -180,7 +190,7 @@ __global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__
   const uint32_t tile_start = tile * TILE;
   for (int k = lane; k < F::NC; k += 32)
     s_run[warp][k] = MODE == 0 ? 0u : cnt[uint64_t(k) * ntiles + tile];
-  load_window(g, G, tile_start, s_win[warp], lane);
+  load_window(g, nmask, G, tile_start, s_win[warp], lane);
   // chromosome of the tile start
   int c = 0;
   {
@@ -245,35 +255,37 @@ void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t
 uint32_t index_num_tiles(uint64_t G) { return uint32_t((G + TILE - 1) / TILE); }
 
 template <class F>
-static void index_count_t(const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+static void index_count_t(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
                           uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_pass<F, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles, cnt,
+  k_index_pass<F, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, G, chr_off, n_chr, ntiles, cnt,
                                                                   nullptr, nullptr, nullptr, nullptr); note_launch();
   scan_rows<uint32_t>(cnt, cnt, ntiles, F::NC, part, totals, st);
 }
 
 template <class F>
-static void index_emit_t(const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+static void index_emit_t(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
                          const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
                          const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_pass<F, 1><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles,
+  k_index_pass<F, 1><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, G, chr_off, n_chr, ntiles,
                                                                   const_cast<uint32_t*>(cnt_scanned),
                                                                   stride, list_off, list_len, lists); note_launch();
 }
 
-void index_count(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+void index_count(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
                  uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
-  if (which == 0) index_count_t<SbsFamilies>(g, G, chr_off, n_chr, cnt, part, totals, st);
-  else index_count_t<IdFamilies>(g, G, chr_off, n_chr, cnt, part, totals, st);
+  if (which == 0) index_count_t<SbsFamilies>(g, nmask, G, chr_off, n_chr, cnt, part, totals, st);
+  else index_count_t<IdFamilies>(g, nmask, G, chr_off, n_chr, cnt, part, totals, st);
 }
 
-void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+void index_emit(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
                 const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
                 const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
-  if (which == 0) index_emit_t<SbsFamilies>(g, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
-  else index_emit_t<IdFamilies>(g, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+  if (which == 0)
+    index_emit_t<SbsFamilies>(g, nmask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+  else
+    index_emit_t<IdFamilies>(g, nmask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
 }
 
 int index_num_classes(int which) { return which == 0 ? SbsFamilies::NC : IdFamilies::NC; }
@@ -331,10 +343,12 @@ const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const
   const int nc = index_num_classes(which);
   // every (class, tile) entry is written by the count pass: nothing to clear
   if (which == 0)
-    k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles, scratch,
+    k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, G, chr_off, n_chr, ntiles,
+                                                                              scratch,
                                                                               nullptr, nullptr, nullptr, nullptr);
   else
-    k_index_pass<IdFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, G, chr_off, n_chr, ntiles, scratch,
+    k_index_pass<IdFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, G, chr_off, n_chr, ntiles,
+                                                                             scratch,
                                                                              nullptr, nullptr, nullptr, nullptr);
   k_class_totals<<<nc, 256, 0, st>>>(scratch, ntiles, totals);
   note_launch(2);
@@ -346,14 +360,36 @@ const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const
 
 namespace pg {
 
-__global__ void k_gather_bases(const uint32_t* __restrict__ g, const uint32_t* __restrict__ pos, uint64_t n,
-                               uint64_t G, uint8_t* __restrict__ out) {
+__global__ void k_gather_bases(const uint32_t* __restrict__ g, const uint32_t* __restrict__ nmask,
+                               const uint32_t* __restrict__ pos, uint64_t n, uint64_t G, uint8_t* __restrict__ out) {
   const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = pos[i] < G ? uint8_t(base_at(g, pos[i])) : uint8_t(BASE_INVALID);
+  if (i < n)
+    out[i] = pos[i] < G && !base_unknown(nmask, pos[i]) ? uint8_t(base_at(g, pos[i])) : uint8_t(BASE_INVALID);
 }
 
-void genome_gather(const uint32_t* g, uint64_t G, const uint32_t* pos, uint64_t n, uint8_t* out, cudaStream_t st) {
-  if (n) { k_gather_bases<<<unsigned((n + 255) / 256), 256, 0, st>>>(g, pos, n, G, out); note_launch(); }
+void genome_gather(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* pos, uint64_t n,
+                   uint8_t* out, cudaStream_t st) {
+  if (n) { k_gather_bases<<<unsigned((n + 255) / 256), 256, 0, st>>>(g, nmask, pos, n, G, out); note_launch(); }
+}
+
+// the unknown bases (codes > 3) of an uploaded genome as one bit per position,
+// and whether there is any
+__global__ void k_genome_nmask(const uint8_t* __restrict__ codes, uint64_t G, uint64_t nwords,
+                               uint32_t* __restrict__ mask, uint32_t* __restrict__ any) {
+  const uint64_t w = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= nwords) return;
+  uint32_t m = 0;
+  for (int j = 0; j < 32; ++j) {
+    const uint64_t i = w * 32 + j;
+    if (i < G && codes[i] > 3u) m |= 1u << j;
+  }
+  mask[w] = m;
+  if (m) atomicOr(any, 1u);
+}
+
+void genome_nmask(const uint8_t* codes, uint64_t G, uint32_t* mask, uint32_t* any, cudaStream_t st) {
+  const uint64_t nwords = (G + 31) / 32;
+  if (nwords) { k_genome_nmask<<<unsigned((nwords + 255) / 256), 256, 0, st>>>(codes, G, nwords, mask, any); note_launch(); }
 }
 
 }  // namespace pg

@@ -21,17 +21,24 @@ void note_launch(uint32_t n = 1);
 // ---------------------------------------------------------------- index
 void genome_synth(uint32_t* words, uint64_t G, uint64_t seed, double gc, cudaStream_t st);
 void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t st);
+// unknown bases (codes > 3, e.g. N) as one bit per position ((G + 31) / 32
+// words); *any (zeroed by the caller) becomes 1 when there is one.  A NULL
+// mask below means a genome without unknown bases.
+void genome_nmask(const uint8_t* codes, uint64_t G, uint32_t* mask, uint32_t* any, cudaStream_t st);
 uint32_t index_num_tiles(uint64_t G);
-void genome_gather(const uint32_t* g, uint64_t G, const uint32_t* pos, uint64_t n, uint8_t* out, cudaStream_t st);
+// bases at pos (BASE_INVALID for positions outside the genome or unknown)
+void genome_gather(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* pos, uint64_t n,
+                   uint8_t* out, cudaStream_t st);
 int index_num_classes(int which);  // 0 = SBS contexts (32), 1 = ID classes (83)
 // allocation-free per-class totals over a caller-held genome (see pg_index.cu);
 // returns nullptr on success, else a message
 constexpr uint32_t NOALLOC_MAX_TILES = 8192;
 const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
                                  uint64_t* totals, cudaStream_t st);
-void index_count(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr, uint32_t* cnt,
-                 uint32_t* part, uint32_t* totals, cudaStream_t st);
-void index_emit(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
+// contexts and repeat sites that touch an unknown base are not indexed
+void index_count(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
+                 uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st);
+void index_emit(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
                 const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
                 const uint32_t* list_len, uint32_t* lists, cudaStream_t st);
 
@@ -195,6 +202,7 @@ struct SeqParams {
   const uint32_t* opt_nleaf;      // 0: the normal cells
   const uint32_t* cls_leaf_tin;   // every sample's leaves grouped by class (Euler indices)
   const uint32_t* opt_cdf;        // option thresholds (see SeqSample)
+  const uint32_t* nmask;          // unknown reference bases (N), one bit each, or NULL (SAM output)
 };
 
 // tile t of chromosome slot c (c_first[c] <= t < c_first[c] + c_ntiles[c],

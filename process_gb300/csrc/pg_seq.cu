@@ -607,7 +607,9 @@ __device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ ge
     uint32_t tb = carried_snv ? alt : b;
     const uint32_t e = err_word(w, q, mate);
     if (e < prm.err_thr) tb = others(tb, site ? int(carried_snv ? b : alt) : -1, e % 3u);
-    seq[n++] = ACGT[tb];
+    // an unknown reference base (N) reads as N
+    const bool unknown = prm.nmask && ((__ldg(prm.nmask + (q >> 5)) >> (q & 31u)) & 1u);
+    seq[n++] = unknown ? 'N' : ACGT[tb];
     push(0u, 1u);
     ++q;
     if (has_indel && indels_open && nc < SAM_MAX_CIGAR - 2) {

@@ -28,7 +28,7 @@ import numpy as np
 from . import _lib
 from ._lib import DomainError, check, lib, ptr
 
-BASES = np.array(list("ACGT"))
+BASES = np.array(list("ACGTN"))   # base codes; 4: unknown (N)
 _SUBS = ["C>A", "C>G", "C>T", "T>A", "T>C", "T>G"]
 SBS_CLASSES = [f"{f}[{s}]{t}" for s in _SUBS for f in "ACGT" for t in "ACGT"]
 ID_CLASSES = (
@@ -66,6 +66,43 @@ class GenomeSpec:
     @property
     def total(self) -> int:
         return int(np.sum(np.asarray(self.chr_lengths, dtype=np.uint64)))
+
+    @classmethod
+    def from_fasta(cls, path: str, chromosomes: Sequence[str] | None = None) -> "GenomeSpec":
+        """A reference genome read from a FASTA file (gzip-compressed when the
+        name ends in .gz), the reference's input to its context and repeat
+        indices (src/mutation_engine.cpp:211-359).  Each record's name is the
+        first word of its header; ``chromosomes`` keeps only those records, in
+        the file's order.  A, C, G, T (either case) become codes 0-3; every
+        other letter (N and the other ambiguity codes) is an unknown base
+        (code 4), which no context or repeat site that touches it indexes."""
+        import gzip
+        opener = gzip.open if str(path).endswith(".gz") else open
+        with opener(path, "rb") as fh:
+            data = fh.read()
+        lut = np.full(256, 4, dtype=np.uint8)
+        for k, c in enumerate(b"ACGT"):
+            lut[c] = k
+            lut[c + 32] = k                       # lower case
+        keep = None if chromosomes is None else {str(c) for c in chromosomes}
+        names, lengths, parts = [], [], []
+        for rec in data.split(b">")[1:]:
+            head, _, body = rec.partition(b"\n")
+            name = head.split()[0].decode() if head.split() else ""
+            if keep is not None and name not in keep:
+                continue
+            seq = body.translate(None, b"\r\n\t ")
+            if not seq:
+                raise DomainError(_lib.PG_ERR_DOMAIN, f'FASTA record "{name}" has no bases')
+            names.append(name)
+            lengths.append(len(seq))
+            parts.append(lut[np.frombuffer(seq, dtype=np.uint8)])
+        if keep is not None and len(set(names)) != len(keep):
+            missing = sorted(keep - set(names))
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"chromosomes not in {path}: {', '.join(missing)}")
+        if not names:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"no chromosome read from {path}")
+        return cls(names, lengths, bases=np.concatenate(parts))
 
 
 # ---------------------------------------------------------------- driver specs
@@ -637,7 +674,7 @@ class PhylogeneticForest:
         alt = np.empty(n, dtype=object)
         snv = kind == 0
         rb = eng.gather_bases(locus[snv])
-        ref[snv] = BASES[np.minimum(rb, 3)]
+        ref[snv] = BASES[np.minimum(rb, 4)]
         alt[snv] = BASES[aux[snv] & 3]
         ind = np.nonzero(~snv)[0]
         if len(ind):
@@ -645,7 +682,7 @@ class PhylogeneticForest:
             ins, ln, bases = (a & 1).astype(bool), (a >> 1) & 7, a >> 8
             # the anchor and the 7 bases after it (a deletion spans at most 7)
             win = np.minimum(locus[ind][:, None] + np.arange(8)[None, :], eng.genome.total - 1)
-            gch = BASES[np.minimum(eng.gather_bases(win.ravel()).reshape(-1, 8), 3)]
+            gch = BASES[np.minimum(eng.gather_bases(win.ravel()).reshape(-1, 8), 4)]
             added = BASES[(bases[:, None] >> (2 * np.arange(7))[None, :]) & 3]
             for length in np.unique(ln):
                 L = int(length)

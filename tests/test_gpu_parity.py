@@ -250,3 +250,51 @@ def test_full_size_copy_number_properties(gpu_lib):
     res = sequence_counts(pf, 9, **w.seq)
     alt, dep = res.counts()
     assert 80 < dep[:3].mean() < 130
+
+
+def test_unknown_bases_genome(gpu_lib, orc, tmp_path):
+    """A genome with unknown bases (N runs, an isolated N, N across a
+    chromosome boundary): the same genome codes (4 for N) and index lists as
+    the oracle, placement and sequencing bit-exact, no mutation on or
+    anchored at an N, and N in the SAM reads over them."""
+    from pathlib import Path
+
+    from process_gb300 import simulate_seq, synth
+    from process_gb300.engine import seq_cfg, sequence_counts
+    w = synth.plain_3mbp(seed=19, n_leaves=150)
+    w.genome.chr_lengths = [60_000, 40_000, 40_000]
+    rng = np.random.default_rng(4)
+    b = rng.integers(0, 4, 140_000).astype(np.uint8)
+    b[1000:3000] = 4
+    b[7777] = 4
+    b[59_990:60_010] = 4
+    b[120_000:121_500] = 4
+    w.genome.bases = b
+    eng, o = make_pair(orc, w)
+    np.testing.assert_array_equal(eng.read_genome(), b)
+    np.testing.assert_array_equal(eng.read_genome(), o.read_genome())
+    for c in range(32):
+        np.testing.assert_array_equal(eng.read_index(0, c), o.read_index(0, c))
+    for c in range(83):
+        np.testing.assert_array_equal(eng.read_index(1, c), o.read_index(1, c))
+    assert int(eng.gather_bases(np.array([7777], dtype=np.uint32))[0]) == 4
+    pf = eng.place_mutations(w.forest, 100, 10, seed=6)
+    op = o.place(w.forest, oracle_species(o, w.forest), 100, 0, 10, 0, seed=6)
+    assert_tables_equal(pf.table(), op.table())
+    loc = pf.table()["locus"].astype(np.int64)
+    assert not (b[loc] == 4).any()
+    cfg = dict(coverage=20, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3, purity=0.8)
+    alt, dep = sequence_counts(pf, 12, tile_size=4096, **cfg).counts()
+    c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=4096, **cfg)
+    oalt, odep, _ = op.sequence(c, 12, flavour=0)
+    np.testing.assert_array_equal(dep, odep)
+    np.testing.assert_array_equal(alt, oalt)
+    out = tmp_path / "sam"
+    simulate_seq(pf, coverage=5, write_SAM=True, output_dir=str(out), insert_size_mean=350, insert_size_stddev=10,
+                 seed=2)
+    n_count = 0
+    for f in sorted(Path(out).glob("*.sam")):
+        for line in f.read_text().splitlines():
+            if not line.startswith("@"):
+                n_count += line.split("\t")[9].count("N")
+    assert n_count > 0
