@@ -949,6 +949,96 @@ class PhylogeneticForest:
     def get_germline_mutations(self) -> dict:
         return {k: np.array([]) for k in ("chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
 
+    def get_driver_mutations(self) -> dict:
+        """The declared driver mutations (src/phylogenetic_forest.cpp:172-218):
+        per mutant, in name order, its drivers in application order, with
+        the columns mutant, order, type ("SID", "CNA" or "WGD"), CNA_type
+        ("A" or "D"), chr, start, end, ref, alt, allele and src_allele (None
+        where the reference reports NA)."""
+        eng = self.engine
+        specs = {}
+        for name, _, drivers in eng._mutant_specs:
+            specs[name] = list(drivers)
+        cols = {k: [] for k in ("mutant", "order", "type", "CNA_type", "chr", "start", "end", "ref", "alt",
+                                "allele", "src_allele")}
+
+        def row(**kw):
+            for k in cols:
+                cols[k].append(kw.get(k))
+
+        for name in sorted(specs):
+            for k, d in enumerate(specs[name]):
+                if d is WGD:
+                    row(mutant=name, order=k, type="WGD")
+                elif isinstance(d, CNA):
+                    row(mutant=name, order=k, type="CNA", CNA_type=d.type, chr=str(d.chr), start=int(d.chr_pos),
+                        end=int(d.chr_pos) + int(d.len) - 1, allele=d.allele,
+                        src_allele=d.src_allele if d.type == "A" else None)
+                else:
+                    ref = d.ref
+                    if "?" in ref:
+                        ref = eng.get_bases(eng._chr_index(d.chr), int(d.chr_pos), max(1, len(ref)))
+                    row(mutant=name, order=k, type="SID", chr=str(d.chr), start=int(d.chr_pos),
+                        end=int(d.chr_pos) + len(ref) - 1, ref=ref, alt=d.alt, allele=d.allele)
+        return {k: np.array(v, dtype=object) for k, v in cols.items()}
+
+    def get_exposures(self) -> dict:
+        """The timed exposures (src/phylogenetic_forest.cpp:644-668): time,
+        signature, exposure and type, the SNV (SBS) rows then the indel (ID)
+        rows, each by time and signature name."""
+        eng = self.engine
+        timed: list[dict] = [{}, {}]
+        for t, coef in eng._exposures:
+            for ty in (0, 1):
+                part = {k: float(v) for k, v in coef.items() if k in eng.sig_names[ty]}
+                if part:
+                    timed[ty][float(t)] = part
+        cols = {k: [] for k in ("time", "signature", "exposure", "type")}
+        for ty, tname in ((0, "SNV"), (1, "indel")):
+            for t in sorted(timed[ty]):
+                for sig in sorted(timed[ty][t]):
+                    cols["time"].append(t)
+                    cols["signature"].append(sig)
+                    cols["exposure"].append(timed[ty][t][sig])
+                    cols["type"].append(tname)
+        return {"time": np.array(cols["time"], dtype=np.float64), "signature": np.array(cols["signature"], dtype=object),
+                "exposure": np.array(cols["exposure"], dtype=np.float64), "type": np.array(cols["type"], dtype=object)}
+
+    def get_first_occurrences(self, mutation) -> list:
+        """The identifiers of the cells in which a mutation (an SNV/indel
+        ``Mutation`` or a ``CNA``) first occurs (src/phylogenetic_forest.cpp:565-622):
+        the cells at the ends of the edges it was placed on (the forest's
+        first cells for a preneoplastic mutation), ascending."""
+        f = self.forest
+        eng = self.engine
+        roots = np.nonzero(f.parent < 0)[0]
+        if isinstance(mutation, CNA):
+            c = self.cna_table()
+            ci = eng._chr_index(mutation.chr)
+            typ = 1 if mutation.type == "A" else 0
+            hit = ((c["type"] == typ) & (c["chr"] == ci) & (c["begin"] == int(mutation.chr_pos)) &
+                   (c["end"] == int(mutation.chr_pos) + int(mutation.len) - 1))
+            nodes = c["node"][hit].astype(np.int64)
+        elif isinstance(mutation, Mutation):
+            t = self.table()
+            ci = eng._chr_index(mutation.chr)
+            locus = int(eng.chr_off[ci]) + int(mutation.chr_pos) - 1
+            cand = np.nonzero(t["locus"].astype(np.int64) == locus)[0]
+            ref, alt = self._ref_alt(t, cand) if len(cand) else (np.array([]), np.array([]))
+            want_ref = None if "?" in mutation.ref else mutation.ref
+            keep = [i for j, i in enumerate(cand)
+                    if alt[j] == mutation.alt and (want_ref is None or ref[j] == want_ref)]
+            nodes = t["edge"][keep].astype(np.int64) if keep else np.zeros(0, dtype=np.int64)
+        else:
+            raise DomainError(_lib.PG_ERR_DOMAIN, "This methods exclusively accepts as the parameters "
+                                                  "SNV, Indel, or CNA objects.")
+        if len(nodes) == 0:
+            raise DomainError(_lib.PG_ERR_DOMAIN, f"The mutation {mutation} does not occurs in the sampled cells.")
+        cells = set()
+        for v in nodes:
+            cells.update(int(x) for x in (f.cell_id[roots] if v >= f.num_of_nodes else [f.cell_id[v]]))
+        return sorted(cells)
+
 
 # ---------------------------------------------------------------- save / load
 FOREST_FORMAT = "process_gb300.phylogenetic_forest"

@@ -1,0 +1,62 @@
+"""PhylogeneticForest getters beside the mutation tables: the declared
+driver mutations, the timed exposures and the cells where a mutation first
+occurs (src/phylogenetic_forest.cpp:172-218, 565-668)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _forest():
+    from process_gb300 import CNA, SNV, WGD, synth
+    w = synth.plain_3mbp(seed=21, n_leaves=200)
+    w.genome.chr_lengths = [200_000, 100_000, 100_000]
+    (na, ra, _), (nb, rb, _) = w.mutants
+    w.mutants = [(na, ra, [SNV("1", 5000, "T"), CNA("A", "2", 10_001, 20_000), CNA("D", "3", 1_001, 5_000, allele=0)]),
+                 (nb, rb, [WGD])]
+    eng = synth.build_engine(w)
+    return w, eng, eng.place_mutations(w.forest, 20, 2, seed=3)
+
+
+def test_driver_mutations_and_exposures(gpu_lib):
+    w, eng, pf = _forest()
+    d = pf.get_driver_mutations()
+    (na, _, _), (nb, _, _) = w.mutants
+    rows = list(zip(d["mutant"], d["order"], d["type"], d["CNA_type"], d["chr"], d["start"], d["end"]))
+    ref = eng.get_bases(0, 5000, 1)
+    want = sorted([(na, 0, "SID", None, "1", 5000, 5000), (na, 1, "CNA", "A", "2", 10_001, 30_000),
+                   (na, 2, "CNA", "D", "3", 1_001, 6_000), (nb, 0, "WGD", None, None, None, None)],
+                  key=lambda r: (r[0], r[1]))
+    assert rows == want
+    sid = list(d["type"]).index("SID")
+    dele = [k for k in range(len(rows)) if d["CNA_type"][k] == "D"][0]
+    assert d["ref"][sid] == ref and d["alt"][sid] == "T" and d["allele"][dele] == 0
+    e = pf.get_exposures()
+    n = sum(len([k for k in c if k in eng.sig_names[0]]) + len([k for k in c if k in eng.sig_names[1]])
+            for _, c in eng._exposures)
+    assert len(e["time"]) == n
+    assert set(e["type"]) <= {"SNV", "indel"}
+    snv = e["type"] == "SNV"
+    assert np.all(np.diff(e["time"][snv]) >= 0) and np.all(np.diff(e["time"][~snv]) >= 0)
+
+
+def test_first_occurrences(gpu_lib):
+    from process_gb300 import CNA, DomainError, Mutation
+    w, eng, pf = _forest()
+    f = w.forest
+    t = pf.table()
+    # a passenger SNV: the cell at the end of its edge
+    i = int(np.nonzero((t["kind"] == 0) & (t["nature"] == 0))[0][0])
+    ref, alt = pf._ref_alt(t, np.array([i]))
+    chrn, pos = pf._chr_pos(t["locus"][[i]])
+    cells = pf.get_first_occurrences(Mutation(str(chrn[0]), int(pos[0]), str(ref[0]), str(alt[0])))
+    assert int(f.cell_id[t["edge"][i]]) in cells
+    # the driver SNV and the driver amplification: the first cell of the mutant's first edge
+    c = pf.cna_table()
+    amp = np.nonzero((c["type"] == 1) & (c["driver"] == 1))[0][0]
+    assert pf.get_first_occurrences(CNA("A", "2", 10_001, 20_000)) == [int(f.cell_id[c["node"][amp]])]
+    drv = np.nonzero(t["nature"] == 1)[0]
+    cells = pf.get_first_occurrences(Mutation("1", 5000, "?", "T"))
+    assert cells == sorted({int(f.cell_id[v]) for v in t["edge"][drv]})
+    with pytest.raises(DomainError, match="does not occurs"):
+        pf.get_first_occurrences(Mutation("1", 7, "A", "C"))
