@@ -949,6 +949,21 @@ class PhylogeneticForest:
     def get_germline_mutations(self) -> dict:
         return {k: np.array([]) for k in ("chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
 
+    def get_species_info(self) -> dict:
+        """The registered species (src/phylogenetic_forest.cpp:220-255):
+        mutant, epistate, SNV_rate, indel_rate and CNA_rate."""
+        r = self.engine.get_species_rates()
+        return {"mutant": r["mutant"], "epistate": r["epistate"], "SNV_rate": r["SNV"], "indel_rate": r["indel"],
+                "CNA_rate": r["CNA"]}
+
+    def get_reference_path(self) -> str:
+        """The reference genome path recorded with the forest (the FASTA the
+        engine was built from, when it was)."""
+        return getattr(self, "_reference_path", "")
+
+    def set_reference_path(self, path: str) -> None:
+        self._reference_path = str(path)
+
     def get_driver_mutations(self) -> dict:
         """The declared driver mutations (src/phylogenetic_forest.cpp:172-218):
         per mutant, in name order, its drivers in application order, with

@@ -31,6 +31,10 @@ def test_driver_mutations_and_exposures(gpu_lib):
     sid = list(d["type"]).index("SID")
     dele = [k for k in range(len(rows)) if d["CNA_type"][k] == "D"][0]
     assert d["ref"][sid] == ref and d["alt"][sid] == "T" and d["allele"][dele] == 0
+    sp = pf.get_species_info()
+    assert set(sp) == {"mutant", "epistate", "SNV_rate", "indel_rate", "CNA_rate"} and len(sp["mutant"]) >= 2
+    pf.set_reference_path("ref.fa")
+    assert pf.get_reference_path() == "ref.fa"
     e = pf.get_exposures()
     n = sum(len([k for k in c if k in eng.sig_names[0]]) + len([k for k in c if k in eng.sig_names[1]])
             for _, c in eng._exposures)
