@@ -201,6 +201,18 @@ pg_status pg_placed_node_classes(const pg_placed* placed, uint32_t* node_class, 
  * arrives: the shim evaluates f on each sampled cell before the call and
  * passes the partition; sample names stay with the caller. */
 pg_status pg_placed_set_samples(pg_placed* placed, uint32_t n_samples, const int32_t* sample_of_node);
+/* The allele-instance lineage behind the per-cell mutation lists of
+ * get_sampled_cell_mutations (src/phylogenetic_forest.cpp:452-507, where an
+ * SID sits on every allele copied from its allele after it and leaves with a
+ * deleted allele): for instance y, its ancestors chain_anc[chain_off[y] ..
+ * chain_off[y+1]) nearest first, each with the order key of the copy that
+ * led towards y; order_key[m] is mutation m's key (tin of its edge << 16 |
+ * order on the edge, in the order of pg_placed_copy).  Instance y carries
+ * mutation m placed on instance x when y == x or x is in y's chain with a
+ * key above order_key[m]. */
+pg_status pg_placed_lineage_dims(const pg_placed* placed, uint32_t* n_instances, uint32_t* n_links);
+pg_status pg_placed_lineage_copy(const pg_placed* placed, uint32_t* chain_off, uint16_t* chain_anc,
+                                 uint64_t* chain_key, uint64_t* order_key);
 /* Genotype classes as segments (for the allelic fragmentation getters,
  * src/phylogenetic_forest.cpp:767-927): class c covers the absolute 0-based
  * intervals [seg_start, seg_end) of its segments seg_off[c] .. seg_off[c+1]-1,

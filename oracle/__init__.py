@@ -49,6 +49,7 @@ def lib() -> C.CDLL:
             "orc_engine_index_info": (None, [P, u64p, u64p, u32p, u32p]),
             "orc_engine_read_index": (None, [P, C.c_int, C.c_uint32, u32p]),
             "orc_engine_read_genome": (None, [P, u8p]),
+            "orc_placed_carriers": (C.c_uint64, [P, u32p, u32p]),
             "orc_engine_set_signatures": (None, [P, C.c_int, C.c_uint32, f64p]),
             "orc_engine_add_exposure": (None, [P, C.c_int, C.c_double, f64p]),
             "orc_engine_set_species_rates": (None, [P, C.c_uint32, C.c_double, C.c_double, C.c_double]),
@@ -283,6 +284,14 @@ class OraclePlaced:
         inst, b, e = (np.empty(n, dtype=np.uint32) for _ in range(3))
         lib().orc_placed_class_pieces(self._h, c, _p(inst, C.c_uint32), _p(b, C.c_uint32), _p(e, C.c_uint32))
         return inst, b, e
+
+    def carriers(self):
+        """Per placed mutation the instances carrying it: (offsets, list)."""
+        n = lib().orc_placed_carriers(self._h, None, None)
+        off = np.empty(len(self.table()["locus"]) + 1, dtype=np.uint32)
+        lst = np.empty(max(n, 1), dtype=np.uint32)
+        lib().orc_placed_carriers(self._h, _p(off, C.c_uint32), _p(lst, C.c_uint32))
+        return off, lst[:n]
 
     def inst_roots(self):
         n = lib().orc_placed_inst_roots(self._h, None)

@@ -1657,6 +1657,19 @@ uint64_t orc_placed_class_pieces(void* pp, uint32_t c, uint32_t* inst, uint32_t*
     }
   return n;
 }
+// carrier instances of every placed mutation (carrier_sets): off has M + 1
+// entries; returns the total (list may be NULL to size it)
+uint64_t orc_placed_carriers(void* pp, uint32_t* off, uint32_t* list) {
+  auto* p = static_cast<Placed*>(pp);
+  const auto cs = carrier_sets(*p);
+  uint64_t n = 0;
+  for (size_t i = 0; i < cs.size(); ++i) {
+    if (off) off[i] = uint32_t(n);
+    for (uint32_t y : cs[i]) { if (list) list[n] = y; ++n; }
+  }
+  if (off) off[cs.size()] = uint32_t(n);
+  return n;
+}
 uint32_t orc_placed_inst_roots(void* pp, uint8_t* root) {
   auto* p = static_cast<Placed*>(pp);
   std::vector<uint32_t> from(p->n_inst);

@@ -279,6 +279,9 @@ struct pg_placed {
   // host copy of the class segments and each instance's germline allele
   std::vector<uint32_t> seg_off_h, seg_start_h, seg_end_h, seg_ioff_h, seg_icnt_h;
   std::vector<uint16_t> inst_list_h;
+  std::vector<uint32_t> chain_off_h;   // instance lineage chains (host copies)
+  std::vector<uint16_t> chain_anc_h;
+  std::vector<uint64_t> chain_key_h;
   std::vector<uint8_t> inst_root_h;
   DBuf<uint32_t> atom_start, atom_ioff, atom_icnt;
   DBuf<uint32_t> node_class, seg_off, seg_start, seg_end, seg_ioff, seg_icnt, chain_off;
@@ -1028,6 +1031,7 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
       chain_off.push_back(uint32_t(chain_anc.size()));
     }
     pl->has_cna = classes.size() > 1 || insts.size() > 2;
+    pl->chain_off_h = chain_off; pl->chain_anc_h = chain_anc; pl->chain_key_h = chain_key;
     pl->seg_off_h = seg_off; pl->seg_start_h = seg_start; pl->seg_end_h = seg_end;
     pl->seg_ioff_h = seg_ioff; pl->seg_icnt_h = seg_icnt; pl->inst_list_h = inst_list;
     pl->inst_root_h.resize(insts.size());
@@ -1297,6 +1301,37 @@ pg_status pg_placed_node_classes(const pg_placed* p, uint32_t* node_class, uint3
     if (node_class) std::copy(p->node_class_h.begin(), p->node_class_h.begin() + p->n_nodes, node_class);
     if (n_classes) *n_classes = p->n_classes;
     if (cn_max) *cn_max = p->cn_max;
+  });
+}
+
+pg_status pg_placed_lineage_dims(const pg_placed* p, uint32_t* n_instances, uint32_t* n_links) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    if (n_instances) *n_instances = p->chain_off_h.empty() ? 0u : uint32_t(p->chain_off_h.size() - 1);
+    if (n_links) *n_links = uint32_t(p->chain_anc_h.size());
+  });
+}
+
+pg_status pg_placed_lineage_copy(const pg_placed* p, uint32_t* chain_off, uint16_t* chain_anc, uint64_t* chain_key,
+                                 uint64_t* order_key) {
+  return guarded([&] {
+    require(p != nullptr, "NULL handle");
+    if (chain_off) std::copy(p->chain_off_h.begin(), p->chain_off_h.end(), chain_off);
+    if (chain_anc) std::copy(p->chain_anc_h.begin(), p->chain_anc_h.end(), chain_anc);
+    if (chain_key) std::copy(p->chain_key_h.begin(), p->chain_key_h.end(), chain_key);
+    if (order_key && p->M) {
+      // (tin of the mutation's edge << 16) | its order on the edge; the
+      // preneoplastic edge has tin 0
+      select_device(p->eng);
+      std::vector<uint32_t> edge(p->M);
+      std::vector<uint16_t> seq(p->M);
+      ck(cudaMemcpy(edge.data(), p->edge.p, sizeof(uint32_t) * p->M, cudaMemcpyDeviceToHost), "copy");
+      ck(cudaMemcpy(seq.data(), p->seq.p, sizeof(uint16_t) * p->M, cudaMemcpyDeviceToHost), "copy");
+      for (uint64_t i = 0; i < p->M; ++i) {
+        const uint64_t tin = edge[i] < p->n_nodes ? p->tin[edge[i]] : 0u;
+        order_key[i] = (tin << 16) | (seq[i] & 0x7fffu);
+      }
+    }
   });
 }
 

@@ -730,9 +730,72 @@ class PhylogeneticForest:
         e = t["edge"]
         return np.isin(e, np.fromiter(path, dtype=np.int64)) | (e == f.num_of_nodes)
 
+    def _lineage(self) -> dict:
+        """Instance lineage chains and every mutation's order key
+        (pg_placed_lineage_copy)."""
+        if getattr(self, "_lin_cache", None) is None:
+            ni, nl = C.c_uint32(), C.c_uint32()
+            check(lib().pg_placed_lineage_dims(self._h, C.byref(ni), C.byref(nl)))
+            d = {"off": np.zeros(ni.value + 1, np.uint32), "anc": np.zeros(max(nl.value, 1), np.uint16),
+                 "key": np.zeros(max(nl.value, 1), np.uint64),
+                 "order": np.zeros(max(self.num_of_mutations, 1), np.uint64)}
+            check(lib().pg_placed_lineage_copy(self._h, ptr(d["off"], C.c_uint32), ptr(d["anc"], C.c_uint16),
+                                               ptr(d["key"], C.c_uint64), ptr(d["order"], C.c_uint64)))
+            d["n_instances"] = ni.value
+            self._lin_cache = d
+        return self._lin_cache
+
+    def _cell_rows(self, leaf: int) -> tuple[np.ndarray, np.ndarray]:
+        """(mutation rows, allele instance) of the mutations sampled cell
+        ``leaf`` holds: those on its root path, once per allele instance of
+        its genome at the locus that carries them (the placed instance, and
+        the copies of it made after the mutation), in mutation order."""
+        t = self.table()
+        idx = np.nonzero(self.leaf_carriers(leaf))[0]
+        lin = self._lineage()
+        cls, n_classes, _ = self.node_classes()
+        if n_classes <= 1 and lin["n_instances"] <= 2:       # no copy-number event
+            return idx, t["allele"][idx].astype(np.int64)
+        d = self._classes()
+        c = int(cls[leaf])
+        lo, hi = int(d["seg_off"][c]), int(d["seg_off"][c + 1])
+        st, en = d["start"][lo:hi].astype(np.int64), d["end"][lo:hi].astype(np.int64)
+        loc = t["locus"][idx].astype(np.int64)
+        k = np.searchsorted(st, loc, side="right") - 1
+        inside = (k >= 0) & (loc < en[np.maximum(k, 0)]) if hi > lo else np.zeros(len(idx), bool)
+        ks = np.maximum(k, 0)
+        ioff = d["ioff"][lo:hi][ks].astype(np.int64) if hi > lo else np.zeros(len(idx), np.int64)
+        icnt = np.where(inside, d["icnt"][lo:hi][ks], 0).astype(np.int64) if hi > lo else np.zeros(len(idx), np.int64)
+        x = t["allele"][idx].astype(np.int64)
+        km = lin["order"][idx]
+        coff = lin["off"].astype(np.int64)
+        rows, alle, slot = [], [], []
+        for j in range(int(icnt.max()) if len(icnt) else 0):
+            sel = np.nonzero(j < icnt)[0]
+            y = d["list"][ioff[sel] + j].astype(np.int64)
+            carry = y == x[sel]
+            # y's lineage: x in its chain with a copy key above the mutation's
+            b, ln = coff[y], coff[y + 1] - coff[y]
+            found = carry.copy()
+            for dep in range(int(ln.max()) if len(ln) else 0):
+                act = ~found & (dep < ln)
+                a = np.where(act, lin["anc"][np.where(act, b + dep, 0)].astype(np.int64), -1)
+                hit = act & (a == x[sel])
+                carry |= hit & (lin["key"][np.where(hit, b + dep, 0)] > km[sel])
+                found |= hit
+            rows.append(idx[sel][carry]); alle.append(y[carry]); slot.append(np.full(int(carry.sum()), j))
+        if not rows:
+            return idx[:0], idx[:0].astype(np.int64)
+        r, a, s_ = np.concatenate(rows), np.concatenate(alle), np.concatenate(slot)
+        o = np.lexsort((s_, r))
+        return r[o], a[o]
+
     def get_sampled_cell_mutations(self, cell_id=None) -> dict:
         """Columns cell_id, chr, chr_pos, allele, ref, alt, type, cause, class
-        (src/phylogenetic_forest.cpp:452-507)."""
+        (src/phylogenetic_forest.cpp:452-507): every mutation a sampled cell
+        holds, once per allele instance of its genome carrying it (an SID is
+        copied with its allele by an amplification or a WGD after it, and
+        leaves with a deleted allele); ``allele`` is the instance."""
         f = self.forest
         t = self.table()
         leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
@@ -741,18 +804,15 @@ class PhylogeneticForest:
             if len(hit) == 0 or not f.is_leaf[hit[0]]:
                 raise DomainError(_lib.PG_ERR_DOMAIN, f'Cell "{cell_id}" is not a leaf')
             leaves = hit
-        ref, alt = self._ref_alt(t)
-        cause = self._cause(t)
-        chrn, pos = self._chr_pos(t["locus"])
-        cols = {k: [] for k in ("cell_id", "chr", "chr_pos", "allele", "ref", "alt", "type", "cause", "class")}
-        for lf in leaves:
-            m = self.leaf_carriers(lf)
-            cols["cell_id"].append(np.full(m.sum(), f.cell_id[lf]))
-            cols["chr"].append(chrn[m]); cols["chr_pos"].append(pos[m]); cols["allele"].append(t["allele"][m])
-            cols["ref"].append(ref[m]); cols["alt"].append(alt[m])
-            cols["type"].append(np.where(t["kind"][m] == 0, "SNV", "indel"))
-            cols["cause"].append(cause[m]); cols["class"].append(NATURES[t["nature"][m]])
-        return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
+        per = [self._cell_rows(int(lf)) for lf in leaves]
+        rows = np.concatenate([r for r, _ in per]) if per else np.zeros(0, np.int64)
+        alle = np.concatenate([a for _, a in per]) if per else np.zeros(0, np.int64)
+        cell = np.concatenate([np.full(len(r), f.cell_id[lf]) for lf, (r, _) in zip(leaves, per)]) if per else rows
+        ref, alt = self._ref_alt(t, rows)
+        chrn, pos = self._chr_pos(t["locus"][rows])
+        return {"cell_id": cell, "chr": chrn, "chr_pos": pos, "allele": alle.astype(np.int64), "ref": ref, "alt": alt,
+                "type": np.where(t["kind"][rows] == 0, "SNV", "indel"), "cause": self._cause(t, rows),
+                "class": NATURES[t["nature"][rows]]}
 
     def cna_table(self) -> dict:
         """Applied CNA / WGD events: node, type (0 deletion, 1 amplification,
