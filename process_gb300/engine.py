@@ -203,10 +203,11 @@ class BasicIlluminaSequencer:
 
 
 # ---------------------------------------------------------------- forest
-def preorder(par: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+def preorder(par: np.ndarray, with_size: bool = False):
     """Depth-first preorder of a forest given parent indices (-1 for roots;
     roots and children visited in index order): the order and each node's
-    position in it.  Level by level with numpy; raises on a cycle."""
+    position in it (and, with_size, each subtree's node count).  Level by
+    level with numpy; raises on a cycle."""
     par = np.asarray(par, dtype=np.int64)
     n = len(par)
     root = par < 0
@@ -243,7 +244,7 @@ def preorder(par: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         pos[lvl] = pos[p] + 1 + (cs - sz) - (cs[head] - sz[head])
     order = np.empty(n, dtype=np.int64)
     order[pos] = np.arange(n)
-    return order, pos
+    return (order, pos, size) if with_size else (order, pos)
 
 
 class SamplesForest:
@@ -292,6 +293,15 @@ class SamplesForest:
         is_parent = np.zeros(n, dtype=bool)
         is_parent[self.parent[self.parent >= 0]] = True
         self.is_leaf = ~is_parent
+
+    def euler(self) -> tuple[np.ndarray, np.ndarray]:
+        """(tin, tout) of every node: its depth-first preorder position and one
+        past its subtree's last, so v is an ancestor-or-self of u iff
+        tin[v] <= tin[u] < tout[v]."""
+        if getattr(self, "_euler", None) is None:
+            _, pos, size = preorder(self.parent, with_size=True)
+            self._euler = (pos, pos + size)
+        return self._euler
 
     def species_codes(self) -> tuple[list[tuple[str, str]], np.ndarray]:
         """The distinct (mutant, epistate) pairs and each node's index among
@@ -719,16 +729,16 @@ class PhylogeneticForest:
         return names, (locus.astype(np.int64) - off[ci].astype(np.int64) + 1)
 
     def leaf_carriers(self, leaf: int) -> np.ndarray:
-        """Mask of the placed mutations carried by node ``leaf``."""
+        """Mask of the placed mutations on the root path of node ``leaf``
+        (their edge an ancestor-or-self of it) and the preneoplastic ones."""
         f = self.forest
-        path = set()
-        v = int(leaf)
-        while v >= 0:
-            path.add(v)
-            v = int(f.parent[v])
-        t = self.table()
-        e = t["edge"]
-        return np.isin(e, np.fromiter(path, dtype=np.int64)) | (e == f.num_of_nodes)
+        tin, tout = f.euler()
+        e = self.table()["edge"].astype(np.int64)
+        n = f.num_of_nodes
+        inner = e < n
+        ec = np.minimum(e, n - 1)
+        x = tin[int(leaf)]
+        return ~inner | ((tin[ec] <= x) & (x < tout[ec]))
 
     def _lineage(self) -> dict:
         """Instance lineage chains and every mutation's order key
@@ -1555,26 +1565,7 @@ def _presence(pf: PhylogeneticForest, n_samples_seq: int, with_normal: bool, pre
     f = pf.forest
     t = pf.table()
     n = f.num_of_nodes
-    # Euler intervals
-    kids = [[] for _ in range(n)]
-    roots = []
-    for v in range(n):
-        (roots if f.parent[v] < 0 else kids[f.parent[v]]).append(v)
-    tin, tout = np.zeros(n, np.int64), np.zeros(n, np.int64)
-    clock = 0
-    for r in roots:
-        stack = [(r, 0)]
-        tin[r] = clock; clock += 1
-        while stack:
-            v, k = stack[-1]
-            if k < len(kids[v]):
-                stack[-1] = (v, k + 1)
-                c = kids[v][k]
-                tin[c] = clock; clock += 1
-                stack.append((c, 0))
-            else:
-                tout[v] = clock
-                stack.pop()
+    tin, tout = f.euler()
     leaf_tins = np.sort(tin[f.is_leaf & (f.sample >= 0)])
     e = t["edge"].astype(np.int64)
     real = e < n

@@ -122,3 +122,29 @@ def test_load_phylogenetic_forest_errors(tmp_path):
                                         dtype=np.uint8))
     with pytest.raises(DomainError, match="format version 99"):
         load_phylogenetic_forest(str(newer))
+
+
+def test_forest_euler_and_path_carriers():
+    """Euler intervals of a samples forest give the ancestor relation, and a
+    cell's path mutations (edge an ancestor-or-self of the cell, or
+    preneoplastic) match a walk up its parents."""
+    import numpy as np
+    from process_gb300 import PhylogeneticForest, synth
+    w = synth.plain_3mbp(seed=4, n_leaves=300)
+    f = w.forest
+    tin, tout = f.euler()
+    rng = np.random.default_rng(1)
+    n = f.num_of_nodes
+    edges = rng.integers(0, n + 1, 5000).astype(np.uint32)   # n: the preneoplastic edge
+    pf = PhylogeneticForest.__new__(PhylogeneticForest)
+    pf.forest = f
+    pf._table = {"edge": edges}
+    for leaf in rng.choice(np.nonzero(f.is_leaf)[0], 20, replace=False):
+        path, v = set(), int(leaf)
+        while v >= 0:
+            path.add(v)
+            v = int(f.parent[v])
+        want = np.isin(edges, np.fromiter(path, dtype=np.int64)) | (edges == n)
+        np.testing.assert_array_equal(pf.leaf_carriers(int(leaf)), want)
+        anc = np.array(sorted(path))
+        assert ((tin[anc] <= tin[leaf]) & (tin[leaf] < tout[anc])).all()
