@@ -99,7 +99,11 @@ pg_status pg_launch_count(uint64_t* n);
  * The per-tile counts live in one fixed 2.7 MB array of the library's own
  * device memory, present on every GPU that loads the library until the
  * process exits.  The first call on a device looks up that array's device
- * address; make it before capturing a stream into a CUDA graph.  All calls
+ * address and keeps it for the life of the process (a cudaDeviceReset
+ * invalidates it: do not call this after resetting the device); make the
+ * first call before capturing a stream into a CUDA graph.  A CUDA error left
+ * pending by earlier work on the calling thread makes the call fail with
+ * PG_ERR_CUDA before launching anything, and stays pending.  All calls
  * share the array: calls whose kernels overlap on the GPU (different
  * streams, or concurrent host threads) race and return wrong counts;
  * serialise them on one stream.  The counts equal pg_engine_genome_info's
@@ -256,6 +260,11 @@ pg_status pg_seq_result_dims(const pg_seq_result* res, uint32_t* n_samples, uint
 pg_status pg_seq_result_copy(const pg_seq_result* res, int32_t* alt, int32_t* depth);
 /* Device time of the read kernel of the call (ms). */
 pg_status pg_seq_result_kernel_ms(const pg_seq_result* res, float* ms);
+/* Tile size (bp of fragment starts per read-kernel work item) the call used:
+ * cfg->tile_size, or the automatic choice when that was 0.  The draws depend
+ * on it, so a replay of the call needs it.  No reference counterpart (the
+ * reference has no tiles). */
+pg_status pg_seq_result_tile_size(const pg_seq_result* res, uint32_t* tile_size);
 /* The observed rows: mutations with an alt read in some sample, the rows the
  * reference's result data frame keeps by default (include_non_sequenced_
  * mutations = FALSE; src/seq_simulation.cpp:52-90, 142-181).  Built on the

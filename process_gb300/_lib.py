@@ -108,6 +108,7 @@ _PROTOS = {
     "pg_seq_result_dims": (C.c_int, [P, u32p, u64p, u64p]),
     "pg_seq_result_copy": (C.c_int, [P, i32p, i32p]),
     "pg_seq_result_kernel_ms": (C.c_int, [P, f32p]),
+    "pg_seq_result_tile_size": (C.c_int, [P, u32p]),
     "pg_seq_result_active": (C.c_int, [P, u64p]),
     "pg_seq_result_copy_active": (C.c_int, [P, u32p, i32p, i32p]),
     "pg_simulate_seq_sam": (C.c_int, [P, C.POINTER(SeqCfg), C.c_uint64, C.POINTER(SamCfg), C.POINTER(P)]),

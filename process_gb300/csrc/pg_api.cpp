@@ -300,6 +300,7 @@ struct pg_seq_result {
   pg_engine* eng = nullptr;
   uint32_t n_samples = 0;
   uint64_t M = 0, n_reads = 0;
+  uint32_t tile_size = 0;      // the tile size the call used (automatic or given)
   DBuf<uint32_t> alt, depth;
   float kernel_ms = 0;
   // observed rows (built on the first request)
@@ -1741,6 +1742,7 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
     res->n_samples = uint32_t(samples.size());
     res->M = pl->M;
     res->n_reads = frags_per_sample * uint64_t(mates) * samples.size();
+    res->tile_size = T;
     res->alt = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
     res->depth = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
     ck(cudaMemsetAsync(res->alt.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
@@ -1920,6 +1922,10 @@ pg_status pg_seq_result_copy_active(const pg_seq_result* r, uint32_t* index, int
 
 pg_status pg_seq_result_kernel_ms(const pg_seq_result* r, float* ms) {
   return guarded([&] { require(r && ms, "NULL argument"); *ms = r->kernel_ms; });
+}
+
+pg_status pg_seq_result_tile_size(const pg_seq_result* r, uint32_t* tile_size) {
+  return guarded([&] { require(r && tile_size, "NULL argument"); *tile_size = r->tile_size; });
 }
 
 }  // extern "C"

@@ -317,7 +317,9 @@ __global__ void k_class_totals(const uint32_t* __restrict__ cnt, uint32_t ntiles
 }
 
 // device address of g_noalloc_tile_counts per device (host code cannot use
-// the symbol itself: on the host it names a stand-in, not device memory)
+// the symbol itself: on the host it names a stand-in, not device memory).
+// The address is looked up once per device and kept; a cudaDeviceReset
+// invalidates it, so the entry point is not for use after a device reset.
 static std::mutex g_noalloc_mu;
 static uint32_t* g_noalloc_addr[64] = {};
 
@@ -341,6 +343,9 @@ const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const
   }
   const uint32_t ntiles = index_num_tiles(G);
   const int nc = index_num_classes(which);
+  // an error left pending by earlier work on this thread is not this call's:
+  // report it as such and leave it pending for its owner, launching nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return "a CUDA error from earlier work is pending; nothing was launched";
   // every (class, tile) entry is written by the count pass: nothing to clear
   if (which == 0)
     k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, G, chr_off, n_chr, ntiles,

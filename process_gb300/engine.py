@@ -1437,6 +1437,13 @@ class SeqResult:
         check(lib().pg_seq_result_kernel_ms(self._h, C.byref(v)))
         return v.value
 
+    def tile_size(self) -> int:
+        """The tile size the call used (the automatic choice when none was
+        given); a replay of the call needs it."""
+        v = C.c_uint32()
+        check(lib().pg_seq_result_tile_size(self._h, C.byref(v)))
+        return v.value
+
 
 INSERT_MODELS = {"binomial": 0, "normal": 1}
 

@@ -298,3 +298,108 @@ def test_unknown_bases_genome(gpu_lib, orc, tmp_path):
             if not line.startswith("@"):
                 n_count += line.split("\t")[9].count("N")
     assert n_count > 0
+
+
+# ---------------------------------------------------------------- named workloads at their own sizes
+def _replay_counts(o_placed, eng, res, seq, seed):
+    """The oracle's replay of a sequencing call, at the tile size the call used."""
+    from process_gb300.engine import seq_cfg
+    c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=res.tile_size(), **seq)
+    return o_placed.sequence(c, seed, flavour=0)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_plain_3mbp_workload_bit_exact(gpu_lib, orc, seed):
+    """The 3 x 1 Mbp workload exactly as named: ~2.5k leaves (species A and
+    the A+ subclone), SNV 1e-6 / indel 1e-7 per base per division, one SBS
+    and one ID signature, 100 + 10 preneoplastic mutations; 80x paired
+    150 bp reads with insert Normal(350, 30) and error rate 1e-3, at the
+    automatic tile size.  Whole placed table and alt/depth tables bit for
+    bit against the Philox replay."""
+    from process_gb300 import synth
+    from process_gb300.engine import sequence_counts
+    w = synth.plain_3mbp(seed=1)
+    assert w.forest.is_leaf.sum() == 2500
+    assert w.seq["insert_model"] == "normal" and w.seq["insert_size_stddev"] == 30 and w.seq["coverage"] == 80
+    eng, o = make_pair(orc, w)
+    pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=seed)
+    op = o.place(w.forest, oracle_species(o, w.forest), w.n_pre_snv, 0, w.n_pre_indel, 0, seed=seed)
+    t = pf.table()
+    assert_tables_equal(t, op.table())
+    assert len(t["locus"]) > 20_000
+    res = sequence_counts(pf, 100 + seed, **w.seq)
+    alt, dep = res.counts()
+    oalt, odep, oreads = _replay_counts(op, eng, res, w.seq, 100 + seed)
+    np.testing.assert_array_equal(dep, odep)
+    np.testing.assert_array_equal(alt, oalt)
+    assert res.dims()[2] == oreads > 3_000_000
+
+
+def test_full_scale_slice_bit_exact(gpu_lib, orc):
+    """1% of the 3.1 Gbp workload (31 Mbp over the same 24 chromosomes, the
+    20 CNA segments and the WGD branch scaled with it) with the full
+    3 x 1e4-leaf forest, 3 epochs, 100x, purity 0.7, error rate 1e-3: the
+    slice the CPU baseline times.  Placement, CNA records, genotype classes
+    and the alt/depth tables of all four samples bit for bit against the
+    Philox replay."""
+    from process_gb300 import synth
+    from process_gb300.engine import sequence_counts
+    w = synth.full_scale(seed=2, genome_scale=0.01)
+    assert w.forest.is_leaf.sum() == 30_000
+    eng, o = make_pair(orc, w)
+    pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=7)
+    op = o.place(w.forest, oracle_species(o, w.forest), w.n_pre_snv, 0, w.n_pre_indel, 0, seed=7)
+    assert_tables_equal(pf.table(), op.table())
+    gc, oc = pf.cna_table(), op.cna_table()
+    for k in oc:
+        np.testing.assert_array_equal(gc[k], oc[k], err_msg=k)
+    assert (gc["type"] == 2).sum() == 1
+    g_cls, g_n, g_max = pf.node_classes()
+    o_cls, o_n, o_max = op.node_classes(w.forest.num_of_nodes)
+    np.testing.assert_array_equal(g_cls, o_cls)
+    assert (g_n, g_max) == (o_n, o_max) and g_n >= 3
+    res = sequence_counts(pf, 9, **w.seq)
+    alt, dep = res.counts()
+    oalt, odep, oreads = _replay_counts(op, eng, res, w.seq, 9)
+    assert alt.shape[0] == 4
+    np.testing.assert_array_equal(dep, odep)
+    np.testing.assert_array_equal(alt, oalt)
+    assert res.dims()[2] == oreads
+
+
+def test_distribution_plain_3mbp_workload(gpu_lib, orc):
+    """64 seeds on the 3 x 1 Mbp, ~2.5k-leaf workload (80x, insert
+    Normal(350, 30), error 1e-3): chi-square on SBS context counts, KS on
+    per-edge passenger SNV counts and on VAF, GPU vs the std::mt19937_64
+    flavour; p > 0.01."""
+    from process_gb300 import synth
+    from process_gb300.engine import sequence_counts
+    w = synth.plain_3mbp(seed=11)
+    eng, o = make_pair(orc, w)
+    sp = oracle_species(o, w.forest)
+    n = w.forest.num_of_nodes
+    seq = dict(w.seq, with_normal_sample=False)
+    g_ctx, m_ctx = np.zeros(96), np.zeros(96)
+    g_edge, m_edge, g_vaf, m_vaf = [], [], [], []
+    for s in range(64):
+        pf = eng.place_mutations(w.forest, w.n_pre_snv, w.n_pre_indel, seed=3000 + s)
+        t = pf.table()
+        op = o.place(w.forest, sp, w.n_pre_snv, 0, w.n_pre_indel, 0, seed=3000 + s, flavour=1)
+        ot = op.table()
+        for tab, ctx, edges in ((t, g_ctx, g_edge), (ot, m_ctx, m_edge)):
+            snv = (tab["kind"] == 0) & (tab["nature"] == 0)
+            ctx += np.bincount(tab["cls"][snv], minlength=96)
+            edges.append(np.bincount(tab["edge"][snv], minlength=n)[:n])
+        if s < 16:
+            res = sequence_counts(pf, 700 + s, **seq)
+            alt, dep = res.counts()
+            from process_gb300.engine import seq_cfg
+            c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=res.tile_size(), **seq)
+            oalt, odep, _ = op.sequence(c, 700 + s, flavour=1)
+            for a, d, out, tab in ((alt, dep, g_vaf, t), (oalt, odep, m_vaf, ot)):
+                keep = (d[0] >= 20) & (tab["kind"] == 0) & ((tab["nature"] == 2) | (a[0] >= 3))
+                out.append(a[0][keep] / d[0][keep])
+    keep = (g_ctx + m_ctx) > 0
+    assert stats.chi2_contingency(np.vstack([g_ctx[keep], m_ctx[keep]]))[1] > 0.01
+    assert stats.ks_2samp(np.concatenate(g_edge), np.concatenate(m_edge)).pvalue > 0.01
+    assert stats.ks_2samp(np.concatenate(g_vaf), np.concatenate(m_vaf)).pvalue > 0.01
