@@ -65,7 +65,7 @@ W4 philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint3
 
 enum : uint32_t {
   TAG_EDGE_SNV = 1, TAG_EDGE_INDEL = 2, TAG_EDGE_CNA = 3, TAG_SNV = 4, TAG_INDEL = 5, TAG_DRIVER = 6,
-  TAG_TILE_SPLIT = 7, TAG_PAIR = 8, TAG_PAIR2 = 9, TAG_ERR = 10, TAG_GENOME = 11, TAG_CNA = 12
+  TAG_TILE_SPLIT = 7, TAG_PAIR = 8, TAG_GENOME = 11, TAG_CNA = 12
 };
 
 static inline uint64_t index64(uint32_t hi, uint32_t lo, uint64_t n) {
@@ -1087,7 +1087,8 @@ SeqSetup seq_setup(const Placed& pl, const SeqCfg& c) {
 
 // error word of the visit of mate `mate` of a fragment to `locus`: the
 // MurmurHash3 fmix32 finaliser (A. Appleby, public domain) of the fragment's
-// Philox word (word 1 of its TAG_PAIR2 block) mixed with locus and mate
+// error word (the XOR of the four words of its Philox block) mixed with
+// locus and mate
 uint32_t error_word(uint32_t w, uint32_t locus, uint32_t mate) {
   uint32_t h = w ^ (locus * 0x9E3779B1u) ^ (mate ? 0x85EBCA77u : 0u);
   h ^= h >> 16;
@@ -1310,37 +1311,48 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
         const uint32_t start = e.g.off[ci] + k * T, len = std::min<uint32_t>(T, S - k * T);
         for (uint32_t j = 0; j < tile_pairs[k]; ++j) {
           out.n_reads += s.paired ? 2 : 1;
-          // start, cell and allele instance
+          // start, cell and allele instance: one Philox block per fragment
+          // (x start / part, y cell / option, z insert, w instance then
+          // leaf from the fraction the instance draw leaves)
           const W4 r = philox(k0, k1, j, t, smp, TAG_PAIR);
-          const W4 r2 = philox(k0, k1, j, t, smp, TAG_PAIR2);
           uint32_t p0, allele;
           int64_t cell;
           if (!pl.has_cna) {
             p0 = start + mulhi32(r.v[0], len);
             const bool normal = sd.all_normal || r.v[1] < sd.normal_thr;
-            cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[2], uint32_t(sd.leaves.size()))]);
             allele = mulhi32(r.v[3], 2);
+            cell = normal ? -1 : int64_t(sd.leaves[mulhi32(r.v[3] * 2u, uint32_t(sd.leaves.size()))]);
           } else {
-            // part (word z of TAG_PAIR2 when the tile meets several atoms),
-            // start in the part, option, leaf of the option, instance
+            // part (when the tile meets several atoms) and start in the part
+            // from word x: the start from the word's place in the part's
+            // threshold interval; option from y; instance, then leaf, from w
             const SampleCn& q = scn[smp];
             const auto& pk = parts[k];
-            const size_t pi = pk.size() > 1 ? lookup(part_thr[k].data(), uint32_t(pk.size()), r2.v[2]) : 0;
+            size_t pi = 0;
+            if (pk.size() > 1) {
+              pi = lookup(part_thr[k].data(), uint32_t(pk.size()), r.v[0]);
+              const uint64_t lo = pi ? part_thr[k][pi - 1] : 0u, hi = part_thr[k][pi];
+              p0 = pk[pi].start + uint32_t((uint64_t((r.v[0] >> 1) - lo) * pk[pi].len) / (hi - lo));
+            } else {
+              p0 = pk[0].start + mulhi32(r.v[0], pk[0].len);
+            }
             const Part& pt = pk[pi];
-            p0 = pt.start + mulhi32(r.v[0], pt.len);
             const uint32_t o = lookup(q.opt_thr[pt.atom].data(), uint32_t(q.opts.size()), r.v[1]);
             const Opt& op = q.opts[o];
-            cell = op.leaves.empty() ? -1 : int64_t(op.leaves[mulhi32(r.v[2], uint32_t(op.leaves.size()))]);
             const auto& cov = pl.atom_cov[pt.atom][op.cls];
             if (cov.empty()) continue;     // an option without DNA here is never drawn
-            allele = cov[mulhi32(r.v[3], uint32_t(cov.size()))];
+            const uint32_t n_cov = uint32_t(cov.size());
+            allele = cov[mulhi32(r.v[3], n_cov)];
+            cell = op.leaves.empty() ? -1
+                                     : int64_t(op.leaves[mulhi32(r.v[3] * n_cov, uint32_t(op.leaves.size()))]);
           }
-          count_mate(pl, car, carriers, p0, s.R, cell, allele, s.err_thr, 0, r2.v[1], alt, dep);
+          const uint32_t fw = r.v[0] ^ r.v[1] ^ r.v[2] ^ r.v[3];
+          count_mate(pl, car, carriers, p0, s.R, cell, allele, s.err_thr, 0, fw, alt, dep);
           if (s.paired) {
-            const uint32_t ins = s.ins_min + lookup(s.ins_thr.data(), uint32_t(s.ins_thr.size()), r2.v[0]);
+            const uint32_t ins = s.ins_min + lookup(s.ins_thr.data(), uint32_t(s.ins_thr.size()), r.v[2]);
             uint32_t p1 = p0 + ins - s.R;
             if (p1 > ce - s.R) p1 = ce - s.R;
-            count_mate(pl, car, carriers, p1, s.R, cell, allele, s.err_thr, 1, r2.v[1], alt, dep);
+            count_mate(pl, car, carriers, p1, s.R, cell, allele, s.err_thr, 1, fw, alt, dep);
           }
         }
       }

@@ -40,7 +40,7 @@ __device__ __forceinline__ U4 philox(uint32_t k0, uint32_t k1,
 enum : uint32_t {
   TAG_EDGE_SNV = 1, TAG_EDGE_INDEL = 2, TAG_EDGE_CNA = 3,
   TAG_SNV = 4, TAG_INDEL = 5, TAG_DRIVER = 6,
-  TAG_TILE_SPLIT = 7, TAG_PAIR = 8, TAG_PAIR2 = 9, TAG_ERR = 10,
+  TAG_TILE_SPLIT = 7, TAG_PAIR = 8,
   TAG_GENOME = 11, TAG_CNA = 12
 };
 

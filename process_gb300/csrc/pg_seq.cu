@@ -23,13 +23,13 @@
 //     allele) and the base is not hit by a substitution error, or when it
 //     does not carry it and an error turns the reference into that alt base.
 //     The error word of a (fragment, mate, locus) visit is the MurmurHash3
-//     fmix32 finaliser of the fragment's Philox word mixed with the locus and
-//     the mate; an error happens when it is below err_thr, and the erroneous
+//     fmix32 finaliser of the fragment's error word (the XOR of its Philox
+//     block) mixed with the locus and the mate; an error happens when it is below err_thr, and the erroneous
 //     base is one of the three others, word % 3 == 0 being the alt base.
 //     Indels are not affected by substitution errors.
 //
 // Kernel layout (one CTA per (tile, sample); fragments in batches):
-//   phase A  every thread generates fragments (two Philox blocks each) and
+//   phase A  every thread generates fragments (one Philox block each) and
 //            writes its two mates to shared memory; mates are bucketed by
 //            start position (16 bp buckets, counting sort);
 //   phase B  work items (mutation record, start bucket) scan the mates of one
@@ -207,7 +207,7 @@ __global__ void k_tile_split_level(uint32_t level, uint32_t n_slots, const uint3
   }
 }
 
-// error word of the visit of mate `mate` of a fragment (Philox word w) to `locus`
+// error word of the visit of mate `mate` of a fragment (error word w) to `locus`
 __device__ __forceinline__ uint32_t err_word(uint32_t w, uint32_t locus, uint32_t mate) {
   uint32_t h = w ^ (locus * 0x9E3779B1u) ^ (mate ? 0x85EBCA77u : 0u);
   h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
@@ -238,15 +238,23 @@ __device__ __forceinline__ bool observed(const SeqParams& prm, uint32_t tin, uin
   return carried ? !err : (err && (e % 3u) == 0u);
 }
 
-// one fragment's draws: mate starts, source cell, allele instance and its
-// error word.  Without copy-number events: start uniform in the tile, cell
-// normal with probability normal_thr / 2^32 else a uniform leaf, allele 0 or
-// 1.  With them, (start, cell, instance) is uniform over the DNA of the
-// sample's cells: the part of the tile (word z of the TAG_PAIR2 block, when
-// the tile meets more than one atom) with probability proportional to its
-// mass, the start uniform in the part, the cell option (normal cells or a
-// leaf class) proportional to its copies in the part's atom, a uniform leaf
-// of the class and a uniform covering instance.
+// One fragment's draws: mate starts, source cell, allele instance and its
+// error word, all from ONE Philox4x32-10 block r (counter (j, t, s, TAG_PAIR)):
+//   r.x  the start: uniform in the tile; with copy-number events, when the
+//        tile meets several atoms, the part by its mass (31-bit thresholds)
+//        and the start uniform in the part from the word's residual within
+//        the part's threshold interval (exact integer arithmetic)
+//   r.y  the cell: normal when below normal_thr, else a sampled leaf; with
+//        copy-number events the cell option (normal cells or a leaf class)
+//        by its copies in the part's atom
+//   r.z  the insert size (31-bit thresholds of its CDF)
+//   r.w  the allele instance, uniform among the n covering ones
+//        (floor(r.w n / 2^32)), then the leaf, uniform in its class, from the
+//        fraction that draw leaves (the low word of r.w n): the two indices
+//        use disjoint information of the word
+//   r.x ^ r.y ^ r.z ^ r.w  the fragment's error word
+// Without copy-number events the instance is allele 0 or 1 and the leaf is
+// uniform over the sample's leaves.
 struct Fragment {
   uint32_t p0, p1, cell, inst, w;
 };
@@ -282,6 +290,12 @@ __device__ __forceinline__ void fill_cn_cache(CnCache& c, const SeqParams& prm, 
   }
 }
 
+// start offset in a part of length plen from the word u that selected the
+// part, whose 31-bit value lies in the part's threshold interval [lo, hi)
+__device__ __forceinline__ uint32_t part_offset(uint32_t u, uint32_t lo, uint32_t hi, uint32_t plen) {
+  return uint32_t((uint64_t((u >> 1) - lo) * plen) / uint64_t(hi - lo));
+}
+
 template <bool INS_SMEM>
 __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
                                                   uint32_t len, uint32_t ce, const SeqSample& sm,
@@ -289,44 +303,56 @@ __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t 
                                                   const uint32_t* ins, const uint16_t* guide,
                                                   const CnCache* cc = nullptr) {
   const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
-  const U4 r2 = philox(key.k0, key.k1, j, t, s, TAG_PAIR2);
   Fragment f;
   const uint32_t R = prm.read_len;
   if (!prm.has_cna) {
     f.p0 = start + __umulhi(r.x, len);
     const bool normal = sm.all_normal || r.y < sm.normal_thr;
-    f.cell = normal ? prm.normal_tin : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.z, sm.n_leaves));
     f.inst = __umulhi(r.w, prm.n_alleles);
+    f.cell = normal ? prm.normal_tin
+                    : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.w * prm.n_alleles, sm.n_leaves));
   } else if (cc) {
-    const uint32_t part = cc->n_parts > 1 ? cdf_lookup(cc->pthr, cc->n_parts, r2.z) : 0u;
-    f.p0 = cc->pstart[part] + __umulhi(r.x, cc->plen[part]);
+    uint32_t part = 0;
+    if (cc->n_parts > 1) {
+      part = cdf_lookup(cc->pthr, cc->n_parts, r.x);
+      f.p0 = cc->pstart[part] + part_offset(r.x, part ? cc->pthr[part - 1] : 0u, cc->pthr[part], cc->plen[part]);
+    } else {
+      f.p0 = cc->pstart[0] + __umulhi(r.x, cc->plen[0]);
+    }
     const uint32_t o = cdf_lookup(cc->othr[part], cc->n_opt, r.y);
-    const uint32_t nl = cc->onl[o];
-    f.cell = nl ? __ldg(prm.cls_leaf_tin + cc->oloff[o] + __umulhi(r.z, nl)) : prm.normal_tin;
-    const uint32_t icnt = cc->oicnt[part][o];
+    const uint32_t nl = cc->onl[o], icnt = cc->oicnt[part][o];
     f.inst = icnt ? uint32_t(__ldg(prm.gc.inst_list + cc->oioff[part][o] + __umulhi(r.w, icnt))) : 0xffffu;
+    f.cell = nl ? __ldg(prm.cls_leaf_tin + cc->oloff[o] + __umulhi(r.w * icnt, nl)) : prm.normal_tin;
   } else {
     const uint32_t pb = __ldg(prm.part_off + t), pn = __ldg(prm.part_off + t + 1) - pb;
-    const uint32_t part = pb + (pn > 1 ? cdf_lookup(prm.part_cdf + uint64_t(s) * prm.n_parts + pb, pn, r2.z) : 0u);
+    uint32_t part = pb;
+    if (pn > 1) {
+      const uint32_t* thr = prm.part_cdf + uint64_t(s) * prm.n_parts + pb;
+      const uint32_t k = cdf_lookup(thr, pn, r.x);
+      part = pb + k;
+      f.p0 = __ldg(prm.part_start + part) +
+             part_offset(r.x, k ? __ldg(thr + k - 1) : 0u, __ldg(thr + k), __ldg(prm.part_len + part));
+    } else {
+      f.p0 = __ldg(prm.part_start + part) + __umulhi(r.x, __ldg(prm.part_len + part));
+    }
     const uint32_t atom = __ldg(prm.part_atom + part);
-    f.p0 = __ldg(prm.part_start + part) + __umulhi(r.x, __ldg(prm.part_len + part));
     const uint32_t o = sm.opt_off + cdf_lookup(prm.opt_cdf + sm.opt_cdf_off + atom * sm.n_opt, sm.n_opt, r.y);
     const uint32_t nl = __ldg(prm.opt_nleaf + o);
-    f.cell = nl ? __ldg(prm.cls_leaf_tin + __ldg(prm.opt_leaf_off + o) + __umulhi(r.z, nl)) : prm.normal_tin;
     const uint32_t ai = atom * prm.n_classes + __ldg(prm.opt_class + o);
     const uint32_t icnt = __ldg(prm.atom_icnt + ai);
     f.inst = icnt ? uint32_t(__ldg(prm.gc.inst_list + __ldg(prm.atom_ioff + ai) + __umulhi(r.w, icnt))) : 0xffffu;
+    f.cell = nl ? __ldg(prm.cls_leaf_tin + __ldg(prm.opt_leaf_off + o) + __umulhi(r.w * icnt, nl)) : prm.normal_tin;
   }
-  f.w = r2.y;
+  f.w = r.x ^ r.y ^ r.z ^ r.w;
   f.p1 = f.p0;
   if (prm.paired) {
     uint32_t k;
     if (INS_SMEM) {
-      const uint32_t v = r2.x >> 1;
+      const uint32_t v = r.z >> 1;
       k = guide[v >> 23];
       while (k + 1 < prm.n_ins && ins[k] <= v) ++k;
     } else {
-      k = cdf_lookup(prm.ins_cdf, prm.n_ins, r2.x);
+      k = cdf_lookup(prm.ins_cdf, prm.n_ins, r.z);
     }
     uint32_t p1 = f.p0 + prm.ins_min + k - R;
     if (p1 > ce - R) p1 = ce - R;
