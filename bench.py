@@ -448,6 +448,20 @@ def gpu_arm(args):
     e2e_value, d2h_step = e2e_run(False, seed0 + 30_000)
     e2e_full_value, d2h_full_step = e2e_run(True, seed0 + 50_000)
 
+    # the result data frame of the last step (simulate_seq's "mutations"):
+    # built in C++ by the library, then turned into numpy columns
+    from process_gb300.engine import _result_frame
+    names = list(w.forest.sample_names) + ["normal_sample"]
+    t0 = time.perf_counter()
+    nrow = C.c_uint64()
+    _lib.check(_lib.lib().pg_seq_result_frame(res._h, pf._h, 0, C.byref(nrow)))
+    t_frame_lib = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    frame = _result_frame(res, pf, False, names)
+    t_frame_all = time.perf_counter() - t0
+    frame_info = {"rows": int(nrow.value), "library_build_s": t_frame_lib, "build_and_columns_s": t_frame_all,
+                  "columns": len(frame)}
+
     cal = None if args.no_calibration else calibration_bench(world, args.calib_replicates)
     batch = None if args.no_batch else batch_bench(stream, args.batch_instances, max(1, min(args.steps, 3)),
                                                    max(1, min(args.warmup, 2)))
@@ -477,6 +491,7 @@ def gpu_arm(args):
                           "sequencing_reads_per_s": value * t[0] / t[2],
                           "place_ms_per_step": float(t[1]) / args.steps, "seq_ms_per_step": float(t[2]) / args.steps,
                           "bracket_wall_s": wall,
+                          "result_frame": frame_info,
                           "e2e_full_tables": {"value": e2e_full_value, "unit": "reads/s",
                                               "d2h_bytes_per_step": d2h_full_step}},
             "roofline": {"kernel": "k_reads", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -129,6 +129,17 @@ pg_status pg_engine_read_index(const pg_engine* eng, int which, uint32_t cls, ui
 pg_status pg_engine_set_signatures(pg_engine* eng, int type, uint32_t n_sigs, const double* probs);
 /* MutationEngine::add_exposure(time, exposure) (src/mutation_engine.cpp:734-739):
  * coefficients over the n_sigs signatures of `type`, active from `time`. */
+/* Signature<SBSType|IDType>::read_from_stream (src/mutation_engine.cpp:389-397):
+ * a tab-separated table whose header is "Type" and the signature names, one
+ * row per class labelled as COSMIC does ("A[C>A]A" for the 96 SBS classes,
+ * "1:Del:C:0" .. "5:Del:M:5" for the 83 ID classes), rows in any order,
+ * every class once.  load: sets the engine's signatures of the type (as
+ * pg_engine_set_signatures) and their names.  read: the table alone, without
+ * an engine or a device: *n_sigs, the names NUL-separated (*names_size
+ * bytes) and probs [n_sigs][96 or 83]; outputs may be NULL. */
+pg_status pg_engine_load_signatures_tsv(pg_engine* eng, int type, const char* path);
+pg_status pg_signature_table_read(int type, const char* path, uint32_t* n_sigs, uint64_t* names_size, char* names,
+                                  double* probs);
 pg_status pg_engine_add_exposure(pg_engine* eng, int type, double time, const double* coeffs);
 /* Passenger rates per base per division of a species (mutant + epistate),
  * MutationEngine::add_mutant / get_passenger_rates (src/mutation_engine.cpp:864-1083). */
@@ -230,6 +241,89 @@ pg_status pg_placed_class_copy(const pg_placed* placed, uint32_t* seg_off, uint3
 /* Device time of the placement kernels of the last place call (ms). */
 pg_status pg_placed_kernel_ms(const pg_placed* placed, float* ms);
 
+/* ------------------------------------------------------------------ data frames
+ * The data frames of the reference's PhylogeneticForest getters, built in
+ * the library so that the Rcpp layer only turns columns into a data frame.
+ * Cells are node ids of leaves (the shim maps them to cell ids); mutations
+ * are row indices in the order of pg_placed_copy.  Each builder keeps its
+ * result in the handle until the next call of the same builder, and its
+ * _copy call fills caller buffers of the returned row count (any pointer may
+ * be NULL).  Builders of one handle must not run concurrently.
+ *
+ * ref / alt strings: PG_SID_CHARS bytes per row, NUL-padded.  SNV: reference
+ * base, alt base; insertion: anchor base, anchor + inserted bases; deletion:
+ * anchor + deleted bases, anchor base.  Unknown reference bases read "N". */
+#define PG_SID_CHARS 16
+
+/* Names of the signatures of a type (0 SBS, 1 ID) as set by
+ * pg_engine_set_signatures (one per signature, in that order), used for the
+ * causes of the data frames; Signature::read_from_stream keeps them with the
+ * probabilities (src/mutation_engine.cpp:389-397). */
+pg_status pg_engine_set_signature_names(pg_engine* eng, int type, uint32_t n, const char* const* names);
+/* Name of signature `index` of a type ("SBS#<index + 1>" / "ID#<index + 1>"
+ * when none was set): *length characters, NUL-terminated into out when out
+ * is not NULL (capacity bytes, truncated). */
+pg_status pg_engine_signature_name(const pg_engine* eng, int type, uint32_t index, char* out, uint32_t capacity,
+                                   uint32_t* length);
+/* Columns of n placed mutations (rows[i], or rows 0..n-1 when rows is NULL):
+ * chromosome index, 1-based position, ref, alt, kind (0 SNV, 1 indel), cause
+ * (signature index of the kind, -1 none: drivers) and nature (0 passenger,
+ * 1 driver, 2 preneoplastic).  The per-row columns of
+ * get_sampled_cell_mutations (src/phylogenetic_forest.cpp:452-507). */
+pg_status pg_placed_mutation_info(const pg_placed* placed, uint64_t n, const uint32_t* rows, uint32_t* chr,
+                                  uint32_t* chr_pos, char* ref, char* alt, uint8_t* kind, int32_t* cause,
+                                  uint8_t* nature);
+/* get_sampled_cell_mutations (src/phylogenetic_forest.cpp:452-507): for each
+ * cell (cells[i], or every sampled leaf by node id when cells is NULL), every
+ * mutation it holds, once per allele instance of its genome that carries it
+ * (the placed instance and its copies made after the mutation, while present
+ * at the locus).  A cell's rows are ordered by chromosome, allele instance,
+ * position, as fill_mutation_lists nests them (:323-351). */
+pg_status pg_placed_cell_mutations(pg_placed* placed, uint32_t n_cells, const uint32_t* cells, uint64_t* n_rows);
+pg_status pg_placed_cell_mutations_copy(const pg_placed* placed, uint32_t* cell, uint32_t* mutation,
+                                        uint32_t* allele);
+/* get_sampled_cell_CNAs (src/phylogenetic_forest.cpp:509-562): for each cell,
+ * the CNA / WGD events on its root path, as indices of pg_placed_cna_copy,
+ * in event order. */
+pg_status pg_placed_cell_cnas(pg_placed* placed, uint32_t n_cells, const uint32_t* cells, uint64_t* n_rows);
+pg_status pg_placed_cell_cnas_copy(const pg_placed* placed, uint32_t* cell, uint32_t* cna_index);
+/* get_cell_allelic_fragmentation (src/phylogenetic_forest.cpp:867-927): for
+ * each cell, its genome cut into maximal stretches of one allelic type
+ * (copies of germline alleles 0 and 1; major the larger), per chromosome;
+ * chromosome index, 1-based inclusive begin / end.  Deleted stretches have
+ * type (0, 0). */
+pg_status pg_placed_cell_fragmentation(pg_placed* placed, uint32_t n_cells, const uint32_t* cells,
+                                       uint64_t* n_rows);
+pg_status pg_placed_cell_fragmentation_copy(const pg_placed* placed, uint32_t* cell, uint32_t* chr, uint32_t* begin,
+                                            uint32_t* end, uint32_t* major, uint32_t* minor);
+/* get_bulk_allelic_fragmentation([sample_name]) (src/phylogenetic_forest.cpp:
+ * 767-820): the genome cut where the allelic type of some sampled cell (of
+ * the sample, or of every sample when sample < 0) changes; per stretch one
+ * row per allelic type with the fraction of cells that show it (ratio),
+ * types ascending, the cells without DNA there last as type (0, 0). */
+pg_status pg_placed_bulk_fragmentation(pg_placed* placed, int32_t sample, uint64_t* n_rows);
+pg_status pg_placed_bulk_fragmentation_copy(const pg_placed* placed, uint32_t* chr, uint32_t* begin, uint32_t* end,
+                                            uint32_t* major, uint32_t* minor, double* ratio);
+/* PhylogeneticForest$save / load_phylogenetic_forest (src/phylogenetic_forest.cpp:
+ * 940-992, src/mutations.cpp:1466-1480).  The reference archives its RACES
+ * forest; this library writes a versioned native archive of the placed
+ * forest (Euler numbering and samples, placed mutations, genotype classes,
+ * allele-instance lineage, CNA events) and a fingerprint of the engine's
+ * genome.  Loading restores the handle without placing again; the engine
+ * must hold the same genome (PG_ERR_DOMAIN otherwise, and for a file that is
+ * missing, not a regular file, of another format version or truncated).
+ * serialize: *size bytes, written to buf when buf is not NULL (capacity >=
+ * *size); save / load: the same bytes in a file. */
+pg_status pg_placed_serialize(const pg_placed* placed, uint8_t* buf, uint64_t capacity, uint64_t* size);
+pg_status pg_placed_deserialize(pg_engine* eng, const uint8_t* buf, uint64_t size, pg_placed** out);
+pg_status pg_placed_save(const pg_placed* placed, const char* path);
+pg_status pg_placed_load(pg_engine* eng, const char* path, pg_placed** out);
+/* get_samples_info (src/phylogenetic_forest.cpp:57-99): per sample its
+ * sampled cells, its DNA quantity (the summed allelic size of their genomes)
+ * and that in normal diploid genomes; arrays of n_samples entries. */
+pg_status pg_placed_samples_info(const pg_placed* placed, uint32_t* n_cells, double* dna_quantity,
+                                 double* equivalent_normal_cells);
+
 /* ------------------------------------------------------------------ sequencing
  * simulate_seq / simulate_normal_seq (src/seq_simulation.cpp:517-679; R
  * defaults src/sequencing.cpp:193-209,268-282) down to the read simulator. */
@@ -274,6 +368,24 @@ pg_status pg_seq_result_active(pg_seq_result* res, uint64_t* n_active);
  * pg_placed_copy) and alt / depth as [n_samples][n_active] int32; any
  * pointer may be NULL.  Requires pg_seq_result_active first. */
 pg_status pg_seq_result_copy_active(const pg_seq_result* res, uint32_t* index, int32_t* alt, int32_t* depth);
+/* The result data frame of simulate_seq (get_result_dataframe,
+ * src/seq_simulation.cpp:52-181), built from a result and the placed
+ * mutations it was simulated from: one row per SID (chromosome, position,
+ * ref, alt) in that order, over the observed mutations (alt read in some
+ * sample) or, with include_non_sequenced, also every mutation present in the
+ * cells of a sequenced sample.  Rows of one SID merge: occurrences add, the
+ * coverage is the locus's, causes are the sorted union of signature names
+ * joined by ';' (empty: NA), classes a bit set of natures (bit 0 passenger,
+ * 1 driver, 2 preneoplastic; the reference joins their sorted names).  Per
+ * sample occurrences, coverage and VAF = occurrences / coverage (0 without
+ * coverage) as [n_samples][n_rows].  causes_off holds n_rows + 1 offsets
+ * into the causes characters (pg_seq_result_frame_causes_size of them). */
+pg_status pg_seq_result_frame(pg_seq_result* res, const pg_placed* placed, int include_non_sequenced,
+                              uint64_t* n_rows);
+pg_status pg_seq_result_frame_causes_size(const pg_seq_result* res, uint64_t* n_chars);
+pg_status pg_seq_result_frame_copy(const pg_seq_result* res, uint32_t* chr, uint32_t* chr_pos, char* ref, char* alt,
+                                   uint64_t* causes_off, char* causes, uint8_t* classes, int32_t* occurrences,
+                                   int32_t* coverage, double* vaf);
 
 /* simulate_seq with write_SAM = TRUE (src/seq_simulation.cpp:540-564; files
  * and naming of vignettes/sequencing.Rmd:137-180, 282-317): the counts of

@@ -123,7 +123,33 @@ _PROTOS = {
     "pg_batch_copy": (C.c_int, [P, C.c_uint32, u32p, u32p, u32p, u8p, u8p, C.POINTER(C.c_uint16), u8p, u8p, i32p,
                                 i32p]),
     "pg_batch_kernel_ms": (C.c_int, [P, f32p, f32p]),
+    # data frames
+    "pg_engine_set_signature_names": (C.c_int, [P, C.c_int, C.c_uint32, C.POINTER(C.c_char_p)]),
+    "pg_engine_signature_name": (C.c_int, [P, C.c_int, C.c_uint32, C.c_char_p, C.c_uint32, u32p]),
+    "pg_placed_mutation_info": (C.c_int, [P, C.c_uint64, u32p, u32p, u32p, C.c_char_p, C.c_char_p, u8p, i32p,
+                                          u8p]),
+    "pg_placed_cell_mutations": (C.c_int, [P, C.c_uint32, u32p, u64p]),
+    "pg_placed_cell_mutations_copy": (C.c_int, [P, u32p, u32p, u32p]),
+    "pg_placed_cell_cnas": (C.c_int, [P, C.c_uint32, u32p, u64p]),
+    "pg_placed_cell_cnas_copy": (C.c_int, [P, u32p, u32p]),
+    "pg_placed_cell_fragmentation": (C.c_int, [P, C.c_uint32, u32p, u64p]),
+    "pg_placed_cell_fragmentation_copy": (C.c_int, [P, u32p, u32p, u32p, u32p, u32p, u32p]),
+    "pg_placed_bulk_fragmentation": (C.c_int, [P, C.c_int32, u64p]),
+    "pg_placed_bulk_fragmentation_copy": (C.c_int, [P, u32p, u32p, u32p, u32p, u32p, f64p]),
+    "pg_placed_samples_info": (C.c_int, [P, u32p, f64p, f64p]),
+    "pg_engine_load_signatures_tsv": (C.c_int, [P, C.c_int, C.c_char_p]),
+    "pg_signature_table_read": (C.c_int, [C.c_int, C.c_char_p, u32p, u64p, C.c_char_p, f64p]),
+    "pg_placed_serialize": (C.c_int, [P, u8p, C.c_uint64, u64p]),
+    "pg_placed_deserialize": (C.c_int, [P, u8p, C.c_uint64, C.POINTER(P)]),
+    "pg_placed_save": (C.c_int, [P, C.c_char_p]),
+    "pg_placed_load": (C.c_int, [P, C.c_char_p, C.POINTER(P)]),
+    "pg_seq_result_frame": (C.c_int, [P, P, C.c_int, u64p]),
+    "pg_seq_result_frame_causes_size": (C.c_int, [P, u64p]),
+    "pg_seq_result_frame_copy": (C.c_int, [P, u32p, u32p, C.c_char_p, C.c_char_p, u64p, C.c_char_p, u8p, i32p,
+                                           i32p, f64p]),
 }
+
+SID_CHARS = 16   # PG_SID_CHARS
 
 # symbols added by later additions to the ABI are bound when present
 OPTIONAL = set()

@@ -13,10 +13,12 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <filesystem>
 #include <fstream>
 #include <map>
 #include <memory>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -222,6 +224,7 @@ struct pg_engine {
   // signatures and exposures
   uint32_t n_sig[2] = {0, 0};
   std::vector<double> sigs[2];
+  std::vector<std::string> sig_names[2];   // optional (the causes of the data frames)
   std::map<double, std::vector<double>> expo[2];
   std::map<uint32_t, Species> species;
   std::map<uint32_t, std::vector<DriverEvent>> drivers;   // per mutant, application order
@@ -261,6 +264,7 @@ struct pg_placed {
   pg_engine* eng = nullptr;
   uint32_t n_nodes = 0, n_samples = 0;
   std::vector<uint32_t> tin, tout;
+  std::vector<int32_t> parent;
   std::vector<std::vector<uint32_t>> leaves;
   uint64_t M = 0;
   DBuf<uint32_t> locus, edge, aux, attempt;
@@ -288,6 +292,13 @@ struct pg_placed {
   DBuf<uint16_t> inst_list, chain_anc;
   DBuf<uint64_t> chain_key;
   std::vector<CnaOut> cnas;
+  // results of the data-frame getters, built on request (pg_placed_cell_*,
+  // pg_placed_bulk_fragmentation) and held until the next request
+  std::vector<uint32_t> cm_cell, cm_row, cm_allele;
+  std::vector<uint32_t> cc_cell, cc_index;
+  std::vector<uint32_t> cf_cell, cf_chr, cf_begin, cf_end, cf_major, cf_minor;
+  std::vector<uint32_t> bf_chr, bf_begin, bf_end, bf_major, bf_minor;
+  std::vector<double> bf_ratio;
   pg::PlaceOut view() const {
     return {locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, seq.p, kind.p, nature.p, attempt.p};
   }
@@ -307,6 +318,20 @@ struct pg_seq_result {
   bool active_done = false;
   uint32_t n_active = 0;
   DBuf<uint32_t> a_index, a_alt, a_depth;
+  // what the result data frame needs: the forest sample of each sequenced
+  // sample (-1 the normal one) and whether normal cells carry the
+  // preneoplastic mutations
+  std::vector<int32_t> sample_src;
+  bool pre_in_normal = false;
+  // the result data frame (pg_seq_result_frame)
+  uint64_t f_rows = 0;
+  std::vector<uint32_t> f_chr, f_pos;
+  std::vector<char> f_ref, f_alt;            // PG_SID_CHARS per row
+  std::vector<uint64_t> f_cause_off;
+  std::vector<char> f_causes;
+  std::vector<uint8_t> f_classes;
+  std::vector<int32_t> f_occ, f_cov;         // [sample][row]
+  std::vector<double> f_vaf;
 };
 
 namespace {
@@ -604,6 +629,7 @@ pg_status pg_engine_set_signatures(pg_engine* e, int type, uint32_t n_sigs, cons
     e->n_sig[type] = n_sigs;
     e->sigs[type].assign(probs, probs + uint64_t(n_sigs) * NC);
     e->expo[type].clear();
+    e->sig_names[type].clear();
   });
 }
 
@@ -1101,7 +1127,7 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     require(n_all < (1ull << 31), "too many mutations for one placement call");
     // ---- outputs
     pl->eng = e; pl->n_nodes = f->n; pl->n_samples = f->n_samples;
-    pl->tin = f->tin; pl->tout = f->tout; pl->leaves = f->leaves;
+    pl->tin = f->tin; pl->tout = f->tout; pl->leaves = f->leaves; pl->parent = f->parent;
     pl->leaf_cls.assign(f->n_samples, {});
     {
       std::vector<uint8_t> has_kid(f->n, 0);
@@ -1743,6 +1769,8 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
     res->M = pl->M;
     res->n_reads = frags_per_sample * uint64_t(mates) * samples.size();
     res->tile_size = T;
+    res->sample_src = sample_src;
+    res->pre_in_normal = c->preneoplastic_in_normal != 0;
     res->alt = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
     res->depth = DBuf<uint32_t>(P, uint64_t(res->n_samples) * pl->M);
     ck(cudaMemsetAsync(res->alt.p, 0, sizeof(uint32_t) * res->n_samples * pl->M, st), "memset");
@@ -2124,3 +2152,6 @@ pg_status pg_calib_adam(pg_calib* c, float* params, uint32_t steps, float lr, fl
 }  // extern "C"
 
 #include "pg_batch_impl.h"
+#include "pg_frames_impl.h"
+#include "pg_archive_impl.h"
+#include "pg_inputs_impl.h"

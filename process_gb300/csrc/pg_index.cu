@@ -377,6 +377,57 @@ void genome_gather(const uint32_t* g, const uint32_t* nmask, uint64_t G, const u
   if (n) { k_gather_bases<<<unsigned((n + 255) / 256), 256, 0, st>>>(g, nmask, pos, n, G, out); note_launch(); }
 }
 
+// SID strings of placed mutations (the ref and alt columns of the result data
+// frames): up to 8 characters each, 4 bits per character (A 1, C 2, G 3, N 4,
+// T 5, the characters' alphabetical order; 0 ends the string), the first in
+// the highest nibble, so that codes compare as the strings do.  An SNV is
+// (reference base, alt base); an insertion (anchor, anchor + inserted bases);
+// a deletion (anchor + deleted bases, anchor).
+__device__ __forceinline__ uint32_t sid_char(const uint32_t* __restrict__ g, const uint32_t* __restrict__ nmask,
+                                             uint64_t G, uint64_t p) {
+  if (p >= G) p = G - 1;
+  if (base_unknown(nmask, p)) return 4u;
+  const uint32_t b = base_at(g, uint32_t(p));
+  return b == 3u ? 5u : b + 1u;
+}
+
+__global__ void k_row_info(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ aux,
+                           const uint8_t* __restrict__ kind, const uint8_t* __restrict__ sig,
+                           const uint8_t* __restrict__ nature, const uint32_t* __restrict__ rows, uint64_t n,
+                           const uint32_t* __restrict__ g, const uint32_t* __restrict__ nmask, uint64_t G,
+                           uint4* __restrict__ out) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t m = rows ? rows[i] : i;
+  const uint32_t L = locus[m], a = aux[m], k = kind[m];
+  const uint32_t anchor = sid_char(g, nmask, G, L) << 28;
+  uint32_t ref = anchor, alt = anchor;
+  if (k == 0) {
+    const uint32_t b = a & 3u;
+    alt = (b == 3u ? 5u : b + 1u) << 28;
+  } else {
+    const uint32_t l = (a >> 1) & 7u;
+    for (uint32_t q = 0; q < l; ++q) {
+      if (a & 1u) {
+        const uint32_t b = (a >> (8 + 2 * q)) & 3u;
+        alt |= (b == 3u ? 5u : b + 1u) << (24 - 4 * q);
+      } else {
+        ref |= sid_char(g, nmask, G, uint64_t(L) + 1 + q) << (24 - 4 * q);
+      }
+    }
+  }
+  out[i] = make_uint4(L, ref, alt, k | (uint32_t(sig[m]) << 8) | (uint32_t(nature[m]) << 16));
+}
+
+void row_info(const uint32_t* locus, const uint32_t* aux, const uint8_t* kind, const uint8_t* sig,
+              const uint8_t* nature, const uint32_t* rows, uint64_t n, const uint32_t* g, const uint32_t* nmask,
+              uint64_t G, uint4* out, cudaStream_t st) {
+  if (n) {
+    k_row_info<<<unsigned((n + 255) / 256), 256, 0, st>>>(locus, aux, kind, sig, nature, rows, n, g, nmask, G, out);
+    note_launch();
+  }
+}
+
 // the unknown bases (codes > 3) of an uploaded genome as one bit per position,
 // and whether there is any
 __global__ void k_genome_nmask(const uint8_t* __restrict__ codes, uint64_t G, uint64_t nwords,

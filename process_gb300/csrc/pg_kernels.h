@@ -29,6 +29,12 @@ uint32_t index_num_tiles(uint64_t G);
 // bases at pos (BASE_INVALID for positions outside the genome or unknown)
 void genome_gather(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* pos, uint64_t n,
                    uint8_t* out, cudaStream_t st);
+// per placed mutation rows[i] (all rows when NULL): {locus, ref code, alt
+// code, kind | signature << 8 | nature << 16}; the codes hold up to 8
+// characters of "ACGNT" coded 1..5, 4 bits each, the first character highest
+void row_info(const uint32_t* locus, const uint32_t* aux, const uint8_t* kind, const uint8_t* sig,
+              const uint8_t* nature, const uint32_t* rows, uint64_t n, const uint32_t* g, const uint32_t* nmask,
+              uint64_t G, uint4* out, cudaStream_t st);
 int index_num_classes(int which);  // 0 = SBS contexts (32), 1 = ID classes (83)
 // allocation-free per-class totals over a caller-held genome (see pg_index.cu);
 // returns nullptr on success, else a message

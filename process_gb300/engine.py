@@ -19,6 +19,7 @@ library through the C-ABI; this module only validates and arranges inputs.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import itertools
 from dataclasses import dataclass, field
 from typing import Iterable, Mapping, Sequence
@@ -62,6 +63,7 @@ class GenomeSpec:
     bases: np.ndarray | None = None
     seed: int = 0
     gc: float = 0.5
+    path: str = ""          # the FASTA file it was read from, if any (a forest's reference path)
 
     @property
     def total(self) -> int:
@@ -102,7 +104,25 @@ class GenomeSpec:
             raise DomainError(_lib.PG_ERR_DOMAIN, f"chromosomes not in {path}: {', '.join(missing)}")
         if not names:
             raise DomainError(_lib.PG_ERR_DOMAIN, f"no chromosome read from {path}")
-        return cls(names, lengths, bases=np.concatenate(parts))
+        return cls(names, lengths, bases=np.concatenate(parts), path=str(path))
+
+
+def read_signature_table(path, type_: int) -> dict:
+    """A signature table in the reference's format
+    (Signature::read_from_stream, src/mutation_engine.cpp:389-397): a
+    tab-separated "Type" column of COSMIC class labels ("A[C>A]A" for SBS,
+    type 0; "1:Del:C:0" .. "5:Del:M:5" for ID, type 1) and one probability
+    column per signature.  Returns {name: probabilities in class order},
+    parsed by the library (pg_signature_table_read)."""
+    n, size = C.c_uint32(), C.c_uint64()
+    p = str(path).encode()
+    check(lib().pg_signature_table_read(type_, p, C.byref(n), C.byref(size), None, None))
+    nc = 96 if type_ == 0 else 83
+    names = C.create_string_buffer(max(size.value, 1))
+    probs = np.empty((n.value, nc), dtype=np.float64)
+    check(lib().pg_signature_table_read(type_, p, C.byref(n), C.byref(size), names, ptr(probs, C.c_double)))
+    keys = names.raw[:size.value].split(b"\0")[:n.value]
+    return {k.decode(): probs[i] for i, k in enumerate(keys)}
 
 
 # ---------------------------------------------------------------- driver specs
@@ -414,13 +434,20 @@ class MutationEngine:
             self._h = None
 
     # -- signatures and exposures ------------------------------------------------
-    def set_signatures(self, type_: int, sigs: Mapping[str, Sequence[float]]) -> None:
+    def set_signatures(self, type_: int, sigs) -> None:
+        """Signatures of a type (0 SBS, 1 ID): a mapping name -> class
+        probabilities, or the path of a signature table in the reference's
+        format (see :func:`read_signature_table`)."""
+        if isinstance(sigs, (str, os.PathLike)):
+            sigs = read_signature_table(sigs, type_)
         nc = 96 if type_ == 0 else 83
         names = list(sigs.keys())
         mat = np.ascontiguousarray(np.array([np.asarray(sigs[k], dtype=np.float64) for k in names]))
         if mat.shape != (len(names), nc):
             raise DomainError(_lib.PG_ERR_DOMAIN, f"signatures must have {nc} classes")
         check(lib().pg_engine_set_signatures(self._h, type_, len(names), ptr(mat, C.c_double)))
+        arr = (C.c_char_p * len(names))(*[str(k).encode() for k in names])
+        check(lib().pg_engine_set_signature_names(self._h, type_, len(names), arr))
         self.sig_names[type_] = names
         self._sigs[type_] = {k: mat[i].tolist() for i, k in enumerate(names)}
 
@@ -623,7 +650,25 @@ class MutationEngine:
                               num_of_preneoplatic_indels=int(num_of_preneoplatic_indels), seed=s,
                               preneoplatic_SNV_signature_name=preneoplatic_SNV_signature_name,
                               preneoplatic_indel_signature_name=preneoplatic_indel_signature_name)
+        # the forest keeps the configuration it was placed with (exposures,
+        # mutants, species rates), as the reference's forest holds its own
+        # copies: later add_exposure / add_mutant calls do not change it
+        pf._config = self._config()
+        pf._species_rates = self.get_species_rates()
+        pf._reference_path = getattr(self.genome, "path", "") or ""
         return pf
+
+    def _config(self) -> dict:
+        """JSON-ready copy of the engine's configuration."""
+        import copy
+        return {"context_sampling": self.context_sampling, "max_motif_size": self.max_motif_size,
+                "max_repetition_storage": self.max_repetition_storage,
+                "avoid_homozygous_losses": self.avoid_homozygous_losses,
+                "infinite_sites_model": self.infinite_sites_model,
+                "SBS_signatures": _plain(self._sigs[0]), "indel_signatures": _plain(self._sigs[1]),
+                "exposures": copy.deepcopy(_plain(self._exposures)),
+                "mutants": copy.deepcopy(_plain(self._mutant_specs)),
+                "passenger_CNAs": _plain(self.passenger_CNAs)}
 
 
 class PhylogeneticForest:
@@ -672,61 +717,29 @@ class PhylogeneticForest:
     def get_nodes(self) -> dict:
         return self.forest.get_nodes()
 
-    def _ref_alt(self, t: dict, rows: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray]:
-        """ref / alt strings of the rows (all when None): one base gather for
-        the SNVs and one for the indels' anchor windows."""
-        eng = self.engine
-        rows = np.arange(len(t["locus"])) if rows is None else np.asarray(rows, dtype=np.int64)
-        n = len(rows)
-        kind, aux = t["kind"][rows], t["aux"][rows].astype(np.int64)
-        locus = t["locus"][rows].astype(np.int64)
-        ref = np.empty(n, dtype=object)
-        alt = np.empty(n, dtype=object)
-        snv = kind == 0
-        rb = eng.gather_bases(locus[snv])
-        ref[snv] = BASES[np.minimum(rb, 4)]
-        alt[snv] = BASES[aux[snv] & 3]
-        ind = np.nonzero(~snv)[0]
-        if len(ind):
-            a = aux[ind]
-            ins, ln, bases = (a & 1).astype(bool), (a >> 1) & 7, a >> 8
-            # the anchor and the 7 bases after it (a deletion spans at most 7)
-            win = np.minimum(locus[ind][:, None] + np.arange(8)[None, :], eng.genome.total - 1)
-            gch = BASES[np.minimum(eng.gather_bases(win.ravel()).reshape(-1, 8), 4)]
-            added = BASES[(bases[:, None] >> (2 * np.arange(7))[None, :]) & 3]
-            for length in np.unique(ln):
-                L = int(length)
-                # insertion: ref = anchor, alt = anchor + L inserted bases
-                sel = np.nonzero(ins & (ln == L))[0]
-                if len(sel):
-                    ref[ind[sel]] = gch[sel, 0]
-                    chars = np.ascontiguousarray(np.concatenate([gch[sel, :1], added[sel, :L]], axis=1))
-                    alt[ind[sel]] = chars.view(f"<U{L + 1}").ravel()
-                # deletion: ref = anchor + L deleted bases, alt = anchor
-                sel = np.nonzero(~ins & (ln == L))[0]
-                if len(sel):
-                    ref[ind[sel]] = np.ascontiguousarray(gch[sel, :L + 1]).view(f"<U{L + 1}").ravel()
-                    alt[ind[sel]] = gch[sel, 0]
-        return ref, alt
-
-    def _cause(self, t: dict, rows: np.ndarray | None = None) -> np.ndarray:
-        """Signature name of each row (None for drivers and unknown indices)."""
-        rows = np.arange(len(t["sig"])) if rows is None else np.asarray(rows, dtype=np.int64)
-        sig, kind = t["sig"][rows].astype(np.int64), t["kind"][rows]
-        out = np.full(len(rows), None, dtype=object)
-        for k in np.unique(kind):
-            names = list(self.engine.sig_names[int(k)]) if int(k) < len(self.engine.sig_names) else []
-            table = np.array(names + [None], dtype=object)
+    def mutation_columns(self, rows=None) -> dict:
+        """The columns chr, chr_pos, ref, alt, type, cause and class of the
+        placed mutations ``rows`` (indices into :meth:`table`; all when None),
+        from pg_placed_mutation_info."""
+        r = None if rows is None else np.ascontiguousarray(rows, dtype=np.uint32)
+        n = self.num_of_mutations if r is None else len(r)
+        chr_, pos = np.empty(n, np.uint32), np.empty(n, np.uint32)
+        ref, alt = np.zeros(n * _lib.SID_CHARS, np.uint8), np.zeros(n * _lib.SID_CHARS, np.uint8)
+        kind, cause, nat = np.empty(n, np.uint8), np.empty(n, np.int32), np.empty(n, np.uint8)
+        if n:
+            check(lib().pg_placed_mutation_info(self._h, n, ptr(r, C.c_uint32), ptr(chr_, C.c_uint32),
+                                                ptr(pos, C.c_uint32), _cbuf(ref), _cbuf(alt), ptr(kind, C.c_uint8),
+                                                ptr(cause, C.c_int32), ptr(nat, C.c_uint8)))
+        names = np.array(self.engine.chr_names, dtype=object)
+        sig = [np.array(list(self.engine.sig_names[k]) + [None], dtype=object) for k in (0, 1)]
+        cz = np.where(cause < 0, 10 ** 6, cause)
+        cnames = np.full(n, None, dtype=object)
+        for k in (0, 1):
             m = kind == k
-            sk = sig[m]
-            out[m] = table[np.where((sk == 0xFF) | (sk >= len(names)), len(names), sk)]
-        return out
-
-    def _chr_pos(self, locus: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
-        off = self.engine.chr_off
-        ci = np.searchsorted(off, locus.astype(np.uint64), side="right") - 1
-        names = np.array(self.engine.chr_names, dtype=object)[ci]
-        return names, (locus.astype(np.int64) - off[ci].astype(np.int64) + 1)
+            cnames[m] = sig[k][np.minimum(cz[m], len(sig[k]) - 1)]
+        return {"chr": names[chr_], "chr_pos": pos.astype(np.int64), "ref": _sid_strings(ref, n),
+                "alt": _sid_strings(alt, n), "type": np.where(kind == 0, "SNV", "indel").astype(object),
+                "cause": cnames, "class": NATURES[nat].astype(object)}
 
     def leaf_carriers(self, leaf: int) -> np.ndarray:
         """Mask of the placed mutations on the root path of node ``leaf``
@@ -740,89 +753,43 @@ class PhylogeneticForest:
         x = tin[int(leaf)]
         return ~inner | ((tin[ec] <= x) & (x < tout[ec]))
 
-    def _lineage(self) -> dict:
-        """Instance lineage chains and every mutation's order key
-        (pg_placed_lineage_copy)."""
-        if getattr(self, "_lin_cache", None) is None:
-            ni, nl = C.c_uint32(), C.c_uint32()
-            check(lib().pg_placed_lineage_dims(self._h, C.byref(ni), C.byref(nl)))
-            d = {"off": np.zeros(ni.value + 1, np.uint32), "anc": np.zeros(max(nl.value, 1), np.uint16),
-                 "key": np.zeros(max(nl.value, 1), np.uint64),
-                 "order": np.zeros(max(self.num_of_mutations, 1), np.uint64)}
-            check(lib().pg_placed_lineage_copy(self._h, ptr(d["off"], C.c_uint32), ptr(d["anc"], C.c_uint16),
-                                               ptr(d["key"], C.c_uint64), ptr(d["order"], C.c_uint64)))
-            d["n_instances"] = ni.value
-            self._lin_cache = d
-        return self._lin_cache
-
-    def _cell_rows(self, leaf: int) -> tuple[np.ndarray, np.ndarray]:
-        """(mutation rows, allele instance) of the mutations sampled cell
-        ``leaf`` holds: those on its root path, once per allele instance of
-        its genome at the locus that carries them (the placed instance, and
-        the copies of it made after the mutation), in mutation order."""
-        t = self.table()
-        idx = np.nonzero(self.leaf_carriers(leaf))[0]
-        lin = self._lineage()
-        cls, n_classes, _ = self.node_classes()
-        if n_classes <= 1 and lin["n_instances"] <= 2:       # no copy-number event
-            return idx, t["allele"][idx].astype(np.int64)
-        d = self._classes()
-        c = int(cls[leaf])
-        lo, hi = int(d["seg_off"][c]), int(d["seg_off"][c + 1])
-        st, en = d["start"][lo:hi].astype(np.int64), d["end"][lo:hi].astype(np.int64)
-        loc = t["locus"][idx].astype(np.int64)
-        k = np.searchsorted(st, loc, side="right") - 1
-        inside = (k >= 0) & (loc < en[np.maximum(k, 0)]) if hi > lo else np.zeros(len(idx), bool)
-        ks = np.maximum(k, 0)
-        ioff = d["ioff"][lo:hi][ks].astype(np.int64) if hi > lo else np.zeros(len(idx), np.int64)
-        icnt = np.where(inside, d["icnt"][lo:hi][ks], 0).astype(np.int64) if hi > lo else np.zeros(len(idx), np.int64)
-        x = t["allele"][idx].astype(np.int64)
-        km = lin["order"][idx]
-        coff = lin["off"].astype(np.int64)
-        rows, alle, slot = [], [], []
-        for j in range(int(icnt.max()) if len(icnt) else 0):
-            sel = np.nonzero(j < icnt)[0]
-            y = d["list"][ioff[sel] + j].astype(np.int64)
-            carry = y == x[sel]
-            # y's lineage: x in its chain with a copy key above the mutation's
-            b, ln = coff[y], coff[y + 1] - coff[y]
-            found = carry.copy()
-            for dep in range(int(ln.max()) if len(ln) else 0):
-                act = ~found & (dep < ln)
-                a = np.where(act, lin["anc"][np.where(act, b + dep, 0)].astype(np.int64), -1)
-                hit = act & (a == x[sel])
-                carry |= hit & (lin["key"][np.where(hit, b + dep, 0)] > km[sel])
-                found |= hit
-            rows.append(idx[sel][carry]); alle.append(y[carry]); slot.append(np.full(int(carry.sum()), j))
-        if not rows:
-            return idx[:0], idx[:0].astype(np.int64)
-        r, a, s_ = np.concatenate(rows), np.concatenate(alle), np.concatenate(slot)
-        o = np.lexsort((s_, r))
-        return r[o], a[o]
-
-    def get_sampled_cell_mutations(self, cell_id=None) -> dict:
-        """Columns cell_id, chr, chr_pos, allele, ref, alt, type, cause, class
-        (src/phylogenetic_forest.cpp:452-507): every mutation a sampled cell
-        holds, once per allele instance of its genome carrying it (an SID is
-        copied with its allele by an amplification or a WGD after it, and
-        leaves with a deleted allele); ``allele`` is the instance."""
+    def _getter_cells(self, cell_id=None) -> np.ndarray:
+        """Node ids of the sampled cells by cell id (the reference's std::map
+        order), or of the one cell ``cell_id``."""
         f = self.forest
-        t = self.table()
-        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
         if cell_id is not None:
             hit = np.nonzero(f.cell_id == int(cell_id))[0]
             if len(hit) == 0 or not f.is_leaf[hit[0]]:
                 raise DomainError(_lib.PG_ERR_DOMAIN, f'Cell "{cell_id}" is not a leaf')
-            leaves = hit
-        per = [self._cell_rows(int(lf)) for lf in leaves]
-        rows = np.concatenate([r for r, _ in per]) if per else np.zeros(0, np.int64)
-        alle = np.concatenate([a for _, a in per]) if per else np.zeros(0, np.int64)
-        cell = np.concatenate([np.full(len(r), f.cell_id[lf]) for lf, (r, _) in zip(leaves, per)]) if per else rows
-        ref, alt = self._ref_alt(t, rows)
-        chrn, pos = self._chr_pos(t["locus"][rows])
-        return {"cell_id": cell, "chr": chrn, "chr_pos": pos, "allele": alle.astype(np.int64), "ref": ref, "alt": alt,
-                "type": np.where(t["kind"][rows] == 0, "SNV", "indel"), "cause": self._cause(t, rows),
-                "class": NATURES[t["nature"][rows]]}
+            return np.ascontiguousarray(hit[:1], dtype=np.uint32)
+        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
+        return np.ascontiguousarray(leaves[np.argsort(f.cell_id[leaves], kind="stable")], dtype=np.uint32)
+
+    def cell_mutation_rows(self, cell_id=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(cell node, mutation row, allele instance) of every mutation each
+        sampled cell holds (pg_placed_cell_mutations), in the order of
+        :meth:`get_sampled_cell_mutations`."""
+        cells = self._getter_cells(cell_id)
+        n = C.c_uint64()
+        check(lib().pg_placed_cell_mutations(self._h, len(cells), ptr(cells, C.c_uint32), C.byref(n)))
+        cell, row, allele = (np.empty(n.value, np.uint32) for _ in range(3))
+        check(lib().pg_placed_cell_mutations_copy(self._h, ptr(cell, C.c_uint32), ptr(row, C.c_uint32),
+                                                  ptr(allele, C.c_uint32)))
+        return cell, row, allele
+
+    def get_sampled_cell_mutations(self, cell_id=None) -> dict:
+        """Columns cell_id, chr, chr_pos, allele, ref, alt, type, cause, class
+        (src/phylogenetic_forest.cpp:452-507), built by the library
+        (pg_placed_cell_mutations): every mutation a sampled cell holds, once
+        per allele instance of its genome carrying it (an SID is copied with
+        its allele by an amplification or a WGD after it, and leaves with a
+        deleted allele); ``allele`` is the instance.  Cells by cell id, each
+        cell's rows by chromosome, allele, position."""
+        cell, row, allele = self.cell_mutation_rows(cell_id)
+        cols = self.mutation_columns(row)
+        return {"cell_id": self.forest.cell_id[cell], "chr": cols["chr"], "chr_pos": cols["chr_pos"],
+                "allele": allele.astype(np.int64), "ref": cols["ref"], "alt": cols["alt"], "type": cols["type"],
+                "cause": cols["cause"], "class": cols["class"]}
 
     def cna_table(self) -> dict:
         """Applied CNA / WGD events: node, type (0 deletion, 1 amplification,
@@ -850,166 +817,76 @@ class PhylogeneticForest:
     def get_sampled_cell_CNAs(self, cell_id=None) -> dict:
         """Columns cell_id, type ("A", "D"; "WGD" for a whole-genome doubling,
         whose chr/begin/end are empty), chr, begin, end, allele, src allele
-        (NA, i.e. -1, for deletions) and class (src/phylogenetic_forest.cpp:509-562)."""
-        f = self.forest
+        (NA, i.e. -1, for deletions) and class (src/phylogenetic_forest.cpp:509-562):
+        the events on each sampled cell's root path (pg_placed_cell_cnas)."""
+        cells = self._getter_cells(cell_id)
         c = self.cna_table()
-        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
-        if cell_id is not None:
-            hit = np.nonzero(f.cell_id == int(cell_id))[0]
-            if len(hit) == 0 or not f.is_leaf[hit[0]]:
-                raise DomainError(_lib.PG_ERR_DOMAIN, f'Cell "{cell_id}" is not a leaf')
-            leaves = hit
+        n = C.c_uint64()
+        check(lib().pg_placed_cell_cnas(self._h, len(cells), ptr(cells, C.c_uint32), C.byref(n)))
+        cell, idx = np.empty(n.value, np.uint32), np.empty(n.value, np.uint32)
+        check(lib().pg_placed_cell_cnas_copy(self._h, ptr(cell, C.c_uint32), ptr(idx, C.c_uint32)))
         names = np.array(self.engine.chr_names + [""], dtype=object)
         tname = np.array(["D", "A", "WGD"], dtype=object)
-        cols = {k: [] for k in ("cell_id", "type", "chr", "begin", "end", "allele", "src allele", "class")}
-        for lf in leaves:
-            path = set()
-            v = int(lf)
-            while v >= 0:
-                path.add(v)
-                v = int(f.parent[v])
-            m = np.isin(c["node"], np.fromiter(path, dtype=np.int64))
-            wgd = c["type"][m] == 2
-            cols["cell_id"].append(np.full(m.sum(), f.cell_id[lf]))
-            cols["type"].append(tname[c["type"][m]])
-            cols["chr"].append(names[np.where(wgd, len(names) - 1, c["chr"][m])])
-            cols["begin"].append(np.where(wgd, -1, c["begin"][m].astype(np.int64)))
-            cols["end"].append(np.where(wgd, -1, c["end"][m].astype(np.int64)))
-            cols["allele"].append(np.where(wgd, -1, c["allele"][m].astype(np.int64)))
-            cols["src allele"].append(np.where(c["type"][m] == 1, c["src"][m].astype(np.int64), -1))
-            cols["class"].append(np.where(c["driver"][m] == 1, "driver", "passenger"))
-        return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
+        typ = c["type"][idx]
+        wgd = typ == 2
+        return {"cell_id": self.forest.cell_id[cell], "type": tname[typ],
+                "chr": names[np.where(wgd, len(names) - 1, c["chr"][idx])],
+                "begin": np.where(wgd, -1, c["begin"][idx].astype(np.int64)),
+                "end": np.where(wgd, -1, c["end"][idx].astype(np.int64)),
+                "allele": np.where(wgd, -1, c["allele"][idx].astype(np.int64)),
+                "src allele": np.where(typ == 1, c["src"][idx].astype(np.int64), -1),
+                "class": np.where(c["driver"][idx] == 1, "driver", "passenger").astype(object)}
 
     # -- copy-number getters (allelic fragmentation) ------------------------------------
-    def _classes(self) -> dict:
-        """Genotype classes as segments with each instance's germline allele."""
-        if getattr(self, "_cls_cache", None) is None:
-            nc, ns, nl, ni = (C.c_uint32() for _ in range(4))
-            check(lib().pg_placed_class_dims(self._h, C.byref(nc), C.byref(ns), C.byref(nl), C.byref(ni)))
-            d = {"seg_off": np.empty(nc.value + 1, np.uint32), "start": np.empty(ns.value, np.uint32),
-                 "end": np.empty(ns.value, np.uint32), "ioff": np.empty(ns.value, np.uint32),
-                 "icnt": np.empty(ns.value, np.uint32), "list": np.empty(max(nl.value, 1), np.uint16),
-                 "root": np.empty(max(ni.value, 1), np.uint8)}
-            check(lib().pg_placed_class_copy(self._h, ptr(d["seg_off"], C.c_uint32), ptr(d["start"], C.c_uint32),
-                                             ptr(d["end"], C.c_uint32), ptr(d["ioff"], C.c_uint32),
-                                             ptr(d["icnt"], C.c_uint32), ptr(d["list"], C.c_uint16),
-                                             ptr(d["root"], C.c_uint8)))
-            # copies of germline allele 1 per segment (the rest descend from allele 0)
-            roots = d["root"][d["list"][:max(nl.value, 1)]].astype(np.int64)
-            csum = np.concatenate([[0], np.cumsum(roots)])
-            d["a1"] = (csum[d["ioff"] + d["icnt"]] - csum[d["ioff"]]).astype(np.int64)
-            d["a0"] = d["icnt"].astype(np.int64) - d["a1"]
-            d["n_classes"] = nc.value
-            self._cls_cache = d
-        return self._cls_cache
-
-    def _class_fragments(self, c: int) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
-        """(absolute begin, end (half-open), copies of allele 0, of allele 1) of
-        the maximal stretches of class c with one allelic type, chromosome by
-        chromosome (uncovered stretches have type (0, 0))."""
-        d = self._classes()
-        lo, hi = int(d["seg_off"][c]), int(d["seg_off"][c + 1])
-        st, en = d["start"][lo:hi].astype(np.int64), d["end"][lo:hi].astype(np.int64)
-        off = self.engine.chr_off.astype(np.int64)
-        cuts = np.unique(np.concatenate([off, st, en]))
-        b, e = cuts[:-1], cuts[1:]
-        k = np.searchsorted(st, b, side="right") - 1
-        inside = (k >= 0) & (b < en[np.maximum(k, 0)])
-        a0 = np.where(inside, d["a0"][lo:hi][np.maximum(k, 0)] if hi > lo else 0, 0)
-        a1 = np.where(inside, d["a1"][lo:hi][np.maximum(k, 0)] if hi > lo else 0, 0)
-        chrom = np.searchsorted(off, b, side="right") - 1
-        new = np.r_[True, (chrom[1:] != chrom[:-1]) | (a0[1:] != a0[:-1]) | (a1[1:] != a1[:-1])]
-        first = np.nonzero(new)[0]
-        last = np.r_[first[1:], len(b)] - 1
-        return b[first], e[last], a0[first], a1[first]
-
-    def _frag_rows(self, b, e, a0, a1):
-        off = self.engine.chr_off.astype(np.int64)
-        ci = np.searchsorted(off, b, side="right") - 1
-        names = np.array(self.engine.chr_names, dtype=object)[ci]
-        return names, b - off[ci] + 1, e - off[ci], np.maximum(a0, a1), np.minimum(a0, a1)
-
     def get_cell_allelic_fragmentation(self) -> dict:
         """Columns cell_id, chr, begin, end, major, minor: every sampled cell's
         genome cut into stretches of one allelic type (copies of the two
-        germline alleles; major = the larger), src/phylogenetic_forest.cpp:867-927."""
-        f = self.forest
-        cls, _, _ = self.node_classes()
-        leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
-        per = {}
-        cols = {k: [] for k in ("cell_id", "chr", "begin", "end", "major", "minor")}
-        for lf in leaves:
-            c = int(cls[lf])
-            if c not in per:
-                per[c] = self._frag_rows(*self._class_fragments(c))
-            names, b, e, mj, mn = per[c]
-            cols["cell_id"].append(np.full(len(b), f.cell_id[lf]))
-            cols["chr"].append(names); cols["begin"].append(b); cols["end"].append(e)
-            cols["major"].append(mj); cols["minor"].append(mn)
-        return {k: (np.concatenate(v) if v else np.array([])) for k, v in cols.items()}
+        germline alleles; major = the larger), src/phylogenetic_forest.cpp:867-927
+        (pg_placed_cell_fragmentation)."""
+        cells = self._getter_cells()
+        n = C.c_uint64()
+        check(lib().pg_placed_cell_fragmentation(self._h, len(cells), ptr(cells, C.c_uint32), C.byref(n)))
+        cell, chr_, b, e, mj, mn = (np.empty(n.value, np.uint32) for _ in range(6))
+        check(lib().pg_placed_cell_fragmentation_copy(self._h, *(ptr(x, C.c_uint32) for x in (cell, chr_, b, e, mj,
+                                                                                              mn))))
+        names = np.array(self.engine.chr_names, dtype=object)
+        return {"cell_id": self.forest.cell_id[cell], "chr": names[chr_], "begin": b.astype(np.int64),
+                "end": e.astype(np.int64), "major": mj.astype(np.int64), "minor": mn.astype(np.int64)}
 
     def get_bulk_allelic_fragmentation(self, sample_name: str | None = None) -> dict:
         """Columns chr, begin, end, major, minor, ratio: for every stretch of
         the genome on which the sampled cells (of one sample, or all) keep
         their allelic types, each type with the fraction of cells showing it
-        (src/phylogenetic_forest.cpp:767-820)."""
+        (src/phylogenetic_forest.cpp:767-820; pg_placed_bulk_fragmentation)."""
         f = self.forest
-        cls, _, _ = self.node_classes()
-        sel = f.is_leaf & (f.sample >= 0)
+        s = -1
         if sample_name is not None:
             if sample_name not in f.sample_names:
                 raise DomainError(_lib.PG_ERR_DOMAIN, f'Unknown sample "{sample_name}".')
-            sel &= f.sample == f.sample_names.index(sample_name)
-        leaf_cls, counts = np.unique(cls[sel], return_counts=True)
-        n_cells = float(counts.sum())
-        frags = [self._class_fragments(int(c)) for c in leaf_cls]
-        cuts = np.unique(np.concatenate([fr[0] for fr in frags] + [fr[1] for fr in frags]))
-        b, e = cuts[:-1], cuts[1:]
-        keep = np.ones(len(b), dtype=bool)
-        types = []
-        for (fb, fe, f0, f1) in frags:
-            k = np.searchsorted(fb, b, side="right") - 1
-            types.append((f0[k], f1[k]))
-        # merge neighbouring stretches with the same type in every class and chromosome
-        off = self.engine.chr_off.astype(np.int64)
-        chrom = np.searchsorted(off, b, side="right") - 1
-        same = np.ones(len(b) - 1, dtype=bool) if len(b) > 1 else np.zeros(0, dtype=bool)
-        for t0, t1 in types:
-            same &= (t0[1:] == t0[:-1]) & (t1[1:] == t1[:-1])
-        same &= chrom[1:] == chrom[:-1]
-        start = np.r_[True, ~same]
-        first = np.nonzero(start)[0]
-        last = np.r_[first[1:], len(b)] - 1
-        cols = {k: [] for k in ("chr", "begin", "end", "major", "minor", "ratio")}
-        for i0, i1 in zip(first, last):
-            agg = {}
-            for (t0, t1), n in zip(types, counts):
-                key = (int(t0[i0]), int(t1[i0]))
-                agg[key] = agg.get(key, 0) + int(n)
-            names, bb, ee, _, _ = self._frag_rows(np.array([b[i0]]), np.array([e[i1]]), np.zeros(1), np.zeros(1))
-            for (x0, x1), n in sorted(agg.items()):
-                cols["chr"].append(names[0]); cols["begin"].append(int(bb[0])); cols["end"].append(int(ee[0]))
-                cols["major"].append(max(x0, x1)); cols["minor"].append(min(x0, x1)); cols["ratio"].append(n / n_cells)
-        return {k: np.array(v, dtype=object if k == "chr" else None) for k, v in cols.items()}
+            s = f.sample_names.index(sample_name)
+        n = C.c_uint64()
+        check(lib().pg_placed_bulk_fragmentation(self._h, s, C.byref(n)))
+        chr_, b, e, mj, mn = (np.empty(n.value, np.uint32) for _ in range(5))
+        ratio = np.empty(n.value, np.float64)
+        check(lib().pg_placed_bulk_fragmentation_copy(self._h, *(ptr(x, C.c_uint32) for x in (chr_, b, e, mj, mn)),
+                                                      ptr(ratio, C.c_double)))
+        names = np.array(self.engine.chr_names, dtype=object)
+        return {"chr": names[chr_], "begin": b.astype(np.int64), "end": e.astype(np.int64),
+                "major": mj.astype(np.int64), "minor": mn.astype(np.int64), "ratio": ratio}
 
     def get_samples_info(self) -> dict:
         """name, tumour_cells, DNA_quantity, equivalent_normal_cells
         (src/phylogenetic_forest.cpp:57-99): the DNA of a sample is the summed
-        allelic size of its sampled cells' genomes."""
+        allelic size of its sampled cells' genomes (pg_placed_samples_info)."""
         info = self.forest.get_samples_info()
-        normal_dna = 2.0 * self.engine.genome.total
         f = self.forest
-        d = self._classes()
-        size = np.zeros(d["n_classes"], dtype=np.float64)
-        seg_cls = np.repeat(np.arange(d["n_classes"]), np.diff(d["seg_off"].astype(np.int64)))
-        np.add.at(size, seg_cls, (d["end"].astype(np.float64) - d["start"]) * d["icnt"])
-        cls, _, _ = self.node_classes()
-        dna = np.zeros(len(info["name"]), dtype=np.float64)
-        for i, name in enumerate(info["name"]):
-            j = f.sample_names.index(name)
-            dna[i] = size[cls[f.is_leaf & (f.sample == j)]].sum()
-        info["DNA_quantity"] = dna
-        info["equivalent_normal_cells"] = dna / normal_dna
+        k = len(f.sample_names)
+        cells, dna, eq = np.empty(max(k, 1), np.uint32), np.empty(max(k, 1)), np.empty(max(k, 1))
+        check(lib().pg_placed_samples_info(self._h, ptr(cells, C.c_uint32), ptr(dna, C.c_double),
+                                           ptr(eq, C.c_double)))
+        order = [f.sample_names.index(name) for name in info["name"]]
+        info["DNA_quantity"] = dna[order]
+        info["equivalent_normal_cells"] = eq[order]
         return info
 
     def save(self, filename: str, quiet: bool = False) -> None:
@@ -1022,9 +899,21 @@ class PhylogeneticForest:
     def get_species_info(self) -> dict:
         """The registered species (src/phylogenetic_forest.cpp:220-255):
         mutant, epistate, SNV_rate, indel_rate and CNA_rate."""
-        r = self.engine.get_species_rates()
+        r = getattr(self, "_species_rates", None) or self.engine.get_species_rates()
         return {"mutant": r["mutant"], "epistate": r["epistate"], "SNV_rate": r["SNV"], "indel_rate": r["indel"],
                 "CNA_rate": r["CNA"]}
+
+    def _mutants(self) -> list:
+        """add_mutant calls in force when the forest was placed."""
+        cfg = getattr(self, "_config", None)
+        if cfg is None:
+            return list(self.engine._mutant_specs)
+        return [(name, rates, [_driver(d) for d in drivers]) for name, rates, drivers in cfg["mutants"]]
+
+    def _exposure_list(self) -> list:
+        """Timed exposures in force when the forest was placed."""
+        cfg = getattr(self, "_config", None)
+        return list(self.engine._exposures) if cfg is None else [(float(t), dict(c)) for t, c in cfg["exposures"]]
 
     def get_reference_path(self) -> str:
         """The reference genome path recorded with the forest (the FASTA the
@@ -1042,7 +931,7 @@ class PhylogeneticForest:
         where the reference reports NA)."""
         eng = self.engine
         specs = {}
-        for name, _, drivers in eng._mutant_specs:
+        for name, _, drivers in self._mutants():
             specs[name] = list(drivers)
         cols = {k: [] for k in ("mutant", "order", "type", "CNA_type", "chr", "start", "end", "ref", "alt",
                                 "allele", "src_allele")}
@@ -1073,7 +962,7 @@ class PhylogeneticForest:
         rows, each by time and signature name."""
         eng = self.engine
         timed: list[dict] = [{}, {}]
-        for t, coef in eng._exposures:
+        for t, coef in self._exposure_list():
             for ty in (0, 1):
                 part = {k: float(v) for k, v in coef.items() if k in eng.sig_names[ty]}
                 if part:
@@ -1109,7 +998,8 @@ class PhylogeneticForest:
             ci = eng._chr_index(mutation.chr)
             locus = int(eng.chr_off[ci]) + int(mutation.chr_pos) - 1
             cand = np.nonzero(t["locus"].astype(np.int64) == locus)[0]
-            ref, alt = self._ref_alt(t, cand) if len(cand) else (np.array([]), np.array([]))
+            cols = self.mutation_columns(cand) if len(cand) else {"ref": np.array([]), "alt": np.array([])}
+            ref, alt = cols["ref"], cols["alt"]
             want_ref = None if "?" in mutation.ref else mutation.ref
             keep = [i for j, i in enumerate(cand)
                     if alt[j] == mutation.alt and (want_ref is None or ref[j] == want_ref)]
@@ -1127,7 +1017,7 @@ class PhylogeneticForest:
 
 # ---------------------------------------------------------------- save / load
 FOREST_FORMAT = "process_gb300.phylogenetic_forest"
-FOREST_VERSION = 1
+FOREST_VERSION = 2
 
 
 def _plain(x):
@@ -1159,43 +1049,33 @@ def _driver(d):
     return WGD
 
 
-def _table_digest(t: dict) -> str:
-    import hashlib
-    h = hashlib.sha256()
-    for k in ("locus", "edge", "aux", "cls", "sig", "allele", "kind", "nature"):
-        h.update(np.ascontiguousarray(t[k]).tobytes())
-    return h.hexdigest()
-
-
 def save_phylogenetic_forest(pf: "PhylogeneticForest", filename: str) -> None:
     """``PhylogeneticForest$save`` (src/phylogenetic_forest.cpp:940-955).  The
-    RACES binary archive layout is unavailable, so the file is a versioned
-    native archive (numpy .npz): the engine's configuration, the samples
-    forest, the placement call and a digest of the placed mutations.  Loading
-    places again (placement is a function of these inputs) and checks the
-    digest."""
+    RACES archive layout is unavailable, so the file is a versioned native
+    archive (numpy .npz) holding the library's archive of the placed forest
+    (pg_placed_serialize: placed mutations, genotype classes, allele
+    lineage, CNA events), the samples forest, the engine configuration the
+    forest was placed with and its reference path.  Loading restores the
+    placed tables without placing again."""
     import json
-    e, f = pf.engine, pf.forest
-    args = getattr(pf, "_place_args", None)
-    if args is None:
-        raise DomainError(_lib.PG_ERR_DOMAIN, "this phylogenetic forest was not made by place_mutations")
+    f = pf.forest
+    n = C.c_uint64()
+    check(lib().pg_placed_serialize(pf._h, None, 0, C.byref(n)))
+    blob = np.empty(n.value, dtype=np.uint8)
+    check(lib().pg_placed_serialize(pf._h, ptr(blob, C.c_uint8), n.value, C.byref(n)))
+    e = pf.engine
     meta = {
         "format": FOREST_FORMAT, "version": FOREST_VERSION,
         "genome": {"chr_names": list(e.chr_names), "chr_lengths": [int(x) for x in e.chr_lengths],
                    "seed": int(e.genome.seed), "gc": float(e.genome.gc), "bases": e.genome.bases is not None},
-        "engine": {"context_sampling": e.context_sampling, "max_motif_size": e.max_motif_size,
-                   "max_repetition_storage": e.max_repetition_storage,
-                   "avoid_homozygous_losses": e.avoid_homozygous_losses,
-                   "infinite_sites_model": e.infinite_sites_model,
-                   "SBS_signatures": _plain(e._sigs[0]), "indel_signatures": _plain(e._sigs[1]),
-                   "exposures": _plain(e._exposures), "mutants": _plain(e._mutant_specs),
-                   "passenger_CNAs": _plain(e.passenger_CNAs)},
-        "place": _plain(args),
-        "digest": _table_digest(pf.table()),
+        "engine": getattr(pf, "_config", None) or e._config(),
+        "species_rates": _plain(getattr(pf, "_species_rates", None) or e.get_species_rates()),
+        "place": _plain(getattr(pf, "_place_args", {"seed": pf.seed})),
+        "reference_path": pf.get_reference_path(),
     }
     ancestor = np.where(f.parent >= 0, f.cell_id[np.maximum(f.parent, 0)], -1)
     sample = np.array([f.sample_names[s] if s >= 0 else "" for s in f.sample], dtype=object)
-    arrays = {"meta": np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8),
+    arrays = {"meta": np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8), "placed": blob,
               "cell_id": f.cell_id, "ancestor": ancestor, "mutant": f.mutant.astype(str),
               "epistate": np.array(["" if x is None else str(x) for x in f.epistate]),
               "sample": sample.astype(str), "birth_time": f.birth_time, "divisions": f.divisions}
@@ -1207,8 +1087,9 @@ def save_phylogenetic_forest(pf: "PhylogeneticForest", filename: str) -> None:
 
 def load_phylogenetic_forest(filename: str, quiet: bool = False) -> "PhylogeneticForest":
     """``load_phylogenetic_forest(filename, quiet)`` (src/mutations.cpp:1466-1480):
-    rebuilds the engine and the samples forest of a saved file, places the
-    mutations again and checks them against the saved digest."""
+    rebuilds the engine (genome, signatures, the configuration the forest was
+    placed with) and the samples forest of a saved file, and restores the
+    placed forest from its archive (pg_placed_deserialize)."""
     import json
     import os
     if not os.path.exists(filename):
@@ -1238,9 +1119,14 @@ def load_phylogenetic_forest(filename: str, quiet: bool = False) -> "Phylogeneti
         sample = np.array([s if s != "" else None for s in z["sample"]], dtype=object)
         forest = SamplesForest(z["cell_id"], z["ancestor"], z["mutant"].astype(object),
                                z["epistate"].astype(object), sample, z["birth_time"], z["divisions"])
-    pf = eng.place_mutations(forest, **meta["place"])
-    if _table_digest(pf.table()) != meta["digest"]:
-        raise _lib.ProcessError(_lib.PG_ERR_RUNTIME, f'"{filename}": the placed mutations differ from the saved ones')
+        blob = np.ascontiguousarray(z["placed"], dtype=np.uint8)
+    ph = C.c_void_p()
+    check(lib().pg_placed_deserialize(eng._h, ptr(blob, C.c_uint8), len(blob), C.byref(ph)))
+    pf = PhylogeneticForest(eng, forest, ph, int(meta["place"].get("seed", 0)))
+    pf._place_args = meta["place"]
+    pf._config = em
+    pf._species_rates = meta.get("species_rates")
+    pf._reference_path = meta.get("reference_path", "")
     return pf
 
 
@@ -1502,86 +1388,73 @@ def _sequencer_rate(sequencer) -> tuple[float, dict | None]:
     raise DomainError(_lib.PG_ERR_DOMAIN, "Unsupported sequencer type")
 
 
-def _result_frame(pf: PhylogeneticForest, idx: np.ndarray, alt: np.ndarray, dep: np.ndarray,
+def _sid_strings(buf: np.ndarray, n: int) -> np.ndarray:
+    """Strings of a buffer of n NUL-padded SID_CHARS-byte fields."""
+    if n == 0:
+        return np.zeros(0, dtype=object)
+    return buf.reshape(n, _lib.SID_CHARS).view(f"S{_lib.SID_CHARS}").ravel().astype(str).astype(object)
+
+
+def _cbuf(arr: np.ndarray):
+    return arr.ctypes.data_as(C.c_char_p)
+
+
+_CLASS_NAMES = None
+
+
+def _class_names() -> np.ndarray:
+    """Joined nature names of every bit set of natures (sorted names, ';')."""
+    global _CLASS_NAMES
+    if _CLASS_NAMES is None:
+        out = []
+        for m in range(16):
+            out.append(";".join(sorted(str(NATURES[b]) for b in range(4) if m >> b & 1)))
+        _CLASS_NAMES = np.array(out, dtype=object)
+    return _CLASS_NAMES
+
+
+def _result_frame(res: "SeqResult", pf: PhylogeneticForest, include_non_sequenced: bool,
                   sample_names: list[str]) -> dict:
-    """The wide data frame of get_result_dataframe (src/seq_simulation.cpp:142-181)
-    over the rows idx (mutation indices, ascending; alt / dep are their
-    [sample][row] tables), merged by (chr, pos, ref, alt) in the order of
-    each SID's first row: occurrences add, the coverage is the first row's,
-    causes and classes are the sorted unions."""
-    t = pf.table()
-    idx = np.asarray(idx, dtype=np.int64)
-    ref, altb = pf._ref_alt(t, idx)
-    cause = pf._cause(t, idx)
-    nat = NATURES[t["nature"][idx]]
-    loc = t["locus"][idx].astype(np.int64)
-    n = len(idx)
-    # group the rows by SID: a stable sort on (locus, ref, alt) keeps each
-    # group's rows in index order
-    _, rc = np.unique(ref.astype(str), return_inverse=True) if n else (None, np.zeros(0, np.int64))
-    _, ac = np.unique(altb.astype(str), return_inverse=True) if n else (None, np.zeros(0, np.int64))
-    order = np.lexsort((ac, rc, loc))
-    if n:
-        ks = np.stack([loc[order], rc[order], ac[order]], axis=1)
-        new = np.ones(n, dtype=bool)
-        new[1:] = np.any(ks[1:] != ks[:-1], axis=1)
-    else:
-        new = np.zeros(0, dtype=bool)
-    gsorted = np.cumsum(new) - 1                     # group of each sorted row
-    first_sorted = order[new]                        # each group's first row (smallest index)
-    gorder = np.argsort(first_sorted, kind="stable")  # groups in the order of their first row
-    rank = np.empty(len(gorder), dtype=np.int64)
-    rank[gorder] = np.arange(len(gorder))
-    group = np.empty(n, dtype=np.int64)
-    group[order] = rank[gsorted]                     # output row of every input row
-    first = first_sorted[gorder]
-    ng = len(first)
-    sizes = np.bincount(group, minlength=ng)
-    chrn, pos = pf._chr_pos(loc[first] if ng else loc[:0])
-    causes = cause[first].copy()
-    classes = nat[first].astype(object)
-    for g in np.nonzero(sizes > 1)[0]:
-        members = np.nonzero(group == g)[0]
-        causes[g] = ";".join(sorted({c for c in cause[members] if c is not None})) or None
-        classes[g] = ";".join(sorted(set(nat[members])))
-    df = {"chr": chrn, "chr_pos": pos, "ref": ref[first], "alt": altb[first], "causes": causes, "classes": classes}
+    """The wide data frame of get_result_dataframe (src/seq_simulation.cpp:52-181),
+    built by the library (pg_seq_result_frame): one row per SID in
+    (chromosome, position, ref, alt) order, occurrences summed over the
+    SID's mutations, the coverage of its locus, causes and classes as the
+    sorted unions joined by ';'."""
+    n = C.c_uint64()
+    check(lib().pg_seq_result_frame(res._h, pf._h, 1 if include_non_sequenced else 0, C.byref(n)))
+    R = n.value
+    nc = C.c_uint64()
+    check(lib().pg_seq_result_frame_causes_size(res._h, C.byref(nc)))
+    S = res.dims()[0]
+    chr_, pos = np.empty(R, np.uint32), np.empty(R, np.uint32)
+    ref, alt = np.zeros(R * _lib.SID_CHARS, np.uint8), np.zeros(R * _lib.SID_CHARS, np.uint8)
+    coff = np.zeros(R + 1, np.uint64)
+    cb = np.zeros(max(nc.value, 1), np.uint8)
+    classes = np.zeros(R, np.uint8)
+    occ, cov = np.empty((S, R), np.int32), np.empty((S, R), np.int32)
+    vaf = np.empty((S, R), np.float64)
+    check(lib().pg_seq_result_frame_copy(res._h, ptr(chr_, C.c_uint32), ptr(pos, C.c_uint32), _cbuf(ref), _cbuf(alt),
+                                         ptr(coff, C.c_uint64), _cbuf(cb), ptr(classes, C.c_uint8),
+                                         ptr(occ, C.c_int32), ptr(cov, C.c_int32), ptr(vaf, C.c_double)))
+    # causes: the joined strings into fixed-width fields, empty ones NA (None)
+    lens = np.diff(coff).astype(np.int64)
+    width = int(lens.max()) if R else 0
+    causes = np.full(R, None, dtype=object)
+    if width:
+        grid = np.zeros((R, width), np.uint8)
+        rows = np.repeat(np.arange(R), lens)
+        cols = np.arange(int(lens.sum())) - np.repeat(coff[:-1].astype(np.int64), lens)
+        grid[rows, cols] = cb[:int(lens.sum())]
+        txt = grid.view(f"S{width}").ravel().astype(str).astype(object)
+        causes[lens > 0] = txt[lens > 0]
+    names = np.array(pf.engine.chr_names, dtype=object)
+    df = {"chr": names[chr_], "chr_pos": pos.astype(np.int64), "ref": _sid_strings(ref, R),
+          "alt": _sid_strings(alt, R), "causes": causes, "classes": _class_names()[classes & 15]}
     for s, name in enumerate(sample_names):
-        occ = np.bincount(group, weights=alt[s], minlength=ng).astype(np.int32) if n else np.zeros(0, np.int32)
-        cov = dep[s, first].astype(np.int32)
-        with np.errstate(divide="ignore", invalid="ignore"):
-            vaf = np.where(cov > 0, occ / np.maximum(cov, 1), 0.0)
-        df[f"{name}.occurrences"] = occ
-        df[f"{name}.coverage"] = cov
-        df[f"{name}.VAF"] = vaf
+        df[f"{name}.occurrences"] = occ[s]
+        df[f"{name}.coverage"] = cov[s]
+        df[f"{name}.VAF"] = vaf[s]
     return df
-
-
-def _result_rows(res: "SeqResult", include_non_sequenced: bool, present: np.ndarray):
-    """Rows of the result frame: the observed rows compacted on the device,
-    or (include_non_sequenced_mutations) those plus every mutation present
-    in a sequenced sample's cells, from the full tables."""
-    if not include_non_sequenced:
-        return res.observed()
-    alt, dep = res.counts()
-    idx = np.nonzero((alt.sum(axis=0) > 0) | present)[0]
-    return idx, alt[:, idx], dep[:, idx]
-
-
-def _presence(pf: PhylogeneticForest, n_samples_seq: int, with_normal: bool, pre_in_normal: bool) -> np.ndarray:
-    """Mutations present in the cells of some sequenced sample."""
-    f = pf.forest
-    t = pf.table()
-    n = f.num_of_nodes
-    tin, tout = f.euler()
-    leaf_tins = np.sort(tin[f.is_leaf & (f.sample >= 0)])
-    e = t["edge"].astype(np.int64)
-    real = e < n
-    present = np.zeros(len(e), dtype=bool)
-    lo = np.searchsorted(leaf_tins, tin[np.minimum(e, n - 1)], side="left")
-    hi = np.searchsorted(leaf_tins, tout[np.minimum(e, n - 1)], side="left")
-    present[real] = (hi > lo)[real]
-    present[~real] = True
-    return present
 
 
 class SampledCell:
@@ -1683,9 +1556,7 @@ def simulate_seq(phylo_forest: PhylogeneticForest, sequencer=None, reference_gen
             base = _forest_partition(phylo_forest)
             check(lib().pg_placed_set_samples(phylo_forest._h, len(phylo_forest.forest.sample_names),
                                               ptr(base, C.c_int32)))
-    present = (_presence(phylo_forest, len(names), with_normal_sample, preneoplastic_in_normal)
-               if include_non_sequenced_mutations else None)
-    df = _result_frame(phylo_forest, *_result_rows(res, include_non_sequenced_mutations, present), names)
+    df = _result_frame(res, phylo_forest, include_non_sequenced_mutations, names)
     params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
               "coverage": coverage, "read_size": read_size, "insert_size_mean": insert_size_mean,
               "insert_size_stddev": insert_size_stddev, "output_dir": output_dir, "write_SAM": write_SAM,
@@ -1712,9 +1583,7 @@ def simulate_normal_seq(phylo_forest: PhylogeneticForest, sequencer=None, refere
                           insert_size_mean=insert_size_mean, insert_size_stddev=insert_size_stddev, error_rate=err,
                           purity=1.0, with_normal_sample=True, preneoplastic_in_normal=with_preneoplastic,
                           normal_only=True, chromosomes=chromosomes, tile_size=tile_size, insert_model=insert_model)
-    t = phylo_forest.table()
-    present = (t["edge"] == phylo_forest.forest.num_of_nodes) & bool(with_preneoplastic)
-    df = _result_frame(phylo_forest, *_result_rows(res, include_non_sequenced_mutations, present), ["normal_sample"])
+    df = _result_frame(res, phylo_forest, include_non_sequenced_mutations, ["normal_sample"])
     params = {"sequencer": seq_data, "reference_genome": reference_genome, "chromosomes": chromosomes,
               "coverage": coverage, "read_size": read_size, "insert_size_mean": insert_size_mean,
               "insert_size_stddev": insert_size_stddev, "output_dir": output_dir, "write_SAM": write_SAM,

@@ -205,45 +205,59 @@ def test_cna_distribution_against_reference_engine(gpu_lib, orc):
 
 
 def test_cell_mutations_follow_allele_copies(gpu_lib, orc):
-    """get_sampled_cell_mutations with copy-number events: in every sampled
-    cell, each mutation on its root path once per allele instance of the
-    cell's genome at the locus that carries it.  The expectation is built
-    from the oracle's own restatement: its class pieces (instances present
-    per position) and its carrier closure over the copies."""
+    """get_sampled_cell_mutations with copy-number events (built in C++ by
+    pg_placed_cell_mutations): in every sampled cell, each mutation on its
+    root path once per allele instance of the cell's genome at the locus that
+    carries it, rows by chromosome, allele, position.  The expectation comes
+    from the oracle alone: the root path by walking the forest's parents, its
+    class pieces (instances present per position) and its carrier closure
+    over the copies."""
     w, cands = _workload(seed=5, n_leaves=300)
     eng, o = _pair(orc, w, cands, True, True)
     f = w.forest
     pf = eng.place_mutations(f, 60, 6, seed=9)
     op = o.place(f, _species(o, f), 60, 0, 6, 0, seed=9)
     _tables_equal(pf.table(), op.table())
-    t = pf.table()
+    ot = op.table()
     off, lst = op.carriers()
     ocls, n_cls, _ = op.node_classes(f.num_of_nodes)
     assert n_cls > 3
+    n = f.num_of_nodes
     leaves = np.nonzero(f.is_leaf & (f.sample >= 0))[0]
     picked = {}
     for lf in leaves:                                  # one leaf per genotype class
         picked.setdefault(int(ocls[lf]), int(lf))
     pieces = {c: op.class_pieces(c) for c in picked}
+    chr_off = np.concatenate([[0], np.cumsum(np.asarray(w.genome.chr_lengths, dtype=np.int64))])
     copies = lost = 0
     for c, lf in picked.items():
-        rows, alle = pf._cell_rows(lf)
-        got = set(zip(rows.tolist(), alle.tolist()))
+        cell, rows, alle = pf.cell_mutation_rows(int(f.cell_id[lf]))
+        assert (cell == lf).all()
+        got = list(zip(rows.tolist(), alle.tolist()))
+        path = set()
+        v = lf
+        while v >= 0:
+            path.add(v)
+            v = int(f.parent[v])
         inst, b, e = pieces[c]
-        want = set()
-        on_path = np.nonzero(pf.leaf_carriers(lf))[0]
-        for m in on_path:
-            L = int(t["locus"][m])
+        want = []
+        for m in range(len(ot["locus"])):
+            if int(ot["edge"][m]) < n and int(ot["edge"][m]) not in path:
+                continue
+            L = int(ot["locus"][m])
             present = set(inst[(b <= L) & (L < e)].tolist())
             car = [int(y) for y in lst[off[m]:off[m + 1]] if int(y) in present]
-            want.update((int(m), y) for y in car)
+            want.extend((m, y) for y in car)
             copies += len(car) > 1
             lost += len(car) == 0
-        assert got == want, (c, len(got ^ want))
+        key = lambda my: (int(np.searchsorted(chr_off, ot["locus"][my[0]], side="right")), my[1],
+                          int(ot["locus"][my[0]]), my[0])
+        assert got == sorted(want, key=key), (c, len(set(got) ^ set(want)))
     assert copies > 0 and lost > 0                     # amplified and deleted mutations both occur
-    # the data frame of one cell matches its rows
+    # the data frame of one cell: its rows, with their alleles, in that order
     lf = next(iter(picked.values()))
     df = pf.get_sampled_cell_mutations(int(f.cell_id[lf]))
-    rows, alle = pf._cell_rows(lf)
+    _, rows, alle = pf.cell_mutation_rows(int(f.cell_id[lf]))
     np.testing.assert_array_equal(df["allele"], alle)
-    assert len(df["chr"]) == len(rows)
+    np.testing.assert_array_equal(df["chr_pos"], ot["locus"][rows].astype(np.int64) + 1
+                                  - chr_off[np.searchsorted(chr_off, ot["locus"][rows], side="right") - 1])

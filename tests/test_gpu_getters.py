@@ -51,9 +51,9 @@ def test_first_occurrences(gpu_lib):
     t = pf.table()
     # a passenger SNV: the cell at the end of its edge
     i = int(np.nonzero((t["kind"] == 0) & (t["nature"] == 0))[0][0])
-    ref, alt = pf._ref_alt(t, np.array([i]))
-    chrn, pos = pf._chr_pos(t["locus"][[i]])
-    cells = pf.get_first_occurrences(Mutation(str(chrn[0]), int(pos[0]), str(ref[0]), str(alt[0])))
+    cols = pf.mutation_columns(np.array([i]))
+    cells = pf.get_first_occurrences(Mutation(str(cols["chr"][0]), int(cols["chr_pos"][0]), str(cols["ref"][0]),
+                                              str(cols["alt"][0])))
     assert int(f.cell_id[t["edge"][i]]) in cells
     # the driver SNV and the driver amplification: the first cell of the mutant's first edge
     c = pf.cna_table()
@@ -64,3 +64,37 @@ def test_first_occurrences(gpu_lib):
     assert cells == sorted({int(f.cell_id[v]) for v in t["edge"][drv]})
     with pytest.raises(DomainError, match="does not occurs"):
         pf.get_first_occurrences(Mutation("1", 7, "A", "C"))
+
+
+def test_signatures_from_table(gpu_lib, tmp_path):
+    """An engine given the signatures as tables in the reference's format
+    (pg_engine_load_signatures_tsv, and through set_signatures with a path)
+    places exactly what the engine given the same probabilities does, and
+    reports the table's names."""
+    import ctypes as C
+
+    from process_gb300 import ID_CLASSES, SBS_CLASSES, _lib, synth
+    w = synth.plain_3mbp(seed=21, n_leaves=120)
+    w.genome.chr_lengths = [100_000, 50_000, 50_000]
+    paths = []
+    for labels, sigs, name in ((SBS_CLASSES, w.sbs, "sbs.tsv"), (ID_CLASSES, w.ids, "id.tsv")):
+        p = tmp_path / name
+        with open(p, "w") as fh:
+            fh.write("\t".join(["Type"] + list(sigs)) + "\n")
+            for i in np.random.default_rng(0).permutation(len(labels)):
+                fh.write("\t".join([labels[i]] + [repr(float(sigs[k][i])) for k in sigs]) + "\n")
+        paths.append(p)
+    a = synth.build_engine(w)
+    w2 = synth.plain_3mbp(seed=21, n_leaves=120)
+    w2.genome.chr_lengths = [100_000, 50_000, 50_000]
+    w2.sbs, w2.ids = str(paths[0]), str(paths[1])
+    b = synth.build_engine(w2)
+    ta = a.place_mutations(w.forest, 30, 3, seed=4).table()
+    tb = b.place_mutations(w.forest, 30, 3, seed=4).table()
+    for k in ta:
+        np.testing.assert_array_equal(ta[k], tb[k], err_msg=k)
+    # the C entry point directly, and the names it keeps
+    _lib.check(_lib.lib().pg_engine_load_signatures_tsv(a._h, 1, str(paths[1]).encode()))
+    buf, n = C.create_string_buffer(64), C.c_uint32()
+    _lib.check(_lib.lib().pg_engine_signature_name(a._h, 1, 0, buf, 64, C.byref(n)))
+    assert buf.value.decode() == list(w.ids)[0]

@@ -1,13 +1,24 @@
-"""PhylogeneticForest save / load (versioned native archive): a loaded forest
-places the same mutations (digest-checked) and sequences identically."""
+"""PhylogeneticForest save / load (versioned native archive of the placed
+forest, pg_placed_serialize / pg_placed_deserialize): a loaded forest holds
+the same tables and getters without placing again, and sequences
+identically; SAM-free I/O helpers."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
+def _frames_equal(a, b):
+    assert set(a) == set(b)
+    for k in a:
+        assert np.asarray(a[k]).tolist() == np.asarray(b[k]).tolist(), k
+
+
 def test_save_load_round_trip(gpu_lib, tmp_path):
-    from process_gb300 import CNA, SNV, WGD, load_phylogenetic_forest, synth
+    from process_gb300 import CNA, SNV, WGD, DomainError, GenomeSpec, MutationEngine, load_phylogenetic_forest, synth
+    from process_gb300 import _lib
     from process_gb300.engine import sequence_counts
     w = synth.plain_3mbp(seed=4, n_leaves=150)
     w.genome.chr_lengths = [200_000, 100_000, 100_000]
@@ -18,6 +29,10 @@ def test_save_load_round_trip(gpu_lib, tmp_path):
     eng.add_passenger_CNAs([CNA("D", "3", 1001, 5000)])
     eng.infinite_sites_model = False
     pf = eng.place_mutations(w.forest, 20, 3, seed=11)
+    pf.set_reference_path("/data/genome.fa")
+    expo = pf.get_exposures()
+    # the engine changes after placement: the forest keeps what it was placed with
+    eng.add_exposure(5.0, {"SBS1": 1.0})
     path = tmp_path / "phylo_forest.sff"
     pf.save(str(path))
     pf2 = load_phylogenetic_forest(str(path))
@@ -27,6 +42,13 @@ def test_save_load_round_trip(gpu_lib, tmp_path):
     np.testing.assert_array_equal(pf2.forest.cell_id, pf.forest.cell_id)
     assert pf2.forest.sample_names == pf.forest.sample_names
     assert not pf2.engine.infinite_sites_model
+    assert pf2.get_reference_path() == "/data/genome.fa"
+    _frames_equal(pf2.get_exposures(), expo)
+    _frames_equal(pf.get_exposures(), expo)
+    for getter in ("get_sampled_cell_mutations", "get_sampled_cell_CNAs", "get_cell_allelic_fragmentation",
+                   "get_bulk_allelic_fragmentation", "get_samples_info", "get_driver_mutations", "get_species_info"):
+        _frames_equal(getattr(pf2, getter)(), getattr(pf, getter)())
+    np.testing.assert_array_equal(pf2.node_classes()[0], pf.node_classes()[0])
     cfg = dict(coverage=10, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=1e-3)
     a1, d1 = sequence_counts(pf, 5, **cfg).counts()
     a2, d2 = sequence_counts(pf2, 5, **cfg).counts()
@@ -35,6 +57,21 @@ def test_save_load_round_trip(gpu_lib, tmp_path):
     c1, c2 = pf.cna_table(), pf2.cna_table()
     for k in c1:
         np.testing.assert_array_equal(c1[k], c2[k], err_msg=k)
+    # the archive refuses an engine with another genome, and a truncated buffer
+    n = C.c_uint64()
+    _lib.check(_lib.lib().pg_placed_serialize(pf._h, None, 0, C.byref(n)))
+    blob = np.empty(n.value, dtype=np.uint8)
+    _lib.check(_lib.lib().pg_placed_serialize(pf._h, _lib.ptr(blob, C.c_uint8), n.value, C.byref(n)))
+    other = MutationEngine(GenomeSpec(["1", "2", "3"], [200_000, 100_000, 100_000], seed=99), w.sbs, w.ids)
+    h = C.c_void_p()
+    assert _lib.lib().pg_placed_deserialize(other._h, _lib.ptr(blob, C.c_uint8), n.value, C.byref(h)) == \
+        _lib.PG_ERR_DOMAIN
+    assert b"another reference genome" in _lib.lib().pg_last_error()
+    assert _lib.lib().pg_placed_deserialize(eng._h, _lib.ptr(blob, C.c_uint8), n.value // 2, C.byref(h)) == \
+        _lib.PG_ERR_DOMAIN
+    assert b"truncated" in _lib.lib().pg_last_error()
+    with pytest.raises(DomainError):
+        _lib.check(_lib.lib().pg_placed_load(eng._h, str(tmp_path / "none.pgpf").encode(), C.byref(h)))
 
 
 def test_counts_into_page_locked_buffers(gpu_lib):
@@ -104,8 +141,9 @@ def test_observed_rows(gpu_lib):
 
 
 def _naive_frame(pf, alt, dep, names):
-    """The result frame built row by row (the definition the vectorised
-    builder must match): SIDs (locus, ref, alt) in order of first row."""
+    """The result frame built row by row (the definition the library's
+    builder must match): SIDs (locus, ref, alt) in the reference's map order
+    (src/seq_simulation.cpp:52-181)."""
     from process_gb300.engine import BASES, NATURES
     t = pf.table()
     eng = pf.engine
@@ -129,17 +167,22 @@ def _naive_frame(pf, alt, dep, names):
             groups[key] = []
             order.append(key)
         groups[key].append(i)
+    order = sorted(order)
     out = {"ref": [k[1] for k in order], "alt": [k[2] for k in order], "locus": [k[0] for k in order]}
     for s, name in enumerate(names):
         out[f"{name}.occurrences"] = [int(alt[s, groups[k]].sum()) for k in order]
         out[f"{name}.coverage"] = [int(dep[s, groups[k][0]]) for k in order]
     out["classes"] = [";".join(sorted(set(NATURES[t["nature"][groups[k]]]))) for k in order]
+    sig = [list(eng.sig_names[0]), list(eng.sig_names[1])]
+    out["causes"] = [";".join(sorted({sig[int(t["kind"][i])][int(t["sig"][i])] for i in groups[k]
+                                      if int(t["sig"][i]) < len(sig[int(t["kind"][i])])})) or None for k in order]
     return out
 
 
 def test_result_frame_matches_row_by_row(gpu_lib):
-    """The vectorised result frame equals the row-by-row definition, with
-    indels and (infinite sites off) several SIDs on one locus."""
+    """The library's result frame (pg_seq_result_frame) equals the
+    row-by-row definition, with indels and (infinite sites off) several SIDs
+    on one locus."""
     from process_gb300 import synth
     from process_gb300.engine import _result_frame, sequence_counts
     w = synth.plain_3mbp(seed=14, n_leaves=150)
@@ -154,7 +197,7 @@ def test_result_frame_matches_row_by_row(gpu_lib):
                         error_rate=1e-3, purity=0.9)
     a, d = r.counts()
     names = [f"s{q}" for q in range(a.shape[0])]
-    df = _result_frame(pf, *r.observed(), names)
+    df = _result_frame(r, pf, False, names)
     ref = _naive_frame(pf, a, d, names)
     assert list(df["ref"]) == ref["ref"] and list(df["alt"]) == ref["alt"]
     assert (t["kind"][np.nonzero(a.sum(axis=0) > 0)[0]] == 1).any()   # some indels observed
@@ -162,6 +205,7 @@ def test_result_frame_matches_row_by_row(gpu_lib):
     loc = np.array([off[eng.chr_names.index(c)] for c in df["chr"]]) + df["chr_pos"] - 1
     assert loc.tolist() == ref["locus"]
     assert list(df["classes"]) == ref["classes"]
+    assert list(df["causes"]) == ref["causes"]
     for name in names:
         assert df[f"{name}.occurrences"].tolist() == ref[f"{name}.occurrences"]
         assert df[f"{name}.coverage"].tolist() == ref[f"{name}.coverage"]
