@@ -68,6 +68,22 @@ typedef struct {
   double synthetic_gc;              /* GC fraction of the synthetic genome */
   uint32_t context_sampling;        /* keep 1 in N occurrences per context (reference default 100) */
   uint32_t max_repetition_storage;  /* positions kept per ID class (reference default 500000) */
+  /* Regions to avoid: positions the SBS context index leaves out, as
+   * build_contex_index does for the driver catalogue (each driver's position
+   * and max(1, |ref|) bases; src/mutation_engine.cpp:240-250, 260); the ID
+   * index keeps them (:323-334).  n_avoid 0: none. */
+  uint32_t n_avoid;
+  const uint32_t* avoid_chr;        /* chromosome index */
+  const uint32_t* avoid_begin;      /* 1-based first position */
+  const uint32_t* avoid_len;        /* bases, at least 1 */
+  /* Directory of the index caches (the reference's .cif / .rsif files,
+   * :199-209, 225-238, 277-318), or NULL / "": no cache.  The context index is
+   * kept as context_index_<context_sampling>.pgcif and the ID index as
+   * rs_index_<max_repetition_storage>.pgrsif, each with a format version, a
+   * fingerprint of the genome and (context index) of the regions to avoid.
+   * An existing file is loaded instead of building the index; a file of
+   * another version, genome or regions is refused with PG_ERR_DOMAIN. */
+  const char* index_cache_dir;
 } pg_genome_desc;
 
 pg_status pg_engine_create(const pg_genome_desc* genome, pg_engine** out);

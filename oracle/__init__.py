@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
             "orc_genome_synth": (None, [C.c_uint64, C.c_uint64, C.c_double, u8p]),
             "orc_engine_create": (P, [C.c_uint32, u32p, u8p, C.c_uint64, C.c_double, C.c_uint32, C.c_uint32]),
             "orc_engine_destroy": (None, [P]),
+            "orc_engine_set_avoid": (None, [P, C.c_uint32, u32p, u32p, u32p]),
             "orc_engine_index_info": (None, [P, u64p, u64p, u32p, u32p]),
             "orc_engine_read_index": (None, [P, C.c_int, C.c_uint32, u32p]),
             "orc_engine_read_genome": (None, [P, u8p]),
@@ -76,6 +77,7 @@ def lib() -> C.CDLL:
             "orc_placed_set": (C.c_int, [P, C.c_uint64, u32p, u32p, u16p, u8p]),
             "orc_seq": (P, [P, C.c_void_p, C.c_uint64, C.c_int, C.c_double, C.c_int]),
             "orc_seq_destroy": (None, [P]),
+            "orc_sam": (C.c_int, [P, C.c_void_p, C.c_uint64, C.c_char_p]),
             "orc_seq_samples": (C.c_uint32, [P]),
             "orc_seq_reads": (C.c_uint64, [P]),
             "orc_seq_copy": (None, [P, i32p, i32p]),
@@ -213,6 +215,13 @@ class OracleEngine:
             else:
                 self.add_driver_wgd(mutant)
 
+    def set_regions_to_avoid(self, regions, chr_index):
+        """(chromosome, 1-based begin, length) triples; rebuilds the indices."""
+        c = np.ascontiguousarray([chr_index(r[0]) for r in regions], dtype=np.uint32)
+        b = np.ascontiguousarray([r[1] for r in regions], dtype=np.uint32)
+        n = np.ascontiguousarray([r[2] for r in regions], dtype=np.uint32)
+        lib().orc_engine_set_avoid(self._h, len(c), _p(c, C.c_uint32), _p(b, C.c_uint32), _p(n, C.c_uint32))
+
     def index_info(self):
         ct, it = np.zeros(32, np.uint64), np.zeros(83, np.uint64)
         cl, il = np.zeros(32, np.uint32), np.zeros(83, np.uint32)
@@ -305,6 +314,18 @@ class OraclePlaced:
         if lib().orc_placed_set(self._h, len(arrs[0]), _p(arrs[0], C.c_uint32), _p(arrs[1], C.c_uint32),
                                 _p(arrs[2], C.c_uint16), _p(arrs[3], C.c_uint8)):
             raise RuntimeError(_err())
+
+    def sam_reads(self, cfg, seed, path) -> dict:
+        """The replay's SAM reads: {(sample, chromosome index): [(FLAG, POS,
+        CIGAR, mate POS, TLEN, SEQ), ...]} in file order (all strings)."""
+        if lib().orc_sam(self._h, C.addressof(cfg), int(seed), str(path).encode()):
+            raise RuntimeError(_err())
+        out = {}
+        with open(path) as fh:
+            for line in fh:
+                f = line.rstrip("\n").split("\t")
+                out.setdefault((int(f[0]), int(f[1])), []).append(tuple(f[2:8]))
+        return out
 
     def sequence(self, cfg, seed, flavour=0, fraction=1.0, threads=1):
         """cfg: a process_gb300._lib.SeqCfg (same layout as the oracle's)."""

@@ -30,6 +30,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <fstream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <random>
@@ -331,8 +333,14 @@ struct Engine {
   std::vector<Cna> cands;                 // passenger CNA candidates
   bool infinite_sites = true;
   bool avoid_losses = true;
+  std::vector<uint8_t> avoid;             // positions the SBS context index leaves out (empty: none)
 };
 
+// ContextIndex::build_index(ref, regions_to_avoid, sampling) and
+// RSIndex::build_index (src/mutation_engine.cpp:260, 344): every position
+// with its trinucleotide context (not inside a region to avoid) and its ID
+// classes, then 1 in `context_sampling` / enough to keep at most max_rep per
+// class, in position order
 void build_index(Engine& e) {
   const uint64_t G = e.g.b.size();
   std::vector<std::vector<uint32_t>> all_ctx(32), all_id(83);
@@ -340,7 +348,8 @@ void build_index(Engine& e) {
     const uint32_t c = e.g.chr_of(uint32_t(p));
     const uint32_t cs = e.g.off[c], ce = e.g.off[c + 1];
     // a context with an unknown base (code 4, N) is not indexed
-    if (p > cs && p + 1 < ce && e.g.b[p - 1] < 4 && e.g.b[p] < 4 && e.g.b[p + 1] < 4)
+    const bool avoided = !e.avoid.empty() && e.avoid[p];
+    if (!avoided && p > cs && p + 1 < ce && e.g.b[p - 1] < 4 && e.g.b[p] < 4 && e.g.b[p + 1] < 4)
       all_ctx[context_of(e.g.b[p - 1], e.g.b[p], e.g.b[p + 1])].push_back(uint32_t(p));
     int cl[16];
     id_classes(e.g, uint32_t(p), cl);
@@ -1164,7 +1173,13 @@ void copies_in(const CellGenome& g, uint32_t a, uint32_t b, uint64_t& sum, uint3
 }
 
 // ---- flavour 0: replay of the tiled read generation
-void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
+// called once per fragment of the replay, in draw order: sample, chromosome,
+// dropped (no DNA under the draw), mate starts, cell (node id, -1 normal),
+// allele instance and the fragment's error word
+using FragmentVisitor = std::function<void(uint32_t smp, uint32_t ci, bool dropped, uint32_t p0, uint32_t p1,
+                                           int64_t cell, uint32_t allele, uint32_t fw)>;
+
+void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out, const FragmentVisitor* visit = nullptr) {
   const Engine& e = *pl.eng;
   const Forest& f = *pl.forest;
   const SeqSetup s = seq_setup(pl, c);
@@ -1340,7 +1355,10 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
             const uint32_t o = lookup(q.opt_thr[pt.atom].data(), uint32_t(q.opts.size()), r.v[1]);
             const Opt& op = q.opts[o];
             const auto& cov = pl.atom_cov[pt.atom][op.cls];
-            if (cov.empty()) continue;     // an option without DNA here is never drawn
+            if (cov.empty()) {             // an option without DNA here is never drawn
+              if (visit) (*visit)(smp, ci, true, p0, p0, -1, 0, 0);
+              continue;
+            }
             const uint32_t n_cov = uint32_t(cov.size());
             allele = cov[mulhi32(r.v[3], n_cov)];
             cell = op.leaves.empty() ? -1
@@ -1348,17 +1366,101 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out) {
           }
           const uint32_t fw = r.v[0] ^ r.v[1] ^ r.v[2] ^ r.v[3];
           count_mate(pl, car, carriers, p0, s.R, cell, allele, s.err_thr, 0, fw, alt, dep);
+          uint32_t p1 = p0;
           if (s.paired) {
             const uint32_t ins = s.ins_min + lookup(s.ins_thr.data(), uint32_t(s.ins_thr.size()), r.v[2]);
-            uint32_t p1 = p0 + ins - s.R;
+            p1 = p0 + ins - s.R;
             if (p1 > ce - s.R) p1 = ce - s.R;
             count_mate(pl, car, carriers, p1, s.R, cell, allele, s.err_thr, 1, fw, alt, dep);
           }
+          if (visit) (*visit)(smp, ci, false, p0, p1, cell, allele, fw);
         }
       }
     }
     tile_base += nt;
   }
+}
+
+// ---- SAM reads of the replay (simulate_seq with write_SAM, the reads of
+// src/seq_simulation.cpp:540-564).  A mate starting at reference position p
+// shows, position by position, the reference base, or the alt base of an SNV
+// its allele carries (the first such record at the position), or a
+// substitution where the visit's error word is below the error threshold:
+// one of the three other bases, chosen by word % 3 among them in the order
+// (counterpart allele first at an SNV site -- the alt base when the read
+// shows the reference, the reference base when it shows the alt --, then
+// the rest ascending).  Unknown reference bases read N.  After the anchor of
+// an indel its allele carries (the first such record), an insertion adds its
+// bases (each with its own error word: the fragment word mixed with the
+// base's rank) and a deletion skips its bases; indels anchored before p are
+// not applied, and none once the CIGAR would pass 16 operations.  The read
+// stops after R bases or at the chromosome end.
+struct OracleRead { std::vector<std::pair<char, uint32_t>> cigar; std::string seq; };
+
+uint32_t other_base(uint32_t tb, int first, uint32_t k) {
+  std::vector<uint32_t> o;
+  if (first >= 0 && uint32_t(first) != tb) o.push_back(uint32_t(first));
+  for (uint32_t x = 0; x < 4; ++x)
+    if (x != tb && (o.empty() || x != o[0])) o.push_back(x);
+  return o[k];
+}
+
+OracleRead oracle_read(const Placed& pl, const Carrier& car, const std::vector<std::vector<uint32_t>>& carriers,
+                       const std::vector<uint32_t>& aux, uint32_t p, uint32_t ce, int64_t cell, uint32_t allele,
+                       uint32_t fw, uint32_t mate, uint32_t R, uint32_t err_thr) {
+  const Genome& g = pl.eng->g;
+  const char* ACGT = "ACGT";
+  const size_t kMaxCigar = 16;
+  OracleRead out;
+  auto push = [&](char op, uint32_t len) {
+    if (!out.cigar.empty() && out.cigar.back().first == op) { out.cigar.back().second += len; return; }
+    if (out.cigar.size() < kMaxCigar) out.cigar.push_back({op, len});
+  };
+  auto is_carried = [&](size_t i) {
+    const auto& cs = carriers[i];
+    return car.ancestor_or_self(pl.edge[i], cell) && std::find(cs.begin(), cs.end(), allele) != cs.end();
+  };
+  bool indels_open = true;
+  uint32_t q = p;
+  while (out.seq.size() < R && q < ce) {
+    const uint32_t b = g.b[q];
+    bool site = false, carried_snv = false, has_indel = false;
+    uint32_t alt = 0, indel = 0;
+    auto it = std::lower_bound(pl.locus.begin(), pl.locus.end(), q);
+    for (size_t i = size_t(it - pl.locus.begin()); i < pl.locus.size() && pl.locus[i] == q; ++i) {
+      if (pl.kind[i] == 0) {
+        if (!site) { site = true; alt = aux[i] & 3u; }
+        if (!carried_snv && is_carried(i)) { carried_snv = true; alt = aux[i] & 3u; }
+      } else if (!has_indel && is_carried(i)) {
+        has_indel = true;
+        indel = aux[i];
+      }
+    }
+    uint32_t tb = carried_snv ? alt : b;
+    const uint32_t ew = error_word(fw, q, mate);
+    if (ew < err_thr) tb = other_base(tb, site ? int(carried_snv ? b : alt) : -1, ew % 3u);
+    out.seq.push_back(b > 3 ? 'N' : ACGT[tb]);
+    push('M', 1);
+    ++q;
+    if (has_indel && indels_open && out.cigar.size() < kMaxCigar - 2) {
+      const uint32_t l = (indel >> 1) & 7u;
+      if (indel & 1u) {
+        for (uint32_t k = 0; k < l && out.seq.size() < R; ++k) {
+          uint32_t ib = (indel >> (8 + 2 * k)) & 3u;
+          const uint32_t ei = error_word(fw ^ (0x9E3779B1u * (k + 1)), q - 1, mate);
+          if (ei < err_thr) ib = other_base(ib, -1, ei % 3u);
+          out.seq.push_back(ACGT[ib]);
+          push('I', 1);
+        }
+      } else if (out.seq.size() < R) {
+        push('D', l);
+        q += l;
+      }
+    } else if (has_indel) {
+      indels_open = false;
+    }
+  }
+  return out;
 }
 
 // ---- flavour 1: sequential reads, std::mt19937_64 and std:: distributions.
@@ -1535,6 +1637,15 @@ void* orc_engine_create(uint32_t n_chr, const uint32_t* chr_len, const uint8_t* 
   } catch (const std::exception& ex) { orc_err = ex.what(); return nullptr; }
 }
 void orc_engine_destroy(void* e) { delete static_cast<Engine*>(e); }
+// regions to avoid (chromosome index, 1-based begin, length), then the
+// indices again
+void orc_engine_set_avoid(void* ep, uint32_t n, const uint32_t* chr, const uint32_t* begin, const uint32_t* len) {
+  Engine& e = *static_cast<Engine*>(ep);
+  e.avoid.assign(e.g.b.size(), 0);
+  for (uint32_t i = 0; i < n; ++i)
+    for (uint32_t q = 0; q < len[i]; ++q) e.avoid[e.g.off[chr[i]] + begin[i] - 1 + q] = 1;
+  build_index(e);
+}
 
 void orc_engine_index_info(void* ep, uint64_t* ctx_total, uint64_t* id_total, uint32_t* ctx_len, uint32_t* id_len) {
   auto* e = static_cast<Engine*>(ep);
@@ -1712,6 +1823,48 @@ void* orc_seq(void* pp, const void* cfg, uint64_t seed, int flavour, double frac
     return o;
   } catch (const std::exception& ex) { orc_err = ex.what(); return nullptr; }
 }
+// the replay's SAM reads as text, one line per read in the order of the
+// SAM files (per chromosome and sample: tiles, fragments, mates): sample,
+// chromosome index, FLAG, POS, CIGAR, mate POS, TLEN, SEQ (1-based positions
+// within the chromosome; "*" fields for a read without DNA)
+int orc_sam(void* pp, const void* cfg, uint64_t seed, const char* path) {
+  try {
+    const Placed& pl = *static_cast<Placed*>(pp);
+    const SeqCfg& c = *static_cast<const SeqCfg*>(cfg);
+    const Engine& e = *pl.eng;
+    const SeqSetup s = seq_setup(pl, c);
+    Carrier car{*pl.forest, c.preneoplastic_in_normal != 0};
+    const auto carriers = carrier_sets(pl);
+    std::ofstream f(path);
+    if (!f) throw std::runtime_error("cannot write the expected reads");
+    const uint32_t R = s.R;
+    FragmentVisitor v = [&](uint32_t smp, uint32_t ci, bool dropped, uint32_t p0, uint32_t p1, int64_t cell,
+                            uint32_t allele, uint32_t fw) {
+      const uint32_t off = e.g.off[ci], ce = e.g.off[ci + 1];
+      for (uint32_t m = 0; m < (s.paired ? 2u : 1u); ++m) {
+        f << smp << '\t' << ci << '\t';
+        if (dropped) { f << "4\t*\t*\t*\t*\t*\n"; continue; }
+        const uint32_t p = m ? p1 : p0;
+        const OracleRead rd = oracle_read(pl, car, carriers, pl.aux, p, ce, cell, allele, fw, m, R, s.err_thr);
+        const uint32_t flag = s.paired ? (0x1u | 0x2u | (m ? (0x80u | 0x10u) : (0x40u | 0x20u))) : 0u;
+        f << flag << '\t' << (p - off + 1) << '\t';
+        for (const auto& [op, len] : rd.cigar) f << len << op;
+        if (rd.cigar.empty()) f << '*';
+        if (s.paired) {
+          const int64_t span = int64_t(p1) + R - p0;
+          f << '\t' << ((m ? p0 : p1) - off + 1) << '\t' << (m ? -span : span);
+        } else {
+          f << "\t0\t0";
+        }
+        f << '\t' << rd.seq << '\n';
+      }
+    };
+    SeqOut out;
+    seq_replay(pl, c, seed, out, &v);
+    return 0;
+  } catch (const std::exception& ex) { orc_err = ex.what(); return 1; }
+}
+
 void orc_seq_destroy(void* o) { delete static_cast<SeqOut*>(o); }
 uint32_t orc_seq_samples(void* o) { return static_cast<SeqOut*>(o)->n_samples; }
 uint64_t orc_seq_reads(void* o) { return static_cast<SeqOut*>(o)->n_reads; }

@@ -51,7 +51,8 @@ class GenomeDesc(C.Structure):
     _fields_ = [
         ("n_chr", C.c_uint32), ("chr_lengths", C.POINTER(C.c_uint32)), ("bases", C.POINTER(C.c_uint8)),
         ("synthetic_seed", C.c_uint64), ("synthetic_gc", C.c_double), ("context_sampling", C.c_uint32),
-        ("max_repetition_storage", C.c_uint32),
+        ("max_repetition_storage", C.c_uint32), ("n_avoid", C.c_uint32), ("avoid_chr", C.POINTER(C.c_uint32)),
+        ("avoid_begin", C.POINTER(C.c_uint32)), ("avoid_len", C.POINTER(C.c_uint32)), ("index_cache_dir", C.c_char_p),
     ]
 
 

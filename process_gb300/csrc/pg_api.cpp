@@ -214,6 +214,9 @@ struct pg_engine {
   uint64_t G = 0;
   DBuf<uint32_t> genome, chr_off_d;
   DBuf<uint32_t> nmask;              // unknown bases (N), one bit each; empty when the genome has none
+  DBuf<uint32_t> amask;              // positions of the regions to avoid (SBS index), one bit each; or empty
+  uint64_t avoid_digest = 0;         // of the regions to avoid (index caches)
+  std::string cache_dir;             // index caches (empty: none)
   uint32_t context_sampling = 100, max_rep = 500000;
   // index
   std::vector<uint64_t> ctx_total, id_total;
@@ -355,45 +358,148 @@ struct Timer {
 
 void select_device(const pg_engine* e) { ck(cudaSetDevice(e->device), "cudaSetDevice"); }
 
+// fingerprint of an engine's genome: lengths and 4096 words at an even
+// stride, FNV-1a (64 bit)
+uint64_t fnv1a(uint64_t h, const void* p, size_t k) {
+  const uint8_t* c = static_cast<const uint8_t*>(p);
+  for (size_t i = 0; i < k; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+  return h;
+}
+
+uint64_t genome_fingerprint(const pg_engine* e) {
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(h, &e->G, sizeof(e->G));
+  h = fnv1a(h, e->chr_len.data(), sizeof(uint32_t) * e->chr_len.size());
+  const uint64_t words = (e->G + 15) / 16;
+  if (words) {
+    const uint64_t k = std::min<uint64_t>(4096, words), stride = words / k;
+    std::vector<uint32_t> smp(k);
+    ck(cudaMemcpy2D(smp.data(), sizeof(uint32_t), e->genome.p, sizeof(uint32_t) * stride, sizeof(uint32_t), k,
+                    cudaMemcpyDeviceToHost), "genome fingerprint");
+    h = fnv1a(h, smp.data(), sizeof(uint32_t) * k);
+  }
+  return h;
+}
+
+// ---- index caches: "PGIX", version, which, genome fingerprint, parameter,
+// regions digest, class count, per class total and stored count, the lists
+constexpr uint32_t INDEX_CACHE_VERSION = 1;
+
+std::string index_cache_path(const pg_engine* e, int which) {
+  return e->cache_dir + (which == 0 ? "/context_index_" + std::to_string(e->context_sampling) + ".pgcif"
+                                    : "/rs_index_" + std::to_string(e->max_rep) + ".pgrsif");
+}
+
+struct IndexTables {
+  std::vector<uint64_t> total;
+  std::vector<uint32_t> len;
+  std::vector<uint32_t> lists;   // host copy (caches only)
+};
+
+void save_index_cache(const pg_engine* e, int which, uint64_t fp, const IndexTables& t) {
+  std::ofstream f(index_cache_path(e, which), std::ios::binary | std::ios::trunc);
+  if (!f) throw std::runtime_error("cannot write the index cache " + index_cache_path(e, which));
+  auto put = [&](const void* p, size_t k) { f.write(static_cast<const char*>(p), std::streamsize(k)); };
+  const uint32_t v = INDEX_CACHE_VERSION, w = uint32_t(which), prm = which == 0 ? e->context_sampling : e->max_rep,
+                 nc = uint32_t(t.total.size());
+  const uint64_t dg = which == 0 ? e->avoid_digest : 0, nl = t.lists.size();
+  put("PGIX", 4); put(&v, 4); put(&w, 4); put(&fp, 8); put(&prm, 4); put(&dg, 8); put(&nc, 4);
+  put(t.total.data(), 8 * nc); put(t.len.data(), 4 * nc); put(&nl, 8); put(t.lists.data(), 4 * nl);
+  put("XIGP", 4);
+  if (!f) throw std::runtime_error("cannot write the index cache " + index_cache_path(e, which));
+}
+
+bool load_index_cache(const pg_engine* e, int which, uint64_t fp, int NC, IndexTables& t) {
+  const std::string path = index_cache_path(e, which);
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  auto get = [&](void* p, size_t k) {
+    f.read(static_cast<char*>(p), std::streamsize(k));
+    if (!f) throw DomainError("the index cache " + path + " is truncated");
+  };
+  char magic[4];
+  uint32_t v = 0, w = 0, prm = 0, nc = 0;
+  uint64_t fp2 = 0, dg = 0, nl = 0;
+  get(magic, 4);
+  if (std::memcmp(magic, "PGIX", 4) != 0) throw DomainError(path + " is not an index cache");
+  get(&v, 4);
+  if (v != INDEX_CACHE_VERSION)
+    throw DomainError("the index cache " + path + " has format version " + std::to_string(v) +
+                      ", this library reads version " + std::to_string(INDEX_CACHE_VERSION));
+  get(&w, 4); get(&fp2, 8); get(&prm, 4); get(&dg, 8); get(&nc, 4);
+  if (w != uint32_t(which) || nc != uint32_t(NC) || prm != (which == 0 ? e->context_sampling : e->max_rep))
+    throw DomainError("the index cache " + path + " holds another index");
+  if (fp2 != fp) throw DomainError("the index cache " + path + " was built for another reference genome");
+  if (which == 0 && dg != e->avoid_digest)
+    throw DomainError("the index cache " + path + " was built with other regions to avoid");
+  t.total.resize(nc); t.len.resize(nc);
+  get(t.total.data(), 8 * nc); get(t.len.data(), 4 * nc); get(&nl, 8);
+  uint64_t want = 0;
+  for (uint32_t k : t.len) want += k;
+  if (nl != want || nl > (uint64_t(1) << 34)) throw DomainError("the index cache " + path + " is inconsistent");
+  t.lists.resize(nl);
+  get(t.lists.data(), 4 * nl);
+  get(magic, 4);
+  if (std::memcmp(magic, "XIGP", 4) != 0) throw DomainError("the index cache " + path + " is inconsistent");
+  return true;
+}
+
 void build_indices(pg_engine* e) {
   const uint32_t ntiles = pg::index_num_tiles(e->G);
+  const uint64_t fp = e->cache_dir.empty() ? 0 : genome_fingerprint(e);
   for (int which = 0; which < 2; ++which) {
     const int NC = pg::index_num_classes(which);
-    DBuf<uint32_t> cnt(&e->pool, uint64_t(NC) * ntiles);
-    DBuf<uint32_t> part(&e->pool, pg::scan_part_elems(ntiles, NC));
-    DBuf<uint32_t> tot(&e->pool, NC);
-    pg::index_count(which, e->genome.p, e->nmask.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, part.p, tot.p, e->st);
-    std::vector<uint32_t> tot_h(NC);
-    ck(cudaMemcpyAsync(tot_h.data(), tot.p, sizeof(uint32_t) * NC, cudaMemcpyDeviceToHost, e->st), "index totals");
-    ck(cudaStreamSynchronize(e->st), "index count");
-    std::vector<uint32_t> stride(NC), len(NC);
+    IndexTables t;
     std::vector<uint64_t> off(NC + 1, 0);
-    std::vector<uint64_t>& total = which == 0 ? e->ctx_total : e->id_total;
-    total.assign(NC, 0);
-    for (int k = 0; k < NC; ++k) {
-      total[k] = tot_h[k];
-      uint64_t sd;
-      if (which == 0) sd = e->context_sampling;
-      else sd = std::max<uint64_t>(1, (uint64_t(tot_h[k]) + e->max_rep - 1) / e->max_rep);
-      stride[k] = uint32_t(sd);
-      len[k] = uint32_t((uint64_t(tot_h[k]) + sd - 1) / sd);
-      off[k + 1] = off[k] + len[k];
+    DBuf<uint32_t> lists;
+    if (!e->cache_dir.empty() && load_index_cache(e, which, fp, NC, t)) {
+      for (int k = 0; k < NC; ++k) off[k + 1] = off[k] + t.len[k];
+      lists = upload(&e->pool, t.lists, e->st);
+    } else {
+      DBuf<uint32_t> cnt(&e->pool, uint64_t(NC) * ntiles);
+      DBuf<uint32_t> part(&e->pool, pg::scan_part_elems(ntiles, NC));
+      DBuf<uint32_t> tot(&e->pool, NC);
+      const uint32_t* am = which == 0 ? e->amask.p : nullptr;
+      pg::index_count(which, e->genome.p, e->nmask.p, am, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, part.p, tot.p,
+                      e->st);
+      std::vector<uint32_t> tot_h(NC);
+      ck(cudaMemcpyAsync(tot_h.data(), tot.p, sizeof(uint32_t) * NC, cudaMemcpyDeviceToHost, e->st), "index totals");
+      ck(cudaStreamSynchronize(e->st), "index count");
+      std::vector<uint32_t> stride(NC);
+      t.total.assign(NC, 0); t.len.assign(NC, 0);
+      for (int k = 0; k < NC; ++k) {
+        t.total[k] = tot_h[k];
+        uint64_t sd;
+        if (which == 0) sd = e->context_sampling;
+        else sd = std::max<uint64_t>(1, (uint64_t(tot_h[k]) + e->max_rep - 1) / e->max_rep);
+        stride[k] = uint32_t(sd);
+        t.len[k] = uint32_t((uint64_t(tot_h[k]) + sd - 1) / sd);
+        off[k + 1] = off[k] + t.len[k];
+      }
+      auto stride_d = upload(&e->pool, stride, e->st);
+      auto len_tmp = upload(&e->pool, t.len, e->st);
+      std::vector<uint64_t> off_k(off.begin(), off.begin() + NC);
+      auto off_tmp = upload(&e->pool, off_k, e->st);
+      lists = DBuf<uint32_t>(&e->pool, off[NC]);
+      pg::index_emit(which, e->genome.p, e->nmask.p, am, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p,
+                     off_tmp.p, len_tmp.p, lists.p, e->st);
+      ck(cudaStreamSynchronize(e->st), "index emit");
+      ck(cudaGetLastError(), "index kernels");
+      if (!e->cache_dir.empty()) {
+        t.lists.resize(off[NC]);
+        if (off[NC]) ck(cudaMemcpy(t.lists.data(), lists.p, 4 * off[NC], cudaMemcpyDeviceToHost), "index cache");
+        save_index_cache(e, which, fp, t);
+      }
     }
-    auto stride_d = upload(&e->pool, stride, e->st);
-    auto len_d = upload(&e->pool, len, e->st);
     std::vector<uint64_t> off_k(off.begin(), off.begin() + NC);
+    auto len_d = upload(&e->pool, t.len, e->st);
     auto off_d = upload(&e->pool, off_k, e->st);
-    DBuf<uint32_t> lists(&e->pool, off[NC]);
-    pg::index_emit(which, e->genome.p, e->nmask.p, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p, off_d.p,
-                   len_d.p,
-                   lists.p, e->st);
-    ck(cudaStreamSynchronize(e->st), "index emit");
-    ck(cudaGetLastError(), "index kernels");
+    ck(cudaStreamSynchronize(e->st), "index upload");
     if (which == 0) {
-      e->ctx_len = len; e->ctx_off = off_k;
+      e->ctx_total = t.total; e->ctx_len = t.len; e->ctx_off = off_k;
       e->ctx_lists = std::move(lists); e->ctx_len_d = std::move(len_d); e->ctx_off_d = std::move(off_d);
     } else {
-      e->id_len = len; e->id_off = off_k;
+      e->id_total = t.total; e->id_len = t.len; e->id_off = off_k;
       e->id_lists = std::move(lists); e->id_len_d = std::move(len_d); e->id_off_d = std::move(off_d);
     }
   }
@@ -514,6 +620,34 @@ pg_status pg_engine_create(const pg_genome_desc* gd, pg_engine** out) {
       pg::genome_synth(e->genome.p, G, gd->synthetic_seed, gd->synthetic_gc, e->st);
     }
     ck(cudaGetLastError(), "genome kernels");
+    // regions to avoid (SBS context index), as a bit per position
+    if (gd->n_avoid) {
+      require(gd->avoid_chr && gd->avoid_begin && gd->avoid_len, "NULL regions to avoid");
+      std::vector<std::pair<uint32_t, uint32_t>> reg;
+      for (uint32_t i = 0; i < gd->n_avoid; ++i) {
+        const uint32_t c = gd->avoid_chr[i], b = gd->avoid_begin[i], l = gd->avoid_len[i];
+        require(c < e->n_chr, "region to avoid on an unknown chromosome");
+        require(b >= 1 && l >= 1 && uint64_t(b) - 1 + l <= e->chr_len[c], "region to avoid outside its chromosome");
+        reg.push_back({e->chr_off[c] + b - 1, e->chr_off[c] + b - 1 + l});
+      }
+      std::vector<uint32_t> pos;     // every avoided position once, ascending
+      for (auto [b, en] : reg)
+        for (uint32_t q = b; q < en; ++q) pos.push_back(q);
+      std::sort(pos.begin(), pos.end());
+      pos.erase(std::unique(pos.begin(), pos.end()), pos.end());
+      e->avoid_digest = fnv1a(1469598103934665603ull, pos.data(), sizeof(uint32_t) * pos.size());
+      e->amask = DBuf<uint32_t>(&e->pool, (G + 31) / 32 + 1);
+      ck(cudaMemsetAsync(e->amask.p, 0, sizeof(uint32_t) * ((G + 31) / 32 + 1), e->st), "memset");
+      auto pos_d = upload(&e->pool, pos, e->st);
+      pg::genome_avoid_mask(pos_d.p, pos.size(), e->amask.p, e->st);
+      ck(cudaStreamSynchronize(e->st), "regions to avoid");
+    }
+    if (gd->index_cache_dir && gd->index_cache_dir[0]) {
+      e->cache_dir = gd->index_cache_dir;
+      std::error_code ec;
+      std::filesystem::create_directories(e->cache_dir, ec);
+      require(std::filesystem::is_directory(e->cache_dir), "index cache directory " + e->cache_dir + " is not a directory");
+    }
     build_indices(e.get());
     *out = e.release();
   });

@@ -39,27 +39,6 @@ struct Reader {
   }
 };
 
-// fingerprint of an engine's genome: lengths and 4096 words at an even
-// stride, FNV-1a (64 bit)
-uint64_t genome_fingerprint(const pg_engine* e) {
-  uint64_t h = 1469598103934665603ull;
-  auto mix = [&](const void* p, size_t k) {
-    const uint8_t* c = static_cast<const uint8_t*>(p);
-    for (size_t i = 0; i < k; ++i) { h ^= c[i]; h *= 1099511628211ull; }
-  };
-  mix(&e->G, sizeof(e->G));
-  mix(e->chr_len.data(), sizeof(uint32_t) * e->chr_len.size());
-  const uint64_t words = (e->G + 15) / 16;
-  if (words) {
-    const uint64_t k = std::min<uint64_t>(4096, words), stride = words / k;
-    std::vector<uint32_t> s(k);
-    ck(cudaMemcpy2D(s.data(), sizeof(uint32_t), e->genome.p, sizeof(uint32_t) * stride, sizeof(uint32_t), k,
-                    cudaMemcpyDeviceToHost), "genome fingerprint");
-    mix(s.data(), sizeof(uint32_t) * k);
-  }
-  return h;
-}
-
 template <class T>
 std::vector<T> download(const DBuf<T>& d, uint64_t n) {
   std::vector<T> v(n);

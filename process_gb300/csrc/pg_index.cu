@@ -74,6 +74,7 @@ __global__ void k_genome_pack(uint32_t* __restrict__ words, const uint8_t* __res
 struct SbsFamilies {
   static constexpr int NF = 1;
   static constexpr int NC = N_CTX;
+  static constexpr bool AVOIDABLE = true;    // positions of the regions to avoid are not indexed
   template <class Get>
   __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
     out[0] = -1;
@@ -101,6 +102,7 @@ struct SbsFamilies {
 struct IdFamilies {
   static constexpr int NF = 16;
   static constexpr int NC = N_ID;
+  static constexpr bool AVOIDABLE = false;
   template <class Get>
   __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
 #pragma unroll
@@ -175,7 +177,8 @@ __device__ __forceinline__ void load_window(const uint32_t* __restrict__ g, cons
 // mode 0: count; mode 1: emit positions
 template <class F, int MODE>
 __global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__ g,
-                                                    const uint32_t* __restrict__ nmask, uint64_t G,
+                                                    const uint32_t* __restrict__ nmask,
+                                                    const uint32_t* __restrict__ amask, uint64_t G,
                                                     const uint32_t* __restrict__ chr_off, int n_chr,
                                                     uint32_t ntiles, uint32_t* __restrict__ cnt,
                                                     const uint32_t* __restrict__ stride,
@@ -209,6 +212,7 @@ __global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__
         return (q >= cs && q < ce) ? uint32_t(s[q - tile_start + WIN_BEFORE]) : BASE_INVALID;
       };
       F::classes(get, p, cs, ce, cls);
+      if (F::AVOIDABLE && base_unknown(amask, p)) cls[0] = -1;   // inside a region to avoid
     } else {
 #pragma unroll
       for (int f = 0; f < F::NF; ++f) cls[f] = -1;
@@ -255,37 +259,50 @@ void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t
 uint32_t index_num_tiles(uint64_t G) { return uint32_t((G + TILE - 1) / TILE); }
 
 template <class F>
-static void index_count_t(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
-                          uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
+static void index_count_t(const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
+                          const uint32_t* chr_off, int n_chr, uint32_t* cnt, uint32_t* part, uint32_t* totals,
+                          cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_pass<F, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, G, chr_off, n_chr, ntiles, cnt,
+  k_index_pass<F, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles, cnt,
                                                                   nullptr, nullptr, nullptr, nullptr); note_launch();
   scan_rows<uint32_t>(cnt, cnt, ntiles, F::NC, part, totals, st);
 }
 
 template <class F>
-static void index_emit_t(const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
-                         const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
-                         const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
+static void index_emit_t(const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
+                         const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
+                         const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_pass<F, 1><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, G, chr_off, n_chr, ntiles,
+  k_index_pass<F, 1><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles,
                                                                   const_cast<uint32_t*>(cnt_scanned),
                                                                   stride, list_off, list_len, lists); note_launch();
 }
 
-void index_count(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
-                 uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
-  if (which == 0) index_count_t<SbsFamilies>(g, nmask, G, chr_off, n_chr, cnt, part, totals, st);
-  else index_count_t<IdFamilies>(g, nmask, G, chr_off, n_chr, cnt, part, totals, st);
+void index_count(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
+                 const uint32_t* chr_off, int n_chr, uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st) {
+  if (which == 0) index_count_t<SbsFamilies>(g, nmask, amask, G, chr_off, n_chr, cnt, part, totals, st);
+  else index_count_t<IdFamilies>(g, nmask, nullptr, G, chr_off, n_chr, cnt, part, totals, st);
 }
 
-void index_emit(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
-                const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
-                const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
+void index_emit(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
+                const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
+                const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
   if (which == 0)
-    index_emit_t<SbsFamilies>(g, nmask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+    index_emit_t<SbsFamilies>(g, nmask, amask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
   else
-    index_emit_t<IdFamilies>(g, nmask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+    index_emit_t<IdFamilies>(g, nmask, nullptr, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists,
+                             st);
+}
+
+// the positions of the regions to avoid as bits of mask ((G + 31) / 32 words,
+// zeroed by the caller)
+__global__ void k_avoid_mask(const uint32_t* __restrict__ pos, uint64_t n, uint32_t* __restrict__ mask) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) atomicOr(mask + (pos[i] >> 5), 1u << (pos[i] & 31u));
+}
+
+void genome_avoid_mask(const uint32_t* pos, uint64_t n, uint32_t* mask, cudaStream_t st) {
+  if (n) { k_avoid_mask<<<unsigned((n + 255) / 256), 256, 0, st>>>(pos, n, mask); note_launch(); }
 }
 
 int index_num_classes(int which) { return which == 0 ? SbsFamilies::NC : IdFamilies::NC; }
@@ -348,11 +365,11 @@ const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const
   if (cudaPeekAtLastError() != cudaSuccess) return "a CUDA error from earlier work is pending; nothing was launched";
   // every (class, tile) entry is written by the count pass: nothing to clear
   if (which == 0)
-    k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, G, chr_off, n_chr, ntiles,
+    k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, nullptr, G, chr_off, n_chr, ntiles,
                                                                               scratch,
                                                                               nullptr, nullptr, nullptr, nullptr);
   else
-    k_index_pass<IdFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, G, chr_off, n_chr, ntiles,
+    k_index_pass<IdFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, nullptr, G, chr_off, n_chr, ntiles,
                                                                              scratch,
                                                                              nullptr, nullptr, nullptr, nullptr);
   k_class_totals<<<nc, 256, 0, st>>>(scratch, ntiles, totals);

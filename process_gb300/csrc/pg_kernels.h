@@ -41,12 +41,15 @@ int index_num_classes(int which);  // 0 = SBS contexts (32), 1 = ID classes (83)
 constexpr uint32_t NOALLOC_MAX_TILES = 8192;
 const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
                                  uint64_t* totals, cudaStream_t st);
-// contexts and repeat sites that touch an unknown base are not indexed
-void index_count(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
-                 uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st);
-void index_emit(int which, const uint32_t* g, const uint32_t* nmask, uint64_t G, const uint32_t* chr_off, int n_chr,
-                const uint32_t* cnt_scanned, const uint32_t* stride, const uint64_t* list_off,
-                const uint32_t* list_len, uint32_t* lists, cudaStream_t st);
+// contexts and repeat sites that touch an unknown base are not indexed; the
+// SBS contexts (which 0) also skip the positions set in amask (regions to
+// avoid; NULL: none)
+void index_count(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
+                 const uint32_t* chr_off, int n_chr, uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st);
+void genome_avoid_mask(const uint32_t* pos, uint64_t n, uint32_t* mask, cudaStream_t st);
+void index_emit(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
+                const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
+                const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st);
 
 // ---------------------------------------------------------------- genome classes
 // Copy-number events are rare, so the cells of a forest fall into few

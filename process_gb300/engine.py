@@ -107,6 +107,13 @@ class GenomeSpec:
         return cls(names, lengths, bases=np.concatenate(parts), path=str(path))
 
 
+def driver_regions(drivers: Iterable) -> list:
+    """The regions build_contex_index leaves out of the context index for a
+    driver catalogue (src/mutation_engine.cpp:240-250): each driver
+    mutation's position and max(1, len(ref)) bases, as (chr, begin, length)."""
+    return [(str(m.chr), int(m.chr_pos), max(1, len(m.ref))) for m in drivers]
+
+
 def read_signature_table(path, type_: int) -> dict:
     """A signature table in the reference's format
     (Signature::read_from_stream, src/mutation_engine.cpp:389-397): a
@@ -363,7 +370,8 @@ class MutationEngine:
     def __init__(self, genome: GenomeSpec, SBS_signatures: Mapping[str, Sequence[float]] | None = None,
                  indel_signatures: Mapping[str, Sequence[float]] | None = None, context_sampling: int = 100,
                  max_motif_size: int = 50, max_repetition_storage: int = 500000,
-                 avoid_homozygous_losses: bool = True, passenger_CNAs: Iterable | None = None):
+                 avoid_homozygous_losses: bool = True, passenger_CNAs: Iterable | None = None,
+                 regions_to_avoid: Iterable | None = None, index_cache_dir: str | None = None):
         self.genome = genome
         self.chr_names = [str(c) for c in genome.chr_names]
         self.chr_lengths = np.asarray(genome.chr_lengths, dtype=np.uint32)
@@ -384,6 +392,18 @@ class MutationEngine:
         d.synthetic_gc = float(genome.gc)
         d.context_sampling = self.context_sampling
         d.max_repetition_storage = self.max_repetition_storage
+        # positions the SBS context index leaves out (build_contex_index
+        # leaves out the driver catalogue, src/mutation_engine.cpp:240-250)
+        self.regions_to_avoid = [(str(c), int(b), int(n)) for c, b, n in (regions_to_avoid or [])]
+        if self.regions_to_avoid:
+            ac = np.ascontiguousarray([self._chr_index(c) for c, _, _ in self.regions_to_avoid], dtype=np.uint32)
+            ab = np.ascontiguousarray([b for _, b, _ in self.regions_to_avoid], dtype=np.uint32)
+            al = np.ascontiguousarray([n for _, _, n in self.regions_to_avoid], dtype=np.uint32)
+            d.n_avoid = len(ac)
+            d.avoid_chr, d.avoid_begin, d.avoid_len = ptr(ac, C.c_uint32), ptr(ab, C.c_uint32), ptr(al, C.c_uint32)
+        self.index_cache_dir = index_cache_dir
+        if index_cache_dir:
+            d.index_cache_dir = str(index_cache_dir).encode()
         h = C.c_void_p()
         check(lib().pg_engine_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -668,7 +688,8 @@ class MutationEngine:
                 "SBS_signatures": _plain(self._sigs[0]), "indel_signatures": _plain(self._sigs[1]),
                 "exposures": copy.deepcopy(_plain(self._exposures)),
                 "mutants": copy.deepcopy(_plain(self._mutant_specs)),
-                "passenger_CNAs": _plain(self.passenger_CNAs)}
+                "passenger_CNAs": _plain(self.passenger_CNAs),
+                "regions_to_avoid": _plain(getattr(self, "regions_to_avoid", []))}
 
 
 class PhylogeneticForest:
@@ -1110,7 +1131,8 @@ def load_phylogenetic_forest(filename: str, quiet: bool = False) -> "Phylogeneti
                              context_sampling=em["context_sampling"], max_motif_size=em["max_motif_size"],
                              max_repetition_storage=em["max_repetition_storage"],
                              avoid_homozygous_losses=em["avoid_homozygous_losses"],
-                             passenger_CNAs=[_driver(c) for c in em["passenger_CNAs"]])
+                             passenger_CNAs=[_driver(c) for c in em["passenger_CNAs"]],
+                             regions_to_avoid=[tuple(r) for r in em.get("regions_to_avoid", [])])
         for name, rates, drivers in em["mutants"]:
             eng.add_mutant(name, rates, [_driver(d) for d in drivers])
         for t, coeffs in em["exposures"]:

@@ -403,3 +403,86 @@ def test_distribution_plain_3mbp_workload(gpu_lib, orc):
     assert stats.chi2_contingency(np.vstack([g_ctx[keep], m_ctx[keep]]))[1] > 0.01
     assert stats.ks_2samp(np.concatenate(g_edge), np.concatenate(m_edge)).pvalue > 0.01
     assert stats.ks_2samp(np.concatenate(g_vaf), np.concatenate(m_vaf)).pvalue > 0.01
+
+
+def test_regions_to_avoid(gpu_lib, orc):
+    """Regions to avoid (the driver catalogue of build_contex_index,
+    src/mutation_engine.cpp:240-262): the SBS context index leaves their
+    positions out, the ID index keeps them; index lists and placement bit
+    for bit against the oracle."""
+    from process_gb300 import SNV, GenomeSpec, Mutation, MutationEngine, driver_regions, synth
+    w = synth.plain_3mbp(seed=23, n_leaves=200)
+    w.genome.chr_lengths = [200_000, 100_000, 100_000]
+    catalogue = [SNV("1", 1000, "T"), Mutation("2", 500, "ACG", "A"), SNV("3", 77, "G")]
+    regions = driver_regions(catalogue) + [("1", 50_001, 20_000)]
+    assert regions[1] == ("2", 500, 3)
+    eng = MutationEngine(w.genome, w.sbs, w.ids, context_sampling=1, regions_to_avoid=regions)
+    plain = MutationEngine(w.genome, w.sbs, w.ids, context_sampling=1)
+    o = orc.OracleEngine(w.genome.chr_lengths, None, w.genome.seed, w.genome.gc, context_sampling=1)
+    o.set_regions_to_avoid(regions, eng._chr_index)
+    gi, oi, pi = eng.index_info(), o.index_info(), plain.index_info()
+    np.testing.assert_array_equal(gi["ctx_total"], oi["ctx_total"])
+    np.testing.assert_array_equal(gi["id_total"], oi["id_total"])
+    np.testing.assert_array_equal(gi["id_total"], pi["id_total"])          # ID index unchanged
+    assert pi["ctx_total"].sum() - gi["ctx_total"].sum() == 20_000 + 1 + 3 + 1
+    off = np.concatenate([[0], np.cumsum(w.genome.chr_lengths)])
+    avoided = set()
+    for c, b, n in regions:
+        base = off[eng._chr_index(c)] + b - 1
+        avoided.update(range(base, base + n))
+    for c in range(32):
+        lst = eng.read_index(0, c)
+        np.testing.assert_array_equal(lst, o.read_index(0, c))
+        assert not avoided & set(lst.tolist())
+    for c in range(83):
+        np.testing.assert_array_equal(eng.read_index(1, c), o.read_index(1, c))
+    # placement over the index without those positions
+    for name, rates, drivers in w.mutants:
+        eng.add_mutant(name, rates, drivers)
+    for t, coeffs in w.exposures:
+        eng.add_exposure(t, coeffs)
+    o2 = orc.OracleEngine.like(w)
+    o2.set_regions_to_avoid(regions, eng._chr_index)
+    pf = eng.place_mutations(w.forest, 40, 4, seed=2)
+    ot = o2.place(w.forest, oracle_species(o2, w.forest), 40, 0, 4, 0, seed=2).table()
+    assert_tables_equal(pf.table(), ot)
+
+
+def test_index_cache(gpu_lib, tmp_path):
+    """Index caches (the reference's .cif / .rsif files): the first engine
+    writes them, the next one with the same genome, parameters and regions
+    loads them and holds the same indices; a cache of another genome, other
+    regions or another format version is refused."""
+    import struct
+
+    from process_gb300 import DomainError, GenomeSpec, MutationEngine, synth
+    w = synth.plain_3mbp(seed=24, n_leaves=50)
+    g = GenomeSpec(["1", "2"], [150_000, 80_000], seed=5, gc=0.45)
+    d = tmp_path / "cache"
+    regions = [("1", 101, 50)]
+    a = MutationEngine(g, w.sbs, w.ids, context_sampling=3, max_repetition_storage=1000, regions_to_avoid=regions,
+                       index_cache_dir=str(d))
+    files = sorted(p.name for p in d.iterdir())
+    assert files == ["context_index_3.pgcif", "rs_index_1000.pgrsif"]
+    b = MutationEngine(g, w.sbs, w.ids, context_sampling=3, max_repetition_storage=1000, regions_to_avoid=regions,
+                       index_cache_dir=str(d))
+    ia, ib = a.index_info(), b.index_info()
+    for k in ia:
+        np.testing.assert_array_equal(ia[k], ib[k], err_msg=k)
+    for c in range(32):
+        np.testing.assert_array_equal(a.read_index(0, c), b.read_index(0, c))
+    for c in range(83):
+        np.testing.assert_array_equal(a.read_index(1, c), b.read_index(1, c))
+    with pytest.raises(DomainError, match="another reference genome"):
+        MutationEngine(GenomeSpec(["1", "2"], [150_000, 80_000], seed=6, gc=0.45), w.sbs, w.ids, context_sampling=3,
+                       max_repetition_storage=1000, regions_to_avoid=regions, index_cache_dir=str(d))
+    with pytest.raises(DomainError, match="other regions to avoid"):
+        MutationEngine(g, w.sbs, w.ids, context_sampling=3, max_repetition_storage=1000,
+                       regions_to_avoid=[("1", 102, 50)], index_cache_dir=str(d))
+    f = d / "rs_index_1000.pgrsif"
+    raw = bytearray(f.read_bytes())
+    raw[4:8] = struct.pack("<I", 7)
+    f.write_bytes(bytes(raw))
+    with pytest.raises(DomainError, match="format version 7"):
+        MutationEngine(g, w.sbs, w.ids, context_sampling=3, max_repetition_storage=1000, regions_to_avoid=regions,
+                       index_cache_dir=str(d))

@@ -140,3 +140,41 @@ def test_sam_indels_naming_and_update(gpu_lib, tmp_path):
     assert (out / "chr_2_1.sam").exists()
     _, reads = _parse(out / "chr_2_1.sam")
     assert reads and all(f[0].startswith("t") for f in reads)
+
+
+def test_sam_reads_match_oracle(gpu_lib, orc, tmp_path):
+    """Every SAM read -- FLAG, POS, CIGAR, mate POS, TLEN and the bases --
+    equals the oracle's own restatement of the read builder (reference
+    window, carried SNVs and indels through its carrier closure, error
+    substitutions, mate positions), read by read in file order, on a forest
+    with CNAs, a WGD and frequent indels, at a high error rate."""
+    from process_gb300.engine import seq_cfg, sequence_counts
+    from test_gpu_cna import _pair, _species, _tables_equal, _workload
+    w, cands = _workload(seed=13, n_leaves=120)
+    w.mutants = [(n, dict(r, indel=3e-6, SNV=5e-6), d) for n, r, d in w.mutants]
+    eng, o = _pair(orc, w, cands, True, True)
+    pf = eng.place_mutations(w.forest, 60, 20, seed=3)
+    op = o.place(w.forest, _species(o, w.forest), 60, 0, 20, 0, seed=3)
+    _tables_equal(pf.table(), op.table())
+    assert (pf.table()["kind"] == 1).sum() > 50
+    cfg = dict(coverage=2, read_size=100, insert_size_mean=250, insert_size_stddev=10, error_rate=2e-2, purity=0.8)
+    names = list(w.forest.sample_names) + ["normal_sample"]
+    out = tmp_path / "sam"
+    res = sequence_counts(pf, 31, sam=dict(output_dir=str(out), sample_names=names), **cfg)
+    c, _ = seq_cfg(chr_index=eng._chr_index, tile_size=res.tile_size(), **cfg)
+    want = op.sam_reads(c, 31, tmp_path / "expected.tsv")
+    got = {}
+    n_indel_reads = 0
+    for path in sorted(out.glob("*.sam")):
+        head, reads = _parse(path)
+        chrom = [h.split("\t")[1][3:] for h in head if h.startswith("@SQ")][0]
+        ci = eng._chr_index(chrom)
+        for f in reads:
+            s = names.index(f[11].split(":")[2])
+            row = ("4", "*", "*", "*", "*", "*") if int(f[1]) & 4 else (f[1], f[3], f[5], f[7], f[8], f[9])
+            n_indel_reads += ("I" in f[5]) or ("D" in f[5])
+            got.setdefault((s, ci), []).append(row)
+    assert set(got) == set(want)
+    for k in want:
+        assert got[k] == want[k], k
+    assert n_indel_reads > 0
