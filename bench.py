@@ -299,16 +299,23 @@ def calibration_bench(world: int, n_rep: int = 512, n_sites: int = 100_000, step
     ev[1].record(s)
     ev[1].synchronize()
     t_adam = ev[0].elapsed_time(ev[1]) / 1000.0
-    # per-instance path: one replicate per call, the caller waiting for each
+    # per-instance path: one replicate per call (pg_calib_nll_grad_one),
+    # stream-ordered with preallocated outputs and one synchronisation at
+    # the end, timed with CUDA events on the handle's stream
+    import ctypes as C
     n_one = min(64, n_rep)
+    nll1 = torch.zeros(n_rep, dtype=torch.float32, device="cuda")
+    grad1 = torch.zeros_like(p0)
+    args = (C.c_void_p(p0.data_ptr()), C.c_void_p(nll1.data_ptr()), C.c_void_p(grad1.data_ptr()))
     for r in range(2):
-        b.nll_grad_one(r, p0)
+        b.L.pg_calib_nll_grad_one(b._h, r, *args)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    ev[0].record(s)
     for r in range(n_one):
-        b.nll_grad_one(r, p0)
-        torch.cuda.synchronize()
-    t_one = (time.perf_counter() - t0) / n_one
+        b.L.pg_calib_nll_grad_one(b._h, r, *args)
+    ev[1].record(s)
+    ev[1].synchronize()
+    t_one = ev[0].elapsed_time(ev[1]) / 1000.0 / n_one
     # FP64 CPU oracle, one replicate
     r0 = (d.alt[: n_sites], d.depth[: n_sites], d.cls[: n_sites], d.signatures, d.epoch_weight[0], d.phi[0], 4, 3)
     t0 = time.perf_counter()
@@ -322,6 +329,7 @@ def calibration_bench(world: int, n_rep: int = 512, n_sites: int = 100_000, step
             "grad_evals_per_s_adam_graph": world * n_rep * steps / t_adam,
             "grad_evals_per_s_per_instance": world / t_one,
             "batched_over_per_instance": t_one / (t_batched / n_rep),
+            "per_instance": "pg_calib_nll_grad_one per replicate, stream-ordered, one synchronisation at the end",
             "adam_200_steps_ms": t_adam * 1000.0,
             "cpu_fp64_grad_evals_per_s_1core": 1.0 / t_cpu,
             "roofline": {"kernel": "k_calib_sites+k_calib_epilogue", "bound": "hbm",
@@ -349,6 +357,10 @@ def gpu_arm(args):
 
     w = synth.full_scale(seed=2, genome_scale=args.genome_scale)
     eng = synth.build_engine(w)
+    ims = (C.c_float * 4)()
+    _lib.check(_lib.lib().pg_engine_index_ms(eng._h, ims))
+    index_ms = {"sbs_count": ims[0], "sbs_emit": ims[1], "id_count": ims[2], "id_emit": ims[3],
+                "total": sum(ims), "what": "device time of the engine's index build (count pass + scan, emit pass)"}
     # a dedicated (non-default) stream: the engine runs on it and the CUDA
     # events that time the steps are recorded on it
     stream = torch.cuda.Stream()
@@ -398,6 +410,9 @@ def gpu_arm(args):
     step_ms = t[0] / args.steps
     # read-locus visits of the last step, for the roofline's algorithmic bytes
     pf, res = last
+    rr = C.c_uint32()
+    _lib.check(_lib.lib().pg_placed_redraw_rounds(pf._h, C.byref(rr)))
+    redraw_rounds = rr.value
     alt, dep = res.counts()
     site_hits = int(dep.astype(np.int64).sum())
     reads_last = res.dims()[2]
@@ -492,6 +507,8 @@ def gpu_arm(args):
                           "place_ms_per_step": float(t[1]) / args.steps, "seq_ms_per_step": float(t[2]) / args.steps,
                           "bracket_wall_s": wall,
                           "result_frame": frame_info,
+                          "index_build_ms": index_ms,
+                          "redraw_rounds_last_step": redraw_rounds,
                           "e2e_full_tables": {"value": e2e_full_value, "unit": "reads/s",
                                               "d2h_bytes_per_step": d2h_full_step}},
             "roofline": {"kernel": "k_reads", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

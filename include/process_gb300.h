@@ -256,6 +256,15 @@ pg_status pg_placed_class_copy(const pg_placed* placed, uint32_t* seg_off, uint3
                                uint32_t* seg_ioff, uint32_t* seg_icnt, uint16_t* inst_list, uint8_t* inst_root);
 /* Device time of the placement kernels of the last place call (ms). */
 pg_status pg_placed_kernel_ms(const pg_placed* placed, float* ms);
+// Redraw rounds of the placement (infinite sites collisions and loci drawn
+// where the cell has no allele left): the round counter after the last
+// round run, counting the first infinite-sites round as round 0; 0 when no
+// round after the first ran.
+pg_status pg_placed_redraw_rounds(const pg_placed* placed, uint32_t* rounds);
+// Device time (ms) of the engine's index build: ms[0] SBS context count pass
+// (with its scan over the units), ms[1] its emit pass, ms[2] and ms[3] the
+// same for the ID83 index; zeros for an index read from a cache.
+pg_status pg_engine_index_ms(const pg_engine* engine, float* ms);
 
 /* ------------------------------------------------------------------ data frames
  * The data frames of the reference's PhylogeneticForest getters, built in

@@ -101,6 +101,8 @@ _PROTOS = {
     "pg_engine_add_passenger_cna": (C.c_int, [P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int]),
     "pg_engine_set_avoid_homozygous_losses": (C.c_int, [P, C.c_int]),
     "pg_placed_kernel_ms": (C.c_int, [P, f32p]),
+    "pg_placed_redraw_rounds": (C.c_int, [P, u32p]),
+    "pg_engine_index_ms": (C.c_int, [P, f32p]),
     "pg_placed_set_samples": (C.c_int, [P, C.c_uint32, i32p]),
     "pg_placed_lineage_dims": (C.c_int, [P, u32p, u32p]),
     "pg_placed_lineage_copy": (C.c_int, [P, u32p, C.POINTER(C.c_uint16), u64p, u64p]),

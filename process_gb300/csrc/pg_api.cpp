@@ -206,6 +206,7 @@ static inline uint32_t mulhi32(uint32_t a, uint32_t b) { return uint32_t((uint64
 
 struct pg_engine {
   int device = 0;
+  float index_ms[4] = {0, 0, 0, 0};  // device time of the index build: SBS count, emit; ID count, emit
   cudaStream_t st = nullptr;         // the stream every call of the engine runs on
   cudaStream_t own_st = nullptr;     // the engine's own stream (destroyed with it)
   Pool pool;
@@ -274,6 +275,7 @@ struct pg_placed {
   DBuf<uint8_t> cls, sig, kind, nature;
   DBuf<uint16_t> allele, seq;
   float kernel_ms = 0;
+  uint32_t redraw_rounds = 0;   // the round counter after the last redraw round (0: none ran)
   // genotype classes (copy-number state) and allele-instance lineage
   bool has_cna = false;
   uint32_t cn_max = 2, n_classes = 1;
@@ -460,8 +462,10 @@ void build_indices(pg_engine* e) {
       DBuf<uint32_t> part(&e->pool, pg::scan_part_elems(ntiles, NC));
       DBuf<uint32_t> tot(&e->pool, NC);
       const uint32_t* am = which == 0 ? e->amask.p : nullptr;
+      Timer t_count(e->st);
       pg::index_count(which, e->genome.p, e->nmask.p, am, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, part.p, tot.p,
                       e->st);
+      e->index_ms[2 * which] = t_count.stop();
       std::vector<uint32_t> tot_h(NC);
       ck(cudaMemcpyAsync(tot_h.data(), tot.p, sizeof(uint32_t) * NC, cudaMemcpyDeviceToHost, e->st), "index totals");
       ck(cudaStreamSynchronize(e->st), "index count");
@@ -481,8 +485,10 @@ void build_indices(pg_engine* e) {
       std::vector<uint64_t> off_k(off.begin(), off.begin() + NC);
       auto off_tmp = upload(&e->pool, off_k, e->st);
       lists = DBuf<uint32_t>(&e->pool, off[NC]);
+      Timer t_emit(e->st);
       pg::index_emit(which, e->genome.p, e->nmask.p, am, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p,
                      off_tmp.p, len_tmp.p, lists.p, e->st);
+      e->index_ms[2 * which + 1] = t_emit.stop();
       ck(cudaStreamSynchronize(e->st), "index emit");
       ck(cudaGetLastError(), "index kernels");
       if (!e->cache_dir.empty()) {
@@ -1280,100 +1286,66 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
                                uint32_t(n_snv + n_id), 0, err.p, st);
     auto drv_d = upload(P, drv, st);
     pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), uint32_t(n_snv + n_id), st);
-    // ---- infinite sites, and loci drawn where the cell has no allele left
-    if ((e->infinite_sites || pl->has_cna) && n_snv + n_id > 0) {
-      const bool unique = e->infinite_sites;
-      DBuf<uint32_t> pend_a(P, n_snv + n_id), pend_b(P, n_snv + n_id);
-      DBuf<uint8_t> lost(P, n_snv + n_id);
-      DBuf<uint32_t> n_next(P, 1);
-      const uint32_t* pending = nullptr;
-      uint32_t n_pend = uint32_t(n_snv + n_id);
-      uint32_t* next = pend_a.p;
-      int round = 0;
-      // infinite sites: the first round over all slots against one table of
-      // its candidates (drivers first); the later rounds' tables are sized
-      // by what it leaves pending
+    // ---- infinite sites, and loci drawn where the cell has no allele left.
+    // Infinite sites: the first round over all slots against one table of
+    // its candidates (drivers first), read back once to size the later
+    // rounds' tables; every later round runs in one cooperative launch.
+    DBuf<pg::TailCtl> tail_ctl;
+    const bool unique = e->infinite_sites;
+    if ((unique || pl->has_cna) && n_snv + n_id > 0) {
+      const uint32_t n_slots = uint32_t(n_snv + n_id);
+      uint32_t n_tail = 0;
+      pg::TailArgs ta{};
+      ta.unique = unique ? 1 : 0;
+      DBuf<uint32_t> pend_a, pend_b, hkeys, ckeys, cvals, hpos;
       DBuf<unsigned long long> first;
-      uint32_t fmask = 0;
       if (unique) {
         uint64_t fcap = 1024;
         while (fcap < 2 * n_all) fcap <<= 1;
         require(fcap <= (uint64_t(1) << 32), "too many mutations for one placement call");
         first = DBuf<unsigned long long>(P, fcap);
-        fmask = uint32_t(fcap - 1);
+        const uint32_t fmask = uint32_t(fcap - 1);
+        pend_a = DBuf<uint32_t>(P, n_slots);
+        DBuf<uint32_t> n_next(P, 1);
+        DBuf<uint8_t> lost(P, n_slots);
         ck(cudaMemsetAsync(first.p, 0xff, sizeof(unsigned long long) * fcap, st), "memset");
         ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-        pg::sites_first_round(locus.p, n_pend, locus.p + n_snv + n_id, uint32_t(drv.size()), first.p, fmask, next,
-                              n_next.p, err.p, st);
-        uint32_t nn = 0;
-        ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
+        pg::sites_first_round(locus.p, n_slots, locus.p + n_slots, uint32_t(drv.size()), first.p, fmask, lost.p,
+                              pend_a.p, n_next.p, err.p, st);
+        ck(cudaMemcpyAsync(&n_tail, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
         ck(cudaStreamSynchronize(st), "first round");
-        if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, nn, 1,
-                                           err.p, st);
-        pending = next;
-        next = pend_b.p;
-        n_pend = nn;
-        round = 1;
+        uint32_t cap = 1024;
+        while (cap < 2 * uint64_t(n_tail)) cap <<= 1;
+        pend_b = DBuf<uint32_t>(P, n_tail);
+        hpos = DBuf<uint32_t>(P, n_tail);
+        hkeys = DBuf<uint32_t>(P, cap); ckeys = DBuf<uint32_t>(P, cap); cvals = DBuf<uint32_t>(P, cap);
+        ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+        ta.redraw_first = 1;
+        ta.round0 = 1;
+        ta.hkeys = hkeys.p; ta.hmask = cap - 1;
+        ta.ckeys = ckeys.p; ta.cvals = cvals.p; ta.cmask = cap - 1;
+        ta.hpos = hpos.p;
+        ta.first = first.p; ta.fmask = fmask;
+      } else {
+        // loci without an allele: round 0 looks at every slot
+        n_tail = n_slots;
+        pend_a = DBuf<uint32_t>(P, n_slots);
+        pend_b = DBuf<uint32_t>(P, n_slots);
+        ta.identity_first = 1;
+        ta.round0 = 0;
       }
-      uint32_t cap = 1024;
-      while (cap < 2 * uint64_t(n_pend)) cap <<= 1;
-      DBuf<uint32_t> hkeys(P, unique ? cap : 1), ckeys(P, unique ? cap : 1), cvals(P, unique ? cap : 1);
-      if (unique) ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-      // Rounds with many pending slots read their count on the host; below
-      // ROUND_TAIL pending slots, groups of ROUND_GROUP rounds run with the
-      // counts in device memory (the grids sized by the group's first count,
-      // which later rounds never exceed), with one host read per group.
-      constexpr uint32_t ROUND_TAIL = 1u << 20;
-      constexpr int ROUND_GROUP = 16;
-      DBuf<uint32_t> counts(P, ROUND_GROUP);
-      while (n_pend > 0) {
-        require(round < 256, unique ? "infinite sites model: no free locus left for some mutations"
-                                    : "no allele left where some mutations were drawn");
-        if (n_pend > ROUND_TAIL) {
-          ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-          if (unique) {
-            ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-            ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-            pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1, lost.p, next,
-                            n_next.p, err.p, st, nullptr, first.p, fmask);
-          } else {
-            pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_next.p, st);
-          }
-          uint32_t nn = 0;
-          ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-          ck(cudaStreamSynchronize(st), "redraw round");
-          if (nn) pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next,
-                                             nn, 1, err.p, st);
-          pending = next;
-          next = (next == pend_a.p) ? pend_b.p : pend_a.p;
-          n_pend = nn;
-          ++round;
-          continue;
-        }
-        uint32_t ctail = 1024;                 // candidate table of the group, in the full table's buffers
-        while (ctail < 2 * n_pend) ctail <<= 1;
-        ck(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * ROUND_GROUP, st), "memset");
-        for (int g = 0; g < ROUND_GROUP; ++g) {
-          const uint32_t* n_dev = g == 0 ? nullptr : counts.p + g - 1;
-          uint32_t* n_out = counts.p + g;
-          if (unique) {
-            ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
-            ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
-            pg::sites_round(locus.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, ctail - 1, lost.p, next,
-                            n_out, err.p, st, n_dev, first.p, fmask);
-          } else {
-            pg::sites_collect_invalid(locus.p, pending, n_pend, next, n_out, st, n_dev);
-          }
-          pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), next, n_pend,
-                                     1, err.p, st, n_out);
-          pending = next;
-          next = (next == pend_a.p) ? pend_b.p : pend_a.p;
-        }
-        uint32_t nn = 0;
-        ck(cudaMemcpyAsync(&nn, counts.p + ROUND_GROUP - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-        ck(cudaStreamSynchronize(st), "redraw rounds");
-        n_pend = nn;
-        round += ROUND_GROUP;
+      ta.list[0] = pend_a.p;
+      ta.list[1] = pend_b.p;
+      if (n_tail) {
+        tail_ctl = DBuf<pg::TailCtl>(P, 1);
+        pg::TailCtl c0{};
+        c0.count[0] = n_tail;
+        ck(cudaMemcpyAsync(tail_ctl.p, &c0, sizeof(c0), cudaMemcpyHostToDevice, st), "rounds");
+        if (const char* msg = pg::sites_tail(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), ta, n_tail, tail_ctl.p,
+                                             err.p, st))
+          throw std::runtime_error(msg);
       }
     }
     // ---- sort by locus
@@ -1391,6 +1363,14 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     ck(cudaGetLastError(), "placement kernels");
     uint32_t err_h = 0;
     ck(cudaMemcpy(&err_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost), "error flag");
+    if (tail_ctl.p) {
+      pg::TailCtl c{};
+      ck(cudaMemcpy(&c, tail_ctl.p, sizeof(c), cudaMemcpyDeviceToHost), "rounds");
+      if (c.status & pg::TAIL_BARRIER_TIMEOUT) throw std::runtime_error("a grid barrier of the redraw rounds timed out");
+      require(!(c.status & pg::TAIL_ROUNDS_EXHAUSTED), unique ? "infinite sites model: no free locus left for some mutations"
+                                                              : "no allele left where some mutations were drawn");
+      pl->redraw_rounds = c.rounds;
+    }
     if (err_h & pg::ERR_EMPTY_CLASS) throw std::runtime_error("a drawn mutation class has no indexed positions");
     if (err_h & pg::ERR_CAPACITY) throw std::runtime_error("internal hash table capacity exceeded");
     engine_retain(e);
@@ -1512,6 +1492,17 @@ pg_status pg_placed_set_samples(pg_placed* p, uint32_t n_samples, const int32_t*
     p->leaf_cls = std::move(leaf_cls);
     p->n_samples = n_samples;
   });
+}
+
+pg_status pg_engine_index_ms(const pg_engine* e, float* ms) {
+  return guarded([&] {
+    require(e && ms, "NULL argument");
+    for (int i = 0; i < 4; ++i) ms[i] = e->index_ms[i];
+  });
+}
+
+pg_status pg_placed_redraw_rounds(const pg_placed* p, uint32_t* rounds) {
+  return guarded([&] { require(p && rounds, "NULL argument"); *rounds = p->redraw_rounds; });
 }
 
 pg_status pg_placed_kernel_ms(const pg_placed* p, float* ms) {

@@ -88,6 +88,17 @@ __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
   return d;
 }
+// base-2 exponential and logarithm (the PTX approximate instructions, FTZ)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 #define PG_F2OP(NAME, OP)                                                                                        \
   __device__ __forceinline__ float2 NAME(float2 a, float2 b) {                                                \
     float2 d;                                                                                                  \
@@ -136,11 +147,13 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
   constexpr uint32_t KH = (K + 1) / 2;
   float2 cst[KH], lv[KH], l1v[KH], w[J][KH];
   auto at = [&](uint32_t k, uint32_t off, float pad) { return k < K ? s_row[off + k] : pad; };
+  // the log-domain terms in base 2 (ex2 / lg2 directly, the NLL scaled back by ln 2)
+  constexpr float LOG2E = 1.4426950408889634f, LN2 = 0.6931471805599453f;
 #pragma unroll
   for (uint32_t h = 0; h < KH; ++h) {
-    cst[h] = make_float2(at(2 * h, 0, 0.f), at(2 * h + 1, 0, -INFINITY));
-    lv[h] = make_float2(at(2 * h, K, 0.f), at(2 * h + 1, K, 0.f));
-    l1v[h] = make_float2(at(2 * h, 2 * K, 0.f), at(2 * h + 1, 2 * K, 0.f));
+    cst[h] = make_float2(LOG2E * at(2 * h, 0, 0.f), at(2 * h + 1, 0, -INFINITY) * LOG2E);
+    lv[h] = make_float2(LOG2E * at(2 * h, K, 0.f), LOG2E * at(2 * h + 1, K, 0.f));
+    l1v[h] = make_float2(LOG2E * at(2 * h, 2 * K, 0.f), LOG2E * at(2 * h + 1, 2 * K, 0.f));
 #pragma unroll
     for (uint32_t j = 0; j < J; ++j)
       w[j][h] = make_float2(s_row[3 * K + 2 * h * J + j], 2 * h + 1 < K ? s_row[3 * K + (2 * h + 1) * J + j] : 0.f);
@@ -175,13 +188,13 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
     float sum = 0.f;
 #pragma unroll
     for (uint32_t h = 0; h < KH; ++h) {
-      e[h] = make_float2(__expf(u[h].x - umax), __expf(u[h].y - umax));
+      e[h] = make_float2(ex2_approx(u[h].x - umax), ex2_approx(u[h].y - umax));
       q[h] = f2mul(make_float2(fmaxf(m[h].x, 1e-30f), fmaxf(m[h].y, 1e-30f)), e[h]);
       sum += q[h].x;
       sum += q[h].y;
     }
     const float inv = __fdividef(1.f, sum);
-    nll -= umax + __logf(sum);
+    nll -= umax + lg2_approx(sum);
     const float2 inv2 = make_float2(inv, inv);
 #pragma unroll
     for (uint32_t h = 0; h < KH; ++h) {
@@ -209,7 +222,7 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
   for (; i < i1; i += CAL_THREADS) site(float(__ldg(a.alt + i)), float(__ldg(a.depth + i)), __ldg(a.cls + i));
   // block partial: warp trees, then a compensated sum over the warps
   float acc[NV];
-  acc[0] = nll;
+  acc[0] = nll * LN2;
 #pragma unroll
   for (uint32_t k = 0; k < K; ++k) {
     const bool hi = k & 1;

@@ -11,11 +11,12 @@
 //
 // Here both are position lists in HBM, u32 absolute positions sorted
 // ascending within each class, built in two streaming passes over the 2-bit
-// genome: (1) per 1024-base tile, per class counts; (2) after a scan over
-// tiles, every warp walks its tile again and writes the positions whose rank
-// within their class is a multiple of the class stride.  Ranks inside a
-// 32-position step come from __match_any_sync, so the lists are in position
-// order without any sort.
+// genome: (1) per 4096-base unit, per class counts; (2) after a scan over
+// the units, every warp walks its unit again and writes the positions whose
+// rank within their class is a multiple of the class stride.  Positions are
+// classified 32 at a time per lane as bit masks (one per class), counted
+// with popcounts and warp reductions and numbered by a lane prefix sum, so
+// the lists come out in position order without any sort.
 #include <mutex>
 
 #include "pg_common.cuh"
@@ -25,11 +26,6 @@
 
 namespace pg {
 
-constexpr int TILE = 1024;
-constexpr int WIN_BEFORE = 8;
-constexpr int WIN_AFTER = 40;
-constexpr int WIN = TILE + WIN_BEFORE + WIN_AFTER;   // bytes per warp
-constexpr int WARPS = 8;
 
 // ------------------------------------------------------------ genome fill
 __global__ void k_genome_synth(uint32_t* __restrict__ words, uint64_t G, uint64_t nwords,
@@ -68,28 +64,74 @@ __global__ void k_genome_pack(uint32_t* __restrict__ words, const uint8_t* __res
   words[w] = out;
 }
 
+// unknown bases (N) are bits of nmask (NULL: none), one bit per position
+__device__ __forceinline__ bool base_unknown(const uint32_t* __restrict__ nmask, uint64_t q) {
+  return nmask && ((__ldg(nmask + (q >> 5)) >> (q & 31u)) & 1u);
+}
+
 // ------------------------------------------------------------ class families
-// SBS: one family, the trinucleotide context of p (needs both neighbours in
-// the same chromosome).
+// Both indices classify every position of the genome from the bases around
+// it.  A lane classifies 32 consecutive positions at once with bit masks
+// (bit i for position base + i): the bases as two bit planes (the low and
+// the high bit of the 2-bit code), a validity plane (known bases of the
+// position's chromosome), and from these one mask per class.  Features are
+// computed on 64-bit windows (bit j = position q0 + j, q0 = base - 16 or
+// base) whose bits 16..31 are the window's 16 positions; classes are
+// bitwise functions of the features, so the two windows' features are
+// packed side by side into 32-bit position masks first.
+struct Planes {
+  uint64_t p0, p1;   // low and high bit of each base
+  uint64_t v;        // known base inside the position's chromosome
+};
+
+__device__ __forceinline__ uint64_t eq_shift(const Planes& w, int s) {   // base(j) == base(j + s), both valid
+  return w.v & (w.v >> s) & ~((w.p0 ^ (w.p0 >> s)) | (w.p1 ^ (w.p1 >> s)));
+}
+
+__device__ __forceinline__ uint32_t pos16(uint64_t x) { return uint32_t(x >> 16) & 0xFFFFu; }
+
+// SBS: one family, the pyrimidine-centred trinucleotide context of p (p - 1,
+// p and p + 1 known and in p's chromosome; p not in a region to avoid).
+// Context s*16 + a*4 + c: a forward-strand centre C (s 0) or T (s 1) with
+// 5' base a and 3' base c, or a reverse-strand centre G (s 0) or A (s 1)
+// whose complemented flanks read a, c on the pyrimidine strand.
 struct SbsFamilies {
-  static constexpr int NF = 1;
   static constexpr int NC = N_CTX;
+  static constexpr int NF = 7;
   static constexpr bool AVOIDABLE = true;    // positions of the regions to avoid are not indexed
-  template <class Get>
-  __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
-    out[0] = -1;
-    if (p <= cs || p + 1 >= ce) return;
-    const uint32_t x = get(p - 1), y = get(p), z = get(p + 1);
-    if (x > 3u || y > 3u || z > 3u) return;          // an unknown base (N) in the context
-    bool fwd;
-    out[0] = context_of(x, y, z, &fwd);
+  // features: 0 indexable; 1, 2 planes of p - 1; 3, 4 of p; 5, 6 of p + 1
+  __device__ static void features(const Planes& w, uint64_t avoid, uint32_t* f, uint32_t keep, int sh) {
+    f[0] |= (pos16(w.v & (w.v << 1) & (w.v >> 1) & ~avoid) << sh) & keep;
+    f[1] |= (pos16(w.p0 << 1) << sh) & keep;
+    f[2] |= (pos16(w.p1 << 1) << sh) & keep;
+    f[3] |= (pos16(w.p0) << sh) & keep;
+    f[4] |= (pos16(w.p1) << sh) & keep;
+    f[5] |= (pos16(w.p0 >> 1) << sh) & keep;
+    f[6] |= (pos16(w.p1 >> 1) << sh) & keep;
+  }
+  template <class Sink>
+  __device__ static void classes(const uint32_t* f, Sink sink) {
+    const uint32_t ok = f[0];
+    // forward centre C (s 0), T (s 1); reverse centre G (-> C), A (-> T)
+    auto cen = [&](int s) { return s ? (f[3] & f[4]) : (f[3] & ~f[4]); };
+    auto rev = [&](int s) { return s ? (~f[3] & ~f[4]) : (~f[3] & f[4]); };
+    // base at p - 1 (x) / p + 1 (z) equal to b
+    auto ex = [&](int b) { return ((b & 1) ? f[1] : ~f[1]) & ((b & 2) ? f[2] : ~f[2]); };
+    auto ez = [&](int b) { return ((b & 1) ? f[5] : ~f[5]) & ((b & 2) ? f[6] : ~f[6]); };
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          sink(s * 16 + a * 4 + c, ok & ((cen(s) & ex(a) & ez(c)) | (rev(s) & ez(3 - a) & ex(3 - c))));
   }
 };
 
 // ID83 (COSMIC order).  A position p (the first deleted base, or the base
-// before which bases are inserted; p-1 is the anchor) belongs to at most one
-// class per family:
-//   F0  1-bp deletion at a homopolymer run start, run length 1..6+     (0-11)
+// before which bases are inserted; p-1 is the anchor, and both are known)
+// belongs to at most one class per family:
+//   F0  1-bp deletion at a homopolymer run start, run length h 1..6+  (0-11)
 //   F1  1-bp insertion at a run start, run length 1..5+               (12-23, idx 1-5)
 //   F2  1-bp C/G insertion with no adjacent C/G                       (12)
 //   F3  1-bp T/A insertion with no adjacent T/A                       (18)
@@ -99,147 +141,291 @@ struct SbsFamilies {
 //         m==0 -> 24+(l-2)*6, else 72+off(l)+m-1
 //   F8-11 l=2..5 insertion of one more unit at a tract start, r>=1   (48+(l-2)*6+min(r,5))
 //   F12-15 l=2..5 insertion of l random bases at a run start          (48+(l-2)*6)
+// The l-families need p..p+l-1 known and p not inside a tract (the l bases
+// before p differ from the unit).  With E_l(q) = base(q) == base(q + l),
+// both known: the run length from p is h >= k+1 iff E_1 holds at p..p+k-1;
+// the repeat count r >= k+1 iff E_l holds at p..p+kl-1 (capped at 6); the
+// microhomology m >= j iff E_l holds at p..p+j-1; "inside a tract" iff E_l
+// holds at p-l..p-1.
 struct IdFamilies {
-  static constexpr int NF = 16;
   static constexpr int NC = N_ID;
+  static constexpr int NF = 43;
   static constexpr bool AVOIDABLE = false;
-  template <class Get>
-  __device__ static void classes(Get get, uint32_t p, uint32_t cs, uint32_t ce, int* out) {
+  // features: 0 p and p-1 known; 1 run start; 2, 3 base of p / p-1 is A or T;
+  // 4..8 h >= 2..6; then per l = 2..5: the family applies, r >= 2..6, m >= 1..l-1
+  __device__ static void features(const Planes& w, uint64_t, uint32_t* f, uint32_t keep, int sh) {
+    auto put = [&](int x, uint64_t m) { f[x] |= (pos16(m) << sh) & keep; };
+    const uint64_t v = w.v, e1 = eq_shift(w, 1), bv = v & (v << 1), pt = ~(w.p0 ^ w.p1);
+    put(0, bv);
+    put(1, bv & ~(e1 << 1));
+    put(2, pt);
+    put(3, pt << 1);
+    uint64_t h = e1;
+    put(4, h);
 #pragma unroll
-    for (int f = 0; f < NF; ++f) out[f] = -1;
-    if (p <= cs || p >= ce) return;
-    const uint32_t b = get(p), prev = get(p - 1);
-    if (b > 3u || prev > 3u) return;                 // the site or its anchor is unknown (N)
-    int h = 1;
-    while (h < 6 && get(p + h) == b) ++h;
-    const bool runstart = prev != b;
-    const bool pyrT = (b == 3u || b == 0u);
-    if (runstart) {
-      out[0] = (pyrT ? 6 : 0) + h - 1;
-      out[1] = 12 + (pyrT ? 6 : 0) + (h < 5 ? h : 5);
-#pragma unroll
-      for (int l = 2; l <= 5; ++l) out[12 + l - 2] = 48 + (l - 2) * 6;
-    }
-    if (b != 1u && b != 2u && prev != 1u && prev != 2u) out[2] = 12;
-    if (b != 0u && b != 3u && prev != 0u && prev != 3u) out[3] = 18;
-    const int mh_off[4] = {0, 1, 3, 6};
+    for (int k = 1; k <= 4; ++k) { h &= e1 >> k; put(4 + k, h); }
+    int o = 9;
 #pragma unroll
     for (int l = 2; l <= 5; ++l) {
-      bool valid = true;
-      for (int i = 0; i < l; ++i) valid = valid && get(p + i) != BASE_INVALID;
-      if (!valid) continue;
-      if (p >= cs + uint32_t(l)) {
-        bool same = true;
-        for (int i = 0; i < l; ++i) same = same && get(p - l + i) == get(p + i);
-        if (same) continue;                       // not the start of the tract
-      }
-      int r = 1;
-      while (r < 6) {
-        bool same = true;
-        for (int i = 0; i < l; ++i) same = same && get(p + r * l + i) == get(p + i);
-        if (!same) break;
-        ++r;
-      }
-      if (r >= 2) {
-        out[4 + l - 2] = 24 + (l - 2) * 6 + (r - 1 < 5 ? r - 1 : 5);
-      } else {
-        int m = 0;
-        while (m < l && get(p + l + m) == get(p + m)) ++m;
-        out[4 + l - 2] = (m == 0) ? 24 + (l - 2) * 6 : 72 + mh_off[l - 2] + m - 1;
-      }
-      out[8 + l - 2] = 48 + (l - 2) * 6 + (r < 5 ? r : 5);
+      const uint64_t el = eq_shift(w, l);
+      uint64_t vl = v, u = el, sb = el << 1;
+#pragma unroll
+      for (int i = 1; i < l; ++i) { vl &= v >> i; u &= el >> i; sb &= el << (i + 1); }
+      put(o, bv & vl & ~sb);
+      uint64_t r = u;
+      put(o + 1, r);
+#pragma unroll
+      for (int q = 2; q <= 5; ++q) { r &= u >> ((q - 1) * l); put(o + q, r); }
+      uint64_t m = el;
+      put(o + 6, m);
+#pragma unroll
+      for (int j = 2; j < l; ++j) { m &= el >> (j - 1); put(o + 5 + j, m); }
+      o += 5 + l;
+    }
+  }
+  template <class Sink>
+  __device__ static void classes(const uint32_t* f, Sink sink) {
+    const uint32_t bv = f[0], rs = f[1], pt = f[2], ptp = f[3];
+    const uint32_t hx[7] = {0u, ~f[4], f[4] & ~f[5], f[5] & ~f[6], f[6] & ~f[7], f[7] & ~f[8], f[8]};  // h exactly
+#pragma unroll
+    for (int c = 0; c < 12; ++c) sink(c, rs & (c >= 6 ? pt : ~pt) & hx[c % 6 + 1]);
+#pragma unroll
+    for (int py = 0; py < 2; ++py)
+#pragma unroll
+      for (int j = 1; j <= 5; ++j) sink(12 + py * 6 + j, rs & (py ? pt : ~pt) & (j < 5 ? hx[j] : f[7]));
+    sink(12, bv & pt & ptp);
+    sink(18, bv & ~pt & ~ptp);
+    sink(48, rs); sink(54, rs); sink(60, rs); sink(66, rs);
+    constexpr int mh_off[4] = {0, 1, 3, 6};
+    int o = 9;
+#pragma unroll
+    for (int l = 2; l <= 5; ++l) {
+      const uint32_t val = f[o], r2 = f[o + 1], r3 = f[o + 2], r4 = f[o + 3], r5 = f[o + 4], r6 = f[o + 5];
+      const int b4 = 24 + (l - 2) * 6, b8 = 48 + (l - 2) * 6;
+      const uint32_t x2 = val & r2 & ~r3, x3 = val & r3 & ~r4, x4 = val & r4 & ~r5, nr = val & ~r2;
+      sink(b4 + 1, x2); sink(b4 + 2, x3); sink(b4 + 3, x4); sink(b4 + 4, val & r5 & ~r6); sink(b4 + 5, val & r6);
+      sink(b4, nr & ~f[o + 6]);
+#pragma unroll
+      for (int j = 1; j < l; ++j) sink(72 + mh_off[l - 2] + j - 1, nr & f[o + 5 + j] & (j + 1 < l ? ~f[o + 6 + j] : ~0u));
+      sink(b8 + 1, nr); sink(b8 + 2, x2); sink(b8 + 3, x3); sink(b8 + 4, x4); sink(b8 + 5, val & r5);
+      o += 5 + l;
     }
   }
 };
 
-// ------------------------------------------------------------ index passes
-struct WarpWindow {
-  uint8_t* s;      // WIN bytes
-  uint32_t start;  // absolute position of s[0]
-};
+// ------------------------------------------------------------ index scans
+// A lane takes 32 positions per round, a warp 32 lanes (1024 positions) per
+// round and IX_ROUNDS rounds per unit; the count pass writes one count per
+// (class, unit), and the emit pass, after a scan of that table over the
+// units, numbers each class's positions in order: units in order, within a
+// unit the rounds, within a round the lanes, within a lane the positions.
+// Position p is written to its class's list when its number is a multiple
+// of the class stride.
+constexpr uint32_t IX_LANE_POS = 32;
+constexpr uint32_t IX_ROUNDS = 4;
+constexpr uint32_t IX_UNIT = 32 * IX_LANE_POS * IX_ROUNDS;   // 4096 positions
+constexpr int IX_WARPS = 8;
 
-// unknown bases (N) are bits of nmask (NULL: none), one bit per position
-__device__ __forceinline__ bool base_unknown(const uint32_t* __restrict__ nmask, uint32_t q) {
-  return nmask && ((__ldg(nmask + (q >> 5)) >> (q & 31u)) & 1u);
+// even bits of x to the low half, odd bits to the high half (an inverse
+// perfect shuffle in four swap steps)
+__device__ __forceinline__ uint32_t unshuffle32(uint32_t x) {
+  uint32_t t = (x ^ (x >> 1)) & 0x22222222u; x ^= t ^ (t << 1);
+  t = (x ^ (x >> 2)) & 0x0C0C0C0Cu; x ^= t ^ (t << 2);
+  t = (x ^ (x >> 4)) & 0x00F000F0u; x ^= t ^ (t << 4);
+  t = (x ^ (x >> 8)) & 0x0000FF00u; x ^= t ^ (t << 8);
+  return x;
 }
 
-__device__ __forceinline__ void load_window(const uint32_t* __restrict__ g, const uint32_t* __restrict__ nmask,
-                                            uint64_t G, uint32_t tile_start, uint8_t* s, int lane) {
-  const int64_t w0 = int64_t(tile_start) - WIN_BEFORE;
-  for (int i = lane; i < WIN; i += 32) {
-    const int64_t q = w0 + i;
-    s[i] = (q >= 0 && uint64_t(q) < G && !base_unknown(nmask, uint32_t(q))) ? uint8_t(base_at(g, uint32_t(q)))
-                                                                           : uint8_t(BASE_INVALID);
-  }
-  __syncwarp();
+// bits [lo, hi) of a 64-bit window, clamped to the window
+__device__ __forceinline__ uint64_t range_bits(int64_t lo, int64_t hi) {
+  lo = lo < 0 ? 0 : lo;
+  hi = hi > 64 ? 64 : hi;
+  if (hi <= lo) return 0;
+  const uint64_t top = hi >= 64 ? ~0ull : ((1ull << hi) - 1ull);
+  return top & ~((1ull << lo) - 1ull);
 }
 
-// mode 0: count; mode 1: emit positions
+// unknown base (N) masks and the like: 1 bit per position, bit q % 32 of word q / 32
+__device__ __forceinline__ uint32_t mask_word(const uint32_t* __restrict__ m, int64_t wi, uint64_t nw) {
+  return (m && wi >= 0 && uint64_t(wi) < nw) ? __ldg(m + wi) : 0u;
+}
+
+// warps per block: the emit pass keeps per warp the round's lane masks of
+// the classes that write (shared memory), so its blocks are smaller
+__host__ __device__ constexpr int ix_warps(int mode) { return mode == 0 ? IX_WARPS : IX_WARPS / 2; }
+
 template <class F, int MODE>
-__global__ void __launch_bounds__(256) k_index_pass(const uint32_t* __restrict__ g,
-                                                    const uint32_t* __restrict__ nmask,
-                                                    const uint32_t* __restrict__ amask, uint64_t G,
-                                                    const uint32_t* __restrict__ chr_off, int n_chr,
-                                                    uint32_t ntiles, uint32_t* __restrict__ cnt,
-                                                    const uint32_t* __restrict__ stride,
-                                                    const uint64_t* __restrict__ list_off,
-                                                    const uint32_t* __restrict__ list_len,
-                                                    uint32_t* __restrict__ lists) {
-  __shared__ uint8_t s_win[WARPS][WIN];
-  __shared__ uint32_t s_run[WARPS][F::NC];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t tile = blockIdx.x * WARPS + warp;
-  if (tile >= ntiles) return;
-  const uint32_t tile_start = tile * TILE;
-  for (int k = lane; k < F::NC; k += 32)
-    s_run[warp][k] = MODE == 0 ? 0u : cnt[uint64_t(k) * ntiles + tile];
-  load_window(g, nmask, G, tile_start, s_win[warp], lane);
-  // chromosome of the tile start
-  int c = 0;
-  {
-    int lo = 0, hi = n_chr;            // largest c with chr_off[c] <= tile_start
-    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (__ldg(chr_off + mid) <= tile_start) lo = mid; else hi = mid; }
-    c = lo;
-  }
-  const uint8_t* s = s_win[warp];
-  for (int step = 0; step < TILE / 32; ++step) {
-    const uint32_t p = tile_start + step * 32 + lane;
-    int cls[F::NF];
-    if (p < G) {
-      while (c + 1 < n_chr && p >= __ldg(chr_off + c + 1)) ++c;
-      const uint32_t cs = __ldg(chr_off + c), ce = __ldg(chr_off + c + 1);
-      auto get = [&](uint32_t q) -> uint32_t {
-        return (q >= cs && q < ce) ? uint32_t(s[q - tile_start + WIN_BEFORE]) : BASE_INVALID;
-      };
-      F::classes(get, p, cs, ce, cls);
-      if (F::AVOIDABLE && base_unknown(amask, p)) cls[0] = -1;   // inside a region to avoid
-    } else {
-#pragma unroll
-      for (int f = 0; f < F::NF; ++f) cls[f] = -1;
+__global__ void __launch_bounds__(32 * ix_warps(MODE)) k_index_scan(const uint32_t* __restrict__ g,
+                                                                   const uint32_t* __restrict__ nmask,
+                                                                   const uint32_t* __restrict__ amask, uint64_t G,
+                                                                   const uint32_t* __restrict__ chr_off, int n_chr,
+                                                                   uint32_t n_units, uint32_t* __restrict__ cnt,
+                                                                   const uint32_t* __restrict__ stride,
+                                                                   const uint64_t* __restrict__ list_off,
+                                                                   const uint32_t* __restrict__ list_len,
+                                                                   uint32_t* __restrict__ lists) {
+  constexpr int NS = (F::NC + 31) / 32;
+  constexpr uint32_t FULL = 0xffffffffu;
+  constexpr int W = ix_warps(MODE);
+  constexpr int QW = MODE == 1 ? W : 1, QN = MODE == 1 ? F::NC : 1;
+  __shared__ uint32_t s_stride[QN], s_len[QN];
+  __shared__ uint64_t s_off[QN];
+  // MODE 1, per warp: the classes of the round with a position to write
+  // (class | hits << 8) and their lane masks; per class the hits before its
+  // next written position and that position's index in the class list
+  __shared__ uint32_t s_qk[QW][QN], s_qmask[QW][QN][32];
+  __shared__ uint32_t s_dist[QW][QN], s_kidx[QW][QN];
+  if (MODE == 1) {
+    for (int k = threadIdx.x; k < F::NC; k += blockDim.x) {
+      s_stride[k] = stride[k];
+      s_len[k] = list_len[k];
+      s_off[k] = list_off[k];
     }
+    __syncthreads();
+  }
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t unit = blockIdx.x * W + w;
+  if (unit >= n_units) return;
+  // MODE 0: per class k the count, held by lane k % 32 in slot k / 32
+  uint32_t run[NS];
 #pragma unroll
-    for (int f = 0; f < F::NF; ++f) {
-      const int k = cls[f];
-      const uint32_t peers = __match_any_sync(0xffffffffu, k);
-      if (k >= 0) {
-        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-        const uint32_t leader = __ffs(peers) - 1;
-        if (MODE == 1) {
-          const uint32_t r = s_run[warp][k] + rank;
-          const uint32_t sd = stride[k];
-          if (r % sd == 0) {
-            const uint32_t idx = r / sd;
-            if (idx < list_len[k]) lists[list_off[k] + idx] = p;
+  for (int s = 0; s < NS; ++s) run[s] = 0;
+  if (MODE == 1) {
+    for (uint32_t k = lane; k < uint32_t(F::NC); k += 32) {
+      const uint32_t r0 = cnt[uint64_t(k) * n_units + unit], sd = s_stride[k];
+      const uint32_t q = r0 / sd, rem = r0 - q * sd;
+      s_dist[MODE == 1 ? w : 0][k] = rem ? sd - rem : 0u;
+      s_kidx[MODE == 1 ? w : 0][k] = q + (rem ? 1u : 0u);
+    }
+    __syncwarp();
+  }
+  const uint32_t qw = MODE == 1 ? w : 0;
+  const uint64_t n_gw = (G + 15) / 16, n_mw = (G + 31) / 32;
+  for (uint32_t round = 0; round < IX_ROUNDS; ++round) {
+    const uint64_t wbase = uint64_t(unit) * IX_UNIT + uint64_t(round) * (32 * IX_LANE_POS);
+    if (wbase >= G) break;
+    const uint64_t base = wbase + uint64_t(lane) * IX_LANE_POS;
+    uint32_t f[F::NF];
+#pragma unroll
+    for (int x = 0; x < F::NF; ++x) f[x] = 0;
+    if (base < G) {
+      // bases [base - 16, base + 64) as bit planes, 16 positions per half word
+      uint32_t lo[5], hi[5];
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const int64_t wi = int64_t(base >> 4) - 1 + i;
+        const uint32_t u = unshuffle32((wi >= 0 && uint64_t(wi) < n_gw) ? __ldg(g + wi) : 0u);
+        lo[i] = u & 0xFFFFu;
+        hi[i] = u >> 16;
+      }
+      uint32_t nw[3], aw[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const int64_t wi = int64_t(base >> 5) - 1 + i;
+        nw[i] = mask_word(nmask, wi, n_mw);
+        aw[i] = F::AVOIDABLE ? mask_word(amask, wi, n_mw) : 0u;
+      }
+      // chromosome of base: the largest c with chr_off[c] <= base
+      int c = 0;
+      {
+        int lo_c = 0, hi_c = n_chr;
+        while (hi_c - lo_c > 1) {
+          const int mid = (lo_c + hi_c) >> 1;
+          if (__ldg(chr_off + mid) <= base) lo_c = mid; else hi_c = mid;
+        }
+        c = lo_c;
+      }
+      // one segment per chromosome that holds some of the lane's positions
+      for (; c < n_chr; ++c) {
+        const uint64_t cs = __ldg(chr_off + c), ce = __ldg(chr_off + c + 1);
+        if (cs >= base + IX_LANE_POS) break;
+        if (ce <= base) continue;
+        const uint32_t keep = uint32_t(range_bits(int64_t(cs) - int64_t(base), int64_t(ce) - int64_t(base)));
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int64_t q0 = int64_t(base) - 16 + 16 * half;
+          Planes wd;
+          wd.p0 = uint64_t(lo[half]) | (uint64_t(lo[half + 1]) << 16) | (uint64_t(lo[half + 2]) << 32) |
+                  (uint64_t(lo[half + 3]) << 48);
+          wd.p1 = uint64_t(hi[half]) | (uint64_t(hi[half + 1]) << 16) | (uint64_t(hi[half + 2]) << 32) |
+                  (uint64_t(hi[half + 3]) << 48);
+          const uint64_t nm = half == 0 ? (uint64_t(nw[0] >> 16) | (uint64_t(nw[1]) << 16) | (uint64_t(nw[2]) << 48))
+                                        : (uint64_t(nw[1]) | (uint64_t(nw[2]) << 32));
+          const uint64_t am = half == 0 ? (uint64_t(aw[0] >> 16) | (uint64_t(aw[1]) << 16) | (uint64_t(aw[2]) << 48))
+                                        : (uint64_t(aw[1]) | (uint64_t(aw[2]) << 32));
+          wd.v = ~nm & range_bits(int64_t(cs) - q0, int64_t(ce) - q0);
+          F::features(wd, am, f, keep, 16 * half);
+        }
+      }
+    }
+    uint32_t nq = 0;
+    F::classes(f, [&](int k, uint32_t m) {
+      const uint32_t t = __reduce_add_sync(FULL, uint32_t(__popc(m)));
+      if constexpr (MODE == 0) {
+        if (lane == (uint32_t(k) & 31u)) run[k >> 5] += t;
+      } else {
+        if (t == 0) return;
+        const uint32_t d = s_dist[qw][k];                   // hits before the next written one
+        if (t <= d) {
+          if (lane == 0) s_dist[qw][k] = d - t;
+          return;
+        }
+        s_qmask[qw][nq][lane] = m;
+        if (lane == 0) s_qk[qw][nq] = uint32_t(k) | (t << 8);
+        ++nq;
+      }
+    });
+    if constexpr (MODE == 1) {
+      __syncwarp();
+      // the classes that write a position this round (one copy of the code)
+      for (uint32_t qi = 0; qi < nq; ++qi) {
+        const uint32_t qk = s_qk[qw][qi], k = qk & 0xffu, t = qk >> 8;
+        const uint32_t m = s_qmask[qw][qi][lane], c = __popc(m);
+        const uint32_t d = s_dist[qw][k], ki = s_kidx[qw][k], sd = s_stride[k];
+        // hit numbers and their gaps within a round are below 1024 (32 lanes
+        // x 32 positions): every quotient below is of a number < 1024
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= uint32_t(o)) incl += y;
+        }
+        const uint32_t ex = incl - c;                          // the lane's hits are numbered ex .. ex + c - 1
+        uint32_t hit = d, idx = ki;                            // the lane's first written hit and its index
+        if (ex > d) {
+          const uint32_t gap = ex - d;
+          const uint32_t q = gap <= sd ? 1u : (gap + sd - 1u) / sd;
+          idx = ki + q;
+          hit = (uint64_t(d) + uint64_t(q) * sd >= uint64_t(ex) + c) ? ex + c : d + q * sd;
+        }
+        if (hit < ex + c) {
+          const uint32_t len = s_len[k];
+          const uint64_t off = s_off[k];
+          uint32_t mm = m, at = ex;
+          while (true) {
+            for (; at < hit; ++at) mm &= mm - 1u;
+            if (idx < len) lists[off + idx] = uint32_t(base + uint32_t(__ffs(mm) - 1));
+            if (uint64_t(hit) + sd >= uint64_t(ex) + c) break;
+            hit += sd;
+            ++idx;
           }
         }
-        __syncwarp(peers);
-        if (uint32_t(lane) == leader) s_run[warp][k] += __popc(peers);
+        if (lane == 0) {
+          const uint32_t span = t - 1u - d;                    // hits after the first written one
+          const uint32_t nk = (span < sd ? 0u : span / sd) + 1u;   // written this round
+          s_dist[qw][k] = uint32_t(uint64_t(d) + uint64_t(nk) * sd - t);
+          s_kidx[qw][k] = ki + nk;
+        }
+        __syncwarp();
       }
-      __syncwarp();
     }
   }
   if (MODE == 0) {
-    for (int k = lane; k < F::NC; k += 32) cnt[uint64_t(k) * ntiles + tile] = s_run[warp][k];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const uint32_t k = s * 32 + lane;
+      if (k < uint32_t(F::NC)) cnt[uint64_t(k) * n_units + unit] = run[s];
+    }
   }
 }
 
@@ -256,15 +442,16 @@ void genome_pack(uint32_t* words, const uint8_t* codes, uint64_t G, cudaStream_t
   k_genome_pack<<<unsigned((nwords + 255) / 256), 256, 0, st>>>(words, codes, G, nwords); note_launch();
 }
 
-uint32_t index_num_tiles(uint64_t G) { return uint32_t((G + TILE - 1) / TILE); }
+uint32_t index_num_tiles(uint64_t G) { return uint32_t((G + IX_UNIT - 1) / IX_UNIT); }
 
 template <class F>
 static void index_count_t(const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
                           const uint32_t* chr_off, int n_chr, uint32_t* cnt, uint32_t* part, uint32_t* totals,
                           cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_pass<F, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles, cnt,
-                                                                  nullptr, nullptr, nullptr, nullptr); note_launch();
+  k_index_scan<F, 0><<<(ntiles + IX_WARPS - 1) / IX_WARPS, 256, 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles,
+                                                                        cnt, nullptr, nullptr, nullptr, nullptr);
+  note_launch();
   scan_rows<uint32_t>(cnt, cnt, ntiles, F::NC, part, totals, st);
 }
 
@@ -273,9 +460,10 @@ static void index_emit_t(const uint32_t* g, const uint32_t* nmask, const uint32_
                          const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
                          const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_pass<F, 1><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles,
-                                                                  const_cast<uint32_t*>(cnt_scanned),
-                                                                  stride, list_off, list_len, lists); note_launch();
+  k_index_scan<F, 1><<<(ntiles + ix_warps(1) - 1) / ix_warps(1), 32 * ix_warps(1), 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles,
+                                                                        const_cast<uint32_t*>(cnt_scanned), stride,
+                                                                        list_off, list_len, lists);
+  note_launch();
 }
 
 void index_count(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
@@ -308,12 +496,13 @@ void genome_avoid_mask(const uint32_t* pos, uint64_t n, uint32_t* mask, cudaStre
 int index_num_classes(int which) { return which == 0 ? SbsFamilies::NC : IdFamilies::NC; }
 
 // ------------------------------------------------------------ allocation-free class counts
-// The count pass above writes one count per (class, tile) into a table the
+// The count pass above writes one count per (class, unit) into a table the
 // engine allocates.  This variant keeps that table in a fixed array of the
 // library's own device memory, so that a caller who may not allocate device
-// memory can still count the classes of a genome it holds.  The array is
-// sized for genomes up to NOALLOC_MAX_TILES tiles of 1024 bases (8 Mbp);
-// every GPU that loads the library holds it (2.7 MB) until the process ends.
+// memory can still count the classes of a genome it holds.  Genomes up to
+// NOALLOC_MAX_BASES (8 Mbp, 2048 units) are accepted; the array (2.7 MB,
+// NOALLOC_MAX_TILES entries per class) stays on every GPU that loads the
+// library until the process ends.
 static __device__ __align__(256) uint32_t g_noalloc_tile_counts[N_ID * NOALLOC_MAX_TILES];
 
 // per-class sum of the tile counts (one block per class)
@@ -342,7 +531,9 @@ static uint32_t* g_noalloc_addr[64] = {};
 
 const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const uint32_t* chr_off, int n_chr,
                                  uint64_t* totals, cudaStream_t st) {
-  if (G == 0 || G > uint64_t(NOALLOC_MAX_TILES) * TILE) return "genome length must be in [1, 8388608] bases";
+  constexpr uint64_t NOALLOC_MAX_BASES = uint64_t(NOALLOC_MAX_TILES) * 1024;
+  static_assert(NOALLOC_MAX_BASES / IX_UNIT <= NOALLOC_MAX_TILES, "count array too small");
+  if (G == 0 || G > NOALLOC_MAX_BASES) return "genome length must be in [1, 8388608] bases";
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return "no current CUDA device";
   uint32_t* scratch = nullptr;
@@ -363,15 +554,14 @@ const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const
   // an error left pending by earlier work on this thread is not this call's:
   // report it as such and leave it pending for its owner, launching nothing
   if (cudaPeekAtLastError() != cudaSuccess) return "a CUDA error from earlier work is pending; nothing was launched";
-  // every (class, tile) entry is written by the count pass: nothing to clear
+  // every (class, unit) entry is written by the count pass: nothing to clear
+  const uint32_t blocks = (ntiles + IX_WARPS - 1) / IX_WARPS;
   if (which == 0)
-    k_index_pass<SbsFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, nullptr, G, chr_off, n_chr, ntiles,
-                                                                              scratch,
-                                                                              nullptr, nullptr, nullptr, nullptr);
+    k_index_scan<SbsFamilies, 0><<<blocks, 256, 0, st>>>(g, nullptr, nullptr, G, chr_off, n_chr, ntiles, scratch,
+                                                         nullptr, nullptr, nullptr, nullptr);
   else
-    k_index_pass<IdFamilies, 0><<<(ntiles + WARPS - 1) / WARPS, 256, 0, st>>>(g, nullptr, nullptr, G, chr_off, n_chr, ntiles,
-                                                                             scratch,
-                                                                             nullptr, nullptr, nullptr, nullptr);
+    k_index_scan<IdFamilies, 0><<<blocks, 256, 0, st>>>(g, nullptr, nullptr, G, chr_off, n_chr, ntiles, scratch,
+                                                        nullptr, nullptr, nullptr, nullptr);
   k_class_totals<<<nc, 256, 0, st>>>(scratch, ntiles, totals);
   note_launch(2);
   if (cudaGetLastError() != cudaSuccess) return "launch of the count kernels failed";

@@ -130,16 +130,44 @@ void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint3
                            uint32_t* n_next, cudaStream_t st, const uint32_t* n_dev = nullptr);
 // first infinite-sites round over slots [0, n) and the drivers' loci:
 // `first` (fmask + 1 entries of 64 bits, all ones) ends holding the taken
-// loci; the losing slots go to next
+// loci; the losing slots go to next (lost: n bytes of scratch)
 void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
-                       unsigned long long* first, uint32_t fmask, uint32_t* next, uint32_t* n_next, uint32_t* err,
-                       cudaStream_t st);
+                       unsigned long long* first, uint32_t fmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
+                       uint32_t* err, cudaStream_t st);
 // a later round: a locus is taken when it is in the accepted set hkeys or
 // (first != NULL) in the first round's table
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
                  uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
                  uint32_t* err, cudaStream_t st, const uint32_t* n_dev = nullptr,
                  const unsigned long long* first = nullptr, uint32_t fmask = 0);
+// All redraw rounds after the first in one cooperative launch (k_sites_tail).
+// list[0] holds the n0 pending slots (identity_first: slots 0 .. n0 - 1, no
+// list); redraw_first: they are redrawn before the first round.  unique:
+// infinite sites (hkeys accepted set, ckeys/cvals candidate table, all
+// EMPTY on entry, capacities powers of two >= 2 n0; hpos n0 entries; first:
+// the first round's table or NULL); else only loci without an allele are
+// redrawn.  ctl (zeroed, count[0] = n0) reports the rounds and the status.
+constexpr uint32_t TAIL_MAX_ROUND = 256;
+enum : uint32_t { TAIL_ROUNDS_EXHAUSTED = 1u, TAIL_BARRIER_TIMEOUT = 2u };
+struct TailCtl {
+  uint32_t count[2];     // pending slots of the two lists
+  uint32_t bar_count, bar_gen;
+  uint32_t status;
+  uint32_t rounds;       // the round counter after the last round run
+};
+struct TailArgs {
+  uint32_t* list[2];
+  int identity_first, redraw_first, unique;
+  uint32_t round0;
+  uint32_t* hkeys; uint32_t hmask;
+  uint32_t* ckeys; uint32_t* cvals; uint32_t cmask;
+  uint32_t* hpos;
+  const unsigned long long* first; uint32_t fmask;
+};
+// returns nullptr, or a message when the launch could not be made
+const char* sites_tail(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
+                       const uint32_t* off_id, uint32_t n_snv, const TailArgs& a, uint32_t n0, TailCtl* ctl,
+                       uint32_t* err, cudaStream_t st);
 uint32_t sort_num_buckets(uint64_t G);
 // sort by (locus, slot) into `sorted`; keys: n 64-bit keys, recs: 2n
 // 16-byte words (the 32-byte records of the gather)

@@ -24,6 +24,8 @@
 //     a contested locus, rounds repeat until no collision is left.  From
 //     attempt RECLASS_ATTEMPTS on, the class is redrawn too (same signature),
 //     so a class whose positions are all taken cannot stall the rounds.
+#include <algorithm>
+
 #include "pg_common.cuh"
 #include "pg_rng.cuh"
 #include "pg_scan.cuh"
@@ -178,19 +180,25 @@ __device__ __forceinline__ void place_one(const PlaceTables& t, const PlaceOut& 
   }
 }
 
-__global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
-                        const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_id,
-                        const uint32_t* __restrict__ pending, uint32_t n_pending,
-                        const uint32_t* __restrict__ n_dev, int redraw, uint32_t* __restrict__ err) {
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= (n_dev ? *n_dev : n_pending)) return;
-  const uint32_t slot = pending ? pending[tid] : tid;
+// slot -> its (edge, epoch) cell and index there, then place_one
+__device__ __forceinline__ void place_slot(const PlaceTables& t, const PlaceOut& o, Key key,
+                                           const uint32_t* __restrict__ off_snv, const uint32_t* __restrict__ off_id,
+                                           uint32_t n_snv, uint32_t slot, int redraw, uint32_t* __restrict__ err) {
   const bool is_id = slot >= n_snv;
   const uint32_t i = is_id ? slot - n_snv : slot;
   const uint32_t ncell = (t.n_nodes + 1) * t.n_epochs;
   const uint32_t* off = is_id ? off_id : off_snv;
   const uint32_t q = find_cell(off, ncell, i);
   place_one(t, o, key, slot, is_id, q / t.n_epochs, q % t.n_epochs, i - off[q], redraw, err);
+}
+
+__global__ void k_place(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
+                        const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_id,
+                        const uint32_t* __restrict__ pending, uint32_t n_pending,
+                        const uint32_t* __restrict__ n_dev, int redraw, uint32_t* __restrict__ err) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (n_dev ? *n_dev : n_pending)) return;
+  place_slot(t, o, key, off_snv, off_id, n_snv, pending ? pending[tid] : tid, redraw, err);
 }
 
 // ------------------------------------------------------------ hash sets
@@ -231,19 +239,30 @@ __device__ __forceinline__ uint32_t hset_insert(uint32_t* __restrict__ keys, uin
 // smallest pending slot wins a free locus).  The table then holds exactly
 // the taken loci (drivers and the round's winners), so the later rounds test
 // it instead of inserting the winners into the accepted set.
+// The losers are marked while inserting: a slot that finds a smaller code
+// at its locus marks itself, one that replaces a larger code marks that
+// code's slot, so every code but the final holder of each locus is marked.
 constexpr unsigned long long FIRST_EMPTY = ~0ull;
 
 __device__ __forceinline__ void first_insert(unsigned long long* __restrict__ tab, uint32_t mask, uint32_t k,
-                                             uint32_t code, uint32_t* __restrict__ err) {
+                                             uint32_t code, uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
   const unsigned long long mine = (static_cast<unsigned long long>(k) << 32) | code;
   uint32_t h = hash32(k) & mask;
   for (uint32_t probe = 0; probe <= mask; ++probe) {
-    unsigned long long x = tab[h];
-    if (x == FIRST_EMPTY) {
-      x = atomicCAS(tab + h, FIRST_EMPTY, mine);
-      if (x == FIRST_EMPTY) return;
+    // the table is mostly empty: try the swap first (one round trip)
+    const unsigned long long x = atomicCAS(tab + h, FIRST_EMPTY, mine);
+    if (x == FIRST_EMPTY) return;
+    if (uint32_t(x >> 32) == k) {
+      unsigned long long old = x;
+      if (x > mine) old = atomicMin(tab + h, mine);
+      if (old < mine) {
+        if (code) lost[code - 1] = 1;                     // a smaller code holds the locus
+      } else if (old > mine) {
+        const uint32_t oc = uint32_t(old);                // replaced: that code's slot loses
+        if (oc) lost[oc - 1] = 1;
+      }
+      return;
     }
-    if (uint32_t(x >> 32) == k) { if (x > mine) atomicMin(tab + h, mine); return; }
     h = (h + 1) & mask;
   }
   atomicOr(err, ERR_CAPACITY);
@@ -261,24 +280,30 @@ __device__ __forceinline__ unsigned long long first_find(const unsigned long lon
   return FIRST_EMPTY;
 }
 
+// lost: n flags, zeroed by the caller
 __global__ void k_first_insert(const uint32_t* __restrict__ locus, uint32_t n, const uint32_t* __restrict__ drv_locus,
                                uint32_t n_drv, unsigned long long* __restrict__ tab, uint32_t mask,
-                               uint32_t* __restrict__ err) {
+                               uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n_drv) first_insert(tab, mask, drv_locus[i], 0u, err);
+  if (i < n_drv) first_insert(tab, mask, drv_locus[i], 0u, lost, err);
   if (i >= n) return;
   const uint32_t k = locus[i];
-  if (k != LOCUS_INVALID) first_insert(tab, mask, k, i + 1, err);
+  if (k == LOCUS_INVALID) lost[i] = 1;                   // no allele at the drawn position
+  else first_insert(tab, mask, k, i + 1, lost, err);
 }
 
-__global__ void k_first_resolve(const uint32_t* __restrict__ locus, uint32_t n,
-                                const unsigned long long* __restrict__ tab, uint32_t mask,
-                                uint32_t* __restrict__ next, uint32_t* __restrict__ n_next) {
+// the marked slots, in no particular order (warp-aggregated appends)
+__global__ void k_first_collect(const uint8_t* __restrict__ lost, uint32_t n, uint32_t* __restrict__ next,
+                                uint32_t* __restrict__ n_next) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t k = locus[i];
-  const bool win = k != LOCUS_INVALID && uint32_t(first_find(tab, mask, k)) == i + 1;
-  if (!win) next[atomicAdd(n_next, 1u)] = i;
+  const bool mine = i < n && lost[i];
+  const uint32_t ballot = __ballot_sync(0xffffffffu, mine);
+  if (!ballot) return;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t base = 0;
+  if (lane == uint32_t(__ffs(ballot) - 1)) base = atomicAdd(n_next, uint32_t(__popc(ballot)));
+  base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
+  if (mine) next[base + __popc(ballot & ((1u << lane) - 1u))] = i;
 }
 
 __global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
@@ -324,6 +349,110 @@ __global__ void k_cand_resolve(const uint32_t* __restrict__ locus, const uint32_
     if (hset_insert(hkeys, hmask, k) == EMPTY) atomicOr(err, ERR_CAPACITY);
   } else {
     next[atomicAdd(n_next, 1u)] = slot;
+  }
+}
+
+// ------------------------------------------------------------ redraw rounds in one launch
+// After the first round, every later round (candidates, winners, redraws of
+// the losers) runs inside one cooperative launch, the phases separated by a
+// grid barrier, so the host waits once for all rounds.  The rules are those
+// of k_cand_insert / k_cand_resolve / k_collect_invalid followed by k_place.
+// A barrier wait gives up after TAIL_SPIN_LIMIT polls (status bit 2); every
+// block then leaves at its next barrier, which also gives up.
+constexpr uint32_t TAIL_SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ bool grid_barrier(TailCtl* __restrict__ c, uint32_t& gen) {
+  __shared__ uint32_t s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_ok = 1u;
+    const uint32_t g = gen;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+      atomicExch(&c->bar_count, 0u);
+      __threadfence();
+      atomicExch(&c->bar_gen, g + 1u);
+    } else {
+      uint32_t polls = 0;
+      while (*reinterpret_cast<volatile uint32_t*>(&c->bar_gen) == g) {
+        if (++polls > TAIL_SPIN_LIMIT) { s_ok = 0u; atomicOr(&c->status, TAIL_BARRIER_TIMEOUT); break; }
+        __nanosleep(128);
+      }
+    }
+    __threadfence();
+    gen = g + 1u;
+  }
+  __syncthreads();
+  return s_ok != 0u;
+}
+
+__device__ __forceinline__ uint32_t ctl_load(const uint32_t* p) { return *reinterpret_cast<const volatile uint32_t*>(p); }
+
+__global__ void __launch_bounds__(256) k_sites_tail(PlaceTables t, PlaceOut o, Key key,
+                                                    const uint32_t* __restrict__ off_snv,
+                                                    const uint32_t* __restrict__ off_id, uint32_t n_snv,
+                                                    TailArgs a, TailCtl* __restrict__ ctl, uint32_t* __restrict__ err) {
+  uint32_t gen = 0;
+  const uint32_t nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t cur = 0;
+  bool ident = a.identity_first != 0;
+  if (a.redraw_first) {   // list 0 holds the first round's losers: redraw them
+    const uint32_t n = ctl_load(&ctl->count[0]);
+    for (uint32_t i = tid; i < n; i += nthr) place_slot(t, o, key, off_snv, off_id, n_snv, a.list[0][i], 1, err);
+    if (!grid_barrier(ctl, gen)) return;
+  }
+  for (uint32_t round = a.round0;; ++round) {
+    const uint32_t n = ctl_load(cur ? &ctl->count[1] : &ctl->count[0]);
+    if (n == 0) break;
+    if (round >= TAIL_MAX_ROUND) {
+      if (tid == 0) atomicOr(&ctl->status, TAIL_ROUNDS_EXHAUSTED);
+      break;
+    }
+    const uint32_t* pend = cur ? a.list[1] : a.list[0];
+    uint32_t* next = cur ? a.list[0] : a.list[1];
+    uint32_t* n_next = cur ? &ctl->count[0] : &ctl->count[1];
+    if (a.unique) {
+      for (uint32_t i = tid; i < n; i += nthr) {
+        const uint32_t slot = ident ? i : pend[i];
+        const uint32_t k = o.locus[slot];
+        uint32_t h = EMPTY;
+        if (!(k == LOCUS_INVALID || hset_contains(a.hkeys, a.hmask, k) ||
+              (a.first && first_find(a.first, a.fmask, k) != FIRST_EMPTY))) {
+          h = hset_insert(a.ckeys, a.cmask, k);
+          if (h == EMPTY) atomicOr(err, ERR_CAPACITY);
+          else atomicMin(a.cvals + h, slot);
+        }
+        a.hpos[i] = h;
+      }
+      if (!grid_barrier(ctl, gen)) return;
+      for (uint32_t i = tid; i < n; i += nthr) {
+        const uint32_t slot = ident ? i : pend[i];
+        const uint32_t h = a.hpos[i];
+        if (h != EMPTY && a.cvals[h] == slot) {
+          if (hset_insert(a.hkeys, a.hmask, o.locus[slot]) == EMPTY) atomicOr(err, ERR_CAPACITY);
+        } else {
+          next[atomicAdd(n_next, 1u)] = slot;
+        }
+      }
+    } else {
+      for (uint32_t i = tid; i < n; i += nthr) {
+        const uint32_t slot = ident ? i : pend[i];
+        if (o.locus[slot] == LOCUS_INVALID) next[atomicAdd(n_next, 1u)] = slot;
+      }
+    }
+    if (!grid_barrier(ctl, gen)) return;
+    // redraw the losers; clear the candidate entries of this round
+    const uint32_t nn = ctl_load(n_next);
+    for (uint32_t i = tid; i < nn; i += nthr) place_slot(t, o, key, off_snv, off_id, n_snv, next[i], 1, err);
+    if (a.unique)
+      for (uint32_t i = tid; i < n; i += nthr) {
+        const uint32_t h = a.hpos[i];
+        if (h != EMPTY) { a.ckeys[h] = EMPTY; a.cvals[h] = EMPTY; }
+      }
+    if (tid == 0) { ctl->count[cur] = 0u; ctl->rounds = round + 1u; }
+    if (!grid_barrier(ctl, gen)) return;
+    cur ^= 1u;
+    ident = false;
   }
 }
 
@@ -589,12 +718,13 @@ void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint3
 }
 
 void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
-                       unsigned long long* first, uint32_t fmask, uint32_t* next, uint32_t* n_next, uint32_t* err,
-                       cudaStream_t st) {
+                       unsigned long long* first, uint32_t fmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
+                       uint32_t* err, cudaStream_t st) {
   if (n == 0 && n_drv == 0) return;
-  k_first_insert<<<nblk(std::max(n, n_drv)), 256, 0, st>>>(locus, n, drv_locus, n_drv, first, fmask, err);
+  if (n) cudaMemsetAsync(lost, 0, n, st);
+  k_first_insert<<<nblk(std::max(n, n_drv)), 256, 0, st>>>(locus, n, drv_locus, n_drv, first, fmask, lost, err);
   note_launch();
-  if (n) { k_first_resolve<<<nblk(n), 256, 0, st>>>(locus, n, first, fmask, next, n_next); note_launch(); }
+  if (n) { k_first_collect<<<nblk(n), 256, 0, st>>>(lost, n, next, n_next); note_launch(); }
 }
 
 void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
@@ -607,6 +737,30 @@ void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uin
   k_cand_resolve<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, ckeys, cvals, cmask, lost, next,
                                           n_next, err);
   note_launch(2);
+}
+
+const char* sites_tail(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
+                       const uint32_t* off_id, uint32_t n_snv, const TailArgs& a, uint32_t n0, TailCtl* ctl,
+                       uint32_t* err, cudaStream_t st) {
+  if (n0 == 0) return nullptr;
+  int dev = 0, n_sm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sites_tail, 256, 0) != cudaSuccess || per_sm < 1)
+    return "cannot size the cooperative launch of the redraw rounds";
+  const uint64_t want = std::max<uint64_t>(1, (uint64_t(n0) + 255) / 256);
+  const unsigned grid = unsigned(std::min<uint64_t>(want, uint64_t(n_sm) * uint64_t(per_sm)));
+  Key key = make_key(seed);
+  PlaceTables tt = t;
+  PlaceOut oo = o;
+  TailArgs aa = a;
+  void* args[] = {&tt, &oo, &key, const_cast<uint32_t**>(&off_snv), const_cast<uint32_t**>(&off_id), &n_snv, &aa,
+                  &ctl, &err};
+  if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_sites_tail), dim3(grid), dim3(256), args, 0, st) !=
+      cudaSuccess)
+    return "cooperative launch of the redraw rounds failed";
+  note_launch();
+  return nullptr;
 }
 
 void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, uint32_t* bfill, uint32_t* part,

@@ -28,10 +28,10 @@ def _instances(seed, n):
     return genome, sbs, ids, insts
 
 
-def _plain(genome, sbs, ids, inst, tile, place_seed, seq_seed):
+def _plain(genome, sbs, ids, inst, tile, place_seed, seq_seed, context_sampling=100):
     from process_gb300 import MutationEngine
     from process_gb300.engine import sequence_counts
-    eng = MutationEngine(genome, sbs, ids)
+    eng = MutationEngine(genome, sbs, ids, context_sampling=context_sampling)
     eng.add_mutant("A", {"SNV": inst["snv"], "indel": inst["indel"]})
     eng.add_exposure(0.0, {**{f"SBS{k + 1}": float(inst["sbs"][k]) for k in range(3)},
                            **{f"ID{k + 1}": float(inst["ids"][k]) for k in range(2)}})
@@ -49,10 +49,10 @@ def _batch(genome, sbs, ids, insts):
     return eng, b
 
 
-def _check(b, genome, sbs, ids, insts, pseeds, sseeds):
+def _check(b, genome, sbs, ids, insts, pseeds, sseeds, context_sampling=100):
     tiles = b.tile_sizes
     for i, inst in enumerate(insts):
-        t, alt, dep = _plain(genome, sbs, ids, inst, tiles[i], int(pseeds[i]), int(sseeds[i]))
+        t, alt, dep = _plain(genome, sbs, ids, inst, tiles[i], int(pseeds[i]), int(sseeds[i]), context_sampling)
         bt = b.table(i)
         for k in ("locus", "edge", "aux", "cls", "sig", "allele", "kind", "nature"):
             np.testing.assert_array_equal(bt[k], t[k], err_msg=f"instance {i} {k}")
@@ -84,3 +84,22 @@ def test_batch_autotune_and_uneven_tiles(gpu_lib):
     b.tile_sizes = [256, 512, 1024, 2048, 4096]       # uneven tiles across instances
     b.run(pseeds, sseeds)
     _check(b, genome, sbs, ids, insts, pseeds, sseeds)
+
+
+def test_batch_at_batched_workload_sizes(gpu_lib):
+    """32 instances drawn like the 256-instance batched workload (forests of
+    1e3-5e4 leaves, log-uniform; SNV 1e-8-1e-7; coverage 30-200x; every
+    position indexed) on a 10 Mbp genome: each instance equals the plain
+    path run alone."""
+    from process_gb300 import synth
+    n = 32
+    w = synth.batch_256(seed=11, n_inst=n, genome_len=10_000_000)
+    leaves = [int(np.sum(np.asarray(f.is_leaf))) for f in w.forests]
+    assert min(leaves) >= 1_000 and max(leaves) > 20_000
+    eng, b = synth.build_batch(w)
+    pseeds, sseeds = np.arange(n) + 300, np.arange(n) + 700
+    b.run(pseeds, sseeds)
+    insts = [dict(forest=w.forests[i], snv=float(w.snv[i]), indel=float(w.indel[i]), sbs=w.sbs_expo[i],
+                  ids=w.id_expo[i], cfg=w.seq[i], n_pre=(0, 0)) for i in range(n)]
+    assert sum(b.dims(i)[0] for i in range(n)) > 10_000
+    _check(b, w.genome, w.sbs, w.ids, insts, pseeds, sseeds, context_sampling=w.context_sampling)
