@@ -823,7 +823,7 @@ void place_replay(const Engine& e, const Forest& f, uint32_t n_pre_snv, uint32_t
     Stream st = stream(seed, sl.m, sl.edge, sl.epoch, sl.indel ? TAG_INDEL : TAG_SNV);
     st.block = 1 + attempt[i];
     const W4 r = st.next();
-    if (attempt[i] >= 16) {   // class redrawn from the same signature after 16 collisions
+    if (attempt[i] >= 4) {   // class redrawn from the same signature after 4 collisions
       const int ty = sl.indel ? 1 : 0;
       const uint32_t NC = ty == 0 ? 96 : 83;
       cls[i] = uint8_t(lookup(&t.sig_cdf[ty][uint64_t(sig[i]) * NC], NC, r.v[3]));

@@ -125,21 +125,12 @@ void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t se
                             uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st,
                             const uint32_t* n_dev = nullptr);
 void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, cudaStream_t st);
-// slots whose locus is invalid (no allele covers the drawn position) -> next list
-void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
-                           uint32_t* n_next, cudaStream_t st, const uint32_t* n_dev = nullptr);
 // first infinite-sites round over slots [0, n) and the drivers' loci:
 // `first` (fmask + 1 entries of 64 bits, all ones) ends holding the taken
 // loci; the losing slots go to next (lost: n bytes of scratch)
 void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
                        unsigned long long* first, uint32_t fmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
                        uint32_t* err, cudaStream_t st);
-// a later round: a locus is taken when it is in the accepted set hkeys or
-// (first != NULL) in the first round's table
-void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
-                 uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev = nullptr,
-                 const unsigned long long* first = nullptr, uint32_t fmask = 0);
 // All redraw rounds after the first in one cooperative launch (k_sites_tail).
 // list[0] holds the n0 pending slots (identity_first: slots 0 .. n0 - 1, no
 // list); redraw_first: they are redrawn before the first round.  unique:

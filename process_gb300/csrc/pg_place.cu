@@ -33,7 +33,7 @@
 
 namespace pg {
 
-constexpr uint32_t RECLASS_ATTEMPTS = 16;
+constexpr uint32_t RECLASS_ATTEMPTS = 4;
 
 // ------------------------------------------------------------ per-edge counts
 // counts of edge v (v == n_nodes: the preneoplastic edge) into
@@ -293,70 +293,33 @@ __global__ void k_first_insert(const uint32_t* __restrict__ locus, uint32_t n, c
 }
 
 // the marked slots, in no particular order (warp-aggregated appends)
-__global__ void k_first_collect(const uint8_t* __restrict__ lost, uint32_t n, uint32_t* __restrict__ next,
-                                uint32_t* __restrict__ n_next) {
+// (one append per block of 256 slots)
+__global__ void __launch_bounds__(256) k_first_collect(const uint8_t* __restrict__ lost, uint32_t n,
+                                                       uint32_t* __restrict__ next, uint32_t* __restrict__ n_next) {
+  __shared__ uint32_t s_cnt[8], s_base;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const bool mine = i < n && lost[i];
   const uint32_t ballot = __ballot_sync(0xffffffffu, mine);
-  if (!ballot) return;
-  const uint32_t lane = threadIdx.x & 31u;
-  uint32_t base = 0;
-  if (lane == uint32_t(__ffs(ballot) - 1)) base = atomicAdd(n_next, uint32_t(__popc(ballot)));
-  base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
-  if (mine) next[base + __popc(ballot & ((1u << lane) - 1u))] = i;
-}
-
-__global__ void k_cand_insert(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
-                              const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ hkeys, uint32_t hmask,
-                              const unsigned long long* __restrict__ first, uint32_t fmask,
-                              uint32_t* __restrict__ ckeys, uint32_t* __restrict__ cvals, uint32_t cmask,
-                              uint8_t* __restrict__ lost, uint32_t* __restrict__ err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (n_dev ? *n_dev : n)) return;
-  const uint32_t slot = pending ? pending[i] : i;
-  const uint32_t k = locus[slot];
-  if (k == LOCUS_INVALID || hset_contains(hkeys, hmask, k) ||
-      (first && first_find(first, fmask, k) != FIRST_EMPTY)) {
-    lost[i] = 1;
-    return;
+  if (lane == 0) s_cnt[warp] = __popc(ballot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int w = 0; w < 8; ++w) { const uint32_t c = s_cnt[w]; s_cnt[w] = tot; tot += c; }
+    s_base = tot ? atomicAdd(n_next, tot) : 0u;
   }
-  lost[i] = 0;
-  const uint32_t h = hset_insert(ckeys, cmask, k);
-  if (h == EMPTY) { atomicOr(err, ERR_CAPACITY); return; }
-  atomicMin(cvals + h, slot);
-}
-
-__global__ void k_cand_resolve(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending, uint32_t n,
-                               const uint32_t* __restrict__ n_dev, uint32_t* __restrict__ hkeys, uint32_t hmask,
-                               const uint32_t* __restrict__ ckeys, const uint32_t* __restrict__ cvals, uint32_t cmask,
-                               const uint8_t* __restrict__ lost, uint32_t* __restrict__ next,
-                               uint32_t* __restrict__ n_next, uint32_t* __restrict__ err) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (n_dev ? *n_dev : n)) return;
-  const uint32_t slot = pending ? pending[i] : i;
-  const uint32_t k = locus[slot];
-  bool win = false;
-  if (!lost[i]) {
-    uint32_t h = hash32(k) & cmask;
-    for (uint32_t probe = 0; probe <= cmask; ++probe) {
-      const uint32_t x = ckeys[h];
-      if (x == k) { win = cvals[h] == slot; break; }
-      if (x == EMPTY) break;
-      h = (h + 1) & cmask;
-    }
-  }
-  if (win) {
-    if (hset_insert(hkeys, hmask, k) == EMPTY) atomicOr(err, ERR_CAPACITY);
-  } else {
-    next[atomicAdd(n_next, 1u)] = slot;
-  }
+  __syncthreads();
+  if (mine) next[s_base + s_cnt[warp] + __popc(ballot & ((1u << lane) - 1u))] = i;
 }
 
 // ------------------------------------------------------------ redraw rounds in one launch
 // After the first round, every later round (candidates, winners, redraws of
 // the losers) runs inside one cooperative launch, the phases separated by a
-// grid barrier, so the host waits once for all rounds.  The rules are those
-// of k_cand_insert / k_cand_resolve / k_collect_invalid followed by k_place.
+// grid barrier, so the host waits once for all rounds.  A round: pending
+// slots whose locus is free enter a candidate table (hkeys: loci accepted in
+// the later rounds; first: the first round's table), the smallest slot of
+// each locus wins and joins hkeys, the others (and slots without an allele
+// at their locus) are redrawn with their next attempt.
 // A barrier wait gives up after TAIL_SPIN_LIMIT polls (status bit 2); every
 // block then leaves at its next barrier, which also gives up.
 constexpr uint32_t TAIL_SPIN_LIMIT = 1u << 22;
@@ -475,15 +438,6 @@ __global__ void k_drivers(PlaceOut o, const DriverRec* __restrict__ drv, uint32_
   o.attempt[slot] = 0;
   o.allele[slot] = uint16_t(d.allele);
   o.seq[slot] = uint16_t(d.seq);
-}
-
-__global__ void k_collect_invalid(const uint32_t* __restrict__ locus, const uint32_t* __restrict__ pending,
-                                  uint32_t n, const uint32_t* __restrict__ n_dev, uint32_t* __restrict__ next,
-                                  uint32_t* __restrict__ n_next) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (n_dev ? *n_dev : n)) return;
-  const uint32_t slot = pending ? pending[i] : i;
-  if (locus[slot] == LOCUS_INVALID) next[atomicAdd(n_next, 1u)] = slot;
 }
 
 // ------------------------------------------------------------ locus sort
@@ -712,11 +666,6 @@ void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint
   k_drivers<<<nblk(n_drv), 256, 0, st>>>(o, drv, n_drv, base_slot); note_launch();
 }
 
-void sites_collect_invalid(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* next,
-                           uint32_t* n_next, cudaStream_t st, const uint32_t* n_dev) {
-  if (n) { k_collect_invalid<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, next, n_next); note_launch(); }
-}
-
 void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
                        unsigned long long* first, uint32_t fmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
                        uint32_t* err, cudaStream_t st) {
@@ -725,18 +674,6 @@ void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_lo
   k_first_insert<<<nblk(std::max(n, n_drv)), 256, 0, st>>>(locus, n, drv_locus, n_drv, first, fmask, lost, err);
   note_launch();
   if (n) { k_first_collect<<<nblk(n), 256, 0, st>>>(lost, n, next, n_next); note_launch(); }
-}
-
-void sites_round(const uint32_t* locus, const uint32_t* pending, uint32_t n, uint32_t* hkeys, uint32_t hmask,
-                 uint32_t* ckeys, uint32_t* cvals, uint32_t cmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                 uint32_t* err, cudaStream_t st, const uint32_t* n_dev, const unsigned long long* first,
-                 uint32_t fmask) {
-  if (n == 0) return;
-  k_cand_insert<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, first, fmask, ckeys, cvals, cmask,
-                                         lost, err);
-  k_cand_resolve<<<nblk(n), 256, 0, st>>>(locus, pending, n, n_dev, hkeys, hmask, ckeys, cvals, cmask, lost, next,
-                                          n_next, err);
-  note_launch(2);
 }
 
 const char* sites_tail(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
