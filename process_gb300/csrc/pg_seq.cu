@@ -38,6 +38,8 @@
 // Both phases keep every lane busy whatever the number of mutations a read
 // covers.  Windows with more records than shared memory holds run a per-read
 // loop on the global arrays instead.
+#include <type_traits>
+
 #include "pg_common.cuh"
 #include "pg_rng.cuh"
 #include "pg_kernels.h"
@@ -290,13 +292,29 @@ __device__ __forceinline__ void fill_cn_cache(CnCache& c, const SeqParams& prm, 
   }
 }
 
+// cdf_lookup for tables of at most NMAX (a power of two) thresholds: the
+// count of thresholds <= u >> 1 by binary lifting, without a data-dependent
+// loop (the same index as cdf_lookup for sorted thresholds)
+template <uint32_t NMAX>
+__device__ __forceinline__ uint32_t cdf_lookup_small(const uint32_t* thr, uint32_t n, uint32_t u) {
+  const uint32_t v = u >> 1;
+  uint32_t lo = 0;
+#pragma unroll
+  for (uint32_t step = NMAX; step >= 1; step >>= 1)
+    if (lo + step <= n && thr[lo + step - 1] <= v) lo += step;
+  return lo < n ? lo : n - 1;
+}
+
 // start offset in a part of length plen from the word u that selected the
 // part, whose 31-bit value lies in the part's threshold interval [lo, hi)
 __device__ __forceinline__ uint32_t part_offset(uint32_t u, uint32_t lo, uint32_t hi, uint32_t plen) {
   return uint32_t((uint64_t((u >> 1) - lo) * plen) / uint64_t(hi - lo));
 }
 
-template <bool INS_SMEM>
+// CN selects the copy-number path at compile time (0: no copy-number
+// events, 1: the tile's tables in shared memory, 2: the tables in global
+// memory) or, -1, at run time from prm.has_cna and cc.
+template <bool INS_SMEM, int CN = -1>
 __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
                                                   uint32_t len, uint32_t ce, const SeqSample& sm,
                                                   const uint32_t* __restrict__ leaf_tin, const SeqParams& prm,
@@ -305,21 +323,22 @@ __device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t 
   const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
   Fragment f;
   const uint32_t R = prm.read_len;
-  if (!prm.has_cna) {
+  const int path = CN >= 0 ? CN : (!prm.has_cna ? 0 : (cc ? 1 : 2));
+  if (path == 0) {
     f.p0 = start + __umulhi(r.x, len);
     const bool normal = sm.all_normal || r.y < sm.normal_thr;
     f.inst = __umulhi(r.w, prm.n_alleles);
     f.cell = normal ? prm.normal_tin
                     : __ldg(leaf_tin + sm.leaf_off + __umulhi(r.w * prm.n_alleles, sm.n_leaves));
-  } else if (cc) {
+  } else if (path == 1) {
     uint32_t part = 0;
     if (cc->n_parts > 1) {
-      part = cdf_lookup(cc->pthr, cc->n_parts, r.x);
+      part = cdf_lookup_small<SEQ_CN_PARTS>(cc->pthr, cc->n_parts, r.x);
       f.p0 = cc->pstart[part] + part_offset(r.x, part ? cc->pthr[part - 1] : 0u, cc->pthr[part], cc->plen[part]);
     } else {
       f.p0 = cc->pstart[0] + __umulhi(r.x, cc->plen[0]);
     }
-    const uint32_t o = cdf_lookup(cc->othr[part], cc->n_opt, r.y);
+    const uint32_t o = cdf_lookup_small<SEQ_CN_OPTS>(cc->othr[part], cc->n_opt, r.y);
     const uint32_t nl = cc->onl[o], icnt = cc->oicnt[part][o];
     f.inst = icnt ? uint32_t(__ldg(prm.gc.inst_list + cc->oioff[part][o] + __umulhi(r.w, icnt))) : 0xffffu;
     f.cell = nl ? __ldg(prm.cls_leaf_tin + cc->oloff[o] + __umulhi(r.w * icnt, nl)) : prm.normal_tin;
@@ -439,6 +458,7 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
                        sm.n_opt <= SEQ_CN_OPTS;
   if (cn_smem) fill_cn_cache(s_cn, prm, sm, t, s, tid);
   const CnCache* cc = cn_smem ? &s_cn : nullptr;
+
   const uint32_t per_batch = SEQ_MCAP / 2;
 
   constexpr uint32_t FPT = SEQ_MCAP / 2 / SEQ_THREADS;   // fragments per thread and batch
@@ -450,27 +470,39 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
     // bucket ranks, both < 2^16, packed in pairs); each mate takes its rank
     // within its start bucket from the histogram's atomic
     uint32_t o01[FPT], ca[FPT], fi[FPT], fw[FPT], rk01[FPT];
+    // one instance of the draw code per (copy-number path, insert table)
+    // pair, chosen once per tile: the unrolled loop holds only that path
+    auto gen = [&](auto cn, auto ins_tag) {
 #pragma unroll
-    for (uint32_t q = 0; q < FPT; ++q) {
-      const uint32_t k = tid + q * SEQ_THREADS;
-      if (k < nb_pairs) {
-        const Fragment f = ins_smem
-            ? make_fragment<true>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, s_ins, s_guide, cc)
-            : make_fragment<false>(key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, nullptr, nullptr, cc);
-        ca[q] = f.cell;
-        fi[q] = f.inst;
-        fw[q] = f.w;
-        const uint32_t o0 = f.p0 - start;
-        uint32_t rk = atomicAdd(s_boff + o0 / SEQ_BW, 1u);
-        uint32_t o1 = 0;
-        if (prm.paired) {
-          o1 = f.p1 - start;
-          rk |= atomicAdd(s_boff + o1 / SEQ_BW, 1u) << 16;
+      for (uint32_t q = 0; q < FPT; ++q) {
+        const uint32_t k = tid + q * SEQ_THREADS;
+        if (k < nb_pairs) {
+          const Fragment f = make_fragment<decltype(ins_tag)::value, decltype(cn)::value>(
+              key, b0 + k, t, s, start, len, ce, sm, leaf_tin, prm, ins_smem ? s_ins : nullptr,
+              ins_smem ? s_guide : nullptr, cc);
+          ca[q] = f.cell;
+          fi[q] = f.inst;
+          fw[q] = f.w;
+          const uint32_t o0 = f.p0 - start;
+          uint32_t rk = atomicAdd(s_boff + o0 / SEQ_BW, 1u);
+          uint32_t o1 = 0;
+          if (prm.paired) {
+            o1 = f.p1 - start;
+            rk |= atomicAdd(s_boff + o1 / SEQ_BW, 1u) << 16;
+          }
+          o01[q] = o0 | (o1 << 16);
+          rk01[q] = rk;
         }
-        o01[q] = o0 | (o1 << 16);
-        rk01[q] = rk;
       }
-    }
+    };
+    using T0 = std::integral_constant<int, 0>;
+    using T1 = std::integral_constant<int, 1>;
+    using T2 = std::integral_constant<int, 2>;
+    using YES = std::true_type;
+    using NO = std::false_type;
+    if (!prm.has_cna) { if (ins_smem) gen(T0{}, YES{}); else gen(T0{}, NO{}); }
+    else if (cc) { if (ins_smem) gen(T1{}, YES{}); else gen(T1{}, NO{}); }
+    else { if (ins_smem) gen(T2{}, YES{}); else gen(T2{}, NO{}); }
     __syncthreads();
     // bucket offsets (exclusive scan of at most 1024 counts)
     {
