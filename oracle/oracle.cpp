@@ -1094,18 +1094,16 @@ SeqSetup seq_setup(const Placed& pl, const SeqCfg& c) {
   return s;
 }
 
-// error word of the visit of mate `mate` of a fragment to `locus`: the
-// MurmurHash3 fmix32 finaliser (A. Appleby, public domain) of the fragment's
-// error word (the XOR of the four words of its Philox block) mixed with
-// locus and mate
+// error words (the read kernel's mate_word / err_word in pg_seq.cu): a
+// mate's word is the fragment's error word (the XOR of the four words of its
+// Philox block) for mate 0 and w * 0x85EBCA6B + 0x27D4EB2F for mate 1; the
+// visit of a mate to `locus` hashes it with the locus by one odd multiply
+// and a xorshift
+uint32_t mate_word(uint32_t w, uint32_t mate) { return mate ? w * 0x85EBCA6Bu + 0x27D4EB2Fu : w; }
+
 uint32_t error_word(uint32_t w, uint32_t locus, uint32_t mate) {
-  uint32_t h = w ^ (locus * 0x9E3779B1u) ^ (mate ? 0x85EBCA77u : 0u);
-  h ^= h >> 16;
-  h *= 0x85EBCA6Bu;
-  h ^= h >> 13;
-  h *= 0xC2B2AE35u;
-  h ^= h >> 16;
-  return h;
+  uint32_t h = (mate_word(w, mate) ^ (locus * 0x9E3779B1u)) * 0xC2B2AE35u;
+  return h ^ (h >> 16);
 }
 
 // Allele instances carrying mutation i: its own instance and every copy made
@@ -1447,7 +1445,7 @@ OracleRead oracle_read(const Placed& pl, const Carrier& car, const std::vector<s
       if (indel & 1u) {
         for (uint32_t k = 0; k < l && out.seq.size() < R; ++k) {
           uint32_t ib = (indel >> (8 + 2 * k)) & 3u;
-          const uint32_t ei = error_word(fw ^ (0x9E3779B1u * (k + 1)), q - 1, mate);
+          const uint32_t ei = error_word(mate_word(fw, mate) ^ (0x9E3779B1u * (k + 1)), q - 1, 0);
           if (ei < err_thr) ib = other_base(ib, -1, ei % 3u);
           out.seq.push_back(ACGT[ib]);
           push('I', 1);

@@ -209,11 +209,16 @@ __global__ void k_tile_split_level(uint32_t level, uint32_t n_slots, const uint3
   }
 }
 
-// error word of the visit of mate `mate` of a fragment (error word w) to `locus`
-__device__ __forceinline__ uint32_t err_word(uint32_t w, uint32_t locus, uint32_t mate) {
-  uint32_t h = w ^ (locus * 0x9E3779B1u) ^ (mate ? 0x85EBCA77u : 0u);
-  h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
-  return h;
+// Error words.  A mate's word: the fragment's error word for mate 0, an
+// odd affine map of it for mate 1.  The visit of a mate (word wm) to locus:
+// a multiplicative hash whose high bits decide the substitution error
+// (e < err_thr) and whose value mod 3 picks the erroneous base.
+__device__ __forceinline__ uint32_t mate_word(uint32_t w, uint32_t mate) {
+  return mate ? w * 0x85EBCA6Bu + 0x27D4EB2Fu : w;
+}
+__device__ __forceinline__ uint32_t err_word(uint32_t wm, uint32_t locus) {
+  uint32_t h = (wm ^ (locus * 0x9E3779B1u)) * 0xC2B2AE35u;
+  return h ^ (h >> 16);
 }
 
 // does allele instance y of the read's cell carry the mutation placed on
@@ -229,13 +234,14 @@ __device__ __forceinline__ bool inst_carries(const SeqParams& prm, uint32_t y, u
   return false;
 }
 
-// did the visit observe the alt base?
+// did the visit of a mate (word wm) observe the alt base?
 __device__ __forceinline__ bool observed(const SeqParams& prm, uint32_t tin, uint32_t tout, uint32_t info,
-                                         uint32_t cell, uint32_t inst, uint32_t w, uint32_t locus, uint32_t mate) {
-  const bool carried = (tin <= cell) && (cell < tout) &&
+                                         uint32_t cell, uint32_t inst, uint32_t wm, uint32_t locus) {
+  // the cell is in the edge's subtree when tin <= cell < tout (one unsigned compare)
+  const bool carried = (cell - tin < tout - tin) &&
                        inst_carries(prm, inst, info & 0xffffu, (uint64_t(tin) << 16) | ((info >> 16) & 0x7fffu));
   if (info >> 31) return carried;   // indel
-  const uint32_t e = err_word(w, locus, mate);
+  const uint32_t e = err_word(wm, locus);
   const bool err = e < prm.err_thr;
   return carried ? !err : (err && (e % 3u) == 0u);
 }
@@ -385,9 +391,9 @@ struct ReadSmem {
   uint32_t s_locus[SEQ_CAP], s_tin[SEQ_CAP], s_tout[SEQ_CAP], s_info[SEQ_CAP];
   uint32_t s_alt[SEQ_CAP], s_dep[SEQ_CAP];
   // mates of the batch in start-bucket order
-  uint32_t s_mpi[SEQ_MCAP];      // start offset in the window | mate << 15 | allele instance << 16
-                                 //   (instance 0xffff: dropped fragment)
-  uint2 s_mcw[SEQ_MCAP];         // source cell (Euler index), the fragment's error word
+  uint32_t s_mpi[SEQ_MCAP];      // start offset in the window | allele instance << 16 (a dropped
+                                 //   fragment: offset 0xffff, instance 0xffff)
+  uint2 s_mcw[SEQ_MCAP];         // source cell (Euler index), the mate's error word
   uint32_t s_boff[SEQ_NBK + 4];  // bucket counts, then offsets
   uint32_t s_ins[SEQ_INS_CAP];
   uint16_t s_guide[SEQ_GUIDE];
@@ -435,7 +441,7 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
           const SeqRec r = grec[i];
           if (r.locus >= a + R) break;
           atomicAdd(gdep + i, 1u);
-          if (observed(prm, r.tin, r.tout, r.info, f.cell, f.inst, f.w, r.locus, mate))
+          if (observed(prm, r.tin, r.tout, r.info, f.cell, f.inst, mate_word(f.w, mate), r.locus))
             atomicAdd(galt + i, 1u);
         }
       }
@@ -522,10 +528,12 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
       if (k < nb_pairs) {
         const uint32_t o0 = o01[q] & 0xffffu, o1 = o01[q] >> 16;
         const uint32_t x0 = s_boff[o0 / SEQ_BW] + (rk01[q] & 0xffffu);
-        s_mpi[x0] = o0 | (fi[q] << 16); s_mcw[x0] = make_uint2(ca[q], fw[q]);
+        // a dropped fragment's mates carry the start offset 0xffff: past every locus
+        const uint32_t oo0 = fi[q] == 0xffffu ? 0xffffu : o0, oo1 = fi[q] == 0xffffu ? 0xffffu : o1;
+        s_mpi[x0] = oo0 | (fi[q] << 16); s_mcw[x0] = make_uint2(ca[q], fw[q]);
         if (prm.paired) {
           const uint32_t x1 = s_boff[o1 / SEQ_BW] + (rk01[q] >> 16);
-          s_mpi[x1] = o1 | 0x8000u | (fi[q] << 16); s_mcw[x1] = make_uint2(ca[q], fw[q]);
+          s_mpi[x1] = oo1 | (fi[q] << 16); s_mcw[x1] = make_uint2(ca[q], mate_word(fw[q], 1u));
         }
       }
     }
@@ -577,11 +585,11 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
           const uint32_t x = base + k;
           const uint32_t pi = s_mpi[x];
           const uint2 cw = s_mcw[x];                          // one 32-bit and one 64-bit load
-          const uint32_t pm = pi & 0xffffu, mi = pi >> 16, ca = cw.x, w = cw.y;
-          const uint32_t o = pm & 0x7fffu;
-          if (o > off || o + R <= off || mi == 0xffffu) continue;   // the mate does not cover L (or was dropped)
+          // the mate covers L when its start o is in (L - R, L] (unsigned: o > off wraps)
+          if (off - (pi & 0xffffu) >= R) continue;
           dep += 1;
-          alt += observed(prm, tin, tout, info, ca, mi, w, L, pm >> 15) ? 1u : 0u;
+          const uint32_t mi = pi >> 16, ca = cw.x, w = cw.y;
+          alt += observed(prm, tin, tout, info, ca, mi, w, L) ? 1u : 0u;
         }
         if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
       }
@@ -631,6 +639,7 @@ __device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ ge
                            uint32_t inst, uint32_t w, uint32_t mate, SamRead& out, char* __restrict__ seq) {
   const char* ACGT = "ACGT";
   const uint32_t R = prm.read_len;
+  const uint32_t wm = mate_word(w, mate);
   uint32_t i = lower_bound_rec(recs, n_recs, p);
   uint32_t q = p, n = 0, nc = 0;
   auto push = [&](uint32_t op, uint32_t len) {
@@ -663,7 +672,7 @@ __device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ ge
       }
     }
     uint32_t tb = carried_snv ? alt : b;
-    const uint32_t e = err_word(w, q, mate);
+    const uint32_t e = err_word(wm, q);
     if (e < prm.err_thr) tb = others(tb, site ? int(carried_snv ? b : alt) : -1, e % 3u);
     // an unknown reference base (N) reads as N
     const bool unknown = prm.nmask && ((__ldg(prm.nmask + (q >> 5)) >> (q & 31u)) & 1u);
@@ -675,7 +684,7 @@ __device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ ge
       if (indel & 1u) {
         for (uint32_t k = 0; k < l && n < R; ++k) {
           uint32_t ib = (indel >> (8 + 2 * k)) & 3u;
-          const uint32_t ei = err_word(w ^ (0x9E3779B1u * (k + 1)), q - 1, mate);
+          const uint32_t ei = err_word(wm ^ (0x9E3779B1u * (k + 1)), q - 1);
           if (ei < prm.err_thr) ib = others(ib, -1, ei % 3u);
           seq[n++] = ACGT[ib];
           push(1u, 1u);
