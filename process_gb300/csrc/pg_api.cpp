@@ -486,8 +486,9 @@ void build_indices(pg_engine* e) {
       auto off_tmp = upload(&e->pool, off_k, e->st);
       lists = DBuf<uint32_t>(&e->pool, off[NC]);
       Timer t_emit(e->st);
+      const bool every = std::all_of(stride.begin(), stride.end(), [](uint32_t x) { return x == 1u; });
       pg::index_emit(which, e->genome.p, e->nmask.p, am, e->G, e->chr_off_d.p, int(e->n_chr), cnt.p, stride_d.p,
-                     off_tmp.p, len_tmp.p, lists.p, e->st);
+                     off_tmp.p, len_tmp.p, lists.p, every, e->st);
       e->index_ms[2 * which + 1] = t_emit.stop();
       ck(cudaStreamSynchronize(e->st), "index emit");
       ck(cudaGetLastError(), "index kernels");

@@ -140,6 +140,7 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
   }
   const pg::PlaceOut o = b->out_view();
   DBuf<uint32_t> err(P, 1);
+  DBuf<pg::TailCtl> tail_ctl;
   ck(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st), "memset");
   pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p, cnt_id.p,
                             uint32_t(n_snv), nullptr, uint32_t(n_all), 0, err.p, st);
@@ -166,61 +167,36 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
       uint32_t nn = 0;
       ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
       ck(cudaStreamSynchronize(st), "first round");
-      if (nn) pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p,
-                                        cnt_id.p, uint32_t(n_snv), next, nn, 1, err.p, st);
       pending = next;
-      next = pend_b.p;
       n_pend = nn;
     }
+    // every later round (the losers' redraws first) in one cooperative
+    // launch, its tables sized by what the first round leaves
     uint64_t cap = 1024;
     while (cap < 2 * uint64_t(n_pend)) cap <<= 1;
-    DBuf<uint64_t> hkeys(P, cap), ckeys(P, cap);
-    DBuf<uint32_t> cvals(P, cap);
-    ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
-    // as the plain path: host-read rounds while many slots are pending, then
-    // groups of rounds with the counts in device memory
-    constexpr uint32_t ROUND_TAIL = 1u << 20;
-    constexpr int ROUND_GROUP = 16;
-    DBuf<uint32_t> counts(P, ROUND_GROUP);
-    for (int round = 1; n_pend > 0;) {
-      require(round < 256, "infinite sites model: no free locus left for some mutations");
-      if (n_pend > ROUND_TAIL) {
-        ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
-        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
-        pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p, cap - 1,
-                              lost.p, next, n_next.p, err.p, st, nullptr, fkeys.p, fcap - 1);
-        uint32_t nn = 0;
-        ck(cudaMemcpyAsync(&nn, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-        ck(cudaStreamSynchronize(st), "redraw round");
-        if (nn) pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p,
-                                          cnt_id.p, uint32_t(n_snv), next, nn, 1, err.p, st);
-        pending = next;
-        next = (next == pend_a.p) ? pend_b.p : pend_a.p;
-        n_pend = nn;
-        ++round;
-        continue;
-      }
-      uint64_t ctail = 1024;
-      while (ctail < 2ull * n_pend) ctail <<= 1;
-      ck(cudaMemsetAsync(counts.p, 0, sizeof(uint32_t) * ROUND_GROUP, st), "memset");
-      for (int g = 0; g < ROUND_GROUP; ++g) {
-        const uint32_t* n_dev = g == 0 ? nullptr : counts.p + g - 1;
-        uint32_t* n_out = counts.p + g;
-        ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * ctail, st), "memset");
-        ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * ctail, st), "memset");
-        pg::sites_round_batch(b->locus.p, b->inst_of.p, pending, n_pend, hkeys.p, cap - 1, ckeys.p, cvals.p,
-                              ctail - 1, lost.p, next, n_out, err.p, st, n_dev, fkeys.p, fcap - 1);
-        pg::place_mutations_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p, cnt_id.p,
-                                  uint32_t(n_snv), next, n_pend, 1, err.p, st, n_out);
-        pending = next;
-        next = (next == pend_a.p) ? pend_b.p : pend_a.p;
-      }
-      uint32_t nn = 0;
-      ck(cudaMemcpyAsync(&nn, counts.p + ROUND_GROUP - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
-      ck(cudaStreamSynchronize(st), "redraw rounds");
-      n_pend = nn;
-      round += ROUND_GROUP;
+    if (n_pend) {
+      DBuf<unsigned long long> hkeys(P, cap), ckeys(P, cap);
+      DBuf<uint32_t> cvals(P, cap);
+      DBuf<uint64_t> hpos(P, n_pend);
+      ck(cudaMemsetAsync(hkeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
+      ck(cudaMemsetAsync(ckeys.p, 0xff, sizeof(uint64_t) * cap, st), "memset");
+      ck(cudaMemsetAsync(cvals.p, 0xff, sizeof(uint32_t) * cap, st), "memset");
+      tail_ctl = DBuf<pg::TailCtl>(P, 1);
+      pg::TailCtl c0{};
+      c0.count[0] = n_pend;
+      ck(cudaMemcpyAsync(tail_ctl.p, &c0, sizeof(c0), cudaMemcpyHostToDevice, st), "rounds");
+      pg::TailArgsB ta{};
+      ta.list[0] = const_cast<uint32_t*>(pending);
+      ta.list[1] = pend_b.p;
+      ta.hkeys = hkeys.p; ta.hmask = cap - 1;
+      ta.ckeys = ckeys.p; ta.cvals = cvals.p; ta.cmask = cap - 1;
+      ta.hpos = hpos.p;
+      ta.fkeys = fkeys.p; ta.fmask = fcap - 1;
+      if (const char* msg = pg::sites_tail_batch(b->tabs.p, B, b->cell_off_d.p, b->pkeys.p, o, b->inst_of.p, cnt_snv.p,
+                                                 cnt_id.p, uint32_t(n_snv), ta, n_pend, tail_ctl.p, err.p, st))
+        throw std::runtime_error(msg);
+      // the tables live until the launch ends: the engine's pool hands them
+      // out again only to later work on this stream
     }
   }
   // sort by (instance, locus); the instance's first record is the exclusive
@@ -246,7 +222,11 @@ void batch_place(pg_batch* b, const uint64_t* place_seed) {
      "record offsets");
   uint32_t err_h = 0;
   ck(cudaMemcpyAsync(&err_h, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "error flag");
+  pg::TailCtl tc{};
+  if (tail_ctl.p) ck(cudaMemcpyAsync(&tc, tail_ctl.p, sizeof(tc), cudaMemcpyDeviceToHost, st), "rounds");
   ck(cudaStreamSynchronize(st), "batch placement");
+  if (tc.status & pg::TAIL_BARRIER_TIMEOUT) throw std::runtime_error("a grid barrier of the redraw rounds timed out");
+  require(!(tc.status & pg::TAIL_ROUNDS_EXHAUSTED), "infinite sites model: no free locus left for some mutations");
   if (err_h & pg::ERR_EMPTY_CLASS) throw std::runtime_error("a drawn mutation class has no indexed positions");
   if (err_h & pg::ERR_CAPACITY) throw std::runtime_error("internal hash table capacity exceeded");
   for (uint32_t i = 0; i < B; ++i) {

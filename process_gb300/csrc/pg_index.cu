@@ -267,15 +267,25 @@ __global__ void __launch_bounds__(32 * ix_warps(MODE)) k_index_scan(const uint32
   constexpr int NS = (F::NC + 31) / 32;
   constexpr uint32_t FULL = 0xffffffffu;
   constexpr int W = ix_warps(MODE);
+  static_assert(MODE != 2 || F::NC == 32, "the every-position emit is for the 32 SBS contexts");
+  constexpr int SN = MODE >= 1 ? F::NC : 1;
   constexpr int QW = MODE == 1 ? W : 1, QN = MODE == 1 ? F::NC : 1;
-  __shared__ uint32_t s_stride[QN], s_len[QN];
-  __shared__ uint64_t s_off[QN];
+  constexpr int PW = MODE == 2 ? W : 1, PN = MODE == 2 ? 32 : 1, PB = MODE == 2 ? 32 * IX_LANE_POS : 1;
+  __shared__ uint32_t s_stride[SN], s_len[SN];
+  __shared__ uint64_t s_off[SN];
   // MODE 1, per warp: the classes of the round with a position to write
   // (class | hits << 8) and their lane masks; per class the hits before its
   // next written position and that position's index in the class list
   __shared__ uint32_t s_qk[QW][QN], s_qmask[QW][QN][32];
   __shared__ uint32_t s_dist[QW][QN], s_kidx[QW][QN];
-  if (MODE == 1) {
+  // MODE 2 (every position written), per warp: the round's positions grouped
+  // by class (class runs in class order, in position order within a run), per
+  // class and lane the lane's next slot in the run, per class the run's start,
+  // its first list index and the next round's
+  __shared__ uint32_t s_ppos[PW][PN][32], s_pbuf[PW][PB];
+  __shared__ uint8_t s_pcls[PW][PB];
+  __shared__ uint32_t s_prun[PW][PN], s_plist[PW][PN], s_pnext[PW][PN];
+  if (MODE >= 1) {
     for (int k = threadIdx.x; k < F::NC; k += blockDim.x) {
       s_stride[k] = stride[k];
       s_len[k] = list_len[k];
@@ -299,7 +309,11 @@ __global__ void __launch_bounds__(32 * ix_warps(MODE)) k_index_scan(const uint32
     }
     __syncwarp();
   }
-  const uint32_t qw = MODE == 1 ? w : 0;
+  const uint32_t qw = MODE == 1 ? w : 0, pw = MODE == 2 ? w : 0;
+  if (MODE == 2) {
+    s_pnext[pw][lane] = cnt[uint64_t(lane) * n_units + unit];
+    __syncwarp();
+  }
   const uint64_t n_gw = (G + 15) / 16, n_mw = (G + 31) / 32;
   for (uint32_t round = 0; round < IX_ROUNDS; ++round) {
     const uint64_t wbase = uint64_t(unit) * IX_UNIT + uint64_t(round) * (32 * IX_LANE_POS);
@@ -358,8 +372,22 @@ __global__ void __launch_bounds__(32 * ix_warps(MODE)) k_index_scan(const uint32
         }
       }
     }
-    uint32_t nq = 0;
+    uint32_t nq = 0, tk = 0;
     F::classes(f, [&](int k, uint32_t m) {
+      if constexpr (MODE == 2) {
+        // the lane's first slot in the class's run, and the run's length (held by lane k)
+        const uint32_t c = __popc(m);
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= uint32_t(o)) incl += y;
+        }
+        s_ppos[pw][k][lane] = incl - c;
+        const uint32_t t = __shfl_sync(FULL, incl, 31);
+        if (lane == uint32_t(k)) tk = t;
+        return;
+      }
       const uint32_t t = __reduce_add_sync(FULL, uint32_t(__popc(m)));
       if constexpr (MODE == 0) {
         if (lane == (uint32_t(k) & 31u)) run[k >> 5] += t;
@@ -375,6 +403,43 @@ __global__ void __launch_bounds__(32 * ix_warps(MODE)) k_index_scan(const uint32
         ++nq;
       }
     });
+    if constexpr (MODE == 2) {
+      // class runs in class order: lane k holds class k's run length tk
+      uint32_t incl = tk;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= uint32_t(o)) incl += y;
+      }
+      const uint32_t tot = __shfl_sync(FULL, incl, 31);
+      s_prun[pw][lane] = incl - tk;
+      s_plist[pw][lane] = s_pnext[pw][lane];
+      s_pnext[pw][lane] += tk;
+      __syncwarp();
+      // each lane's positions into their class runs, in position order
+      const uint32_t ok = f[0];
+#pragma unroll 4
+      for (uint32_t i = 0; i < IX_LANE_POS; ++i) {
+        if ((ok >> i) & 1u) {
+          const uint32_t x = ((f[1] >> i) & 1u) | (((f[2] >> i) & 1u) << 1);
+          const uint32_t y0 = (f[3] >> i) & 1u, y1 = (f[4] >> i) & 1u;
+          const uint32_t z = ((f[5] >> i) & 1u) | (((f[6] >> i) & 1u) << 1);
+          // the context as SbsFamilies::classes numbers it
+          const uint32_t k = y0 ? ((y1 << 4) | (x << 2) | z) : (((y1 ^ 1u) << 4) | ((3u - z) << 2) | (3u - x));
+          const uint32_t slot = s_prun[pw][k] + s_ppos[pw][k][lane]++;
+          s_pbuf[pw][slot] = uint32_t(base) + i;
+          s_pcls[pw][slot] = uint8_t(k);
+        }
+      }
+      __syncwarp();
+      // the runs to the class lists, consecutive lanes to consecutive entries
+      for (uint32_t e = lane; e < tot; e += 32) {
+        const uint32_t k = s_pcls[pw][e];
+        const uint32_t idx = s_plist[pw][k] + (e - s_prun[pw][k]);
+        if (idx < s_len[k]) lists[s_off[k] + idx] = s_pbuf[pw][e];
+      }
+      __syncwarp();
+    }
     if constexpr (MODE == 1) {
       __syncwarp();
       // the classes that write a position this round (one copy of the code)
@@ -458,11 +523,23 @@ static void index_count_t(const uint32_t* g, const uint32_t* nmask, const uint32
 template <class F>
 static void index_emit_t(const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
                          const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
-                         const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
+                         const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, bool every,
+                         cudaStream_t st) {
   const uint32_t ntiles = index_num_tiles(G);
-  k_index_scan<F, 1><<<(ntiles + ix_warps(1) - 1) / ix_warps(1), 32 * ix_warps(1), 0, st>>>(g, nmask, amask, G, chr_off, n_chr, ntiles,
-                                                                        const_cast<uint32_t*>(cnt_scanned), stride,
-                                                                        list_off, list_len, lists);
+  bool done = false;
+  if constexpr (F::NC == N_CTX) {
+    if (every) {   // stride 1 for every context: each indexed position is written
+      k_index_scan<F, 2><<<(ntiles + ix_warps(2) - 1) / ix_warps(2), 32 * ix_warps(2), 0, st>>>(
+          g, nmask, amask, G, chr_off, n_chr, ntiles, const_cast<uint32_t*>(cnt_scanned), stride, list_off, list_len,
+          lists);
+      done = true;
+    }
+  }
+  if (!done) {
+    k_index_scan<F, 1><<<(ntiles + ix_warps(1) - 1) / ix_warps(1), 32 * ix_warps(1), 0, st>>>(
+        g, nmask, amask, G, chr_off, n_chr, ntiles, const_cast<uint32_t*>(cnt_scanned), stride, list_off, list_len,
+        lists);
+  }
   note_launch();
 }
 
@@ -474,12 +551,13 @@ void index_count(int which, const uint32_t* g, const uint32_t* nmask, const uint
 
 void index_emit(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
                 const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
-                const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st) {
+                const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, bool every, cudaStream_t st) {
   if (which == 0)
-    index_emit_t<SbsFamilies>(g, nmask, amask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists, st);
+    index_emit_t<SbsFamilies>(g, nmask, amask, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists,
+                              every, st);
   else
     index_emit_t<IdFamilies>(g, nmask, nullptr, G, chr_off, n_chr, cnt_scanned, stride, list_off, list_len, lists,
-                             st);
+                             every, st);
 }
 
 // the positions of the regions to avoid as bits of mask ((G + 31) / 32 words,

@@ -47,9 +47,10 @@ const char* index_counts_noalloc(int which, const uint32_t* g, uint64_t G, const
 void index_count(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
                  const uint32_t* chr_off, int n_chr, uint32_t* cnt, uint32_t* part, uint32_t* totals, cudaStream_t st);
 void genome_avoid_mask(const uint32_t* pos, uint64_t n, uint32_t* mask, cudaStream_t st);
+// every: all strides are 1 (each indexed position is written)
 void index_emit(int which, const uint32_t* g, const uint32_t* nmask, const uint32_t* amask, uint64_t G,
                 const uint32_t* chr_off, int n_chr, const uint32_t* cnt_scanned, const uint32_t* stride,
-                const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, cudaStream_t st);
+                const uint64_t* list_off, const uint32_t* list_len, uint32_t* lists, bool every, cudaStream_t st);
 
 // ---------------------------------------------------------------- genome classes
 // Copy-number events are rare, so the cells of a forest fall into few
@@ -154,6 +155,15 @@ struct TailArgs {
   uint32_t* ckeys; uint32_t* cvals; uint32_t cmask;
   uint32_t* hpos;
   const unsigned long long* first; uint32_t fmask;
+};
+// the batched form: keys (instance << 32 | locus); list 0 holds the first
+// round's losers, redrawn first; fkeys: the first round's table
+struct TailArgsB {
+  uint32_t* list[2];
+  unsigned long long* hkeys; uint64_t hmask;
+  unsigned long long* ckeys; uint32_t* cvals; uint64_t cmask;
+  uint64_t* hpos;
+  const uint64_t* fkeys; uint64_t fmask;
 };
 // returns nullptr, or a message when the launch could not be made
 const char* sites_tail(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
@@ -337,6 +347,13 @@ void sites_round_batch(const uint32_t* locus, const uint16_t* inst_of, const uin
                        uint64_t* hkeys, uint64_t hmask, uint64_t* ckeys, uint32_t* cvals, uint64_t cmask,
                        uint8_t* lost, uint32_t* next, uint32_t* n_next, uint32_t* err, cudaStream_t st,
                        const uint32_t* n_dev = nullptr, const uint64_t* fkeys = nullptr, uint64_t fmask = 0);
+// every round after the first in one cooperative launch (k_sites_tail_b);
+// list 0 of `a` holds the n0 losers of the first round; returns nullptr or
+// a message when the launch could not be made
+const char* sites_tail_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* cell_off, const Key* keys,
+                             const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
+                             uint32_t n_snv, const TailArgsB& a, uint32_t n0, TailCtl* ctl, uint32_t* err,
+                             cudaStream_t st);
 // sort by (instance, locus, slot); bcnt holds n_inst * sort_num_buckets(G)
 // + 1 entries and ends as the exclusive scan of the bucket counts; keys: n
 // 64-bit keys, recs: 2n 16-byte words

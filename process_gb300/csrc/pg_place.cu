@@ -529,14 +529,11 @@ __global__ void k_edge_counts_b(const PlaceTables* __restrict__ tabs, uint32_t n
   edge_counts_one(t, g - node_off[i], keys[i], cnt_snv + cell_off[i], cnt_id + cell_off[i], pre_snv[i], pre_id[i]);
 }
 
-__global__ void k_place_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst, const uint32_t* __restrict__ cell_off,
-                          const Key* __restrict__ keys, PlaceOut o, uint16_t* __restrict__ inst_of,
-                          const uint32_t* __restrict__ off_snv, const uint32_t* __restrict__ off_id, uint32_t n_snv,
-                          const uint32_t* __restrict__ pending, uint32_t n_pending,
-                          const uint32_t* __restrict__ n_dev, int redraw, uint32_t* __restrict__ err) {
-  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= (n_dev ? *n_dev : n_pending)) return;
-  const uint32_t slot = pending ? pending[tid] : tid;
+__device__ __forceinline__ void place_slot_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst,
+                                             const uint32_t* __restrict__ cell_off, const Key* __restrict__ keys,
+                                             const PlaceOut& o, uint16_t* __restrict__ inst_of,
+                                             const uint32_t* __restrict__ off_snv, const uint32_t* __restrict__ off_id,
+                                             uint32_t n_snv, uint32_t slot, int redraw, uint32_t* __restrict__ err) {
   const bool is_id = slot >= n_snv;
   const uint32_t j = is_id ? slot - n_snv : slot;
   const uint32_t n_cells = cell_off[n_inst];
@@ -547,6 +544,17 @@ __global__ void k_place_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst,
   const uint32_t lq = q - cell_off[i];
   if (!redraw) inst_of[slot] = uint16_t(i);
   place_one(t, o, keys[i], slot, is_id, lq / t.n_epochs, lq % t.n_epochs, j - off[q], redraw, err);
+}
+
+__global__ void k_place_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst, const uint32_t* __restrict__ cell_off,
+                          const Key* __restrict__ keys, PlaceOut o, uint16_t* __restrict__ inst_of,
+                          const uint32_t* __restrict__ off_snv, const uint32_t* __restrict__ off_id, uint32_t n_snv,
+                          const uint32_t* __restrict__ pending, uint32_t n_pending,
+                          const uint32_t* __restrict__ n_dev, int redraw, uint32_t* __restrict__ err) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (n_dev ? *n_dev : n_pending)) return;
+  place_slot_b(tabs, n_inst, cell_off, keys, o, inst_of, off_snv, off_id, n_snv, pending ? pending[tid] : tid, redraw,
+               err);
 }
 
 // infinite-sites rounds of a batch: loci are unique per instance, so the
@@ -625,6 +633,73 @@ __global__ void k_cand_resolve_b(const uint32_t* __restrict__ locus, const uint1
   }
 }
 
+// The later rounds of a batch in one cooperative launch: k_sites_tail's
+// rounds with (instance << 32 | locus) keys.
+__global__ void __launch_bounds__(256) k_sites_tail_b(const PlaceTables* __restrict__ tabs, uint32_t n_inst,
+                                                      const uint32_t* __restrict__ cell_off,
+                                                      const Key* __restrict__ keys, PlaceOut o,
+                                                      uint16_t* __restrict__ inst_of,
+                                                      const uint32_t* __restrict__ off_snv,
+                                                      const uint32_t* __restrict__ off_id, uint32_t n_snv,
+                                                      TailArgsB a, TailCtl* __restrict__ ctl,
+                                                      uint32_t* __restrict__ err) {
+  uint32_t gen = 0;
+  const uint32_t nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t cur = 0;
+  {   // list 0 holds the first round's losers: redraw them
+    const uint32_t n = ctl_load(&ctl->count[0]);
+    for (uint32_t i = tid; i < n; i += nthr)
+      place_slot_b(tabs, n_inst, cell_off, keys, o, inst_of, off_snv, off_id, n_snv, a.list[0][i], 1, err);
+    if (!grid_barrier(ctl, gen)) return;
+  }
+  for (uint32_t round = 1;; ++round) {
+    const uint32_t n = ctl_load(cur ? &ctl->count[1] : &ctl->count[0]);
+    if (n == 0) break;
+    if (round >= TAIL_MAX_ROUND) {
+      if (tid == 0) atomicOr(&ctl->status, TAIL_ROUNDS_EXHAUSTED);
+      break;
+    }
+    const uint32_t* pend = cur ? a.list[1] : a.list[0];
+    uint32_t* next = cur ? a.list[0] : a.list[1];
+    uint32_t* n_next = cur ? &ctl->count[0] : &ctl->count[1];
+    for (uint32_t i = tid; i < n; i += nthr) {
+      const uint32_t slot = pend[i];
+      const uint32_t l = o.locus[slot];
+      const uint64_t k = (uint64_t(inst_of[slot]) << 32) | l;
+      uint64_t h = EMPTY64;
+      if (!(l == LOCUS_INVALID || hset64_contains(reinterpret_cast<const uint64_t*>(a.hkeys), a.hmask, k) ||
+            hset64_contains(a.fkeys, a.fmask, k))) {
+        h = hset64_insert(a.ckeys, a.cmask, k);
+        if (h == EMPTY64) atomicOr(err, ERR_CAPACITY);
+        else atomicMin(a.cvals + h, slot);
+      }
+      a.hpos[i] = h;
+    }
+    if (!grid_barrier(ctl, gen)) return;
+    for (uint32_t i = tid; i < n; i += nthr) {
+      const uint32_t slot = pend[i];
+      const uint64_t h = a.hpos[i];
+      if (h != EMPTY64 && a.cvals[h] == slot) {
+        if (hset64_insert(a.hkeys, a.hmask, (uint64_t(inst_of[slot]) << 32) | o.locus[slot]) == EMPTY64)
+          atomicOr(err, ERR_CAPACITY);
+      } else {
+        next[atomicAdd(n_next, 1u)] = slot;
+      }
+    }
+    if (!grid_barrier(ctl, gen)) return;
+    const uint32_t nn = ctl_load(n_next);
+    for (uint32_t i = tid; i < nn; i += nthr)
+      place_slot_b(tabs, n_inst, cell_off, keys, o, inst_of, off_snv, off_id, n_snv, next[i], 1, err);
+    for (uint32_t i = tid; i < n; i += nthr) {
+      const uint64_t h = a.hpos[i];
+      if (h != EMPTY64) { a.ckeys[h] = EMPTY64; a.cvals[h] = EMPTY; }
+    }
+    if (tid == 0) { ctl->count[cur] = 0u; ctl->rounds = round + 1u; }
+    if (!grid_barrier(ctl, gen)) return;
+    cur ^= 1u;
+  }
+}
+
 // sort of a batch by (instance, locus): bucket = instance * nb + locus >> 10
 __global__ void k_bucket_count_b(const uint32_t* __restrict__ locus, const uint16_t* __restrict__ inst_of, uint32_t n,
                                  uint32_t nb, uint32_t* __restrict__ bcnt) {
@@ -694,6 +769,28 @@ const char* sites_tail(const PlaceTables& t, const PlaceOut& o, uint64_t seed, c
   void* args[] = {&tt, &oo, &key, const_cast<uint32_t**>(&off_snv), const_cast<uint32_t**>(&off_id), &n_snv, &aa,
                   &ctl, &err};
   if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_sites_tail), dim3(grid), dim3(256), args, 0, st) !=
+      cudaSuccess)
+    return "cooperative launch of the redraw rounds failed";
+  note_launch();
+  return nullptr;
+}
+
+const char* sites_tail_batch(const PlaceTables* tabs, uint32_t n_inst, const uint32_t* cell_off, const Key* keys,
+                             const PlaceOut& o, uint16_t* inst_of, const uint32_t* off_snv, const uint32_t* off_id,
+                             uint32_t n_snv, const TailArgsB& a, uint32_t n0, TailCtl* ctl, uint32_t* err,
+                             cudaStream_t st) {
+  if (n0 == 0) return nullptr;
+  int dev = 0, n_sm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sites_tail_b, 256, 0) != cudaSuccess || per_sm < 1)
+    return "cannot size the cooperative launch of the redraw rounds";
+  const uint64_t want = std::max<uint64_t>(1, (uint64_t(n0) + 255) / 256);
+  const unsigned grid = unsigned(std::min<uint64_t>(want, uint64_t(n_sm) * uint64_t(per_sm)));
+  PlaceOut oo = o;
+  TailArgsB aa = a;
+  void* args[] = {&tabs, &n_inst, &cell_off, &keys, &oo, &inst_of, &off_snv, &off_id, &n_snv, &aa, &ctl, &err};
+  if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_sites_tail_b), dim3(grid), dim3(256), args, 0, st) !=
       cudaSuccess)
     return "cooperative launch of the redraw rounds failed";
   note_launch();
