@@ -1283,36 +1283,45 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     pg::PlaceOut o{locus.p, edge.p, aux.p, cls.p, sig.p, allele.p, seqv.p, kind.p, nature.p, attempt.p};
     DBuf<uint32_t> err(P, 1);
     ck(cudaMemsetAsync(err.p, 0, sizeof(uint32_t), st), "memset");
-    pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), nullptr,
-                               uint32_t(n_snv + n_id), 0, err.p, st);
+    // infinite sites: the first draw goes into the first round's table as it
+    // is made (the drivers' loci follow; the losers are read back below)
+    const bool unique = e->infinite_sites;
+    const uint32_t n_slots = uint32_t(n_snv + n_id);
+    DBuf<unsigned long long> first;
+    DBuf<uint8_t> lost1;
+    uint32_t fmask = 0;
+    if (unique && n_slots > 0) {
+      uint64_t fcap = 1024;
+      while (fcap < 2 * n_all) fcap <<= 1;
+      require(fcap <= (uint64_t(1) << 32), "too many mutations for one placement call");
+      first = DBuf<unsigned long long>(P, fcap);
+      fmask = uint32_t(fcap - 1);
+      lost1 = DBuf<uint8_t>(P, n_slots);
+      ck(cudaMemsetAsync(first.p, 0xff, sizeof(unsigned long long) * fcap, st), "memset");
+      pg::place_first_round(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), n_slots, first.p, fmask, lost1.p, err.p,
+                            st);
+    } else {
+      pg::place_mutations_launch(t, o, seed, off_snv.p, off_id.p, uint32_t(n_snv), uint32_t(n_id), nullptr, n_slots, 0,
+                                 err.p, st);
+    }
     auto drv_d = upload(P, drv, st);
-    pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), uint32_t(n_snv + n_id), st);
+    pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), n_slots, st);
     // ---- infinite sites, and loci drawn where the cell has no allele left.
     // Infinite sites: the first round over all slots against one table of
     // its candidates (drivers first), read back once to size the later
     // rounds' tables; every later round runs in one cooperative launch.
     DBuf<pg::TailCtl> tail_ctl;
-    const bool unique = e->infinite_sites;
-    if ((unique || pl->has_cna) && n_snv + n_id > 0) {
-      const uint32_t n_slots = uint32_t(n_snv + n_id);
+    if ((unique || pl->has_cna) && n_slots > 0) {
       uint32_t n_tail = 0;
       pg::TailArgs ta{};
       ta.unique = unique ? 1 : 0;
       DBuf<uint32_t> pend_a, pend_b, hkeys, ckeys, cvals, hpos;
-      DBuf<unsigned long long> first;
       if (unique) {
-        uint64_t fcap = 1024;
-        while (fcap < 2 * n_all) fcap <<= 1;
-        require(fcap <= (uint64_t(1) << 32), "too many mutations for one placement call");
-        first = DBuf<unsigned long long>(P, fcap);
-        const uint32_t fmask = uint32_t(fcap - 1);
         pend_a = DBuf<uint32_t>(P, n_slots);
         DBuf<uint32_t> n_next(P, 1);
-        DBuf<uint8_t> lost(P, n_slots);
-        ck(cudaMemsetAsync(first.p, 0xff, sizeof(unsigned long long) * fcap, st), "memset");
         ck(cudaMemsetAsync(n_next.p, 0, sizeof(uint32_t), st), "memset");
-        pg::sites_first_round(locus.p, n_slots, locus.p + n_slots, uint32_t(drv.size()), first.p, fmask, lost.p,
-                              pend_a.p, n_next.p, err.p, st);
+        pg::sites_first_finish(locus.p + n_slots, uint32_t(drv.size()), first.p, fmask, lost1.p, n_slots, pend_a.p,
+                               n_next.p, err.p, st);
         ck(cudaMemcpyAsync(&n_tail, n_next.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "round");
         ck(cudaStreamSynchronize(st), "first round");
         uint32_t cap = 1024;

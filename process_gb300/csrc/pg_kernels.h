@@ -126,12 +126,16 @@ void place_mutations_launch(const PlaceTables& t, const PlaceOut& o, uint64_t se
                             uint32_t n_pending, int redraw, uint32_t* err, cudaStream_t st,
                             const uint32_t* n_dev = nullptr);
 void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint32_t base_slot, cudaStream_t st);
-// first infinite-sites round over slots [0, n) and the drivers' loci:
-// `first` (fmask + 1 entries of 64 bits, all ones) ends holding the taken
-// loci; the losing slots go to next (lost: n bytes of scratch)
-void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
-                       unsigned long long* first, uint32_t fmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                       uint32_t* err, cudaStream_t st);
+// the first draw of slots [0, n_slots) fused with their insertion into the
+// first round's table `first` (fmask + 1 entries, all ones on entry; lost:
+// n_slots bytes of scratch); then sites_first_finish inserts the drivers'
+// loci and lists the losing slots in next
+void place_first_round(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
+                       const uint32_t* off_id, uint32_t n_snv, uint32_t n_slots, unsigned long long* first,
+                       uint32_t fmask, uint8_t* lost, uint32_t* err, cudaStream_t st);
+void sites_first_finish(const uint32_t* drv_locus, uint32_t n_drv, unsigned long long* first, uint32_t fmask,
+                        uint8_t* lost, uint32_t n_slots, uint32_t* next, uint32_t* n_next, uint32_t* err,
+                        cudaStream_t st);
 // All redraw rounds after the first in one cooperative launch (k_sites_tail).
 // list[0] holds the n0 pending slots (identity_first: slots 0 .. n0 - 1, no
 // list); redraw_first: they are redrawn before the first round.  unique:

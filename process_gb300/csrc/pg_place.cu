@@ -312,6 +312,24 @@ __global__ void __launch_bounds__(256) k_first_collect(const uint8_t* __restrict
   if (mine) next[s_base + s_cnt[warp] + __popc(ballot & ((1u << lane) - 1u))] = i;
 }
 
+// The first draw of every slot with its insertion into the first round's
+// table fused in (infinite sites): the insertion's atomics overlap the
+// draws' gathers.  The drivers go in afterwards (k_first_insert with no
+// passenger slots); the table's final state and the marks do not depend on
+// the order of the insertions.  tab (all ones) and lost (zeros) are set by
+// the caller.
+__global__ void k_place_first(PlaceTables t, PlaceOut o, Key key, const uint32_t* __restrict__ off_snv,
+                              const uint32_t* __restrict__ off_id, uint32_t n_snv, uint32_t n_slots,
+                              unsigned long long* __restrict__ tab, uint32_t mask, uint8_t* __restrict__ lost,
+                              uint32_t* __restrict__ err) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_slots) return;
+  place_slot(t, o, key, off_snv, off_id, n_snv, i, 0, err);
+  const uint32_t k = o.locus[i];
+  if (k == LOCUS_INVALID) lost[i] = 1;                   // no allele at the drawn position
+  else first_insert(tab, mask, k, i + 1, lost, err);
+}
+
 // ------------------------------------------------------------ redraw rounds in one launch
 // After the first round, every later round (candidates, winners, redraws of
 // the losers) runs inside one cooperative launch, the phases separated by a
@@ -741,14 +759,24 @@ void place_drivers(const PlaceOut& o, const DriverRec* drv, uint32_t n_drv, uint
   k_drivers<<<nblk(n_drv), 256, 0, st>>>(o, drv, n_drv, base_slot); note_launch();
 }
 
-void sites_first_round(const uint32_t* locus, uint32_t n, const uint32_t* drv_locus, uint32_t n_drv,
-                       unsigned long long* first, uint32_t fmask, uint8_t* lost, uint32_t* next, uint32_t* n_next,
-                       uint32_t* err, cudaStream_t st) {
-  if (n == 0 && n_drv == 0) return;
-  if (n) cudaMemsetAsync(lost, 0, n, st);
-  k_first_insert<<<nblk(std::max(n, n_drv)), 256, 0, st>>>(locus, n, drv_locus, n_drv, first, fmask, lost, err);
+void place_first_round(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,
+                       const uint32_t* off_id, uint32_t n_snv, uint32_t n_slots, unsigned long long* first,
+                       uint32_t fmask, uint8_t* lost, uint32_t* err, cudaStream_t st) {
+  if (n_slots == 0) return;
+  cudaMemsetAsync(lost, 0, n_slots, st);
+  k_place_first<<<nblk(n_slots), 256, 0, st>>>(t, o, make_key(seed), off_snv, off_id, n_snv, n_slots, first, fmask,
+                                               lost, err);
   note_launch();
-  if (n) { k_first_collect<<<nblk(n), 256, 0, st>>>(lost, n, next, n_next); note_launch(); }
+}
+
+void sites_first_finish(const uint32_t* drv_locus, uint32_t n_drv, unsigned long long* first, uint32_t fmask,
+                        uint8_t* lost, uint32_t n_slots, uint32_t* next, uint32_t* n_next, uint32_t* err,
+                        cudaStream_t st) {
+  if (n_drv) {
+    k_first_insert<<<nblk(n_drv), 256, 0, st>>>(nullptr, 0, drv_locus, n_drv, first, fmask, lost, err);
+    note_launch();
+  }
+  if (n_slots) { k_first_collect<<<nblk(n_slots), 256, 0, st>>>(lost, n_slots, next, n_next); note_launch(); }
 }
 
 const char* sites_tail(const PlaceTables& t, const PlaceOut& o, uint64_t seed, const uint32_t* off_snv,

@@ -21,6 +21,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import itertools
+import weakref
 from dataclasses import dataclass, field
 from typing import Iterable, Mapping, Sequence
 
@@ -320,6 +321,33 @@ class SamplesForest:
         is_parent = np.zeros(n, dtype=bool)
         is_parent[self.parent[self.parent >= 0]] = True
         self.is_leaf = ~is_parent
+        # a samples forest does not change once built (as the reference's);
+        # its columns are read-only, so the library's copy can be kept
+        for a in (self.cell_id, self.parent, self.mutant, self.epistate, self.birth_time, self.divisions,
+                  self.sample, self.is_leaf):
+            a.flags.writeable = False
+
+    def _library_forest(self, species: np.ndarray) -> C.c_void_p:
+        """The library's forest (pg_forest) for these species ids, created once
+        per species assignment and destroyed with this object."""
+        cache = self.__dict__.get("_handles")
+        if cache is None:
+            cache = self._handles = {}
+            weakref.finalize(self, _destroy_forests, cache)
+        key = np.ascontiguousarray(species, dtype=np.uint32).tobytes()
+        h = cache.get(key)
+        if h is None:
+            h = C.c_void_p()
+            sp = np.ascontiguousarray(species, dtype=np.uint32)
+            parent = np.ascontiguousarray(self.parent, dtype=np.int32)
+            birth = np.ascontiguousarray(self.birth_time, dtype=np.float64)
+            sample = np.ascontiguousarray(np.where(self.is_leaf, self.sample, -1), dtype=np.int32)
+            div = np.ascontiguousarray(self.divisions, dtype=np.uint32)
+            check(lib().pg_forest_create(self.num_of_nodes, ptr(parent, C.c_int32), ptr(birth, C.c_double),
+                                         ptr(sp, C.c_uint32), ptr(sample, C.c_int32), ptr(div, C.c_uint32),
+                                         len(self.sample_names), C.byref(h)))
+            cache[key] = h
+        return h
 
     def euler(self) -> tuple[np.ndarray, np.ndarray]:
         """(tin, tout) of every node: its depth-first preorder position and one
@@ -650,21 +678,11 @@ class MutationEngine:
 
         pre_s = sig_index(0, preneoplatic_SNV_signature_name, num_of_preneoplatic_SNVs)
         pre_i = sig_index(1, preneoplatic_indel_signature_name, num_of_preneoplatic_indels)
-        fh = C.c_void_p()
-        parent = np.ascontiguousarray(f.parent, dtype=np.int32)
-        birth = np.ascontiguousarray(f.birth_time, dtype=np.float64)
-        sample = np.ascontiguousarray(np.where(f.is_leaf, f.sample, -1), dtype=np.int32)
-        div = np.ascontiguousarray(f.divisions, dtype=np.uint32)
-        check(lib().pg_forest_create(f.num_of_nodes, ptr(parent, C.c_int32), ptr(birth, C.c_double),
-                                     ptr(species, C.c_uint32), ptr(sample, C.c_int32), ptr(div, C.c_uint32),
-                                     len(f.sample_names), C.byref(fh)))
-        try:
-            ph = C.c_void_p()
-            s = _seed(seed)
-            check(lib().pg_place_mutations(self._h, fh, int(num_of_preneoplatic_SNVs), pre_s,
-                                           int(num_of_preneoplatic_indels), pre_i, s, C.byref(ph)))
-        finally:
-            lib().pg_forest_destroy(fh)
+        fh = f._library_forest(species)
+        ph = C.c_void_p()
+        s = _seed(seed)
+        check(lib().pg_place_mutations(self._h, fh, int(num_of_preneoplatic_SNVs), pre_s,
+                                       int(num_of_preneoplatic_indels), pre_i, s, C.byref(ph)))
         pf = PhylogeneticForest(self, f, ph, s)
         pf._place_args = dict(num_of_preneoplatic_SNVs=int(num_of_preneoplatic_SNVs),
                               num_of_preneoplatic_indels=int(num_of_preneoplatic_indels), seed=s,
@@ -690,6 +708,13 @@ class MutationEngine:
                 "mutants": copy.deepcopy(_plain(self._mutant_specs)),
                 "passenger_CNAs": _plain(self.passenger_CNAs),
                 "regions_to_avoid": _plain(getattr(self, "regions_to_avoid", []))}
+
+
+def _destroy_forests(cache: dict) -> None:
+    if _lib._LIB is not None:
+        for h in cache.values():
+            _lib._LIB.pg_forest_destroy(h)
+    cache.clear()
 
 
 class PhylogeneticForest:
