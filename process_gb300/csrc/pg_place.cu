@@ -475,23 +475,43 @@ __global__ void k_bucket_scatter_keys(const uint32_t* __restrict__ locus, uint32
   const uint32_t k = locus[i], b = k >> BUCKET_SHIFT;
   keys[boff[b] + atomicAdd(bfill + b, 1u)] = (static_cast<unsigned long long>(k) << 32) | i;
 }
-__global__ void k_bucket_sort_keys(const uint32_t* __restrict__ boff, uint32_t nb, uint32_t n,
-                                   unsigned long long* __restrict__ keys, uint32_t* __restrict__ order) {
-  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nb) return;
-  const uint32_t lo = boff[b], hi = (b + 1 < nb) ? boff[b + 1] : n;
-  for (uint32_t i = lo + 1; i < hi; ++i) {
-    const unsigned long long kx = keys[i];
-    uint32_t j = i;
-    while (j > lo) {
-      const unsigned long long ky = keys[j - 1];
-      if (ky <= kx) break;
-      keys[j] = ky;
-      --j;
+// One block per 256 consecutive buckets: their keys (one contiguous range)
+// are staged in shared memory, each thread insertion-sorts one bucket there,
+// and the block writes the order coalesced.  A range larger than the stage
+// is sorted in place in global memory instead.
+constexpr uint32_t SORT_BUCKETS = 256, SORT_STAGE = 5120;   // 40 KB of keys
+
+__global__ void __launch_bounds__(SORT_BUCKETS) k_bucket_sort_keys(const uint32_t* __restrict__ boff, uint32_t nb,
+                                                                   uint32_t n, unsigned long long* __restrict__ keys,
+                                                                   uint32_t* __restrict__ order) {
+  __shared__ unsigned long long s_keys[SORT_STAGE];
+  const uint32_t b0 = blockIdx.x * SORT_BUCKETS, b1 = min(b0 + SORT_BUCKETS, nb), b = b0 + threadIdx.x;
+  const uint32_t k0 = boff[b0], k1 = b1 < nb ? boff[b1] : n;
+  auto isort = [](unsigned long long* a, uint32_t lo, uint32_t hi) {
+    for (uint32_t i = lo + 1; i < hi; ++i) {
+      const unsigned long long kx = a[i];
+      uint32_t j = i;
+      while (j > lo) {
+        const unsigned long long ky = a[j - 1];
+        if (ky <= kx) break;
+        a[j] = ky;
+        --j;
+      }
+      a[j] = kx;
     }
-    keys[j] = kx;
+  };
+  if (k1 - k0 <= SORT_STAGE) {
+    for (uint32_t i = k0 + threadIdx.x; i < k1; i += SORT_BUCKETS) s_keys[i - k0] = keys[i];
+    __syncthreads();
+    if (b < b1) isort(s_keys, boff[b] - k0, (b + 1 < nb ? boff[b + 1] : n) - k0);
+    __syncthreads();
+    for (uint32_t i = k0 + threadIdx.x; i < k1; i += SORT_BUCKETS) order[i] = uint32_t(s_keys[i - k0]);
+  } else {
+    if (b >= b1) return;
+    const uint32_t lo = boff[b], hi = (b + 1 < nb) ? boff[b + 1] : n;
+    isort(keys, lo, hi);
+    for (uint32_t i = lo; i < hi; ++i) order[i] = uint32_t(keys[i]);
   }
-  for (uint32_t i = lo; i < hi; ++i) order[i] = uint32_t(keys[i]);
 }
 
 // The gather of the sorted columns through 32-byte records: every slot's
@@ -835,7 +855,7 @@ void sort_by_locus(const PlaceOut& o, uint32_t n, uint64_t G, uint32_t* bcnt, ui
   k_bucket_count<<<nblk(n), 256, 0, st>>>(o.locus, n, bcnt); note_launch();
   scan_rows<uint32_t>(bcnt, bcnt, nb, 1, part, nullptr, st);
   k_bucket_scatter_keys<<<nblk(n), 256, 0, st>>>(o.locus, n, bcnt, bfill, keys); note_launch();
-  k_bucket_sort_keys<<<nblk(nb), 256, 0, st>>>(bcnt, nb, n, keys, order); note_launch();
+  k_bucket_sort_keys<<<nblk(nb, SORT_BUCKETS), SORT_BUCKETS, 0, st>>>(bcnt, nb, n, keys, order); note_launch();
   k_pack_records<<<nblk(n), 256, 0, st>>>(o, nullptr, n, recs); note_launch();
   k_gather_records<<<nblk(n), 256, 0, st>>>(recs, order, n, sorted, nullptr); note_launch();
 }
@@ -882,7 +902,8 @@ void sort_batch(const PlaceOut& o, const uint16_t* inst_of, uint32_t n, uint32_t
   k_bucket_count_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt); note_launch();
   scan_rows<uint32_t>(bcnt, bcnt, nbt, 1, part, bcnt + nbt, st);
   k_bucket_scatter_b<<<nblk(n), 256, 0, st>>>(o.locus, inst_of, n, nb, bcnt, bfill, keys); note_launch();
-  k_bucket_sort_keys<<<nblk(nbt), 256, 0, st>>>(bcnt, uint32_t(nbt), n, keys, order); note_launch();
+  k_bucket_sort_keys<<<nblk(nbt, SORT_BUCKETS), SORT_BUCKETS, 0, st>>>(bcnt, uint32_t(nbt), n, keys, order);
+  note_launch();
   k_pack_records<<<nblk(n), 256, 0, st>>>(o, inst_of, n, recs); note_launch();
   k_gather_records<<<nblk(n), 256, 0, st>>>(recs, order, n, sorted, inst_sorted); note_launch();
 }
