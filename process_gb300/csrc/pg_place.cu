@@ -341,6 +341,7 @@ __global__ void k_place_first(PlaceTables t, PlaceOut o, Key key, const uint32_t
 // A barrier wait gives up after TAIL_SPIN_LIMIT polls (status bit 2); every
 // block then leaves at its next barrier, which also gives up.
 constexpr uint32_t TAIL_SPIN_LIMIT = 1u << 22;
+constexpr uint32_t TAIL_SOLO = 2048;   // pending slots below which one block runs the rounds
 
 __device__ __forceinline__ bool grid_barrier(TailCtl* __restrict__ c, uint32_t& gen) {
   __shared__ uint32_t s_ok;
@@ -374,9 +375,16 @@ __global__ void __launch_bounds__(256) k_sites_tail(PlaceTables t, PlaceOut o, K
                                                     const uint32_t* __restrict__ off_id, uint32_t n_snv,
                                                     TailArgs a, TailCtl* __restrict__ ctl, uint32_t* __restrict__ err) {
   uint32_t gen = 0;
-  const uint32_t nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cur = 0;
   bool ident = a.identity_first != 0;
+  // once few slots are pending, block 0 runs the remaining rounds alone
+  // (block barriers instead of grid barriers)
+  bool solo = gridDim.x == 1;
+  auto sync = [&]() -> bool {
+    if (solo) { __syncthreads(); return true; }
+    return grid_barrier(ctl, gen);
+  };
   if (a.redraw_first) {   // list 0 holds the first round's losers: redraw them
     const uint32_t n = ctl_load(&ctl->count[0]);
     for (uint32_t i = tid; i < n; i += nthr) place_slot(t, o, key, off_snv, off_id, n_snv, a.list[0][i], 1, err);
@@ -385,6 +393,12 @@ __global__ void __launch_bounds__(256) k_sites_tail(PlaceTables t, PlaceOut o, K
   for (uint32_t round = a.round0;; ++round) {
     const uint32_t n = ctl_load(cur ? &ctl->count[1] : &ctl->count[0]);
     if (n == 0) break;
+    if (!solo && n <= TAIL_SOLO) {   // every block reads the same count after the barrier
+      if (blockIdx.x != 0) return;
+      solo = true;
+      nthr = blockDim.x;
+      tid = threadIdx.x;
+    }
     if (round >= TAIL_MAX_ROUND) {
       if (tid == 0) atomicOr(&ctl->status, TAIL_ROUNDS_EXHAUSTED);
       break;
@@ -405,7 +419,7 @@ __global__ void __launch_bounds__(256) k_sites_tail(PlaceTables t, PlaceOut o, K
         }
         a.hpos[i] = h;
       }
-      if (!grid_barrier(ctl, gen)) return;
+      if (!sync()) return;
       for (uint32_t i = tid; i < n; i += nthr) {
         const uint32_t slot = ident ? i : pend[i];
         const uint32_t h = a.hpos[i];
@@ -421,7 +435,7 @@ __global__ void __launch_bounds__(256) k_sites_tail(PlaceTables t, PlaceOut o, K
         if (o.locus[slot] == LOCUS_INVALID) next[atomicAdd(n_next, 1u)] = slot;
       }
     }
-    if (!grid_barrier(ctl, gen)) return;
+    if (!sync()) return;
     // redraw the losers; clear the candidate entries of this round
     const uint32_t nn = ctl_load(n_next);
     for (uint32_t i = tid; i < nn; i += nthr) place_slot(t, o, key, off_snv, off_id, n_snv, next[i], 1, err);
@@ -431,7 +445,7 @@ __global__ void __launch_bounds__(256) k_sites_tail(PlaceTables t, PlaceOut o, K
         if (h != EMPTY) { a.ckeys[h] = EMPTY; a.cvals[h] = EMPTY; }
       }
     if (tid == 0) { ctl->count[cur] = 0u; ctl->rounds = round + 1u; }
-    if (!grid_barrier(ctl, gen)) return;
+    if (!sync()) return;
     cur ^= 1u;
     ident = false;
   }
@@ -682,8 +696,13 @@ __global__ void __launch_bounds__(256) k_sites_tail_b(const PlaceTables* __restr
                                                       TailArgsB a, TailCtl* __restrict__ ctl,
                                                       uint32_t* __restrict__ err) {
   uint32_t gen = 0;
-  const uint32_t nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cur = 0;
+  bool solo = gridDim.x == 1;   // as k_sites_tail: block 0 alone once few slots are pending
+  auto sync = [&]() -> bool {
+    if (solo) { __syncthreads(); return true; }
+    return grid_barrier(ctl, gen);
+  };
   {   // list 0 holds the first round's losers: redraw them
     const uint32_t n = ctl_load(&ctl->count[0]);
     for (uint32_t i = tid; i < n; i += nthr)
@@ -693,6 +712,12 @@ __global__ void __launch_bounds__(256) k_sites_tail_b(const PlaceTables* __restr
   for (uint32_t round = 1;; ++round) {
     const uint32_t n = ctl_load(cur ? &ctl->count[1] : &ctl->count[0]);
     if (n == 0) break;
+    if (!solo && n <= TAIL_SOLO) {
+      if (blockIdx.x != 0) return;
+      solo = true;
+      nthr = blockDim.x;
+      tid = threadIdx.x;
+    }
     if (round >= TAIL_MAX_ROUND) {
       if (tid == 0) atomicOr(&ctl->status, TAIL_ROUNDS_EXHAUSTED);
       break;
@@ -713,7 +738,7 @@ __global__ void __launch_bounds__(256) k_sites_tail_b(const PlaceTables* __restr
       }
       a.hpos[i] = h;
     }
-    if (!grid_barrier(ctl, gen)) return;
+    if (!sync()) return;
     for (uint32_t i = tid; i < n; i += nthr) {
       const uint32_t slot = pend[i];
       const uint64_t h = a.hpos[i];
@@ -724,7 +749,7 @@ __global__ void __launch_bounds__(256) k_sites_tail_b(const PlaceTables* __restr
         next[atomicAdd(n_next, 1u)] = slot;
       }
     }
-    if (!grid_barrier(ctl, gen)) return;
+    if (!sync()) return;
     const uint32_t nn = ctl_load(n_next);
     for (uint32_t i = tid; i < nn; i += nthr)
       place_slot_b(tabs, n_inst, cell_off, keys, o, inst_of, off_snv, off_id, n_snv, next[i], 1, err);
@@ -733,7 +758,7 @@ __global__ void __launch_bounds__(256) k_sites_tail_b(const PlaceTables* __restr
       if (h != EMPTY64) { a.ckeys[h] = EMPTY64; a.cvals[h] = EMPTY; }
     }
     if (tid == 0) { ctl->count[cur] = 0u; ctl->rounds = round + 1u; }
-    if (!grid_barrier(ctl, gen)) return;
+    if (!sync()) return;
     cur ^= 1u;
   }
 }

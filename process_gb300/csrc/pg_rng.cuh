@@ -35,6 +35,28 @@ __device__ __forceinline__ U4 philox(uint32_t k0, uint32_t k1,
   return {c0, c1, c2, c3};
 }
 
+// The round keys of one key, computed on the host: a kernel that takes them
+// as a parameter reads them as constant operands instead of stepping the
+// key schedule per block (the same words as philox()).
+struct RoundKeys { uint32_t k0[10], k1[10]; };
+
+__host__ __device__ inline RoundKeys round_keys(uint32_t k0, uint32_t k1) {
+  RoundKeys r;
+  for (int i = 0; i < 10; ++i) { r.k0[i] = k0; r.k1[i] = k1; k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+  return r;
+}
+
+__device__ __forceinline__ U4 philox(const RoundKeys& rk, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ rk.k0[i], n2 = hi0 ^ c3 ^ rk.k1[i];
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+  return {c0, c1, c2, c3};
+}
+
 // Stream tags (counter word c3). One tag per kind of decision keeps the
 // streams of different decisions disjoint for the same object id.
 enum : uint32_t {

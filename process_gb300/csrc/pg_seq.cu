@@ -320,13 +320,21 @@ __device__ __forceinline__ uint32_t part_offset(uint32_t u, uint32_t lo, uint32_
 // CN selects the copy-number path at compile time (0: no copy-number
 // events, 1: the tile's tables in shared memory, 2: the tables in global
 // memory) or, -1, at run time from prm.has_cna and cc.
-template <bool INS_SMEM, int CN = -1>
-__device__ __forceinline__ Fragment make_fragment(Key key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
+// (KeyT: Key, or the precomputed RoundKeys of the same key)
+__device__ __forceinline__ U4 pair_block(const Key& key, uint32_t j, uint32_t t, uint32_t s) {
+  return philox(key.k0, key.k1, j, t, s, TAG_PAIR);
+}
+__device__ __forceinline__ U4 pair_block(const RoundKeys& rk, uint32_t j, uint32_t t, uint32_t s) {
+  return philox(rk, j, t, s, TAG_PAIR);
+}
+
+template <bool INS_SMEM, int CN = -1, class KeyT>
+__device__ __forceinline__ Fragment make_fragment(const KeyT& key, uint32_t j, uint32_t t, uint32_t s, uint32_t start,
                                                   uint32_t len, uint32_t ce, const SeqSample& sm,
                                                   const uint32_t* __restrict__ leaf_tin, const SeqParams& prm,
                                                   const uint32_t* ins, const uint16_t* guide,
                                                   const CnCache* cc = nullptr) {
-  const U4 r = philox(key.k0, key.k1, j, t, s, TAG_PAIR);
+  const U4 r = pair_block(key, j, t, s);
   Fragment f;
   const uint32_t R = prm.read_len;
   const int path = CN >= 0 ? CN : (!prm.has_cna ? 0 : (cc ? 1 : 2));
@@ -408,10 +416,11 @@ struct ReadSmem {
 // records [lo, lo + nw) of g_recs) for sample s, counted into the rows
 // g_alt_row / g_dep_row (indexed by record).  Called by every thread of the
 // CTA with the same arguments.
+template <class KeyT>
 __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict__ g_recs, uint32_t t, uint32_t s,
                                           uint32_t n_pairs, uint32_t lo, uint32_t nw, uint32_t start, uint32_t len,
                                           uint32_t ce, const SeqSample& sm, const uint32_t* __restrict__ leaf_tin,
-                                          const SeqParams& prm, Key key, uint32_t* __restrict__ g_alt_row,
+                                          const SeqParams& prm, const KeyT& key, uint32_t* __restrict__ g_alt_row,
                                           uint32_t* __restrict__ g_dep_row) {
   auto& s_locus = sh.s_locus; auto& s_tin = sh.s_tin; auto& s_tout = sh.s_tout; auto& s_info = sh.s_info;
   auto& s_alt = sh.s_alt; auto& s_dep = sh.s_dep;
@@ -611,7 +620,7 @@ __global__ void __launch_bounds__(SEQ_THREADS, 4) k_reads(const SeqRec* __restri
                                                           const uint32_t* __restrict__ pair_cnt,
                                                           const SeqSample* __restrict__ samples,
                                                           const uint32_t* __restrict__ leaf_tin, SeqParams prm,
-                                                          Key key, uint64_t n_recs, uint32_t* __restrict__ g_alt,
+                                                          RoundKeys key, uint64_t n_recs, uint32_t* __restrict__ g_alt,
                                                           uint32_t* __restrict__ g_dep) {
   __shared__ ReadSmem sh;
   const uint32_t t = blockIdx.x, s = blockIdx.y;
@@ -1110,8 +1119,9 @@ void seq_reads(const SeqRec* recs, uint32_t n_recs, const SeqTiles& tiles, const
                uint64_t seed, uint32_t* alt, uint32_t* depth, cudaStream_t st) {
   if (tiles.n_tiles == 0 || n_samples == 0 || n_recs == 0) return;
   dim3 grid(tiles.n_tiles, n_samples);
-  k_reads<<<grid, SEQ_THREADS, 0, st>>>(recs, tiles, pair_cnt, samples, leaf_tin, prm, make_key(seed), n_recs, alt,
-                                         depth); note_launch();
+  const Key k = make_key(seed);
+  k_reads<<<grid, SEQ_THREADS, 0, st>>>(recs, tiles, pair_cnt, samples, leaf_tin, prm, round_keys(k.k0, k.k1), n_recs,
+                                         alt, depth); note_launch();
 }
 
 void seq_batch_records(const PlaceOut& sorted, const uint16_t* inst_sorted, const uint32_t* n_dev, uint32_t cap,
