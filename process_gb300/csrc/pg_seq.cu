@@ -238,12 +238,18 @@ __device__ __forceinline__ bool inst_carries(const SeqParams& prm, uint32_t y, u
 __device__ __forceinline__ bool observed(const SeqParams& prm, uint32_t tin, uint32_t tout, uint32_t info,
                                          uint32_t cell, uint32_t inst, uint32_t wm, uint32_t locus) {
   // the cell is in the edge's subtree when tin <= cell < tout (one unsigned compare)
-  const bool carried = (cell - tin < tout - tin) &&
-                       inst_carries(prm, inst, info & 0xffffu, (uint64_t(tin) << 16) | ((info >> 16) & 0x7fffu));
-  if (info >> 31) return carried;   // indel
+  // branch-free but for the lineage walk of a copied instance: the error
+  // word is computed for indels too, and the caller evaluates every
+  // candidate mate (covering or not), so that a warp does not diverge
+  const bool sub = cell - tin < tout - tin;
+  const uint32_t x = info & 0xffffu;
+  bool carried = sub && inst == x;
+  if (sub && inst != x && prm.has_cna)
+    carried = inst_carries(prm, inst, x, (uint64_t(tin) << 16) | ((info >> 16) & 0x7fffu));
   const uint32_t e = err_word(wm, locus);
   const bool err = e < prm.err_thr;
-  return carried ? !err : (err && (e % 3u) == 0u);
+  const bool snv = carried ? !err : (err & ((e % 3u) == 0u));
+  return (info >> 31) ? carried : snv;
 }
 
 // One fragment's draws: mate starts, source cell, allele instance and its
@@ -595,10 +601,10 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
           const uint32_t pi = s_mpi[x];
           const uint2 cw = s_mcw[x];                          // one 32-bit and one 64-bit load
           // the mate covers L when its start o is in (L - R, L] (unsigned: o > off wraps)
-          if (off - (pi & 0xffffu) >= R) continue;
-          dep += 1;
-          const uint32_t mi = pi >> 16, ca = cw.x, w = cw.y;
-          alt += observed(prm, tin, tout, info, ca, mi, w, L) ? 1u : 0u;
+          const bool cov = off - (pi & 0xffffu) < R;
+          const bool ob = observed(prm, tin, tout, info, cw.x, pi >> 16, cw.y, L);
+          dep += cov ? 1u : 0u;
+          alt += (cov & ob) ? 1u : 0u;
         }
         if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
       }
