@@ -588,7 +588,7 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
         uint32_t L = s_locus[i], off = L - start, tin = s_tin[i], tout = s_tout[i], info = s_info[i];
         uint32_t base = s_wstart[i] - s_wpre[i];
         uint32_t dep = 0, alt = 0;
-        for (uint32_t k = k0; k < k1; ++k) {
+        for (uint32_t k = k0; k < k1;) {
           while (k >= next) {                                 // the run of the next record starts
             if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
             dep = 0; alt = 0;
@@ -597,14 +597,19 @@ __device__ __forceinline__ void read_tile(ReadSmem& sh, const SeqRec* __restrict
             L = s_locus[i]; off = L - start; tin = s_tin[i]; tout = s_tout[i]; info = s_info[i];
             base = s_wstart[i] - s_wpre[i];
           }
-          const uint32_t x = base + k;
-          const uint32_t pi = s_mpi[x];
-          const uint2 cw = s_mcw[x];                          // one 32-bit and one 64-bit load
+          // two visits of the same record at a time when the run allows it
+          const uint32_t nv = (k + 1 < next && k + 1 < k1) ? 2u : 1u;
+          const uint32_t x = base + k, x1 = nv == 2u ? x + 1u : x;
+          const uint32_t pi = s_mpi[x], pj = s_mpi[x1];
+          const uint2 cw = s_mcw[x], cv = s_mcw[x1];
           // the mate covers L when its start o is in (L - R, L] (unsigned: o > off wraps)
           const bool cov = off - (pi & 0xffffu) < R;
+          const bool cov1 = nv == 2u && off - (pj & 0xffffu) < R;
           const bool ob = observed(prm, tin, tout, info, cw.x, pi >> 16, cw.y, L);
-          dep += cov ? 1u : 0u;
-          alt += (cov & ob) ? 1u : 0u;
+          const bool ob1 = observed(prm, tin, tout, info, cv.x, pj >> 16, cv.y, L);
+          dep += (cov ? 1u : 0u) + (cov1 ? 1u : 0u);
+          alt += ((cov & ob) ? 1u : 0u) + ((cov1 & ob1) ? 1u : 0u);
+          k += nv;
         }
         if (dep) { atomicAdd(s_dep + i, dep); if (alt) atomicAdd(s_alt + i, alt); }
       }
