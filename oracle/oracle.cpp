@@ -1097,13 +1097,19 @@ SeqSetup seq_setup(const Placed& pl, const SeqCfg& c) {
 // error words (the read kernel's mate_word / err_word in pg_seq.cu): a
 // mate's word is the fragment's error word (the XOR of the four words of its
 // Philox block) for mate 0 and w * 0x85EBCA6B + 0x27D4EB2F for mate 1; the
-// visit of a mate to `locus` hashes it with the locus by one odd multiply
-// and a xorshift
+// visit of a mate to `locus` hashes it with the locus by one odd multiply.
+// A word below the error threshold thr is a substitution error; the
+// erroneous base is the first, second or third of the other bases as the
+// word lies in [0, thr/3), [thr/3, 2thr/3) or [2thr/3, thr) (integer thirds)
 uint32_t mate_word(uint32_t w, uint32_t mate) { return mate ? w * 0x85EBCA6Bu + 0x27D4EB2Fu : w; }
 
 uint32_t error_word(uint32_t w, uint32_t locus, uint32_t mate) {
-  uint32_t h = (mate_word(w, mate) ^ (locus * 0x9E3779B1u)) * 0xC2B2AE35u;
-  return h ^ (h >> 16);
+  return (mate_word(w, mate) ^ (locus * 0x9E3779B1u)) * 0xC2B2AE35u;
+}
+
+uint32_t error_third(uint32_t e, uint32_t thr) {
+  const uint32_t t1 = thr / 3u, t2 = uint32_t(uint64_t(thr) * 2u / 3u);
+  return e < t1 ? 0u : (e < t2 ? 1u : 2u);
 }
 
 // Allele instances carrying mutation i: its own instance and every copy made
@@ -1144,7 +1150,7 @@ void count_mate(const Placed& pl, const Carrier& car, const std::vector<std::vec
     else {
       const uint32_t e = error_word(w, pl.locus[i], mate);
       const bool err = e < err_thr;
-      obs = carried ? !err : (err && e % 3 == 0);   // the erroneous base is one of three
+      obs = carried ? !err : (err && error_third(e, err_thr) == 0);   // the erroneous base is one of three
     }
     dep[i] += 1;
     if (obs) alt[i] += 1;
@@ -1384,7 +1390,7 @@ void seq_replay(const Placed& pl, const SeqCfg& c, uint64_t seed, SeqOut& out, c
 // shows, position by position, the reference base, or the alt base of an SNV
 // its allele carries (the first such record at the position), or a
 // substitution where the visit's error word is below the error threshold:
-// one of the three other bases, chosen by word % 3 among them in the order
+// one of the three other bases, chosen by error_third among them in the order
 // (counterpart allele first at an SNV site -- the alt base when the read
 // shows the reference, the reference base when it shows the alt --, then
 // the rest ascending).  Unknown reference bases read N.  After the anchor of
@@ -1436,7 +1442,7 @@ OracleRead oracle_read(const Placed& pl, const Carrier& car, const std::vector<s
     }
     uint32_t tb = carried_snv ? alt : b;
     const uint32_t ew = error_word(fw, q, mate);
-    if (ew < err_thr) tb = other_base(tb, site ? int(carried_snv ? b : alt) : -1, ew % 3u);
+    if (ew < err_thr) tb = other_base(tb, site ? int(carried_snv ? b : alt) : -1, error_third(ew, err_thr));
     out.seq.push_back(b > 3 ? 'N' : ACGT[tb]);
     push('M', 1);
     ++q;
@@ -1446,7 +1452,7 @@ OracleRead oracle_read(const Placed& pl, const Carrier& car, const std::vector<s
         for (uint32_t k = 0; k < l && out.seq.size() < R; ++k) {
           uint32_t ib = (indel >> (8 + 2 * k)) & 3u;
           const uint32_t ei = error_word(mate_word(fw, mate) ^ (0x9E3779B1u * (k + 1)), q - 1, 0);
-          if (ei < err_thr) ib = other_base(ib, -1, ei % 3u);
+          if (ei < err_thr) ib = other_base(ib, -1, error_third(ei, err_thr));
           out.seq.push_back(ACGT[ib]);
           push('I', 1);
         }

@@ -1978,6 +1978,7 @@ void simulate_seq_impl(const pg_placed* pl, const pg_seq_cfg* c, uint64_t seed, 
     prm.ins_guide = guide_d.p;
     double et = std::floor(c->error_rate * 4294967296.0);
     prm.err_thr = et >= 4294967295.0 ? 0xffffffffu : uint32_t(et);
+    pg::err_thirds(prm.err_thr, prm.err_t1, prm.err_t2);
     prm.normal_tin = N;
     prm.n_alleles = 2;
     prm.has_cna = pl->has_cna ? 1u : 0u;

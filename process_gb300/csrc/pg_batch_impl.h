@@ -331,6 +331,7 @@ void batch_layout(pg_batch* b) {
     prm.ins_min = ins_min; prm.n_ins = uint32_t(thr.size());
     double et = std::floor(c.error_rate * 4294967296.0);
     prm.err_thr = et >= 4294967295.0 ? 0xffffffffu : uint32_t(et);
+    pg::err_thirds(prm.err_thr, prm.err_t1, prm.err_t2);
     prm.normal_tin = N;
     prm.n_alleles = 2;
     prm.has_cna = 0;

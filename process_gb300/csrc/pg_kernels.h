@@ -211,6 +211,13 @@ struct SeqSample {
   uint32_t opt_off, n_opt, opt_cdf_off;
 };
 
+// The thresholds that split a substitution error's word range [0, thr) into
+// the three other bases: [0, t1), [t1, t2), [t2, thr).
+inline void err_thirds(uint32_t thr, uint32_t& t1, uint32_t& t2) {
+  t1 = thr / 3u;
+  t2 = uint32_t(uint64_t(thr) * 2u / 3u);
+}
+
 struct SeqParams {
   uint32_t read_len;
   uint32_t paired;
@@ -219,6 +226,8 @@ struct SeqParams {
   const uint32_t* ins_cdf;
   const uint16_t* ins_guide; // 256 entries: first index whose threshold exceeds g * 2^23
   uint32_t err_thr;        // substitution error iff u < err_thr
+  uint32_t err_t1, err_t2; // the erroneous base: the first of the three others iff u < err_t1,
+                           //   the second iff err_t1 <= u < err_t2, else the third
   uint32_t normal_tin;     // Euler index of normal cells
   uint32_t n_alleles;
   // copy-number state (has_cna == 0: every cell has instances 0 and 1 everywhere)

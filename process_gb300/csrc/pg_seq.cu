@@ -22,10 +22,11 @@
 //     when it carries the mutation (edge is an ancestor of the cell, same
 //     allele) and the base is not hit by a substitution error, or when it
 //     does not carry it and an error turns the reference into that alt base.
-//     The error word of a (fragment, mate, locus) visit is the MurmurHash3
-//     fmix32 finaliser of the fragment's error word (the XOR of its Philox
-//     block) mixed with the locus and the mate; an error happens when it is below err_thr, and the erroneous
-//     base is one of the three others, word % 3 == 0 being the alt base.
+//     The error word of a (mate, locus) visit is a multiplicative hash of the
+//     mate's word (from the XOR of the fragment's Philox block) and the
+//     locus; an error happens when it is below err_thr, and the erroneous
+//     base is one of the three others by the third of [0, err_thr) the word
+//     falls in, the first third being the alt base.
 //     Indels are not affected by substitution errors.
 //
 // Kernel layout (one CTA per (tile, sample); fragments in batches):
@@ -211,14 +212,18 @@ __global__ void k_tile_split_level(uint32_t level, uint32_t n_slots, const uint3
 
 // Error words.  A mate's word: the fragment's error word for mate 0, an
 // odd affine map of it for mate 1.  The visit of a mate (word wm) to locus:
-// a multiplicative hash whose high bits decide the substitution error
-// (e < err_thr) and whose value mod 3 picks the erroneous base.
+// a multiplicative hash (uniform, as wm is), compared with err_thr for the
+// substitution error and with its thirds err_t1, err_t2 for the erroneous
+// base.
 __device__ __forceinline__ uint32_t mate_word(uint32_t w, uint32_t mate) {
   return mate ? w * 0x85EBCA6Bu + 0x27D4EB2Fu : w;
 }
 __device__ __forceinline__ uint32_t err_word(uint32_t wm, uint32_t locus) {
-  uint32_t h = (wm ^ (locus * 0x9E3779B1u)) * 0xC2B2AE35u;
-  return h ^ (h >> 16);
+  return (wm ^ (locus * 0x9E3779B1u)) * 0xC2B2AE35u;
+}
+// which of the three other bases an error word below err_thr picks
+__device__ __forceinline__ uint32_t err_third(const SeqParams& prm, uint32_t e) {
+  return e < prm.err_t1 ? 0u : (e < prm.err_t2 ? 1u : 2u);
 }
 
 // does allele instance y of the read's cell carry the mutation placed on
@@ -240,15 +245,16 @@ __device__ __forceinline__ bool observed(const SeqParams& prm, uint32_t tin, uin
   // the cell is in the edge's subtree when tin <= cell < tout (one unsigned compare)
   // branch-free but for the lineage walk of a copied instance: the error
   // word is computed for indels too, and the caller evaluates every
-  // candidate mate (covering or not), so that a warp does not diverge
+  // candidate mate (covering or not), so that a warp does not diverge.
+  // A copy has a larger instance number than its source, and instances 0
+  // and 1 have no source: the walk is needed only when inst > max(x, 1).
   const bool sub = cell - tin < tout - tin;
   const uint32_t x = info & 0xffffu;
   bool carried = sub && inst == x;
-  if (sub && inst != x && prm.has_cna)
+  if (sub && inst > max(x, 1u) && prm.has_cna)
     carried = inst_carries(prm, inst, x, (uint64_t(tin) << 16) | ((info >> 16) & 0x7fffu));
   const uint32_t e = err_word(wm, locus);
-  const bool err = e < prm.err_thr;
-  const bool snv = carried ? !err : (err & ((e % 3u) == 0u));
+  const bool snv = carried ? e >= prm.err_thr : e < prm.err_t1;
   return (info >> 31) ? carried : snv;
 }
 
@@ -649,7 +655,8 @@ static inline unsigned nblk(uint64_t n, int b = 256) { return unsigned((n + b - 
 // the carried SNVs (alt base) and indels (inserted bases; skipped deleted
 // bases, anchored at the base before them), and a substitution wherever the
 // visit's error word is below the threshold.  A substitution picks one of the
-// three other bases with (word % 3); at an SNV site the first of them is the
+// three other bases by the third of [0, err_thr) its word falls in; at an SNV
+// site the first of them is the
 // counterpart allele (the alt base when the read shows the reference, the
 // reference when it shows the alt), so that the bases agree with the alt
 // counts of the read kernel.  Inserted bases draw their errors from the word
@@ -693,7 +700,7 @@ __device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ ge
     }
     uint32_t tb = carried_snv ? alt : b;
     const uint32_t e = err_word(wm, q);
-    if (e < prm.err_thr) tb = others(tb, site ? int(carried_snv ? b : alt) : -1, e % 3u);
+    if (e < prm.err_thr) tb = others(tb, site ? int(carried_snv ? b : alt) : -1, err_third(prm, e));
     // an unknown reference base (N) reads as N
     const bool unknown = prm.nmask && ((__ldg(prm.nmask + (q >> 5)) >> (q & 31u)) & 1u);
     seq[n++] = unknown ? 'N' : ACGT[tb];
@@ -705,7 +712,7 @@ __device__ void build_read(const SeqParams& prm, const uint32_t* __restrict__ ge
         for (uint32_t k = 0; k < l && n < R; ++k) {
           uint32_t ib = (indel >> (8 + 2 * k)) & 3u;
           const uint32_t ei = err_word(wm ^ (0x9E3779B1u * (k + 1)), q - 1);
-          if (ei < prm.err_thr) ib = others(ib, -1, ei % 3u);
+          if (ei < prm.err_thr) ib = others(ib, -1, err_third(prm, ei));
           seq[n++] = ACGT[ib];
           push(1u, 1u);
         }
