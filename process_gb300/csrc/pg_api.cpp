@@ -235,6 +235,12 @@ struct pg_engine {
   std::vector<CnaSpec> cna_cands;                          // passenger CNA candidates
   bool infinite_sites = true;
   bool avoid_homozygous_losses = true;
+  // device copies of the last placed forest's columns (a forest is immutable:
+  // its uid keys them)
+  uint64_t fc_uid = 0;
+  DBuf<int32_t> fc_parent;
+  DBuf<double> fc_birth;
+  DBuf<uint32_t> fc_species, fc_div;
   // the caller's reference plus one per live placed/sequencing handle: the
   // engine (its pool and stream) outlives every handle that draws from it
   std::atomic<int> refs{1};
@@ -248,6 +254,7 @@ struct pg_engine {
 };
 
 struct pg_forest {
+  uint64_t uid = 0;                            // unique per forest (never reused): device-copy cache key
   uint32_t n = 0, n_samples = 0;
   std::vector<int32_t> parent, sample;
   std::vector<double> birth;
@@ -891,7 +898,9 @@ pg_status pg_forest_create(uint32_t n, const int32_t* parent, const double* birt
     require(out && parent && birth && species && sample, "NULL argument");
     require(n > 0, "empty forest");
     require(n < (1u << 30), "forest too large");
+    static std::atomic<uint64_t> next_uid{0};
     auto f = std::make_unique<pg_forest>();
+    f->uid = ++next_uid;
     f->n = n; f->n_samples = n_samples;
     f->parent.assign(parent, parent + n);
     f->birth.assign(birth, birth + n);
@@ -1008,10 +1017,14 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     }
     // ---- device tables
     Pool* P = &e->pool;
-    auto parent_d = upload(P, f->parent, st);
-    auto birth_d = upload(P, f->birth, st);
-    auto species_d = upload(P, f->species, st);
-    auto div_d = upload(P, f->divisions, st);
+    if (e->fc_uid != f->uid) {      // the last placed forest's columns stay on the device
+      e->fc_uid = 0;
+      e->fc_parent = upload(P, f->parent, st);
+      e->fc_birth = upload(P, f->birth, st);
+      e->fc_species = upload(P, f->species, st);
+      e->fc_div = upload(P, f->divisions, st);
+      e->fc_uid = f->uid;
+    }
     auto times_d = upload(P, times, st);
     auto snv_d = upload(P, snv_rate, st);
     auto id_d = upload(P, id_rate, st);
@@ -1029,7 +1042,8 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     passenger_cnas = passenger_cnas && !e->cna_cands.empty();
     auto cna_d = upload(P, cna_rate, st);
     pg::PlaceTables t{};
-    t.n_nodes = f->n; t.parent = parent_d.p; t.birth = birth_d.p; t.species = species_d.p; t.divisions = div_d.p;
+    t.n_nodes = f->n; t.parent = e->fc_parent.p; t.birth = e->fc_birth.p; t.species = e->fc_species.p;
+    t.divisions = e->fc_div.p;
     t.n_epochs = E; t.epoch_start = times_d.p; t.snv_rate = snv_d.p; t.indel_rate = id_d.p; t.cna_rate = cna_d.p;
     t.n_sbs_sigs = std::max<uint32_t>(e->n_sig[0], 1); t.n_id_sigs = std::max<uint32_t>(e->n_sig[1], 1);
     t.sbs_expo_cdf = sbs_expo_d.p; t.sbs_sig_cdf = sbs_sig_d.p; t.id_expo_cdf = id_expo_d.p; t.id_sig_cdf = id_sig_d.p;
@@ -1057,10 +1071,12 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     std::vector<uint32_t> node_class(f->n + 1, 0);
     std::vector<pg::DriverRec> drv;
     uint32_t drv_index = 0;
-    auto mut_of = [&](uint32_t node) {
-      auto it = e->species.find(f->species[node]);
-      return it == e->species.end() ? 0u : it->second.mutant;
-    };
+    std::vector<uint32_t> mutant_of(S, 0u);
+    for (uint32_t s2 = 0; s2 < S; ++s2) {
+      auto it = e->species.find(s2);
+      if (it != e->species.end()) mutant_of[s2] = it->second.mutant;
+    }
+    auto mut_of = [&](uint32_t node) { return mutant_of[f->species[node]]; };
     // order key of the copy made by event j on edge v (see SEQ_PASSENGER)
     auto key_of = [&](uint32_t v, uint32_t j) { return (uint64_t(f->tin[v]) << 16) | (j + 1u); };
     for (uint32_t v = 0; v < f->n; ++v) {
@@ -1170,10 +1186,24 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
       }
     }
     require(insts.size() < 0xffff, "too many allele instances");
-    // ---- class tables (segments), node sizes, instance lineage chains
+    // ---- node sizes, then the per-edge counts (they need nothing else of
+    // the classes), launched before the host builds the class tables
+    std::vector<double> class_size(classes.size());
+    for (size_t c = 0; c < classes.size(); ++c) class_size[c] = double(pg::frag_size(classes[c]));
+    std::vector<double> node_size(f->n + 1);
+    for (uint32_t v = 0; v < f->n; ++v) node_size[v] = class_size[node_class[v]];
+    node_size[f->n] = class_size[0];
+    auto node_size_d = upload(P, node_size, st);
+    t.node_size = node_size_d.p;
+    const uint64_t ncell = uint64_t(f->n + 1) * E;
+    DBuf<uint32_t> cnt_snv(P, ncell), cnt_id(P, ncell), off_snv(P, ncell), off_id(P, ncell);
+    DBuf<uint32_t> part(P, pg::scan_part_elems(ncell, 1)), tot(P, 2);
+    pg::place_edge_counts(t, cnt_snv.p, cnt_id.p, seed, n_pre_snv, n_pre_id, st);
+    pg::scan_rows<uint32_t>(cnt_snv.p, off_snv.p, ncell, 1, part.p, tot.p, st);
+    pg::scan_rows<uint32_t>(cnt_id.p, off_id.p, ncell, 1, part.p, tot.p + 1, st);
+    // ---- class tables (segments) and instance lineage chains
     std::vector<uint32_t> seg_off{0}, seg_start, seg_end, seg_ioff, seg_icnt;
     std::vector<uint16_t> inst_list;
-    std::vector<double> class_size(classes.size());
     uint32_t cn_max = 0;
     for (size_t c = 0; c < classes.size(); ++c) {
       for (const auto& sg : pg::segments_of(classes[c])) {
@@ -1183,11 +1213,7 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
         cn_max = std::max<uint32_t>(cn_max, uint32_t(sg.insts.size()));
       }
       seg_off.push_back(uint32_t(seg_start.size()));
-      class_size[c] = double(pg::frag_size(classes[c]));
     }
-    std::vector<double> node_size(f->n + 1);
-    for (uint32_t v = 0; v < f->n; ++v) node_size[v] = class_size[node_class[v]];
-    node_size[f->n] = class_size[0];
     std::vector<uint32_t> chain_off{0};
     std::vector<uint16_t> chain_anc;
     std::vector<uint64_t> chain_key;
@@ -1249,17 +1275,8 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     pl->inst_list = upload(P, inst_list, st);
     if (chain_anc.empty()) { chain_anc.push_back(0); chain_key.push_back(0); }
     pl->chain_off = upload(P, chain_off, st); pl->chain_anc = upload(P, chain_anc, st); pl->chain_key = upload(P, chain_key, st);
-    auto node_size_d = upload(P, node_size, st);
-    t.node_size = node_size_d.p;
     t.gc = pl->classes_view();
-
-    // ---- per-edge counts and offsets
-    const uint64_t ncell = uint64_t(f->n + 1) * E;
-    DBuf<uint32_t> cnt_snv(P, ncell), cnt_id(P, ncell), off_snv(P, ncell), off_id(P, ncell);
-    DBuf<uint32_t> part(P, pg::scan_part_elems(ncell, 1)), tot(P, 2);
-    pg::place_edge_counts(t, cnt_snv.p, cnt_id.p, seed, n_pre_snv, n_pre_id, st);
-    pg::scan_rows<uint32_t>(cnt_snv.p, off_snv.p, ncell, 1, part.p, tot.p, st);
-    pg::scan_rows<uint32_t>(cnt_id.p, off_id.p, ncell, 1, part.p, tot.p + 1, st);
+    // ---- the edge counts' totals size the outputs
     uint32_t tot_h[2];
     ck(cudaMemcpyAsync(tot_h, tot.p, sizeof(tot_h), cudaMemcpyDeviceToHost, st), "counts");
     ck(cudaStreamSynchronize(st), "edge counts");
@@ -1267,15 +1284,6 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     const uint64_t n_all = n_snv + n_id + drv.size();
     require(n_all < (1ull << 31), "too many mutations for one placement call");
     // ---- outputs
-    pl->eng = e; pl->n_nodes = f->n; pl->n_samples = f->n_samples;
-    pl->tin = f->tin; pl->tout = f->tout; pl->leaves = f->leaves; pl->parent = f->parent;
-    pl->leaf_cls.assign(f->n_samples, {});
-    {
-      std::vector<uint8_t> has_kid(f->n, 0);
-      for (uint32_t v = 0; v < f->n; ++v) if (f->parent[v] >= 0) has_kid[f->parent[v]] = 1;
-      for (uint32_t v = 0; v < f->n; ++v)
-        if (!has_kid[v] && f->sample[v] >= 0) pl->leaf_cls[f->sample[v]].push_back(node_class[v]);
-    }
     pl->M = n_all;
     DBuf<uint32_t> locus(P, n_all), edge(P, n_all), aux(P, n_all), attempt(P, n_all);
     DBuf<uint8_t> cls(P, n_all), sig(P, n_all), kind(P, n_all), nature(P, n_all);
@@ -1306,6 +1314,16 @@ pg_status pg_place_mutations(pg_engine* e, const pg_forest* f, uint32_t n_pre_sn
     }
     auto drv_d = upload(P, drv, st);
     pg::place_drivers(o, drv_d.p, uint32_t(drv.size()), n_slots, st);
+    // the handle's host columns, while the first round runs
+    pl->eng = e; pl->n_nodes = f->n; pl->n_samples = f->n_samples;
+    pl->tin = f->tin; pl->tout = f->tout; pl->leaves = f->leaves; pl->parent = f->parent;
+    pl->leaf_cls.assign(f->n_samples, {});
+    {
+      std::vector<uint8_t> has_kid(f->n, 0);
+      for (uint32_t v = 0; v < f->n; ++v) if (f->parent[v] >= 0) has_kid[f->parent[v]] = 1;
+      for (uint32_t v = 0; v < f->n; ++v)
+        if (!has_kid[v] && f->sample[v] >= 0) pl->leaf_cls[f->sample[v]].push_back(node_class[v]);
+    }
     // ---- infinite sites, and loci drawn where the cell has no allele left.
     // Infinite sites: the first round over all slots against one table of
     // its candidates (drivers first), read back once to size the later

@@ -226,6 +226,21 @@ constexpr uint32_t IX_ROUNDS = 4;
 constexpr uint32_t IX_UNIT = 32 * IX_LANE_POS * IX_ROUNDS;   // 4096 positions
 constexpr int IX_WARPS = 8;
 
+// bit index of the n-th (from 0) set bit of m, n < popc(m): halving steps
+// on popcounts, without a data-dependent loop
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
+  uint32_t pos = 0;
+#pragma unroll
+  for (uint32_t w = 16; w >= 1; w >>= 1) {
+    const uint32_t c = __popc(m & ((1u << w) - 1u));
+    const bool up = n >= c;
+    n = up ? n - c : n;
+    pos = up ? pos + w : pos;
+    m = up ? m >> w : m;
+  }
+  return pos;
+}
+
 // even bits of x to the low half, odd bits to the high half (an inverse
 // perfect shuffle in four swap steps)
 __device__ __forceinline__ uint32_t unshuffle32(uint32_t x) {
@@ -464,15 +479,12 @@ __global__ void __launch_bounds__(32 * ix_warps(MODE)) k_index_scan(const uint32
           hit = (uint64_t(d) + uint64_t(q) * sd >= uint64_t(ex) + c) ? ex + c : d + q * sd;
         }
         if (hit < ex + c) {
+          // the lane's written hits have ranks r, r + sd, ... (< c) among its set bits
           const uint32_t len = s_len[k];
           const uint64_t off = s_off[k];
-          uint32_t mm = m, at = ex;
-          while (true) {
-            for (; at < hit; ++at) mm &= mm - 1u;
-            if (idx < len) lists[off + idx] = uint32_t(base + uint32_t(__ffs(mm) - 1));
-            if (uint64_t(hit) + sd >= uint64_t(ex) + c) break;
-            hit += sd;
-            ++idx;
+          for (uint32_t r = hit - ex;; r += sd, ++idx) {
+            if (idx < len) lists[off + idx] = uint32_t(base + nth_set_bit(m, r));
+            if (sd >= c - r) break;
           }
         }
         if (lane == 0) {

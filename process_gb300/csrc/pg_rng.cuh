@@ -257,6 +257,35 @@ __device__ __forceinline__ uint64_t binomial(Stream& st, uint64_t n, double p) {
   return flip ? n - k : k;
 }
 
+// The first attempt of binomial(st, n, p) alone: true, with k its result,
+// when binomial decides within that attempt without BTRS's exact test (the
+// trivial cases and the squeeze); false when it needs more (BINV, or an
+// attempt past the squeeze).  The expressions are binomial's, in its order,
+// so a true answer equals binomial's result; Stream is taken by value.
+__device__ __forceinline__ bool binomial_first(Stream st, uint64_t n, double p, uint64_t& k) {
+  if (n == 0 || !(p > 0.0)) { k = 0; return true; }
+  if (!(p < 1.0)) { k = n; return true; }
+  const bool flip = p > 0.5;
+  const double pp = flip ? 1.0 - p : p;
+  const double q = 1.0 - pp;
+  const double nd = double(n);
+  if (nd * pp < 10.0) return false;
+  const double spq = sqrt(nd * pp * q);
+  const double b = 1.15 + 2.53 * spq;
+  const double a = -0.0873 + 0.0248 * b + 0.01 * pp;
+  const double c = nd * pp + 0.5;
+  const double vr = 0.92 - 4.2 / b;
+  const U4 r = st.next();
+  const double U = u01_open(r.x, r.y) - 0.5;
+  const double V = u01_open(r.z, r.w);
+  const double us = 0.5 - fabs(U);
+  const double kd = floor((2.0 * a / us + b) * U + c);
+  if (kd < 0.0 || kd > nd) return false;
+  if (!(us >= 0.07 && V <= vr)) return false;
+  k = flip ? n - uint64_t(kd) : uint64_t(kd);
+  return true;
+}
+
 // Inverse-CDF lookup with integer thresholds: thr[k] = floor(CDF(k) * 2^31)
 // (the last class with positive mass holds 2^31); returns the first k with
 // thr[k] > u/2, so zero-mass classes are never returned.

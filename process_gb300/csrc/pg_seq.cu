@@ -105,20 +105,30 @@ struct TileSplit {
     return y - x;
   }
   __device__ __forceinline__ double c(uint64_t a) const { return a < nt ? cum[a] : tot; }
-  __device__ __forceinline__ uint64_t left(Key key, uint32_t h, uint32_t chr, uint32_t s, uint64_t n, uint64_t lo,
-                                           uint64_t mid, uint64_t hi) const {
-    double p;
+  // the left child's share of the node [lo, hi) (0 when the node has no mass)
+  __device__ __forceinline__ double share(uint64_t n, uint64_t lo, uint64_t mid, uint64_t hi) const {
     if (cum == nullptr) {
       const uint64_t wt = w(lo, hi);
-      if (n == 0 || wt == 0) return 0;
-      p = double(w(lo, mid)) / double(wt);
-    } else {
-      const double base = c(lo), wt = c(hi) - base;
-      if (n == 0 || !(wt > 0.0)) return 0;
-      p = (c(mid) - base) / wt;
+      if (n == 0 || wt == 0) return 0.0;
+      return double(w(lo, mid)) / double(wt);
     }
+    const double base = c(lo), wt = c(hi) - base;
+    if (n == 0 || !(wt > 0.0)) return 0.0;
+    return (c(mid) - base) / wt;
+  }
+  __device__ __forceinline__ uint64_t left(Key key, uint32_t h, uint32_t chr, uint32_t s, uint64_t n, uint64_t lo,
+                                           uint64_t mid, uint64_t hi) const {
+    const double p = share(n, lo, mid, hi);
+    if (!(p > 0.0)) return 0;
     Stream st{key, h, chr, s, TAG_TILE_SPLIT, 0u};
     return binomial(st, n, p);
+  }
+  // left() when its draw settles in the first attempt (false: call left())
+  __device__ __forceinline__ bool left_first(Key key, uint32_t h, uint32_t chr, uint32_t s, uint64_t n, uint64_t lo,
+                                             uint64_t mid, uint64_t hi, uint64_t& nl) const {
+    const double p = share(n, lo, mid, hi);
+    if (!(p > 0.0)) { nl = 0; return true; }
+    return binomial_first(Stream{key, h, chr, s, TAG_TILE_SPLIT, 0u}, n, p, nl);
   }
 };
 
@@ -176,37 +186,67 @@ __device__ __forceinline__ void tile_counts_one(uint32_t s, uint32_t bi, const u
 // level, one thread per (sample, chromosome, node of the level) whose range
 // meets the chromosome's tiles; node counts live in a per-(sample,
 // chromosome) heap in global memory.  Every node draws with its own heap id,
-// as in tile_counts_one, so the counts are the same.
-__global__ void k_tile_split_level(uint32_t level, uint32_t n_slots, const uint32_t* __restrict__ chr_first_tile,
-                                   const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
-                                   const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
-                                   const uint64_t* __restrict__ chr_pairs, const uint64_t* __restrict__ heap_base,
-                                   uint64_t heap_total, uint32_t T, uint32_t n_tiles,
-                                   const double* __restrict__ mass_cum, const double* __restrict__ mass_tot, Key key,
-                                   uint32_t* __restrict__ heap, uint32_t* __restrict__ pair_cnt) {
+// as in tile_counts_one, so the counts are the same.  A node whose draw
+// settles in BTRS's first attempt (most do) is written at once; the others
+// queue in shared memory and are drawn in full by consecutive threads, so
+// that the exact test's logarithms run on dense warps.
+constexpr uint32_t SPLIT_THREADS = 128;
+__global__ void __launch_bounds__(SPLIT_THREADS) k_tile_split_level(
+    uint32_t level, uint32_t n_slots, const uint32_t* __restrict__ chr_first_tile,
+    const uint32_t* __restrict__ chr_ntiles, const uint32_t* __restrict__ chr_depth,
+    const uint32_t* __restrict__ chr_nstarts, const uint32_t* __restrict__ chr_id,
+    const uint64_t* __restrict__ chr_pairs, const uint64_t* __restrict__ heap_base, uint64_t heap_total, uint32_t T,
+    uint32_t n_tiles, const double* __restrict__ mass_cum, const double* __restrict__ mass_tot, Key key,
+    uint32_t* __restrict__ heap, uint32_t* __restrict__ pair_cnt) {
+  __shared__ uint32_t s_q[SPLIT_THREADS];
+  __shared__ uint32_t s_nq;
   const uint32_t s = blockIdx.z, slot = blockIdx.y;
   const uint32_t D = chr_depth[slot], nt = chr_ntiles[slot], first = chr_first_tile[slot];
-  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   uint32_t* cnt = pair_cnt + uint64_t(s) * n_tiles + first;
   if (D == 0) {   // one tile: it takes every pair
-    if (level == 0 && i == 0) cnt[0] = uint32_t(chr_pairs[slot]);
+    if (level == 0 && blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = uint32_t(chr_pairs[slot]);
     return;
   }
-  if (level >= D || i >= (uint64_t(1) << level)) return;
-  const uint64_t size = uint64_t(1) << (D - level), lo = i * size;
-  if (lo >= nt) return;
+  // whole blocks past the level's nodes leave together
+  if (level >= D || uint64_t(blockIdx.x) * SPLIT_THREADS >= (uint64_t(1) << level)) return;
+  if (threadIdx.x == 0) s_nq = 0;
+  __syncthreads();
   const TileSplit sp{chr_nstarts[slot], T, nt, mass_cum ? mass_cum + uint64_t(s) * n_tiles + first : nullptr,
                      mass_cum ? mass_tot[uint64_t(s) * n_slots + slot] : 0.0};
   uint32_t* hp = heap + uint64_t(s) * heap_total + heap_base[slot];
-  const uint32_t h = uint32_t((uint64_t(1) << level) + i);
-  const uint64_t n = level == 0 ? chr_pairs[slot] : hp[h];
-  const uint64_t nl = sp.left(key, h, chr_id[slot], s, n, lo, lo + (size >> 1), lo + size);
-  if (level + 1 == D) {   // the children are tiles lo and lo + 1
-    cnt[lo] = uint32_t(nl);
-    if (lo + 1 < nt) cnt[lo + 1] = uint32_t(n - nl);
-  } else {
-    hp[2 * h] = uint32_t(nl);
-    hp[2 * h + 1] = uint32_t(n - nl);
+  const uint64_t size = uint64_t(1) << (D - level);
+  const uint32_t chr = chr_id[slot];
+  // node of thread x of the block: its index in the level (valid when its
+  // range meets the tiles), heap id, pair count
+  auto node = [&](uint32_t x, uint64_t& i, uint32_t& h, uint64_t& n) {
+    i = uint64_t(blockIdx.x) * SPLIT_THREADS + x;
+    if (i >= (uint64_t(1) << level) || i * size >= nt) return false;
+    h = uint32_t((uint64_t(1) << level) + i);
+    n = level == 0 ? chr_pairs[slot] : hp[h];
+    return true;
+  };
+  auto put = [&](uint64_t i, uint32_t h, uint64_t n, uint64_t nl) {
+    const uint64_t lo = i * size;
+    if (level + 1 == D) {   // the children are tiles lo and lo + 1
+      cnt[lo] = uint32_t(nl);
+      if (lo + 1 < nt) cnt[lo + 1] = uint32_t(n - nl);
+    } else {
+      hp[2 * h] = uint32_t(nl);
+      hp[2 * h + 1] = uint32_t(n - nl);
+    }
+  };
+  uint64_t i, n;
+  uint32_t h;
+  if (node(threadIdx.x, i, h, n)) {
+    const uint64_t lo = i * size;
+    uint64_t nl;
+    if (sp.left_first(key, h, chr, s, n, lo, lo + (size >> 1), lo + size, nl)) put(i, h, n, nl);
+    else s_q[atomicAdd(&s_nq, 1u)] = threadIdx.x;
+  }
+  __syncthreads();
+  if (threadIdx.x < s_nq && node(s_q[threadIdx.x], i, h, n)) {
+    const uint64_t lo = i * size;
+    put(i, h, n, sp.left(key, h, chr, s, n, lo, lo + (size >> 1), lo + size));
   }
 }
 
@@ -1083,8 +1123,8 @@ void seq_tile_counts(uint32_t n_samples, uint32_t n_slots, uint32_t max_depth, c
   if (n_samples == 0 || n_slots == 0) return;
   const Key key = make_key(seed);
   for (uint32_t level = 0; level < std::max<uint32_t>(max_depth, 1); ++level) {
-    const dim3 grid(nblk(uint64_t(1) << level, 128), n_slots, n_samples);
-    k_tile_split_level<<<grid, 128, 0, st>>>(level, n_slots, chr_first_tile, chr_ntiles, chr_depth, chr_nstarts,
+    const dim3 grid(nblk(uint64_t(1) << level, SPLIT_THREADS), n_slots, n_samples);
+    k_tile_split_level<<<grid, SPLIT_THREADS, 0, st>>>(level, n_slots, chr_first_tile, chr_ntiles, chr_depth, chr_nstarts,
                                              chr_id, chr_pairs, heap_base, heap_total, tile_size, n_tiles, mass_cum,
                                              mass_tot, key, heap, pair_cnt);
     note_launch();
