@@ -145,24 +145,25 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
   // epochs in pairs (packed f32x2 arithmetic); an odd K gets a padding
   // epoch of weight exp(-inf) = 0
   constexpr uint32_t KH = (K + 1) / 2;
-  float2 cst[KH], lv[KH], l1v[KH], w[J][KH];
+  float2 cst[KH], dlv[KH], l1v[KH], w[J][KH];
   auto at = [&](uint32_t k, uint32_t off, float pad) { return k < K ? s_row[off + k] : pad; };
   // the log-domain terms in base 2 (ex2 / lg2 directly, the NLL scaled back by ln 2)
   constexpr float LOG2E = 1.4426950408889634f, LN2 = 0.6931471805599453f;
 #pragma unroll
   for (uint32_t h = 0; h < KH; ++h) {
     cst[h] = make_float2(LOG2E * at(2 * h, 0, 0.f), at(2 * h + 1, 0, -INFINITY) * LOG2E);
-    lv[h] = make_float2(LOG2E * at(2 * h, K, 0.f), LOG2E * at(2 * h + 1, K, 0.f));
+    // u_k = cst_k + a log v_k + (d - a) log(1 - v_k) = cst_k + a dlv_k + d l1v_k
     l1v[h] = make_float2(LOG2E * at(2 * h, 2 * K, 0.f), LOG2E * at(2 * h + 1, 2 * K, 0.f));
+    dlv[h] = make_float2(LOG2E * at(2 * h, K, 0.f) - l1v[h].x, LOG2E * at(2 * h + 1, K, 0.f) - l1v[h].y);
 #pragma unroll
     for (uint32_t j = 0; j < J; ++j)
       w[j][h] = make_float2(s_row[3 * K + 2 * h * J + j], 2 * h + 1 < K ? s_row[3 * K + (2 * h + 1) * J + j] : 0.f);
   }
   float nll = 0.f;
-  float2 A[KH], B[KH], G[KH], H[J][KH];
+  float2 A[KH], D[KH], G[KH], H[J][KH];   // D_k = sum gamma_ik d_i (B_k = D_k - A_k)
 #pragma unroll
   for (uint32_t h = 0; h < KH; ++h) {
-    A[h] = B[h] = G[h] = make_float2(0.f, 0.f);
+    A[h] = D[h] = G[h] = make_float2(0.f, 0.f);
 #pragma unroll
     for (uint32_t j = 0; j < J; ++j) H[j][h] = make_float2(0.f, 0.f);
   }
@@ -173,26 +174,29 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
       const float4 x = *reinterpret_cast<const float4*>(s_sig + c * JP + j);
       sg[j] = x.x; sg[j + 1] = x.y; sg[j + 2] = x.z; sg[j + 3] = x.w;
     }
-    const float2 al2 = make_float2(al, al), dal2 = make_float2(dl - al, dl - al);
+    const float2 al2 = make_float2(al, al), dl2 = make_float2(dl, dl);
     float2 u[KH], m[KH];
     float umax = -INFINITY;
 #pragma unroll
     for (uint32_t h = 0; h < KH; ++h) {
-      u[h] = f2fma(dal2, l1v[h], f2fma(al2, lv[h], cst[h]));
+      u[h] = f2fma(dl2, l1v[h], f2fma(al2, dlv[h], cst[h]));
       umax = fmaxf(umax, fmaxf(u[h].x, u[h].y));
       m[h] = f2mul(w[0][h], make_float2(sg[0], sg[0]));
 #pragma unroll
       for (uint32_t j = 1; j < J; ++j) m[h] = f2fma(w[j][h], make_float2(sg[j], sg[j]), m[h]);
     }
-    float2 e[KH], q[KH];
-    float sum = 0.f;
+    float2 e[KH], q[KH], s2;
+    const float2 nmax = make_float2(-umax, -umax);
 #pragma unroll
     for (uint32_t h = 0; h < KH; ++h) {
-      e[h] = make_float2(ex2_approx(u[h].x - umax), ex2_approx(u[h].y - umax));
-      q[h] = f2mul(make_float2(fmaxf(m[h].x, 1e-30f), fmaxf(m[h].y, 1e-30f)), e[h]);
-      sum += q[h].x;
-      sum += q[h].y;
+      const float2 z = f2add(u[h], nmax);
+      e[h] = make_float2(ex2_approx(z.x), ex2_approx(z.y));
+      q[h] = f2mul(m[h], e[h]);
+      s2 = h ? f2add(s2, q[h]) : q[h];
     }
+    // a class that no epoch's mixture can emit (every M_k(c) = 0) keeps a
+    // finite, tiny sum
+    const float sum = fmaxf(s2.x + s2.y, 1e-30f);
     const float inv = __fdividef(1.f, sum);
     nll -= umax + lg2_approx(sum);
     const float2 inv2 = make_float2(inv, inv);
@@ -200,26 +204,47 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
     for (uint32_t h = 0; h < KH; ++h) {
       const float2 g = f2mul(q[h], inv2), r = f2mul(e[h], inv2);
       A[h] = f2fma(g, al2, A[h]);
-      B[h] = f2fma(g, dal2, B[h]);
+      D[h] = f2fma(g, dl2, D[h]);
       G[h] = f2add(G[h], g);
 #pragma unroll
       for (uint32_t j = 0; j < J; ++j) H[j][h] = f2fma(r, make_float2(sg[j], sg[j]), H[j][h]);
     }
   };
-  uint64_t i = i0 + threadIdx.x;
-  for (; i + (U - 1) * CAL_THREADS < i1; i += U * CAL_THREADS) {
-    float al[U], dl[U];
-    int32_t c[U];
+  auto site_at = [&](uint64_t x) { site(float(__ldg(a.alt + x)), float(__ldg(a.depth + x)), __ldg(a.cls + x)); };
+  auto site4 = [&](const int4& x, const int4& y, const int4& z) {
+    site(float(x.x), float(y.x), z.x); site(float(x.y), float(y.y), z.y);
+    site(float(x.z), float(y.z), z.z); site(float(x.w), float(y.w), z.w);
+  };
+  const bool vec = ((reinterpret_cast<uintptr_t>(a.alt) | reinterpret_cast<uintptr_t>(a.depth) |
+                     reinterpret_cast<uintptr_t>(a.cls)) & 15u) == 0;
+  if (vec) {
+    // four consecutive sites per 16-byte load of each column; the unaligned
+    // head [i0, v0) and tail [v1, i1) (under four sites each) site by site
+    const uint64_t v0 = min((i0 + 3) & ~uint64_t(3), i1), v1 = max(i1 & ~uint64_t(3), v0);
+    if (threadIdx.x < v0 - i0) site_at(i0 + threadIdx.x);
+    if (threadIdx.x < i1 - v1) site_at(v1 + threadIdx.x);
+    const int4* a4 = reinterpret_cast<const int4*>(a.alt);
+    const int4* d4 = reinterpret_cast<const int4*>(a.depth);
+    const int4* c4 = reinterpret_cast<const int4*>(a.cls);
+    const uint64_t q1 = v1 / 4;
+    for (uint64_t q = v0 / 4 + threadIdx.x; q < q1; q += CAL_THREADS) site4(__ldg(a4 + q), __ldg(d4 + q), __ldg(c4 + q));
+  } else {
+    // columns not 16-byte aligned: U sites in flight per thread, strided
+    uint64_t i = i0 + threadIdx.x;
+    for (; i + (U - 1) * CAL_THREADS < i1; i += U * CAL_THREADS) {
+      float al[U], dl[U];
+      int32_t c[U];
 #pragma unroll
-    for (uint32_t u = 0; u < U; ++u) {
-      al[u] = float(__ldg(a.alt + i + u * CAL_THREADS));
-      dl[u] = float(__ldg(a.depth + i + u * CAL_THREADS));
-      c[u] = __ldg(a.cls + i + u * CAL_THREADS);
+      for (uint32_t u = 0; u < U; ++u) {
+        al[u] = float(__ldg(a.alt + i + u * CAL_THREADS));
+        dl[u] = float(__ldg(a.depth + i + u * CAL_THREADS));
+        c[u] = __ldg(a.cls + i + u * CAL_THREADS);
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < U; ++u) site(al[u], dl[u], c[u]);
     }
-#pragma unroll
-    for (uint32_t u = 0; u < U; ++u) site(al[u], dl[u], c[u]);
+    for (; i < i1; i += CAL_THREADS) site(float(__ldg(a.alt + i)), float(__ldg(a.depth + i)), __ldg(a.cls + i));
   }
-  for (; i < i1; i += CAL_THREADS) site(float(__ldg(a.alt + i)), float(__ldg(a.depth + i)), __ldg(a.cls + i));
   // block partial: warp trees, then a compensated sum over the warps
   float acc[NV];
   acc[0] = nll * LN2;
@@ -227,7 +252,7 @@ __global__ void __launch_bounds__(CAL_THREADS, calib_min_blocks(K, J)) k_calib_s
   for (uint32_t k = 0; k < K; ++k) {
     const bool hi = k & 1;
     acc[1 + k] = hi ? A[k / 2].y : A[k / 2].x;
-    acc[1 + K + k] = hi ? B[k / 2].y : B[k / 2].x;
+    acc[1 + K + k] = hi ? D[k / 2].y - A[k / 2].y : D[k / 2].x - A[k / 2].x;
     acc[1 + 2 * K + k] = hi ? G[k / 2].y : G[k / 2].x;
 #pragma unroll
     for (uint32_t j = 0; j < J; ++j) acc[1 + 3 * K + k * J + j] = hi ? H[j][k / 2].y : H[j][k / 2].x;

@@ -60,6 +60,29 @@ def test_adjoint_matches_fp64_gradient_2e5_sites(gpu_lib):
 
 
 @pytest.mark.gpu
+def test_adjoint_replicates_off_the_four_site_grid(gpu_lib):
+    """Replicates of 10,001 sites: every chunk but the first starts and ends
+    off a multiple of four sites, so the kernel's site-by-site head and tail
+    run beside its four-site loads; each replicate against the FP64 gradient."""
+    import torch
+
+    import oracle.calib as oc
+    from process_gb300 import calib
+    d = calib.synthetic(3, 10_001, [40, 90, 160], seed=12)
+    assert d.site_off[1] % 4 != 0
+    b = calib.batch_of(d)
+    p = torch.tensor(d.true_params + 0.3, dtype=torch.float32, device="cuda")
+    nll, grad = b.nll_grad(p)
+    torch.cuda.synchronize()
+    p32 = p.double().cpu().numpy()
+    for r in range(d.n_rep):
+        f, g = oc.nll_grad(p32[r], *_rep(d, r))
+        gg = grad.double().cpu().numpy()[r]
+        assert abs(float(nll[r]) - f) / abs(f) < 1e-5
+        assert np.linalg.norm(gg - g) / np.linalg.norm(g) < 1e-4
+
+
+@pytest.mark.gpu
 def test_batched_equals_per_instance_and_autograd(gpu_lib):
     import torch
 
