@@ -164,6 +164,28 @@ def test_sequencing_replay_depth_and_vaf(orc):
     assert alt[1].sum() == 0
 
 
+def test_sequencing_replay_error_thirds(orc):
+    """Substitution errors: the normal sample carries no passenger, so each
+    of its SNV depth units shows the alt base exactly when the visit's error
+    word falls in the first third of [0, err_thr): a rate of e/3.  Indels
+    see no substitution errors."""
+    from process_gb300.engine import seq_cfg
+    w = small_workload(leaves=200)
+    e = orc.OracleEngine.like(w)
+    sp = species_of(e, w.forest)
+    p = e.place(w.forest, sp, 0, 0, 0, 0, seed=3)
+    err = 0.09
+    cfg, _ = seq_cfg(coverage=30, read_size=150, insert_size_mean=350, insert_size_stddev=10, error_rate=err,
+                     tile_size=8192, chr_index=lambda x: int(x) - 1)
+    alt, dep, _ = p.sequence(cfg, 7, flavour=0)
+    t = p.table()
+    snv, ind = t["kind"] == 0, t["kind"] == 1
+    n = dep[1, snv].sum()
+    rate = alt[1, snv].sum() / n
+    assert abs(rate - err / 3) < 4 * np.sqrt(err / 3 / n)
+    assert alt[1, ind].sum() == 0 and dep[1, ind].sum() > 0
+
+
 def test_insert_size_model_rejects_large_variance(orc):
     from process_gb300.engine import seq_cfg
     w = small_workload(leaves=50)
